@@ -1,0 +1,516 @@
+"""SciMLBase-shaped host API over the C ABI.
+
+Mirrors the surface the reference re-exports (src/DifferentialEquations.jl:8-9;
+allow-list test/qa/qa.jl): ODEProblem (qa.jl:86), SDEProblem (qa.jl:103),
+remake (qa.jl:183), EnsembleProblem (qa.jl:50), solve (qa.jl:192),
+ReturnCode (qa.jl:213), EnsembleSolution (qa.jl:52), the algorithm types
+Tsit5 / Vern7 / Rosenbrock23 / Rodas5P (qa.jl:119,126,98,97) plus Rodas5, EM
+and SOSRI, and a new ensemble algorithm `EnsembleGB300` that routes the whole
+ensemble through one `gbde_ensemble_solve` call.
+
+Semantics kept from the reference's pinned tests (test/core.jl):
+  * saveat=0.1 on (0, 1) stores 11 points, t0 and tf included (core.jl:90-96);
+  * the first stored state equals u0 exactly (core.jl:34);
+  * remake(prob; u0=...) changes u0 (core.jl:81-88);
+  * a Robertson solve with Rodas5P to t=1e5 returns Success (core.jl:38-49).
+Unsupported solve keywords (callback, dense=True, save_everystep=True) raise
+instead of silently changing behaviour.
+"""
+import copy
+import enum
+from fractions import Fraction
+
+import numpy as np
+
+from . import _capi as capi
+
+
+class ReturnCode(enum.IntEnum):
+    """SciMLBase.ReturnCode subset (qa.jl:213)."""
+    Default = capi.RET_DEFAULT
+    Success = capi.RET_SUCCESS
+    MaxIters = capi.RET_MAXITERS
+    DtLessThanMin = capi.RET_DTLESSTHANMIN
+    Unstable = capi.RET_UNSTABLE
+    InitialFailure = capi.RET_INITIALFAILURE
+    Timeout = capi.RET_TIMEOUT
+
+
+# ---------------------------------------------------------------- models
+class Model:
+    """A built-in right-hand side f!(du, u, p, t) (and noise g for SDEs)."""
+
+    def __init__(self, name, model_id, n_state, n_param, noise=False, doc=""):
+        self.name, self.id = name, model_id
+        self.n_state, self.n_param, self.noise = n_state, n_param, noise
+        self.__doc__ = doc
+
+    def __repr__(self):
+        return "Model(%s, n_state=%d, n_param=%d)" % (self.name, self.n_state, self.n_param)
+
+    def __deepcopy__(self, memo):
+        return self  # built-in models are immutable singletons
+
+
+class models:
+    linear = Model("linear", capi.MODEL_LINEAR, 1, 1, doc="du = a u (test/core.jl:10)")
+    lorenz = Model("lorenz", capi.MODEL_LORENZ, 3, 3, doc="Lorenz (test/core.jl:22-27)")
+    robertson = Model("robertson", capi.MODEL_ROBERTSON, 3, 3,
+                      doc="Robertson kinetics (test/core.jl:39-45)")
+    vdp_ring8 = Model("vdp_ring8", capi.MODEL_VDP_RING8, 16, 2,
+                      doc="ring of 8 Van der Pol oscillators, p=[mu, kappa]")
+    lotka_volterra = Model("lotka_volterra", capi.MODEL_LOTKA_VOLTERRA, 2, 5, noise=True,
+                           doc="Lotka-Volterra drift, diagonal noise sigma*u; "
+                               "p=[alpha, beta, gamma, delta, sigma]")
+
+
+# -------------------------------------------------------------- problems
+class ODEProblem:
+    """ODEProblem(f, u0, tspan, p; kwargs...) with a built-in model as f."""
+
+    is_sde = False
+
+    def __init__(self, f, u0, tspan, p=None, **kwargs):
+        if not isinstance(f, Model):
+            raise TypeError("f must be a built-in Model (models.lorenz, ...); user RHS "
+                            "functions are not compiled by this library")
+        self.f = f
+        self.u0 = np.atleast_1d(np.asarray(u0, dtype=np.float64)).copy()
+        self.tspan = (float(tspan[0]), float(tspan[1]))
+        self.p = (np.zeros(f.n_param) if p is None
+                  else np.atleast_1d(np.asarray(p, dtype=np.float64)).copy())
+        self.kwargs = dict(kwargs)
+        if self.u0.shape != (f.n_state,):
+            raise ValueError("u0 must have %d entries for %s" % (f.n_state, f.name))
+        if self.p.shape != (f.n_param,):
+            raise ValueError("p must have %d entries for %s" % (f.n_param, f.name))
+
+
+class SDEProblem(ODEProblem):
+    """SDEProblem(f, g, u0, tspan, p): the model carries both drift and noise."""
+
+    is_sde = True
+
+    def __init__(self, f, g, u0, tspan, p=None, **kwargs):
+        if not (isinstance(f, Model) and f.noise):
+            raise TypeError("SDEProblem needs a built-in model with a noise term")
+        if g is not None and g is not f:
+            raise TypeError("the noise term is part of the built-in model; pass g=None or g=f")
+        super().__init__(f, u0, tspan, p, **kwargs)
+
+
+def remake(prob, u0=None, tspan=None, p=None, **kwargs):
+    """remake(prob; u0, tspan, p, kwargs...) (qa.jl:183, core.jl:81-88)."""
+    q = copy.copy(prob)
+    q.u0 = prob.u0.copy() if u0 is None else np.atleast_1d(np.asarray(u0, np.float64)).copy()
+    q.p = prob.p.copy() if p is None else np.atleast_1d(np.asarray(p, np.float64)).copy()
+    q.tspan = prob.tspan if tspan is None else (float(tspan[0]), float(tspan[1]))
+    q.kwargs = dict(prob.kwargs)
+    q.kwargs.update(kwargs)
+    if q.u0.shape != (prob.f.n_state,) or q.p.shape != (prob.f.n_param,):
+        raise ValueError("remake: u0 / p have the wrong size for %s" % prob.f.name)
+    return q
+
+
+class EnsembleProblem:
+    """EnsembleProblem(prob; prob_func, output_func, reduction, safetycopy)
+    (qa.jl:50).
+
+    prob_func(prob, i, repeat) -> problem for trajectory i (0-based here).
+    batch(prob, N) -> dict with any of "u0" (N, n_state), "p" (N, n_param),
+    "tspan" (N, 2), "saveat" (N, n_save): a vectorised prob_func for large
+    ensembles (an extension; SciMLBase evaluates prob_func per trajectory).
+    """
+
+    def __init__(self, prob, prob_func=None, output_func=None, reduction=None,
+                 safetycopy=True, batch=None):
+        self.prob = prob
+        self.prob_func = prob_func
+        self.output_func = output_func
+        self.reduction = reduction
+        self.safetycopy = safetycopy
+        self.batch = batch
+
+
+# ------------------------------------------------------------ algorithms
+class _Alg:
+    alg_id = 0
+    sde = False
+
+    def __repr__(self):
+        return type(self).__name__ + "()"
+
+
+class Tsit5(_Alg):
+    alg_id = capi.ALG_TSIT5
+
+
+class Vern7(_Alg):
+    alg_id = capi.ALG_VERN7
+
+
+class Rosenbrock23(_Alg):
+    alg_id = capi.ALG_ROSENBROCK23
+
+
+class Rodas5(_Alg):
+    alg_id = capi.ALG_RODAS5
+
+
+class Rodas5P(_Alg):
+    alg_id = capi.ALG_RODAS5P
+
+
+class EM(_Alg):
+    alg_id = capi.ALG_EM
+    sde = True
+
+
+class SOSRI(_Alg):
+    alg_id = capi.ALG_SOSRI
+    sde = True
+
+
+class EnsembleGB300:
+    """Ensemble algorithm that solves every trajectory on one GB300 GPU.
+
+    precision: "fp64" or "mixed" (FP32 state/stages; FP64 compensated time,
+    error norm and W-matrix LU).  batching: "plain" (one launch, a thread per
+    trajectory) or "persistent" (threads refill from a device work queue).
+    """
+
+    def __init__(self, device=0, precision="fp64", batching="plain", learned=False,
+                 block_size=0, ctas_per_sm=0, chunk=0, out_dtype=None, timeout_s=0.0):
+        if precision not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        if batching not in ("plain", "persistent"):
+            raise ValueError("batching must be 'plain' or 'persistent'")
+        self.device, self.precision, self.batching = device, precision, batching
+        self.learned, self.block_size, self.ctas_per_sm = learned, block_size, ctas_per_sm
+        self.chunk, self.timeout_s = chunk, timeout_s
+        self.out_dtype = out_dtype or ("f64" if precision == "fp64" else "f32")
+
+
+class EnsembleThreads:
+    """The reference's CPU ensemble algorithm (qa.jl:56).  This library does
+    not solve on the CPU; pass EnsembleGB300() instead."""
+
+
+class EnsembleSerial(EnsembleThreads):
+    """(qa.jl:51) -- see EnsembleThreads."""
+
+
+# ------------------------------------------------------------- solutions
+class ODESolution:
+    """One trajectory's solution: views into the ensemble arrays."""
+
+    def __init__(self, t, u, retcode, prob=None, stats=None):
+        self.t = t
+        self._u = u
+        self.retcode = ReturnCode(int(retcode))
+        self.prob = prob
+        self.stats = stats or {}
+
+    @property
+    def u(self):
+        return [self._u[j] for j in range(self._u.shape[0])]
+
+    def __getitem__(self, j):
+        return self._u[j]
+
+    def __len__(self):
+        return self._u.shape[0]
+
+    def __call__(self, t):
+        """Linear interpolation between the stored points."""
+        return np.array([np.interp(t, self.t, self._u[:, c]) for c in range(self._u.shape[1])])
+
+
+class EnsembleSolution:
+    """EnsembleSolution (qa.jl:52): `u` is the list of per-trajectory
+    solutions; `U`, `t`, `retcode` expose the underlying arrays."""
+
+    def __init__(self, U, t, retcode, lengths, stats, elapsed_ms, device_ms, output_func=None,
+                 reduction=None, probs=None):
+        self.U = U                  # (N, n_save, n_state)
+        self.t = t                  # (n_save,) or (N, n_save)
+        self.retcode = retcode      # (N,) int32
+        self.lengths = lengths      # (N,) stored points per trajectory
+        self.stats = stats          # dict of (N,) arrays
+        self.elapsedTime = elapsed_ms / 1e3
+        self.device_ms = device_ms
+        self._output_func = output_func
+        self._probs = probs
+
+    def __len__(self):
+        return self.U.shape[0]
+
+    def solution(self, i):
+        n = int(self.lengths[i])
+        t = self.t[:n] if self.t.ndim == 1 else self.t[i, :n]
+        st = {k: v[i] for k, v in self.stats.items()}
+        return ODESolution(t, self.U[i, :n], self.retcode[i],
+                           None if self._probs is None else self._probs[i], st)
+
+    def __getitem__(self, i):
+        return self.solution(i)
+
+    @property
+    def u(self):
+        return [self.solution(i) for i in range(len(self))]
+
+    @property
+    def converged(self):
+        return bool(np.all(self.retcode == capi.RET_SUCCESS))
+
+
+# ----------------------------------------------------------- save times
+def _dec(x):
+    """Exact rational of the shortest decimal that round-trips x (so that
+    t0 + k*0.1 is the correctly rounded k/10, as a decimal step range)."""
+    return Fraction(repr(float(x)))
+
+
+def save_grid(t0, tf, saveat, save_start=None, save_end=None):
+    """Save times for one trajectory with the reference's defaults:
+    a number Δ gives t0, t0+Δ, ..., and tf (save_start/save_end default
+    True); a vector keeps the times in [t0, tf], with t0 / tf stored only if
+    listed (or requested)."""
+    if np.isscalar(saveat):
+        d = float(saveat)
+        if not d > 0:
+            raise ValueError("saveat step must be > 0")
+        ts = []
+        f0, fd, ff = _dec(t0), _dec(d), _dec(tf)
+        k = 1
+        while True:
+            tk = f0 + k * fd
+            if tk >= ff:
+                break
+            ts.append(float(tk))
+            k += 1
+        start = True if save_start is None else save_start
+        end = True if save_end is None else save_end
+        out = ([t0] if start else []) + ts + ([tf] if end else [])
+        return np.asarray(out, np.float64)
+    v = np.asarray(saveat, np.float64).ravel()
+    inside = v[(v > t0) & (v < tf)]
+    start = (t0 in v) if save_start is None else save_start
+    end = (tf in v) if save_end is None else save_end
+    out = np.concatenate([[t0] if start else [], np.sort(inside), [tf] if end else []])
+    return out.astype(np.float64)
+
+
+# ----------------------------------------------------------------- solve
+_UNSUPPORTED = ("callback", "dense", "save_everystep", "tstops", "save_idxs")
+
+
+def _gather_inputs(ens, N):
+    prob = ens.prob
+    ns, np_ = prob.f.n_state, prob.f.n_param
+    u0 = np.broadcast_to(prob.u0, (N, ns)).copy()
+    p = np.broadcast_to(prob.p, (N, np_)).copy()
+    tspan = np.broadcast_to(np.asarray(prob.tspan), (N, 2)).copy()
+    saves = None
+    probs = None
+    if ens.batch is not None:
+        b = ens.batch(prob, N)
+        if "u0" in b:
+            u0 = np.ascontiguousarray(b["u0"], np.float64).reshape(N, ns)
+        if "p" in b:
+            p = np.ascontiguousarray(b["p"], np.float64).reshape(N, np_)
+        if "tspan" in b:
+            tspan = np.ascontiguousarray(b["tspan"], np.float64).reshape(N, 2)
+        if "saveat" in b:
+            saves = np.ascontiguousarray(b["saveat"], np.float64).reshape(N, -1)
+    elif ens.prob_func is not None:
+        probs = []
+        per_save = []
+        for i in range(N):
+            base = copy.deepcopy(prob) if ens.safetycopy else prob
+            pi = ens.prob_func(base, i, 1)
+            if pi.f is not prob.f:
+                raise ValueError("prob_func must keep the model of the ensemble's problem")
+            u0[i], p[i], tspan[i] = pi.u0, pi.p, pi.tspan
+            per_save.append(pi.kwargs.get("saveat"))
+            probs.append(pi)
+        if any(s is not None for s in per_save):
+            saves = per_save
+    return u0, p, tspan, saves, probs
+
+
+def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start=None,
+          save_end=None, reltol=None, abstol=None, dt=None, adaptive=None, maxiters=None,
+          dtmin=None, dtmax=None, seed=0, **kwargs):
+    """solve(EnsembleProblem, alg, EnsembleGB300(); trajectories, saveat,
+    reltol, abstol, ...) -> EnsembleSolution.  A plain ODEProblem /
+    SDEProblem is solved as an ensemble of one trajectory."""
+    for k in _UNSUPPORTED:
+        if k in kwargs and kwargs[k] not in (None, False):
+            raise NotImplementedError("solve keyword %r is not supported by EnsembleGB300" % k)
+    extra = set(kwargs) - set(_UNSUPPORTED) - {"qmin", "qmax", "gamma", "beta1", "beta2",
+                                               "qsteady_min", "qsteady_max", "qoldinit"}
+    if extra:
+        raise TypeError("unknown solve keywords: %s" % sorted(extra))
+    single = not isinstance(ens, EnsembleProblem)
+    if single:
+        ens = EnsembleProblem(ens)
+        trajectories = 1
+    if ensemblealg is None:
+        ensemblealg = EnsembleGB300()
+    if not isinstance(ensemblealg, EnsembleGB300):
+        raise NotImplementedError("this library solves ensembles on the GPU only: "
+                                  "use EnsembleGB300()")
+    if not isinstance(alg, _Alg):
+        raise TypeError("alg must be one of Tsit5(), Vern7(), Rosenbrock23(), Rodas5(), "
+                        "Rodas5P(), EM(), SOSRI()")
+    prob = ens.prob
+    if alg.sde and not prob.is_sde:
+        raise TypeError("%r needs an SDEProblem" % alg)
+    if trajectories is None or int(trajectories) < 0:
+        raise ValueError("trajectories must be a non-negative integer")
+    N = int(trajectories)
+    if saveat is None:
+        saveat = prob.kwargs.get("saveat")
+    u0, p, tspan, saves, probs = _gather_inputs(ens, N)
+    t0 = np.ascontiguousarray(tspan[:, 0])
+    tf = np.ascontiguousarray(tspan[:, 1])
+
+    # ---- save layout
+    if isinstance(saves, np.ndarray):
+        save_kind, save_arr = capi.SAVE_PER_TRAJ, saves
+        lengths = np.full(N, saves.shape[1], np.int64)
+    else:
+        per = None
+        if isinstance(saves, list):
+            per = [s if s is not None else saveat for s in saves]
+        if per is None and saveat is None:
+            if save_end is False and save_start is False:
+                raise ValueError("nothing to save")
+            raise NotImplementedError(
+                "EnsembleGB300 stores fixed save grids: pass saveat (a step or a vector) "
+                "(saving every step is not supported)")
+        uniform = per is None and (N == 0 or (np.all(t0 == t0[0]) and np.all(tf == tf[0])))
+        if uniform:
+            grid = save_grid(t0[0] if N else prob.tspan[0], tf[0] if N else prob.tspan[1],
+                             saveat, save_start, save_end)
+            save_kind, save_arr = capi.SAVE_GRID, grid
+            lengths = np.full(N, len(grid), np.int64)
+        else:
+            grids = [save_grid(t0[i], tf[i], per[i] if per else saveat, save_start, save_end)
+                     for i in range(N)]
+            lengths = np.array([len(g) for g in grids], np.int64)
+            m = int(lengths.max()) if N else 0
+            save_arr = np.empty((N, m), np.float64)
+            for i, g in enumerate(grids):
+                save_arr[i, :len(g)] = g
+                save_arr[i, len(g):] = tf[i]  # padding: repeats of the final state
+            save_kind = capi.SAVE_PER_TRAJ
+
+    opts = capi.opts_default(alg.alg_id)
+    opts.precision = capi.PREC_MIXED if ensemblealg.precision == "mixed" else capi.PREC_FP64
+    opts.batching = (capi.BATCH_PERSISTENT if ensemblealg.batching == "persistent"
+                     else capi.BATCH_PLAIN)
+    if reltol is not None:
+        opts.reltol = reltol
+    if abstol is not None:
+        opts.abstol = abstol
+    if dt is not None:
+        opts.dt = dt
+    if adaptive is not None:
+        opts.adaptive = int(bool(adaptive))
+    if maxiters is not None:
+        opts.maxiters = int(maxiters)
+    if dtmin is not None:
+        opts.dtmin = dtmin
+    if dtmax is not None:
+        opts.dtmax = dtmax
+    for k in ("qmin", "qmax", "gamma", "beta1", "beta2", "qsteady_min", "qsteady_max",
+              "qoldinit"):
+        if k in kwargs:
+            setattr(opts, k, float(kwargs[k]))
+    opts.seed = int(seed)
+    opts.learned = int(bool(ensemblealg.learned))
+    opts.block_size = int(ensemblealg.block_size)
+    opts.ctas_per_sm = int(ensemblealg.ctas_per_sm)
+    opts.chunk = int(ensemblealg.chunk)
+    opts.timeout_s = float(ensemblealg.timeout_s)
+
+    res = solve_arrays(prob.f, opts, p, u0, t0, tf, save_arr, save_kind,
+                       u_dtype=ensemblealg.out_dtype, device=ensemblealg.device)
+    t_out = save_arr
+    sol = EnsembleSolution(res["u"], t_out, res["retcode"], lengths,
+                           {k: res[k] for k in ("naccept", "nreject", "nf", "t_end")},
+                           res["total_ms"], res["device_ms"], probs=probs)
+    if ens.output_func is not None:
+        outs = []
+        for i in range(N):
+            o, _rerun = ens.output_func(sol.solution(i), i)
+            outs.append(o)
+        sol.outputs = outs
+    if single:
+        return sol.solution(0)
+    return sol
+
+
+def solve_arrays(model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", device=0,
+                 out=None, stats=True):
+    """Low-level entry: arrays in, arrays out, one gbde_ensemble_solve call.
+
+    Host numpy arrays -> GBDE_MEM_HOST (the call stages the copies).
+    CUDA torch tensors -> GBDE_MEM_DEVICE on the tensors' device and the
+    current torch stream; results are CUDA tensors.
+    """
+    N = int(u0.shape[0])
+    n_save = int(saveat.shape[-1]) if saveat is not None else 0
+    on_device = not isinstance(u0, np.ndarray)
+    prob = capi.Problem()
+    prob.model = model.id
+    prob.n_state, prob.n_param = model.n_state, model.n_param
+    prob.n_traj = N
+    prob.save_kind = save_kind
+    prob.n_save = n_save
+    outs = capi.Outputs()
+    outs.u_dtype = capi.F32 if u_dtype == "f32" else capi.F64
+    ctx = capi.context(device)
+    if on_device:
+        import torch
+        prob.mem = capi.MEM_DEVICE
+        dev = u0.device
+        tdt = torch.float32 if u_dtype == "f32" else torch.float64
+        res = out or {
+            "u": torch.empty((N, n_save, model.n_state), dtype=tdt, device=dev),
+            "retcode": torch.empty(N, dtype=torch.int32, device=dev),
+        }
+        if stats and out is None:
+            for k in ("naccept", "nreject", "nf"):
+                res[k] = torch.empty(N, dtype=torch.int32, device=dev)
+            res["t_end"] = torch.empty(N, dtype=torch.float64, device=dev)
+        ctx.set_stream(torch.cuda.current_stream(dev).cuda_stream)
+        arrs = (p, u0, t0, tf, saveat)
+    else:
+        prob.mem = capi.MEM_HOST
+        arrs = tuple(np.ascontiguousarray(a, np.float64) if a is not None else None
+                     for a in (p, u0, t0, tf, saveat))
+        res = out or {
+            "u": np.empty((N, n_save, model.n_state),
+                          np.float32 if u_dtype == "f32" else np.float64),
+            "retcode": np.empty(N, np.int32),
+        }
+        if stats and out is None:
+            for k in ("naccept", "nreject", "nf"):
+                res[k] = np.empty(N, np.int32)
+            res["t_end"] = np.empty(N, np.float64)
+        ctx.set_stream(0)
+    prob.p, prob.u0, prob.t0, prob.tf, prob.saveat = [capi.ptr(a) for a in arrs]
+    outs.u = capi.ptr(res["u"])
+    outs.retcode = capi.ptr(res["retcode"])
+    for k in ("naccept", "nreject", "nf", "t_end", "method"):
+        if k in res:
+            setattr(outs, k, capi.ptr(res[k]))
+    for k in ("naccept", "nreject", "nf", "t_end"):
+        res.setdefault(k, None)
+    ctx.solve(prob, opts, outs)
+    res["device_ms"] = outs.device_ms
+    res["total_ms"] = outs.total_ms
+    return res

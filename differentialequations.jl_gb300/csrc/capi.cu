@@ -1,0 +1,430 @@
+// capi.cu -- the extern "C" boundary (include/gbde.h): context, argument
+// validation, device buffers, host<->device staging, launch dispatch.
+//
+// gbde_ensemble_solve() stands in for
+//   SciMLBase.__solve(::EnsembleProblem, alg, ::EnsembleThreads; trajectories, ...)
+// (EnsembleProblem qa.jl:50, EnsembleThreads qa.jl:56, solve qa.jl:192):
+// one call solves every trajectory and fills the solution arrays.
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/gbde.h"
+#include "launch.h"
+#include "philox.h"
+
+using namespace gbde;
+
+namespace {
+
+thread_local std::string g_thread_err;
+
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    size_t want = bytes < 256 ? 256 : bytes;
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+  }
+};
+
+}  // namespace
+
+struct gbde_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::mutex mu;
+  std::string err;
+  // staging for GBDE_MEM_HOST calls
+  DevBuf p, u0, t0, tf, saveat, u, ret, nacc, nrej, nf, tend, method;
+  DevBuf work;  // queue counter + status flag
+  // learned predictor (filled by the MLP entry points)
+  DevBuf pred_dt;
+};
+
+static int set_err(gbde_ctx* ctx, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->err = buf;
+  else g_thread_err = buf;
+  return code;
+}
+
+#define GBDE_CUDA(ctx, call)                                                               \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return set_err(ctx, e_ == cudaErrorMemoryAllocation ? GBDE_ERR_NOMEM : GBDE_ERR_CUDA, \
+                     "%s failed: %s", #call, cudaGetErrorString(e_));                      \
+  } while (0)
+
+namespace gbde {
+int ctx_device(const gbde_ctx* ctx, int* device, int* num_sms, cudaStream_t* stream) {
+  if (!ctx) return GBDE_ERR_INVALID;
+  *device = ctx->device;
+  *num_sms = ctx->num_sms;
+  *stream = ctx->stream;
+  return GBDE_OK;
+}
+}  // namespace gbde
+
+extern "C" {
+
+int gbde_version(void) { return GBDE_ABI_VERSION; }
+
+const char* gbde_last_error(const gbde_ctx* ctx) {
+  return ctx ? ctx->err.c_str() : g_thread_err.c_str();
+}
+
+int gbde_model_info(int32_t model, int32_t* n_state, int32_t* n_param) {
+  int ns = 0, np = 0;
+  switch (model) {
+    case GBDE_MODEL_LINEAR: ns = Linear::N; np = Linear::NP; break;
+    case GBDE_MODEL_LORENZ: ns = Lorenz::N; np = Lorenz::NP; break;
+    case GBDE_MODEL_ROBERTSON: ns = Robertson::N; np = Robertson::NP; break;
+    case GBDE_MODEL_VDP_RING8: ns = VdpRing8::N; np = VdpRing8::NP; break;
+    case GBDE_MODEL_LOTKA_VOLTERRA: ns = LotkaVolterra::N; np = LotkaVolterra::NP; break;
+    default: return set_err(nullptr, GBDE_ERR_INVALID, "unknown model id %d", model);
+  }
+  if (n_state) *n_state = ns;
+  if (n_param) *n_param = np;
+  return GBDE_OK;
+}
+
+int gbde_ctx_create(int device, gbde_ctx** out) {
+  if (!out) return set_err(nullptr, GBDE_ERR_INVALID, "gbde_ctx_create: out is NULL");
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return set_err(nullptr, GBDE_ERR_CUDA, "no CUDA device available (%s)",
+                   cudaGetErrorString(e));
+  if (device < 0 || device >= ndev)
+    return set_err(nullptr, GBDE_ERR_INVALID, "device %d out of range [0,%d)", device, ndev);
+  gbde_ctx* c = new gbde_ctx();
+  c->device = device;
+  e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+  if (e != cudaSuccess) {
+    int r = set_err(nullptr, GBDE_ERR_CUDA, "context setup failed: %s", cudaGetErrorString(e));
+    delete c;
+    return r;
+  }
+  c->stream = c->own;
+  *out = c;
+  return GBDE_OK;
+}
+
+int gbde_ctx_destroy(gbde_ctx* ctx) {
+  if (!ctx) return GBDE_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (DevBuf* b : {&ctx->p, &ctx->u0, &ctx->t0, &ctx->tf, &ctx->saveat, &ctx->u, &ctx->ret,
+                    &ctx->nacc, &ctx->nrej, &ctx->nf, &ctx->tend, &ctx->method, &ctx->work,
+                    &ctx->pred_dt})
+    b->release();
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->own) cudaStreamDestroy(ctx->own);
+  delete ctx;
+  return GBDE_OK;
+}
+
+int gbde_ctx_set_stream(gbde_ctx* ctx, void* stream) {
+  if (!ctx) return set_err(nullptr, GBDE_ERR_INVALID, "ctx is NULL");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own;
+  return GBDE_OK;
+}
+
+int gbde_opts_default(int32_t alg, gbde_opts* o) {
+  if (!o) return set_err(nullptr, GBDE_ERR_INVALID, "gbde_opts_default: out is NULL");
+  std::memset(o, 0, sizeof(*o));
+  o->alg = alg;
+  o->precision = GBDE_PREC_FP64;
+  o->batching = GBDE_BATCH_PLAIN;
+  o->adaptive = 1;
+  o->reltol = 1e-3;
+  o->abstol = 1e-6;
+  o->dt = 0.0;
+  o->dtmin = 0.0;
+  o->dtmax = 0.0;
+  o->maxiters = 100000;
+  o->qmin = 0.2;
+  o->qmax = 10.0;
+  o->gamma = 0.9;
+  o->qsteady_min = 1.0;
+  o->qsteady_max = 1.0;
+  o->qoldinit = 1e-4;
+  o->seed = 0;
+  o->stiff_threshold = 0.0;
+  switch (alg) {
+    case GBDE_ALG_TSIT5:  // Dormand-Prince style PI constants (HNW I, II.4)
+      o->beta2 = 0.04;
+      o->beta1 = 0.2 - 0.75 * 0.04;
+      break;
+    case GBDE_ALG_VERN7:
+      o->beta2 = 2.0 / (5.0 * 7.0);
+      o->beta1 = 7.0 / (10.0 * 7.0);
+      break;
+    case GBDE_ALG_ROSENBROCK23:  // error ~ h^3: I-controller
+      o->beta1 = 1.0 / 3.0;
+      o->beta2 = 0.0;
+      break;
+    case GBDE_ALG_RODAS5:
+    case GBDE_ALG_RODAS5P:  // embedded order 4: error ~ h^5
+      o->beta1 = 1.0 / 5.0;
+      o->beta2 = 0.0;
+      break;
+    case GBDE_ALG_EM:
+      o->adaptive = 0;
+      o->beta1 = 0.5;
+      break;
+    case GBDE_ALG_SOSRI:  // strong order 1.5 pair: error ~ h^2 (I-controller)
+      o->beta1 = 1.0 / 2.0;
+      o->beta2 = 0.0;
+      o->reltol = 1e-2;
+      o->abstol = 1e-2;
+      break;
+    case GBDE_ALG_AUTO:
+      o->beta2 = 0.04;
+      o->beta1 = 0.17;
+      break;
+    default:
+      return set_err(nullptr, GBDE_ERR_INVALID, "unknown algorithm id %d", alg);
+  }
+  return GBDE_OK;
+}
+
+static bool is_ode_alg(int a) {
+  return a == GBDE_ALG_TSIT5 || a == GBDE_ALG_VERN7 || a == GBDE_ALG_ROSENBROCK23 ||
+         a == GBDE_ALG_RODAS5 || a == GBDE_ALG_RODAS5P || a == GBDE_ALG_AUTO;
+}
+static bool is_sde_alg(int a) { return a == GBDE_ALG_EM || a == GBDE_ALG_SOSRI; }
+
+int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts* opts,
+                        gbde_outputs* out) {
+  if (!ctx) return set_err(nullptr, GBDE_ERR_INVALID, "ctx is NULL");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  const auto wall0 = std::chrono::steady_clock::now();
+  if (!prob || !opts || !out)
+    return set_err(ctx, GBDE_ERR_INVALID, "prob, opts and out must be non-NULL");
+  int32_t ns = 0, np = 0;
+  if (gbde_model_info(prob->model, &ns, &np) != GBDE_OK)
+    return set_err(ctx, GBDE_ERR_INVALID, "unknown model id %d", prob->model);
+  if (prob->n_state != ns || prob->n_param != np)
+    return set_err(ctx, GBDE_ERR_INVALID,
+                   "model %d has n_state=%d n_param=%d; got n_state=%d n_param=%d", prob->model,
+                   ns, np, prob->n_state, prob->n_param);
+  const int64_t N = prob->n_traj;
+  if (N < 0) return set_err(ctx, GBDE_ERR_INVALID, "n_traj must be >= 0 (got %lld)", (long long)N);
+  if (prob->mem != GBDE_MEM_HOST && prob->mem != GBDE_MEM_DEVICE)
+    return set_err(ctx, GBDE_ERR_INVALID, "mem must be GBDE_MEM_HOST or GBDE_MEM_DEVICE");
+  if (prob->save_kind != GBDE_SAVE_GRID && prob->save_kind != GBDE_SAVE_PER_TRAJ)
+    return set_err(ctx, GBDE_ERR_INVALID, "unknown save_kind %d", prob->save_kind);
+  if (prob->n_save < 0) return set_err(ctx, GBDE_ERR_INVALID, "n_save must be >= 0");
+  if (N > 0 && (!prob->p || !prob->u0 || !prob->t0 || !prob->tf))
+    return set_err(ctx, GBDE_ERR_INVALID, "p, u0, t0 and tf must be non-NULL");
+  if (prob->n_save > 0 && !prob->saveat)
+    return set_err(ctx, GBDE_ERR_INVALID, "saveat must be non-NULL when n_save > 0");
+  if (N > 0 && (!out->retcode || (prob->n_save > 0 && !out->u)))
+    return set_err(ctx, GBDE_ERR_INVALID, "out->u and out->retcode must be non-NULL");
+  if (out->u_dtype != GBDE_F64 && out->u_dtype != GBDE_F32)
+    return set_err(ctx, GBDE_ERR_INVALID, "u_dtype must be GBDE_F64 or GBDE_F32");
+  const int alg = opts->alg;
+  if (!is_ode_alg(alg) && !is_sde_alg(alg))
+    return set_err(ctx, GBDE_ERR_INVALID, "unknown algorithm id %d", alg);
+  if (is_sde_alg(alg) && prob->model != GBDE_MODEL_LOTKA_VOLTERRA)
+    return set_err(ctx, GBDE_ERR_UNSUPPORTED, "SDE algorithms need a model with a noise term");
+  if (opts->precision != GBDE_PREC_FP64 && opts->precision != GBDE_PREC_MIXED)
+    return set_err(ctx, GBDE_ERR_INVALID, "unknown precision %d", opts->precision);
+  if (opts->batching != GBDE_BATCH_PLAIN && opts->batching != GBDE_BATCH_PERSISTENT)
+    return set_err(ctx, GBDE_ERR_INVALID, "unknown batching %d", opts->batching);
+  if (opts->adaptive && !(opts->reltol > 0.0 && opts->abstol > 0.0))
+    return set_err(ctx, GBDE_ERR_INVALID, "adaptive stepping needs reltol > 0 and abstol > 0");
+  if (!opts->adaptive && !(opts->dt > 0.0))
+    return set_err(ctx, GBDE_ERR_INVALID, "fixed-step solving needs dt > 0");
+  if (opts->maxiters <= 0) return set_err(ctx, GBDE_ERR_INVALID, "maxiters must be > 0");
+  if (opts->adaptive && !(opts->qmin > 0.0 && opts->qmax >= 1.0 && opts->gamma > 0.0))
+    return set_err(ctx, GBDE_ERR_INVALID, "controller needs qmin > 0, qmax >= 1, gamma > 0");
+  if (opts->learned && ctx->pred_dt.ptr == nullptr)
+    return set_err(ctx, GBDE_ERR_STATE, "learned=1 but no predictor output is available");
+  if ((alg == GBDE_ALG_ROSENBROCK23 || alg == GBDE_ALG_RODAS5 || alg == GBDE_ALG_RODAS5P) &&
+      prob->model == GBDE_MODEL_VDP_RING8)
+    return set_err(ctx, GBDE_ERR_UNSUPPORTED,
+                   "one-thread-per-trajectory Rosenbrock kernels support n_state <= 3");
+  if (alg == GBDE_ALG_AUTO)
+    return set_err(ctx, GBDE_ERR_UNSUPPORTED, "GBDE_ALG_AUTO is not available in this build");
+
+  GBDE_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const size_t n_save = (size_t)prob->n_save;
+  const size_t esz = out->u_dtype == GBDE_F32 ? 4 : 8;
+  const size_t save_elems = prob->save_kind == GBDE_SAVE_GRID ? n_save : n_save * (size_t)N;
+  const size_t u_bytes = (size_t)N * n_save * (size_t)ns * esz;
+
+  KArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.N = N;
+  a.n_save = prob->n_save;
+  a.save_kind = prob->save_kind;
+  a.out_f32 = out->u_dtype == GBDE_F32;
+  a.reltol = opts->reltol;
+  a.abstol = opts->abstol;
+  a.dt0 = opts->dt;
+  a.dtmin = opts->dtmin;
+  a.dtmax = opts->dtmax;
+  a.maxiters = opts->maxiters;
+  a.adaptive = opts->adaptive;
+  a.qmin = opts->qmin;
+  a.qmax = opts->qmax;
+  a.gamma = opts->gamma;
+  a.beta1 = opts->beta1;
+  a.beta2 = opts->beta2;
+  a.qsteady_min = opts->qsteady_min;
+  a.qsteady_max = opts->qsteady_max;
+  a.qoldinit = opts->qoldinit;
+  a.seed = opts->seed;
+  a.timeout_ns = opts->timeout_s > 0 ? (uint64_t)(opts->timeout_s * 1e9) : 0;
+
+  const bool host = prob->mem == GBDE_MEM_HOST;
+  if (host) {
+    GBDE_CUDA(ctx, ctx->p.ensure((size_t)N * np * 8));
+    GBDE_CUDA(ctx, ctx->u0.ensure((size_t)N * ns * 8));
+    GBDE_CUDA(ctx, ctx->t0.ensure((size_t)N * 8));
+    GBDE_CUDA(ctx, ctx->tf.ensure((size_t)N * 8));
+    GBDE_CUDA(ctx, ctx->saveat.ensure(save_elems * 8));
+    GBDE_CUDA(ctx, ctx->u.ensure(u_bytes));
+    GBDE_CUDA(ctx, ctx->ret.ensure((size_t)N * 4));
+    if (N > 0) {
+      GBDE_CUDA(ctx, cudaMemcpyAsync(ctx->p.ptr, prob->p, (size_t)N * np * 8, cudaMemcpyHostToDevice, s));
+      GBDE_CUDA(ctx, cudaMemcpyAsync(ctx->u0.ptr, prob->u0, (size_t)N * ns * 8, cudaMemcpyHostToDevice, s));
+      GBDE_CUDA(ctx, cudaMemcpyAsync(ctx->t0.ptr, prob->t0, (size_t)N * 8, cudaMemcpyHostToDevice, s));
+      GBDE_CUDA(ctx, cudaMemcpyAsync(ctx->tf.ptr, prob->tf, (size_t)N * 8, cudaMemcpyHostToDevice, s));
+    }
+    if (save_elems > 0)
+      GBDE_CUDA(ctx, cudaMemcpyAsync(ctx->saveat.ptr, prob->saveat, save_elems * 8, cudaMemcpyHostToDevice, s));
+    a.p = (const double*)ctx->p.ptr;
+    a.u0 = (const double*)ctx->u0.ptr;
+    a.t0 = (const double*)ctx->t0.ptr;
+    a.tf = (const double*)ctx->tf.ptr;
+    a.saveat = (const double*)ctx->saveat.ptr;
+    a.u_out = ctx->u.ptr;
+    a.retcode = (int32_t*)ctx->ret.ptr;
+    if (out->naccept) { GBDE_CUDA(ctx, ctx->nacc.ensure((size_t)N * 4)); a.naccept = (int32_t*)ctx->nacc.ptr; }
+    if (out->nreject) { GBDE_CUDA(ctx, ctx->nrej.ensure((size_t)N * 4)); a.nreject = (int32_t*)ctx->nrej.ptr; }
+    if (out->nf) { GBDE_CUDA(ctx, ctx->nf.ensure((size_t)N * 4)); a.nf = (int32_t*)ctx->nf.ptr; }
+    if (out->t_end) { GBDE_CUDA(ctx, ctx->tend.ensure((size_t)N * 8)); a.t_end = (double*)ctx->tend.ptr; }
+    if (out->method) { GBDE_CUDA(ctx, ctx->method.ensure((size_t)N * 4)); a.method_out = (int32_t*)ctx->method.ptr; }
+  } else {
+    a.p = prob->p;
+    a.u0 = prob->u0;
+    a.t0 = prob->t0;
+    a.tf = prob->tf;
+    a.saveat = prob->saveat;
+    a.u_out = out->u;
+    a.retcode = out->retcode;
+    a.naccept = out->naccept;
+    a.nreject = out->nreject;
+    a.nf = out->nf;
+    a.t_end = out->t_end;
+    a.method_out = out->method;
+  }
+  GBDE_CUDA(ctx, ctx->work.ensure(256));
+  unsigned long long* work = (unsigned long long*)ctx->work.ptr;
+  GBDE_CUDA(ctx, cudaMemsetAsync(work, 0, 256, s));
+  a.queue = opts->batching == GBDE_BATCH_PERSISTENT ? work : nullptr;
+  a.flag = (int32_t*)(work + 1);
+  if (opts->learned) a.pred_dt = (const float*)ctx->pred_dt.ptr;
+
+  LaunchCfg cfg;
+  cfg.alg = alg;
+  cfg.model = prob->model;
+  cfg.precision = opts->precision;
+  cfg.persistent = opts->batching == GBDE_BATCH_PERSISTENT;
+  cfg.block = opts->block_size > 0 ? opts->block_size : 128;
+  cfg.grid = 0;
+  cfg.ctas_per_sm = opts->ctas_per_sm;
+  cfg.num_sms = ctx->num_sms;
+  if (cfg.block > 128 || (cfg.block & 31))
+    return set_err(ctx, GBDE_ERR_INVALID, "block_size must be a multiple of 32 and <= 128");
+
+  GBDE_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
+  if (N > 0) {
+    cudaError_t e;
+    if (alg == GBDE_ALG_TSIT5 || alg == GBDE_ALG_VERN7) e = launch_explicit(cfg, a, s);
+    else if (is_sde_alg(alg)) e = launch_sde(cfg, a, s);
+    else e = launch_rosenbrock(cfg, a, s);
+    if (e == cudaErrorNotSupported)
+      return set_err(ctx, GBDE_ERR_UNSUPPORTED, "algorithm %d is not built for model %d", alg,
+                     prob->model);
+    if (e != cudaSuccess)
+      return set_err(ctx, GBDE_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+  }
+  GBDE_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
+
+  int32_t flag = 0;
+  if (host) {
+    if (u_bytes) GBDE_CUDA(ctx, cudaMemcpyAsync(out->u, ctx->u.ptr, u_bytes, cudaMemcpyDeviceToHost, s));
+    if (N > 0) {
+      GBDE_CUDA(ctx, cudaMemcpyAsync(out->retcode, ctx->ret.ptr, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
+      if (out->naccept) GBDE_CUDA(ctx, cudaMemcpyAsync(out->naccept, a.naccept, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
+      if (out->nreject) GBDE_CUDA(ctx, cudaMemcpyAsync(out->nreject, a.nreject, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
+      if (out->nf) GBDE_CUDA(ctx, cudaMemcpyAsync(out->nf, a.nf, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
+      if (out->t_end) GBDE_CUDA(ctx, cudaMemcpyAsync(out->t_end, a.t_end, (size_t)N * 8, cudaMemcpyDeviceToHost, s));
+      if (out->method) GBDE_CUDA(ctx, cudaMemcpyAsync(out->method, a.method_out, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
+    }
+  }
+  GBDE_CUDA(ctx, cudaMemcpyAsync(&flag, a.flag, 4, cudaMemcpyDeviceToHost, s));
+  GBDE_CUDA(ctx, cudaStreamSynchronize(s));
+  float ms = 0.f;
+  GBDE_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  out->device_ms = ms;
+  out->total_ms = (float)std::chrono::duration<double, std::milli>(
+                      std::chrono::steady_clock::now() - wall0).count();
+  if (flag & 1)
+    return set_err(ctx, GBDE_ERR_TIMEOUT, "device deadline of %.3f s reached; unfinished "
+                   "trajectories carry GBDE_RET_TIMEOUT", opts->timeout_s);
+  return GBDE_OK;
+}
+
+int gbde_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  if (!ctr || !key || !out) return set_err(nullptr, GBDE_ERR_INVALID, "NULL argument");
+  Philox4 r = philox4x32_10(Philox4{ctr[0], ctr[1], ctr[2], ctr[3]}, key[0], key[1]);
+  out[0] = r.x; out[1] = r.y; out[2] = r.z; out[3] = r.w;
+  return GBDE_OK;
+}
+
+int gbde_philox_normals(uint64_t seed, uint64_t traj, uint64_t counter, int64_t n, double* out) {
+  if (n < 0 || (n > 0 && !out)) return set_err(nullptr, GBDE_ERR_INVALID, "bad n or out");
+  for (int64_t k = 0; k < n; ++k) out[k] = philox_normal_f64(seed, traj, counter + (uint64_t)k);
+  return GBDE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,37 @@
+// k_explicit.cu -- Tsit5 / Vern7 ensemble kernels (one trajectory per thread).
+#include "explicit_rk.cuh"
+#include "launch.h"
+
+namespace gbde {
+
+template <class Alg, class M, class T, bool MIXED>
+__global__ void __launch_bounds__(128) k_erk(const KArgs a) {
+  integrate_all<Alg, M, T, MIXED>(a);
+}
+
+template <template <class, class> class AlgT, class M>
+static cudaError_t dispatch_prec(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
+  if (cfg.precision == GBDE_PREC_MIXED)
+    return launch_kernel(k_erk<AlgT<M, float>, M, float, true>, cfg, a, s);
+  return launch_kernel(k_erk<AlgT<M, double>, M, double, false>, cfg, a, s);
+}
+
+template <template <class, class> class AlgT>
+static cudaError_t dispatch_model(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
+  switch (cfg.model) {
+    case GBDE_MODEL_LINEAR: return dispatch_prec<AlgT, Linear>(cfg, a, s);
+    case GBDE_MODEL_LORENZ: return dispatch_prec<AlgT, Lorenz>(cfg, a, s);
+    case GBDE_MODEL_ROBERTSON: return dispatch_prec<AlgT, Robertson>(cfg, a, s);
+    case GBDE_MODEL_VDP_RING8: return dispatch_prec<AlgT, VdpRing8>(cfg, a, s);
+    case GBDE_MODEL_LOTKA_VOLTERRA: return dispatch_prec<AlgT, LotkaVolterra>(cfg, a, s);
+  }
+  return cudaErrorNotSupported;
+}
+
+cudaError_t launch_explicit(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
+  if (cfg.alg == GBDE_ALG_TSIT5) return dispatch_model<Tsit5Alg>(cfg, a, s);
+  if (cfg.alg == GBDE_ALG_VERN7) return dispatch_model<Vern7Alg>(cfg, a, s);
+  return cudaErrorNotSupported;
+}
+
+}  // namespace gbde

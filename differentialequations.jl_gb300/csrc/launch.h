@@ -1,0 +1,46 @@
+// launch.h -- internal interface between the C ABI layer and the kernel
+// translation units.  Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include "solver.cuh"
+
+namespace gbde {
+
+struct LaunchCfg {
+  int alg, model, precision;
+  bool persistent;
+  int block;          // threads per CTA
+  int grid;           // CTAs (persistent) -- 0 = derive from N
+  int ctas_per_sm;    // persistent: resident CTAs per SM (0 = occupancy max)
+  int num_sms;
+};
+
+// Returns cudaSuccess, or cudaErrorNotSupported for an unknown combination.
+cudaError_t launch_explicit(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
+cudaError_t launch_rosenbrock(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
+cudaError_t launch_sde(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
+
+// Launch geometry helper shared by the translation units.
+template <class K>
+cudaError_t launch_kernel(K kern, const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
+  int block = cfg.block > 0 ? cfg.block : 128;
+  int grid;
+  if (cfg.persistent) {
+    int per_sm = cfg.ctas_per_sm;
+    if (per_sm <= 0) {
+      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, 0);
+      if (e != cudaSuccess) return e;
+      if (per_sm < 1) per_sm = 1;
+    }
+    grid = per_sm * cfg.num_sms;
+    const long long need = (a.N + block - 1) / block;
+    if (grid > need) grid = (int)(need > 0 ? need : 1);
+  } else {
+    const long long g = (a.N + block - 1) / block;
+    grid = (int)(g > 0 ? g : 1);
+  }
+  kern<<<grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace gbde

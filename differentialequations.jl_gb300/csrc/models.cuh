@@ -1,0 +1,124 @@
+// models.cuh -- built-in right-hand sides f(u, p) and analytic Jacobians.
+//
+// These stand in for the in-place ODEFunction f!(du, u, p, t) of the
+// reference (ODEFunction, test/qa/qa.jl:84).  All models are autonomous.
+// Formulas:
+//   LINEAR     du = a u                                  (test/core.jl:10)
+//   LORENZ     du = [s(y-x), x(r-z)-y, xy-bz]            (test/core.jl:22-27)
+//   ROBERTSON  du = [-k1 y1 + k3 y2 y3,
+//                    k1 y1 - k2 y2^2 - k3 y2 y3,
+//                    k2 y2^2]                            (test/core.jl:39-45)
+//   VDP_RING8  x_i' = v_i,
+//              v_i' = mu (1 - x_i^2) v_i - x_i + kappa (x_{i-1} - 2 x_i + x_{i+1})
+//              on a ring of 8 oscillators, state [x0, v0, x1, v1, ...]
+//   LOTKA_VOLTERRA (SDE) drift [a x - b x y, d x y - g y], noise sigma * u
+#pragma once
+#include "common.cuh"
+#include "../../include/gbde.h"
+
+namespace gbde {
+
+struct Linear {
+  static constexpr int N = 1, NP = 1, ID = GBDE_MODEL_LINEAR;
+  static constexpr int F_FLOPS = 1;
+  template <class T> GBDE_HD static void f(T* du, const T* u, const T* p) { du[0] = p[0] * u[0]; }
+  template <class T> GBDE_HD static void jac(T (*J)[1], const T* u, const T* p) { J[0][0] = p[0]; }
+};
+
+struct Lorenz {
+  static constexpr int N = 3, NP = 3, ID = GBDE_MODEL_LORENZ;
+  static constexpr int F_FLOPS = 11;  // 2 + 4 + 3 (+2 subtractions)
+  template <class T> GBDE_HD static void f(T* du, const T* u, const T* p) {
+    du[0] = p[0] * (u[1] - u[0]);
+    du[1] = u[0] * (p[1] - u[2]) - u[1];
+    du[2] = u[0] * u[1] - p[2] * u[2];
+  }
+  template <class T> GBDE_HD static void jac(T (*J)[3], const T* u, const T* p) {
+    J[0][0] = -p[0]; J[0][1] = p[0]; J[0][2] = T(0);
+    J[1][0] = p[1] - u[2]; J[1][1] = T(-1); J[1][2] = -u[0];
+    J[2][0] = u[1]; J[2][1] = u[0]; J[2][2] = -p[2];
+  }
+};
+
+struct Robertson {
+  static constexpr int N = 3, NP = 3, ID = GBDE_MODEL_ROBERTSON;
+  static constexpr int F_FLOPS = 12;
+  template <class T> GBDE_HD static void f(T* du, const T* u, const T* p) {
+    T r1 = p[0] * u[0];
+    T r2 = p[1] * u[1] * u[1];
+    T r3 = p[2] * u[1] * u[2];
+    du[0] = -r1 + r3;
+    du[1] = r1 - r2 - r3;
+    du[2] = r2;
+  }
+  template <class T> GBDE_HD static void jac(T (*J)[3], const T* u, const T* p) {
+    J[0][0] = -p[0]; J[0][1] = p[2] * u[2]; J[0][2] = p[2] * u[1];
+    J[1][0] = p[0]; J[1][1] = T(-2) * p[1] * u[1] - p[2] * u[2]; J[1][2] = -p[2] * u[1];
+    J[2][0] = T(0); J[2][1] = T(2) * p[1] * u[1]; J[2][2] = T(0);
+  }
+};
+
+struct VdpRing8 {
+  static constexpr int N = 16, NP = 2, ID = GBDE_MODEL_VDP_RING8;
+  static constexpr int F_FLOPS = 8 * 9;
+  template <class T> GBDE_HD static void f(T* du, const T* u, const T* p) {
+    const T mu = p[0], ka = p[1];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const T x = u[2 * i], v = u[2 * i + 1];
+      const T xl = u[2 * ((i + 7) & 7)], xr = u[2 * ((i + 1) & 7)];
+      du[2 * i] = v;
+      du[2 * i + 1] = mu * (T(1) - x * x) * v - x + ka * (xl - T(2) * x + xr);
+    }
+  }
+  template <class T> GBDE_HD static void jac(T (*J)[16], const T* u, const T* p) {
+    const T mu = p[0], ka = p[1];
+#pragma unroll
+    for (int r = 0; r < 16; ++r)
+#pragma unroll
+      for (int c = 0; c < 16; ++c) J[r][c] = T(0);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const T x = u[2 * i], v = u[2 * i + 1];
+      J[2 * i][2 * i + 1] = T(1);
+      J[2 * i + 1][2 * i] = T(-2) * mu * x * v - T(1) - T(2) * ka;
+      J[2 * i + 1][2 * i + 1] = mu * (T(1) - x * x);
+      J[2 * i + 1][2 * ((i + 7) & 7)] += ka;
+      J[2 * i + 1][2 * ((i + 1) & 7)] += ka;
+    }
+  }
+  // Row r of the Jacobian (for the warp-cooperative Rosenbrock path).
+  template <class T> GBDE_HD static T jac_entry(int r, int c, const T* u, const T* p) {
+    const T mu = p[0], ka = p[1];
+    const int i = r >> 1;
+    if ((r & 1) == 0) return c == r + 1 ? T(1) : T(0);
+    const T x = u[2 * i], v = u[2 * i + 1];
+    T val = T(0);
+    if (c == 2 * i) val = T(-2) * mu * x * v - T(1) - T(2) * ka;
+    if (c == 2 * i + 1) val = mu * (T(1) - x * x);
+    if (c == 2 * ((i + 7) & 7)) val += ka;
+    if (c == 2 * ((i + 1) & 7)) val += ka;
+    return val;
+  }
+};
+
+struct LotkaVolterra {
+  static constexpr int N = 2, NP = 5, ID = GBDE_MODEL_LOTKA_VOLTERRA;
+  static constexpr int F_FLOPS = 7, G_FLOPS = 2;
+  template <class T> GBDE_HD static void f(T* du, const T* u, const T* p) {
+    const T xy = u[0] * u[1];
+    du[0] = p[0] * u[0] - p[1] * xy;
+    du[1] = p[3] * xy - p[2] * u[1];
+  }
+  // diagonal noise g(u) = sigma * u
+  template <class T> GBDE_HD static void g(T* gu, const T* u, const T* p) {
+    gu[0] = p[4] * u[0];
+    gu[1] = p[4] * u[1];
+  }
+  template <class T> GBDE_HD static void jac(T (*J)[2], const T* u, const T* p) {
+    J[0][0] = p[0] - p[1] * u[1]; J[0][1] = -p[1] * u[0];
+    J[1][0] = p[3] * u[1]; J[1][1] = p[3] * u[0] - p[2];
+  }
+};
+
+}  // namespace gbde

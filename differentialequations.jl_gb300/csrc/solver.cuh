@@ -1,0 +1,343 @@
+// solver.cuh -- the per-trajectory integration driver shared by every
+// ODE method: step-size controller, error norm, initial dt, saveat writer,
+// tf handling, return codes and the work source (plain launch or persistent
+// device queue).
+//
+// The driver replaces, per trajectory, OrdinaryDiffEq's solve! loop
+// (perform_step!, the PI controller, savevalues!) that SciMLBase's
+// EnsembleThreads maps over trajectories (EnsembleThreads, test/qa/qa.jl:56;
+// the controller accessors it exposes are get_proposed_dt / set_proposed_dt!
+// / auto_dt_reset!, qa.jl:151,187,135).  Controller formulas follow
+// Hairer-Norsett-Wanner I, Sec. II.4 and Gustafsson's PI control:
+//     q11 = EEst^beta1,  q = q11 / qold^beta2,
+//     q   = clamp(q / gamma, 1/qmax, 1/qmin)
+//     accept (EEst <= 1): q = 1 if qsteady_min <= q <= qsteady_max;
+//                         dt <- dt / q;  qold = max(EEst, qoldinit)
+//     reject:             dt <- dt / min(1/qmin, q11 / gamma)
+// with the scaled RMS norm
+//     EEst = sqrt(mean_i (err_i / (abstol + reltol max(|u_i|, |unew_i|)))^2).
+#pragma once
+#include <cooperative_groups.h>
+#include "common.cuh"
+#include "models.cuh"
+
+namespace gbde {
+
+// Kernel arguments (passed by value; lives in the constant bank).
+struct KArgs {
+  int64_t N;
+  int32_t n_save, save_kind;
+  const double* p;
+  const double* u0;
+  const double* t0;
+  const double* tf;
+  const double* saveat;
+  void* u_out;
+  int32_t out_f32;
+  int32_t* retcode;
+  int32_t* naccept;
+  int32_t* nreject;
+  int32_t* nf;
+  double* t_end;
+  int32_t* method_out;
+  double reltol, abstol, dt0, dtmin, dtmax;
+  int64_t maxiters;
+  int32_t adaptive;
+  double qmin, qmax, gamma, beta1, beta2, qsteady_min, qsteady_max, qoldinit;
+  uint64_t seed;
+  unsigned long long* queue;  // persistent work counter (NULL = plain launch)
+  const int32_t* order;       // optional trajectory order for the queue
+  uint64_t timeout_ns;        // 0 = no deadline
+  int32_t* flag;              // device status word (bit 0: deadline hit)
+  const float* pred_dt;       // optional predicted first dt per trajectory
+};
+
+GBDE_D uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// ----------------------------------------------------------- work source
+// Plain launch: each thread takes its own index once.  Persistent launch:
+// threads that need work take consecutive indices from a global counter
+// with one atomic per group of converged lanes (warp-aggregated).
+struct WorkSource {
+  int64_t first;
+  bool used;
+  GBDE_D void init() {
+    first = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    used = false;
+  }
+  GBDE_D int64_t next(const KArgs& a) {
+    if (a.queue == nullptr) {
+      if (used) return -1;
+      used = true;
+      return first < a.N ? first : -1;
+    }
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(a.queue, (unsigned long long)g.size());
+    base = g.shfl(base, 0);
+    const unsigned long long idx = base + g.thread_rank();
+    if (idx >= (unsigned long long)a.N) return -1;
+    return a.order ? (int64_t)a.order[idx] : (int64_t)idx;
+  }
+};
+
+// ------------------------------------------------------------- saving
+GBDE_D double save_time(const KArgs& a, int64_t i, int j) {
+  return a.save_kind == GBDE_SAVE_GRID ? __ldg(a.saveat + j)
+                                       : __ldg(a.saveat + (size_t)i * a.n_save + j);
+}
+
+template <int N, class T>
+GBDE_D void store_state(const KArgs& a, int64_t i, int j, const T* v) {
+  const size_t base = ((size_t)i * a.n_save + j) * N;
+  if (a.out_f32) {
+    float* o = (float*)a.u_out + base;
+    if constexpr (N % 4 == 0) {
+#pragma unroll
+      for (int c = 0; c < N; c += 4)
+        *reinterpret_cast<float4*>(o + c) =
+            make_float4((float)v[c], (float)v[c + 1], (float)v[c + 2], (float)v[c + 3]);
+    } else if constexpr (N % 2 == 0) {
+#pragma unroll
+      for (int c = 0; c < N; c += 2)
+        *reinterpret_cast<float2*>(o + c) = make_float2((float)v[c], (float)v[c + 1]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < N; ++c) o[c] = (float)v[c];
+    }
+  } else {
+    double* o = (double*)a.u_out + base;
+    if constexpr (N % 2 == 0) {
+#pragma unroll
+      for (int c = 0; c < N; c += 2)
+        *reinterpret_cast<double2*>(o + c) = make_double2((double)v[c], (double)v[c + 1]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < N; ++c) o[c] = (double)v[c];
+    }
+  }
+}
+
+// --------------------------------------------------------- error norm
+template <int N, class T>
+GBDE_HD double err_norm(const T* err, const T* u, const T* unew, double abstol, double reltol) {
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    const double sc = abstol + reltol * fmax(fabs((double)u[c]), fabs((double)unew[c]));
+    const double e = (double)err[c] / sc;
+    s += e * e;
+  }
+  return sqrt(s / N);
+}
+
+// Hairer-Wanner starting step (HNW I, Sec. II.4): d0 = |u0|, d1 = |f0|,
+// h0 = 0.01 d0/d1, one explicit Euler trial step for d2 = |f1 - f0|/h0,
+// h1 = (0.01 / max(d1, d2))^(1/(order+1)), dt = min(100 h0, h1, tf - t0).
+template <class M, class T>
+GBDE_D double initial_dt(const T* u0, const T* f0, const T* p, double tspan, int order,
+                         double abstol, double reltol, int& nf) {
+  constexpr int N = M::N;
+  double d0 = 0.0, d1 = 0.0;
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    const double sc = abstol + fabs((double)u0[c]) * reltol;
+    const double x = (double)u0[c] / sc, y = (double)f0[c] / sc;
+    d0 += x * x;
+    d1 += y * y;
+  }
+  d0 = sqrt(d0 / N);
+  d1 = sqrt(d1 / N);
+  double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
+  h0 = fmin(h0, tspan);
+  T u1[N], f1[N];
+#pragma unroll
+  for (int c = 0; c < N; ++c) u1[c] = u0[c] + T(h0) * f0[c];
+  M::f(f1, u1, p);
+  ++nf;
+  double d2 = 0.0;
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    const double sc = abstol + fabs((double)u0[c]) * reltol;
+    const double y = ((double)f1[c] - (double)f0[c]) / sc;
+    d2 += y * y;
+  }
+  d2 = sqrt(d2 / N) / h0;
+  const double m = fmax(d1, d2);
+  const double h1 = (m <= 1e-15) ? fmax(1e-6, h0 * 1e-3) : pow(0.01 / m, 1.0 / (order + 1));
+  return fmin(fmin(100.0 * h0, h1), tspan);
+}
+
+// ------------------------------------------------------------- driver
+// Alg provides:  static constexpr int ORDER (for beta defaults / init dt),
+//   void init(const T* u0, const T* p, int& nf)       -- u = u0, f(u) cache
+//   double attempt(double dt, const T* p, double abstol, double reltol, int& nf)
+//                                                       -- returns EEst
+//   void interp(double theta, double dt, T* out, const T* p, int& nf)
+//                                                       -- dense output
+//   void accept(const T* p, int& nf)                    -- u = unew, caches
+//   const T* u() / unew() / f0()
+template <class Alg, class M, class T, bool MIXED>
+__device__ void integrate_all(const KArgs& a) {
+  constexpr int N = M::N;
+  WorkSource src;
+  src.init();
+  Alg alg;
+  T p[M::NP];
+  int64_t i = -1;
+  bool active = false;
+  double t = 0.0, tlo = 0.0, tf = 0.0, dt = 0.0, qold = 1.0;
+  int js = 0, nacc = 0, nrej = 0, nfev = 0;
+  int64_t iters = 0;
+  int ret = GBDE_RET_DEFAULT;
+  const uint64_t t_start = a.timeout_ns ? global_ns() : 0;
+
+  while (true) {
+    if (!active) {
+      i = src.next(a);
+      if (i < 0) break;
+      // ---- load the trajectory
+      T u0[N];
+#pragma unroll
+      for (int k = 0; k < M::NP; ++k) p[k] = (T)__ldg(a.p + (size_t)i * M::NP + k);
+#pragma unroll
+      for (int c = 0; c < N; ++c) u0[c] = (T)__ldg(a.u0 + (size_t)i * N + c);
+      t = __ldg(a.t0 + i);
+      tlo = 0.0;
+      tf = __ldg(a.tf + i);
+      js = 0;
+      nacc = nrej = nfev = 0;
+      iters = 0;
+      qold = a.qoldinit;
+      ret = GBDE_RET_DEFAULT;
+      bool bad = !(tf >= t) || !isfinite(t) || !isfinite(tf);
+#pragma unroll
+      for (int c = 0; c < N; ++c) bad |= !isfinite((double)u0[c]);
+      // save points at t0 store u0 exactly
+      while (js < a.n_save && save_time(a, i, js) <= t) {
+        store_state<N>(a, i, js, u0);
+        ++js;
+      }
+      if (bad) {
+        ret = GBDE_RET_INITIALFAILURE;
+      } else {
+        alg.init(u0, p, nfev);
+        if (a.pred_dt != nullptr && a.pred_dt[i] > 0.f) {
+          dt = fmin((double)a.pred_dt[i], tf - t);
+        } else if (a.dt0 > 0.0 || !a.adaptive) {
+          dt = a.dt0;
+        } else {
+          dt = initial_dt<M, T>(alg.u(), alg.f0(), p, tf - t, Alg::ORDER, a.abstol, a.reltol,
+                                nfev);
+        }
+        if (a.dtmax > 0.0) dt = fmin(dt, a.dtmax);
+        if (!(t < tf)) ret = GBDE_RET_SUCCESS;
+        else if (!(dt > 0.0)) ret = GBDE_RET_DTLESSTHANMIN;
+      }
+      active = true;
+    }
+
+    if (ret == GBDE_RET_DEFAULT) {
+      // ---- one attempted step
+      const double rem = tf - t;
+      double h = dt;
+      bool last = false;
+      if (h * (1.0 + 1e-10) >= rem) {
+        h = rem;
+        last = true;
+      }
+      const double EEst = alg.attempt(h, p, a.abstol, a.reltol, nfev);
+      ++iters;
+      const bool ok = !a.adaptive || EEst <= 1.0;
+      if (ok) {
+        // controller proposal for the next step
+        double dtnew = h;
+        if (a.adaptive) {
+          const double q11 = pow(EEst, a.beta1);
+          double q = q11 / pow(qold, a.beta2);
+          q = fmax(1.0 / a.qmax, fmin(1.0 / a.qmin, q / a.gamma));
+          if (q >= a.qsteady_min && q <= a.qsteady_max) q = 1.0;
+          dtnew = h / q;
+          qold = fmax(EEst, a.qoldinit);
+        }
+        // time update (compensated in the mixed-precision path)
+        double tnew;
+        if (last) {
+          tnew = tf;
+          tlo = 0.0;
+        } else if (MIXED) {
+          double s, e;
+          two_sum(t, h, s, e);
+          e += tlo;
+          tnew = s + e;
+          tlo = e - (tnew - s);
+        } else {
+          tnew = t + h;
+        }
+        // saveat: dense output at every save time in (t, tnew]
+        while (js < a.n_save) {
+          const double ts = save_time(a, i, js);
+          if (!(ts <= tnew)) break;
+          if (ts >= tnew) {
+            store_state<N>(a, i, js, alg.unew());
+          } else {
+            T tmp[N];
+            alg.interp(((ts - t) - tlo) / h, h, tmp, p, nfev);
+            store_state<N>(a, i, js, tmp);
+          }
+          ++js;
+        }
+        alg.accept(p, nfev);
+        t = tnew;
+        ++nacc;
+        bool fin = true;
+#pragma unroll
+        for (int c = 0; c < N; ++c) fin &= isfinite((double)alg.u()[c]);
+        if (!fin) ret = GBDE_RET_UNSTABLE;
+        else if (last) ret = GBDE_RET_SUCCESS;
+        dt = a.dtmax > 0.0 ? fmin(dtnew, a.dtmax) : dtnew;
+      } else {
+        ++nrej;
+        if (isfinite(EEst)) {
+          const double q11 = pow(EEst, a.beta1);
+          dt = h / fmin(1.0 / a.qmin, q11 / a.gamma);
+        } else {
+          dt = h * a.qmin;
+        }
+      }
+      if (ret == GBDE_RET_DEFAULT) {
+        if (iters >= a.maxiters) ret = GBDE_RET_MAXITERS;
+        else if (a.adaptive && (dt < a.dtmin || dt <= 4.0 * 2.220446049250313e-16 * fabs(t)))
+          ret = GBDE_RET_DTLESSTHANMIN;
+        else if (a.timeout_ns && (iters & 31) == 0 && global_ns() - t_start > a.timeout_ns) {
+          ret = GBDE_RET_TIMEOUT;
+          atomicOr(a.flag, 1);
+        }
+      }
+    }
+
+    if (ret != GBDE_RET_DEFAULT) {
+      // ---- finish the trajectory; save slots never reached hold NaN
+      if (js < a.n_save) {
+        T nanv[N];
+#pragma unroll
+        for (int c = 0; c < N; ++c) nanv[c] = (T)__longlong_as_double(0x7ff8000000000000ll);
+        for (; js < a.n_save; ++js) store_state<N>(a, i, js, nanv);
+      }
+      a.retcode[i] = ret;
+      if (a.naccept) a.naccept[i] = nacc;
+      if (a.nreject) a.nreject[i] = nrej;
+      if (a.nf) a.nf[i] = nfev;
+      if (a.t_end) a.t_end[i] = t + tlo;
+      if (a.method_out) a.method_out[i] = Alg::ALG_ID;
+      active = false;
+    }
+  }
+}
+
+}  // namespace gbde

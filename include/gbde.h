@@ -1,0 +1,220 @@
+/*
+ * gbde.h -- C ABI of the GB300 ensemble ODE/SDE solver (libgbde.so).
+ *
+ * This is the drop-in boundary for the data-parallel hot path of
+ * DifferentialEquations.jl:
+ *
+ *     solve(EnsembleProblem(prob; prob_func), alg, ensemblealg;
+ *           trajectories, saveat, reltol, abstol)
+ *
+ * The reference re-exports that surface from SciMLBase / OrdinaryDiffEq
+ * (src/DifferentialEquations.jl:8-9); the names it allow-lists are
+ * EnsembleProblem (test/qa/qa.jl:50), EnsembleThreads (qa.jl:56),
+ * solve (qa.jl:192), remake (qa.jl:183), ReturnCode (qa.jl:213),
+ * Tsit5 (qa.jl:119), Vern7 (qa.jl:126), Rosenbrock23 (qa.jl:98),
+ * Rodas5P (qa.jl:97), SDEProblem (qa.jl:103).  The per-trajectory solve
+ * that EnsembleThreads maps over trajectories lives in OrdinaryDiffEq v7 /
+ * SciMLBase v3 (Project.toml:13,18), which the reference does not vendor.
+ *
+ * gbde_ensemble_solve() replaces the whole
+ *     SciMLBase.__solve(::EnsembleProblem, alg, ::EnsembleAlgorithm)
+ * branch: the host evaluates prob_func into structure-of-arrays inputs,
+ * makes ONE call, and wraps the returned arrays as per-trajectory solutions.
+ *
+ * Conventions
+ *   - Every function returns an int status: GBDE_OK (0) or a negative
+ *     GBDE_ERR_* code; gbde_last_error() describes the last failure.
+ *   - No call aborts the process; per-trajectory outcomes are written to
+ *     outputs.retcode[] (GBDE_RET_*), never raised.
+ *   - Arrays are C-order ("row-major"); the trajectory index is the slowest
+ *     dimension of every per-trajectory array, which is Julia's column-major
+ *     Array{Float64}(n, N) / Array{Float64,3}(n_state, n_save, N).
+ *   - A context is bound to one device and one CUDA stream; calls on one
+ *     context are serialised by an internal mutex.
+ */
+#ifndef GBDE_H
+#define GBDE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBDE_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define GBDE_API __attribute__((visibility("default")))
+#else
+#define GBDE_API
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define GBDE_OK 0
+#define GBDE_ERR_INVALID (-1)     /* bad argument (sizes, pointers, enums) */
+#define GBDE_ERR_CUDA (-2)        /* a CUDA runtime call failed           */
+#define GBDE_ERR_UNSUPPORTED (-3) /* valid but not implemented combination */
+#define GBDE_ERR_TIMEOUT (-4)     /* device work gave up after its deadline */
+#define GBDE_ERR_NOMEM (-5)       /* device or pinned allocation failed    */
+#define GBDE_ERR_STATE (-6)       /* e.g. learned=1 without a loaded MLP   */
+
+/* ---- per-trajectory return codes (SciMLBase ReturnCode, qa.jl:213) ---- */
+#define GBDE_RET_DEFAULT 0        /* not solved                            */
+#define GBDE_RET_SUCCESS 1        /* ReturnCode.Success                    */
+#define GBDE_RET_MAXITERS 2       /* ReturnCode.MaxIters                   */
+#define GBDE_RET_DTLESSTHANMIN 3  /* ReturnCode.DtLessThanMin              */
+#define GBDE_RET_UNSTABLE 4       /* ReturnCode.Unstable (non-finite state)*/
+#define GBDE_RET_INITIALFAILURE 5 /* ReturnCode.InitialFailure (bad input) */
+#define GBDE_RET_TIMEOUT 6        /* device deadline hit (no Julia analog) */
+
+/* ---- built-in right-hand sides (ODEFunction f!(du,u,p,t), qa.jl:84) ---- */
+#define GBDE_MODEL_LINEAR 1    /* n=1, p=[a]:           du = a*u (test/core.jl:10) */
+#define GBDE_MODEL_LORENZ 2    /* n=3, p=[sigma,rho,beta]          (test/core.jl:22-27) */
+#define GBDE_MODEL_ROBERTSON 3 /* n=3, p=[k1,k2,k3]                (test/core.jl:39-45) */
+#define GBDE_MODEL_VDP_RING8 4 /* n=16, p=[mu,kappa]: 8 Van der Pol oscillators on a ring */
+#define GBDE_MODEL_LOTKA_VOLTERRA 5 /* n=2, p=[alpha,beta,gamma,delta,sigma]:
+                                       drift [a x - b x y, d x y - g y],
+                                       diagonal noise sigma*u (SDE)            */
+
+/* ---- algorithms ------------------------------------------------------- */
+#define GBDE_ALG_TSIT5 1        /* Tsitouras 5(4), FSAL, free 4th-order interpolant */
+#define GBDE_ALG_VERN7 2        /* Verner 7(6)                                      */
+#define GBDE_ALG_ROSENBROCK23 3 /* Shampine-Reichelt 2(3) W-method                  */
+#define GBDE_ALG_RODAS5 4       /* Di Marzo 5(4) Rosenbrock, stiffly accurate       */
+#define GBDE_ALG_RODAS5P 5      /* Steinebach 5(4) Rosenbrock                       */
+#define GBDE_ALG_EM 6           /* Euler-Maruyama, fixed step                       */
+#define GBDE_ALG_SOSRI 7        /* SRI strong 1.5, adaptive with rejection sampling
+                                   with memory                                      */
+#define GBDE_ALG_AUTO 8         /* per-trajectory Tsit5 / Rodas5 choice (threshold
+                                   on the stiffness parameter, or the learned MLP)  */
+
+/* ---- precision -------------------------------------------------------- */
+#define GBDE_PREC_FP64 0  /* everything in FP64                                  */
+#define GBDE_PREC_MIXED 1 /* FP32 state and stages; FP64 compensated time, FP64
+                             error norm, FP64 W-matrix LU                         */
+
+/* ---- batching --------------------------------------------------------- */
+#define GBDE_BATCH_PLAIN 0      /* one thread per trajectory, one launch      */
+#define GBDE_BATCH_PERSISTENT 1 /* persistent CTAs refill finished threads from a
+                                   device work queue (longest trajectories first) */
+
+/* ---- save-time layout ------------------------------------------------- */
+#define GBDE_SAVE_GRID 0     /* saveat[n_save] shared by all trajectories   */
+#define GBDE_SAVE_PER_TRAJ 1 /* saveat[N][n_save]                             */
+
+/* ---- memory space of the problem / output pointers -------------------- */
+#define GBDE_MEM_HOST 0   /* host pointers: the call copies H2D and D2H     */
+#define GBDE_MEM_DEVICE 1 /* device pointers on the context's device: no copies */
+
+/* ---- output element type ---------------------------------------------- */
+#define GBDE_F64 0
+#define GBDE_F32 1
+
+typedef struct gbde_ctx gbde_ctx;
+
+/* One ensemble: N trajectories of the same model with per-trajectory
+ * parameters, initial states and time spans (the result of prob_func /
+ * remake over i = 1..N).  Save times must be non-decreasing and lie in
+ * [t0_i, tf_i]; a save time equal to t0_i stores u0_i exactly (the
+ * reference pins sol.u[1] == u0 at test/core.jl:34), one equal to tf_i
+ * stores the final state.  The host layer decides whether t0 / tf are in
+ * the list (save_start / save_end; test/core.jl:90-96 expects 11 points
+ * for saveat=0.1 on (0,1)). */
+typedef struct {
+  int32_t model;       /* GBDE_MODEL_*                                     */
+  int32_t n_state;     /* must equal the model's state size               */
+  int32_t n_param;     /* must equal the model's parameter count          */
+  int32_t mem;         /* GBDE_MEM_HOST or GBDE_MEM_DEVICE                */
+  int64_t n_traj;      /* N >= 0                                          */
+  const double* p;     /* [N][n_param]                                    */
+  const double* u0;    /* [N][n_state]                                    */
+  const double* t0;    /* [N]                                             */
+  const double* tf;    /* [N], tf_i >= t0_i                               */
+  int32_t save_kind;   /* GBDE_SAVE_GRID or GBDE_SAVE_PER_TRAJ            */
+  int32_t n_save;      /* >= 0 save times per trajectory                  */
+  const double* saveat;/* [n_save] or [N][n_save]                         */
+} gbde_problem;
+
+/* Solver options: the solve() keyword arguments of the reference
+ * (reltol, abstol, dt, adaptive, maxiters, dtmin, dtmax, qmin, qmax, gamma,
+ * beta1, beta2, qsteady_min, qsteady_max, qoldinit; seed for the noise).
+ * Fill with gbde_opts_default() and override. */
+typedef struct {
+  int32_t alg;         /* GBDE_ALG_*                                      */
+  int32_t precision;   /* GBDE_PREC_*                                     */
+  int32_t batching;    /* GBDE_BATCH_*                                    */
+  int32_t adaptive;    /* 1 = error-controlled steps; 0 = fixed dt        */
+  double reltol, abstol;
+  double dt;           /* initial dt (0 = automatic), or the fixed step   */
+  double dtmin;        /* a step below dtmin ends with DtLessThanMin      */
+  double dtmax;        /* 0 = unlimited                                   */
+  int64_t maxiters;    /* attempted steps per trajectory                  */
+  double qmin, qmax, gamma, beta1, beta2, qsteady_min, qsteady_max, qoldinit;
+  uint64_t seed;       /* Philox key for SDE noise                        */
+  int32_t learned;     /* 1 = the loaded MLP predicts first dt / method   */
+  int32_t block_size;  /* threads per CTA (0 = tuned default)             */
+  int32_t chunk;       /* persistent-queue trajectories per fetch (0 = default) */
+  int32_t ctas_per_sm; /* persistent CTAs per SM (0 = tuned default)      */
+  double stiff_threshold; /* GBDE_ALG_AUTO without MLP: stiff iff p[0] > this */
+  double timeout_s;    /* device deadline per call (0 = none)             */
+} gbde_opts;
+
+/* Results.  u is [N][n_save][n_state] of u_dtype; retcode [N]; the step
+ * statistics may be NULL. */
+typedef struct {
+  void* u;             /* [N][n_save][n_state]                            */
+  int32_t u_dtype;     /* GBDE_F64 or GBDE_F32                            */
+  int32_t* retcode;    /* [N] GBDE_RET_*                                  */
+  int32_t* naccept;    /* [N] or NULL: accepted steps                     */
+  int32_t* nreject;    /* [N] or NULL: rejected steps                     */
+  int32_t* nf;         /* [N] or NULL: right-hand-side evaluations        */
+  double* t_end;       /* [N] or NULL: time reached                       */
+  int32_t* method;     /* [N] or NULL: GBDE_ALG_* actually used (AUTO)    */
+  float device_ms;     /* out: device time of the solve kernels           */
+  float total_ms;      /* out: wall time of the whole call                */
+} gbde_outputs;
+
+/* ABI version of the loaded library (GBDE_ABI_VERSION). */
+GBDE_API int gbde_version(void);
+
+/* Create a context on CUDA device `device`; allocates nothing large. */
+GBDE_API int gbde_ctx_create(int device, gbde_ctx** out);
+/* Destroy a context and release its device/pinned buffers. NULL is a no-op. */
+GBDE_API int gbde_ctx_destroy(gbde_ctx* ctx);
+/* Description of the last error on ctx (valid until the next call on it);
+ * with ctx == NULL, the last context-less error of this thread. */
+GBDE_API const char* gbde_last_error(const gbde_ctx* ctx);
+/* Use `stream` (a cudaStream_t on the context's device, or NULL for the
+ * context's own stream) for all following launches and copies. */
+GBDE_API int gbde_ctx_set_stream(gbde_ctx* ctx, void* stream);
+
+/* Fill `out` with this library's defaults for algorithm `alg`. */
+GBDE_API int gbde_opts_default(int32_t alg, gbde_opts* out);
+
+/* Solve the ensemble.  Blocks until the results are in `out` (host mode) or
+ * the kernels have finished (device mode). */
+GBDE_API int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob,
+                        const gbde_opts* opts, gbde_outputs* out);
+
+/* Model metadata: state and parameter counts of a built-in model. */
+GBDE_API int gbde_model_info(int32_t model, int32_t* n_state, int32_t* n_param);
+
+/* Host regeneration of the noise stream: the standard normals the SDE
+ * kernels draw for trajectory `traj` at draw indices counter..counter+n-1
+ * (two normals per Philox4x32-10 block in FP64).  Bit-identical to the
+ * device stream; lets a caller reproduce any trajectory's Brownian path. */
+GBDE_API int gbde_philox_normals(uint64_t seed, uint64_t traj, uint64_t counter,
+                        int64_t n, double* out);
+/* Raw Philox4x32-10 block: out[4] = philox(ctr[4], key[2]). */
+GBDE_API int gbde_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
+                       uint32_t out[4]);
+
+/* Measure the device's FP64 / FP32 FMA throughput (TFLOP/s, FMA = 2 flops)
+ * with a dependent-chain-free FMA loop; kind 0 = FP64, 1 = FP32. */
+GBDE_API int gbde_measure_fma_peak(gbde_ctx* ctx, int32_t kind, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBDE_H */

@@ -1,0 +1,1050 @@
+// gbde_oracle.cpp -- CPU FP64 oracle for the ensemble hot path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker: the tests, the smoke
+// check and the benchmark's CPU-baseline leg call it; the product library
+// (libgbde.so) never links or calls it.
+//
+// It is an independent restatement of the per-trajectory solve that
+// SciMLBase's EnsembleThreads maps over trajectories (EnsembleThreads,
+// test/qa/qa.jl:56; solve qa.jl:192), for the methods named by the
+// reference's API: Tsit5 (qa.jl:119; test/core.jl:14,32), Vern7 (qa.jl:126),
+// Rosenbrock23 (qa.jl:98), Rodas5P (qa.jl:97; test/core.jl:47,
+// src/DifferentialEquations.jl:28) and Rodas5, and for the SDE methods EM and
+// SOSRI of StochasticDiffEq (SDEProblem qa.jl:103).  The reference's own
+// implementations live in OrdinaryDiffEq v7 / SciMLBase v3 / StochasticDiffEq
+// (Project.toml:6-18), which are neither vendored nor runnable here (no Julia
+// runtime); the numeric pins are the order conditions of the coefficient
+// tables (tableaus.h, tests/test_tableaus.py), analytic solutions, scipy
+// solve_ivp references and the reference's pinned behaviours
+// (test/core.jl:9-19, 21-36, 38-49, 90-96).
+//
+// Everything is FP64 scalar code with runtime state size n <= 16.  The
+// EnsembleThreads-equivalent baseline splits trajectories over a
+// std::thread pool (oracle_ensemble_solve's nthreads argument).
+//
+// Build: oracle/build_oracle.py (g++ -O2 -ffp-contract=off).
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "../include/gbde.h"
+#include "../differentialequations.jl_gb300/csrc/tableaus.h"
+
+namespace {
+
+constexpr int NMAX = 16;
+using Vec = double[NMAX];
+
+// ------------------------------------------------------------- models
+struct Model {
+  int id, n, np;
+};
+
+void rhs(int id, const double* u, const double* p, double* du) {
+  switch (id) {
+    case GBDE_MODEL_LINEAR: du[0] = p[0] * u[0]; break;
+    case GBDE_MODEL_LORENZ:  // test/core.jl:22-27
+      du[0] = p[0] * (u[1] - u[0]);
+      du[1] = u[0] * (p[1] - u[2]) - u[1];
+      du[2] = u[0] * u[1] - p[2] * u[2];
+      break;
+    case GBDE_MODEL_ROBERTSON: {  // test/core.jl:39-45
+      const double r1 = p[0] * u[0], r2 = p[1] * u[1] * u[1], r3 = p[2] * u[1] * u[2];
+      du[0] = -r1 + r3;
+      du[1] = r1 - r2 - r3;
+      du[2] = r2;
+      break;
+    }
+    case GBDE_MODEL_VDP_RING8:
+      for (int i = 0; i < 8; ++i) {
+        const double x = u[2 * i], v = u[2 * i + 1];
+        const double xl = u[2 * ((i + 7) % 8)], xr = u[2 * ((i + 1) % 8)];
+        du[2 * i] = v;
+        du[2 * i + 1] = p[0] * (1.0 - x * x) * v - x + p[1] * (xl - 2.0 * x + xr);
+      }
+      break;
+    case GBDE_MODEL_LOTKA_VOLTERRA:
+      du[0] = p[0] * u[0] - p[1] * u[0] * u[1];
+      du[1] = p[3] * u[0] * u[1] - p[2] * u[1];
+      break;
+  }
+}
+
+void noise(int id, const double* u, const double* p, double* g) {
+  if (id == GBDE_MODEL_LOTKA_VOLTERRA) {
+    g[0] = p[4] * u[0];
+    g[1] = p[4] * u[1];
+  }
+}
+
+// Jacobian by rows: J[r*n + c] = d f_r / d u_c
+void jacobian(int id, int n, const double* u, const double* p, double* J) {
+  for (int k = 0; k < n * n; ++k) J[k] = 0.0;
+  switch (id) {
+    case GBDE_MODEL_LINEAR: J[0] = p[0]; break;
+    case GBDE_MODEL_LORENZ:
+      J[0] = -p[0]; J[1] = p[0];
+      J[3] = p[1] - u[2]; J[4] = -1.0; J[5] = -u[0];
+      J[6] = u[1]; J[7] = u[0]; J[8] = -p[2];
+      break;
+    case GBDE_MODEL_ROBERTSON:
+      J[0] = -p[0]; J[1] = p[2] * u[2]; J[2] = p[2] * u[1];
+      J[3] = p[0]; J[4] = -2.0 * p[1] * u[1] - p[2] * u[2]; J[5] = -p[2] * u[1];
+      J[7] = 2.0 * p[1] * u[1];
+      break;
+    case GBDE_MODEL_VDP_RING8:
+      for (int i = 0; i < 8; ++i) {
+        const double x = u[2 * i], v = u[2 * i + 1];
+        const int r = 2 * i + 1;
+        J[(2 * i) * n + 2 * i + 1] = 1.0;
+        J[r * n + 2 * i] += -2.0 * p[0] * x * v - 1.0 - 2.0 * p[1];
+        J[r * n + 2 * i + 1] += p[0] * (1.0 - x * x);
+        J[r * n + 2 * ((i + 7) % 8)] += p[1];
+        J[r * n + 2 * ((i + 1) % 8)] += p[1];
+      }
+      break;
+    case GBDE_MODEL_LOTKA_VOLTERRA:
+      J[0] = p[0] - p[1] * u[1]; J[1] = -p[1] * u[0];
+      J[2] = p[3] * u[1]; J[3] = p[3] * u[0] - p[2];
+      break;
+  }
+}
+
+bool model_of(int id, Model& m) {
+  switch (id) {
+    case GBDE_MODEL_LINEAR: m = {id, 1, 1}; return true;
+    case GBDE_MODEL_LORENZ: m = {id, 3, 3}; return true;
+    case GBDE_MODEL_ROBERTSON: m = {id, 3, 3}; return true;
+    case GBDE_MODEL_VDP_RING8: m = {id, 16, 2}; return true;
+    case GBDE_MODEL_LOTKA_VOLTERRA: m = {id, 2, 5}; return true;
+  }
+  return false;
+}
+
+// ------------------------------------------------------ dense LU (n x n)
+struct LU {
+  int n;
+  double A[NMAX * NMAX];
+  int piv[NMAX];
+  void factor() {
+    for (int k = 0; k < n; ++k) {
+      int pk = k;
+      double best = std::fabs(A[k * n + k]);
+      for (int r = k + 1; r < n; ++r)
+        if (std::fabs(A[r * n + k]) > best) { best = std::fabs(A[r * n + k]); pk = r; }
+      piv[k] = pk;
+      if (pk != k)
+        for (int c = 0; c < n; ++c) std::swap(A[k * n + c], A[pk * n + c]);
+      for (int r = k + 1; r < n; ++r) {
+        const double l = A[r * n + k] / A[k * n + k];
+        A[r * n + k] = l;
+        for (int c = k + 1; c < n; ++c) A[r * n + c] -= l * A[k * n + c];
+      }
+    }
+  }
+  void solve(const double* b, double* x) const {
+    for (int c = 0; c < n; ++c) x[c] = b[c];
+    for (int k = 0; k < n; ++k) {
+      if (piv[k] != k) std::swap(x[k], x[piv[k]]);
+      for (int r = k + 1; r < n; ++r) x[r] -= A[r * n + k] * x[k];
+    }
+    for (int k = n - 1; k >= 0; --k) {
+      double s = x[k];
+      for (int c = k + 1; c < n; ++c) s -= A[k * n + c] * x[c];
+      x[k] = s / A[k * n + k];
+    }
+  }
+};
+
+// ---------------------------------------------------------- utilities
+double wrms(int n, const double* e, const double* u, const double* un, double at, double rt) {
+  double s = 0.0;
+  for (int c = 0; c < n; ++c) {
+    const double sc = at + rt * std::fmax(std::fabs(u[c]), std::fabs(un[c]));
+    s += (e[c] / sc) * (e[c] / sc);
+  }
+  return std::sqrt(s / n);
+}
+
+// Hairer-Norsett-Wanner I, Sec. II.4 starting step
+double init_dt(const Model& m, const double* u0, const double* f0, const double* p,
+               double tspan, int order, double at, double rt, int& nf) {
+  const int n = m.n;
+  double d0 = 0, d1 = 0;
+  for (int c = 0; c < n; ++c) {
+    const double sc = at + std::fabs(u0[c]) * rt;
+    d0 += (u0[c] / sc) * (u0[c] / sc);
+    d1 += (f0[c] / sc) * (f0[c] / sc);
+  }
+  d0 = std::sqrt(d0 / n);
+  d1 = std::sqrt(d1 / n);
+  double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
+  h0 = std::fmin(h0, tspan);
+  Vec u1, f1;
+  for (int c = 0; c < n; ++c) u1[c] = u0[c] + h0 * f0[c];
+  rhs(m.id, u1, p, f1);
+  ++nf;
+  double d2 = 0;
+  for (int c = 0; c < n; ++c) {
+    const double sc = at + std::fabs(u0[c]) * rt;
+    d2 += ((f1[c] - f0[c]) / sc) * ((f1[c] - f0[c]) / sc);
+  }
+  d2 = std::sqrt(d2 / n) / h0;
+  const double mx = std::fmax(d1, d2);
+  const double h1 = mx <= 1e-15 ? std::fmax(1e-6, h0 * 1e-3) : std::pow(0.01 / mx, 1.0 / (order + 1));
+  return std::fmin(std::fmin(100.0 * h0, h1), tspan);
+}
+
+struct Ctl {  // controller constants (gbde_opts)
+  double at, rt, qmin, qmax, gamma, beta1, beta2, qsmin, qsmax, qoldinit, dtmin, dtmax, dt0;
+  int64_t maxiters;
+  int adaptive;
+};
+
+// ---------------------------------------------------------- one trajectory
+struct Out {
+  const gbde_problem* P;
+  gbde_outputs* O;
+  int64_t i;
+  void save(int j, const double* v, int n) {
+    const size_t base = ((size_t)i * P->n_save + j) * n;
+    if (O->u_dtype == GBDE_F32)
+      for (int c = 0; c < n; ++c) ((float*)O->u)[base + c] = (float)v[c];
+    else
+      for (int c = 0; c < n; ++c) ((double*)O->u)[base + c] = v[c];
+  }
+  double ts(int j) const {
+    return P->save_kind == GBDE_SAVE_GRID ? P->saveat[j] : P->saveat[(size_t)i * P->n_save + j];
+  }
+};
+
+// Method interface for the ODE driver (virtual-free: a switch on alg).
+struct Stepper {
+  int alg, n, id;
+  const double* p;
+  double u[NMAX], un[NMAX], f0[NMAX];
+  double k[11][NMAX];  // stages (RK) or transformed stages (Rodas)
+  double J[NMAX * NMAX];
+  bool fresh, have11;
+
+  void init(const double* u0, int& nf) {
+    for (int c = 0; c < n; ++c) u[c] = u0[c];
+    rhs(id, u, p, f0);
+    ++nf;
+    fresh = false;
+    have11 = false;
+    if (alg == GBDE_ALG_RODAS5 || alg == GBDE_ALG_RODAS5P) {
+      jacobian(id, n, u, p, J);
+      fresh = true;
+    }
+  }
+
+  // ---- Tsit5 (Tsitouras 2011)
+  double tsit5(double h, const Ctl& C, int& nf) {
+    using namespace gbde::tab::tsit5;
+    const double A[7][6] = {{0},
+                            {a21},
+                            {a31, a32},
+                            {a41, a42, a43},
+                            {a51, a52, a53, a54},
+                            {a61, a62, a63, a64, a65},
+                            {a71, a72, a73, a74, a75, a76}};
+    const double bt[7] = {bt1, bt2, bt3, bt4, bt5, bt6, bt7};
+    for (int c = 0; c < n; ++c) k[0][c] = f0[c];
+    double y[NMAX];
+    for (int s = 1; s < 7; ++s) {
+      for (int c = 0; c < n; ++c) {
+        double acc = 0.0;
+        for (int j = 0; j < s; ++j) acc += A[s][j] * k[j][c];
+        y[c] = u[c] + h * acc;
+      }
+      if (s == 6)
+        for (int c = 0; c < n; ++c) un[c] = y[c];
+      rhs(id, y, p, k[s]);
+    }
+    nf += 6;
+    double e[NMAX];
+    for (int c = 0; c < n; ++c) {
+      double acc = 0.0;
+      for (int j = 0; j < 7; ++j) acc += bt[j] * k[j][c];
+      e[c] = h * acc;
+    }
+    return wrms(n, e, u, un, C.at, C.rt);
+  }
+  void tsit5_interp(double th, double h, double* out) {
+    using namespace gbde::tab::tsit5;
+    const double t2 = th * th;
+    const double b[7] = {r11 * th * (th - r12) * (t2 - r13 * th + r14),
+                         r21 * t2 * (t2 - r22 * th + r23),
+                         r31 * t2 * (t2 - r32 * th + r33),
+                         r41 * (th - r42) * (th - r43) * t2,
+                         r51 * (th - r52) * (th - r53) * t2,
+                         r61 * (th - r62) * (th - r63) * t2,
+                         r71 * (th - r72) * (th - r73) * t2};
+    for (int c = 0; c < n; ++c) {
+      double acc = 0.0;
+      for (int j = 0; j < 7; ++j) acc += b[j] * k[j][c];
+      out[c] = u[c] + h * acc;
+    }
+  }
+
+  // ---- Vern7 (Verner 2010) with the 5th-order extension over k1..k10, f(y1)
+  double vern7(double h, const Ctl& C, int& nf) {
+    using namespace gbde::tab::vern7;
+    double A[10][9] = {};
+    A[1][0] = a21;
+    A[2][0] = a31; A[2][1] = a32;
+    A[3][0] = a41; A[3][2] = a43;
+    A[4][0] = a51; A[4][2] = a53; A[4][3] = a54;
+    A[5][0] = a61; A[5][2] = a63; A[5][3] = a64; A[5][4] = a65;
+    A[6][0] = a71; A[6][2] = a73; A[6][3] = a74; A[6][4] = a75; A[6][5] = a76;
+    A[7][0] = a81; A[7][2] = a83; A[7][3] = a84; A[7][4] = a85; A[7][5] = a86; A[7][6] = a87;
+    A[8][0] = a91; A[8][2] = a93; A[8][3] = a94; A[8][4] = a95; A[8][5] = a96; A[8][6] = a97;
+    A[8][7] = a98;
+    A[9][0] = a101; A[9][2] = a103; A[9][3] = a104; A[9][4] = a105; A[9][5] = a106;
+    A[9][6] = a107;
+    const double b[10] = {b1, 0, 0, b4, b5, b6, b7, b8, b9, 0};
+    const double bh[10] = {bh1, 0, 0, bh4, bh5, bh6, bh7, 0, 0, bh10};
+    for (int c = 0; c < n; ++c) k[0][c] = f0[c];
+    double y[NMAX];
+    for (int s = 1; s < 10; ++s) {
+      for (int c = 0; c < n; ++c) {
+        double acc = 0.0;
+        for (int j = 0; j < s; ++j) acc += A[s][j] * k[j][c];
+        y[c] = u[c] + h * acc;
+      }
+      rhs(id, y, p, k[s]);
+    }
+    nf += 9;
+    double e[NMAX];
+    for (int c = 0; c < n; ++c) {
+      double a1 = 0.0, a2 = 0.0;
+      for (int j = 0; j < 10; ++j) {
+        a1 += b[j] * k[j][c];
+        a2 += (b[j] - bh[j]) * k[j][c];
+      }
+      un[c] = u[c] + h * a1;
+      e[c] = h * a2;
+    }
+    have11 = false;
+    return wrms(n, e, u, un, C.at, C.rt);
+  }
+  void vern7_interp(double th, double h, double* out, int& nf) {
+    using namespace gbde::tab::vern7d;
+    if (!have11) {
+      rhs(id, un, p, k[10]);
+      ++nf;
+      have11 = true;
+    }
+    const double B[11][5] = {{B1_1, B1_2, B1_3, B1_4, B1_5},      {B2_1, B2_2, B2_3, B2_4, B2_5},
+                             {B3_1, B3_2, B3_3, B3_4, B3_5},      {B4_1, B4_2, B4_3, B4_4, B4_5},
+                             {B5_1, B5_2, B5_3, B5_4, B5_5},      {B6_1, B6_2, B6_3, B6_4, B6_5},
+                             {B7_1, B7_2, B7_3, B7_4, B7_5},      {B8_1, B8_2, B8_3, B8_4, B8_5},
+                             {B9_1, B9_2, B9_3, B9_4, B9_5},      {B10_1, B10_2, B10_3, B10_4, B10_5},
+                             {B11_1, B11_2, B11_3, B11_4, B11_5}};
+    double w[11];
+    for (int j = 0; j < 11; ++j) {
+      double pw = th, acc = 0.0;
+      for (int q = 0; q < 5; ++q) {
+        acc += B[j][q] * pw;
+        pw *= th;
+      }
+      w[j] = acc;
+    }
+    for (int c = 0; c < n; ++c) {
+      double acc = 0.0;
+      for (int j = 0; j < 11; ++j) acc += w[j] * k[j][c];
+      out[c] = u[c] + h * acc;
+    }
+  }
+
+  // ---- Rosenbrock23 (Shampine-Reichelt 1997)
+  double ros23(double h, const Ctl& C, int& nf) {
+    using gbde::tab::ros23::d;
+    using gbde::tab::ros23::e32;
+    if (!fresh) {
+      jacobian(id, n, u, p, J);
+      fresh = true;
+    }
+    LU W;
+    W.n = n;
+    for (int r = 0; r < n; ++r)
+      for (int c = 0; c < n; ++c) W.A[r * n + c] = (r == c ? 1.0 : 0.0) - h * d * J[r * n + c];
+    W.factor();
+    double y[NMAX], F1[NMAX], r3[NMAX], k3[NMAX], tmp[NMAX];
+    W.solve(f0, k[0]);
+    for (int c = 0; c < n; ++c) y[c] = u[c] + 0.5 * h * k[0][c];
+    rhs(id, y, p, F1);
+    for (int c = 0; c < n; ++c) tmp[c] = F1[c] - k[0][c];
+    W.solve(tmp, k[1]);
+    for (int c = 0; c < n; ++c) {
+      k[1][c] += k[0][c];
+      un[c] = u[c] + h * k[1][c];
+    }
+    rhs(id, un, p, k[2]);  // F2
+    nf += 2;
+    for (int c = 0; c < n; ++c)
+      r3[c] = k[2][c] - e32 * (k[1][c] - F1[c]) - 2.0 * (k[0][c] - f0[c]);
+    W.solve(r3, k3);
+    double e[NMAX];
+    for (int c = 0; c < n; ++c) e[c] = h / 6.0 * (k[0][c] - 2.0 * k[1][c] + k3[c]);
+    return wrms(n, e, u, un, C.at, C.rt);
+  }
+  void ros23_interp(double th, double h, double* out) {
+    using gbde::tab::ros23::d;
+    const double w1 = th * (1.0 - th) / (1.0 - 2.0 * d), w2 = th * (th - 2.0 * d) / (1.0 - 2.0 * d);
+    for (int c = 0; c < n; ++c) out[c] = u[c] + h * (w1 * k[0][c] + w2 * k[1][c]);
+  }
+
+  // ---- Rodas5 / Rodas5P (transformed form, Hairer-Wanner IV.7 (7.4')):
+  //   (I/(h gamma) - J) u_i = f(y0 + sum_j a_ij u_j) + sum_j (C_ij / h) u_j
+  //   a_7j = a_6j, a_76 = 1, a_8j = a_7j, a_87 = 1; y1 = U_8 + u_8; err = u_8.
+  struct RodasTab {
+    double g, a[8][7], C[8][7], H2[7], H3[7], H4[7];
+  };
+  static const RodasTab& rodas_tab(int which) {
+    static RodasTab t5 = make_tab<5>(), t5p = make_tab<6>();
+    return which == GBDE_ALG_RODAS5 ? t5 : t5p;
+  }
+  template <int W>
+  static RodasTab make_tab() {
+    RodasTab T{};
+#define GBDE_FILL(NS, DNS)                                                                       \
+    {                                                                                            \
+      using namespace gbde::tab::NS;                                                             \
+      T.g = gbde::tab::NS::gamma;                                                                \
+      T.a[1][0] = a21;                                                                           \
+      T.a[2][0] = a31; T.a[2][1] = a32;                                                          \
+      T.a[3][0] = a41; T.a[3][1] = a42; T.a[3][2] = a43;                                         \
+      T.a[4][0] = a51; T.a[4][1] = a52; T.a[4][2] = a53; T.a[4][3] = a54;                        \
+      T.a[5][0] = a61; T.a[5][1] = a62; T.a[5][2] = a63; T.a[5][3] = a64; T.a[5][4] = a65;       \
+      T.C[1][0] = C21;                                                                           \
+      T.C[2][0] = C31; T.C[2][1] = C32;                                                          \
+      T.C[3][0] = C41; T.C[3][1] = C42; T.C[3][2] = C43;                                         \
+      T.C[4][0] = C51; T.C[4][1] = C52; T.C[4][2] = C53; T.C[4][3] = C54;                        \
+      T.C[5][0] = C61; T.C[5][1] = C62; T.C[5][2] = C63; T.C[5][3] = C64; T.C[5][4] = C65;       \
+      T.C[6][0] = C71; T.C[6][1] = C72; T.C[6][2] = C73; T.C[6][3] = C74; T.C[6][4] = C75;       \
+      T.C[6][5] = C76;                                                                           \
+      T.C[7][0] = C81; T.C[7][1] = C82; T.C[7][2] = C83; T.C[7][3] = C84; T.C[7][4] = C85;       \
+      T.C[7][5] = C86; T.C[7][6] = C87;                                                          \
+    }                                                                                            \
+    {                                                                                            \
+      using namespace gbde::tab::DNS;                                                            \
+      const double h2[7] = {H2_1, H2_2, H2_3, H2_4, H2_5, H2_6, H2_7};                           \
+      const double h3[7] = {H3_1, H3_2, H3_3, H3_4, H3_5, H3_6, H3_7};                           \
+      const double h4[7] = {H4_1, H4_2, H4_3, H4_4, H4_5, H4_6, H4_7};                           \
+      for (int j = 0; j < 7; ++j) { T.H2[j] = h2[j]; T.H3[j] = h3[j]; T.H4[j] = h4[j]; }         \
+    }
+    if (W == 5) {
+      GBDE_FILL(rodas5, rodas5d)
+    } else {
+      GBDE_FILL(rodas5p, rodas5pd)
+    }
+#undef GBDE_FILL
+    for (int j = 0; j < 5; ++j) T.a[6][j] = T.a[5][j];
+    T.a[6][5] = 1.0;
+    for (int j = 0; j < 6; ++j) T.a[7][j] = T.a[6][j];
+    T.a[7][6] = 1.0;
+    return T;
+  }
+
+  double rodas(double h, const Ctl& C, int& nf) {
+    const RodasTab& T = rodas_tab(alg);
+    if (!fresh) {
+      rhs(id, u, p, f0);
+      ++nf;
+      jacobian(id, n, u, p, J);
+      fresh = true;
+    }
+    LU W;
+    W.n = n;
+    for (int r = 0; r < n; ++r)
+      for (int c = 0; c < n; ++c)
+        W.A[r * n + c] = (r == c ? 1.0 / (h * T.g) : 0.0) - J[r * n + c];
+    W.factor();
+    double y[NMAX], fy[NMAX], rr[NMAX];
+    W.solve(f0, k[0]);
+    for (int s = 1; s < 8; ++s) {
+      for (int c = 0; c < n; ++c) {
+        double acc = u[c];
+        for (int j = 0; j < s; ++j) acc += T.a[s][j] * k[j][c];
+        y[c] = acc;
+      }
+      rhs(id, y, p, fy);
+      for (int c = 0; c < n; ++c) {
+        double acc = fy[c];
+        for (int j = 0; j < s; ++j) acc += (T.C[s][j] / h) * k[j][c];
+        rr[c] = acc;
+      }
+      W.solve(rr, k[s]);
+    }
+    nf += 7;
+    for (int c = 0; c < n; ++c) un[c] = y[c] + k[7][c];
+    return wrms(n, k[7], u, un, C.at, C.rt);
+  }
+  void rodas_interp(double th, double* out) {
+    const RodasTab& T = rodas_tab(alg);
+    for (int c = 0; c < n; ++c) {
+      double k2 = 0, k3 = 0, k4 = 0;
+      for (int j = 0; j < 7; ++j) {
+        k2 += T.H2[j] * k[j][c];
+        k3 += T.H3[j] * k[j][c];
+        k4 += T.H4[j] * k[j][c];
+      }
+      out[c] = (1.0 - th) * u[c] + th * un[c] + th * (1.0 - th) * (k2 + th * (k3 + th * k4));
+    }
+  }
+
+  double attempt(double h, const Ctl& C, int& nf) {
+    switch (alg) {
+      case GBDE_ALG_TSIT5: return tsit5(h, C, nf);
+      case GBDE_ALG_VERN7: return vern7(h, C, nf);
+      case GBDE_ALG_ROSENBROCK23: return ros23(h, C, nf);
+      default: return rodas(h, C, nf);
+    }
+  }
+  void interp(double th, double h, double* out, int& nf) {
+    switch (alg) {
+      case GBDE_ALG_TSIT5: tsit5_interp(th, h, out); break;
+      case GBDE_ALG_VERN7: vern7_interp(th, h, out, nf); break;
+      case GBDE_ALG_ROSENBROCK23: ros23_interp(th, h, out); break;
+      default: rodas_interp(th, out); break;
+    }
+  }
+  void accept(int& nf) {
+    for (int c = 0; c < n; ++c) u[c] = un[c];
+    if (alg == GBDE_ALG_TSIT5) {
+      for (int c = 0; c < n; ++c) f0[c] = k[6][c];
+    } else if (alg == GBDE_ALG_VERN7) {
+      if (have11) for (int c = 0; c < n; ++c) f0[c] = k[10][c];
+      else { rhs(id, u, p, f0); ++nf; }
+      have11 = false;
+    } else if (alg == GBDE_ALG_ROSENBROCK23) {
+      for (int c = 0; c < n; ++c) f0[c] = k[2][c];
+      fresh = false;
+    } else {
+      fresh = false;
+    }
+  }
+  int order() const {
+    switch (alg) {
+      case GBDE_ALG_TSIT5: return 5;
+      case GBDE_ALG_VERN7: return 7;
+      case GBDE_ALG_ROSENBROCK23: return 2;
+      default: return 4;
+    }
+  }
+};
+
+
+// ------------------------------------------------------------ ODE driver
+// One trajectory: PI controller (HNW I, II.4; Gustafsson), scaled RMS norm,
+// HNW starting step, dense output at save times, tf snapping, return codes.
+void solve_ode_traj(const Model& m, int alg, const Ctl& C, Out& o) {
+  const gbde_problem* P = o.P;
+  const int64_t i = o.i;
+  const int n = m.n;
+  const double* p = P->p + (size_t)i * m.np;
+  const double* u0 = P->u0 + (size_t)i * n;
+  double t = P->t0[i];
+  const double tf = P->tf[i];
+  int js = 0, nacc = 0, nrej = 0, nf = 0;
+  int64_t iters = 0;
+  int ret = GBDE_RET_DEFAULT;
+  while (js < P->n_save && o.ts(js) <= t) o.save(js++, u0, n);
+  bool bad = !(tf >= t) || !std::isfinite(t) || !std::isfinite(tf);
+  for (int c = 0; c < n; ++c) bad |= !std::isfinite(u0[c]);
+  Stepper S;
+  S.alg = alg;
+  S.n = n;
+  S.id = m.id;
+  S.p = p;
+  double dt = 0.0, qold = C.qoldinit;
+  if (bad) {
+    ret = GBDE_RET_INITIALFAILURE;
+  } else {
+    S.init(u0, nf);
+    if (C.dt0 > 0.0 || !C.adaptive) dt = C.dt0;
+    else dt = init_dt(m, S.u, S.f0, p, tf - t, S.order(), C.at, C.rt, nf);
+    if (C.dtmax > 0.0) dt = std::fmin(dt, C.dtmax);
+    if (!(t < tf)) ret = GBDE_RET_SUCCESS;
+    else if (!(dt > 0.0)) ret = GBDE_RET_DTLESSTHANMIN;
+  }
+  while (ret == GBDE_RET_DEFAULT) {
+    const double rem = tf - t;
+    double h = dt;
+    bool last = false;
+    if (h * (1.0 + 1e-10) >= rem) {
+      h = rem;
+      last = true;
+    }
+    const double E = S.attempt(h, C, nf);
+    ++iters;
+    if (!C.adaptive || E <= 1.0) {
+      double dtnew = h;
+      if (C.adaptive) {
+        const double q11 = std::pow(E, C.beta1);
+        double q = q11 / std::pow(qold, C.beta2);
+        q = std::fmax(1.0 / C.qmax, std::fmin(1.0 / C.qmin, q / C.gamma));
+        if (q >= C.qsmin && q <= C.qsmax) q = 1.0;
+        dtnew = h / q;
+        qold = std::fmax(E, C.qoldinit);
+      }
+      const double tnew = last ? tf : t + h;
+      while (js < P->n_save) {
+        const double ts = o.ts(js);
+        if (!(ts <= tnew)) break;
+        if (ts >= tnew) {
+          o.save(js, S.un, n);
+        } else {
+          double tmp[NMAX];
+          S.interp((ts - t) / h, h, tmp, nf);
+          o.save(js, tmp, n);
+        }
+        ++js;
+      }
+      S.accept(nf);
+      t = tnew;
+      ++nacc;
+      bool fin = true;
+      for (int c = 0; c < n; ++c) fin &= std::isfinite(S.u[c]);
+      if (!fin) ret = GBDE_RET_UNSTABLE;
+      else if (last) ret = GBDE_RET_SUCCESS;
+      dt = C.dtmax > 0.0 ? std::fmin(dtnew, C.dtmax) : dtnew;
+    } else {
+      ++nrej;
+      dt = std::isfinite(E) ? h / std::fmin(1.0 / C.qmin, std::pow(E, C.beta1) / C.gamma)
+                            : h * C.qmin;
+    }
+    if (ret == GBDE_RET_DEFAULT) {
+      if (iters >= C.maxiters) ret = GBDE_RET_MAXITERS;
+      else if (C.adaptive && (dt < C.dtmin || dt <= 4.0 * 2.220446049250313e-16 * std::fabs(t)))
+        ret = GBDE_RET_DTLESSTHANMIN;
+    }
+  }
+  double nanv[NMAX];
+  for (int c = 0; c < n; ++c) nanv[c] = NAN;
+  for (; js < P->n_save; ++js) o.save(js, nanv, n);
+  gbde_outputs* O = o.O;
+  O->retcode[i] = ret;
+  if (O->naccept) O->naccept[i] = nacc;
+  if (O->nreject) O->nreject[i] = nrej;
+  if (O->nf) O->nf[i] = nf;
+  if (O->t_end) O->t_end[i] = t;
+  if (O->method) O->method[i] = alg;
+}
+
+// ------------------------------------------------- Philox4x32-10 + normals
+// Salmon et al., SC'11.  Counter (block_lo, block_hi, traj_lo, traj_hi), key
+// (seed_lo, seed_hi).  Box-Muller with series log / sin / cos evaluated with
+// explicit fma (compiled with -ffp-contract=off so no other contraction).
+void philox(const uint32_t in[4], uint32_t k0, uint32_t k1, uint32_t out[4]) {
+  uint32_t c0 = in[0], c1 = in[1], c2 = in[2], c3 = in[3];
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n1 = (uint32_t)p1;
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1, n3 = (uint32_t)p0;
+    c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+template <class T> T fma_t(T a, T b, T c);
+template <> double fma_t(double a, double b, double c) { return std::fma(a, b, c); }
+template <> float fma_t(float a, float b, float c) { return std::fmaf(a, b, c); }
+
+// log x = e ln2 + 2 atanh((m-1)/(m+1)), m in [1/sqrt2, sqrt2)
+template <class T>
+T series_log(T x, int nterms, T ln2hi, T ln2lo, T sqrth) {
+  int e;
+  T m = std::frexp(x, &e);
+  if (m < sqrth) { m = m + m; e -= 1; }
+  const T s = (m - T(1)) / (m + T(1));
+  const T s2 = s * s;
+  T acc = T(1) / T(2 * nterms + 1);
+  for (int k = nterms - 1; k >= 0; --k) acc = fma_t<T>(acc, s2, T(1) / T(2 * k + 1));
+  const T lm = (s + s) * acc;
+  const T fe = (T)e;
+  return fma_t<T>(fe, ln2hi, lm) + fe * ln2lo;
+}
+
+template <class T>
+void series_sincos2pi(T u, int nterms, T pio2hi, T pio2lo, T& co, T& si) {
+  const T v = u * T(4);
+  const T qf = std::floor(v);
+  T f = v - qf;
+  int q = (int)qf;
+  if (f > T(0.5)) { f = f - T(1); q += 1; }
+  q &= 3;
+  const T r = fma_t<T>(f, pio2hi, f * pio2lo);
+  const T r2 = r * r;
+  std::vector<T> sc(nterms + 1), cc(nterms + 1);
+  T fs = 1, fc = 1;
+  for (int k = 0; k <= nterms; ++k) {
+    sc[k] = ((k & 1) ? T(-1) : T(1)) / fs;
+    cc[k] = ((k & 1) ? T(-1) : T(1)) / fc;
+    fs = fs * T((2 * k + 2) * (2 * k + 3));
+    fc = fc * T((2 * k + 1) * (2 * k + 2));
+  }
+  T sp = sc[nterms], cp = cc[nterms];
+  for (int k = nterms - 1; k >= 0; --k) {
+    sp = fma_t<T>(sp, r2, sc[k]);
+    cp = fma_t<T>(cp, r2, cc[k]);
+  }
+  const T sr = r * sp, cr = cp;
+  switch (q) {
+    case 0: co = cr; si = sr; break;
+    case 1: co = -sr; si = cr; break;
+    case 2: co = -cr; si = -sr; break;
+    default: co = sr; si = -cr; break;
+  }
+}
+
+void normal_pair_f64(uint64_t seed, uint64_t traj, uint64_t b, double& z0, double& z1) {
+  const uint32_t ctr[4] = {(uint32_t)b, (uint32_t)(b >> 32), (uint32_t)traj, (uint32_t)(traj >> 32)};
+  uint32_t r[4];
+  philox(ctr, (uint32_t)seed, (uint32_t)(seed >> 32), r);
+  const uint64_t a = ((uint64_t)(r[0] >> 5) << 26) | (r[1] >> 6);
+  const uint64_t c = ((uint64_t)(r[2] >> 5) << 26) | (r[3] >> 6);
+  const double u1 = ((double)a + 0.5) * 0x1p-53, u2 = (double)c * 0x1p-53;
+  const double rad = std::sqrt(-2.0 * series_log<double>(u1, 12, 0.6931471805599453,
+                                                          2.3190468138462996e-17,
+                                                          0.7071067811865476));
+  double co, si;
+  series_sincos2pi<double>(u2, 9, 1.5707963267948966, 6.123233995736766e-17, co, si);
+  z0 = rad * co;
+  z1 = rad * si;
+}
+
+void normal_quad_f32(uint64_t seed, uint64_t traj, uint64_t b, float* z) {
+  const uint32_t ctr[4] = {(uint32_t)b, (uint32_t)(b >> 32), (uint32_t)traj, (uint32_t)(traj >> 32)};
+  uint32_t r[4];
+  philox(ctr, (uint32_t)seed, (uint32_t)(seed >> 32), r);
+  float u[4];
+  for (int k = 0; k < 4; ++k) u[k] = (float)(r[k] >> 8) * 0x1p-24f;
+  u[0] = ((float)(r[0] >> 8) + 0.5f) * 0x1p-24f;
+  u[2] = ((float)(r[2] >> 8) + 0.5f) * 0x1p-24f;
+  for (int k = 0; k < 2; ++k) {
+    const float rad = std::sqrt(-2.0f * series_log<float>(u[2 * k], 6, 0.693147182f,
+                                                           -1.90465421e-09f, 0.707106781f));
+    float co, si;
+    series_sincos2pi<float>(u[2 * k + 1], 5, 1.57079637f, -4.37113883e-08f, co, si);
+    z[2 * k] = rad * co;
+    z[2 * k + 1] = rad * si;
+  }
+}
+
+// Per-trajectory normal stream; f32 = 1 reads the FP32 stream (promoted).
+struct Normals {
+  uint64_t seed, traj, d = 0, blk = ~0ull;
+  int f32;
+  double buf[4];
+  double next() {
+    const int per = f32 ? 4 : 2;
+    const uint64_t b = d / per;
+    if (b != blk) {
+      if (f32) {
+        float z[4];
+        normal_quad_f32(seed, traj, b, z);
+        for (int k = 0; k < 4; ++k) buf[k] = z[k];
+      } else {
+        normal_pair_f64(seed, traj, b, buf[0], buf[1]);
+      }
+      blk = b;
+    }
+    return buf[d++ % per];
+  }
+};
+
+// ------------------------------------------------------------ SDE drivers
+void finish(Out& o, int n, int js, int ret, int nacc, int nrej, int nf, double t, int alg) {
+  double nanv[NMAX];
+  for (int c = 0; c < n; ++c) nanv[c] = NAN;
+  for (; js < o.P->n_save; ++js) o.save(js, nanv, n);
+  gbde_outputs* O = o.O;
+  O->retcode[o.i] = ret;
+  if (O->naccept) O->naccept[o.i] = nacc;
+  if (O->nreject) O->nreject[o.i] = nrej;
+  if (O->nf) O->nf[o.i] = nf;
+  if (O->t_end) O->t_end[o.i] = t;
+  if (O->method) O->method[o.i] = alg;
+}
+
+// Euler-Maruyama (Kloeden-Platen): step n spans [t0 + n h, min(t0 + (n+1) h, tf)],
+// normal n*N + c drives component c; linear interpolation at save times.
+void solve_em_traj(const Model& m, const Ctl& C, uint64_t seed, int f32, Out& o) {
+  const gbde_problem* P = o.P;
+  const int64_t i = o.i;
+  const int n = m.n;
+  const double* p = P->p + (size_t)i * m.np;
+  double u[NMAX];
+  for (int c = 0; c < n; ++c) u[c] = P->u0[(size_t)i * n + c];
+  const double t0 = P->t0[i], tf = P->tf[i], h = C.dt0;
+  int js = 0;
+  while (js < P->n_save && o.ts(js) <= t0) o.save(js++, u, n);
+  bool bad = !(tf >= t0) || !std::isfinite(t0) || !std::isfinite(tf);
+  for (int c = 0; c < n; ++c) bad |= !std::isfinite(u[c]);
+  if (bad) return finish(o, n, js, GBDE_RET_INITIALFAILURE, 0, 0, 0, t0, GBDE_ALG_EM);
+  Normals z{seed, (uint64_t)i};
+  z.f32 = f32;
+  int ret = GBDE_RET_SUCCESS;
+  int64_t k = 0;
+  double t = t0;
+  while (t < tf) {
+    if (k >= C.maxiters) { ret = GBDE_RET_MAXITERS; break; }
+    double tn1 = t0 + (double)(k + 1) * h;
+    if (tn1 * (1.0 + 1e-14) >= tf || tn1 > tf) tn1 = tf;
+    const double hs = tn1 - t, sq = std::sqrt(hs);
+    double fu[NMAX], gu[NMAX], un[NMAX];
+    rhs(m.id, u, p, fu);
+    noise(m.id, u, p, gu);
+    for (int c = 0; c < n; ++c) un[c] = u[c] + fu[c] * hs + gu[c] * (sq * z.next());
+    while (js < P->n_save) {
+      const double ts = o.ts(js);
+      if (!(ts <= tn1)) break;
+      if (ts >= tn1) o.save(js, un, n);
+      else {
+        const double th = (ts - t) / hs;
+        double tmp[NMAX];
+        for (int c = 0; c < n; ++c) tmp[c] = u[c] + th * (un[c] - u[c]);
+        o.save(js, tmp, n);
+      }
+      ++js;
+    }
+    bool fin = true;
+    for (int c = 0; c < n; ++c) { u[c] = un[c]; fin &= std::isfinite(un[c]); }
+    t = tn1;
+    ++k;
+    if (!fin) { ret = GBDE_RET_UNSTABLE; break; }
+  }
+  finish(o, n, js, ret, (int)k, 0, (int)(2 * k), t, GBDE_ALG_EM);
+}
+
+// SRIW1 (Roessler 2010) with rejection sampling with memory (Rackauckas &
+// Nie 2017): future Brownian pieces on a stack (nearest on top), split by a
+// Brownian bridge when longer than needed; 8 entries, the two farthest
+// pieces merge when full.
+struct Piece {
+  double dt, W[NMAX], Z[NMAX];
+};
+
+void solve_sri_traj(const Model& m, const Ctl& C, uint64_t seed, int f32, Out& o) {
+  using namespace gbde::tab::sriw1;
+  const double al[2] = {al1, al2};
+  const double b1[4] = {b1_1, b1_2, b1_3, b1_4};
+  const double b2[4] = {b2_1, b2_2, b2_3, b2_4};
+  const double b3[4] = {b3_1, b3_2, b3_3, b3_4};
+  const double b4[4] = {b4_1, b4_2, b4_3, b4_4};
+  const gbde_problem* P = o.P;
+  const int64_t i = o.i;
+  const int n = m.n;
+  const double* p = P->p + (size_t)i * m.np;
+  double u[NMAX];
+  for (int c = 0; c < n; ++c) u[c] = P->u0[(size_t)i * n + c];
+  const double t0 = P->t0[i], tf = P->tf[i];
+  int js = 0;
+  while (js < P->n_save && o.ts(js) <= t0) o.save(js++, u, n);
+  bool bad = !(tf >= t0) || !std::isfinite(t0) || !std::isfinite(tf);
+  for (int c = 0; c < n; ++c) bad |= !std::isfinite(u[c]);
+  if (bad) return finish(o, n, js, GBDE_RET_INITIALFAILURE, 0, 0, 0, t0, GBDE_ALG_SOSRI);
+  Normals z{seed, (uint64_t)i};
+  z.f32 = f32;
+  Piece stk[8];
+  int sp = 0;
+  int nf = 0, nacc = 0, nrej = 0;
+  double t = t0, h;
+  if (C.dt0 > 0.0) h = C.dt0;
+  else {
+    double f0[NMAX];
+    rhs(m.id, u, p, f0);
+    ++nf;
+    h = init_dt(m, u, f0, p, tf - t0, 1, C.at, C.rt, nf);
+  }
+  if (C.dtmax > 0.0) h = std::fmin(h, C.dtmax);
+  int ret = t < tf ? GBDE_RET_DEFAULT : GBDE_RET_SUCCESS;
+  int64_t iters = 0;
+  while (ret == GBDE_RET_DEFAULT) {
+    const double rem = tf - t;
+    double hs = h;
+    bool last = false;
+    if (hs * (1.0 + 1e-10) >= rem) { hs = rem; last = true; }
+    // increments over [t, t + hs]
+    double dW[NMAX] = {0}, dZ[NMAX] = {0}, acc = 0.0;
+    while (true) {
+      const double r = hs - acc;
+      if (!(r > 1e-14 * hs)) break;
+      if (sp > 0) {
+        Piece& top = stk[sp - 1];
+        if (top.dt <= r * (1.0 + 1e-12)) {
+          acc += top.dt;
+          for (int c = 0; c < n; ++c) { dW[c] += top.W[c]; dZ[c] += top.Z[c]; }
+          --sp;
+        } else {
+          const double frac = r / top.dt, sd = std::sqrt(r * (top.dt - r) / top.dt);
+          for (int c = 0; c < n; ++c) {
+            const double wr = top.W[c] * frac + sd * z.next();
+            const double zr = top.Z[c] * frac + sd * z.next();
+            dW[c] += wr; dZ[c] += zr;
+            top.W[c] -= wr; top.Z[c] -= zr;
+          }
+          top.dt -= r;
+          acc = hs;
+        }
+      } else {
+        const double sq = std::sqrt(r);
+        for (int c = 0; c < n; ++c) {
+          dW[c] += sq * z.next();
+          dZ[c] += sq * z.next();
+        }
+        acc = hs;
+      }
+    }
+    const double sqh = std::sqrt(hs), ih = 1.0 / hs, isqh = 1.0 / std::sqrt(hs);
+    double I10[NMAX], I11[NMAX], I111[NMAX];
+    for (int c = 0; c < n; ++c) {
+      I10[c] = 0.5 * hs * (dW[c] + dZ[c] * 0.57735026918962576451);
+      I11[c] = 0.5 * (dW[c] * dW[c] - hs);
+      I111[c] = (dW[c] * dW[c] * dW[c] - 3.0 * hs * dW[c]) * (1.0 / 6.0);
+    }
+    double F1[NMAX], F2[NMAX], G[4][NMAX], Y[NMAX], un[NMAX], err[NMAX];
+    rhs(m.id, u, p, F1);
+    noise(m.id, u, p, G[0]);
+    for (int c = 0; c < n; ++c) Y[c] = u[c] + A0_21 * F1[c] * hs + B0_21 * G[0][c] * I10[c] * ih;
+    rhs(m.id, Y, p, F2);
+    for (int c = 0; c < n; ++c) Y[c] = u[c] + A1_21 * F1[c] * hs + B1_21 * G[0][c] * sqh;
+    noise(m.id, Y, p, G[1]);
+    for (int c = 0; c < n; ++c) Y[c] = u[c] + A1_31 * F1[c] * hs + B1_31 * G[0][c] * sqh;
+    noise(m.id, Y, p, G[2]);
+    for (int c = 0; c < n; ++c)
+      Y[c] = u[c] + A1_43 * F1[c] * hs + (B1_41 * G[0][c] + B1_42 * G[1][c] + B1_43 * G[2][c]) * sqh;
+    noise(m.id, Y, p, G[3]);
+    nf += 2;
+    for (int c = 0; c < n; ++c) {
+      double sto = 0.0, en3 = 0.0, en4 = 0.0;
+      for (int s = 0; s < 4; ++s) {
+        sto += (b1[s] * dW[c] + b2[s] * I11[c] * isqh + b3[s] * I10[c] * ih + b4[s] * I111[c] * ih) * G[s][c];
+        en3 += b3[s] * G[s][c];
+        en4 += b4[s] * G[s][c];
+      }
+      un[c] = u[c] + hs * (al[0] * F1[c] + al[1] * F2[c]) + sto;
+      const double ed = hs * ((al[0] - 1.0) * F1[c] + al[1] * F2[c]);
+      const double en = en3 * I10[c] * ih + en4 * I111[c] * ih;
+      err[c] = std::fabs(ed) + std::fabs(en);
+    }
+    const double E = wrms(n, err, u, un, C.at, C.rt);
+    ++iters;
+    if (!C.adaptive || E <= 1.0) {
+      const double tnew = last ? tf : t + hs;
+      while (js < P->n_save) {
+        const double ts = o.ts(js);
+        if (!(ts <= tnew)) break;
+        if (ts >= tnew) o.save(js, un, n);
+        else {
+          const double th = (ts - t) / hs;
+          double tmp[NMAX];
+          for (int c = 0; c < n; ++c) tmp[c] = u[c] + th * (un[c] - u[c]);
+          o.save(js, tmp, n);
+        }
+        ++js;
+      }
+      bool fin = true;
+      for (int c = 0; c < n; ++c) { u[c] = un[c]; fin &= std::isfinite(un[c]); }
+      t = tnew;
+      ++nacc;
+      if (!fin) ret = GBDE_RET_UNSTABLE;
+      else if (last) ret = GBDE_RET_SUCCESS;
+      if (C.adaptive) {
+        double q = std::pow(E, C.beta1);
+        q = std::fmax(1.0 / C.qmax, std::fmin(1.0 / C.qmin, q / C.gamma));
+        h = hs / q;
+      }
+    } else {
+      ++nrej;
+      if (sp == 8) {  // merge the two farthest pieces
+        stk[0].dt += stk[1].dt;
+        for (int c = 0; c < n; ++c) { stk[0].W[c] += stk[1].W[c]; stk[0].Z[c] += stk[1].Z[c]; }
+        for (int k = 1; k < 7; ++k) stk[k] = stk[k + 1];
+        sp = 7;
+      }
+      stk[sp].dt = hs;
+      for (int c = 0; c < n; ++c) { stk[sp].W[c] = dW[c]; stk[sp].Z[c] = dZ[c]; }
+      ++sp;
+      h = std::isfinite(E) ? hs / std::fmin(1.0 / C.qmin, std::pow(E, C.beta1) / C.gamma) : hs * C.qmin;
+    }
+    if (C.dtmax > 0.0) h = std::fmin(h, C.dtmax);
+    if (ret == GBDE_RET_DEFAULT) {
+      if (iters >= C.maxiters) ret = GBDE_RET_MAXITERS;
+      else if (C.adaptive && (h < C.dtmin || h <= 4.0 * 2.220446049250313e-16 * std::fabs(t)))
+        ret = GBDE_RET_DTLESSTHANMIN;
+    }
+  }
+  finish(o, n, js, ret, nacc, nrej, nf, t, GBDE_ALG_SOSRI);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------- C entry
+extern "C" {
+
+// Solve the ensemble on the CPU in FP64 with `nthreads` std::threads
+// (EnsembleThreads-equivalent; nthreads <= 1 runs serially, EnsembleSerial).
+// Same structs as gbde_ensemble_solve; host pointers only.  noise_f32 = 1
+// drives the SDE methods with the FP32 normal stream (promoted to FP64), the
+// stream the mixed-precision GPU path draws.
+int oracle_ensemble_solve(const gbde_problem* P, const gbde_opts* O, gbde_outputs* out,
+                          int nthreads, int noise_f32) {
+  Model m;
+  if (!P || !O || !out || !model_of(P->model, m)) return GBDE_ERR_INVALID;
+  if (P->n_state != m.n || P->n_param != m.np || P->mem != GBDE_MEM_HOST) return GBDE_ERR_INVALID;
+  Ctl C{O->abstol, O->reltol, O->qmin, O->qmax, O->gamma, O->beta1, O->beta2, O->qsteady_min,
+        O->qsteady_max, O->qoldinit, O->dtmin, O->dtmax, O->dt, O->maxiters, O->adaptive};
+  const int alg = O->alg;
+  const int64_t N = P->n_traj;
+  std::atomic<int64_t> next{0};
+  auto work = [&]() {
+    const int64_t chunk = 64;
+    while (true) {
+      const int64_t b = next.fetch_add(chunk);
+      if (b >= N) break;
+      const int64_t e = b + chunk < N ? b + chunk : N;
+      for (int64_t i = b; i < e; ++i) {
+        Out o{P, out, i};
+        if (alg == GBDE_ALG_EM) solve_em_traj(m, C, O->seed, noise_f32, o);
+        else if (alg == GBDE_ALG_SOSRI) solve_sri_traj(m, C, O->seed, noise_f32, o);
+        else solve_ode_traj(m, alg, C, o);
+      }
+    }
+  };
+  if (nthreads <= 1) {
+    work();
+  } else {
+    std::vector<std::thread> pool;
+    for (int k = 0; k < nthreads; ++k) pool.emplace_back(work);
+    for (auto& th : pool) th.join();
+  }
+  return GBDE_OK;
+}
+
+void oracle_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  philox(ctr, key[0], key[1], out);
+}
+
+void oracle_normals(uint64_t seed, uint64_t traj, uint64_t counter, int64_t n, int f32,
+                    double* out) {
+  Normals z{seed, traj};
+  z.f32 = f32;
+  z.d = counter;
+  for (int64_t k = 0; k < n; ++k) out[k] = z.next();
+}
+
+int oracle_hardware_threads(void) {
+  const unsigned h = std::thread::hardware_concurrency();
+  return h ? (int)h : 1;
+}
+
+}  // extern "C"

@@ -1,0 +1,327 @@
+"""GPU parity: every kernel through the C ABI against the CPU FP64 oracle on
+identical seeded inputs.
+
+Tolerances: adaptive methods pass when the weighted error
+max |u - u*| / (abstol + reltol |u*|) against the oracle (same algorithm,
+same tolerances) is <= 10; FP64 runs are held to <= 1 (they differ from the
+oracle only by FMA contraction).  Fixed-step EM in FP64 on identical noise is
+held to 1e-12 relative."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def make_inputs(de, model, N, rng, tf=None):
+    if model is de.models.lorenz:
+        p = np.array([10.0, 28.0, 8.0 / 3.0]) * rng.uniform(0.9, 1.1, (N, 3))
+        u0 = np.tile([1.0, 0.0, 0.0], (N, 1))
+        tf = np.ones(N) if tf is None else tf
+    elif model is de.models.robertson:
+        p = np.array([0.04, 3e7, 1e4]) * 10 ** rng.uniform(-1, 1, (N, 3))
+        u0 = np.tile([1.0, 0.0, 0.0], (N, 1))
+        tf = 10 ** rng.uniform(1, 5, N) if tf is None else tf
+    elif model is de.models.linear:
+        p = rng.uniform(0.5, 1.5, (N, 1))
+        u0 = rng.uniform(0.1, 1.0, (N, 1))
+        tf = np.ones(N) if tf is None else tf
+    elif model is de.models.lotka_volterra:
+        p = np.array([1.5, 1.0, 3.0, 1.0, 0.1]) * np.c_[rng.uniform(0.8, 1.2, (N, 4)), np.ones(N)]
+        u0 = np.ones((N, 2))
+        tf = np.full(N, 10.0) if tf is None else tf
+    elif model is de.models.vdp_ring8:
+        p = np.c_[10 ** rng.uniform(-1, 3, N), np.full(N, 0.05)]
+        u0 = rng.uniform(-2, 2, (N, 16))
+        tf = np.full(N, 20.0) if tf is None else tf
+    return p, u0, np.zeros(N), np.asarray(tf, float)
+
+
+def run_both(de, oracle, model, alg_id, p, u0, t0, tf, saveat, save_kind, precision="fp64",
+             batching="plain", noise_f32=False, u_dtype="f64", **kw):
+    capi = de._capi
+    opts = capi.opts_default(alg_id)
+    for k, v in kw.items():
+        setattr(opts, k, v)
+    opts_gpu = capi.opts_default(alg_id)
+    for k, v in kw.items():
+        setattr(opts_gpu, k, v)
+    opts_gpu.precision = capi.PREC_MIXED if precision == "mixed" else capi.PREC_FP64
+    opts_gpu.batching = capi.BATCH_PERSISTENT if batching == "persistent" else capi.BATCH_PLAIN
+    g = de.solve_arrays(model, opts_gpu, p, u0, t0, tf, saveat, save_kind, u_dtype=u_dtype)
+    r = oracle.solve(capi, model, opts, p, u0, t0, tf, saveat, save_kind, nthreads=8,
+                     noise_f32=noise_f32)
+    return g, r, opts
+
+
+ODE_CASES = [
+    ("lorenz", "TSIT5", 1e-8, 1e-8), ("lorenz", "VERN7", 1e-8, 1e-8),
+    ("linear", "TSIT5", 1e-8, 1e-8), ("linear", "VERN7", 1e-10, 1e-10),
+    ("robertson", "ROSENBROCK23", 1e-6, 1e-10), ("robertson", "RODAS5", 1e-6, 1e-10),
+    ("robertson", "RODAS5P", 1e-6, 1e-10), ("lorenz", "RODAS5", 1e-7, 1e-7),
+    ("linear", "RODAS5P", 1e-8, 1e-8),
+]
+
+
+@pytest.mark.parametrize("model_name,alg,rt,at", ODE_CASES)
+def test_ode_fp64_parity(de, oracle, rng, model_name, alg, rt, at):
+    capi = de._capi
+    model = getattr(de.models, model_name)
+    N = 777
+    p, u0, t0, tf = make_inputs(de, model, N, rng)
+    if model_name == "robertson":
+        saveat = tf[:, None] * 10 ** (-5 + 5 * np.arange(20) / 19)
+        kind = capi.SAVE_PER_TRAJ
+    else:
+        saveat = de.save_grid(0.0, 1.0, 0.1)
+        kind = capi.SAVE_GRID
+    g, r, _ = run_both(de, oracle, model, getattr(capi, "ALG_" + alg), p, u0, t0, tf, saveat,
+                       kind, reltol=rt, abstol=at)
+    assert np.array_equal(g["retcode"], r["retcode"])
+    assert np.all(g["retcode"] == capi.RET_SUCCESS)
+    err = oracle.weighted_error(g["u"], r["u"], at, rt)
+    assert err <= 1.0, err
+    # step statistics agree except for rare FMA-rounding-induced differences
+    assert np.mean(g["naccept"] == r["naccept"]) > 0.95
+    # first save point is u0 exactly
+    assert np.array_equal(g["u"][:, 0, :], u0) or kind == capi.SAVE_PER_TRAJ
+
+
+@pytest.mark.parametrize("alg", ["TSIT5", "RODAS5"])
+def test_persistent_is_bitwise_plain(de, oracle, rng, alg):
+    capi = de._capi
+    model = de.models.robertson if alg == "RODAS5" else de.models.lorenz
+    N = 5000
+    p, u0, t0, tf = make_inputs(de, model, N, rng)
+    saveat = tf[:, None] * np.linspace(0.1, 1.0, 10)
+    outs = []
+    for b in ("plain", "persistent"):
+        opts = capi.opts_default(getattr(capi, "ALG_" + alg))
+        opts.reltol, opts.abstol = (1e-6, 1e-10) if alg == "RODAS5" else (1e-8, 1e-8)
+        opts.batching = capi.BATCH_PERSISTENT if b == "persistent" else capi.BATCH_PLAIN
+        outs.append(de.solve_arrays(model, opts, p, u0, t0, tf, saveat, capi.SAVE_PER_TRAJ))
+    assert np.array_equal(outs[0]["u"], outs[1]["u"])
+    assert np.array_equal(outs[0]["naccept"], outs[1]["naccept"])
+
+
+@pytest.mark.parametrize("model_name,alg,rt,at", [
+    ("lorenz", "TSIT5", 1e-5, 1e-5), ("lorenz", "VERN7", 1e-5, 1e-5),
+    ("robertson", "RODAS5", 1e-6, 1e-10), ("robertson", "ROSENBROCK23", 1e-5, 1e-9),
+    ("vdp_ring8", "TSIT5", 1e-5, 1e-5)])
+def test_mixed_precision_vs_fp64_oracle(de, oracle, rng, model_name, alg, rt, at):
+    capi = de._capi
+    model = getattr(de.models, model_name)
+    N = 512
+    p, u0, t0, tf = make_inputs(de, model, N, rng)
+    if model_name == "vdp_ring8":
+        p[:, 0] = 10 ** rng.uniform(-1, 0.5, N)  # non-stiff part of the distribution
+        saveat = de.save_grid(0.0, 20.0, 1.0)
+        kind = capi.SAVE_GRID
+    elif model_name == "robertson":
+        saveat = tf[:, None] * 10 ** (-5 + 5 * np.arange(20) / 19)
+        kind = capi.SAVE_PER_TRAJ
+    else:
+        saveat = de.save_grid(0.0, 1.0, 0.1)
+        kind = capi.SAVE_GRID
+    g, r, _ = run_both(de, oracle, model, getattr(capi, "ALG_" + alg), p, u0, t0, tf, saveat,
+                       kind, precision="mixed", u_dtype="f32", reltol=rt, abstol=at,
+                       maxiters=10 ** 6)
+    assert np.all(g["retcode"] == capi.RET_SUCCESS)
+    err = oracle.weighted_error(g["u"], r["u"], at, rt)
+    assert err <= 10.0, err
+
+
+def test_em_fp64_identical_noise(de, oracle, rng):
+    capi = de._capi
+    model = de.models.lotka_volterra
+    N = 1000
+    p, u0, t0, tf = make_inputs(de, model, N, rng, tf=np.full(N, 2.0))
+    saveat = de.save_grid(0.0, 2.0, 0.25)
+    g, r, _ = run_both(de, oracle, model, capi.ALG_EM, p, u0, t0, tf, saveat, capi.SAVE_GRID,
+                       dt=1e-3, seed=20261204)
+    assert np.all(g["retcode"] == capi.RET_SUCCESS)
+    rel = np.max(np.abs(g["u"] - r["u"]) / np.abs(r["u"]))
+    assert rel <= 1e-12, rel
+
+
+def test_em_fp32_on_fp32_stream(de, oracle, rng):
+    capi = de._capi
+    model = de.models.lotka_volterra
+    N = 1000
+    p, u0, t0, tf = make_inputs(de, model, N, rng, tf=np.full(N, 2.0))
+    saveat = de.save_grid(0.0, 2.0, 0.25)
+    g, r, _ = run_both(de, oracle, model, capi.ALG_EM, p, u0, t0, tf, saveat, capi.SAVE_GRID,
+                       precision="mixed", noise_f32=True, u_dtype="f32", dt=1e-3, seed=7)
+    rel = np.max(np.abs(g["u"] - r["u"]) / np.abs(r["u"]))
+    assert rel <= 1e-4, rel
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_sosri_parity(de, oracle, rng, precision):
+    capi = de._capi
+    model = de.models.lotka_volterra
+    N = 1000
+    p, u0, t0, tf = make_inputs(de, model, N, rng)
+    saveat = de.save_grid(0.0, 10.0, 1.0)
+    g, r, _ = run_both(de, oracle, model, capi.ALG_SOSRI, p, u0, t0, tf, saveat, capi.SAVE_GRID,
+                       precision=precision, noise_f32=(precision == "mixed"),
+                       u_dtype="f64" if precision == "fp64" else "f32",
+                       reltol=1e-3, abstol=1e-3, seed=11)
+    assert np.all(g["retcode"] == capi.RET_SUCCESS)
+    assert g["nreject"].sum() > 0
+    if precision == "fp64":
+        same = np.all(np.abs(g["u"] - r["u"]) <= 1e-9 * np.abs(r["u"]) + 1e-12, axis=(1, 2))
+        assert same.mean() > 0.99, same.mean()  # identical paths except rare decision flips
+    else:
+        err = np.abs(g["u"] - r["u"]) / (1e-3 + 1e-3 * np.abs(r["u"]))
+        assert np.median(err.max(axis=(1, 2))) <= 10.0
+
+
+def test_failure_codes_gpu(de, oracle, rng):
+    capi = de._capi
+    model = de.models.lorenz
+    p = np.tile([10.0, 28.0, 8.0 / 3.0], (4, 1))
+    u0 = np.array([[1.0, 0, 0], [np.nan, 0, 0], [1.0, 0, 0], [1.0, 0, 0]])
+    t0 = np.zeros(4)
+    tf = np.array([1.0, 1.0, -1.0, 0.0])
+    saveat = np.array([0.0])
+    opts = capi.opts_default(capi.ALG_TSIT5)
+    g = de.solve_arrays(model, opts, p, u0, t0, tf, saveat, capi.SAVE_GRID)
+    assert list(g["retcode"]) == [capi.RET_SUCCESS, capi.RET_INITIALFAILURE,
+                                  capi.RET_INITIALFAILURE, capi.RET_SUCCESS]
+    opts.maxiters = 3
+    opts.reltol = opts.abstol = 1e-10
+    g = de.solve_arrays(model, opts, p[:1], u0[:1], t0[:1], np.ones(1),
+                        np.array([0.0, 0.5, 1.0]), capi.SAVE_GRID)
+    assert g["retcode"][0] == capi.RET_MAXITERS and np.isnan(g["u"][0, 2]).all()
+    # empty ensemble and empty save list
+    g = de.solve_arrays(model, opts, p[:0], u0[:0], t0[:0], tf[:0], saveat, capi.SAVE_GRID)
+    assert g["u"].shape == (0, 1, 3)
+    g = de.solve_arrays(model, capi.opts_default(capi.ALG_TSIT5), p[:1], u0[:1], t0[:1],
+                        np.ones(1), np.zeros(0), capi.SAVE_GRID)
+    assert g["retcode"][0] == capi.RET_SUCCESS and g["t_end"][0] == 1.0
+
+
+def test_invalid_arguments_rejected(de):
+    capi = de._capi
+    model = de.models.lorenz
+    p = np.tile([10.0, 28.0, 8.0 / 3.0], (2, 1))
+    u0 = np.tile([1.0, 0, 0], (2, 1))
+    opts = capi.opts_default(capi.ALG_TSIT5)
+    opts.reltol = -1.0
+    with pytest.raises(capi.GBDEError) as e:
+        de.solve_arrays(model, opts, p, u0, np.zeros(2), np.ones(2), np.array([1.0]),
+                        capi.SAVE_GRID)
+    assert e.value.code == capi.GBDE_ERR_INVALID
+    opts = capi.opts_default(capi.ALG_EM)
+    opts.dt = 0.1
+    with pytest.raises(capi.GBDEError) as e:
+        de.solve_arrays(model, opts, p, u0, np.zeros(2), np.ones(2), np.array([1.0]),
+                        capi.SAVE_GRID)
+    assert e.value.code == capi.GBDE_ERR_UNSUPPORTED
+
+
+def test_device_deadline_returns_status(de, rng):
+    """A deadline that expires mid-solve ends the kernel with an error status
+    the host reads (no fault, no hang); the context stays usable."""
+    capi = de._capi
+    model = de.models.robertson
+    N = 20000
+    p, u0, t0, tf = make_inputs(de, model, N, rng)
+    opts = capi.opts_default(capi.ALG_RODAS5)
+    opts.reltol, opts.abstol = 1e-10, 1e-14
+    opts.timeout_s = 1e-6
+    with pytest.raises(capi.GBDEError) as e:
+        g = de.solve_arrays(model, opts, p, u0, t0, tf, tf[:, None], capi.SAVE_PER_TRAJ)
+    assert e.value.code == capi.GBDE_ERR_TIMEOUT
+    opts.timeout_s = 0.0
+    opts.reltol, opts.abstol = 1e-6, 1e-10
+    g = de.solve_arrays(model, opts, p[:100], u0[:100], t0[:100], tf[:100], tf[:100, None],
+                        capi.SAVE_PER_TRAJ)
+    assert np.all(g["retcode"] == capi.RET_SUCCESS)
+
+
+def test_device_mode_matches_host_mode(de, rng):
+    import torch
+    capi = de._capi
+    model = de.models.lorenz
+    N = 300
+    p, u0, t0, tf = make_inputs(de, model, N, rng)
+    saveat = de.save_grid(0.0, 1.0, 0.1)
+    opts = capi.opts_default(capi.ALG_TSIT5)
+    h = de.solve_arrays(model, opts, p, u0, t0, tf, saveat, capi.SAVE_GRID)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (p, u0, t0, tf, saveat)]
+    d = de.solve_arrays(model, opts, *dev, capi.SAVE_GRID)
+    torch.cuda.synchronize()
+    assert np.array_equal(d["u"].cpu().numpy(), h["u"])
+    assert np.array_equal(d["retcode"].cpu().numpy(), h["retcode"])
+
+
+def test_public_api_core_pins(de):
+    """The reference's pinned behaviours through solve(EnsembleProblem, ...,
+    EnsembleGB300()) (test/core.jl:9-19, 21-36, 38-49, 81-96)."""
+    prob = de.ODEProblem(de.models.linear, 0.5, (0.0, 1.0), [1.01])
+    sol = de.solve(prob, de.Tsit5(), de.EnsembleGB300(), saveat=0.1, reltol=1e-8, abstol=1e-8)
+    assert sol.retcode == de.ReturnCode.Success
+    assert len(sol.t) == 11 and sol.u[0][0] == 0.5 and sol.u[5][0] > 0.5
+    lor = de.ODEProblem(de.models.lorenz, [1.0, 0.0, 0.0], (0.0, 1.0), [10.0, 28.0, 8.0 / 3.0])
+    sol = de.solve(lor, de.Tsit5(), de.EnsembleGB300(), saveat=0.1)
+    assert sol.retcode == de.ReturnCode.Success and list(sol.u[0]) == [1.0, 0.0, 0.0]
+    assert len(sol.u[-1]) == 3
+    rob = de.ODEProblem(de.models.robertson, [1.0, 0.0, 0.0], (0.0, 1e5), [0.04, 3e7, 1e4])
+    sol = de.solve(rob, de.Rodas5P(), de.EnsembleGB300(), saveat=[1e5])
+    assert sol.retcode == de.ReturnCode.Success
+    prob2 = de.remake(prob, u0=1.0)
+    sol = de.solve(prob2, de.Tsit5(), de.EnsembleGB300(), saveat=0.5)
+    assert sol.retcode == de.ReturnCode.Success and sol.u[0][0] == 1.0
+    # an ensemble through prob_func
+    ens = de.EnsembleProblem(lor, prob_func=lambda pr, i, rep: de.remake(pr, p=pr.p * (1 + 0.01 * i)))
+    es = de.solve(ens, de.Tsit5(), de.EnsembleGB300(), trajectories=64, saveat=0.1)
+    assert es.converged and len(es.u) == 64 and es.U.shape == (64, 11, 3)
+
+
+def test_config1_full_size(de, oracle):
+    """Lorenz ensemble, Float64, 10,000 trajectories (parameters scaled by
+    U[0.9, 1.1]), Tsit5 at 1e-8, saveat 0.1: every trajectory vs the oracle."""
+    capi = de._capi
+    rng = np.random.default_rng(20261204)
+    N = 10000
+    p, u0, t0, tf = make_inputs(de, de.models.lorenz, N, rng)
+    g, r, _ = run_both(de, oracle, de.models.lorenz, capi.ALG_TSIT5, p, u0, t0, tf,
+                       de.save_grid(0.0, 1.0, 0.1), capi.SAVE_GRID, reltol=1e-8, abstol=1e-8)
+    assert np.all(g["retcode"] == capi.RET_SUCCESS)
+    assert oracle.weighted_error(g["u"], r["u"], 1e-8, 1e-8) <= 1.0
+
+
+def test_config2_full_size_properties(de, oracle):
+    """Robertson ensemble, 100,000 trajectories, Rodas5 and Rosenbrock23:
+    every trajectory succeeds and conserves mass; a 2,000-trajectory sample
+    matches the oracle; plain and persistent launches agree bitwise."""
+    capi = de._capi
+    rng = np.random.default_rng(20261204)
+    N = 100000
+    p, u0, t0, tf = make_inputs(de, de.models.robertson, N, rng)
+    saveat = tf[:, None] * 10 ** (-5 + 5 * np.arange(20) / 19)
+    for alg in (capi.ALG_RODAS5, capi.ALG_ROSENBROCK23):
+        res = {}
+        for b in (capi.BATCH_PLAIN, capi.BATCH_PERSISTENT):
+            opts = capi.opts_default(alg)
+            opts.reltol, opts.abstol, opts.batching = 1e-6, 1e-10, b
+            res[b] = de.solve_arrays(de.models.robertson, opts, p, u0, t0, tf, saveat,
+                                     capi.SAVE_PER_TRAJ)
+        g = res[capi.BATCH_PLAIN]
+        assert np.all(g["retcode"] == capi.RET_SUCCESS)
+        assert np.max(np.abs(g["u"].sum(axis=2) - 1.0)) < 1e-8
+        assert np.array_equal(g["u"], res[capi.BATCH_PERSISTENT]["u"])
+        idx = rng.choice(N, 2000, replace=False)
+        opts = capi.opts_default(alg)
+        opts.reltol, opts.abstol = 1e-6, 1e-10
+        r = oracle.solve(capi, de.models.robertson, opts, p[idx], u0[idx], t0[idx], tf[idx],
+                         saveat[idx], capi.SAVE_PER_TRAJ, nthreads=8)
+        assert oracle.weighted_error(g["u"][idx], r["u"], 1e-10, 1e-6) <= 1.0
+
+
+def test_fma_peak_microbenchmark(de):
+    ctx = de._capi.context(0)
+    f64 = ctx.fma_peak(0)
+    f32 = ctx.fma_peak(1)
+    assert f64 > 0.1 and f32 > f64
