@@ -31,13 +31,20 @@ sys.path.insert(0, ROOT)
 SEED = 20261204
 
 # Algorithmic FP64 flops per attempted step / per accepted step / per save
-# point (FMA = 2 flops, division and sqrt = 1), counted from the kernels'
-# arithmetic for n = 3 ("roofline").
+# point (FMA = 2 flops, division and sqrt = 1), counted from the methods'
+# arithmetic for n = 3: Rodas5 = 7 RHS evaluations, 3x3 LU, 8 triangular
+# solves, the stage sums and the error norm; +16 per accepted step for the
+# Jacobian and f at the new point; +150 per dense-output save point.
 FLOPS = {
-    ("rodas5", "robertson"): (510.0, 16.0, 275.0),
+    ("rodas5", "robertson"): (510.0, 16.0, 150.0),
     ("rosenbrock23", "robertson"): (156.0, 16.0, 20.0),
     ("tsit5", "lorenz"): (272.0, 0.0, 85.0),
 }
+
+# DRAM bytes (read + write) per trajectory of the Rodas5 solve kernel, from one
+# ncu capture (20,000 trajectories: 4.587 MB read + 8.2 KB written; the saved
+# states stay in L2 until after the kernel), scaled by trajectories.
+TRAFFIC_PER_TRAJ = (4.586752e6 + 8192.0) / 20000.0
 
 
 def parse():
@@ -50,7 +57,7 @@ def parse():
     ap.add_argument("--trajectories", type=int, default=100000)
     ap.add_argument("--chosen", default="persistent",
                     help="chosen form: plain | persistent | persistent-mixed")
-    ap.add_argument("--cpu-sample", type=int, default=20000)
+    ap.add_argument("--cpu-sample", type=int, default=100000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -319,10 +326,14 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         threads = oracle.hardware_threads()
         sample = min(args.cpu_sample, N)
-        v, dt, _ = cpu_reference(de, alg_id, args, sample, SEED, threads)
+        cpu_reference(de, alg_id, args, max(256, sample // 20), SEED, threads)  # warm-up
+        runs = [cpu_reference(de, alg_id, args, sample, SEED, threads)[:2] for _ in range(3)]
+        v = float(np.median([r[0] for r in runs]))
+        dt = float(np.median([r[1] for r in runs]))
         cpu = {"value": v, "unit": "trajectories/s", "cores": threads, "kind": "port",
-               "sample": "%d trajectories of the workload in %.1f s (EnsembleThreads-equivalent "
-                         "C++ FP64 restatement, std::thread pool)" % (sample, dt)}
+               "sample": "%d trajectories of the workload, median of 3 runs of %.2f s "
+                         "(EnsembleThreads-equivalent C++ FP64 restatement, std::thread pool "
+                         "over all host cores)" % (sample, dt)}
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -351,7 +362,10 @@ def main():
         "e2e": {"value": total / (e2e_ms * 1e-3), "unit": "trajectories/s",
                 "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
-                     "frac": achieved / peak64, "traffic": None,
+                     "frac": achieved / peak64,
+                     "traffic": TRAFFIC_PER_TRAJ * N if args.alg == "rodas5" else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                       "20,000-trajectory launch, scaled by trajectories",
                      "peak_source": "in-run FP64 FMA microbenchmark (gbde_measure_fma_peak)",
                      "fp32_peak_tflops": peak32,
                      "algorithmic_flops_per_step": flops, "kernel_ms": chosen_kern},

@@ -27,6 +27,15 @@ GBDE_HD void two_sum(double a, double b, double& s, double& e) {
   e = (a - (s - bb)) + (b - bb);
 }
 
+// TwoSum in the working precision T (the FP32 path keeps its state as an
+// unevaluated sum hi + lo so that rounding does not accumulate over steps).
+template <class T>
+GBDE_HD void two_sum_t(T a, T b, T& s, T& e) {
+  s = a + b;
+  T bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
 // Compensated time: t = hi + lo.
 struct CTime {
   double hi, lo;

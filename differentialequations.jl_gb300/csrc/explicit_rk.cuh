@@ -12,7 +12,20 @@ namespace gbde {
 template <class M, class T>
 struct Tsit5Alg {
   static constexpr int ORDER = 5, ALG_ID = GBDE_ALG_TSIT5, N = M::N;
+  // FP32 path: the state is the unevaluated sum uu + lo (compensated), so
+  // the per-step rounding of u + h*sum(b k) does not accumulate.
+  static constexpr bool CMP = sizeof(T) == 4;
   T uu[N], un[N], k1[N], k2[N], k3[N], k4[N], k5[N], k6[N], k7[N];
+  T lo[N], lon[N];
+
+  GBDE_D T at(int c, T inc) const {
+    if constexpr (CMP) return uu[c] + (lo[c] + inc);
+    else return uu[c] + inc;
+  }
+  GBDE_D void advance(int c, T inc) {
+    if constexpr (CMP) two_sum_t(uu[c], lo[c] + inc, un[c], lon[c]);
+    else un[c] = uu[c] + inc;
+  }
 
   GBDE_D const T* u() const { return uu; }
   GBDE_D const T* unew() const { return un; }
@@ -20,7 +33,10 @@ struct Tsit5Alg {
 
   GBDE_D void init(const T* u0, const T* p, int& nf) {
 #pragma unroll
-    for (int c = 0; c < N; ++c) uu[c] = u0[c];
+    for (int c = 0; c < N; ++c) {
+      uu[c] = u0[c];
+      lo[c] = T(0);
+    }
     M::f(k1, uu, p);
     ++nf;
   }
@@ -30,28 +46,28 @@ struct Tsit5Alg {
     const T h = (T)dt;
     T y[N];
 #pragma unroll
-    for (int c = 0; c < N; ++c) y[c] = uu[c] + h * (T(a21) * k1[c]);
+    for (int c = 0; c < N; ++c) y[c] = at(c, h * (T(a21) * k1[c]));
     M::f(k2, y, p);
 #pragma unroll
-    for (int c = 0; c < N; ++c) y[c] = uu[c] + h * (T(a31) * k1[c] + T(a32) * k2[c]);
+    for (int c = 0; c < N; ++c) y[c] = at(c, h * (T(a31) * k1[c] + T(a32) * k2[c]));
     M::f(k3, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      y[c] = uu[c] + h * (T(a41) * k1[c] + T(a42) * k2[c] + T(a43) * k3[c]);
+      y[c] = at(c, h * (T(a41) * k1[c] + T(a42) * k2[c] + T(a43) * k3[c]));
     M::f(k4, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      y[c] = uu[c] + h * (T(a51) * k1[c] + T(a52) * k2[c] + T(a53) * k3[c] + T(a54) * k4[c]);
+      y[c] = at(c, h * (T(a51) * k1[c] + T(a52) * k2[c] + T(a53) * k3[c] + T(a54) * k4[c]));
     M::f(k5, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      y[c] = uu[c] + h * (T(a61) * k1[c] + T(a62) * k2[c] + T(a63) * k3[c] + T(a64) * k4[c] +
-                          T(a65) * k5[c]);
+      y[c] = at(c, h * (T(a61) * k1[c] + T(a62) * k2[c] + T(a63) * k3[c] + T(a64) * k4[c] +
+                          T(a65) * k5[c]));
     M::f(k6, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      un[c] = uu[c] + h * (T(a71) * k1[c] + T(a72) * k2[c] + T(a73) * k3[c] + T(a74) * k4[c] +
-                           T(a75) * k5[c] + T(a76) * k6[c]);
+      advance(c, h * (T(a71) * k1[c] + T(a72) * k2[c] + T(a73) * k3[c] + T(a74) * k4[c] +
+                      T(a75) * k5[c] + T(a76) * k6[c]));
     M::f(k7, un, p);
     nf += 6;
     T err[N];
@@ -75,14 +91,15 @@ struct Tsit5Alg {
     const T h = (T)dt;
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      out[c] = uu[c] + h * (b1 * k1[c] + b2 * k2[c] + b3 * k3[c] + b4 * k4[c] + b5 * k5[c] +
-                            b6 * k6[c] + b7 * k7[c]);
+      out[c] = at(c, h * (b1 * k1[c] + b2 * k2[c] + b3 * k3[c] + b4 * k4[c] + b5 * k5[c] +
+                          b6 * k6[c] + b7 * k7[c]));
   }
 
   GBDE_D void accept(const T*, int&) {
 #pragma unroll
     for (int c = 0; c < N; ++c) {
       uu[c] = un[c];
+      if constexpr (CMP) lo[c] = lon[c];
       k1[c] = k7[c];
     }
   }
@@ -91,9 +108,20 @@ struct Tsit5Alg {
 template <class M, class T>
 struct Vern7Alg {
   static constexpr int ORDER = 7, ALG_ID = GBDE_ALG_VERN7, N = M::N;
+  static constexpr bool CMP = sizeof(T) == 4;  // compensated FP32 state (as Tsit5Alg)
   T uu[N], un[N], k1[N], k4[N], k5[N], k6[N], k7[N], k8[N], k9[N], k10[N], k11[N];
   T k2[N], k3[N];
+  T lo[N], lon[N];
   bool have11;
+
+  GBDE_D T at(int c, T inc) const {
+    if constexpr (CMP) return uu[c] + (lo[c] + inc);
+    else return uu[c] + inc;
+  }
+  GBDE_D void advance(int c, T inc) {
+    if constexpr (CMP) two_sum_t(uu[c], lo[c] + inc, un[c], lon[c]);
+    else un[c] = uu[c] + inc;
+  }
 
   GBDE_D const T* u() const { return uu; }
   GBDE_D const T* unew() const { return un; }
@@ -101,7 +129,10 @@ struct Vern7Alg {
 
   GBDE_D void init(const T* u0, const T* p, int& nf) {
 #pragma unroll
-    for (int c = 0; c < N; ++c) uu[c] = u0[c];
+    for (int c = 0; c < N; ++c) {
+      uu[c] = u0[c];
+      lo[c] = T(0);
+    }
     M::f(k1, uu, p);
     ++nf;
     have11 = false;
@@ -112,48 +143,48 @@ struct Vern7Alg {
     const T h = (T)dt;
     T y[N];
 #pragma unroll
-    for (int c = 0; c < N; ++c) y[c] = uu[c] + h * (T(a21) * k1[c]);
+    for (int c = 0; c < N; ++c) y[c] = at(c, h * (T(a21) * k1[c]));
     M::f(k2, y, p);
 #pragma unroll
-    for (int c = 0; c < N; ++c) y[c] = uu[c] + h * (T(a31) * k1[c] + T(a32) * k2[c]);
+    for (int c = 0; c < N; ++c) y[c] = at(c, h * (T(a31) * k1[c] + T(a32) * k2[c]));
     M::f(k3, y, p);
 #pragma unroll
-    for (int c = 0; c < N; ++c) y[c] = uu[c] + h * (T(a41) * k1[c] + T(a43) * k3[c]);
+    for (int c = 0; c < N; ++c) y[c] = at(c, h * (T(a41) * k1[c] + T(a43) * k3[c]));
     M::f(k4, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      y[c] = uu[c] + h * (T(a51) * k1[c] + T(a53) * k3[c] + T(a54) * k4[c]);
+      y[c] = at(c, h * (T(a51) * k1[c] + T(a53) * k3[c] + T(a54) * k4[c]));
     M::f(k5, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      y[c] = uu[c] + h * (T(a61) * k1[c] + T(a63) * k3[c] + T(a64) * k4[c] + T(a65) * k5[c]);
+      y[c] = at(c, h * (T(a61) * k1[c] + T(a63) * k3[c] + T(a64) * k4[c] + T(a65) * k5[c]));
     M::f(k6, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      y[c] = uu[c] + h * (T(a71) * k1[c] + T(a73) * k3[c] + T(a74) * k4[c] + T(a75) * k5[c] +
-                          T(a76) * k6[c]);
+      y[c] = at(c, h * (T(a71) * k1[c] + T(a73) * k3[c] + T(a74) * k4[c] + T(a75) * k5[c] +
+                          T(a76) * k6[c]));
     M::f(k7, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      y[c] = uu[c] + h * (T(a81) * k1[c] + T(a83) * k3[c] + T(a84) * k4[c] + T(a85) * k5[c] +
-                          T(a86) * k6[c] + T(a87) * k7[c]);
+      y[c] = at(c, h * (T(a81) * k1[c] + T(a83) * k3[c] + T(a84) * k4[c] + T(a85) * k5[c] +
+                          T(a86) * k6[c] + T(a87) * k7[c]));
     M::f(k8, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      y[c] = uu[c] + h * (T(a91) * k1[c] + T(a93) * k3[c] + T(a94) * k4[c] + T(a95) * k5[c] +
-                          T(a96) * k6[c] + T(a97) * k7[c] + T(a98) * k8[c]);
+      y[c] = at(c, h * (T(a91) * k1[c] + T(a93) * k3[c] + T(a94) * k4[c] + T(a95) * k5[c] +
+                          T(a96) * k6[c] + T(a97) * k7[c] + T(a98) * k8[c]));
     M::f(k9, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      y[c] = uu[c] + h * (T(a101) * k1[c] + T(a103) * k3[c] + T(a104) * k4[c] +
-                          T(a105) * k5[c] + T(a106) * k6[c] + T(a107) * k7[c]);
+      y[c] = at(c, h * (T(a101) * k1[c] + T(a103) * k3[c] + T(a104) * k4[c] +
+                          T(a105) * k5[c] + T(a106) * k6[c] + T(a107) * k7[c]));
     M::f(k10, y, p);
     nf += 9;
     T err[N];
 #pragma unroll
     for (int c = 0; c < N; ++c) {
-      un[c] = uu[c] + h * (T(b1) * k1[c] + T(b4) * k4[c] + T(b5) * k5[c] + T(b6) * k6[c] +
-                           T(b7) * k7[c] + T(b8) * k8[c] + T(b9) * k9[c]);
+      advance(c, h * (T(b1) * k1[c] + T(b4) * k4[c] + T(b5) * k5[c] + T(b6) * k6[c] +
+                      T(b7) * k7[c] + T(b8) * k8[c] + T(b9) * k9[c]));
       err[c] = h * (T(b1 - bh1) * k1[c] + T(b4 - bh4) * k4[c] + T(b5 - bh5) * k5[c] +
                     T(b6 - bh6) * k6[c] + T(b7 - bh7) * k7[c] + T(b8) * k8[c] + T(b9) * k9[c] -
                     T(bh10) * k10[c]);
@@ -177,13 +208,16 @@ struct Vern7Alg {
     const T h = (T)dt;
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      out[c] = uu[c] + h * (w1 * k1[c] + w4 * k4[c] + w5 * k5[c] + w6 * k6[c] + w7 * k7[c] +
-                            w8 * k8[c] + w9 * k9[c] + w10 * k10[c] + w11 * k11[c]);
+      out[c] = at(c, h * (w1 * k1[c] + w4 * k4[c] + w5 * k5[c] + w6 * k6[c] + w7 * k7[c] +
+                          w8 * k8[c] + w9 * k9[c] + w10 * k10[c] + w11 * k11[c]));
   }
 
   GBDE_D void accept(const T* p, int& nf) {
 #pragma unroll
-    for (int c = 0; c < N; ++c) uu[c] = un[c];
+    for (int c = 0; c < N; ++c) {
+      uu[c] = un[c];
+      if constexpr (CMP) lo[c] = lon[c];
+    }
     if (have11) {
 #pragma unroll
       for (int c = 0; c < N; ++c) k1[c] = k11[c];
