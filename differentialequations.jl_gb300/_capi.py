@@ -85,6 +85,8 @@ SIGNATURES = {
                                       C.c_void_p]),
     "gbde_philox4x32_10": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "gbde_measure_fma_peak": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),
+    "gbde_ensemble_solve_noalloc": (C.c_int, [C.POINTER(Problem), C.POINTER(Opts),
+                                              C.POINTER(Outputs), C.c_void_p]),
 }
 
 _lib = None

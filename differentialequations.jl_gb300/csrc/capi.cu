@@ -82,6 +82,13 @@ static int set_err(gbde_ctx* ctx, int code, const char* fmt, ...) {
   } while (0)
 
 namespace gbde {
+// Records the calling thread's context-less error (gbde_last_error(NULL)) for
+// entry points that take no context.
+int set_thread_error(int code, const char* msg) {
+  g_thread_err = msg;
+  return code;
+}
+
 int ctx_device(const gbde_ctx* ctx, int* device, int* num_sms, cudaStream_t* stream) {
   if (!ctx) return GBDE_ERR_INVALID;
   *device = ctx->device;

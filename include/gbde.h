@@ -210,6 +210,40 @@ GBDE_API int gbde_philox_normals(uint64_t seed, uint64_t traj, uint64_t counter,
 GBDE_API int gbde_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
                        uint32_t out[4]);
 
+/* ---- solve without device allocation -------------------------------------
+ * No counterpart in the reference: this entry point exists for callers of
+ * this library that must not allocate device memory -- code inside a
+ * real-time loop where cudaMalloc's implicit device synchronisation is not
+ * allowed, a process whose device memory is owned by one allocator (a
+ * framework's caching pool, the array pool of a garbage-collected host
+ * language), or an embedding with a fixed device-memory budget.
+ *
+ * Same problem, options and outputs as gbde_ensemble_solve(), with these
+ * differences:
+ *   - every problem and output pointer is device memory on the calling
+ *     thread's current device (prob->mem must be GBDE_MEM_DEVICE);
+ *   - no context: the work runs on `stream` (NULL = the legacy default
+ *     stream) and errors are read with gbde_last_error(NULL);
+ *   - it calls no cudaMalloc / cudaFree / allocating library routine.  The
+ *     solve's scratch (the persistent work-queue counter and the status word
+ *     of the device deadline, 16 bytes whatever the ensemble size) lives in a
+ *     static device array of GBDE_NOALLOC_SCRATCH_BYTES inside libgbde.so,
+ *     which every GPU that loads the library holds until the process exits.
+ *     A solve whose scratch would exceed that array is rejected with
+ *     GBDE_ERR_INVALID;
+ *   - the first call on a device looks up that array's device address
+ *     (cudaGetSymbolAddress, with the device current); make that first call
+ *     before any stream capture;
+ *   - every call on a device shares the one array, which keeps the last
+ *     call's contents (each call clears what it needs in stream order).
+ *     Calls that overlap on the GPU race: serialise them on one stream or
+ *     with events;
+ *   - learned=1 is rejected (GBDE_ERR_STATE); device_ms is not measured (0).
+ * Blocks until the kernels have finished. */
+#define GBDE_NOALLOC_SCRATCH_BYTES 256
+GBDE_API int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_opts* opts,
+                                gbde_outputs* out, void* stream);
+
 /* Measure the device's FP64 / FP32 FMA throughput (TFLOP/s, FMA = 2 flops)
  * with a dependent-chain-free FMA loop; kind 0 = FP64, 1 = FP32. */
 GBDE_API int gbde_measure_fma_peak(gbde_ctx* ctx, int32_t kind, double* tflops);
