@@ -87,6 +87,7 @@ SIGNATURES = {
     "gbde_measure_fma_peak": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),
     "gbde_ensemble_solve_noalloc": (C.c_int, [C.POINTER(Problem), C.POINTER(Opts),
                                               C.POINTER(Outputs), C.c_void_p]),
+    "gbde_check_rcp64": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double)]),
 }
 
 _lib = None
@@ -159,6 +160,11 @@ class Context:
     def fma_peak(self, kind):
         v = C.c_double()
         check(lib().gbde_measure_fma_peak(self.handle, kind, C.byref(v)), self.handle)
+        return v.value
+
+    def check_rcp64(self, n):
+        v = C.c_double()
+        check(lib().gbde_check_rcp64(self.handle, int(n), C.byref(v)), self.handle)
         return v.value
 
     def solve(self, prob, opts, outs):

@@ -6,6 +6,7 @@
 // (EnsembleProblem qa.jl:50, EnsembleThreads qa.jl:56, solve qa.jl:192):
 // one call solves every trajectory and fills the solution arrays.
 #include <chrono>
+#include <climits>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -58,6 +59,7 @@ struct gbde_ctx {
   // staging for GBDE_MEM_HOST calls
   DevBuf p, u0, t0, tf, saveat, u, ret, nacc, nrej, nf, tend, method;
   DevBuf work;  // queue counter + status flag
+  DevBuf order; // persistent queue order (longest span first) + sort counters
   // learned predictor (filled by the MLP entry points)
   DevBuf pred_dt;
 };
@@ -154,7 +156,7 @@ int gbde_ctx_destroy(gbde_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf* b : {&ctx->p, &ctx->u0, &ctx->t0, &ctx->tf, &ctx->saveat, &ctx->u, &ctx->ret,
                     &ctx->nacc, &ctx->nrej, &ctx->nf, &ctx->tend, &ctx->method, &ctx->work,
-                    &ctx->pred_dt})
+                    &ctx->order, &ctx->pred_dt})
     b->release();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -319,6 +321,8 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
   a.qoldinit = opts->qoldinit;
   a.seed = opts->seed;
   a.timeout_ns = opts->timeout_s > 0 ? (uint64_t)(opts->timeout_s * 1e9) : 0;
+  a.ctl = ctl_consts(opts->beta1, opts->beta2, opts->gamma, opts->qmin, opts->qmax,
+                     opts->qsteady_min, opts->qsteady_max, opts->qoldinit);
 
   const bool host = prob->mem == GBDE_MEM_HOST;
   if (host) {
@@ -383,6 +387,13 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
     return set_err(ctx, GBDE_ERR_INVALID, "block_size must be a multiple of 32 and <= 128");
 
   GBDE_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
+  if (cfg.persistent && N > 1 && N <= INT32_MAX) {
+    // queue order: longest spans first (order.cu)
+    GBDE_CUDA(ctx, ctx->order.ensure(span_order_scratch_bytes(N)));
+    const int32_t* ord = nullptr;
+    GBDE_CUDA(ctx, build_span_order(a.t0, a.tf, N, ctx->order.ptr, ctx->num_sms, s, &ord));
+    a.order = ord;
+  }
   if (N > 0) {
     cudaError_t e;
     if (alg == GBDE_ALG_TSIT5 || alg == GBDE_ALG_VERN7) e = launch_explicit(cfg, a, s);

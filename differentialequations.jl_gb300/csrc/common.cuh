@@ -1,6 +1,7 @@
 // common.cuh -- host/device helpers shared by every solver kernel.
 #pragma once
 #include <stdint.h>
+#include <string.h>
 #include <math.h>
 
 #if defined(__CUDACC__)
@@ -18,6 +19,35 @@ template <class T> GBDE_HD T tmin(T a, T b) { return a < b ? a : b; }
 template <class T> GBDE_HD T tabs(T a) { return a < T(0) ? -a : a; }
 
 GBDE_HD bool finite_d(double x) { return isfinite(x); }
+
+// ---- non-contracted arithmetic (identical rounding on host and device)
+#if defined(__CUDA_ARCH__)
+GBDE_HD double xmul(double a, double b) { return __dmul_rn(a, b); }
+GBDE_HD double xadd(double a, double b) { return __dadd_rn(a, b); }
+GBDE_HD double xfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+GBDE_HD float xmul(float a, float b) { return __fmul_rn(a, b); }
+GBDE_HD float xadd(float a, float b) { return __fadd_rn(a, b); }
+GBDE_HD float xfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+#else
+GBDE_HD double xmul(double a, double b) { return a * b; }
+GBDE_HD double xadd(double a, double b) { return a + b; }
+GBDE_HD double xfma(double a, double b, double c) { return fma(a, b, c); }
+GBDE_HD float xmul(float a, float b) { return a * b; }
+GBDE_HD float xadd(float a, float b) { return a + b; }
+GBDE_HD float xfma(float a, float b, float c) { return fmaf(a, b, c); }
+#endif
+
+// |x| as an ordered integer: for non-NaN doubles, mag_bits(a) < mag_bits(b)
+// iff |a| < |b|.  Compares on the integer pipe instead of the FP64 pipe.
+GBDE_HD uint64_t mag_bits(double x) {
+#if defined(__CUDA_ARCH__)
+  return (uint64_t)__double_as_longlong(x) & 0x7fffffffffffffffull;
+#else
+  uint64_t b;
+  memcpy(&b, &x, sizeof(b));
+  return b & 0x7fffffffffffffffull;
+#endif
+}
 
 // Error-free sum (Knuth TwoSum): s + e == a + b exactly.  Used for the
 // compensated time accumulation of the mixed-precision path.

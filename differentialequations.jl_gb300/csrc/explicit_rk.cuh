@@ -75,7 +75,7 @@ struct Tsit5Alg {
     for (int c = 0; c < N; ++c)
       err[c] = h * (T(bt1) * k1[c] + T(bt2) * k2[c] + T(bt3) * k3[c] + T(bt4) * k4[c] +
                     T(bt5) * k5[c] + T(bt6) * k6[c] + T(bt7) * k7[c]);
-    return err_norm<N>(err, uu, un, abstol, reltol);
+    return err_ms<N>(err, uu, un, abstol, reltol);
   }
 
   GBDE_D void interp(double th, double dt, T* out, const T*, int&) {
@@ -190,7 +190,7 @@ struct Vern7Alg {
                     T(bh10) * k10[c]);
     }
     have11 = false;
-    return err_norm<N>(err, uu, un, abstol, reltol);
+    return err_ms<N>(err, uu, un, abstol, reltol);
   }
 
   GBDE_D void interp(double th, double dt, T* out, const T* p, int& nf) {

@@ -20,6 +20,11 @@ cudaError_t launch_explicit(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s
 cudaError_t launch_rosenbrock(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
 cudaError_t launch_sde(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
 
+// Longest-span-first order of the persistent queue (order.cu).
+size_t span_order_scratch_bytes(int64_t n);
+cudaError_t build_span_order(const double* t0, const double* tf, int64_t n, void* scratch,
+                             int num_sms, cudaStream_t s, const int32_t** order_out);
+
 // Launch geometry helper shared by the translation units.
 template <class K>
 cudaError_t launch_kernel(K kern, const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {

@@ -215,6 +215,8 @@ extern "C" int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_
   a.qoldinit = opts->qoldinit;
   a.seed = opts->seed;
   a.timeout_ns = opts->timeout_s > 0 ? (uint64_t)(opts->timeout_s * 1e9) : 0;
+  a.ctl = ctl_consts(opts->beta1, opts->beta2, opts->gamma, opts->qmin, opts->qmax,
+                     opts->qsteady_min, opts->qsteady_max, opts->qoldinit);
   a.queue = opts->batching == GBDE_BATCH_PERSISTENT ? queue : nullptr;
   a.flag = flag_dev;
 

@@ -60,23 +60,6 @@ GBDE_HD Philox4 philox4x32_10(Philox4 c, uint32_t k0, uint32_t k1) {
   return c;
 }
 
-// ---- non-contracted arithmetic (identical rounding on host and device)
-#if defined(__CUDA_ARCH__)
-GBDE_HD double xmul(double a, double b) { return __dmul_rn(a, b); }
-GBDE_HD double xadd(double a, double b) { return __dadd_rn(a, b); }
-GBDE_HD double xfma(double a, double b, double c) { return __fma_rn(a, b, c); }
-GBDE_HD float xmul(float a, float b) { return __fmul_rn(a, b); }
-GBDE_HD float xadd(float a, float b) { return __fadd_rn(a, b); }
-GBDE_HD float xfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-#else
-GBDE_HD double xmul(double a, double b) { return a * b; }
-GBDE_HD double xadd(double a, double b) { return a + b; }
-GBDE_HD double xfma(double a, double b, double c) { return fma(a, b, c); }
-GBDE_HD float xmul(float a, float b) { return a * b; }
-GBDE_HD float xadd(float a, float b) { return a + b; }
-GBDE_HD float xfma(float a, float b, float c) { return fmaf(a, b, c); }
-#endif
-
 template <class T> struct BMConst;
 template <> struct BMConst<double> {
   static constexpr int NLOG = 12;   // atanh terms: s^2 <= 0.0295, 0.0295^12 < 1e-18

@@ -17,7 +17,9 @@ namespace gbde {
 // ---------------------------------------------------------------- LU
 // Partial-pivot LU of an N x N matrix held in registers.  Row swaps are done
 // with compile-time indices and selects so that nothing spills to local
-// memory; the reciprocal pivots are kept for the triangular solves.
+// memory; the reciprocal pivots (Newton-refined, controller.h) are kept for
+// the triangular solves, and the pivot search compares magnitudes as
+// integers.
 template <int N>
 struct SmallLU {
   double A[N][N];
@@ -28,10 +30,10 @@ struct SmallLU {
 #pragma unroll
     for (int k = 0; k < N; ++k) {
       int pk = k;
-      double best = fabs(A[k][k]);
+      uint64_t best = mag_bits(A[k][k]);
 #pragma unroll
       for (int r = k + 1; r < N; ++r) {
-        const double v = fabs(A[r][k]);
+        const uint64_t v = mag_bits(A[r][k]);
         if (v > best) {
           best = v;
           pk = r;
@@ -48,7 +50,7 @@ struct SmallLU {
           A[r][c] = sw ? x : y;
         }
       }
-      inv[k] = 1.0 / A[k][k];
+      inv[k] = rcp64(A[k][k]);
 #pragma unroll
       for (int r = k + 1; r < N; ++r) {
         const double l = A[r][k] * inv[k];
@@ -154,7 +156,7 @@ struct Ros23Alg {
     T err[N];
 #pragma unroll
     for (int c = 0; c < N; ++c) err[c] = h / T(6) * (k1[c] - T(2) * k2[c] + k3[c]);
-    return err_norm<N>(err, uu, un, abstol, reltol);
+    return err_ms<N>(err, uu, un, abstol, reltol);
   }
 
   GBDE_D void interp(double th, double dt, T* out, const T*, int&) {
@@ -253,13 +255,13 @@ struct RodasAlg {
       fresh = true;
     }
     SmallLU<N> W;
-    const double dg = 1.0 / (dt * K::g);
+    const double ih = rcp64(dt);
+    const double dg = ih * (1.0 / K::g);
 #pragma unroll
     for (int r = 0; r < N; ++r)
 #pragma unroll
-      for (int c = 0; c < N; ++c) W.A[r][c] = (r == c ? dg : 0.0) - (double)J[r][c];
+      for (int c = 0; c < N; ++c) W.A[r][c] = r == c ? dg - (double)J[r][c] : -(double)J[r][c];
     W.factor();
-    const double ih = 1.0 / dt;
     const T c21 = T(K::C21 * ih), c31 = T(K::C31 * ih), c32 = T(K::C32 * ih);
     const T c41 = T(K::C41 * ih), c42 = T(K::C42 * ih), c43 = T(K::C43 * ih);
     const T c51 = T(K::C51 * ih), c52 = T(K::C52 * ih), c53 = T(K::C53 * ih),
@@ -337,7 +339,7 @@ struct RodasAlg {
     nf += 7;
 #pragma unroll
     for (int c = 0; c < N; ++c) un[c] = y[c] + s8[c];
-    return err_norm<N>(s8, uu, un, abstol, reltol);
+    return err_ms<N>(s8, uu, un, abstol, reltol);
   }
 
   GBDE_D void interp(double th, double, T* out, const T*, int&) {

@@ -286,6 +286,7 @@ __device__ void sri_all(const KArgs& a) {
     if (a.dtmax > 0.0) h = fmin(h, a.dtmax);
     int ret = GBDE_RET_DEFAULT;
     int64_t iters = 0;
+    float lqold = a.ctl.lqoldinit;
     if (!(t < tf)) ret = GBDE_RET_SUCCESS;
     while (ret == GBDE_RET_DEFAULT) {
       const double rem = tf - t;
@@ -337,9 +338,9 @@ __device__ void sri_all(const KArgs& a) {
                      (T(b4_1) * G1[c] + T(b4_2) * G2[c] + T(b4_3) * G3[c] + T(b4_4) * G4[c]) * I111[c] * ih;
         err[c] = (ed < T(0) ? -ed : ed) + (en < T(0) ? -en : en);
       }
-      const double EEst = err_norm<N>(err, u, un, a.abstol, a.reltol);
+      const double ms = err_ms<N>(err, u, un, a.abstol, a.reltol);  // EEst^2
       ++iters;
-      if (!a.adaptive || EEst <= 1.0) {
+      if (!a.adaptive || ms <= 1.0) {
         double tnew;
         if (last) {
           tnew = tf;
@@ -377,15 +378,11 @@ __device__ void sri_all(const KArgs& a) {
         ++nacc;
         if (!fin) ret = GBDE_RET_UNSTABLE;
         else if (last) ret = GBDE_RET_SUCCESS;
-        if (a.adaptive) {
-          double q = pow(EEst, a.beta1);
-          q = fmax(1.0 / a.qmax, fmin(1.0 / a.qmin, q / a.gamma));
-          h = hs / q;
-        }
+        if (a.adaptive) h = hs * (double)ctl_accept(a.ctl, ms, lqold);
       } else {
         ++nrej;
         stk.push(hs, dW, dZ);
-        h = isfinite(EEst) ? hs / fmin(1.0 / a.qmin, pow(EEst, a.beta1) / a.gamma) : hs * a.qmin;
+        h = hs * (double)ctl_reject(a.ctl, ms);
       }
       if (a.dtmax > 0.0) h = fmin(h, a.dtmax);
       if (ret == GBDE_RET_DEFAULT) {

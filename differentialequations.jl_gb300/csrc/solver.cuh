@@ -19,6 +19,7 @@
 #pragma once
 #include <cooperative_groups.h>
 #include "common.cuh"
+#include "controller.h"
 #include "models.cuh"
 
 namespace gbde {
@@ -50,6 +51,7 @@ struct KArgs {
   uint64_t timeout_ns;        // 0 = no deadline
   int32_t* flag;              // device status word (bit 0: deadline hit)
   const float* pred_dt;       // optional predicted first dt per trajectory
+  CtlK ctl;                   // step-size controller constants (controller.h)
 };
 
 GBDE_D uint64_t global_ns() {
@@ -124,6 +126,21 @@ GBDE_D void store_state(const KArgs& a, int64_t i, int j, const T* v) {
 }
 
 // --------------------------------------------------------- error norm
+// Mean square of the scaled error, ms = EEst^2 (the accept test is ms <= 1).
+// Each err_c / sc_c uses the Newton-refined reciprocal of controller.h
+// instead of an IEEE division.
+template <int N, class T>
+GBDE_HD double err_ms(const T* err, const T* u, const T* unew, double abstol, double reltol) {
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    const double sc = abstol + reltol * fmax(fabs((double)u[c]), fabs((double)unew[c]));
+    const double e = (double)err[c] * rcp64(sc);
+    s += e * e;
+  }
+  return s * (1.0 / N);
+}
+
 template <int N, class T>
 GBDE_HD double err_norm(const T* err, const T* u, const T* unew, double abstol, double reltol) {
   double s = 0.0;
@@ -136,48 +153,43 @@ GBDE_HD double err_norm(const T* err, const T* u, const T* unew, double abstol, 
   return sqrt(s / N);
 }
 
-// Hairer-Wanner starting step (HNW I, Sec. II.4): d0 = |u0|, d1 = |f0|,
-// h0 = 0.01 d0/d1, one explicit Euler trial step for d2 = |f1 - f0|/h0,
-// h1 = (0.01 / max(d1, d2))^(1/(order+1)), dt = min(100 h0, h1, tf - t0).
+// Hairer-Wanner starting step (HNW I, Sec. II.4): mean squares of the
+// scaled u0, f0 and of one explicit Euler trial step's change in f, then
+// hw_h0 / hw_dt (controller.h).
 template <class M, class T>
 GBDE_D double initial_dt(const T* u0, const T* f0, const T* p, double tspan, int order,
                          double abstol, double reltol, int& nf) {
   constexpr int N = M::N;
-  double d0 = 0.0, d1 = 0.0;
+  double s0 = 0.0, s1 = 0.0, rs[N];
 #pragma unroll
   for (int c = 0; c < N; ++c) {
-    const double sc = abstol + fabs((double)u0[c]) * reltol;
-    const double x = (double)u0[c] / sc, y = (double)f0[c] / sc;
-    d0 += x * x;
-    d1 += y * y;
+    rs[c] = rcp64(abstol + fabs((double)u0[c]) * reltol);
+    const double x = (double)u0[c] * rs[c], y = (double)f0[c] * rs[c];
+    s0 += x * x;
+    s1 += y * y;
   }
-  d0 = sqrt(d0 / N);
-  d1 = sqrt(d1 / N);
-  double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
-  h0 = fmin(h0, tspan);
+  s0 *= 1.0 / N;
+  s1 *= 1.0 / N;
+  const double h0 = hw_h0(s0, s1, tspan);
   T u1[N], f1[N];
 #pragma unroll
   for (int c = 0; c < N; ++c) u1[c] = u0[c] + T(h0) * f0[c];
   M::f(f1, u1, p);
   ++nf;
-  double d2 = 0.0;
+  double s2 = 0.0;
 #pragma unroll
   for (int c = 0; c < N; ++c) {
-    const double sc = abstol + fabs((double)u0[c]) * reltol;
-    const double y = ((double)f1[c] - (double)f0[c]) / sc;
-    d2 += y * y;
+    const double y = ((double)f1[c] - (double)f0[c]) * rs[c];
+    s2 += y * y;
   }
-  d2 = sqrt(d2 / N) / h0;
-  const double m = fmax(d1, d2);
-  const double h1 = (m <= 1e-15) ? fmax(1e-6, h0 * 1e-3) : pow(0.01 / m, 1.0 / (order + 1));
-  return fmin(fmin(100.0 * h0, h1), tspan);
+  return hw_dt(h0, s1, s2 * (1.0 / N), tspan, order);
 }
 
 // ------------------------------------------------------------- driver
 // Alg provides:  static constexpr int ORDER (for beta defaults / init dt),
 //   void init(const T* u0, const T* p, int& nf)       -- u = u0, f(u) cache
 //   double attempt(double dt, const T* p, double abstol, double reltol, int& nf)
-//                                                       -- returns EEst
+//                                                       -- returns EEst^2
 //   void interp(double theta, double dt, T* out, const T* p, int& nf)
 //                                                       -- dense output
 //   void accept(const T* p, int& nf)                    -- u = unew, caches
@@ -191,7 +203,8 @@ __device__ void integrate_all(const KArgs& a) {
   T p[M::NP];
   int64_t i = -1;
   bool active = false;
-  double t = 0.0, tlo = 0.0, tf = 0.0, dt = 0.0, qold = 1.0;
+  double t = 0.0, tlo = 0.0, tf = 0.0, dt = 0.0;
+  float lqold = 0.0f;  // log2(qold)
   int js = 0, nacc = 0, nrej = 0, nfev = 0;
   int64_t iters = 0;
   int ret = GBDE_RET_DEFAULT;
@@ -213,7 +226,7 @@ __device__ void integrate_all(const KArgs& a) {
       js = 0;
       nacc = nrej = nfev = 0;
       iters = 0;
-      qold = a.qoldinit;
+      lqold = a.ctl.lqoldinit;
       ret = GBDE_RET_DEFAULT;
       bool bad = !(tf >= t) || !isfinite(t) || !isfinite(tf);
 #pragma unroll
@@ -251,20 +264,13 @@ __device__ void integrate_all(const KArgs& a) {
         h = rem;
         last = true;
       }
-      const double EEst = alg.attempt(h, p, a.abstol, a.reltol, nfev);
+      const double ms = alg.attempt(h, p, a.abstol, a.reltol, nfev);  // EEst^2
       ++iters;
-      const bool ok = !a.adaptive || EEst <= 1.0;
+      const bool ok = !a.adaptive || ms <= 1.0;
       if (ok) {
         // controller proposal for the next step
         double dtnew = h;
-        if (a.adaptive) {
-          const double q11 = pow(EEst, a.beta1);
-          double q = q11 / pow(qold, a.beta2);
-          q = fmax(1.0 / a.qmax, fmin(1.0 / a.qmin, q / a.gamma));
-          if (q >= a.qsteady_min && q <= a.qsteady_max) q = 1.0;
-          dtnew = h / q;
-          qold = fmax(EEst, a.qoldinit);
-        }
+        if (a.adaptive) dtnew = h * (double)ctl_accept(a.ctl, ms, lqold);
         // time update (compensated in the mixed-precision path)
         double tnew;
         if (last) {
@@ -303,12 +309,7 @@ __device__ void integrate_all(const KArgs& a) {
         dt = a.dtmax > 0.0 ? fmin(dtnew, a.dtmax) : dtnew;
       } else {
         ++nrej;
-        if (isfinite(EEst)) {
-          const double q11 = pow(EEst, a.beta1);
-          dt = h / fmin(1.0 / a.qmin, q11 / a.gamma);
-        } else {
-          dt = h * a.qmin;
-        }
+        dt = h * (double)ctl_reject(a.ctl, ms);
       }
       if (ret == GBDE_RET_DEFAULT) {
         if (iters >= a.maxiters) ret = GBDE_RET_MAXITERS;

@@ -248,6 +248,12 @@ GBDE_API int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_op
  * with a dependent-chain-free FMA loop; kind 0 = FP64, 1 = FP32. */
 GBDE_API int gbde_measure_fma_peak(gbde_ctx* ctx, int32_t kind, double* tflops);
 
+/* Self-check (no counterpart in the reference): the largest relative
+ * difference, over n pseudo-random x with |x| in [2^-60, 2^61), between the
+ * Newton-refined reciprocal the kernels use and the IEEE division 1/x on the
+ * device.  Within one ulp means <= 2^-52. */
+GBDE_API int gbde_check_rcp64(gbde_ctx* ctx, int64_t n, double* max_rel_err);
+
 #ifdef __cplusplus
 }
 #endif

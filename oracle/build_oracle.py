@@ -16,6 +16,9 @@ LIB = os.path.join(HERE, "liboracle_gbde.so")
 DEPS = [SRC, os.path.join(HERE, "..", "include", "gbde.h"),
         os.path.join(HERE, "..", "differentialequations.jl_gb300", "csrc", "tableaus.h"),
         os.path.join(HERE, "..", "differentialequations.jl_gb300", "csrc", "dense_coeffs.h"),
+        os.path.join(HERE, "..", "differentialequations.jl_gb300", "csrc", "controller.h"),
+        os.path.join(HERE, "..", "differentialequations.jl_gb300", "csrc", "philox.h"),
+        os.path.join(HERE, "..", "differentialequations.jl_gb300", "csrc", "common.cuh"),
         __file__]
 
 

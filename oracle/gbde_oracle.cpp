@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "../include/gbde.h"
+#include "../differentialequations.jl_gb300/csrc/controller.h"
 #include "../differentialequations.jl_gb300/csrc/tableaus.h"
 
 namespace {
@@ -160,48 +161,48 @@ struct LU {
 };
 
 // ---------------------------------------------------------- utilities
+// Mean square of the scaled error, EEst^2 (accept iff <= 1).
 double wrms(int n, const double* e, const double* u, const double* un, double at, double rt) {
   double s = 0.0;
   for (int c = 0; c < n; ++c) {
     const double sc = at + rt * std::fmax(std::fabs(u[c]), std::fabs(un[c]));
     s += (e[c] / sc) * (e[c] / sc);
   }
-  return std::sqrt(s / n);
+  return s / n;
 }
 
-// Hairer-Norsett-Wanner I, Sec. II.4 starting step
+// Hairer-Norsett-Wanner I, Sec. II.4 starting step: mean squares of the
+// scaled u0, f0 and f(u0 + h0 f0) - f0; the powers go through the shared
+// hw_h0 / hw_dt (controller.h), as in the kernels.
 double init_dt(const Model& m, const double* u0, const double* f0, const double* p,
                double tspan, int order, double at, double rt, int& nf) {
   const int n = m.n;
-  double d0 = 0, d1 = 0;
+  double s0 = 0, s1 = 0;
   for (int c = 0; c < n; ++c) {
     const double sc = at + std::fabs(u0[c]) * rt;
-    d0 += (u0[c] / sc) * (u0[c] / sc);
-    d1 += (f0[c] / sc) * (f0[c] / sc);
+    s0 += (u0[c] / sc) * (u0[c] / sc);
+    s1 += (f0[c] / sc) * (f0[c] / sc);
   }
-  d0 = std::sqrt(d0 / n);
-  d1 = std::sqrt(d1 / n);
-  double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
-  h0 = std::fmin(h0, tspan);
+  s0 /= n;
+  s1 /= n;
+  const double h0 = gbde::hw_h0(s0, s1, tspan);
   Vec u1, f1;
   for (int c = 0; c < n; ++c) u1[c] = u0[c] + h0 * f0[c];
   rhs(m.id, u1, p, f1);
   ++nf;
-  double d2 = 0;
+  double s2 = 0;
   for (int c = 0; c < n; ++c) {
     const double sc = at + std::fabs(u0[c]) * rt;
-    d2 += ((f1[c] - f0[c]) / sc) * ((f1[c] - f0[c]) / sc);
+    s2 += ((f1[c] - f0[c]) / sc) * ((f1[c] - f0[c]) / sc);
   }
-  d2 = std::sqrt(d2 / n) / h0;
-  const double mx = std::fmax(d1, d2);
-  const double h1 = mx <= 1e-15 ? std::fmax(1e-6, h0 * 1e-3) : std::pow(0.01 / mx, 1.0 / (order + 1));
-  return std::fmin(std::fmin(100.0 * h0, h1), tspan);
+  return gbde::hw_dt(h0, s1, s2 / n, tspan, order);
 }
 
 struct Ctl {  // controller constants (gbde_opts)
   double at, rt, qmin, qmax, gamma, beta1, beta2, qsmin, qsmax, qoldinit, dtmin, dtmax, dt0;
   int64_t maxiters;
   int adaptive;
+  gbde::CtlK k;  // step-size factor constants (controller.h, shared with the kernels)
 };
 
 // ---------------------------------------------------------- one trajectory
@@ -562,7 +563,8 @@ void solve_ode_traj(const Model& m, int alg, const Ctl& C, Out& o) {
   S.n = n;
   S.id = m.id;
   S.p = p;
-  double dt = 0.0, qold = C.qoldinit;
+  double dt = 0.0;
+  float lqold = C.k.lqoldinit;
   if (bad) {
     ret = GBDE_RET_INITIALFAILURE;
   } else {
@@ -581,18 +583,11 @@ void solve_ode_traj(const Model& m, int alg, const Ctl& C, Out& o) {
       h = rem;
       last = true;
     }
-    const double E = S.attempt(h, C, nf);
+    const double E = S.attempt(h, C, nf);  // EEst^2
     ++iters;
     if (!C.adaptive || E <= 1.0) {
       double dtnew = h;
-      if (C.adaptive) {
-        const double q11 = std::pow(E, C.beta1);
-        double q = q11 / std::pow(qold, C.beta2);
-        q = std::fmax(1.0 / C.qmax, std::fmin(1.0 / C.qmin, q / C.gamma));
-        if (q >= C.qsmin && q <= C.qsmax) q = 1.0;
-        dtnew = h / q;
-        qold = std::fmax(E, C.qoldinit);
-      }
+      if (C.adaptive) dtnew = h * (double)gbde::ctl_accept(C.k, E, lqold);
       const double tnew = last ? tf : t + h;
       while (js < P->n_save) {
         const double ts = o.ts(js);
@@ -616,8 +611,7 @@ void solve_ode_traj(const Model& m, int alg, const Ctl& C, Out& o) {
       dt = C.dtmax > 0.0 ? std::fmin(dtnew, C.dtmax) : dtnew;
     } else {
       ++nrej;
-      dt = std::isfinite(E) ? h / std::fmin(1.0 / C.qmin, std::pow(E, C.beta1) / C.gamma)
-                            : h * C.qmin;
+      dt = h * (double)gbde::ctl_reject(C.k, E);
     }
     if (ret == GBDE_RET_DEFAULT) {
       if (iters >= C.maxiters) ret = GBDE_RET_MAXITERS;
@@ -868,6 +862,7 @@ void solve_sri_traj(const Model& m, const Ctl& C, uint64_t seed, int f32, Out& o
   if (C.dtmax > 0.0) h = std::fmin(h, C.dtmax);
   int ret = t < tf ? GBDE_RET_DEFAULT : GBDE_RET_SUCCESS;
   int64_t iters = 0;
+  float lqold = C.k.lqoldinit;
   while (ret == GBDE_RET_DEFAULT) {
     const double rem = tf - t;
     double hs = h;
@@ -958,11 +953,7 @@ void solve_sri_traj(const Model& m, const Ctl& C, uint64_t seed, int f32, Out& o
       ++nacc;
       if (!fin) ret = GBDE_RET_UNSTABLE;
       else if (last) ret = GBDE_RET_SUCCESS;
-      if (C.adaptive) {
-        double q = std::pow(E, C.beta1);
-        q = std::fmax(1.0 / C.qmax, std::fmin(1.0 / C.qmin, q / C.gamma));
-        h = hs / q;
-      }
+      if (C.adaptive) h = hs * (double)gbde::ctl_accept(C.k, E, lqold);
     } else {
       ++nrej;
       if (sp == 8) {  // merge the two farthest pieces
@@ -974,7 +965,7 @@ void solve_sri_traj(const Model& m, const Ctl& C, uint64_t seed, int f32, Out& o
       stk[sp].dt = hs;
       for (int c = 0; c < n; ++c) { stk[sp].W[c] = dW[c]; stk[sp].Z[c] = dZ[c]; }
       ++sp;
-      h = std::isfinite(E) ? hs / std::fmin(1.0 / C.qmin, std::pow(E, C.beta1) / C.gamma) : hs * C.qmin;
+      h = hs * (double)gbde::ctl_reject(C.k, E);
     }
     if (C.dtmax > 0.0) h = std::fmin(h, C.dtmax);
     if (ret == GBDE_RET_DEFAULT) {
@@ -1002,7 +993,9 @@ int oracle_ensemble_solve(const gbde_problem* P, const gbde_opts* O, gbde_output
   if (!P || !O || !out || !model_of(P->model, m)) return GBDE_ERR_INVALID;
   if (P->n_state != m.n || P->n_param != m.np || P->mem != GBDE_MEM_HOST) return GBDE_ERR_INVALID;
   Ctl C{O->abstol, O->reltol, O->qmin, O->qmax, O->gamma, O->beta1, O->beta2, O->qsteady_min,
-        O->qsteady_max, O->qoldinit, O->dtmin, O->dtmax, O->dt, O->maxiters, O->adaptive};
+        O->qsteady_max, O->qoldinit, O->dtmin, O->dtmax, O->dt, O->maxiters, O->adaptive,
+        gbde::ctl_consts(O->beta1, O->beta2, O->gamma, O->qmin, O->qmax, O->qsteady_min,
+                         O->qsteady_max, O->qoldinit)};
   const int alg = O->alg;
   const int64_t N = P->n_traj;
   std::atomic<int64_t> next{0};

@@ -360,3 +360,10 @@ def test_fma_peak_microbenchmark(de):
     f64 = ctx.fma_peak(0)
     f32 = ctx.fma_peak(1)
     assert f64 > 0.1 and f32 > f64
+
+
+def test_rcp64_within_one_ulp(de):
+    """The Newton-refined reciprocal of the hot loops (error norm, LU pivots,
+    1/dt) agrees with the device's IEEE division to one ulp."""
+    err = de._capi.context(0).check_rcp64(1 << 22)
+    assert err <= 2.0 ** -52, err
