@@ -59,6 +59,10 @@ def parse():
                     help="chosen form: plain | persistent | persistent-mixed")
     ap.add_argument("--cpu-sample", type=int, default=100000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="robertson",
+                    choices=["robertson", "lorenz", "lv_em", "lv_sosri", "vdp_auto"],
+                    help="robertson = the headline (default); the others print the line of "
+                         "another configuration")
     return ap.parse_args()
 
 
@@ -149,6 +153,184 @@ def cpu_reference(de, alg_id, args, N_sample, seed, threads):
     return N_sample / dt, dt, r
 
 
+# ------------------------------------------------------- other configurations
+# Each returns the inputs and the forms compared: (model, p, u0, t0, tf, saveat,
+# save_kind, plain_opts, chosen_opts, out dtypes, config dict, error kind).
+def other_workload(de, name, N, seed):
+    capi = de._capi
+    rng = np.random.default_rng(seed)
+
+    def opts(alg, **kw):
+        o = capi.opts_default(alg)
+        for k, v in kw.items():
+            setattr(o, k, v)
+        return o
+
+    if name == "lorenz":
+        p = np.array([10.0, 28.0, 8.0 / 3.0]) * rng.uniform(0.9, 1.1, (N, 3))
+        u0 = np.tile([1.0, 0.0, 0.0], (N, 1))
+        t0, tf = np.zeros(N), np.ones(N)
+        saveat = de.save_grid(0.0, 1.0, 0.1)
+        base = dict(reltol=1e-8, abstol=1e-8)
+        plain = opts(capi.ALG_TSIT5, **base)
+        chosen = opts(capi.ALG_TSIT5, batching=capi.BATCH_PERSISTENT, **base)
+        cfg = {"workload": "lorenz_tsit5_fp64_N%d" % N, "model": "lorenz", "alg": "tsit5",
+               "reltol": 1e-8, "abstol": 1e-8, "saveat": "0:0.1:1 (11 points)",
+               "chosen_form": "persistent fp64"}
+        return (de.models.lorenz, p, u0, t0, tf, saveat, capi.SAVE_GRID, plain, chosen,
+                ("f64", "f64"), cfg, "weighted")
+    if name in ("lv_em", "lv_sosri"):
+        p = np.c_[np.array([1.5, 1.0, 3.0, 1.0]) * rng.uniform(0.8, 1.2, (N, 4)), np.full(N, 0.1)]
+        u0 = np.ones((N, 2))
+        t0, tf = np.zeros(N), np.full(N, 10.0)
+        saveat = de.save_grid(0.0, 10.0, 1.0)
+        if name == "lv_em":
+            base = dict(dt=1e-3, seed=SEED)
+            plain = opts(capi.ALG_EM, **base)
+            chosen = opts(capi.ALG_EM, precision=capi.PREC_MIXED, **base)
+            cfg = {"workload": "lotka_volterra_em_N%d" % N, "alg": "em", "dt": 1e-3,
+                   "chosen_form": "FP32 state, FP64 time, FP32 noise stream"}
+        else:
+            base = dict(reltol=1e-3, abstol=1e-3, seed=SEED)
+            plain = opts(capi.ALG_SOSRI, **base)
+            chosen = opts(capi.ALG_SOSRI, precision=capi.PREC_MIXED,
+                          batching=capi.BATCH_PERSISTENT, **base)
+            cfg = {"workload": "lotka_volterra_sosri_N%d" % N, "alg": "sosri (SRIW1 + RSwM)",
+                   "reltol": 1e-3, "abstol": 1e-3,
+                   "chosen_form": "persistent, FP32 state, FP64 time"}
+        cfg.update({"model": "lotka_volterra", "noise": "diagonal 0.1 u",
+                    "saveat": "0:1:10 (11 points)"})
+        return (de.models.lotka_volterra, p, u0, t0, tf, saveat, capi.SAVE_GRID, plain, chosen,
+                ("f64", "f32"), cfg, "sde")
+    if name == "vdp_auto":
+        p = np.c_[10 ** rng.uniform(-1, 3, N), np.full(N, 0.05)]
+        u0 = rng.uniform(-2, 2, (N, 16))
+        t0, tf = np.zeros(N), np.full(N, 20.0)
+        saveat = de.save_grid(0.0, 20.0, 1.0)
+        base = dict(reltol=1e-5, abstol=1e-5, stiff_threshold=100.0, maxiters=10 ** 6)
+        plain = opts(capi.ALG_AUTO, **base)
+        chosen = opts(capi.ALG_AUTO, precision=capi.PREC_MIXED, batching=capi.BATCH_PERSISTENT,
+                      **base)
+        cfg = {"workload": "vdp_ring8_auto_N%d" % N, "model": "vdp_ring8 (16 states)",
+               "alg": "auto: tsit5 if mu <= 100 else rodas5", "reltol": 1e-5,
+               "saveat": "0:1:20 (21 points)",
+               "chosen_form": "persistent; Tsit5 FP32 compensated state, Rodas5 FP64"}
+        return (de.models.vdp_ring8, p, u0, t0, tf, saveat, capi.SAVE_GRID, plain, chosen,
+                ("f64", "f32"), cfg, "vdp")
+    raise ValueError(name)
+
+
+def run_other(args, de):
+    import torch
+    import oracle
+    capi = de._capi
+    N = args.trajectories
+    (model, p, u0, t0, tf, saveat, kind, plain, chosen, dts, cfg, ekind) = other_workload(
+        de, args.workload, N, SEED)
+    dev = torch.device("cuda", 0)
+    host = [np.ascontiguousarray(a) for a in (p, u0, t0, tf, saveat)]
+    dptr = [torch.from_numpy(a).to(dev) for a in host]
+    ctx = capi.context(0)
+    peak64, peak32 = ctx.fma_peak(0), ctx.fma_peak(1)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+
+    def timed(o, dt, K, W):
+        for _ in range(W):
+            de.solve_arrays(model, o, *dptr, kind, u_dtype=dt)
+        ts, r = [], None
+        for _ in range(K):
+            flush.zero_()
+            torch.cuda.synchronize()
+            r = de.solve_arrays(model, o, *dptr, kind, u_dtype=dt)
+            ts.append(r["device_ms"])
+        return float(np.median(ts)), r
+
+    with ClockSampler(0) as clk:
+        plain_ms, rp = timed(plain, dts[0], args.steps, args.warmup)
+        chosen_ms, rc = timed(chosen, dts[1], args.steps, args.warmup)
+    res = {k: {kk: (v.cpu().numpy() if v is not None else None) for kk, v in r.items()
+               if kk in ("u", "retcode", "naccept", "nreject")}
+           for k, r in (("plain", rp), ("chosen", rc))}
+    # accuracy on a sample against the FP64 oracle (same algorithm, same inputs)
+    rng = np.random.default_rng(1)
+    ns = min(N, 512 if ekind == "vdp" else 2000)
+    # SDE noise is keyed by the trajectory index: compare the leading block
+    idx = np.arange(ns) if ekind == "sde" else np.sort(rng.choice(N, ns, replace=False))
+    sub = [a[idx] for a in host[:4]]
+    acc = {}
+    if ekind == "weighted":
+        ref = oracle.solve(capi, model, plain, *sub, saveat, kind, nthreads=oracle.hardware_threads())
+        for f in ("plain", "chosen"):
+            acc[f] = oracle.weighted_error(res[f]["u"][idx], ref["u"], plain.abstol, plain.reltol)
+    elif ekind == "sde":
+        ref64 = oracle.solve(capi, model, plain, *sub, saveat, kind,
+                             nthreads=oracle.hardware_threads())
+        ref32 = oracle.solve(capi, model, plain, *sub, saveat, kind,
+                             nthreads=oracle.hardware_threads(), noise_f32=True)
+        rel = lambda u, r: float(np.max(np.abs(u - r) / np.abs(r)))
+        if plain.alg == capi.ALG_EM:
+            acc = {"plain_fp64_vs_oracle_identical_noise_rel": rel(res["plain"]["u"][idx], ref64["u"]),
+                   "chosen_fp32_vs_fp64_oracle_same_fp32_noise_rel":
+                       rel(res["chosen"]["u"][idx].astype(np.float64), ref32["u"])}
+        else:
+            w = lambda u, r: (np.abs(u - r) / (plain.abstol + plain.reltol * np.abs(r))).max(axis=(1, 2))
+            acc = {"plain_identical_path_fraction": float(np.mean(w(res["plain"]["u"][idx], ref64["u"]) <= 1e-6)),
+                   "chosen_weighted_median": float(np.median(w(res["chosen"]["u"][idx].astype(np.float64), ref32["u"])))}
+    else:  # vdp: per-partition FP64 oracle and a reltol-1e-10 truth
+        st = sub[0][:, 0] > plain.stiff_threshold
+        ref = np.empty((ns, len(saveat), 16))
+        for mask, alg in ((~st, capi.ALG_TSIT5), (st, capi.ALG_RODAS5)):
+            if mask.any():
+                o = capi.opts_default(alg)
+                o.reltol, o.abstol, o.maxiters = plain.reltol, plain.abstol, plain.maxiters
+                ref[mask] = oracle.solve(capi, model, o, *[a[mask] for a in sub], saveat, kind,
+                                         nthreads=oracle.hardware_threads())["u"]
+        o = capi.opts_default(capi.ALG_RODAS5)
+        o.reltol = o.abstol = 1e-10
+        o.maxiters = 10 ** 7
+        truth = oracle.solve(capi, model, o, *sub, saveat, kind, nthreads=oracle.hardware_threads())["u"]
+        w = lambda u, r: (np.abs(np.asarray(u, np.float64) - r) / (1e-5 + 1e-5 * np.abs(r))).max(axis=(1, 2))
+        for f in ("plain", "chosen"):
+            e_o, e_t = w(res[f]["u"][idx], ref), w(res[f]["u"][idx], truth)
+            acc[f] = {"vs_oracle_p50": float(np.median(e_o)), "vs_oracle_p90": float(np.percentile(e_o, 90)),
+                      "vs_truth_p50": float(np.median(e_t)), "vs_truth_p90": float(np.percentile(e_t, 90))}
+        e_ot = w(ref, truth)
+        acc["fp64_oracle_vs_truth"] = {"p50": float(np.median(e_ot)), "p90": float(np.percentile(e_ot, 90))}
+    # CPU baseline: the oracle on a bounded sample, all host threads
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = oracle.hardware_threads()
+        # a sample of the same distribution sized for ~0.2-2 s on 16 cores
+        nc = {"lorenz": 200000, "lv_em": 8000, "lv_sosri": 40000, "vdp_auto": 8000}[args.workload]
+        big = other_workload(de, args.workload, nc, SEED + 1)
+        sub = [np.ascontiguousarray(a) for a in big[1:5]]
+        t = time.perf_counter()
+        if ekind == "vdp":
+            st = sub[0][:, 0] > plain.stiff_threshold
+            for mask, alg in ((~st, capi.ALG_TSIT5), (st, capi.ALG_RODAS5)):
+                o = capi.opts_default(alg)
+                o.reltol, o.abstol, o.maxiters = plain.reltol, plain.abstol, plain.maxiters
+                oracle.solve(capi, model, o, *[a[mask] for a in sub], saveat, kind, nthreads=threads)
+        else:
+            oracle.solve(capi, model, plain, *sub, saveat, kind, nthreads=threads)
+        dtc = time.perf_counter() - t
+        cpu = {"value": nc / dtc, "unit": "trajectories/s", "cores": threads, "kind": "port",
+               "sample": "%d trajectories in %.2f s (C++ FP64 restatement, std::thread pool)" % (nc, dtc)}
+    line = {"metric": "trajectories/sec at <=10x reltol error vs FP64 oracle",
+            "value": N / (chosen_ms * 1e-3), "unit": "trajectories/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": chosen_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "data": "synthetic (seeded, config distributions)",
+            "config": dict(cfg, trajectories=N, l2="flushed between timed steps (256 MB write)"),
+            "plain": {"value": N / (plain_ms * 1e-3), "ms_per_step": plain_ms},
+            "speedup_vs_plain": plain_ms / chosen_ms, "accuracy": acc,
+            "steps_per_traj_mean": float((res["chosen"]["naccept"] + res["chosen"]["nreject"]).mean()),
+            "all_success": bool(np.all(res["chosen"]["retcode"] == capi.RET_SUCCESS)),
+            "fp64_peak_tflops": peak64, "fp32_peak_tflops": peak32,
+            "clocks": clk.summary(), "cpu_baseline": cpu}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
@@ -156,6 +338,12 @@ def main():
     de = __graft_entry__.load_package()
     capi = de._capi
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    if args.workload != "robertson":
+        if args.impl == "reference":
+            raise SystemExit("--impl reference times the headline workload only")
+        if "--trajectories" not in sys.argv:
+            args.trajectories = {"lorenz": 10000}.get(args.workload, 1000000)
+        return run_other(args, de)
     alg_id = capi.ALG_RODAS5 if args.alg == "rodas5" else capi.ALG_ROSENBROCK23
     config = {"workload": "robertson_%s_fp64_N%d" % (args.alg, args.trajectories),
               "model": "robertson", "alg": args.alg, "trajectories": args.trajectories,

@@ -483,7 +483,7 @@ def solve_arrays(model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", d
             "retcode": torch.empty(N, dtype=torch.int32, device=dev),
         }
         if stats and out is None:
-            for k in ("naccept", "nreject", "nf"):
+            for k in ("naccept", "nreject", "nf", "method"):
                 res[k] = torch.empty(N, dtype=torch.int32, device=dev)
             res["t_end"] = torch.empty(N, dtype=torch.float64, device=dev)
         ctx.set_stream(torch.cuda.current_stream(dev).cuda_stream)
@@ -498,7 +498,7 @@ def solve_arrays(model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", d
             "retcode": np.empty(N, np.int32),
         }
         if stats and out is None:
-            for k in ("naccept", "nreject", "nf"):
+            for k in ("naccept", "nreject", "nf", "method"):
                 res[k] = np.empty(N, np.int32)
             res["t_end"] = np.empty(N, np.float64)
         ctx.set_stream(0)
@@ -508,7 +508,7 @@ def solve_arrays(model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", d
     for k in ("naccept", "nreject", "nf", "t_end", "method"):
         if k in res:
             setattr(outs, k, capi.ptr(res[k]))
-    for k in ("naccept", "nreject", "nf", "t_end"):
+    for k in ("naccept", "nreject", "nf", "t_end", "method"):
         res.setdefault(k, None)
     ctx.solve(prob, opts, outs)
     res["device_ms"] = outs.device_ms

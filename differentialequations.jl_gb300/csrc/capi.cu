@@ -60,6 +60,8 @@ struct gbde_ctx {
   DevBuf p, u0, t0, tf, saveat, u, ret, nacc, nrej, nf, tend, method;
   DevBuf work;  // queue counter + status flag
   DevBuf order; // persistent queue order (longest span first) + sort counters
+  DevBuf part;  // GBDE_ALG_AUTO: non-stiff and stiff trajectory lists
+  DevBuf pred_stiff;  // learned stiff / non-stiff labels (int8 per trajectory)
   // learned predictor (filled by the MLP entry points)
   DevBuf pred_dt;
 };
@@ -89,6 +91,18 @@ namespace gbde {
 int set_thread_error(int code, const char* msg) {
   g_thread_err = msg;
   return code;
+}
+
+// One algorithm over a (sub)ensemble: team kernels for the 16-state ring,
+// one thread per trajectory otherwise.
+cudaError_t launch_alg(int alg, LaunchCfg cfg, const KArgs& a, cudaStream_t s) {
+  cfg.alg = alg;
+  if (cfg.model == GBDE_MODEL_VDP_RING8 &&
+      (alg == GBDE_ALG_TSIT5 || alg == GBDE_ALG_RODAS5 || alg == GBDE_ALG_RODAS5P))
+    return launch_team(cfg, a, s);
+  if (alg == GBDE_ALG_TSIT5 || alg == GBDE_ALG_VERN7) return launch_explicit(cfg, a, s);
+  if (alg == GBDE_ALG_EM || alg == GBDE_ALG_SOSRI) return launch_sde(cfg, a, s);
+  return launch_rosenbrock(cfg, a, s);
 }
 
 int ctx_device(const gbde_ctx* ctx, int* device, int* num_sms, cudaStream_t* stream) {
@@ -156,7 +170,7 @@ int gbde_ctx_destroy(gbde_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf* b : {&ctx->p, &ctx->u0, &ctx->t0, &ctx->tf, &ctx->saveat, &ctx->u, &ctx->ret,
                     &ctx->nacc, &ctx->nrej, &ctx->nf, &ctx->tend, &ctx->method, &ctx->work,
-                    &ctx->order, &ctx->pred_dt})
+                    &ctx->order, &ctx->part, &ctx->pred_stiff, &ctx->pred_dt})
     b->release();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -221,9 +235,10 @@ int gbde_opts_default(int32_t alg, gbde_opts* o) {
       o->reltol = 1e-2;
       o->abstol = 1e-2;
       break;
-    case GBDE_ALG_AUTO:
+    case GBDE_ALG_AUTO:  // Tsit5's PI constants for both methods
       o->beta2 = 0.04;
-      o->beta1 = 0.17;
+      o->beta1 = 0.2 - 0.75 * 0.04;
+      o->stiff_threshold = 30.0;
       break;
     default:
       return set_err(nullptr, GBDE_ERR_INVALID, "unknown algorithm id %d", alg);
@@ -236,6 +251,57 @@ static bool is_ode_alg(int a) {
          a == GBDE_ALG_RODAS5 || a == GBDE_ALG_RODAS5P || a == GBDE_ALG_AUTO;
 }
 static bool is_sde_alg(int a) { return a == GBDE_ALG_EM || a == GBDE_ALG_SOSRI; }
+
+// GBDE_ALG_AUTO: classify every trajectory (stiff iff p[0] > stiff_threshold,
+// or the learned predictor's label), then run the non-stiff list with Tsit5
+// (FP32 state in mixed precision) and the stiff list with Rodas5 (FP64).
+// The options' controller exponents (Tsit5's by default) drive the Tsit5
+// part; the Rodas5 part uses Rodas5's default exponents.
+static int solve_auto(gbde_ctx* ctx, const LaunchCfg& cfg, const KArgs& a, int np,
+                      const gbde_opts* opts, cudaStream_t s) {
+  const int64_t N = a.N;
+  if (N == 0) return GBDE_OK;
+  unsigned long long* work = (unsigned long long*)ctx->work.ptr;
+  unsigned* counters = reinterpret_cast<unsigned*>(work + 3);
+  GBDE_CUDA(ctx, ctx->part.ensure(partition_scratch_bytes(N)));
+  int32_t *nonstiff = nullptr, *stiff = nullptr;
+  const int8_t* pred = opts->learned ? (const int8_t*)ctx->pred_stiff.ptr : nullptr;
+  GBDE_CUDA(ctx, build_partition(a.p, np, opts->stiff_threshold, pred, N, ctx->part.ptr,
+                                 counters, ctx->num_sms, s, &nonstiff, &stiff));
+  unsigned cnt[2] = {0, 0};
+  GBDE_CUDA(ctx, cudaMemcpyAsync(cnt, counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+  GBDE_CUDA(ctx, cudaStreamSynchronize(s));
+  const struct {
+    int alg, precision;
+    unsigned n;
+    const int32_t* list;
+    unsigned long long* queue;
+  } parts[2] = {{GBDE_ALG_TSIT5, cfg.precision, cnt[0], nonstiff, work},
+                {GBDE_ALG_RODAS5, GBDE_PREC_FP64, cnt[1], stiff, work + 2}};
+  for (const auto& part : parts) {
+    if (part.n == 0) continue;
+    KArgs b = a;
+    b.N = part.n;
+    b.order = part.list;
+    b.queue = cfg.persistent ? part.queue : nullptr;
+    if (part.alg == GBDE_ALG_RODAS5) {
+      // the stiff part runs with Rodas5's own controller exponents
+      gbde_opts r;
+      gbde_opts_default(GBDE_ALG_RODAS5, &r);
+      b.ctl = ctl_consts(r.beta1, r.beta2, opts->gamma, opts->qmin, opts->qmax,
+                         opts->qsteady_min, opts->qsteady_max, opts->qoldinit);
+    }
+    LaunchCfg c = cfg;
+    c.precision = part.precision;
+    const cudaError_t e = launch_alg(part.alg, c, b, s);
+    if (e == cudaErrorNotSupported)
+      return set_err(ctx, GBDE_ERR_UNSUPPORTED, "GBDE_ALG_AUTO is not built for model %d",
+                     cfg.model);
+    if (e != cudaSuccess)
+      return set_err(ctx, GBDE_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+  }
+  return GBDE_OK;
+}
 
 int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts* opts,
                         gbde_outputs* out) {
@@ -284,12 +350,11 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
     return set_err(ctx, GBDE_ERR_INVALID, "controller needs qmin > 0, qmax >= 1, gamma > 0");
   if (opts->learned && ctx->pred_dt.ptr == nullptr)
     return set_err(ctx, GBDE_ERR_STATE, "learned=1 but no predictor output is available");
-  if ((alg == GBDE_ALG_ROSENBROCK23 || alg == GBDE_ALG_RODAS5 || alg == GBDE_ALG_RODAS5P) &&
-      prob->model == GBDE_MODEL_VDP_RING8)
+  if (alg == GBDE_ALG_ROSENBROCK23 && prob->model == GBDE_MODEL_VDP_RING8)
     return set_err(ctx, GBDE_ERR_UNSUPPORTED,
-                   "one-thread-per-trajectory Rosenbrock kernels support n_state <= 3");
-  if (alg == GBDE_ALG_AUTO)
-    return set_err(ctx, GBDE_ERR_UNSUPPORTED, "GBDE_ALG_AUTO is not available in this build");
+                   "Rosenbrock23 is built for n_state <= 3 (use Rodas5 / Rodas5P for the ring)");
+  if (alg == GBDE_ALG_AUTO && N > INT32_MAX)
+    return set_err(ctx, GBDE_ERR_INVALID, "GBDE_ALG_AUTO supports n_traj < 2^31");
 
   GBDE_CUDA(ctx, cudaSetDevice(ctx->device));
   cudaStream_t s = ctx->stream;
@@ -387,18 +452,18 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
     return set_err(ctx, GBDE_ERR_INVALID, "block_size must be a multiple of 32 and <= 128");
 
   GBDE_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
-  if (cfg.persistent && N > 1 && N <= INT32_MAX) {
+  if (alg == GBDE_ALG_AUTO) {
+    const int rc = solve_auto(ctx, cfg, a, np, opts, s);
+    if (rc != GBDE_OK) return rc;
+  } else if (cfg.persistent && N > 1 && N <= INT32_MAX) {
     // queue order: longest spans first (order.cu)
     GBDE_CUDA(ctx, ctx->order.ensure(span_order_scratch_bytes(N)));
     const int32_t* ord = nullptr;
     GBDE_CUDA(ctx, build_span_order(a.t0, a.tf, N, ctx->order.ptr, ctx->num_sms, s, &ord));
     a.order = ord;
   }
-  if (N > 0) {
-    cudaError_t e;
-    if (alg == GBDE_ALG_TSIT5 || alg == GBDE_ALG_VERN7) e = launch_explicit(cfg, a, s);
-    else if (is_sde_alg(alg)) e = launch_sde(cfg, a, s);
-    else e = launch_rosenbrock(cfg, a, s);
+  if (N > 0 && alg != GBDE_ALG_AUTO) {
+    const cudaError_t e = launch_alg(alg, cfg, a, s);
     if (e == cudaErrorNotSupported)
       return set_err(ctx, GBDE_ERR_UNSUPPORTED, "algorithm %d is not built for model %d", alg,
                      prob->model);

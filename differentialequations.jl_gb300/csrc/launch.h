@@ -48,4 +48,37 @@ cudaError_t launch_kernel(K kern, const LaunchCfg& cfg, const KArgs& a, cudaStre
   return cudaGetLastError();
 }
 
+// Any ODE/SDE algorithm id except GBDE_ALG_AUTO (capi.cu).
+cudaError_t launch_alg(int alg, LaunchCfg cfg, const KArgs& a, cudaStream_t s);
+
+// Stiff / non-stiff lists for GBDE_ALG_AUTO (auto.cu).
+size_t partition_scratch_bytes(int64_t n);
+cudaError_t build_partition(const double* p, int np, double thr, const int8_t* pred, int64_t n,
+                            void* scratch, unsigned* counters, int num_sms, cudaStream_t s,
+                            int32_t** nonstiff, int32_t** stiff);
+
+// Team kernels (team.cuh): 16 threads per trajectory.
+cudaError_t launch_team(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
+
+template <class K>
+cudaError_t launch_team_kernel(K kern, const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
+  const int block = cfg.block > 0 ? cfg.block : 128;
+  const long long need = (a.N * 16 + block - 1) / block;
+  int grid;
+  if (cfg.persistent) {
+    int per_sm = cfg.ctas_per_sm;
+    if (per_sm <= 0) {
+      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, 0);
+      if (e != cudaSuccess) return e;
+      if (per_sm < 1) per_sm = 1;
+    }
+    grid = per_sm * cfg.num_sms;
+    if (grid > need) grid = (int)(need > 0 ? need : 1);
+  } else {
+    grid = (int)(need > 0 ? need : 1);
+  }
+  kern<<<grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 }  // namespace gbde

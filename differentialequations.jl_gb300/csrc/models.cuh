@@ -87,6 +87,46 @@ struct VdpRing8 {
       J[2 * i + 1][2 * ((i + 1) & 7)] += ka;
     }
   }
+  // Team kernels (team.cuh): lane r owns component r; `sh.bcast(v, src)`
+  // reads lane src's value of v.  f_lane returns f_r(u); jac_lane fills row r
+  // of the Jacobian.  Only the components row r depends on are fetched.
+  template <class T, class Sh>
+  GBDE_D static void ring_neighbours(int r, T y, const Sh& sh, T& x, T& v, T& xl, T& xr) {
+    const int e = r & ~1;
+    x = sh.bcast(y, e);
+    v = sh.bcast(y, e | 1);
+    xl = sh.bcast(y, (e + 14) & 15);
+    xr = sh.bcast(y, (e + 2) & 15);
+  }
+  template <class T, class Sh>
+  GBDE_D static T f_lane(int r, T y, const T* p, const Sh& sh) {
+    T x, v, xl, xr;
+    ring_neighbours(r, y, sh, x, v, xl, xr);
+    const T dv = p[0] * (T(1) - x * x) * v - x + p[1] * (xl - T(2) * x + xr);
+    return (r & 1) ? dv : v;
+  }
+  template <class T, class Sh>
+  GBDE_D static void jac_lane(int r, T y, const T* p, const Sh& sh, T* Jr) {
+    T x, v, xl, xr;
+    ring_neighbours(r, y, sh, x, v, xl, xr);
+    const T mu = p[0], ka = p[1];
+    const int e = r & ~1;
+    const bool odd = r & 1;
+    const T dx = T(-2) * mu * x * v - T(1) - T(2) * ka, dvv = mu * (T(1) - x * x);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      T val = T(0);
+      if (odd) {
+        if (c == e) val = dx;
+        if (c == e + 1) val = dvv;
+        if (c == ((e + 14) & 15)) val += ka;
+        if (c == ((e + 2) & 15)) val += ka;
+      } else if (c == r + 1) {
+        val = T(1);
+      }
+      Jr[c] = val;
+    }
+  }
   // Row r of the Jacobian (for the warp-cooperative Rosenbrock path).
   template <class T> GBDE_HD static T jac_entry(int r, int c, const T* u, const T* p) {
     const T mu = p[0], ka = p[1];

@@ -135,7 +135,9 @@ extern "C" int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_
     return fail(GBDE_ERR_INVALID, "u_dtype must be GBDE_F64 or GBDE_F32");
   const int alg = opts->alg;
   if (alg == GBDE_ALG_AUTO)
-    return fail(GBDE_ERR_UNSUPPORTED, "GBDE_ALG_AUTO is not available in this build");
+    return fail(GBDE_ERR_UNSUPPORTED,
+                "GBDE_ALG_AUTO needs per-trajectory lists (device scratch that grows with "
+                "n_traj): use gbde_ensemble_solve");
   if (!is_ode(alg) && !is_sde(alg)) return fail(GBDE_ERR_INVALID, "unknown algorithm id %d", alg);
   if (is_sde(alg) && prob->model != GBDE_MODEL_LOTKA_VOLTERRA)
     return fail(GBDE_ERR_UNSUPPORTED, "SDE algorithms need a model with a noise term");
@@ -152,10 +154,9 @@ extern "C" int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_
     return fail(GBDE_ERR_INVALID, "controller needs qmin > 0, qmax >= 1, gamma > 0");
   if (opts->learned)
     return fail(GBDE_ERR_STATE, "gbde_ensemble_solve_noalloc has no learned predictor (learned=1)");
-  if ((alg == GBDE_ALG_ROSENBROCK23 || alg == GBDE_ALG_RODAS5 || alg == GBDE_ALG_RODAS5P) &&
-      prob->model == GBDE_MODEL_VDP_RING8)
+  if (alg == GBDE_ALG_ROSENBROCK23 && prob->model == GBDE_MODEL_VDP_RING8)
     return fail(GBDE_ERR_UNSUPPORTED,
-                "one-thread-per-trajectory Rosenbrock kernels support n_state <= 3");
+                "Rosenbrock23 is built for n_state <= 3 (use Rodas5 / Rodas5P for the ring)");
   const int block = opts->block_size > 0 ? opts->block_size : 128;
   if (block > 128 || (block & 31))
     return fail(GBDE_ERR_INVALID, "block_size must be a multiple of 32 and <= 128");
@@ -231,10 +232,7 @@ extern "C" int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_
   cfg.num_sms = dev.num_sms;
 
   if (N > 0) {
-    cudaError_t e;
-    if (alg == GBDE_ALG_TSIT5 || alg == GBDE_ALG_VERN7) e = launch_explicit(cfg, a, s);
-    else if (is_sde(alg)) e = launch_sde(cfg, a, s);
-    else e = launch_rosenbrock(cfg, a, s);
+    const cudaError_t e = launch_alg(alg, cfg, a, s);
     if (e == cudaErrorNotSupported)
       return fail(GBDE_ERR_UNSUPPORTED, "algorithm %d is not built for model %d", alg, prob->model);
     if (e != cudaSuccess) return fail(GBDE_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));

@@ -75,7 +75,8 @@ struct WorkSource {
     if (a.queue == nullptr) {
       if (used) return -1;
       used = true;
-      return first < a.N ? first : -1;
+      if (first >= a.N) return -1;
+      return a.order ? (int64_t)a.order[first] : first;
     }
     namespace cg = cooperative_groups;
     cg::coalesced_group g = cg::coalesced_threads();

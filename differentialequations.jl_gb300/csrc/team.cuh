@@ -1,0 +1,410 @@
+// team.cuh -- trajectories that do not fit one thread: a team of W = 16
+// lanes (half a warp) integrates one trajectory of a 16-state model, lane r
+// owning state component r, row r of the Jacobian and row r of the W-matrix.
+//
+// Used for the ring of 8 Van der Pol oscillators (n = 16).  One thread per
+// trajectory would need the 16x16 FP64 W-matrix (2 KB) and 7-8 stage vectors
+// of 16 in registers, which spills; split over 16 lanes, each lane holds one
+// row and one component of every stage.
+//   * RHS: each lane evaluates its own row f_r(u) (M::f_lane), fetching the
+//     few components that row depends on from the other lanes by shuffles.
+//   * Error norm: a butterfly sum over the team; every lane then takes the
+//     same accept/reject decision, so control flow stays team-uniform.
+//   * LU with partial pivoting, distributed by rows without moving rows: at
+//     step k the team picks the unpivoted row with the largest |a_k| (shuffle
+//     max on the magnitude bits + ballot), broadcasts that row and every
+//     unpivoted lane eliminates.  Triangular solves run in pivot order.
+//   * Saves: the 16 lanes store the 16 components of a save point as one
+//     contiguous, coalesced 128-byte (FP64) or 64-byte (FP32) segment.
+#pragma once
+#include "rosenbrock.cuh"
+#include "explicit_rk.cuh"
+
+namespace gbde {
+
+constexpr int TEAM = 16;
+
+struct Team {
+  unsigned mask;  // the team's 16 lanes within the warp
+  int lane;       // 0..15
+  GBDE_D void init() {
+    const int l = threadIdx.x & 31;
+    lane = l & (TEAM - 1);
+    mask = 0xFFFFu << (l & TEAM);
+  }
+  template <class T> GBDE_D T bcast(T v, int src) const { return __shfl_sync(mask, v, src, TEAM); }
+  GBDE_D double sum(double v) const {
+#pragma unroll
+    for (int o = TEAM / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o, TEAM);
+    return v;
+  }
+};
+
+// ------------------------------------------------------------- team LU
+// Row-distributed LU of W (16 x 16) with partial pivoting.  Lane r keeps its
+// row in a[]: after factor(), a[c] for c < step holds the multipliers (L) and
+// a[c] for c >= step the U entries, where `step` is the elimination step at
+// which row r was the pivot.  piv packs the pivot lane of step k in bits
+// [4k, 4k+4).
+struct TeamLU {
+  double a[TEAM];
+  double invp;   // 1 / pivot of this lane's step
+  int step;
+  uint64_t piv;
+
+  GBDE_D void factor(const Team& tm) {
+    step = -1;
+    piv = 0;
+    invp = 0.0;
+#pragma unroll
+    for (int k = 0; k < TEAM; ++k) {
+      // pivot: unpivoted lane with the largest |a_k| (ties: lowest lane)
+      const uint64_t key = step < 0 ? mag_bits(a[k]) + 1ull : 0ull;
+      uint64_t m = key;
+#pragma unroll
+      for (int o = TEAM / 2; o > 0; o >>= 1) {
+        const uint64_t x = __shfl_xor_sync(tm.mask, m, o, TEAM);
+        m = x > m ? x : m;
+      }
+      const unsigned bal = __ballot_sync(tm.mask, key == m) >> ((threadIdx.x & 31) & TEAM);
+      const int p = __ffs(bal) - 1;
+      piv |= (uint64_t)p << (4 * k);
+      double prow[TEAM];
+#pragma unroll
+      for (int c = k; c < TEAM; ++c) prow[c] = tm.bcast(a[c], p);
+      const double inv = rcp64(prow[k]);
+      if (tm.lane == p) {
+        step = k;
+        invp = inv;
+      } else if (step < 0) {
+        const double l = a[k] * inv;
+        a[k] = l;
+#pragma unroll
+        for (int c = k + 1; c < TEAM; ++c) a[c] = fma(-l, prow[c], a[c]);
+      }
+    }
+  }
+
+  GBDE_D int pivot_lane(int k) const { return (int)((piv >> (4 * k)) & 15u); }
+
+  // Solve W x = b; b is this lane's right-hand side component, the return
+  // value this lane's component of x.
+  GBDE_D double solve(double b, const Team& tm) const {
+#pragma unroll
+    for (int k = 0; k < TEAM; ++k) {  // forward: L z = P b
+      const double z = tm.bcast(b, pivot_lane(k));
+      if (step > k) b = fma(-a[k], z, b);
+    }
+    double x = 0.0;
+#pragma unroll
+    for (int k = TEAM - 1; k >= 0; --k) {  // backward: U x = z
+      const double xk = tm.bcast(b * invp, pivot_lane(k));
+      if (step < k) b = fma(-a[k], xk, b);
+      if (tm.lane == k) x = xk;
+    }
+    return x;
+  }
+};
+
+// ------------------------------------------------ team Rodas5 / Rodas5P
+// Same transformed form as RodasAlg (rosenbrock.cuh), one component per lane.
+template <class M, class T, class Tag>
+struct TeamRodas {
+  using K = RodasCoef<Tag>;
+  static constexpr int ORDER = 4, ALG_ID = K::ALG_ID;
+  static_assert(M::N == TEAM, "team kernels are for 16-state models");
+  T uu, un, F0, s1, s2, s3, s4, s5, s6, s7;
+  T Jr[TEAM];  // row r of the Jacobian at uu
+  bool fresh;
+
+  GBDE_D T u() const { return uu; }
+  GBDE_D T unew() const { return un; }
+  GBDE_D T f0() const { return F0; }
+
+  GBDE_D T rhs(T y, const T* p, const Team& tm) const { return M::f_lane(tm.lane, y, p, tm); }
+
+  GBDE_D void refresh(const T* p, const Team& tm) {
+    F0 = M::f_lane(tm.lane, uu, p, tm);
+    M::jac_lane(tm.lane, uu, p, tm, Jr);
+    fresh = true;
+  }
+
+  GBDE_D void init(T u0, const T* p, const Team& tm, int& nf) {
+    uu = u0;
+    refresh(p, tm);
+    ++nf;
+  }
+
+  GBDE_D double attempt(double dt, const T* p, double abstol, double reltol, const Team& tm,
+                        int& nf) {
+    if (!fresh) {
+      refresh(p, tm);
+      ++nf;
+    }
+    TeamLU W;
+    const double ih = rcp64(dt);
+    const double dg = ih * (1.0 / K::g);
+#pragma unroll
+    for (int c = 0; c < TEAM; ++c) W.a[c] = c == tm.lane ? dg - (double)Jr[c] : -(double)Jr[c];
+    W.factor(tm);
+    const T c21 = T(K::C21 * ih), c31 = T(K::C31 * ih), c32 = T(K::C32 * ih);
+    const T c41 = T(K::C41 * ih), c42 = T(K::C42 * ih), c43 = T(K::C43 * ih);
+    const T c51 = T(K::C51 * ih), c52 = T(K::C52 * ih), c53 = T(K::C53 * ih),
+            c54 = T(K::C54 * ih);
+    const T c61 = T(K::C61 * ih), c62 = T(K::C62 * ih), c63 = T(K::C63 * ih),
+            c64 = T(K::C64 * ih), c65 = T(K::C65 * ih);
+    const T c71 = T(K::C71 * ih), c72 = T(K::C72 * ih), c73 = T(K::C73 * ih),
+            c74 = T(K::C74 * ih), c75 = T(K::C75 * ih), c76 = T(K::C76 * ih);
+    const T c81 = T(K::C81 * ih), c82 = T(K::C82 * ih), c83 = T(K::C83 * ih),
+            c84 = T(K::C84 * ih), c85 = T(K::C85 * ih), c86 = T(K::C86 * ih),
+            c87 = T(K::C87 * ih);
+    s1 = (T)W.solve((double)F0, tm);
+    T y = uu + T(K::a21) * s1;
+    s2 = (T)W.solve((double)(rhs(y, p, tm) + c21 * s1), tm);
+    y = uu + T(K::a31) * s1 + T(K::a32) * s2;
+    s3 = (T)W.solve((double)(rhs(y, p, tm) + c31 * s1 + c32 * s2), tm);
+    y = uu + T(K::a41) * s1 + T(K::a42) * s2 + T(K::a43) * s3;
+    s4 = (T)W.solve((double)(rhs(y, p, tm) + c41 * s1 + c42 * s2 + c43 * s3), tm);
+    y = uu + T(K::a51) * s1 + T(K::a52) * s2 + T(K::a53) * s3 + T(K::a54) * s4;
+    s5 = (T)W.solve((double)(rhs(y, p, tm) + c51 * s1 + c52 * s2 + c53 * s3 + c54 * s4), tm);
+    y = uu + T(K::a61) * s1 + T(K::a62) * s2 + T(K::a63) * s3 + T(K::a64) * s4 +
+        T(K::a65) * s5;
+    s6 = (T)W.solve((double)(rhs(y, p, tm) + c61 * s1 + c62 * s2 + c63 * s3 + c64 * s4 +
+                             c65 * s5), tm);
+    y += s6;
+    s7 = (T)W.solve((double)(rhs(y, p, tm) + c71 * s1 + c72 * s2 + c73 * s3 + c74 * s4 +
+                             c75 * s5 + c76 * s6), tm);
+    y += s7;
+    const T s8 = (T)W.solve((double)(rhs(y, p, tm) + c81 * s1 + c82 * s2 + c83 * s3 +
+                                     c84 * s4 + c85 * s5 + c86 * s6 + c87 * s7), tm);
+    nf += 7;
+    un = y + s8;
+    const double sc = abstol + reltol * fmax(fabs((double)uu), fabs((double)un));
+    const double e = (double)s8 * rcp64(sc);
+    return tm.sum(e * e) * (1.0 / TEAM);
+  }
+
+  GBDE_D T interp(double th, double) const {
+    const T a = (T)(1.0 - th), b = (T)th, w = (T)(th * (1.0 - th)), tt = (T)th;
+    const T k2 = T(K::H2[0]) * s1 + T(K::H2[1]) * s2 + T(K::H2[2]) * s3 + T(K::H2[3]) * s4 +
+                 T(K::H2[4]) * s5 + T(K::H2[5]) * s6 + T(K::H2[6]) * s7;
+    const T k3 = T(K::H3[0]) * s1 + T(K::H3[1]) * s2 + T(K::H3[2]) * s3 + T(K::H3[3]) * s4 +
+                 T(K::H3[4]) * s5 + T(K::H3[5]) * s6 + T(K::H3[6]) * s7;
+    const T k4 = T(K::H4[0]) * s1 + T(K::H4[1]) * s2 + T(K::H4[2]) * s3 + T(K::H4[3]) * s4 +
+                 T(K::H4[4]) * s5 + T(K::H4[5]) * s6 + T(K::H4[6]) * s7;
+    return a * uu + b * un + w * (k2 + tt * (k3 + tt * k4));
+  }
+
+  GBDE_D void accept() {
+    uu = un;
+    fresh = false;
+  }
+};
+
+// ------------------------------------------------------------ team Tsit5
+// Tsit5Alg (explicit_rk.cuh) with one component per lane; the FP32 path keeps
+// the compensated state uu + lo.
+template <class M, class T>
+struct TeamTsit5 {
+  static constexpr int ORDER = 5, ALG_ID = GBDE_ALG_TSIT5;
+  static constexpr bool CMP = sizeof(T) == 4;
+  static_assert(M::N == TEAM, "team kernels are for 16-state models");
+  T uu, un, lo, lon, k1, k2, k3, k4, k5, k6, k7;
+
+  GBDE_D T u() const { return uu; }
+  GBDE_D T unew() const { return un; }
+  GBDE_D T f0() const { return k1; }
+
+  GBDE_D T at(T inc) const {
+    if constexpr (CMP) return uu + (lo + inc);
+    else return uu + inc;
+  }
+  GBDE_D T rhs(T y, const T* p, const Team& tm) const { return M::f_lane(tm.lane, y, p, tm); }
+
+  GBDE_D void init(T u0, const T* p, const Team& tm, int& nf) {
+    uu = u0;
+    lo = T(0);
+    k1 = rhs(uu, p, tm);
+    ++nf;
+  }
+
+  GBDE_D double attempt(double dt, const T* p, double abstol, double reltol, const Team& tm,
+                        int& nf) {
+    using namespace tab::tsit5;
+    const T h = (T)dt;
+    k2 = rhs(at(h * (T(a21) * k1)), p, tm);
+    k3 = rhs(at(h * (T(a31) * k1 + T(a32) * k2)), p, tm);
+    k4 = rhs(at(h * (T(a41) * k1 + T(a42) * k2 + T(a43) * k3)), p, tm);
+    k5 = rhs(at(h * (T(a51) * k1 + T(a52) * k2 + T(a53) * k3 + T(a54) * k4)), p, tm);
+    k6 = rhs(at(h * (T(a61) * k1 + T(a62) * k2 + T(a63) * k3 + T(a64) * k4 + T(a65) * k5)), p,
+             tm);
+    const T inc = h * (T(a71) * k1 + T(a72) * k2 + T(a73) * k3 + T(a74) * k4 + T(a75) * k5 +
+                       T(a76) * k6);
+    if constexpr (CMP) two_sum_t(uu, lo + inc, un, lon);
+    else un = uu + inc;
+    k7 = rhs(un, p, tm);
+    nf += 6;
+    const T err = h * (T(bt1) * k1 + T(bt2) * k2 + T(bt3) * k3 + T(bt4) * k4 + T(bt5) * k5 +
+                       T(bt6) * k6 + T(bt7) * k7);
+    const double sc = abstol + reltol * fmax(fabs((double)uu), fabs((double)un));
+    const double e = (double)err * rcp64(sc);
+    return tm.sum(e * e) * (1.0 / TEAM);
+  }
+
+  GBDE_D T interp(double th, double dt) const {
+    using namespace tab::tsit5;
+    const double t2 = th * th;
+    const T b1 = (T)(r11 * th * (th - r12) * (t2 - r13 * th + r14));
+    const T b2 = (T)(r21 * t2 * (t2 - r22 * th + r23));
+    const T b3 = (T)(r31 * t2 * (t2 - r32 * th + r33));
+    const T b4 = (T)(r41 * (th - r42) * (th - r43) * t2);
+    const T b5 = (T)(r51 * (th - r52) * (th - r53) * t2);
+    const T b6 = (T)(r61 * (th - r62) * (th - r63) * t2);
+    const T b7 = (T)(r71 * (th - r72) * (th - r73) * t2);
+    const T h = (T)dt;
+    return at(h * (b1 * k1 + b2 * k2 + b3 * k3 + b4 * k4 + b5 * k5 + b6 * k6 + b7 * k7));
+  }
+
+  GBDE_D void accept() {
+    uu = un;
+    if constexpr (CMP) lo = lon;
+    k1 = k7;
+  }
+};
+
+// ----------------------------------------------------------- team driver
+// integrate_all (solver.cuh) for teams: the same controller, saves, return
+// codes and deadline; every scalar decision is team-uniform.
+template <class Alg, class M, class T, bool MIXED>
+__device__ void integrate_team(const KArgs& a) {
+  Team tm;
+  tm.init();
+  const int64_t team_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / TEAM;
+  const uint64_t t_start = a.timeout_ns ? global_ns() : 0;
+  bool first = true;
+  Alg alg;
+  T p[M::NP];
+  while (true) {
+    // ---- next trajectory (team-uniform)
+    int64_t i;
+    if (a.queue == nullptr) {
+      if (!first) break;
+      i = team_id < a.N ? (a.order ? (int64_t)a.order[team_id] : team_id) : -1;
+    } else {
+      unsigned long long idx = 0;
+      if (tm.lane == 0) idx = atomicAdd(a.queue, 1ull);
+      idx = tm.bcast(idx, 0);
+      i = idx < (unsigned long long)a.N ? (a.order ? (int64_t)a.order[idx] : (int64_t)idx) : -1;
+    }
+    first = false;
+    if (i < 0) break;
+#pragma unroll
+    for (int k = 0; k < M::NP; ++k) p[k] = (T)__ldg(a.p + (size_t)i * M::NP + k);
+    const T u0 = (T)__ldg(a.u0 + (size_t)i * TEAM + tm.lane);
+    double t = __ldg(a.t0 + i), tlo = 0.0;
+    const double tf = __ldg(a.tf + i);
+    int js = 0, nacc = 0, nrej = 0, nfev = 0;
+    int64_t iters = 0;
+    float lqold = a.ctl.lqoldinit;
+    int ret = GBDE_RET_DEFAULT;
+    const bool bad_lane = !isfinite((double)u0);
+    const bool bad = !(tf >= t) || !isfinite(t) || !isfinite(tf) ||
+                     __any_sync(tm.mask, bad_lane);
+    auto store = [&](int j, T v) {
+      const size_t o = ((size_t)i * a.n_save + j) * TEAM + tm.lane;
+      if (a.out_f32) ((float*)a.u_out)[o] = (float)v;
+      else ((double*)a.u_out)[o] = (double)v;
+    };
+    while (js < a.n_save && save_time(a, i, js) <= t) store(js++, u0);
+    double dt = 0.0;
+    if (bad) {
+      ret = GBDE_RET_INITIALFAILURE;
+    } else {
+      alg.init(u0, p, tm, nfev);
+      if (a.dt0 > 0.0 || !a.adaptive) {
+        dt = a.dt0;
+      } else {
+        // Hairer-Wanner starting step (hw_h0 / hw_dt, controller.h)
+        const double r = rcp64(a.abstol + fabs((double)alg.u()) * a.reltol);
+        const double x = (double)alg.u() * r, y = (double)alg.f0() * r;
+        const double s0 = tm.sum(x * x) * (1.0 / TEAM), s1 = tm.sum(y * y) * (1.0 / TEAM);
+        const double h0 = hw_h0(s0, s1, tf - t);
+        const T f1 = alg.rhs(alg.u() + T(h0) * alg.f0(), p, tm);
+        ++nfev;
+        const double z = ((double)f1 - (double)alg.f0()) * r;
+        dt = hw_dt(h0, s1, tm.sum(z * z) * (1.0 / TEAM), tf - t, Alg::ORDER);
+      }
+      if (a.dtmax > 0.0) dt = fmin(dt, a.dtmax);
+      if (!(t < tf)) ret = GBDE_RET_SUCCESS;
+      else if (!(dt > 0.0)) ret = GBDE_RET_DTLESSTHANMIN;
+    }
+    while (ret == GBDE_RET_DEFAULT) {
+      const double rem = tf - t;
+      double h = dt;
+      bool last = false;
+      if (h * (1.0 + 1e-10) >= rem) {
+        h = rem;
+        last = true;
+      }
+      const double ms = alg.attempt(h, p, a.abstol, a.reltol, tm, nfev);
+      ++iters;
+      if (!a.adaptive || ms <= 1.0) {
+        double dtnew = h;
+        if (a.adaptive) dtnew = h * (double)ctl_accept(a.ctl, ms, lqold);
+        double tnew;
+        if (last) {
+          tnew = tf;
+          tlo = 0.0;
+        } else if (MIXED) {
+          double s, e;
+          two_sum(t, h, s, e);
+          e += tlo;
+          tnew = s + e;
+          tlo = e - (tnew - s);
+        } else {
+          tnew = t + h;
+        }
+        while (js < a.n_save) {
+          const double ts = save_time(a, i, js);
+          if (!(ts <= tnew)) break;
+          store(js, ts >= tnew ? alg.unew() : alg.interp(((ts - t) - tlo) / h, h));
+          ++js;
+        }
+        alg.accept();
+        t = tnew;
+        ++nacc;
+        if (__any_sync(tm.mask, !isfinite((double)alg.u()))) ret = GBDE_RET_UNSTABLE;
+        else if (last) ret = GBDE_RET_SUCCESS;
+        dt = a.dtmax > 0.0 ? fmin(dtnew, a.dtmax) : dtnew;
+      } else {
+        ++nrej;
+        dt = h * (double)ctl_reject(a.ctl, ms);
+      }
+      if (ret == GBDE_RET_DEFAULT) {
+        if (iters >= a.maxiters) ret = GBDE_RET_MAXITERS;
+        else if (a.adaptive && (dt < a.dtmin || dt <= 4.0 * 2.220446049250313e-16 * fabs(t)))
+          ret = GBDE_RET_DTLESSTHANMIN;
+        else if (a.timeout_ns && (iters & 31) == 0) {
+          // lane 0's clock decides for the team
+          const int late = tm.bcast((int)(global_ns() - t_start > a.timeout_ns), 0);
+          if (late) {
+            ret = GBDE_RET_TIMEOUT;
+            if (tm.lane == 0) atomicOr(a.flag, 1);
+          }
+        }
+      }
+    }
+    const T nanv = (T)__longlong_as_double(0x7ff8000000000000ll);
+    for (; js < a.n_save; ++js) store(js, nanv);
+    if (tm.lane == 0) {
+      a.retcode[i] = ret;
+      if (a.naccept) a.naccept[i] = nacc;
+      if (a.nreject) a.nreject[i] = nrej;
+      if (a.nf) a.nf[i] = nfev;
+      if (a.t_end) a.t_end[i] = t + tlo;
+      if (a.method_out) a.method_out[i] = Alg::ALG_ID;
+    }
+  }
+}
+
+}  // namespace gbde

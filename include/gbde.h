@@ -72,7 +72,8 @@ extern "C" {
 #define GBDE_MODEL_LINEAR 1    /* n=1, p=[a]:           du = a*u (test/core.jl:10) */
 #define GBDE_MODEL_LORENZ 2    /* n=3, p=[sigma,rho,beta]          (test/core.jl:22-27) */
 #define GBDE_MODEL_ROBERTSON 3 /* n=3, p=[k1,k2,k3]                (test/core.jl:39-45) */
-#define GBDE_MODEL_VDP_RING8 4 /* n=16, p=[mu,kappa]: 8 Van der Pol oscillators on a ring */
+#define GBDE_MODEL_VDP_RING8 4 /* n=16, p=[mu,kappa]: 8 Van der Pol oscillators on a ring;
+                                  Tsit5 / Rodas5 / Rodas5P run 16 lanes per trajectory */
 #define GBDE_MODEL_LOTKA_VOLTERRA 5 /* n=2, p=[alpha,beta,gamma,delta,sigma]:
                                        drift [a x - b x y, d x y - g y],
                                        diagonal noise sigma*u (SDE)            */
@@ -86,8 +87,13 @@ extern "C" {
 #define GBDE_ALG_EM 6           /* Euler-Maruyama, fixed step                       */
 #define GBDE_ALG_SOSRI 7        /* SRI strong 1.5, adaptive with rejection sampling
                                    with memory                                      */
-#define GBDE_ALG_AUTO 8         /* per-trajectory Tsit5 / Rodas5 choice (threshold
-                                   on the stiffness parameter, or the learned MLP)  */
+#define GBDE_ALG_AUTO 8         /* per-trajectory Tsit5 / Rodas5 choice, made once
+                                   before integration: stiff iff p[0] >
+                                   stiff_threshold (or the learned predictor's label);
+                                   stands in for AutoTsit5(Rosenbrock23()),
+                                   test/qa/qa.jl:15.  Stiff trajectories always run
+                                   Rodas5 in FP64; with GBDE_PREC_MIXED the others run
+                                   Tsit5 with FP32 state.                             */
 
 /* ---- precision -------------------------------------------------------- */
 #define GBDE_PREC_FP64 0  /* everything in FP64                                  */
