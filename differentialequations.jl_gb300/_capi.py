@@ -66,8 +66,16 @@ class Outputs(C.Structure):
         ("u", C.c_void_p), ("u_dtype", C.c_int32), ("retcode", C.c_void_p),
         ("naccept", C.c_void_p), ("nreject", C.c_void_p), ("nf", C.c_void_p),
         ("t_end", C.c_void_p), ("method", C.c_void_p),
-        ("device_ms", C.c_float), ("total_ms", C.c_float),
+        ("device_ms", C.c_float), ("total_ms", C.c_float), ("dt_first", C.c_void_p),
     ]
+
+
+class MlpTrainOpts(C.Structure):
+    _fields_ = [("epochs", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float),
+                ("weight_decay", C.c_float), ("seed", C.c_uint64)]
+
+
+MLP_IN, MLP_PARAMS, MLP_NET_FLOATS = 8, 9026, 9044
 
 
 # Every function gbde.h declares, with its ctypes signature.
@@ -88,6 +96,14 @@ SIGNATURES = {
     "gbde_ensemble_solve_noalloc": (C.c_int, [C.POINTER(Problem), C.POINTER(Opts),
                                               C.POINTER(Outputs), C.c_void_p]),
     "gbde_check_rcp64": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double)]),
+    "gbde_mlp_init": (C.c_int, [C.c_uint64, C.c_void_p]),
+    "gbde_mlp_features": (C.c_int, [C.c_void_p, C.POINTER(Problem), C.c_void_p]),
+    "gbde_mlp_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                 C.POINTER(MlpTrainOpts), C.c_void_p, C.c_void_p]),
+    "gbde_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "gbde_mlp_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                C.c_void_p, C.POINTER(C.c_float)]),
+    "gbde_mlp_load": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
 }
 
 _lib = None

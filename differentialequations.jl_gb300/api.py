@@ -486,6 +486,7 @@ def solve_arrays(model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", d
             for k in ("naccept", "nreject", "nf", "method"):
                 res[k] = torch.empty(N, dtype=torch.int32, device=dev)
             res["t_end"] = torch.empty(N, dtype=torch.float64, device=dev)
+            res["dt_first"] = torch.empty(N, dtype=torch.float64, device=dev)
         ctx.set_stream(torch.cuda.current_stream(dev).cuda_stream)
         arrs = (p, u0, t0, tf, saveat)
     else:
@@ -501,14 +502,15 @@ def solve_arrays(model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", d
             for k in ("naccept", "nreject", "nf", "method"):
                 res[k] = np.empty(N, np.int32)
             res["t_end"] = np.empty(N, np.float64)
+            res["dt_first"] = np.empty(N, np.float64)
         ctx.set_stream(0)
     prob.p, prob.u0, prob.t0, prob.tf, prob.saveat = [capi.ptr(a) for a in arrs]
     outs.u = capi.ptr(res["u"])
     outs.retcode = capi.ptr(res["retcode"])
-    for k in ("naccept", "nreject", "nf", "t_end", "method"):
+    for k in ("naccept", "nreject", "nf", "t_end", "method", "dt_first"):
         if k in res:
             setattr(outs, k, capi.ptr(res[k]))
-    for k in ("naccept", "nreject", "nf", "t_end", "method"):
+    for k in ("naccept", "nreject", "nf", "t_end", "method", "dt_first"):
         res.setdefault(k, None)
     ctx.solve(prob, opts, outs)
     res["device_ms"] = outs.device_ms

@@ -62,6 +62,9 @@ struct gbde_ctx {
   DevBuf order; // persistent queue order (longest span first) + sort counters
   DevBuf part;  // GBDE_ALG_AUTO: non-stiff and stiff trajectory lists
   DevBuf pred_stiff;  // learned stiff / non-stiff labels (int8 per trajectory)
+  DevBuf dt1;         // staging of the first-accepted-step log (host calls)
+  DevBuf mlp_net;     // learned predictor (GBDE_MLP_NET_FLOATS floats)
+  int mlp_model = 0;  // model the loaded predictor belongs to (0 = none)
   // learned predictor (filled by the MLP entry points)
   DevBuf pred_dt;
 };
@@ -170,7 +173,8 @@ int gbde_ctx_destroy(gbde_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf* b : {&ctx->p, &ctx->u0, &ctx->t0, &ctx->tf, &ctx->saveat, &ctx->u, &ctx->ret,
                     &ctx->nacc, &ctx->nrej, &ctx->nf, &ctx->tend, &ctx->method, &ctx->work,
-                    &ctx->order, &ctx->part, &ctx->pred_stiff, &ctx->pred_dt})
+                    &ctx->order, &ctx->part, &ctx->pred_stiff, &ctx->pred_dt, &ctx->dt1,
+                    &ctx->mlp_net})
     b->release();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -348,8 +352,9 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
   if (opts->maxiters <= 0) return set_err(ctx, GBDE_ERR_INVALID, "maxiters must be > 0");
   if (opts->adaptive && !(opts->qmin > 0.0 && opts->qmax >= 1.0 && opts->gamma > 0.0))
     return set_err(ctx, GBDE_ERR_INVALID, "controller needs qmin > 0, qmax >= 1, gamma > 0");
-  if (opts->learned && ctx->pred_dt.ptr == nullptr)
-    return set_err(ctx, GBDE_ERR_STATE, "learned=1 but no predictor output is available");
+  if (opts->learned && ctx->mlp_model != prob->model)
+    return set_err(ctx, GBDE_ERR_STATE,
+                   "learned=1 needs a predictor for model %d (gbde_mlp_load)", prob->model);
   if (alg == GBDE_ALG_ROSENBROCK23 && prob->model == GBDE_MODEL_VDP_RING8)
     return set_err(ctx, GBDE_ERR_UNSUPPORTED,
                    "Rosenbrock23 is built for n_state <= 3 (use Rodas5 / Rodas5P for the ring)");
@@ -418,6 +423,7 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
     if (out->nf) { GBDE_CUDA(ctx, ctx->nf.ensure((size_t)N * 4)); a.nf = (int32_t*)ctx->nf.ptr; }
     if (out->t_end) { GBDE_CUDA(ctx, ctx->tend.ensure((size_t)N * 8)); a.t_end = (double*)ctx->tend.ptr; }
     if (out->method) { GBDE_CUDA(ctx, ctx->method.ensure((size_t)N * 4)); a.method_out = (int32_t*)ctx->method.ptr; }
+    if (out->dt_first) { GBDE_CUDA(ctx, ctx->dt1.ensure((size_t)N * 8)); a.dt_first = (double*)ctx->dt1.ptr; }
   } else {
     a.p = prob->p;
     a.u0 = prob->u0;
@@ -431,13 +437,13 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
     a.nf = out->nf;
     a.t_end = out->t_end;
     a.method_out = out->method;
+    a.dt_first = out->dt_first;
   }
   GBDE_CUDA(ctx, ctx->work.ensure(256));
   unsigned long long* work = (unsigned long long*)ctx->work.ptr;
   GBDE_CUDA(ctx, cudaMemsetAsync(work, 0, 256, s));
   a.queue = opts->batching == GBDE_BATCH_PERSISTENT ? work : nullptr;
   a.flag = (int32_t*)(work + 1);
-  if (opts->learned) a.pred_dt = (const float*)ctx->pred_dt.ptr;
 
   LaunchCfg cfg;
   cfg.alg = alg;
@@ -452,6 +458,15 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
     return set_err(ctx, GBDE_ERR_INVALID, "block_size must be a multiple of 32 and <= 128");
 
   GBDE_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
+  if (opts->learned && N > 0) {
+    // learned predictions: first dt (all methods) and stiff label (AUTO)
+    GBDE_CUDA(ctx, ctx->pred_dt.ensure((size_t)N * sizeof(float)));
+    GBDE_CUDA(ctx, ctx->pred_stiff.ensure((size_t)N));
+    GBDE_CUDA(ctx, mlp_predict(prob->model, (const float*)ctx->mlp_net.ptr, a,
+                               (float*)ctx->pred_dt.ptr, (int8_t*)ctx->pred_stiff.ptr,
+                               ctx->num_sms, s));
+    a.pred_dt = (const float*)ctx->pred_dt.ptr;
+  }
   if (alg == GBDE_ALG_AUTO) {
     const int rc = solve_auto(ctx, cfg, a, np, opts, s);
     if (rc != GBDE_OK) return rc;
@@ -482,6 +497,7 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
       if (out->nf) GBDE_CUDA(ctx, cudaMemcpyAsync(out->nf, a.nf, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
       if (out->t_end) GBDE_CUDA(ctx, cudaMemcpyAsync(out->t_end, a.t_end, (size_t)N * 8, cudaMemcpyDeviceToHost, s));
       if (out->method) GBDE_CUDA(ctx, cudaMemcpyAsync(out->method, a.method_out, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
+      if (out->dt_first) GBDE_CUDA(ctx, cudaMemcpyAsync(out->dt_first, a.dt_first, (size_t)N * 8, cudaMemcpyDeviceToHost, s));
     }
   }
   GBDE_CUDA(ctx, cudaMemcpyAsync(&flag, a.flag, 4, cudaMemcpyDeviceToHost, s));
@@ -494,6 +510,20 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
   if (flag & 1)
     return set_err(ctx, GBDE_ERR_TIMEOUT, "device deadline of %.3f s reached; unfinished "
                    "trajectories carry GBDE_RET_TIMEOUT", opts->timeout_s);
+  return GBDE_OK;
+}
+
+int gbde_mlp_load(gbde_ctx* ctx, int32_t model, const float* net) {
+  if (!ctx || !net) return set_err(nullptr, GBDE_ERR_INVALID, "ctx and net must be non-NULL");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (gbde_model_info(model, nullptr, nullptr) != GBDE_OK)
+    return set_err(ctx, GBDE_ERR_INVALID, "unknown model id %d", model);
+  GBDE_CUDA(ctx, cudaSetDevice(ctx->device));
+  GBDE_CUDA(ctx, ctx->mlp_net.ensure(sizeof(float) * GBDE_MLP_NET_FLOATS));
+  GBDE_CUDA(ctx, cudaMemcpyAsync(ctx->mlp_net.ptr, net, sizeof(float) * GBDE_MLP_NET_FLOATS,
+                                 cudaMemcpyHostToDevice, ctx->stream));
+  GBDE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->mlp_model = model;
   return GBDE_OK;
 }
 

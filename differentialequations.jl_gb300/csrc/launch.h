@@ -57,6 +57,10 @@ cudaError_t build_partition(const double* p, int np, double thr, const int8_t* p
                             void* scratch, unsigned* counters, int num_sms, cudaStream_t s,
                             int32_t** nonstiff, int32_t** stiff);
 
+// Learned predictions for a solve (mlp.cu): pred_dt[N] and pred_stiff[N].
+cudaError_t mlp_predict(int model, const float* net, const KArgs& a, float* pred_dt,
+                        int8_t* pred_stiff, int num_sms, cudaStream_t s);
+
 // Team kernels (team.cuh): 16 threads per trajectory.
 cudaError_t launch_team(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
 

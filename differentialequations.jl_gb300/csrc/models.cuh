@@ -18,11 +18,22 @@
 
 namespace gbde {
 
+// log10 of a positive parameter (clamped away from 0) for the learned
+// predictor's features
+GBDE_HD float flog10(double x) { return (float)log10(fmax(fabs(x), 1e-30)); }
+
+// Learned-predictor features (mlp.cuh): 8 numbers per trajectory from its
+// parameters, initial state and time span, defined per model below.
+
 struct Linear {
   static constexpr int N = 1, NP = 1, ID = GBDE_MODEL_LINEAR;
   static constexpr int F_FLOPS = 1;
   template <class T> GBDE_HD static void f(T* du, const T* u, const T* p) { du[0] = p[0] * u[0]; }
   template <class T> GBDE_HD static void jac(T (*J)[1], const T* u, const T* p) { J[0][0] = p[0]; }
+  GBDE_HD static void features(const double* p, const double* u0, double span, float* f) {
+    f[0] = (float)p[0]; f[1] = (float)u0[0]; f[2] = flog10(span);
+    f[3] = f[4] = f[5] = f[6] = f[7] = 0.0f;
+  }
 };
 
 struct Lorenz {
@@ -37,6 +48,10 @@ struct Lorenz {
     J[0][0] = -p[0]; J[0][1] = p[0]; J[0][2] = T(0);
     J[1][0] = p[1] - u[2]; J[1][1] = T(-1); J[1][2] = -u[0];
     J[2][0] = u[1]; J[2][1] = u[0]; J[2][2] = -p[2];
+  }
+  GBDE_HD static void features(const double* p, const double* u0, double span, float* f) {
+    f[0] = flog10(p[0]); f[1] = flog10(p[1]); f[2] = flog10(p[2]);
+    f[3] = (float)u0[0]; f[4] = (float)u0[1]; f[5] = (float)u0[2]; f[6] = flog10(span); f[7] = 0.0f;
   }
 };
 
@@ -55,6 +70,10 @@ struct Robertson {
     J[0][0] = -p[0]; J[0][1] = p[2] * u[2]; J[0][2] = p[2] * u[1];
     J[1][0] = p[0]; J[1][1] = T(-2) * p[1] * u[1] - p[2] * u[2]; J[1][2] = -p[2] * u[1];
     J[2][0] = T(0); J[2][1] = T(2) * p[1] * u[1]; J[2][2] = T(0);
+  }
+  GBDE_HD static void features(const double* p, const double* u0, double span, float* f) {
+    f[0] = flog10(p[0]); f[1] = flog10(p[1]); f[2] = flog10(p[2]);
+    f[3] = (float)u0[0]; f[4] = (float)u0[1]; f[5] = (float)u0[2]; f[6] = flog10(span); f[7] = 0.0f;
   }
 };
 
@@ -127,6 +146,20 @@ struct VdpRing8 {
       Jr[c] = val;
     }
   }
+  // mu, kappa, span and summaries of the oscillators' initial state
+  GBDE_HD static void features(const double* p, const double* u0, double span, float* f) {
+    double mx = 0.0, mv = 0.0, sx = 0.0, sv = 0.0, sm = 0.0;
+    for (int i = 0; i < 8; ++i) {
+      const double x = u0[2 * i], v = u0[2 * i + 1];
+      mx = fmax(mx, fabs(x));
+      mv = fmax(mv, fabs(v));
+      sx += x * x;
+      sv += v * v;
+      sm += fabs(1.0 - x * x) * fabs(v);
+    }
+    f[0] = flog10(p[0]); f[1] = (float)p[1]; f[2] = flog10(span); f[3] = (float)mx;
+    f[4] = (float)mv; f[5] = (float)(sx / 8); f[6] = (float)(sv / 8); f[7] = flog10(p[0] * sm / 8);
+  }
   // Row r of the Jacobian (for the warp-cooperative Rosenbrock path).
   template <class T> GBDE_HD static T jac_entry(int r, int c, const T* u, const T* p) {
     const T mu = p[0], ka = p[1];
@@ -158,6 +191,10 @@ struct LotkaVolterra {
   template <class T> GBDE_HD static void jac(T (*J)[2], const T* u, const T* p) {
     J[0][0] = p[0] - p[1] * u[1]; J[0][1] = -p[1] * u[0];
     J[1][0] = p[3] * u[1]; J[1][1] = p[3] * u[0] - p[2];
+  }
+  GBDE_HD static void features(const double* p, const double* u0, double span, float* f) {
+    f[0] = flog10(p[0]); f[1] = flog10(p[1]); f[2] = flog10(p[2]); f[3] = flog10(p[3]);
+    f[4] = (float)p[4]; f[5] = (float)u0[0]; f[6] = (float)u0[1]; f[7] = flog10(span);
   }
 };
 

@@ -199,6 +199,7 @@ extern "C" int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_
   a.nf = out->nf;
   a.t_end = out->t_end;
   a.method_out = out->method;
+  a.dt_first = out->dt_first;
   a.reltol = opts->reltol;
   a.abstol = opts->abstol;
   a.dt0 = opts->dt;

@@ -64,7 +64,7 @@ struct NormalStream {
 
 template <int N, class T>
 GBDE_D void finish_sde(const KArgs& a, int64_t i, int ret, int js, int nacc, int nrej, int nfev,
-                       double t, int alg) {
+                       double t, int alg, double dt1) {
   if (js < a.n_save) {
     T nanv[N];
 #pragma unroll
@@ -77,6 +77,7 @@ GBDE_D void finish_sde(const KArgs& a, int64_t i, int ret, int js, int nacc, int
   if (a.nf) a.nf[i] = nfev;
   if (a.t_end) a.t_end[i] = t;
   if (a.method_out) a.method_out[i] = alg;
+  if (a.dt_first) a.dt_first[i] = dt1;
 }
 
 // ------------------------------------------------------------------ EM
@@ -105,7 +106,8 @@ __device__ void em_all(const KArgs& a) {
 #pragma unroll
     for (int c = 0; c < N; ++c) bad |= !isfinite((double)u[c]);
     if (bad) {
-      finish_sde<N, T>(a, i, GBDE_RET_INITIALFAILURE, js, 0, 0, 0, t0, GBDE_ALG_EM);
+      finish_sde<N, T>(a, i, GBDE_RET_INITIALFAILURE, js, 0, 0, 0, t0, GBDE_ALG_EM,
+                       __longlong_as_double(0x7ff8000000000000ll));
       continue;
     }
     NormalStream<T> ns;
@@ -154,7 +156,7 @@ __device__ void em_all(const KArgs& a) {
         break;
       }
     }
-    finish_sde<N, T>(a, i, ret, js, (int)n, 0, (int)(2 * n), t, GBDE_ALG_EM);
+    finish_sde<N, T>(a, i, ret, js, (int)n, 0, (int)(2 * n), t, GBDE_ALG_EM, h);
   }
 }
 
@@ -266,7 +268,8 @@ __device__ void sri_all(const KArgs& a) {
 #pragma unroll
     for (int c = 0; c < N; ++c) bad |= !isfinite((double)u[c]);
     if (bad) {
-      finish_sde<N, T>(a, i, GBDE_RET_INITIALFAILURE, js, 0, 0, 0, t0, GBDE_ALG_SOSRI);
+      finish_sde<N, T>(a, i, GBDE_RET_INITIALFAILURE, js, 0, 0, 0, t0, GBDE_ALG_SOSRI,
+                       __longlong_as_double(0x7ff8000000000000ll));
       continue;
     }
     NormalStream<T> ns;
@@ -274,8 +277,10 @@ __device__ void sri_all(const KArgs& a) {
     stk.sp = 0;
     int nfev = 0, nacc = 0, nrej = 0;
     double t = t0, tlo = 0.0;
-    double h;
-    if (a.dt0 > 0.0) {
+    double h, dt1 = __longlong_as_double(0x7ff8000000000000ll);
+    if (a.pred_dt != nullptr && a.pred_dt[i] > 0.f) {
+      h = fmin((double)a.pred_dt[i], tf - t0);
+    } else if (a.dt0 > 0.0) {
       h = a.dt0;
     } else {
       T f0[N];
@@ -375,6 +380,7 @@ __device__ void sri_all(const KArgs& a) {
           fin &= isfinite((double)un[c]);
         }
         t = tnew;
+        if (nacc == 0) dt1 = hs;
         ++nacc;
         if (!fin) ret = GBDE_RET_UNSTABLE;
         else if (last) ret = GBDE_RET_SUCCESS;
@@ -391,7 +397,7 @@ __device__ void sri_all(const KArgs& a) {
           ret = GBDE_RET_DTLESSTHANMIN;
       }
     }
-    finish_sde<N, T>(a, i, ret, js, nacc, nrej, nfev, t + tlo, GBDE_ALG_SOSRI);
+    finish_sde<N, T>(a, i, ret, js, nacc, nrej, nfev, t + tlo, GBDE_ALG_SOSRI, dt1);
   }
 }
 

@@ -52,6 +52,7 @@ struct KArgs {
   int32_t* flag;              // device status word (bit 0: deadline hit)
   const float* pred_dt;       // optional predicted first dt per trajectory
   CtlK ctl;                   // step-size controller constants (controller.h)
+  double* dt_first;           // optional: size of the first accepted step
 };
 
 GBDE_D uint64_t global_ns() {
@@ -204,7 +205,7 @@ __device__ void integrate_all(const KArgs& a) {
   T p[M::NP];
   int64_t i = -1;
   bool active = false;
-  double t = 0.0, tlo = 0.0, tf = 0.0, dt = 0.0;
+  double t = 0.0, tlo = 0.0, tf = 0.0, dt = 0.0, dt1 = 0.0;
   float lqold = 0.0f;  // log2(qold)
   int js = 0, nacc = 0, nrej = 0, nfev = 0;
   int64_t iters = 0;
@@ -228,6 +229,7 @@ __device__ void integrate_all(const KArgs& a) {
       nacc = nrej = nfev = 0;
       iters = 0;
       lqold = a.ctl.lqoldinit;
+      dt1 = __longlong_as_double(0x7ff8000000000000ll);
       ret = GBDE_RET_DEFAULT;
       bool bad = !(tf >= t) || !isfinite(t) || !isfinite(tf);
 #pragma unroll
@@ -301,6 +303,7 @@ __device__ void integrate_all(const KArgs& a) {
         }
         alg.accept(p, nfev);
         t = tnew;
+        if (nacc == 0) dt1 = h;
         ++nacc;
         bool fin = true;
 #pragma unroll
@@ -337,6 +340,7 @@ __device__ void integrate_all(const KArgs& a) {
       if (a.nf) a.nf[i] = nfev;
       if (a.t_end) a.t_end[i] = t + tlo;
       if (a.method_out) a.method_out[i] = Alg::ALG_ID;
+      if (a.dt_first) a.dt_first[i] = dt1;
       active = false;
     }
   }

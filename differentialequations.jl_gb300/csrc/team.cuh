@@ -306,6 +306,7 @@ __device__ void integrate_team(const KArgs& a) {
     int js = 0, nacc = 0, nrej = 0, nfev = 0;
     int64_t iters = 0;
     float lqold = a.ctl.lqoldinit;
+    double dt1 = __longlong_as_double(0x7ff8000000000000ll);
     int ret = GBDE_RET_DEFAULT;
     const bool bad_lane = !isfinite((double)u0);
     const bool bad = !(tf >= t) || !isfinite(t) || !isfinite(tf) ||
@@ -321,7 +322,9 @@ __device__ void integrate_team(const KArgs& a) {
       ret = GBDE_RET_INITIALFAILURE;
     } else {
       alg.init(u0, p, tm, nfev);
-      if (a.dt0 > 0.0 || !a.adaptive) {
+      if (a.pred_dt != nullptr && a.pred_dt[i] > 0.f) {
+        dt = fmin((double)a.pred_dt[i], tf - t);
+      } else if (a.dt0 > 0.0 || !a.adaptive) {
         dt = a.dt0;
       } else {
         // Hairer-Wanner starting step (hw_h0 / hw_dt, controller.h)
@@ -372,6 +375,7 @@ __device__ void integrate_team(const KArgs& a) {
         }
         alg.accept();
         t = tnew;
+        if (nacc == 0) dt1 = h;
         ++nacc;
         if (__any_sync(tm.mask, !isfinite((double)alg.u()))) ret = GBDE_RET_UNSTABLE;
         else if (last) ret = GBDE_RET_SUCCESS;
@@ -403,6 +407,7 @@ __device__ void integrate_team(const KArgs& a) {
       if (a.nf) a.nf[i] = nfev;
       if (a.t_end) a.t_end[i] = t + tlo;
       if (a.method_out) a.method_out[i] = Alg::ALG_ID;
+      if (a.dt_first) a.dt_first[i] = dt1;
     }
   }
 }

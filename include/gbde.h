@@ -179,6 +179,8 @@ typedef struct {
   int32_t* method;     /* [N] or NULL: GBDE_ALG_* actually used (AUTO)    */
   float device_ms;     /* out: device time of the solve kernels           */
   float total_ms;      /* out: wall time of the whole call                */
+  double* dt_first;    /* [N] or NULL: size of the first accepted step (the
+                          step log the learned predictor is trained on)   */
 } gbde_outputs;
 
 /* ABI version of the loaded library (GBDE_ABI_VERSION). */
@@ -253,6 +255,53 @@ GBDE_API int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_op
 /* Measure the device's FP64 / FP32 FMA throughput (TFLOP/s, FMA = 2 flops)
  * with a dependent-chain-free FMA loop; kind 0 = FP64, 1 = FP32. */
 GBDE_API int gbde_measure_fma_peak(gbde_ctx* ctx, int32_t kind, double* tflops);
+
+/* ---- learned step-size / stiffness predictor ----------------------------
+ * No counterpart in the reference (its nearest relative is the runtime
+ * stiffness switching of AutoTsit5(Rosenbrock23()), test/qa/qa.jl:15).
+ * A 4-layer MLP 8 -> 64 -> 64 -> 64 -> 2 with GELU, BF16 weights and FP32
+ * accumulation maps 8 features of a trajectory (its parameters, initial state
+ * and time span; gbde_mlp_features) to (log10 of the first accepted dt,
+ * logit of "stiff").  With opts.learned = 1 a solve runs the loaded network
+ * first: the prediction replaces the Hairer-Wanner starting step, and
+ * GBDE_ALG_AUTO uses the stiff label instead of the threshold.  The error
+ * controller still accepts or rejects every step.
+ * Network blob: GBDE_MLP_NET_FLOATS floats, FP32:
+ *   W1[8][64] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[64][2] b4[2]
+ *   x_mean[8] x_scale[8] y_mean y_scale                                   */
+#define GBDE_MLP_IN 8
+#define GBDE_MLP_PARAMS 9026
+#define GBDE_MLP_NET_FLOATS 9044
+
+typedef struct {
+  int32_t epochs;      /* passes over the data                              */
+  int32_t batch;       /* minibatch size                                    */
+  float lr;            /* AdamW learning rate                               */
+  float weight_decay;  /* decoupled weight decay (matrices only)            */
+  uint64_t seed;       /* minibatch shuffling                               */
+} gbde_mlp_train_opts;
+
+/* He-uniform initial weights (seeded), identity normalisation. */
+GBDE_API int gbde_mlp_init(uint64_t seed, float* net);
+/* features[N][8] (device memory) of every trajectory of a device-memory
+ * problem. */
+GBDE_API int gbde_mlp_features(gbde_ctx* ctx, const gbde_problem* prob, float* features);
+/* Train on the GPU: x[n][8] features, y[n][2] targets (log10 first accepted
+ * dt, stiff label 0/1; NaN = no label), host memory.  `net` holds the initial
+ * weights on entry and the trained network on return (the normalisation
+ * fields are set from the data); loss_history[epochs] may be NULL. */
+GBDE_API int gbde_mlp_train(gbde_ctx* ctx, const float* x, const float* y, int64_t n,
+                   const gbde_mlp_train_opts* opts, float* net, float* loss_history);
+/* Raw outputs y[n][2] (normalised log10 dt, stiff logit) for x[n][8]; host
+ * memory. */
+GBDE_API int gbde_mlp_forward(gbde_ctx* ctx, const float* net, const float* x, int64_t n,
+                     float* y);
+/* Gradient of the mean training loss over (x, y) w.r.t. the GBDE_MLP_PARAMS
+ * weights, and the loss; host memory. */
+GBDE_API int gbde_mlp_grad(gbde_ctx* ctx, const float* net, const float* x, const float* y,
+                  int64_t n, float* grad, float* loss);
+/* Make `net` (host) the network that learned=1 solves of `model` use. */
+GBDE_API int gbde_mlp_load(gbde_ctx* ctx, int32_t model, const float* net);
 
 /* Self-check (no counterpart in the reference): the largest relative
  * difference, over n pseudo-random x with |x| in [2^-60, 2^61), between the
