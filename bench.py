@@ -60,7 +60,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=100000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="robertson",
-                    choices=["robertson", "lorenz", "lv_em", "lv_sosri", "vdp_auto"],
+                    choices=["robertson", "lorenz", "lv_em", "lv_sosri", "vdp_auto",
+                             "learned_lorenz", "learned_lv", "learned_vdp"],
                     help="robertson = the headline (default); the others print the line of "
                          "another configuration")
     return ap.parse_args()
@@ -331,6 +332,112 @@ def run_other(args, de):
     print(json.dumps(line))
 
 
+def run_learned(args, de):
+    """Learned predictor (configuration 5): train from scratch on step logs
+    of the plain solver, then time learned vs plain on held-out trajectories."""
+    import torch
+    import oracle
+    capi = de._capi
+    base = {"learned_lorenz": "lorenz", "learned_lv": "lv_sosri", "learned_vdp": "vdp_auto"}[
+        args.workload]
+    n_train = 1000000 if base == "vdp_auto" else 2000000
+    N = args.trajectories
+    tr = other_workload(de, base, n_train, SEED + 1000)
+    model, saveat, kind, plain = tr[0], tr[5], tr[6], tr[7]
+    t = time.perf_counter()
+    # step logs of the plain solver (persistent launch)
+    log_opts = other_workload(de, base, 1, 0)[8]
+    dev = torch.device("cuda", 0)
+    dtr = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in tr[1:6]]
+    odt = tr[9][1]
+    r = de.solve_arrays(model, log_opts, *dtr, kind, u_dtype=odt)
+    dt1 = r["dt_first"].cpu().numpy()
+    if base == "vdp_auto":
+        lab, cost = de.learned.stiff_labels(de.solve_arrays, model, *dtr[:5], kind, plain.reltol,
+                                            plain.abstol)
+    else:
+        lab, cost = np.zeros(n_train, np.float32), None
+    x = de.learned.features(model, *tr[1:5])
+    y = np.c_[np.log10(dt1), lab].astype(np.float32)
+    logs_s = time.perf_counter() - t
+    t = time.perf_counter()
+    net, hist = de.learned.train(x, y, epochs=8, batch=4096, lr=2e-3, seed=SEED)
+    train_s = time.perf_counter() - t
+    de.learned.load(model, net)
+    # held-out evaluation
+    ev = other_workload(de, base, N, SEED + 2000)
+    host = [np.ascontiguousarray(a) for a in ev[1:6]]
+    dptr = [torch.from_numpy(a).to(dev) for a in host]
+    chosen = ev[8]
+    learned = ev[8]
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+
+    def timed(o, K, W):
+        for _ in range(W):
+            de.solve_arrays(model, o, *dptr, kind, u_dtype=odt)
+        ts, rr = [], None
+        for _ in range(K):
+            flush.zero_()
+            torch.cuda.synchronize()
+            rr = de.solve_arrays(model, o, *dptr, kind, u_dtype=odt)
+            ts.append(rr["device_ms"])
+        return float(np.median(ts)), rr
+
+    with ClockSampler(0) as clk:
+        chosen.learned = 0
+        base_ms, rb = timed(chosen, args.steps, args.warmup)
+        learned.learned = 1
+        learned_ms, rl = timed(learned, args.steps, args.warmup)
+        learned.learned = 0
+    ok = bool(np.all(rl["retcode"].cpu().numpy() == capi.RET_SUCCESS))
+    # accuracy of the learned solve on a sample against the FP64 oracle
+    ns = min(N, 512 if base == "vdp_auto" else 2000)
+    idx = np.arange(ns)  # leading block (SDE noise is keyed by trajectory index)
+    u_l = rl["u"].cpu().numpy()[idx].astype(np.float64)
+    u_b = rb["u"].cpu().numpy()[idx].astype(np.float64)
+    if base == "vdp_auto":
+        st = host[0][idx, 0] > chosen.stiff_threshold
+        ref = np.empty_like(u_l)
+        for mask, alg in ((~st, capi.ALG_TSIT5), (st, capi.ALG_RODAS5)):
+            if mask.any():
+                o = capi.opts_default(alg)
+                o.reltol, o.abstol, o.maxiters = chosen.reltol, chosen.abstol, chosen.maxiters
+                ref[mask] = oracle.solve(capi, model, o, *[a[idx][mask] for a in host[:4]],
+                                         host[4], kind, nthreads=oracle.hardware_threads())["u"]
+    else:
+        ref = oracle.solve(capi, model, plain, *[a[idx] for a in host[:4]], host[4], kind,
+                           nthreads=oracle.hardware_threads(),
+                           noise_f32=(base == "lv_sosri"))["u"]
+    w = lambda u: (np.abs(u - ref) / (chosen.abstol + chosen.reltol * np.abs(ref))).max(axis=(1, 2))
+    pred_dt, pred_st = de.learned.predict(net, de.learned.features(model, *host[:4]))
+    st_l = rl["naccept"] + rl["nreject"]
+    st_b = rb["naccept"] + rb["nreject"]
+    line = {"metric": "trajectories/sec at <=10x reltol error vs FP64 oracle; learned vs plain",
+            "value": N / (learned_ms * 1e-3), "unit": "trajectories/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": learned_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "data": "synthetic (seeded, config distributions); held-out seed",
+            "config": {"workload": "learned_" + base + "_N%d" % N, "train_pairs": n_train,
+                       "net": "8-64-64-64-2 GELU, BF16 weights, FP32 accumulation",
+                       "train": "8 epochs, batch 4096, AdamW lr 2e-3 (GPU, own kernels)",
+                       "form": "same launch (%s) with and without learned=1" % (
+                           "persistent" if chosen.batching else "plain")},
+            "without_learned": {"value": N / (base_ms * 1e-3), "ms_per_step": base_ms},
+            "speedup_vs_without": base_ms / learned_ms,
+            "all_success": ok,
+            "steps_per_traj": {"learned": float(st_l.float().mean()), "without": float(st_b.float().mean())},
+            "nf_per_traj": {"learned": float(rl["nf"].float().mean()), "without": float(rb["nf"].float().mean())},
+            "accuracy_vs_fp64_oracle": {"learned_p50": float(np.median(w(u_l))),
+                                        "learned_max": float(w(u_l).max()),
+                                        "without_p50": float(np.median(w(u_b))),
+                                        "without_max": float(w(u_b).max())},
+            "first_dt_log10_abs_err_median": float(np.median(np.abs(
+                np.log10(pred_dt[idx]) - np.log10(rb["dt_first"].cpu().numpy()[idx])))),
+            "step_log_s": logs_s, "train_s": train_s, "loss_first_last": [float(hist[0]), float(hist[-1])],
+            "stiff_cost_model": cost, "clocks": clk.summary()}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
@@ -343,6 +450,8 @@ def main():
             raise SystemExit("--impl reference times the headline workload only")
         if "--trajectories" not in sys.argv:
             args.trajectories = {"lorenz": 10000}.get(args.workload, 1000000)
+        if args.workload.startswith("learned_"):
+            return run_learned(args, de)
         return run_other(args, de)
     alg_id = capi.ALG_RODAS5 if args.alg == "rodas5" else capi.ALG_ROSENBROCK23
     config = {"workload": "robertson_%s_fp64_N%d" % (args.alg, args.trajectories),

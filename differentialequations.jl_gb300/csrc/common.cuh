@@ -37,6 +37,18 @@ GBDE_HD float xadd(float a, float b) { return a + b; }
 GBDE_HD float xfma(float a, float b, float c) { return fmaf(a, b, c); }
 #endif
 
+// x as an ordered integer: for non-NaN doubles (either sign),
+// ord_bits(a) <= ord_bits(b) iff a <= b.  Comparisons on the integer pipe.
+GBDE_HD uint64_t ord_bits(double x) {
+#if defined(__CUDA_ARCH__)
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t b;
+  memcpy(&b, &x, sizeof(b));
+#endif
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
 // |x| as an ordered integer: for non-NaN doubles, mag_bits(a) < mag_bits(b)
 // iff |a| < |b|.  Compares on the integer pipe instead of the FP64 pipe.
 GBDE_HD uint64_t mag_bits(double x) {

@@ -342,22 +342,27 @@ struct RodasAlg {
     return err_ms<N>(s8, uu, un, abstol, reltol);
   }
 
+  // y(theta) = (1-theta) y0 + theta y1 + theta(1-theta)(K2 + theta K3 + theta^2 K4),
+  // K_q = sum_j Hq_j u_j, evaluated as y0 + theta (y1 - y0) + sum_j e_j u_j with
+  // the scalar weights e_j = theta(1-theta)(H2_j + theta H3_j + theta^2 H4_j):
+  // one 7-term combination per component instead of three.
   GBDE_D void interp(double th, double, T* out, const T*, int&) {
-    const T a = (T)(1.0 - th), b = (T)th, w = (T)(th * (1.0 - th));
+    const double w = th * (1.0 - th);
+    T e[7];
+#define GBDE_RODAS_E(j)                                                        \
+  {                                                                            \
+    constexpr double h2 = K::H2[j], h3 = K::H3[j], h4 = K::H4[j];              \
+    e[j] = (T)(w * (h2 + th * (h3 + th * h4)));                                \
+  }
+    GBDE_RODAS_E(0); GBDE_RODAS_E(1); GBDE_RODAS_E(2); GBDE_RODAS_E(3);
+    GBDE_RODAS_E(4); GBDE_RODAS_E(5); GBDE_RODAS_E(6);
+#undef GBDE_RODAS_E
     const T tt = (T)th;
 #pragma unroll
-    for (int c = 0; c < N; ++c) {
-      const T k2 = T(K::H2[0]) * s1[c] + T(K::H2[1]) * s2[c] + T(K::H2[2]) * s3[c] +
-                   T(K::H2[3]) * s4[c] + T(K::H2[4]) * s5[c] + T(K::H2[5]) * s6[c] +
-                   T(K::H2[6]) * s7[c];
-      const T k3 = T(K::H3[0]) * s1[c] + T(K::H3[1]) * s2[c] + T(K::H3[2]) * s3[c] +
-                   T(K::H3[3]) * s4[c] + T(K::H3[4]) * s5[c] + T(K::H3[5]) * s6[c] +
-                   T(K::H3[6]) * s7[c];
-      const T k4 = T(K::H4[0]) * s1[c] + T(K::H4[1]) * s2[c] + T(K::H4[2]) * s3[c] +
-                   T(K::H4[3]) * s4[c] + T(K::H4[4]) * s5[c] + T(K::H4[5]) * s6[c] +
-                   T(K::H4[6]) * s7[c];
-      out[c] = a * uu[c] + b * un[c] + w * (k2 + tt * (k3 + tt * k4));
-    }
+    for (int c = 0; c < N; ++c)
+      out[c] = uu[c] + tt * (un[c] - uu[c]) + (e[0] * s1[c] + e[1] * s2[c] + e[2] * s3[c] +
+                                               e[3] * s4[c] + e[4] * s5[c] + e[5] * s6[c] +
+                                               e[6] * s7[c]);
   }
 
   GBDE_D void accept(const T*, int&) {

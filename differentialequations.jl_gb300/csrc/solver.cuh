@@ -269,7 +269,8 @@ __device__ void integrate_all(const KArgs& a) {
       }
       const double ms = alg.attempt(h, p, a.abstol, a.reltol, nfev);  // EEst^2
       ++iters;
-      const bool ok = !a.adaptive || ms <= 1.0;
+      // ms <= 1 (ms >= 0; NaN rejects), compared on the integer pipe
+      const bool ok = !a.adaptive || mag_bits(ms) <= 0x3FF0000000000000ull;
       if (ok) {
         // controller proposal for the next step
         double dtnew = h;
@@ -289,10 +290,12 @@ __device__ void integrate_all(const KArgs& a) {
           tnew = t + h;
         }
         // saveat: dense output at every save time in (t, tnew]
+        const uint64_t tnew_o = ord_bits(tnew);
         while (js < a.n_save) {
           const double ts = save_time(a, i, js);
-          if (!(ts <= tnew)) break;
-          if (ts >= tnew) {
+          const uint64_t ts_o = ord_bits(ts);
+          if (ts_o > tnew_o) break;
+          if (ts_o == tnew_o) {
             store_state<N>(a, i, js, alg.unew());
           } else {
             T tmp[N];

@@ -184,15 +184,19 @@ struct TeamRodas {
     return tm.sum(e * e) * (1.0 / TEAM);
   }
 
-  GBDE_D T interp(double th, double) const {
-    const T a = (T)(1.0 - th), b = (T)th, w = (T)(th * (1.0 - th)), tt = (T)th;
-    const T k2 = T(K::H2[0]) * s1 + T(K::H2[1]) * s2 + T(K::H2[2]) * s3 + T(K::H2[3]) * s4 +
-                 T(K::H2[4]) * s5 + T(K::H2[5]) * s6 + T(K::H2[6]) * s7;
-    const T k3 = T(K::H3[0]) * s1 + T(K::H3[1]) * s2 + T(K::H3[2]) * s3 + T(K::H3[3]) * s4 +
-                 T(K::H3[4]) * s5 + T(K::H3[5]) * s6 + T(K::H3[6]) * s7;
-    const T k4 = T(K::H4[0]) * s1 + T(K::H4[1]) * s2 + T(K::H4[2]) * s3 + T(K::H4[3]) * s4 +
-                 T(K::H4[4]) * s5 + T(K::H4[5]) * s6 + T(K::H4[6]) * s7;
-    return a * uu + b * un + w * (k2 + tt * (k3 + tt * k4));
+  GBDE_D T interp(double th, double) const {  // as RodasAlg::interp
+    const double w = th * (1.0 - th);
+    T e[7];
+#define GBDE_RODAS_E(j)                                                        \
+  {                                                                            \
+    constexpr double h2 = K::H2[j], h3 = K::H3[j], h4 = K::H4[j];              \
+    e[j] = (T)(w * (h2 + th * (h3 + th * h4)));                                \
+  }
+    GBDE_RODAS_E(0); GBDE_RODAS_E(1); GBDE_RODAS_E(2); GBDE_RODAS_E(3);
+    GBDE_RODAS_E(4); GBDE_RODAS_E(5); GBDE_RODAS_E(6);
+#undef GBDE_RODAS_E
+    return uu + (T)th * (un - uu) + (e[0] * s1 + e[1] * s2 + e[2] * s3 + e[3] * s4 + e[4] * s5 +
+                                     e[5] * s6 + e[6] * s7);
   }
 
   GBDE_D void accept() {
@@ -351,7 +355,7 @@ __device__ void integrate_team(const KArgs& a) {
       }
       const double ms = alg.attempt(h, p, a.abstol, a.reltol, tm, nfev);
       ++iters;
-      if (!a.adaptive || ms <= 1.0) {
+      if (!a.adaptive || mag_bits(ms) <= 0x3FF0000000000000ull) {  // ms <= 1 (integer pipe)
         double dtnew = h;
         if (a.adaptive) dtnew = h * (double)ctl_accept(a.ctl, ms, lqold);
         double tnew;
@@ -367,10 +371,12 @@ __device__ void integrate_team(const KArgs& a) {
         } else {
           tnew = t + h;
         }
+        const uint64_t tnew_o = ord_bits(tnew);
         while (js < a.n_save) {
           const double ts = save_time(a, i, js);
-          if (!(ts <= tnew)) break;
-          store(js, ts >= tnew ? alg.unew() : alg.interp(((ts - t) - tlo) / h, h));
+          const uint64_t ts_o = ord_bits(ts);
+          if (ts_o > tnew_o) break;
+          store(js, ts_o == tnew_o ? alg.unew() : alg.interp(((ts - t) - tlo) / h, h));
           ++js;
         }
         alg.accept();

@@ -23,6 +23,11 @@ import numpy as np
 from . import _capi as capi
 
 
+def _np(a):
+    """numpy view of a result array (host arrays pass through, CUDA tensors copy)."""
+    return a if isinstance(a, np.ndarray) else a.cpu().numpy()
+
+
 def _dev_problem(model, arrs, save_kind=None, n_save=0):
     prob = capi.Problem()
     prob.model, prob.n_state, prob.n_param = model.id, model.n_state, model.n_param
@@ -119,8 +124,8 @@ def stiff_labels(solve_arrays, model, p, u0, t0, tf, saveat, save_kind, reltol, 
         o.batching = capi.BATCH_PERSISTENT
         r = solve_arrays(model, o, p, u0, t0, tf, saveat, save_kind,
                          u_dtype="f32" if prec == capi.PREC_MIXED else "f64")
-        steps = (r["naccept"] + r["nreject"]).astype(np.float64)
-        res[name] = (steps, r["device_ms"] / max(steps.sum(), 1.0), r["retcode"])
+        steps = (_np(r["naccept"]) + _np(r["nreject"])).astype(np.float64)
+        res[name] = (steps, r["device_ms"] / max(steps.sum(), 1.0), _np(r["retcode"]))
     (st_t, c_t, rc_t), (st_r, c_r, _) = res["tsit5"], res["rodas5"]
     stiff = (st_r * c_r < st_t * c_t) | (rc_t != capi.RET_SUCCESS)
     return stiff.astype(np.float32), {"tsit5_ms_per_step": c_t, "rodas5_ms_per_step": c_r}
