@@ -505,14 +505,15 @@ def main():
     peak32 = ctx.fma_peak(1)
 
     forms = {"plain": ("plain", "fp64"), "persistent": ("persistent", "fp64"),
-             "persistent-mixed": ("persistent", "mixed"), "plain-mixed": ("plain", "mixed")}
+             "persistent-mixed": ("persistent", "mixed"), "plain-mixed": ("plain", "mixed"),
+             "persistent-f32x2": ("persistent", "f32x2"), "plain-f32x2": ("plain", "f32x2")}
 
     def opts_for(form):
         b, prec = forms[form]
         o = capi.opts_default(alg_id)
         o.reltol, o.abstol = 1e-6, 1e-10
         o.batching = capi.BATCH_PERSISTENT if b == "persistent" else capi.BATCH_PLAIN
-        o.precision = capi.PREC_MIXED if prec == "mixed" else capi.PREC_FP64
+        o.precision = {"mixed": capi.PREC_MIXED, "f32x2": capi.PREC_F32X2}.get(prec, capi.PREC_FP64)
         return o
 
     def out_dtype(form):
@@ -636,6 +637,7 @@ def main():
             dist.destroy_process_group()
         return
     mixed = forms[args.chosen][1] == "mixed"
+    pairs = forms[args.chosen][1] == "f32x2"
     line = {
         "metric": metric,
         "value": total / (chosen_ms * 1e-3),
@@ -647,7 +649,8 @@ def main():
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32-state/f64-lu" if mixed else "f64",
+        "dtype": ("f32-state/f64-lu" if mixed else
+                  "f32x2-state/f64-lu" if pairs else "f64"),
         "data": "synthetic (seeded, config distributions)",
         "config": dict(config, chosen_form=args.chosen, l2="flushed between timed steps (256 MB write)",
                        parallelism="trajectory shards, no collective" if world > 1 else "single GPU"),

@@ -8,7 +8,7 @@ The compute path is libgbde.so (hand-written sm_103a kernels behind a C ABI,
 include/gbde.h); this package is the host-side mirror of the reference's
 SciMLBase interface over that ABI.
 """
-from . import _capi, learned
+from . import _capi, learned, tuning
 from .api import (EM, SOSRI, EnsembleGB300, EnsembleProblem, EnsembleSerial,
                   EnsembleSolution, EnsembleThreads, ODEProblem, ODESolution, ReturnCode,
                   Rodas5, Rodas5P, Rosenbrock23, SDEProblem, Tsit5, Vern7, models, remake,

@@ -30,7 +30,7 @@ MODEL_LINEAR, MODEL_LORENZ, MODEL_ROBERTSON, MODEL_VDP_RING8, MODEL_LOTKA_VOLTER
 ALG_TSIT5, ALG_VERN7, ALG_ROSENBROCK23, ALG_RODAS5, ALG_RODAS5P = 1, 2, 3, 4, 5
 ALG_EM, ALG_SOSRI, ALG_AUTO = 6, 7, 8
 
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_F32X2 = 0, 1, 2
 BATCH_PLAIN, BATCH_PERSISTENT = 0, 1
 SAVE_GRID, SAVE_PER_TRAJ = 0, 1
 MEM_HOST, MEM_DEVICE = 0, 1
@@ -58,6 +58,7 @@ class Opts(C.Structure):
         ("seed", C.c_uint64), ("learned", C.c_int32), ("block_size", C.c_int32),
         ("chunk", C.c_int32), ("ctas_per_sm", C.c_int32),
         ("stiff_threshold", C.c_double), ("timeout_s", C.c_double),
+        ("threads_per_traj", C.c_int32), ("reserved_", C.c_int32),
     ]
 
 
@@ -76,6 +77,11 @@ class MlpTrainOpts(C.Structure):
 
 
 MLP_IN, MLP_PARAMS, MLP_NET_FLOATS = 8, 9026, 9044
+
+
+class TuneEntry(C.Structure):
+    _fields_ = [("batching", C.c_int32), ("block_size", C.c_int32), ("ctas_per_sm", C.c_int32),
+                ("chunk", C.c_int32), ("threads_per_traj", C.c_int32), ("device_ms", C.c_float)]
 
 
 # Every function gbde.h declares, with its ctypes signature.
@@ -104,6 +110,13 @@ SIGNATURES = {
     "gbde_mlp_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                 C.c_void_p, C.POINTER(C.c_float)]),
     "gbde_mlp_load": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "gbde_graph_create": (C.c_int, [C.c_void_p, C.POINTER(Problem), C.POINTER(Opts),
+                                    C.POINTER(Outputs), C.POINTER(C.c_void_p)]),
+    "gbde_graph_launch": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "gbde_graph_destroy": (C.c_int, [C.c_void_p]),
+    "gbde_autotune": (C.c_int, [C.c_void_p, C.POINTER(Problem), C.POINTER(Opts),
+                                C.POINTER(Outputs), C.c_int32, C.POINTER(Opts),
+                                C.POINTER(TuneEntry), C.c_int32, C.POINTER(C.c_int32)]),
 }
 
 _lib = None

@@ -46,6 +46,17 @@ struct DevBuf {
   }
 };
 
+// Device scratch of one ensemble solve: [0] queue counter, [1] status word,
+// [2] second queue (AUTO), [3] AUTO list sizes; the persistent order; the
+// AUTO lists; the learned predictions.  A context keeps one set for its
+// solves; a captured graph keeps its own.
+struct Scratch {
+  DevBuf work, order, part, pred_dt, pred_stiff;
+  void release() {
+    for (DevBuf* b : {&work, &order, &part, &pred_dt, &pred_stiff}) b->release();
+  }
+};
+
 }  // namespace
 
 struct gbde_ctx {
@@ -58,15 +69,10 @@ struct gbde_ctx {
   std::string err;
   // staging for GBDE_MEM_HOST calls
   DevBuf p, u0, t0, tf, saveat, u, ret, nacc, nrej, nf, tend, method;
-  DevBuf work;  // queue counter + status flag
-  DevBuf order; // persistent queue order (longest span first) + sort counters
-  DevBuf part;  // GBDE_ALG_AUTO: non-stiff and stiff trajectory lists
-  DevBuf pred_stiff;  // learned stiff / non-stiff labels (int8 per trajectory)
+  Scratch scratch;    // device scratch of ensemble solves (queue, order, lists, predictions)
   DevBuf dt1;         // staging of the first-accepted-step log (host calls)
   DevBuf mlp_net;     // learned predictor (GBDE_MLP_NET_FLOATS floats)
   int mlp_model = 0;  // model the loaded predictor belongs to (0 = none)
-  // learned predictor (filled by the MLP entry points)
-  DevBuf pred_dt;
 };
 
 static int set_err(gbde_ctx* ctx, int code, const char* fmt, ...) {
@@ -101,7 +107,8 @@ int set_thread_error(int code, const char* msg) {
 cudaError_t launch_alg(int alg, LaunchCfg cfg, const KArgs& a, cudaStream_t s) {
   cfg.alg = alg;
   if (cfg.model == GBDE_MODEL_VDP_RING8 &&
-      (alg == GBDE_ALG_TSIT5 || alg == GBDE_ALG_RODAS5 || alg == GBDE_ALG_RODAS5P))
+      (alg == GBDE_ALG_RODAS5 || alg == GBDE_ALG_RODAS5P ||
+       (alg == GBDE_ALG_TSIT5 && cfg.tpt != 1)))
     return launch_team(cfg, a, s);
   if (alg == GBDE_ALG_TSIT5 || alg == GBDE_ALG_VERN7) return launch_explicit(cfg, a, s);
   if (alg == GBDE_ALG_EM || alg == GBDE_ALG_SOSRI) return launch_sde(cfg, a, s);
@@ -172,10 +179,10 @@ int gbde_ctx_destroy(gbde_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf* b : {&ctx->p, &ctx->u0, &ctx->t0, &ctx->tf, &ctx->saveat, &ctx->u, &ctx->ret,
-                    &ctx->nacc, &ctx->nrej, &ctx->nf, &ctx->tend, &ctx->method, &ctx->work,
-                    &ctx->order, &ctx->part, &ctx->pred_stiff, &ctx->pred_dt, &ctx->dt1,
+                    &ctx->nacc, &ctx->nrej, &ctx->nf, &ctx->tend, &ctx->method, &ctx->dt1,
                     &ctx->mlp_net})
     b->release();
+  ctx->scratch.release();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->own) cudaStreamDestroy(ctx->own);
@@ -261,16 +268,15 @@ static bool is_sde_alg(int a) { return a == GBDE_ALG_EM || a == GBDE_ALG_SOSRI; 
 // (FP32 state in mixed precision) and the stiff list with Rodas5 (FP64).
 // The options' controller exponents (Tsit5's by default) drive the Tsit5
 // part; the Rodas5 part uses Rodas5's default exponents.
-static int solve_auto(gbde_ctx* ctx, const LaunchCfg& cfg, const KArgs& a, int np,
+static int solve_auto(gbde_ctx* ctx, Scratch& sc, const LaunchCfg& cfg, const KArgs& a, int np,
                       const gbde_opts* opts, cudaStream_t s) {
   const int64_t N = a.N;
   if (N == 0) return GBDE_OK;
-  unsigned long long* work = (unsigned long long*)ctx->work.ptr;
+  unsigned long long* work = (unsigned long long*)sc.work.ptr;
   unsigned* counters = reinterpret_cast<unsigned*>(work + 3);
-  GBDE_CUDA(ctx, ctx->part.ensure(partition_scratch_bytes(N)));
   int32_t *nonstiff = nullptr, *stiff = nullptr;
-  const int8_t* pred = opts->learned ? (const int8_t*)ctx->pred_stiff.ptr : nullptr;
-  GBDE_CUDA(ctx, build_partition(a.p, np, opts->stiff_threshold, pred, N, ctx->part.ptr,
+  const int8_t* pred = opts->learned ? (const int8_t*)sc.pred_stiff.ptr : nullptr;
+  GBDE_CUDA(ctx, build_partition(a.p, np, opts->stiff_threshold, pred, N, sc.part.ptr,
                                  counters, ctx->num_sms, s, &nonstiff, &stiff));
   unsigned cnt[2] = {0, 0};
   GBDE_CUDA(ctx, cudaMemcpyAsync(cnt, counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
@@ -307,11 +313,10 @@ static int solve_auto(gbde_ctx* ctx, const LaunchCfg& cfg, const KArgs& a, int n
   return GBDE_OK;
 }
 
-int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts* opts,
-                        gbde_outputs* out) {
-  if (!ctx) return set_err(nullptr, GBDE_ERR_INVALID, "ctx is NULL");
-  std::lock_guard<std::mutex> lk(ctx->mu);
-  const auto wall0 = std::chrono::steady_clock::now();
+// Every argument check of an ensemble solve (shared by gbde_ensemble_solve,
+// gbde_graph_create and gbde_autotune).
+static int check_solve_args(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts* opts,
+                            const gbde_outputs* out, int32_t* ns_out, int32_t* np_out) {
   if (!prob || !opts || !out)
     return set_err(ctx, GBDE_ERR_INVALID, "prob, opts and out must be non-NULL");
   int32_t ns = 0, np = 0;
@@ -341,8 +346,13 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
     return set_err(ctx, GBDE_ERR_INVALID, "unknown algorithm id %d", alg);
   if (is_sde_alg(alg) && prob->model != GBDE_MODEL_LOTKA_VOLTERRA)
     return set_err(ctx, GBDE_ERR_UNSUPPORTED, "SDE algorithms need a model with a noise term");
-  if (opts->precision != GBDE_PREC_FP64 && opts->precision != GBDE_PREC_MIXED)
+  if (opts->precision != GBDE_PREC_FP64 && opts->precision != GBDE_PREC_MIXED &&
+      opts->precision != GBDE_PREC_F32X2)
     return set_err(ctx, GBDE_ERR_INVALID, "unknown precision %d", opts->precision);
+  if (opts->precision == GBDE_PREC_F32X2 &&
+      (is_sde_alg(alg) || alg == GBDE_ALG_AUTO || prob->model == GBDE_MODEL_VDP_RING8))
+    return set_err(ctx, GBDE_ERR_UNSUPPORTED,
+                   "GBDE_PREC_F32X2 is built for the one-thread-per-trajectory ODE kernels");
   if (opts->batching != GBDE_BATCH_PLAIN && opts->batching != GBDE_BATCH_PERSISTENT)
     return set_err(ctx, GBDE_ERR_INVALID, "unknown batching %d", opts->batching);
   if (opts->adaptive && !(opts->reltol > 0.0 && opts->abstol > 0.0))
@@ -361,16 +371,28 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
   if (alg == GBDE_ALG_AUTO && N > INT32_MAX)
     return set_err(ctx, GBDE_ERR_INVALID, "GBDE_ALG_AUTO supports n_traj < 2^31");
 
-  GBDE_CUDA(ctx, cudaSetDevice(ctx->device));
-  cudaStream_t s = ctx->stream;
-  const size_t n_save = (size_t)prob->n_save;
-  const size_t esz = out->u_dtype == GBDE_F32 ? 4 : 8;
-  const size_t save_elems = prob->save_kind == GBDE_SAVE_GRID ? n_save : n_save * (size_t)N;
-  const size_t u_bytes = (size_t)N * n_save * (size_t)ns * esz;
+  if (opts->threads_per_traj != 0 && opts->threads_per_traj != 1 && opts->threads_per_traj != 16)
+    return set_err(ctx, GBDE_ERR_INVALID, "threads_per_traj must be 0, 1 or 16");
+  if (opts->threads_per_traj == 16 && prob->model != GBDE_MODEL_VDP_RING8)
+    return set_err(ctx, GBDE_ERR_UNSUPPORTED, "16-lane teams are built for the 16-state ring");
+  if (opts->threads_per_traj == 1 && prob->model == GBDE_MODEL_VDP_RING8 &&
+      alg != GBDE_ALG_TSIT5 && alg != GBDE_ALG_VERN7)
+    return set_err(ctx, GBDE_ERR_UNSUPPORTED,
+                   "Rosenbrock methods on the 16-state ring run as 16-lane teams only");
+  if (opts->chunk < 0) return set_err(ctx, GBDE_ERR_INVALID, "chunk must be >= 0");
+  if (opts->block_size != 0 && (opts->block_size > 128 || opts->block_size < 32 ||
+                                (opts->block_size & 31)))
+    return set_err(ctx, GBDE_ERR_INVALID, "block_size must be a multiple of 32 and <= 128");
+  *ns_out = ns;
+  *np_out = np;
+  return GBDE_OK;
+}
 
-  KArgs a;
+// Scalar solver arguments.
+static void fill_common(KArgs& a, const gbde_problem* prob, const gbde_opts* opts,
+                        const gbde_outputs* out) {
   std::memset(&a, 0, sizeof(a));
-  a.N = N;
+  a.N = prob->n_traj;
   a.n_save = prob->n_save;
   a.save_kind = prob->save_kind;
   a.out_f32 = out->u_dtype == GBDE_F32;
@@ -393,7 +415,109 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
   a.timeout_ns = opts->timeout_s > 0 ? (uint64_t)(opts->timeout_s * 1e9) : 0;
   a.ctl = ctl_consts(opts->beta1, opts->beta2, opts->gamma, opts->qmin, opts->qmax,
                      opts->qsteady_min, opts->qsteady_max, opts->qoldinit);
+  a.chunk = opts->chunk > 0 ? opts->chunk : 1;
+}
 
+static void fill_device_ptrs(KArgs& a, const gbde_problem* prob, const gbde_outputs* out) {
+  a.p = prob->p;
+  a.u0 = prob->u0;
+  a.t0 = prob->t0;
+  a.tf = prob->tf;
+  a.saveat = prob->saveat;
+  a.u_out = out->u;
+  a.retcode = out->retcode;
+  a.naccept = out->naccept;
+  a.nreject = out->nreject;
+  a.nf = out->nf;
+  a.t_end = out->t_end;
+  a.method_out = out->method;
+  a.dt_first = out->dt_first;
+}
+
+static LaunchCfg make_cfg(const gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts* opts) {
+  LaunchCfg cfg;
+  cfg.alg = opts->alg;
+  cfg.model = prob->model;
+  cfg.precision = opts->precision;
+  cfg.persistent = opts->batching == GBDE_BATCH_PERSISTENT;
+  cfg.block = opts->block_size > 0 ? opts->block_size : 128;
+  cfg.grid = 0;
+  cfg.ctas_per_sm = opts->ctas_per_sm;
+  cfg.num_sms = ctx->num_sms;
+  cfg.tpt = opts->threads_per_traj;
+  return cfg;
+}
+
+// Allocate every scratch buffer a solve of N trajectories with these options
+// uses, before any work is enqueued (a stream capture must not meet a
+// cudaMalloc).
+static int reserve_scratch(gbde_ctx* ctx, Scratch& sc, int64_t N, const gbde_opts* opts) {
+  GBDE_CUDA(ctx, sc.work.ensure(256));
+  if (opts->learned && N > 0) {
+    GBDE_CUDA(ctx, sc.pred_dt.ensure((size_t)N * sizeof(float)));
+    GBDE_CUDA(ctx, sc.pred_stiff.ensure((size_t)N));
+  }
+  if (opts->alg == GBDE_ALG_AUTO && N > 0)
+    GBDE_CUDA(ctx, sc.part.ensure(partition_scratch_bytes(N)));
+  else if (opts->batching == GBDE_BATCH_PERSISTENT && N > 1 && N <= INT32_MAX)
+    GBDE_CUDA(ctx, sc.order.ensure(span_order_scratch_bytes(N)));
+  return GBDE_OK;
+}
+
+// Enqueue the device work of one solve on stream s: clear the queue and status
+// words, learned predictions, queue order (or AUTO's lists), the step kernels.
+// No host synchronisation except GBDE_ALG_AUTO's list sizes.
+static int enqueue_solve(gbde_ctx* ctx, Scratch& sc, KArgs& a, const LaunchCfg& cfg,
+                         const gbde_opts* opts, int np, cudaStream_t s) {
+  const int64_t N = a.N;
+  const int alg = opts->alg;
+  unsigned long long* work = (unsigned long long*)sc.work.ptr;
+  GBDE_CUDA(ctx, cudaMemsetAsync(work, 0, 256, s));
+  a.queue = cfg.persistent ? work : nullptr;
+  a.flag = (int32_t*)(work + 1);
+  if (opts->learned && N > 0) {
+    // learned predictions: first dt (all methods) and stiff label (AUTO)
+    GBDE_CUDA(ctx, mlp_predict(cfg.model, (const float*)ctx->mlp_net.ptr, a,
+                               (float*)sc.pred_dt.ptr, (int8_t*)sc.pred_stiff.ptr, ctx->num_sms,
+                               s));
+    a.pred_dt = (const float*)sc.pred_dt.ptr;
+  }
+  if (alg == GBDE_ALG_AUTO) return solve_auto(ctx, sc, cfg, a, np, opts, s);
+  if (cfg.persistent && N > 1 && N <= INT32_MAX) {
+    // queue order: longest spans first (order.cu)
+    const int32_t* ord = nullptr;
+    GBDE_CUDA(ctx, build_span_order(a.t0, a.tf, N, sc.order.ptr, ctx->num_sms, s, &ord));
+    a.order = ord;
+  }
+  if (N > 0) {
+    const cudaError_t e = launch_alg(alg, cfg, a, s);
+    if (e == cudaErrorNotSupported)
+      return set_err(ctx, GBDE_ERR_UNSUPPORTED, "algorithm %d is not built for model %d", alg,
+                     cfg.model);
+    if (e != cudaSuccess)
+      return set_err(ctx, GBDE_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+  }
+  return GBDE_OK;
+}
+
+int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts* opts,
+                        gbde_outputs* out) {
+  if (!ctx) return set_err(nullptr, GBDE_ERR_INVALID, "ctx is NULL");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  const auto wall0 = std::chrono::steady_clock::now();
+  int32_t ns = 0, np = 0;
+  const int rc0 = check_solve_args(ctx, prob, opts, out, &ns, &np);
+  if (rc0 != GBDE_OK) return rc0;
+  const int64_t N = prob->n_traj;
+  GBDE_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const size_t n_save = (size_t)prob->n_save;
+  const size_t esz = out->u_dtype == GBDE_F32 ? 4 : 8;
+  const size_t save_elems = prob->save_kind == GBDE_SAVE_GRID ? n_save : n_save * (size_t)N;
+  const size_t u_bytes = (size_t)N * n_save * (size_t)ns * esz;
+
+  KArgs a;
+  fill_common(a, prob, opts, out);
   const bool host = prob->mem == GBDE_MEM_HOST;
   if (host) {
     GBDE_CUDA(ctx, ctx->p.ensure((size_t)N * np * 8));
@@ -425,66 +549,12 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
     if (out->method) { GBDE_CUDA(ctx, ctx->method.ensure((size_t)N * 4)); a.method_out = (int32_t*)ctx->method.ptr; }
     if (out->dt_first) { GBDE_CUDA(ctx, ctx->dt1.ensure((size_t)N * 8)); a.dt_first = (double*)ctx->dt1.ptr; }
   } else {
-    a.p = prob->p;
-    a.u0 = prob->u0;
-    a.t0 = prob->t0;
-    a.tf = prob->tf;
-    a.saveat = prob->saveat;
-    a.u_out = out->u;
-    a.retcode = out->retcode;
-    a.naccept = out->naccept;
-    a.nreject = out->nreject;
-    a.nf = out->nf;
-    a.t_end = out->t_end;
-    a.method_out = out->method;
-    a.dt_first = out->dt_first;
+    fill_device_ptrs(a, prob, out);
   }
-  GBDE_CUDA(ctx, ctx->work.ensure(256));
-  unsigned long long* work = (unsigned long long*)ctx->work.ptr;
-  GBDE_CUDA(ctx, cudaMemsetAsync(work, 0, 256, s));
-  a.queue = opts->batching == GBDE_BATCH_PERSISTENT ? work : nullptr;
-  a.flag = (int32_t*)(work + 1);
-
-  LaunchCfg cfg;
-  cfg.alg = alg;
-  cfg.model = prob->model;
-  cfg.precision = opts->precision;
-  cfg.persistent = opts->batching == GBDE_BATCH_PERSISTENT;
-  cfg.block = opts->block_size > 0 ? opts->block_size : 128;
-  cfg.grid = 0;
-  cfg.ctas_per_sm = opts->ctas_per_sm;
-  cfg.num_sms = ctx->num_sms;
-  if (cfg.block > 128 || (cfg.block & 31))
-    return set_err(ctx, GBDE_ERR_INVALID, "block_size must be a multiple of 32 and <= 128");
-
+  const LaunchCfg cfg = make_cfg(ctx, prob, opts);
+  { const int rc = reserve_scratch(ctx, ctx->scratch, N, opts); if (rc != GBDE_OK) return rc; }
   GBDE_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
-  if (opts->learned && N > 0) {
-    // learned predictions: first dt (all methods) and stiff label (AUTO)
-    GBDE_CUDA(ctx, ctx->pred_dt.ensure((size_t)N * sizeof(float)));
-    GBDE_CUDA(ctx, ctx->pred_stiff.ensure((size_t)N));
-    GBDE_CUDA(ctx, mlp_predict(prob->model, (const float*)ctx->mlp_net.ptr, a,
-                               (float*)ctx->pred_dt.ptr, (int8_t*)ctx->pred_stiff.ptr,
-                               ctx->num_sms, s));
-    a.pred_dt = (const float*)ctx->pred_dt.ptr;
-  }
-  if (alg == GBDE_ALG_AUTO) {
-    const int rc = solve_auto(ctx, cfg, a, np, opts, s);
-    if (rc != GBDE_OK) return rc;
-  } else if (cfg.persistent && N > 1 && N <= INT32_MAX) {
-    // queue order: longest spans first (order.cu)
-    GBDE_CUDA(ctx, ctx->order.ensure(span_order_scratch_bytes(N)));
-    const int32_t* ord = nullptr;
-    GBDE_CUDA(ctx, build_span_order(a.t0, a.tf, N, ctx->order.ptr, ctx->num_sms, s, &ord));
-    a.order = ord;
-  }
-  if (N > 0 && alg != GBDE_ALG_AUTO) {
-    const cudaError_t e = launch_alg(alg, cfg, a, s);
-    if (e == cudaErrorNotSupported)
-      return set_err(ctx, GBDE_ERR_UNSUPPORTED, "algorithm %d is not built for model %d", alg,
-                     prob->model);
-    if (e != cudaSuccess)
-      return set_err(ctx, GBDE_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
-  }
+  { const int rc = enqueue_solve(ctx, ctx->scratch, a, cfg, opts, np, s); if (rc != GBDE_OK) return rc; }
   GBDE_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
 
   int32_t flag = 0;
@@ -511,6 +581,150 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
     return set_err(ctx, GBDE_ERR_TIMEOUT, "device deadline of %.3f s reached; unfinished "
                    "trajectories carry GBDE_RET_TIMEOUT", opts->timeout_s);
   return GBDE_OK;
+}
+
+// ---------------------------------------------------------- CUDA graphs
+struct gbde_graph {
+  gbde_ctx* ctx = nullptr;
+  Scratch scratch;  // the graph's own scratch: later solves cannot move it
+  cudaGraphExec_t exec = nullptr;
+  double timeout_s = 0.0;
+};
+
+int gbde_graph_create(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts* opts,
+                      gbde_outputs* out, gbde_graph** graph) {
+  if (!ctx || !graph) return set_err(ctx, GBDE_ERR_INVALID, "ctx and graph must be non-NULL");
+  *graph = nullptr;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  int32_t ns = 0, np = 0;
+  const int rc0 = check_solve_args(ctx, prob, opts, out, &ns, &np);
+  if (rc0 != GBDE_OK) return rc0;
+  if (prob->mem != GBDE_MEM_DEVICE)
+    return set_err(ctx, GBDE_ERR_INVALID, "a graph captures a device-memory problem (GBDE_MEM_DEVICE)");
+  if (opts->alg == GBDE_ALG_AUTO)
+    return set_err(ctx, GBDE_ERR_UNSUPPORTED,
+                   "GBDE_ALG_AUTO sizes its launches on the host and cannot be captured");
+  GBDE_CUDA(ctx, cudaSetDevice(ctx->device));
+  KArgs a;
+  fill_common(a, prob, opts, out);
+  fill_device_ptrs(a, prob, out);
+  const LaunchCfg cfg = make_cfg(ctx, prob, opts);
+  gbde_graph* G = new gbde_graph();
+  G->ctx = ctx;
+  G->timeout_s = opts->timeout_s;
+  int rc = reserve_scratch(ctx, G->scratch, prob->n_traj, opts);
+  if (rc != GBDE_OK) {
+    delete G;
+    return rc;
+  }
+  cudaStream_t s = ctx->stream;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    rc = enqueue_solve(ctx, G->scratch, a, cfg, opts, np, s);
+    e = cudaStreamEndCapture(s, &g);
+  }
+  if (e == cudaSuccess && rc == GBDE_OK) e = cudaGraphInstantiate(&G->exec, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (e != cudaSuccess || rc != GBDE_OK) {
+    G->scratch.release();
+    delete G;
+    return rc != GBDE_OK ? rc : set_err(ctx, GBDE_ERR_CUDA, "graph capture failed: %s",
+                                        cudaGetErrorString(e));
+  }
+  *graph = G;
+  return GBDE_OK;
+}
+
+int gbde_graph_launch(gbde_graph* G, float* device_ms) {
+  if (!G) return set_err(nullptr, GBDE_ERR_INVALID, "graph is NULL");
+  gbde_ctx* ctx = G->ctx;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  GBDE_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  int32_t flag = 0;
+  GBDE_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
+  GBDE_CUDA(ctx, cudaGraphLaunch(G->exec, s));
+  GBDE_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
+  GBDE_CUDA(ctx, cudaMemcpyAsync(&flag, (unsigned long long*)G->scratch.work.ptr + 1, 4,
+                                 cudaMemcpyDeviceToHost, s));
+  GBDE_CUDA(ctx, cudaStreamSynchronize(s));
+  if (device_ms) GBDE_CUDA(ctx, cudaEventElapsedTime(device_ms, ctx->ev0, ctx->ev1));
+  if (flag & 1)
+    return set_err(ctx, GBDE_ERR_TIMEOUT, "device deadline of %.3f s reached; unfinished "
+                   "trajectories carry GBDE_RET_TIMEOUT", G->timeout_s);
+  return GBDE_OK;
+}
+
+int gbde_graph_destroy(gbde_graph* G) {
+  if (!G) return GBDE_OK;
+  gbde_ctx* ctx = G->ctx;
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (G->exec) cudaGraphExecDestroy(G->exec);
+    G->scratch.release();
+  }
+  delete G;
+  return GBDE_OK;
+}
+
+// ------------------------------------------------------------ autotuner
+// Times the solve under each launch configuration (batching, block size,
+// resident CTAs per SM, queue chunk, threads per trajectory) on the caller's
+// own problem and returns the fastest in *best.  `out` receives the results
+// of a final run with the best configuration.
+int gbde_autotune(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts* opts,
+                  gbde_outputs* out, int32_t reps, gbde_opts* best, gbde_tune_entry* table,
+                  int32_t table_cap, int32_t* n_entries) {
+  if (!ctx || !prob || !opts || !out || !best)
+    return set_err(ctx, GBDE_ERR_INVALID, "ctx, prob, opts, out and best must be non-NULL");
+  if (reps <= 0) reps = 2;
+  std::vector<gbde_opts> cand;
+  auto add = [&](int batching, int block, int cps, int chunk, int tpt) {
+    gbde_opts o = *opts;
+    o.batching = batching;
+    o.block_size = block;
+    o.ctas_per_sm = cps;
+    o.chunk = chunk;
+    o.threads_per_traj = tpt;
+    cand.push_back(o);
+  };
+  std::vector<int> tpts = {opts->threads_per_traj};
+  if (prob->model == GBDE_MODEL_VDP_RING8 && opts->alg == GBDE_ALG_TSIT5) tpts = {16, 1};
+  for (int tpt : tpts) {
+    for (int block : {64, 128}) add(GBDE_BATCH_PLAIN, block, 0, 0, tpt);
+    for (int block : {64, 128})
+      for (int cps : {0, 2, 4})
+        for (int chunk : {1, 4}) add(GBDE_BATCH_PERSISTENT, block, cps, chunk, tpt);
+  }
+  float best_ms = 1e30f;
+  int best_i = -1, count = 0;
+  for (size_t k = 0; k < cand.size(); ++k) {
+    float ms = 1e30f;
+    for (int r = 0; r < reps; ++r) {
+      const int rc = gbde_ensemble_solve(ctx, prob, &cand[k], out);
+      if (rc != GBDE_OK) {
+        ms = 1e30f;
+        break;
+      }
+      ms = out->device_ms < ms ? out->device_ms : ms;
+    }
+    if (table && count < table_cap) {
+      table[count] = {cand[k].batching, cand[k].block_size, cand[k].ctas_per_sm, cand[k].chunk,
+                      cand[k].threads_per_traj, ms};
+    }
+    ++count;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best_i = (int)k;
+    }
+  }
+  if (n_entries) *n_entries = count < table_cap ? count : table_cap;
+  if (best_i < 0) return set_err(ctx, GBDE_ERR_INVALID, "no launch configuration ran");
+  *best = cand[best_i];
+  return gbde_ensemble_solve(ctx, prob, best, out);
 }
 
 int gbde_mlp_load(gbde_ctx* ctx, int32_t model, const float* net) {

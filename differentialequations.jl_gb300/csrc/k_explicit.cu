@@ -1,5 +1,6 @@
 // k_explicit.cu -- Tsit5 / Vern7 ensemble kernels (one trajectory per thread).
 #include "explicit_rk.cuh"
+#include "ff.cuh"
 #include "launch.h"
 
 namespace gbde {
@@ -13,6 +14,12 @@ template <template <class, class> class AlgT, class M>
 static cudaError_t dispatch_prec(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
   if (cfg.precision == GBDE_PREC_MIXED)
     return launch_kernel(k_erk<AlgT<M, float>, M, float, true>, cfg, a, s);
+  if (cfg.precision == GBDE_PREC_F32X2) {
+    if constexpr (M::N <= 8)  // pairs double the register state; the 16-state ring has team kernels
+      return launch_kernel(k_erk<AlgT<M, ff>, M, ff, true>, cfg, a, s);
+    else
+      return cudaErrorNotSupported;
+  }
   return launch_kernel(k_erk<AlgT<M, double>, M, double, false>, cfg, a, s);
 }
 

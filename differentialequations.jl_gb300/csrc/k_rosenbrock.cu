@@ -1,6 +1,7 @@
 // k_rosenbrock.cu -- Rosenbrock23 / Rodas5 / Rodas5P ensemble kernels
 // (one trajectory per thread, W-matrix LU in registers; models with n <= 3).
 #include "rosenbrock.cuh"
+#include "ff.cuh"
 #include "launch.h"
 
 namespace gbde {
@@ -17,6 +18,8 @@ template <template <class, class> class AlgT, class M>
 static cudaError_t dispatch_prec(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
   if (cfg.precision == GBDE_PREC_MIXED)
     return launch_kernel(k_ros<AlgT<M, float>, M, float, true>, cfg, a, s);
+  if (cfg.precision == GBDE_PREC_F32X2)
+    return launch_kernel(k_ros<AlgT<M, ff>, M, ff, true>, cfg, a, s);
   return launch_kernel(k_ros<AlgT<M, double>, M, double, false>, cfg, a, s);
 }
 

@@ -13,6 +13,7 @@ struct LaunchCfg {
   int grid;           // CTAs (persistent) -- 0 = derive from N
   int ctas_per_sm;    // persistent: resident CTAs per SM (0 = occupancy max)
   int num_sms;
+  int tpt = 0;        // threads per trajectory (0 = model default, 1, 16)
 };
 
 // Returns cudaSuccess, or cudaErrorNotSupported for an unknown combination.

@@ -141,8 +141,13 @@ extern "C" int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_
   if (!is_ode(alg) && !is_sde(alg)) return fail(GBDE_ERR_INVALID, "unknown algorithm id %d", alg);
   if (is_sde(alg) && prob->model != GBDE_MODEL_LOTKA_VOLTERRA)
     return fail(GBDE_ERR_UNSUPPORTED, "SDE algorithms need a model with a noise term");
-  if (opts->precision != GBDE_PREC_FP64 && opts->precision != GBDE_PREC_MIXED)
+  if (opts->precision != GBDE_PREC_FP64 && opts->precision != GBDE_PREC_MIXED &&
+      opts->precision != GBDE_PREC_F32X2)
     return fail(GBDE_ERR_INVALID, "unknown precision %d", opts->precision);
+  if (opts->precision == GBDE_PREC_F32X2 &&
+      (is_sde(alg) || prob->model == GBDE_MODEL_VDP_RING8))
+    return fail(GBDE_ERR_UNSUPPORTED,
+                "GBDE_PREC_F32X2 is built for the one-thread-per-trajectory ODE kernels");
   if (opts->batching != GBDE_BATCH_PLAIN && opts->batching != GBDE_BATCH_PERSISTENT)
     return fail(GBDE_ERR_INVALID, "unknown batching %d", opts->batching);
   if (opts->adaptive && !(opts->reltol > 0.0 && opts->abstol > 0.0))
@@ -219,6 +224,7 @@ extern "C" int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_
   a.timeout_ns = opts->timeout_s > 0 ? (uint64_t)(opts->timeout_s * 1e9) : 0;
   a.ctl = ctl_consts(opts->beta1, opts->beta2, opts->gamma, opts->qmin, opts->qmax,
                      opts->qsteady_min, opts->qsteady_max, opts->qoldinit);
+  a.chunk = opts->chunk > 0 ? opts->chunk : 1;
   a.queue = opts->batching == GBDE_BATCH_PERSISTENT ? queue : nullptr;
   a.flag = flag_dev;
 
@@ -231,6 +237,7 @@ extern "C" int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_
   cfg.grid = 0;
   cfg.ctas_per_sm = opts->ctas_per_sm;
   cfg.num_sms = dev.num_sms;
+  cfg.tpt = opts->threads_per_traj;
 
   if (N > 0) {
     const cudaError_t e = launch_alg(alg, cfg, a, s);

@@ -9,6 +9,7 @@
 // WOperator / StaticWOperator of qa.jl:129,113 and whose LU the reference
 // delegates to LinearSolve.  W and its LU are FP64 in both precision modes.
 #pragma once
+#include "ff.cuh"
 #include "solver.cuh"
 #include "tableaus.h"
 
@@ -95,6 +96,71 @@ struct SmallLU {
   }
 };
 
+// The FP64 LU factors rounded to ff, with the triangular solves in ff
+// arithmetic (the F32X2 precision: the factorisation stays FP64, each of the
+// 3-8 solves per step runs on the FP32 pipe).
+template <int N>
+struct FFLU {
+  ff A[N][N];
+  ff inv[N];
+  int piv[N];
+  GBDE_D void from(const SmallLU<N>& W) {
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+#pragma unroll
+      for (int c = 0; c < N; ++c) A[r][c] = ff(W.A[r][c]);
+      inv[r] = ff(W.inv[r]);
+      piv[r] = W.piv[r];
+    }
+  }
+  GBDE_D void solve_t(const ff* rhs, ff* x) const {
+    ff b[N];
+#pragma unroll
+    for (int c = 0; c < N; ++c) b[c] = rhs[c];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+#pragma unroll
+      for (int r = k + 1; r < N; ++r) {
+        const bool sw = (piv[k] == r);
+        const ff xk = b[k], yr = b[r];
+        b[k] = sw ? yr : xk;
+        b[r] = sw ? xk : yr;
+      }
+#pragma unroll
+      for (int r = k + 1; r < N; ++r) b[r] -= A[r][k] * b[k];
+    }
+#pragma unroll
+    for (int k = N - 1; k >= 0; --k) {
+      ff acc = b[k];
+#pragma unroll
+      for (int c = k + 1; c < N; ++c) acc -= A[k][c] * x[c];
+      x[k] = acc * inv[k];
+    }
+  }
+};
+
+// W-matrix solver for a stepper in precision T: the FP64 LU itself, or its
+// ff copy for T = ff.
+template <int N, class T>
+struct WSolver {
+  SmallLU<N> W;  // a register copy (no address of the factor escapes)
+  GBDE_D void setup(const SmallLU<N>& w) { W = w; }
+  GBDE_D void solve_t(const T* rhs, T* x) const { W.solve_t(rhs, x); }
+};
+template <int N>
+struct WSolver<N, ff> {
+  FFLU<N> L;
+  GBDE_D void setup(const SmallLU<N>& w) { L.from(w); }
+  GBDE_D void solve_t(const ff* rhs, ff* x) const { L.solve_t(rhs, x); }
+};
+
+// C / h in precision T (for ff from ff operands, with no FP64 conversion)
+template <class T>
+GBDE_D T c_over_h(double C, double ih, T ih_t) {
+  if constexpr (is_ff<T>::value) return T(C) * ih_t;
+  else return T(C * ih);
+}
+
 // -------------------------------------------------------- Rosenbrock23
 // Shampine & Reichelt (1997): W = I - h d J,
 //   k1 = W^{-1} F0,  F1 = f(y0 + h/2 k1),  k2 = W^{-1}(F1 - k1) + k1,
@@ -133,15 +199,17 @@ struct Ros23Alg {
 #pragma unroll
       for (int c = 0; c < N; ++c) W.A[r][c] = (r == c ? 1.0 : 0.0) - hd * (double)J[r][c];
     W.factor();
+    WSolver<N, T> S;
+    S.setup(W);
     const T h = (T)dt;
-    W.solve_t(F0, k1);
+    S.solve_t(F0, k1);
     T y[N], F1[N], r3[N], k3[N];
 #pragma unroll
     for (int c = 0; c < N; ++c) y[c] = uu[c] + T(0.5) * h * k1[c];
     M::f(F1, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c) y[c] = F1[c] - k1[c];
-    W.solve_t(y, k2);
+    S.solve_t(y, k2);
 #pragma unroll
     for (int c = 0; c < N; ++c) {
       k2[c] += k1[c];
@@ -152,10 +220,13 @@ struct Ros23Alg {
 #pragma unroll
     for (int c = 0; c < N; ++c)
       r3[c] = F2[c] - T(e32) * (k2[c] - F1[c]) - T(2) * (k1[c] - F0[c]);
-    W.solve_t(r3, k3);
+    S.solve_t(r3, k3);
     T err[N];
+    T h6;
+    if constexpr (is_ff<T>::value) h6 = h * T(1.0 / 6.0);  // ff has no division
+    else h6 = h / T(6);
 #pragma unroll
-    for (int c = 0; c < N; ++c) err[c] = h / T(6) * (k1[c] - T(2) * k2[c] + k3[c]);
+    for (int c = 0; c < N; ++c) err[c] = h6 * (k1[c] - T(2) * k2[c] + k3[c]);
     return err_ms<N>(err, uu, un, abstol, reltol);
   }
 
@@ -262,34 +333,37 @@ struct RodasAlg {
 #pragma unroll
       for (int c = 0; c < N; ++c) W.A[r][c] = r == c ? dg - (double)J[r][c] : -(double)J[r][c];
     W.factor();
-    const T c21 = T(K::C21 * ih), c31 = T(K::C31 * ih), c32 = T(K::C32 * ih);
-    const T c41 = T(K::C41 * ih), c42 = T(K::C42 * ih), c43 = T(K::C43 * ih);
-    const T c51 = T(K::C51 * ih), c52 = T(K::C52 * ih), c53 = T(K::C53 * ih),
-            c54 = T(K::C54 * ih);
-    const T c61 = T(K::C61 * ih), c62 = T(K::C62 * ih), c63 = T(K::C63 * ih),
-            c64 = T(K::C64 * ih), c65 = T(K::C65 * ih);
-    const T c71 = T(K::C71 * ih), c72 = T(K::C72 * ih), c73 = T(K::C73 * ih),
-            c74 = T(K::C74 * ih), c75 = T(K::C75 * ih), c76 = T(K::C76 * ih);
-    const T c81 = T(K::C81 * ih), c82 = T(K::C82 * ih), c83 = T(K::C83 * ih),
-            c84 = T(K::C84 * ih), c85 = T(K::C85 * ih), c86 = T(K::C86 * ih),
-            c87 = T(K::C87 * ih);
+    WSolver<N, T> S;
+    S.setup(W);
+    const T iht = (T)ih;
+#define GBDE_CH(X) c_over_h<T>(K::X, ih, iht)
+    const T c21 = GBDE_CH(C21), c31 = GBDE_CH(C31), c32 = GBDE_CH(C32);
+    const T c41 = GBDE_CH(C41), c42 = GBDE_CH(C42), c43 = GBDE_CH(C43);
+    const T c51 = GBDE_CH(C51), c52 = GBDE_CH(C52), c53 = GBDE_CH(C53), c54 = GBDE_CH(C54);
+    const T c61 = GBDE_CH(C61), c62 = GBDE_CH(C62), c63 = GBDE_CH(C63), c64 = GBDE_CH(C64),
+            c65 = GBDE_CH(C65);
+    const T c71 = GBDE_CH(C71), c72 = GBDE_CH(C72), c73 = GBDE_CH(C73), c74 = GBDE_CH(C74),
+            c75 = GBDE_CH(C75), c76 = GBDE_CH(C76);
+    const T c81 = GBDE_CH(C81), c82 = GBDE_CH(C82), c83 = GBDE_CH(C83), c84 = GBDE_CH(C84),
+            c85 = GBDE_CH(C85), c86 = GBDE_CH(C86), c87 = GBDE_CH(C87);
+#undef GBDE_CH
     T y[N], fy[N], r[N], s8[N];
     // stage 1
-    W.solve_t(F0, s1);
+    S.solve_t(F0, s1);
     // stage 2
 #pragma unroll
     for (int c = 0; c < N; ++c) y[c] = uu[c] + T(K::a21) * s1[c];
     M::f(fy, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c) r[c] = fy[c] + c21 * s1[c];
-    W.solve_t(r, s2);
+    S.solve_t(r, s2);
     // stage 3
 #pragma unroll
     for (int c = 0; c < N; ++c) y[c] = uu[c] + T(K::a31) * s1[c] + T(K::a32) * s2[c];
     M::f(fy, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c) r[c] = fy[c] + c31 * s1[c] + c32 * s2[c];
-    W.solve_t(r, s3);
+    S.solve_t(r, s3);
     // stage 4
 #pragma unroll
     for (int c = 0; c < N; ++c)
@@ -297,7 +371,7 @@ struct RodasAlg {
     M::f(fy, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c) r[c] = fy[c] + c41 * s1[c] + c42 * s2[c] + c43 * s3[c];
-    W.solve_t(r, s4);
+    S.solve_t(r, s4);
     // stage 5
 #pragma unroll
     for (int c = 0; c < N; ++c)
@@ -307,7 +381,7 @@ struct RodasAlg {
 #pragma unroll
     for (int c = 0; c < N; ++c)
       r[c] = fy[c] + c51 * s1[c] + c52 * s2[c] + c53 * s3[c] + c54 * s4[c];
-    W.solve_t(r, s5);
+    S.solve_t(r, s5);
     // stage 6
 #pragma unroll
     for (int c = 0; c < N; ++c)
@@ -317,7 +391,7 @@ struct RodasAlg {
 #pragma unroll
     for (int c = 0; c < N; ++c)
       r[c] = fy[c] + c61 * s1[c] + c62 * s2[c] + c63 * s3[c] + c64 * s4[c] + c65 * s5[c];
-    W.solve_t(r, s6);
+    S.solve_t(r, s6);
     // stage 7: y = U_6 + u_6
 #pragma unroll
     for (int c = 0; c < N; ++c) y[c] += s6[c];
@@ -326,7 +400,7 @@ struct RodasAlg {
     for (int c = 0; c < N; ++c)
       r[c] = fy[c] + c71 * s1[c] + c72 * s2[c] + c73 * s3[c] + c74 * s4[c] + c75 * s5[c] +
              c76 * s6[c];
-    W.solve_t(r, s7);
+    S.solve_t(r, s7);
     // stage 8: y = U_7 + u_7
 #pragma unroll
     for (int c = 0; c < N; ++c) y[c] += s7[c];
@@ -335,7 +409,7 @@ struct RodasAlg {
     for (int c = 0; c < N; ++c)
       r[c] = fy[c] + c81 * s1[c] + c82 * s2[c] + c83 * s3[c] + c84 * s4[c] + c85 * s5[c] +
              c86 * s6[c] + c87 * s7[c];
-    W.solve_t(r, s8);
+    S.solve_t(r, s8);
     nf += 7;
 #pragma unroll
     for (int c = 0; c < N; ++c) un[c] = y[c] + s8[c];

@@ -53,6 +53,7 @@ struct KArgs {
   const float* pred_dt;       // optional predicted first dt per trajectory
   CtlK ctl;                   // step-size controller constants (controller.h)
   double* dt_first;           // optional: size of the first accepted step
+  int32_t chunk;              // persistent queue positions per fetch (>= 1)
 };
 
 GBDE_D uint64_t global_ns() {
@@ -65,12 +66,15 @@ GBDE_D uint64_t global_ns() {
 // Plain launch: each thread takes its own index once.  Persistent launch:
 // threads that need work take consecutive indices from a global counter
 // with one atomic per group of converged lanes (warp-aggregated).
+// With chunk c > 1 a thread takes c consecutive queue positions per fetch.
 struct WorkSource {
   int64_t first;
   bool used;
+  unsigned long long cur, end;  // this thread's remaining chunk [cur, end)
   GBDE_D void init() {
     first = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     used = false;
+    cur = end = 0;
   }
   GBDE_D int64_t next(const KArgs& a) {
     if (a.queue == nullptr) {
@@ -79,13 +83,21 @@ struct WorkSource {
       if (first >= a.N) return -1;
       return a.order ? (int64_t)a.order[first] : first;
     }
-    namespace cg = cooperative_groups;
-    cg::coalesced_group g = cg::coalesced_threads();
-    unsigned long long base = 0;
-    if (g.thread_rank() == 0) base = atomicAdd(a.queue, (unsigned long long)g.size());
-    base = g.shfl(base, 0);
-    const unsigned long long idx = base + g.thread_rank();
-    if (idx >= (unsigned long long)a.N) return -1;
+    if (cur >= end) {
+      namespace cg = cooperative_groups;
+      const unsigned long long c = a.chunk > 1 ? (unsigned long long)a.chunk : 1ull;
+      cg::coalesced_group g = cg::coalesced_threads();
+      unsigned long long base = 0;
+      if (g.thread_rank() == 0) base = atomicAdd(a.queue, (unsigned long long)g.size() * c);
+      base = g.shfl(base, 0);
+      cur = base + g.thread_rank() * c;
+      end = cur + c;
+    }
+    const unsigned long long idx = cur++;
+    if (idx >= (unsigned long long)a.N) {
+      cur = end = ~0ull;  // exhausted
+      return -1;
+    }
     return a.order ? (int64_t)a.order[idx] : (int64_t)idx;
   }
 };

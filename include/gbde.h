@@ -99,6 +99,12 @@ extern "C" {
 #define GBDE_PREC_FP64 0  /* everything in FP64                                  */
 #define GBDE_PREC_MIXED 1 /* FP32 state and stages; FP64 compensated time, FP64
                              error norm, FP64 W-matrix LU                         */
+#define GBDE_PREC_F32X2 2 /* state, stages and right-hand sides as unevaluated
+                             pairs of FP32 (~48-bit significand) on the FP32 pipe;
+                             FP64 W-matrix LU (solves on its pair-rounded factors),
+                             FP64 error norm and compensated time.  One thread per
+                             trajectory ODE kernels (not SDE, not the 16-state
+                             ring, not AUTO)                                       */
 
 /* ---- batching --------------------------------------------------------- */
 #define GBDE_BATCH_PLAIN 0      /* one thread per trajectory, one launch      */
@@ -164,6 +170,9 @@ typedef struct {
   int32_t ctas_per_sm; /* persistent CTAs per SM (0 = tuned default)      */
   double stiff_threshold; /* GBDE_ALG_AUTO without MLP: stiff iff p[0] > this */
   double timeout_s;    /* device deadline per call (0 = none)             */
+  int32_t threads_per_traj; /* 0 = model default; 1 = one thread per trajectory;
+                          16 = a 16-lane team (16-state models)            */
+  int32_t reserved_;   /* zero                                            */
 } gbde_opts;
 
 /* Results.  u is [N][n_save][n_state] of u_dtype; retcode [N]; the step
@@ -204,6 +213,36 @@ GBDE_API int gbde_opts_default(int32_t alg, gbde_opts* out);
  * the kernels have finished (device mode). */
 GBDE_API int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob,
                         const gbde_opts* opts, gbde_outputs* out);
+
+/* ---- CUDA graphs ---------------------------------------------------------
+ * Capture the whole device work of one solve of a device-memory problem
+ * (queue and status words, learned predictions, queue order, step kernels)
+ * as a CUDA graph; gbde_graph_launch replays it on the context's stream.
+ * The graph keeps the problem's and outputs' device pointers: refill the
+ * input arrays in place between launches.  No counterpart in the reference
+ * (the spec batching: repeated ensembles at launch-free cost).
+ * GBDE_ALG_AUTO cannot be captured (it sizes its launches on the host). */
+typedef struct gbde_graph gbde_graph;
+GBDE_API int gbde_graph_create(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts* opts,
+                      gbde_outputs* out, gbde_graph** graph);
+/* Replays and waits; device_ms (may be NULL) receives the replay's time. */
+GBDE_API int gbde_graph_launch(gbde_graph* graph, float* device_ms);
+GBDE_API int gbde_graph_destroy(gbde_graph* graph);
+
+/* ---- autotuner -----------------------------------------------------------
+ * Times the solve of `prob` under each launch configuration -- batching,
+ * block size, resident CTAs per SM, persistent-queue chunk and (16-state
+ * ring, Tsit5) threads per trajectory -- `reps` times each, writes the
+ * fastest options to *best and the timing table to table[0..*n_entries),
+ * and leaves the results of a final run with *best in `out`.  No
+ * counterpart in the reference. */
+typedef struct {
+  int32_t batching, block_size, ctas_per_sm, chunk, threads_per_traj;
+  float device_ms;     /* best of reps; 1e30 if the configuration failed  */
+} gbde_tune_entry;
+GBDE_API int gbde_autotune(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts* opts,
+                  gbde_outputs* out, int32_t reps, gbde_opts* best,
+                  gbde_tune_entry* table, int32_t table_cap, int32_t* n_entries);
 
 /* Model metadata: state and parameter counts of a built-in model. */
 GBDE_API int gbde_model_info(int32_t model, int32_t* n_state, int32_t* n_param);

@@ -367,3 +367,51 @@ def test_rcp64_within_one_ulp(de):
     1/dt) agrees with the device's IEEE division to one ulp."""
     err = de._capi.context(0).check_rcp64(1 << 22)
     assert err <= 2.0 ** -52, err
+
+
+# F32X2: state, stages and right-hand sides as FP32 pairs (~48 bits), FP64 LU,
+# norm and time.  Near-FP64 accuracy: the steps follow the FP64 oracle's and
+# the saved states agree to well inside the tolerance.
+@pytest.mark.parametrize("model_name,alg,rt,at", [
+    ("robertson", "RODAS5", 1e-6, 1e-10), ("robertson", "RODAS5P", 1e-6, 1e-10),
+    ("robertson", "ROSENBROCK23", 1e-6, 1e-10), ("lorenz", "TSIT5", 1e-8, 1e-8),
+    ("lorenz", "VERN7", 1e-8, 1e-8), ("lorenz", "RODAS5", 1e-7, 1e-7)])
+def test_f32x2_vs_fp64_oracle(de, oracle, rng, model_name, alg, rt, at):
+    capi = de._capi
+    model = getattr(de.models, model_name)
+    N = 2000
+    p, u0, t0, tf = make_inputs(de, model, N, rng)
+    if model_name == "robertson":
+        saveat = tf[:, None] * 10 ** (-5 + 5 * np.arange(20) / 19)
+        kind = capi.SAVE_PER_TRAJ
+    else:
+        saveat = de.save_grid(0.0, 1.0, 0.1)
+        kind = capi.SAVE_GRID
+    for batching in ("plain", "persistent"):
+        g, r, _ = run_both(de, oracle, model, getattr(capi, "ALG_" + alg), p, u0, t0, tf, saveat,
+                           kind, batching=batching, reltol=rt, abstol=at)
+        g2 = de.solve_arrays(model, _f32x2(capi, alg, rt, at, batching), p, u0, t0, tf, saveat, kind)
+        assert np.all(g2["retcode"] == capi.RET_SUCCESS)
+        e = (np.abs(g2["u"] - r["u"]) / (at + rt * np.abs(r["u"]))).max(axis=(1, 2))
+        assert np.percentile(e, 99) <= 0.1, np.percentile(e, 99)
+        assert e.max() <= 10.0, e.max()
+        assert np.mean(g2["naccept"] == r["naccept"]) >= 0.99
+
+
+def _f32x2(capi, alg, rt, at, batching):
+    o = capi.opts_default(getattr(capi, "ALG_" + alg))
+    o.reltol, o.abstol = rt, at
+    o.precision = capi.PREC_F32X2
+    o.batching = capi.BATCH_PERSISTENT if batching == "persistent" else capi.BATCH_PLAIN
+    return o
+
+
+def test_f32x2_rejected_where_not_built(de, rng):
+    capi = de._capi
+    o = capi.opts_default(capi.ALG_EM)
+    o.dt = 1e-2
+    o.precision = capi.PREC_F32X2
+    p, u0, t0, tf = make_inputs(de, de.models.lotka_volterra, 4, rng)
+    with pytest.raises(capi.GBDEError) as e:
+        de.solve_arrays(de.models.lotka_volterra, o, p, u0, t0, tf, np.array([0.0]), capi.SAVE_GRID)
+    assert e.value.code == capi.GBDE_ERR_UNSUPPORTED
