@@ -670,9 +670,10 @@ def main():
                      "fp32_peak_tflops": peak32,
                      "algorithmic_flops_per_step": flops, "kernel_ms": chosen_kern},
         "steps_per_traj_mean": float((st["naccept"] + st["nreject"]).mean()),
-        # per timed step: the solve kernel, plus histogram / scan / scatter of
-        # the longest-span-first queue order for persistent forms
-        "gpu_launches": args.steps * (4 if forms[args.chosen][0] == "persistent" else 1),
+        # per timed step: the initial-dt pre-pass and the solve kernel, plus
+        # histogram / scan / scatter of the longest-span-first queue order for
+        # persistent forms
+        "gpu_launches": args.steps * (5 if forms[args.chosen][0] == "persistent" else 2),
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
     }

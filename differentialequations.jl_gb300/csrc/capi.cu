@@ -51,9 +51,9 @@ struct DevBuf {
 // AUTO lists; the learned predictions.  A context keeps one set for its
 // solves; a captured graph keeps its own.
 struct Scratch {
-  DevBuf work, order, part, pred_dt, pred_stiff;
+  DevBuf work, order, part, pred_dt, pred_stiff, dt_init;
   void release() {
-    for (DevBuf* b : {&work, &order, &part, &pred_dt, &pred_stiff}) b->release();
+    for (DevBuf* b : {&work, &order, &part, &pred_dt, &pred_stiff, &dt_init}) b->release();
   }
 };
 
@@ -451,7 +451,21 @@ static LaunchCfg make_cfg(const gbde_ctx* ctx, const gbde_problem* prob, const g
 // Allocate every scratch buffer a solve of N trajectories with these options
 // uses, before any work is enqueued (a stream capture must not meet a
 // cudaMalloc).
-static int reserve_scratch(gbde_ctx* ctx, Scratch& sc, int64_t N, const gbde_opts* opts) {
+// Adaptive one-thread-per-trajectory ODE solves start from the Hairer-Wanner
+// step computed by a converged pre-pass kernel (k_init_dt) instead of inside
+// the step kernel, where each refill would run it for one lane of a warp.
+static bool uses_dt_prepass(const gbde_opts* o, int model) {
+  const int a = o->alg;
+  const bool ode = a == GBDE_ALG_TSIT5 || a == GBDE_ALG_VERN7 || a == GBDE_ALG_ROSENBROCK23 ||
+                   a == GBDE_ALG_RODAS5 || a == GBDE_ALG_RODAS5P;
+  const bool team = model == GBDE_MODEL_VDP_RING8 &&
+                    (a == GBDE_ALG_RODAS5 || a == GBDE_ALG_RODAS5P ||
+                     (a == GBDE_ALG_TSIT5 && o->threads_per_traj != 1));
+  return ode && !team && o->adaptive && !(o->dt > 0.0) && !o->learned;
+}
+
+static int reserve_scratch(gbde_ctx* ctx, Scratch& sc, int64_t N, const gbde_opts* opts,
+                           int model) {
   GBDE_CUDA(ctx, sc.work.ensure(256));
   if (opts->learned && N > 0) {
     GBDE_CUDA(ctx, sc.pred_dt.ensure((size_t)N * sizeof(float)));
@@ -461,6 +475,8 @@ static int reserve_scratch(gbde_ctx* ctx, Scratch& sc, int64_t N, const gbde_opt
     GBDE_CUDA(ctx, sc.part.ensure(partition_scratch_bytes(N)));
   else if (opts->batching == GBDE_BATCH_PERSISTENT && N > 1 && N <= INT32_MAX)
     GBDE_CUDA(ctx, sc.order.ensure(span_order_scratch_bytes(N)));
+  if (uses_dt_prepass(opts, model) && N > 0)
+    GBDE_CUDA(ctx, sc.dt_init.ensure((size_t)N * sizeof(double)));
   return GBDE_OK;
 }
 
@@ -490,7 +506,9 @@ static int enqueue_solve(gbde_ctx* ctx, Scratch& sc, KArgs& a, const LaunchCfg& 
     a.order = ord;
   }
   if (N > 0) {
-    const cudaError_t e = launch_alg(alg, cfg, a, s);
+    LaunchCfg c = cfg;
+    if (uses_dt_prepass(opts, cfg.model)) c.dt_init = (double*)sc.dt_init.ptr;
+    const cudaError_t e = launch_alg(alg, c, a, s);
     if (e == cudaErrorNotSupported)
       return set_err(ctx, GBDE_ERR_UNSUPPORTED, "algorithm %d is not built for model %d", alg,
                      cfg.model);
@@ -552,7 +570,7 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
     fill_device_ptrs(a, prob, out);
   }
   const LaunchCfg cfg = make_cfg(ctx, prob, opts);
-  { const int rc = reserve_scratch(ctx, ctx->scratch, N, opts); if (rc != GBDE_OK) return rc; }
+  { const int rc = reserve_scratch(ctx, ctx->scratch, N, opts, prob->model); if (rc != GBDE_OK) return rc; }
   GBDE_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
   { const int rc = enqueue_solve(ctx, ctx->scratch, a, cfg, opts, np, s); if (rc != GBDE_OK) return rc; }
   GBDE_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
@@ -612,7 +630,7 @@ int gbde_graph_create(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts* 
   gbde_graph* G = new gbde_graph();
   G->ctx = ctx;
   G->timeout_s = opts->timeout_s;
-  int rc = reserve_scratch(ctx, G->scratch, prob->n_traj, opts);
+  int rc = reserve_scratch(ctx, G->scratch, prob->n_traj, opts, prob->model);
   if (rc != GBDE_OK) {
     delete G;
     return rc;

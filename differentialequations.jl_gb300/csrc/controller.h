@@ -162,19 +162,18 @@ GBDE_HD double hw_dt(double h0, double s1, double s2, double tspan, int order) {
   return fmin(fmin(100.0 * h0, h1), tspan);
 }
 
-// Reciprocal for the hot loops: a fast hardware estimate refined by two
-// Newton-Raphson steps r <- r + r (1 - x r) (quadratic convergence: the
-// estimate's ~2^-22 relative error becomes ~2^-88, i.e. the result is within
-// an ulp of 1/x).  Used where an IEEE division would cost ~10 FP64
+// Reciprocal for the hot loops: a fast hardware estimate refined by one
+// Newton-Raphson step r <- r + r (1 - x r) (quadratic convergence: the
+// estimate's ~2^-20 relative error becomes ~2^-40; measured on the GPU
+// against IEEE division: 9.6e-13).  Its uses -- the error norm's scales, 1/h, the LU
+// pivots -- need far less than that, and an IEEE division costs ~10 FP64
 // instructions on GB300's narrow FP64 pipe.  x must be finite, normal and
 // non-zero; otherwise the result is not finite.
 GBDE_HD double rcp64(double x) {
 #if defined(__CUDA_ARCH__)
   double r;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
-  double e = fma(-x, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-x, r, 1.0);
+  const double e = fma(-x, r, 1.0);
   return fma(r, e, r);
 #else
   return 1.0 / x;

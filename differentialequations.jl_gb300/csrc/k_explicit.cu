@@ -13,14 +13,16 @@ __global__ void __launch_bounds__(128) k_erk(const KArgs a) {
 template <template <class, class> class AlgT, class M>
 static cudaError_t dispatch_prec(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
   if (cfg.precision == GBDE_PREC_MIXED)
-    return launch_kernel(k_erk<AlgT<M, float>, M, float, true>, cfg, a, s);
+    return launch_step_kernel<AlgT<M, float>, M, float>(k_erk<AlgT<M, float>, M, float, true>,
+                                                         cfg, a, s);
   if (cfg.precision == GBDE_PREC_F32X2) {
     if constexpr (M::N <= 8)  // pairs double the register state; the 16-state ring has team kernels
-      return launch_kernel(k_erk<AlgT<M, ff>, M, ff, true>, cfg, a, s);
+      return launch_step_kernel<AlgT<M, ff>, M, ff>(k_erk<AlgT<M, ff>, M, ff, true>, cfg, a, s);
     else
       return cudaErrorNotSupported;
   }
-  return launch_kernel(k_erk<AlgT<M, double>, M, double, false>, cfg, a, s);
+  return launch_step_kernel<AlgT<M, double>, M, double>(k_erk<AlgT<M, double>, M, double, false>,
+                                                         cfg, a, s);
 }
 
 template <template <class, class> class AlgT>

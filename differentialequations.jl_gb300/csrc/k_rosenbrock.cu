@@ -17,10 +17,12 @@ template <class M, class T> using Rodas5PA = RodasAlg<M, T, Rodas5PTag>;
 template <template <class, class> class AlgT, class M>
 static cudaError_t dispatch_prec(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
   if (cfg.precision == GBDE_PREC_MIXED)
-    return launch_kernel(k_ros<AlgT<M, float>, M, float, true>, cfg, a, s);
+    return launch_step_kernel<AlgT<M, float>, M, float>(k_ros<AlgT<M, float>, M, float, true>,
+                                                         cfg, a, s);
   if (cfg.precision == GBDE_PREC_F32X2)
-    return launch_kernel(k_ros<AlgT<M, ff>, M, ff, true>, cfg, a, s);
-  return launch_kernel(k_ros<AlgT<M, double>, M, double, false>, cfg, a, s);
+    return launch_step_kernel<AlgT<M, ff>, M, ff>(k_ros<AlgT<M, ff>, M, ff, true>, cfg, a, s);
+  return launch_step_kernel<AlgT<M, double>, M, double>(k_ros<AlgT<M, double>, M, double, false>,
+                                                         cfg, a, s);
 }
 
 template <template <class, class> class AlgT>

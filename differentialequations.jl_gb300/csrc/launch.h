@@ -14,6 +14,7 @@ struct LaunchCfg {
   int ctas_per_sm;    // persistent: resident CTAs per SM (0 = occupancy max)
   int num_sms;
   int tpt = 0;        // threads per trajectory (0 = model default, 1, 16)
+  double* dt_init = nullptr;  // scratch [N]: run the initial-dt pre-pass into it
 };
 
 // Returns cudaSuccess, or cudaErrorNotSupported for an unknown combination.
@@ -61,6 +62,19 @@ cudaError_t build_partition(const double* p, int np, double thr, const int8_t* p
 // Learned predictions for a solve (mlp.cu): pred_dt[N] and pred_stiff[N].
 cudaError_t mlp_predict(int model, const float* net, const KArgs& a, float* pred_dt,
                         int8_t* pred_stiff, int num_sms, cudaStream_t s);
+
+// One-thread-per-trajectory step kernel, preceded by the initial-dt pre-pass
+// (k_init_dt) when cfg.dt_init is set.
+template <class Alg, class M, class T, class K>
+cudaError_t launch_step_kernel(K kern, const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
+  if (cfg.dt_init == nullptr) return launch_kernel(kern, cfg, a, s);
+  const long long want = (a.N + 127) / 128, cap = 8LL * cfg.num_sms;
+  const int grid = (int)(want < cap ? (want > 0 ? want : 1) : cap);
+  k_init_dt<Alg, M, T><<<grid, 128, 0, s>>>(a, cfg.dt_init);
+  KArgs b = a;
+  b.dt_init = cfg.dt_init;
+  return launch_kernel(kern, cfg, b, s);
+}
 
 // Team kernels (team.cuh): 16 threads per trajectory.
 cudaError_t launch_team(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);

@@ -154,13 +154,6 @@ struct WSolver<N, ff> {
   GBDE_D void solve_t(const ff* rhs, ff* x) const { L.solve_t(rhs, x); }
 };
 
-// C / h in precision T (for ff from ff operands, with no FP64 conversion)
-template <class T>
-GBDE_D T c_over_h(double C, double ih, T ih_t) {
-  if constexpr (is_ff<T>::value) return T(C) * ih_t;
-  else return T(C * ih);
-}
-
 // -------------------------------------------------------- Rosenbrock23
 // Shampine & Reichelt (1997): W = I - h d J,
 //   k1 = W^{-1} F0,  F1 = f(y0 + h/2 k1),  k2 = W^{-1}(F1 - k1) + k1,
@@ -335,18 +328,8 @@ struct RodasAlg {
     W.factor();
     WSolver<N, T> S;
     S.setup(W);
+    // r_i = f(y_i) + (1/h) sum_j C_ij u_j, with 1/h applied once per stage
     const T iht = (T)ih;
-#define GBDE_CH(X) c_over_h<T>(K::X, ih, iht)
-    const T c21 = GBDE_CH(C21), c31 = GBDE_CH(C31), c32 = GBDE_CH(C32);
-    const T c41 = GBDE_CH(C41), c42 = GBDE_CH(C42), c43 = GBDE_CH(C43);
-    const T c51 = GBDE_CH(C51), c52 = GBDE_CH(C52), c53 = GBDE_CH(C53), c54 = GBDE_CH(C54);
-    const T c61 = GBDE_CH(C61), c62 = GBDE_CH(C62), c63 = GBDE_CH(C63), c64 = GBDE_CH(C64),
-            c65 = GBDE_CH(C65);
-    const T c71 = GBDE_CH(C71), c72 = GBDE_CH(C72), c73 = GBDE_CH(C73), c74 = GBDE_CH(C74),
-            c75 = GBDE_CH(C75), c76 = GBDE_CH(C76);
-    const T c81 = GBDE_CH(C81), c82 = GBDE_CH(C82), c83 = GBDE_CH(C83), c84 = GBDE_CH(C84),
-            c85 = GBDE_CH(C85), c86 = GBDE_CH(C86), c87 = GBDE_CH(C87);
-#undef GBDE_CH
     T y[N], fy[N], r[N], s8[N];
     // stage 1
     S.solve_t(F0, s1);
@@ -355,14 +338,14 @@ struct RodasAlg {
     for (int c = 0; c < N; ++c) y[c] = uu[c] + T(K::a21) * s1[c];
     M::f(fy, y, p);
 #pragma unroll
-    for (int c = 0; c < N; ++c) r[c] = fy[c] + c21 * s1[c];
+    for (int c = 0; c < N; ++c) r[c] = fy[c] + iht * (T(K::C21) * s1[c]);
     S.solve_t(r, s2);
     // stage 3
 #pragma unroll
     for (int c = 0; c < N; ++c) y[c] = uu[c] + T(K::a31) * s1[c] + T(K::a32) * s2[c];
     M::f(fy, y, p);
 #pragma unroll
-    for (int c = 0; c < N; ++c) r[c] = fy[c] + c31 * s1[c] + c32 * s2[c];
+    for (int c = 0; c < N; ++c) r[c] = fy[c] + iht * (T(K::C31) * s1[c] + T(K::C32) * s2[c]);
     S.solve_t(r, s3);
     // stage 4
 #pragma unroll
@@ -370,7 +353,7 @@ struct RodasAlg {
       y[c] = uu[c] + T(K::a41) * s1[c] + T(K::a42) * s2[c] + T(K::a43) * s3[c];
     M::f(fy, y, p);
 #pragma unroll
-    for (int c = 0; c < N; ++c) r[c] = fy[c] + c41 * s1[c] + c42 * s2[c] + c43 * s3[c];
+    for (int c = 0; c < N; ++c) r[c] = fy[c] + iht * (T(K::C41) * s1[c] + T(K::C42) * s2[c] + T(K::C43) * s3[c]);
     S.solve_t(r, s4);
     // stage 5
 #pragma unroll
@@ -380,7 +363,7 @@ struct RodasAlg {
     M::f(fy, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      r[c] = fy[c] + c51 * s1[c] + c52 * s2[c] + c53 * s3[c] + c54 * s4[c];
+      r[c] = fy[c] + iht * (T(K::C51) * s1[c] + T(K::C52) * s2[c] + T(K::C53) * s3[c] + T(K::C54) * s4[c]);
     S.solve_t(r, s5);
     // stage 6
 #pragma unroll
@@ -390,7 +373,7 @@ struct RodasAlg {
     M::f(fy, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      r[c] = fy[c] + c61 * s1[c] + c62 * s2[c] + c63 * s3[c] + c64 * s4[c] + c65 * s5[c];
+      r[c] = fy[c] + iht * (T(K::C61) * s1[c] + T(K::C62) * s2[c] + T(K::C63) * s3[c] + T(K::C64) * s4[c] + T(K::C65) * s5[c]);
     S.solve_t(r, s6);
     // stage 7: y = U_6 + u_6
 #pragma unroll
@@ -398,8 +381,7 @@ struct RodasAlg {
     M::f(fy, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      r[c] = fy[c] + c71 * s1[c] + c72 * s2[c] + c73 * s3[c] + c74 * s4[c] + c75 * s5[c] +
-             c76 * s6[c];
+      r[c] = fy[c] + iht * (T(K::C71) * s1[c] + T(K::C72) * s2[c] + T(K::C73) * s3[c] + T(K::C74) * s4[c] + T(K::C75) * s5[c] + T(K::C76) * s6[c]);
     S.solve_t(r, s7);
     // stage 8: y = U_7 + u_7
 #pragma unroll
@@ -407,8 +389,7 @@ struct RodasAlg {
     M::f(fy, y, p);
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      r[c] = fy[c] + c81 * s1[c] + c82 * s2[c] + c83 * s3[c] + c84 * s4[c] + c85 * s5[c] +
-             c86 * s6[c] + c87 * s7[c];
+      r[c] = fy[c] + iht * (T(K::C81) * s1[c] + T(K::C82) * s2[c] + T(K::C83) * s3[c] + T(K::C84) * s4[c] + T(K::C85) * s5[c] + T(K::C86) * s6[c] + T(K::C87) * s7[c]);
     S.solve_t(r, s8);
     nf += 7;
 #pragma unroll

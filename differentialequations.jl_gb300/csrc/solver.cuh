@@ -54,6 +54,7 @@ struct KArgs {
   CtlK ctl;                   // step-size controller constants (controller.h)
   double* dt_first;           // optional: size of the first accepted step
   int32_t chunk;              // persistent queue positions per fetch (>= 1)
+  const double* dt_init;      // optional: starting step per trajectory (k_init_dt)
 };
 
 GBDE_D uint64_t global_ns() {
@@ -199,6 +200,33 @@ GBDE_D double initial_dt(const T* u0, const T* f0, const T* p, double tspan, int
   return hw_dt(h0, s1, s2 * (1.0 / N), tspan, order);
 }
 
+// Pre-pass: the Hairer-Wanner starting step of every trajectory, one thread
+// each, all lanes converged.  Same loads, Alg::init and initial_dt as the
+// step kernel, so the step kernel starts from the identical value.
+template <class Alg, class M, class T>
+__global__ void __launch_bounds__(128) k_init_dt(const KArgs a, double* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.N;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    T p[M::NP], u0[M::N];
+#pragma unroll
+    for (int k = 0; k < M::NP; ++k) p[k] = (T)__ldg(a.p + (size_t)i * M::NP + k);
+#pragma unroll
+    for (int c = 0; c < M::N; ++c) u0[c] = (T)__ldg(a.u0 + (size_t)i * M::N + c);
+    const double t0 = __ldg(a.t0 + i), tf = __ldg(a.tf + i);
+    bool bad = !(tf > t0) || !isfinite(t0) || !isfinite(tf);
+#pragma unroll
+    for (int c = 0; c < M::N; ++c) bad |= !isfinite((double)u0[c]);
+    double dt = 0.0;
+    if (!bad) {
+      Alg alg;
+      int nf = 0;
+      alg.init(u0, p, nf);
+      dt = initial_dt<M, T>(alg.u(), alg.f0(), p, tf - t0, Alg::ORDER, a.abstol, a.reltol, nf);
+    }
+    out[i] = dt;
+  }
+}
+
 // ------------------------------------------------------------- driver
 // Alg provides:  static constexpr int ORDER (for beta defaults / init dt),
 //   void init(const T* u0, const T* p, int& nf)       -- u = u0, f(u) cache
@@ -259,6 +287,9 @@ __device__ void integrate_all(const KArgs& a) {
           dt = fmin((double)a.pred_dt[i], tf - t);
         } else if (a.dt0 > 0.0 || !a.adaptive) {
           dt = a.dt0;
+        } else if (a.dt_init != nullptr) {
+          dt = __ldg(a.dt_init + i);  // k_init_dt: the same computation, done beforehand
+          ++nfev;                     // its trial evaluation of f
         } else {
           dt = initial_dt<M, T>(alg.u(), alg.f0(), p, tf - t, Alg::ORDER, a.abstol, a.reltol,
                                 nfev);

@@ -147,36 +147,23 @@ struct TeamRodas {
 #pragma unroll
     for (int c = 0; c < TEAM; ++c) W.a[c] = c == tm.lane ? dg - (double)Jr[c] : -(double)Jr[c];
     W.factor(tm);
-    const T c21 = T(K::C21 * ih), c31 = T(K::C31 * ih), c32 = T(K::C32 * ih);
-    const T c41 = T(K::C41 * ih), c42 = T(K::C42 * ih), c43 = T(K::C43 * ih);
-    const T c51 = T(K::C51 * ih), c52 = T(K::C52 * ih), c53 = T(K::C53 * ih),
-            c54 = T(K::C54 * ih);
-    const T c61 = T(K::C61 * ih), c62 = T(K::C62 * ih), c63 = T(K::C63 * ih),
-            c64 = T(K::C64 * ih), c65 = T(K::C65 * ih);
-    const T c71 = T(K::C71 * ih), c72 = T(K::C72 * ih), c73 = T(K::C73 * ih),
-            c74 = T(K::C74 * ih), c75 = T(K::C75 * ih), c76 = T(K::C76 * ih);
-    const T c81 = T(K::C81 * ih), c82 = T(K::C82 * ih), c83 = T(K::C83 * ih),
-            c84 = T(K::C84 * ih), c85 = T(K::C85 * ih), c86 = T(K::C86 * ih),
-            c87 = T(K::C87 * ih);
+    const T iht = (T)ih;  // r_i = f(y_i) + (1/h) sum_j C_ij u_j
     s1 = (T)W.solve((double)F0, tm);
     T y = uu + T(K::a21) * s1;
-    s2 = (T)W.solve((double)(rhs(y, p, tm) + c21 * s1), tm);
+    s2 = (T)W.solve((double)(rhs(y, p, tm) + iht * (T(K::C21) * s1)), tm);
     y = uu + T(K::a31) * s1 + T(K::a32) * s2;
-    s3 = (T)W.solve((double)(rhs(y, p, tm) + c31 * s1 + c32 * s2), tm);
+    s3 = (T)W.solve((double)(rhs(y, p, tm) + iht * (T(K::C31) * s1 + T(K::C32) * s2)), tm);
     y = uu + T(K::a41) * s1 + T(K::a42) * s2 + T(K::a43) * s3;
-    s4 = (T)W.solve((double)(rhs(y, p, tm) + c41 * s1 + c42 * s2 + c43 * s3), tm);
+    s4 = (T)W.solve((double)(rhs(y, p, tm) + iht * (T(K::C41) * s1 + T(K::C42) * s2 + T(K::C43) * s3)), tm);
     y = uu + T(K::a51) * s1 + T(K::a52) * s2 + T(K::a53) * s3 + T(K::a54) * s4;
-    s5 = (T)W.solve((double)(rhs(y, p, tm) + c51 * s1 + c52 * s2 + c53 * s3 + c54 * s4), tm);
+    s5 = (T)W.solve((double)(rhs(y, p, tm) + iht * (T(K::C51) * s1 + T(K::C52) * s2 + T(K::C53) * s3 + T(K::C54) * s4)), tm);
     y = uu + T(K::a61) * s1 + T(K::a62) * s2 + T(K::a63) * s3 + T(K::a64) * s4 +
         T(K::a65) * s5;
-    s6 = (T)W.solve((double)(rhs(y, p, tm) + c61 * s1 + c62 * s2 + c63 * s3 + c64 * s4 +
-                             c65 * s5), tm);
+    s6 = (T)W.solve((double)(rhs(y, p, tm) + iht * (T(K::C61) * s1 + T(K::C62) * s2 + T(K::C63) * s3 + T(K::C64) * s4 + T(K::C65) * s5)), tm);
     y += s6;
-    s7 = (T)W.solve((double)(rhs(y, p, tm) + c71 * s1 + c72 * s2 + c73 * s3 + c74 * s4 +
-                             c75 * s5 + c76 * s6), tm);
+    s7 = (T)W.solve((double)(rhs(y, p, tm) + iht * (T(K::C71) * s1 + T(K::C72) * s2 + T(K::C73) * s3 + T(K::C74) * s4 + T(K::C75) * s5 + T(K::C76) * s6)), tm);
     y += s7;
-    const T s8 = (T)W.solve((double)(rhs(y, p, tm) + c81 * s1 + c82 * s2 + c83 * s3 +
-                                     c84 * s4 + c85 * s5 + c86 * s6 + c87 * s7), tm);
+    const T s8 = (T)W.solve((double)(rhs(y, p, tm) + iht * (T(K::C81) * s1 + T(K::C82) * s2 + T(K::C83) * s3 + T(K::C84) * s4 + T(K::C85) * s5 + T(K::C86) * s6 + T(K::C87) * s7)), tm);
     nf += 7;
     un = y + s8;
     const double sc = abstol + reltol * fmax(fabs((double)uu), fabs((double)un));

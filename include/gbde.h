@@ -345,7 +345,7 @@ GBDE_API int gbde_mlp_load(gbde_ctx* ctx, int32_t model, const float* net);
 /* Self-check (no counterpart in the reference): the largest relative
  * difference, over n pseudo-random x with |x| in [2^-60, 2^61), between the
  * Newton-refined reciprocal the kernels use and the IEEE division 1/x on the
- * device.  Within one ulp means <= 2^-52. */
+ * device (one Newton step: about 2^-40). */
 GBDE_API int gbde_check_rcp64(gbde_ctx* ctx, int64_t n, double* max_rel_err);
 
 #ifdef __cplusplus
