@@ -1,6 +1,9 @@
 // k_rosenbrock.cu -- Rosenbrock23 / Rodas5 / Rodas5P ensemble kernels
 // (one trajectory per thread, W-matrix LU in registers; models with n <= 3).
+// In the F32X2 precision Rodas5 / Rodas5P run the compact pair stepper of
+// rodas_ff.cuh.
 #include "rosenbrock.cuh"
+#include "rodas_ff.cuh"
 #include "ff.cuh"
 #include "launch.h"
 
@@ -11,8 +14,10 @@ __global__ void __launch_bounds__(128) k_ros(const KArgs a) {
   integrate_all<Alg, M, T, MIXED>(a);
 }
 
-template <class M, class T> using Rodas5A = RodasAlg<M, T, Rodas5Tag>;
-template <class M, class T> using Rodas5PA = RodasAlg<M, T, Rodas5PTag>;
+template <class M, class T, class Tag> struct RodasSel { using type = RodasAlg<M, T, Tag>; };
+template <class M, class Tag> struct RodasSel<M, ff, Tag> { using type = RodasFF<M, Tag>; };
+template <class M, class T> using Rodas5A = typename RodasSel<M, T, Rodas5Tag>::type;
+template <class M, class T> using Rodas5PA = typename RodasSel<M, T, Rodas5PTag>::type;
 
 template <template <class, class> class AlgT, class M>
 static cudaError_t dispatch_prec(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {

@@ -1,0 +1,337 @@
+// rodas_ff.cuh -- Rodas5 / Rodas5P in FP32 pairs (the F32X2 precision) with a
+// compact step body.
+//
+// Same method as RodasAlg (rosenbrock.cuh; OrdinaryDiffEq's Rodas5P, test/qa/qa.jl:97,
+// the stiff method of test/core.jl:38-49): the transformed 8-stage form
+//   (I/(h gamma) - J) u_i = f(y0 + sum_{j<i} a_ij u_j) + (1/h) sum_{j<i} C_ij u_j,
+// y1 = U_7 + u_8, error estimate u_8.  What differs is where each operation runs:
+//
+//  * state, stages, right-hand sides and the stage combinations are FP32 pairs
+//    (ff.cuh, ~48 significant bits) on the FP32 pipe, which GB300 runs at 61x its
+//    FP64 rate;
+//  * the Jacobian, the W-matrix and its partial-pivot LU are FP64, as is the error
+//    norm's accumulation; the LU factors reach the pair solves through an
+//    integer-pipe split (ff_split), not through FP64 conversions;
+//  * the stage loop is not unrolled and the transformed stages live in shared
+//    memory (7 x N pairs per thread), so the body stays small enough for the
+//    instruction cache -- a fully unrolled pair body is several times larger than
+//    its FP64 counterpart;
+//  * sums of products accumulate unnormalised (FfAcc: one TwoSum per term, one
+//    renormalisation per sum) instead of renormalising after every operation.
+// The FP64 pipe then carries about 55 instructions per attempted step instead of
+// about 430 (Robertson, n = 3).
+#pragma once
+#include "ff.cuh"
+#include "rosenbrock.cuh"
+
+namespace gbde {
+
+// Split a double into a pair without FP64 arithmetic: hi keeps the leading 24
+// significant bits (truncated), lo the remaining 29 bits rounded to 24 (one
+// integer-to-float conversion and an exact power-of-two scaling).  |lo| < ulp(hi).
+// |d| below 2^-126 gives a signed zero (below 2^-74 lo is dropped); |d| >= 2^128
+// gives an infinity (NaN stays NaN).
+GBDE_D ff ff_split(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
+  const unsigned sign = hw & 0x80000000u;
+  const int ex = (int)((hw >> 20) & 0x7ffu);
+  if (ex < 897) return ff(__uint_as_float(sign), 0.0f);
+  if (ex > 1150) {
+    const bool nan = ex == 2047 && (b << 12) != 0ull;
+    return ff(__uint_as_float(nan ? 0x7fc00000u : (sign | 0x7f800000u)), 0.0f);
+  }
+  const unsigned m23 = ((hw & 0xfffffu) << 3) | (lw >> 29);
+  const float hi = __uint_as_float(sign | ((unsigned)(ex - 896) << 23) | m23);
+  float lo = 0.0f;
+  if (ex >= 949) lo = xmul(__uint2float_rn(lw & 0x1fffffffu), __uint_as_float((unsigned)(ex - 948) << 23));
+  return ff(hi, sign ? -lo : lo);
+}
+
+// Unnormalised accumulator of a sum of pair products: value = s + e.  Each term
+// costs one TwoProd with cross terms and one TwoSum; get() renormalises once.
+struct FfAcc {
+  float s, e;
+  GBDE_D void set(ff x) {
+    s = x.hi;
+    e = x.lo;
+  }
+  GBDE_D void fma(ff a, ff b) {  // += a b
+    const float p = xmul(a.hi, b.hi);
+    float pe = xfma(a.hi, b.hi, -p);
+    pe = xfma(a.hi, b.lo, xfma(a.lo, b.hi, pe));
+    const float t = xadd(s, p);
+    const float bb = xadd(t, -s);
+    const float err = xadd(xadd(s, -xadd(t, -bb)), xadd(p, -bb));
+    s = t;
+    e = xadd(e, xadd(err, pe));
+  }
+  GBDE_D void add(ff x) {  // += x
+    const float t = xadd(s, x.hi);
+    const float bb = xadd(t, -s);
+    const float err = xadd(xadd(s, -xadd(t, -bb)), xadd(x.hi, -bb));
+    s = t;
+    e = xadd(e, xadd(err, x.lo));
+  }
+  GBDE_D ff get() const {  // TwoSum renormalisation (|e| may exceed |s| after cancellation)
+    const float t = xadd(s, e);
+    const float bb = xadd(t, -s);
+    const float err = xadd(xadd(s, -xadd(t, -bb)), xadd(e, -bb));
+    return ff(t, err);
+  }
+};
+
+// The FP64 LU factors as pairs, negated so that the substitutions are sums of
+// products: nL (strictly lower), nU (strictly upper), inv (reciprocal pivots).
+// The row swaps recorded in piv are applied to the right-hand side first (the
+// factorisation swaps whole rows: P W = L U).
+template <int N>
+struct FfLU {
+  ff nL[N][N], nU[N][N], inv[N];
+  int piv[N];
+  GBDE_D void from(const SmallLU<N>& W) {
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+#pragma unroll
+      for (int c = 0; c < N; ++c) {
+        if (c < r) nL[r][c] = ff_split(-W.A[r][c]);
+        if (c > r) nU[r][c] = ff_split(-W.A[r][c]);
+      }
+      inv[r] = ff_split(W.inv[r]);
+      piv[r] = W.piv[r];
+    }
+  }
+  GBDE_D void solve(ff* b) const {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+#pragma unroll
+      for (int r = k + 1; r < N; ++r) {
+        const bool sw = piv[k] == r;
+        const ff x = b[k], y = b[r];
+        b[k] = sw ? y : x;
+        b[r] = sw ? x : y;
+      }
+    }
+#pragma unroll
+    for (int r = 1; r < N; ++r) {
+      FfAcc acc;
+      acc.set(b[r]);
+#pragma unroll
+      for (int k = 0; k < r; ++k) acc.fma(nL[r][k], b[k]);
+      b[r] = acc.get();
+    }
+#pragma unroll
+    for (int r = N - 1; r >= 0; --r) {
+      FfAcc acc;
+      acc.set(b[r]);
+#pragma unroll
+      for (int c = r + 1; c < N; ++c) acc.fma(nU[r][c], b[c]);
+      b[r] = acc.get() * inv[r];
+    }
+  }
+};
+
+// Stage coefficients as pairs, indexed by the (warp-uniform) stage counters:
+// ra[i][j] = a_{i+1,j+1} for the stages whose argument is a fresh sum (i <= 5),
+// rc[i][j] = C_{i+1,j+1}.
+struct RodasFfTab {
+  ff ra[6][5];
+  ff rc[8][7];
+};
+
+template <class K>
+constexpr RodasFfTab rodas_ff_tab() {
+  return RodasFfTab{
+      {{ff(0.0), ff(0.0), ff(0.0), ff(0.0), ff(0.0)},
+       {ff(K::a21), ff(0.0), ff(0.0), ff(0.0), ff(0.0)},
+       {ff(K::a31), ff(K::a32), ff(0.0), ff(0.0), ff(0.0)},
+       {ff(K::a41), ff(K::a42), ff(K::a43), ff(0.0), ff(0.0)},
+       {ff(K::a51), ff(K::a52), ff(K::a53), ff(K::a54), ff(0.0)},
+       {ff(K::a61), ff(K::a62), ff(K::a63), ff(K::a64), ff(K::a65)}},
+      {{ff(0.0), ff(0.0), ff(0.0), ff(0.0), ff(0.0), ff(0.0), ff(0.0)},
+       {ff(K::C21), ff(0.0), ff(0.0), ff(0.0), ff(0.0), ff(0.0), ff(0.0)},
+       {ff(K::C31), ff(K::C32), ff(0.0), ff(0.0), ff(0.0), ff(0.0), ff(0.0)},
+       {ff(K::C41), ff(K::C42), ff(K::C43), ff(0.0), ff(0.0), ff(0.0), ff(0.0)},
+       {ff(K::C51), ff(K::C52), ff(K::C53), ff(K::C54), ff(0.0), ff(0.0), ff(0.0)},
+       {ff(K::C61), ff(K::C62), ff(K::C63), ff(K::C64), ff(K::C65), ff(0.0), ff(0.0)},
+       {ff(K::C71), ff(K::C72), ff(K::C73), ff(K::C74), ff(K::C75), ff(K::C76), ff(0.0)},
+       {ff(K::C81), ff(K::C82), ff(K::C83), ff(K::C84), ff(K::C85), ff(K::C86), ff(K::C87)}}};
+}
+
+static __constant__ RodasFfTab c_rodas_ff[2] = {rodas_ff_tab<RodasCoef<Rodas5Tag>>(),
+                                                rodas_ff_tab<RodasCoef<Rodas5PTag>>()};
+
+template <class Tag> struct RodasFfIdx;
+template <> struct RodasFfIdx<Rodas5Tag> { static constexpr int v = 0; };
+template <> struct RodasFfIdx<Rodas5PTag> { static constexpr int v = 1; };
+
+// Threads per CTA the stage buffer is sized for (the step kernels launch at
+// most 128: __launch_bounds__(128)).
+constexpr int kFfStageThreads = 128;
+
+template <class M, class Tag>
+struct RodasFF {
+  using K = RodasCoef<Tag>;
+  using T = ff;
+  static constexpr int ORDER = 4, ALG_ID = K::ALG_ID, N = M::N;
+  ff uu[N], un[N], F0[N];
+  double pd[M::NP];
+  double J[N][N];
+  bool fresh;  // F0 and J valid for uu
+
+  GBDE_D const ff* u() const { return uu; }
+  GBDE_D const ff* unew() const { return un; }
+  GBDE_D const ff* f0() const { return F0; }
+
+  // Transformed stages u_1..u_7 of the current step, pair (hi, lo) per
+  // component: slot (i N + c) of this thread at stride kFfStageThreads.
+  GBDE_D static float2* stages() {
+    __shared__ float2 buf[7 * N * kFfStageThreads];
+    return buf + threadIdx.x;
+  }
+  GBDE_D static ff ld(const float2* st, int slot) {
+    const float2 v = st[slot * kFfStageThreads];
+    return ff(v.x, v.y);
+  }
+  GBDE_D static void st(float2* st, int slot, ff x) { st[slot * kFfStageThreads] = make_float2(x.hi, x.lo); }
+
+  GBDE_D void jac_fp64() {
+    double ud[N];
+#pragma unroll
+    for (int c = 0; c < N; ++c) ud[c] = (double)uu[c];
+    M::jac(J, ud, pd);
+  }
+
+  GBDE_D void init(const ff* u0, const ff* p, int& nf) {
+#pragma unroll
+    for (int k = 0; k < M::NP; ++k) pd[k] = (double)p[k];
+#pragma unroll
+    for (int c = 0; c < N; ++c) uu[c] = u0[c];
+    M::f(F0, uu, p);
+    ++nf;
+    jac_fp64();
+    fresh = true;
+  }
+
+  GBDE_D double attempt(double dt, const ff* p, double abstol, double reltol, int& nf) {
+    if (!fresh) {
+      M::f(F0, uu, p);
+      ++nf;
+      jac_fp64();
+      fresh = true;
+    }
+    // W = I/(h gamma) - J and its LU in FP64
+    SmallLU<N> W;
+    const double ih = rcp64(dt);
+    const double dg = ih * (1.0 / K::g);
+#pragma unroll
+    for (int r = 0; r < N; ++r)
+#pragma unroll
+      for (int c = 0; c < N; ++c) W.A[r][c] = r == c ? dg - J[r][c] : -J[r][c];
+    W.factor();
+    FfLU<N> L;
+    L.from(W);
+    const ff iht = ff_split(ih);
+    const RodasFfTab& tb = c_rodas_ff[RodasFfIdx<Tag>::v];
+    float2* sb = stages();
+    ff y[N], s[N];
+#pragma unroll 1
+    for (int i = 0; i < 8; ++i) {
+      ff r[N];
+      if (i == 0) {
+#pragma unroll
+        for (int c = 0; c < N; ++c) r[c] = F0[c];
+      } else {
+        // stage argument: a fresh combination for stages 2-6; for 7 and 8 the
+        // previous argument plus the previous stage (a_7j = a_6j, a_76 = 1, ...)
+        FfAcc ya[N], ca[N];
+        const bool fresh_arg = i <= 5;
+#pragma unroll
+        for (int c = 0; c < N; ++c) {
+          ya[c].set(fresh_arg ? uu[c] : y[c]);
+          ca[c].set(ff(0.0f, 0.0f));
+        }
+#pragma unroll 1
+        for (int j = 0; j < i; ++j) {
+          const ff cij = tb.rc[i][j];
+          const ff aij = tb.ra[fresh_arg ? i : 0][fresh_arg ? j : 0];
+          const bool last = j == i - 1;
+#pragma unroll
+          for (int c = 0; c < N; ++c) {
+            const ff sj = ld(sb, j * N + c);
+            if (fresh_arg) ya[c].fma(aij, sj);
+            else if (last) ya[c].add(sj);
+            ca[c].fma(cij, sj);
+          }
+        }
+        ff fy[N];
+#pragma unroll
+        for (int c = 0; c < N; ++c) y[c] = ya[c].get();
+        M::f(fy, y, p);
+#pragma unroll
+        for (int c = 0; c < N; ++c) {
+          FfAcc ra;
+          ra.set(fy[c]);
+          ra.fma(iht, ca[c].get());
+          r[c] = ra.get();
+        }
+      }
+      L.solve(r);
+      if (i < 7) {
+#pragma unroll
+        for (int c = 0; c < N; ++c) st(sb, i * N + c, r[c]);
+      } else {
+#pragma unroll
+        for (int c = 0; c < N; ++c) s[c] = r[c];
+      }
+    }
+    nf += 7;
+    // y1 = U_7 + u_8; error estimate u_8, norm in FP64
+    double ms = 0.0;
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      FfAcc a;
+      a.set(y[c]);
+      a.add(s[c]);
+      un[c] = a.get();
+      const float m = fmaxf(fabsf(uu[c].hi), fabsf(un[c].hi));
+      const double e = (double)s[c].hi * rcp64(abstol + reltol * (double)m);
+      ms = fma(e, e, ms);
+    }
+    return ms * (1.0 / N);
+  }
+
+  // y(theta) = y0 + theta (y1 - y0) + sum_j e_j u_j, with
+  // e_j = theta (1 - theta) (H2_j + theta H3_j + theta^2 H4_j) (as RodasAlg::interp)
+  GBDE_D void interp(double th, double, ff* out, const ff*, int&) {
+    const double w = th * (1.0 - th);
+    ff e[7];
+#define GBDE_RODAS_FF_E(j)                                                     \
+  {                                                                            \
+    constexpr double h2 = K::H2[j], h3 = K::H3[j], h4 = K::H4[j];              \
+    e[j] = ff_split(w * (h2 + th * (h3 + th * h4)));                           \
+  }
+    GBDE_RODAS_FF_E(0); GBDE_RODAS_FF_E(1); GBDE_RODAS_FF_E(2); GBDE_RODAS_FF_E(3);
+    GBDE_RODAS_FF_E(4); GBDE_RODAS_FF_E(5); GBDE_RODAS_FF_E(6);
+#undef GBDE_RODAS_FF_E
+    const ff tt = ff_split(th);
+    const float2* sb = stages();
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      FfAcc a;
+      a.set(uu[c]);
+      a.fma(tt, un[c] - uu[c]);
+#pragma unroll
+      for (int j = 0; j < 7; ++j) a.fma(e[j], ld(sb, j * N + c));
+      out[c] = a.get();
+    }
+  }
+
+  GBDE_D void accept(const ff*, int&) {
+#pragma unroll
+    for (int c = 0; c < N; ++c) uu[c] = un[c];
+    fresh = false;
+  }
+};
+
+}  // namespace gbde
