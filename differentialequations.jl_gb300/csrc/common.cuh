@@ -61,6 +61,37 @@ GBDE_HD uint64_t mag_bits(double x) {
 #endif
 }
 
+// float -> double widening on the integer pipe (the conversion instruction runs
+// on GB300's narrow FP64 pipe): exact for normal floats, infinities and NaN;
+// zeros and subnormal floats give a signed zero.
+GBDE_HD double f2d_bits(float x) {
+  uint32_t b;
+#if defined(__CUDA_ARCH__)
+  b = __float_as_uint(x);
+#else
+  memcpy(&b, &x, sizeof(b));
+#endif
+  const uint32_t e = (b >> 23) & 0xffu, s = b & 0x80000000u, m = b & 0x7fffffu;
+  const uint32_t ed = e == 0u ? 0u : (e == 0xffu ? 0x7ffu : e + 896u);
+  const uint32_t hw = s | (ed << 20) | (e == 0u ? 0u : (m >> 3));
+  const uint32_t lw = e == 0u ? 0u : (m << 29);
+#if defined(__CUDA_ARCH__)
+  return __hiloint2double((int)hw, (int)lw);
+#else
+  const uint64_t v = ((uint64_t)hw << 32) | lw;
+  double d;
+  memcpy(&d, &v, sizeof(d));
+  return d;
+#endif
+}
+
+// Finiteness of a state component: through the FP64 value for double and
+// float; the pair type (ff.cuh) overloads it with a test of its leading part.
+template <class T>
+GBDE_HD bool val_finite(T x) {
+  return isfinite((double)x);
+}
+
 // Error-free sum (Knuth TwoSum): s + e == a + b exactly.  Used for the
 // compensated time accumulation of the mixed-precision path.
 GBDE_HD void two_sum(double a, double b, double& s, double& e) {

@@ -62,6 +62,9 @@ GBDE_HD ff& operator-=(ff& a, ff b) { return a = a - b; }
 GBDE_HD ff& operator*=(ff& a, ff b) { return a = a * b; }
 GBDE_HD bool operator<(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 
+// a pair is finite iff its leading part is
+GBDE_HD bool val_finite(ff x) { return isfinite(x.hi); }
+
 template <class T> struct is_ff { static constexpr bool value = false; };
 template <> struct is_ff<ff> { static constexpr bool value = true; };
 

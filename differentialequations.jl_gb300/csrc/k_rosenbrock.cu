@@ -24,8 +24,9 @@ static cudaError_t dispatch_prec(const LaunchCfg& cfg, const KArgs& a, cudaStrea
   if (cfg.precision == GBDE_PREC_MIXED)
     return launch_step_kernel<AlgT<M, float>, M, float>(k_ros<AlgT<M, float>, M, float, true>,
                                                          cfg, a, s);
-  if (cfg.precision == GBDE_PREC_F32X2)
+  if (cfg.precision == GBDE_PREC_F32X2) {
     return launch_step_kernel<AlgT<M, ff>, M, ff>(k_ros<AlgT<M, ff>, M, ff, true>, cfg, a, s);
+  }
   return launch_step_kernel<AlgT<M, double>, M, double>(k_ros<AlgT<M, double>, M, double, false>,
                                                          cfg, a, s);
 }

@@ -18,8 +18,8 @@
 //    its FP64 counterpart;
 //  * sums of products accumulate unnormalised (FfAcc: one TwoSum per term, one
 //    renormalisation per sum) instead of renormalising after every operation.
-// The FP64 pipe then carries about 55 instructions per attempted step instead of
-// about 430 (Robertson, n = 3).
+// The FP64 pipe then carries about a quarter of the instructions per attempted
+// step that the FP64 stepper issues (Robertson, n = 3).
 #pragma once
 #include "ff.cuh"
 #include "rosenbrock.cuh"
@@ -174,10 +174,10 @@ struct RodasFF {
   using K = RodasCoef<Tag>;
   using T = ff;
   static constexpr int ORDER = 4, ALG_ID = K::ALG_ID, N = M::N;
-  ff uu[N], un[N], F0[N];
+  ff uu[N], un[N];
+  ff F0[N];  // f(u0): read only by the Hairer-Wanner starting step after init()
   double pd[M::NP];
-  double J[N][N];
-  bool fresh;  // F0 and J valid for uu
+  bool fresh;  // uu's f evaluation already counted
 
   GBDE_D const ff* u() const { return uu; }
   GBDE_D const ff* unew() const { return un; }
@@ -195,13 +195,6 @@ struct RodasFF {
   }
   GBDE_D static void st(float2* st, int slot, ff x) { st[slot * kFfStageThreads] = make_float2(x.hi, x.lo); }
 
-  GBDE_D void jac_fp64() {
-    double ud[N];
-#pragma unroll
-    for (int c = 0; c < N; ++c) ud[c] = (double)uu[c];
-    M::jac(J, ud, pd);
-  }
-
   GBDE_D void init(const ff* u0, const ff* p, int& nf) {
 #pragma unroll
     for (int k = 0; k < M::NP; ++k) pd[k] = (double)p[k];
@@ -209,72 +202,74 @@ struct RodasFF {
     for (int c = 0; c < N; ++c) uu[c] = u0[c];
     M::f(F0, uu, p);
     ++nf;
-    jac_fp64();
     fresh = true;
   }
 
+  // One attempted step.  f(uu) and the Jacobian are evaluated afresh on every
+  // attempt instead of being kept across a rejection: keeping them would hold
+  // 3N + 2N^2 registers through the stage loop for the ~15% of attempts that
+  // follow a rejection.  nf counts f(uu) once per accepted state, as a caching
+  // implementation would evaluate it.
   GBDE_D double attempt(double dt, const ff* p, double abstol, double reltol, int& nf) {
     if (!fresh) {
-      M::f(F0, uu, p);
       ++nf;
-      jac_fp64();
       fresh = true;
     }
-    // W = I/(h gamma) - J and its LU in FP64
+    // W = I/(h gamma) - J(uu) and its LU in FP64
     SmallLU<N> W;
-    const double ih = rcp64(dt);
-    const double dg = ih * (1.0 / K::g);
+    {
+      double ud[N], J[N][N];
 #pragma unroll
-    for (int r = 0; r < N; ++r)
+      for (int c = 0; c < N; ++c) ud[c] = (double)uu[c];
+      M::jac(J, ud, pd);
+      const double dg0 = rcp64(dt) * (1.0 / K::g);
 #pragma unroll
-      for (int c = 0; c < N; ++c) W.A[r][c] = r == c ? dg - J[r][c] : -J[r][c];
+      for (int r = 0; r < N; ++r)
+#pragma unroll
+        for (int c = 0; c < N; ++c) W.A[r][c] = r == c ? dg0 - J[r][c] : -J[r][c];
+    }
     W.factor();
     FfLU<N> L;
     L.from(W);
-    const ff iht = ff_split(ih);
+    const ff iht = ff_split(rcp64(dt));
     const RodasFfTab& tb = c_rodas_ff[RodasFfIdx<Tag>::v];
     float2* sb = stages();
     ff y[N], s[N];
 #pragma unroll 1
     for (int i = 0; i < 8; ++i) {
-      ff r[N];
-      if (i == 0) {
+      // stage argument: u0 for stage 1, a fresh combination for stages 2-6; for
+      // 7 and 8 the previous argument plus the previous stage (a_7j = a_6j,
+      // a_76 = 1, a_8j = a_7j, a_87 = 1)
+      FfAcc ya[N], ca[N];
+      const bool fresh_arg = i <= 5;
 #pragma unroll
-        for (int c = 0; c < N; ++c) r[c] = F0[c];
-      } else {
-        // stage argument: a fresh combination for stages 2-6; for 7 and 8 the
-        // previous argument plus the previous stage (a_7j = a_6j, a_76 = 1, ...)
-        FfAcc ya[N], ca[N];
-        const bool fresh_arg = i <= 5;
-#pragma unroll
-        for (int c = 0; c < N; ++c) {
-          ya[c].set(fresh_arg ? uu[c] : y[c]);
-          ca[c].set(ff(0.0f, 0.0f));
-        }
+      for (int c = 0; c < N; ++c) {
+        ya[c].set(fresh_arg ? uu[c] : y[c]);
+        ca[c].set(ff(0.0f, 0.0f));
+      }
 #pragma unroll 1
-        for (int j = 0; j < i; ++j) {
-          const ff cij = tb.rc[i][j];
-          const ff aij = tb.ra[fresh_arg ? i : 0][fresh_arg ? j : 0];
-          const bool last = j == i - 1;
-#pragma unroll
-          for (int c = 0; c < N; ++c) {
-            const ff sj = ld(sb, j * N + c);
-            if (fresh_arg) ya[c].fma(aij, sj);
-            else if (last) ya[c].add(sj);
-            ca[c].fma(cij, sj);
-          }
-        }
-        ff fy[N];
-#pragma unroll
-        for (int c = 0; c < N; ++c) y[c] = ya[c].get();
-        M::f(fy, y, p);
+      for (int j = 0; j < i; ++j) {
+        const ff cij = tb.rc[i][j];
+        const ff aij = tb.ra[fresh_arg ? i : 0][fresh_arg ? j : 0];
+        const bool last = j == i - 1;
 #pragma unroll
         for (int c = 0; c < N; ++c) {
-          FfAcc ra;
-          ra.set(fy[c]);
-          ra.fma(iht, ca[c].get());
-          r[c] = ra.get();
+          const ff sj = ld(sb, j * N + c);
+          if (fresh_arg) ya[c].fma(aij, sj);
+          else if (last) ya[c].add(sj);
+          ca[c].fma(cij, sj);
         }
+      }
+      ff fy[N], r[N];
+#pragma unroll
+      for (int c = 0; c < N; ++c) y[c] = ya[c].get();
+      M::f(fy, y, p);
+#pragma unroll
+      for (int c = 0; c < N; ++c) {
+        FfAcc ra;
+        ra.set(fy[c]);
+        if (i > 0) ra.fma(iht, ca[c].get());
+        r[c] = ra.get();
       }
       L.solve(r);
       if (i < 7) {
@@ -295,7 +290,7 @@ struct RodasFF {
       a.add(s[c]);
       un[c] = a.get();
       const float m = fmaxf(fabsf(uu[c].hi), fabsf(un[c].hi));
-      const double e = (double)s[c].hi * rcp64(abstol + reltol * (double)m);
+      const double e = f2d_bits(s[c].hi) * rcp64(abstol + reltol * f2d_bits(m));
       ms = fma(e, e, ms);
     }
     return ms * (1.0 / N);

@@ -317,7 +317,7 @@ __device__ void integrate_all(const KArgs& a) {
       if (ok) {
         // controller proposal for the next step
         double dtnew = h;
-        if (a.adaptive) dtnew = h * (double)ctl_accept(a.ctl, ms, lqold);
+        if (a.adaptive) dtnew = h * f2d_bits(ctl_accept(a.ctl, ms, lqold));
         // time update (compensated in the mixed-precision path)
         double tnew;
         if (last) {
@@ -353,13 +353,13 @@ __device__ void integrate_all(const KArgs& a) {
         ++nacc;
         bool fin = true;
 #pragma unroll
-        for (int c = 0; c < N; ++c) fin &= isfinite((double)alg.u()[c]);
+        for (int c = 0; c < N; ++c) fin &= val_finite(alg.u()[c]);
         if (!fin) ret = GBDE_RET_UNSTABLE;
         else if (last) ret = GBDE_RET_SUCCESS;
         dt = a.dtmax > 0.0 ? fmin(dtnew, a.dtmax) : dtnew;
       } else {
         ++nrej;
-        dt = h * (double)ctl_reject(a.ctl, ms);
+        dt = h * f2d_bits(ctl_reject(a.ctl, ms));
       }
       if (ret == GBDE_RET_DEFAULT) {
         if (iters >= a.maxiters) ret = GBDE_RET_MAXITERS;
