@@ -9,8 +9,10 @@ A "step" is one ensemble solve of all trajectories.  `value` is trajectories
 per second of the chosen form with inputs resident in HBM (device pointers,
 one gbde_ensemble_solve); `e2e` is the same through the C ABI with pinned
 host buffers (H2D + solve + D2H inside the timed region).  `plain` is the
-plain one-thread-per-trajectory launch for comparison.  The chosen form's
-result is checked against the CPU FP64 oracle on a sample before timing.
+plain one-thread-per-trajectory FP64 launch for comparison.  The chosen form
+(default: the persistent longest-span-first queue with state, stages and
+right-hand sides in FP32 pairs, FP64 Jacobian / LU / error norm / compensated
+time) is checked against the CPU FP64 oracle on a sample before timing.
 
 --impl reference times the CPU FP64 restatement (EnsembleThreads-equivalent
 std::thread pool over all host cores) on the same workload.
@@ -42,9 +44,11 @@ FLOPS = {
 }
 
 # DRAM bytes (read + write) per trajectory of the Rodas5 solve kernel, from one
-# ncu capture (20,000 trajectories: 4.587 MB read + 8.2 KB written; the saved
-# states stay in L2 until after the kernel), scaled by trajectories.
-TRAFFIC_PER_TRAJ = (4.586752e6 + 8192.0) / 20000.0
+# ncu capture each, scaled by trajectories.  FP64 stepper: 20,000 trajectories,
+# 4.587 MB read + 8.2 KB written (the saved states stay in L2 until after the
+# kernel).  FP32-pair stepper: 100,000 trajectories, persistent launch.
+TRAFFIC_PER_TRAJ = {"fp64": (4.586752e6 + 8192.0) / 20000.0,
+                    "f32x2": (28.150272e6 + 6.957824e6) / 100000.0}
 
 
 def parse():
@@ -55,8 +59,9 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--alg", default="rodas5", choices=["rodas5", "rosenbrock23"])
     ap.add_argument("--trajectories", type=int, default=100000)
-    ap.add_argument("--chosen", default="persistent",
-                    help="chosen form: plain | persistent | persistent-mixed")
+    ap.add_argument("--chosen", default="persistent-f32x2",
+                    help="chosen form: persistent-f32x2 | plain-f32x2 | persistent | plain | "
+                         "persistent-mixed | plain-mixed")
     ap.add_argument("--cpu-sample", type=int, default=100000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="robertson",
@@ -663,9 +668,15 @@ def main():
                 "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
                      "frac": achieved / peak64,
-                     "traffic": TRAFFIC_PER_TRAJ * N if args.alg == "rodas5" else None,
+                     "basis": "the method's FP64 flops (FMA = 2) / kernel time / measured FP64 FMA "
+                              "peak" + ("; this form executes them as FP32-pair arithmetic with an "
+                                        "FP64 Jacobian, LU, error norm and time, so the fraction "
+                                        "is FP64-equivalent and is not capped at 1" if pairs else ""),
+                     "traffic": (TRAFFIC_PER_TRAJ["f32x2" if pairs else "fp64"] * N
+                                 if args.alg == "rodas5" else None),
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
-                                       "20,000-trajectory launch, scaled by trajectories",
+                                       "launch (%s trajectories), scaled by trajectories"
+                                       % ("100,000" if pairs else "20,000"),
                      "peak_source": "in-run FP64 FMA microbenchmark (gbde_measure_fma_peak)",
                      "fp32_peak_tflops": peak32,
                      "algorithmic_flops_per_step": flops, "kernel_ms": chosen_kern},

@@ -92,9 +92,19 @@ inline CtlK ctl_consts(double beta1, double beta2, double gamma, double qmin, do
   return k;
 }
 
-// log2 of the mean square, clamped to [-120, 120] (float range of the exponent)
+// log2 of the mean square, clamped to [-120, 120] (float range of the exponent).
+// ms is finite and >= 0 (the callers test finiteness first), so the clamp to
+// [2^-120, 2^120] compares bit patterns on the integer pipe.
 GBDE_HD float ctl_log2_ms(double ms) {
-  const double c = fmin(fmax(ms, 7.52316384526264e-37), 1.329227995784916e36);  // 2^-120, 2^120
+  const uint64_t lo = 0x3870000000000000ull, hi = 0x4770000000000000ull;  // 2^-120, 2^120
+  uint64_t b = mag_bits(ms);
+  b = b < lo ? lo : (b > hi ? hi : b);
+  double c;
+#if defined(__CUDA_ARCH__)
+  c = __longlong_as_double((long long)b);
+#else
+  memcpy(&c, &b, sizeof(c));
+#endif
   return ctl_log2f((float)c);
 }
 

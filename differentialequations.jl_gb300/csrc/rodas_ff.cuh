@@ -134,9 +134,11 @@ struct FfLU {
 // Stage coefficients as pairs, indexed by the (warp-uniform) stage counters:
 // ra[i][j] = a_{i+1,j+1} for the stages whose argument is a fresh sum (i <= 5),
 // rc[i][j] = C_{i+1,j+1}.
+// h2, h3, h4: the dense-output coefficients H2_j, H3_j, H4_j.
 struct RodasFfTab {
   ff ra[6][5];
   ff rc[8][7];
+  ff h2[7], h3[7], h4[7];
 };
 
 template <class K>
@@ -155,7 +157,10 @@ constexpr RodasFfTab rodas_ff_tab() {
        {ff(K::C51), ff(K::C52), ff(K::C53), ff(K::C54), ff(0.0), ff(0.0), ff(0.0)},
        {ff(K::C61), ff(K::C62), ff(K::C63), ff(K::C64), ff(K::C65), ff(0.0), ff(0.0)},
        {ff(K::C71), ff(K::C72), ff(K::C73), ff(K::C74), ff(K::C75), ff(K::C76), ff(0.0)},
-       {ff(K::C81), ff(K::C82), ff(K::C83), ff(K::C84), ff(K::C85), ff(K::C86), ff(K::C87)}}};
+       {ff(K::C81), ff(K::C82), ff(K::C83), ff(K::C84), ff(K::C85), ff(K::C86), ff(K::C87)}},
+      {ff(K::H2[0]), ff(K::H2[1]), ff(K::H2[2]), ff(K::H2[3]), ff(K::H2[4]), ff(K::H2[5]), ff(K::H2[6])},
+      {ff(K::H3[0]), ff(K::H3[1]), ff(K::H3[2]), ff(K::H3[3]), ff(K::H3[4]), ff(K::H3[5]), ff(K::H3[6])},
+      {ff(K::H4[0]), ff(K::H4[1]), ff(K::H4[2]), ff(K::H4[3]), ff(K::H4[4]), ff(K::H4[5]), ff(K::H4[6])}};
 }
 
 static __constant__ RodasFfTab c_rodas_ff[2] = {rodas_ff_tab<RodasCoef<Rodas5Tag>>(),
@@ -220,7 +225,7 @@ struct RodasFF {
     {
       double ud[N], J[N][N];
 #pragma unroll
-      for (int c = 0; c < N; ++c) ud[c] = (double)uu[c];
+      for (int c = 0; c < N; ++c) ud[c] = f2d_bits(uu[c].hi) + f2d_bits(uu[c].lo);
       M::jac(J, ud, pd);
       const double dg0 = rcp64(dt) * (1.0 / K::g);
 #pragma unroll
@@ -296,30 +301,35 @@ struct RodasFF {
     return ms * (1.0 / N);
   }
 
-  // y(theta) = y0 + theta (y1 - y0) + sum_j e_j u_j, with
-  // e_j = theta (1 - theta) (H2_j + theta H3_j + theta^2 H4_j) (as RodasAlg::interp)
+  // y(theta) = y0 + theta (y1 - y0) + sum_j e_j u_j with
+  // e_j = theta (1 - theta) (H2_j + theta H3_j + theta^2 H4_j) (as RodasAlg::interp),
+  // all in pair arithmetic; the loop over j reads the coefficients from the
+  // constant table.
   GBDE_D void interp(double th, double, ff* out, const ff*, int&) {
-    const double w = th * (1.0 - th);
-    ff e[7];
-#define GBDE_RODAS_FF_E(j)                                                     \
-  {                                                                            \
-    constexpr double h2 = K::H2[j], h3 = K::H3[j], h4 = K::H4[j];              \
-    e[j] = ff_split(w * (h2 + th * (h3 + th * h4)));                           \
-  }
-    GBDE_RODAS_FF_E(0); GBDE_RODAS_FF_E(1); GBDE_RODAS_FF_E(2); GBDE_RODAS_FF_E(3);
-    GBDE_RODAS_FF_E(4); GBDE_RODAS_FF_E(5); GBDE_RODAS_FF_E(6);
-#undef GBDE_RODAS_FF_E
+    const RodasFfTab& tb = c_rodas_ff[RodasFfIdx<Tag>::v];
     const ff tt = ff_split(th);
+    const ff w = tt * (ff(1.0f, 0.0f) - tt);
     const float2* sb = stages();
+    FfAcc a[N];
 #pragma unroll
     for (int c = 0; c < N; ++c) {
-      FfAcc a;
-      a.set(uu[c]);
-      a.fma(tt, un[c] - uu[c]);
-#pragma unroll
-      for (int j = 0; j < 7; ++j) a.fma(e[j], ld(sb, j * N + c));
-      out[c] = a.get();
+      a[c].set(uu[c]);
+      a[c].fma(tt, un[c] - uu[c]);
     }
+#pragma unroll 1
+    for (int j = 0; j < 7; ++j) {
+      FfAcc q;
+      q.set(tb.h3[j]);
+      q.fma(tt, tb.h4[j]);
+      const ff q3 = q.get();
+      q.set(tb.h2[j]);
+      q.fma(tt, q3);
+      const ff e = w * q.get();
+#pragma unroll
+      for (int c = 0; c < N; ++c) a[c].fma(e, ld(sb, j * N + c));
+    }
+#pragma unroll
+    for (int c = 0; c < N; ++c) out[c] = a[c].get();
   }
 
   GBDE_D void accept(const ff*, int&) {

@@ -103,6 +103,16 @@ struct WorkSource {
   }
 };
 
+// dt < dtmin or dt <= 4 eps |t| (no representable progress), compared as
+// integers: 4 eps |t| = |t| 2^-50 is |t|'s bit pattern with the exponent
+// lowered by 50 (taken as 0 for |t| < 2^-972).  dt and dtmin are not NaN.
+GBDE_D bool dt_too_small(double dt, double dtmin, double t) {
+  if (ord_bits(dt) < ord_bits(dtmin)) return true;
+  const uint64_t tb = mag_bits(t), sh = 50ull << 52;
+  const uint64_t lim = tb > sh ? tb - sh : 0ull;
+  return (__double_as_longlong(dt) < 0) || mag_bits(dt) <= lim;
+}
+
 // ------------------------------------------------------------- saving
 GBDE_D double save_time(const KArgs& a, int64_t i, int j) {
   return a.save_kind == GBDE_SAVE_GRID ? __ldg(a.saveat + j)
@@ -306,7 +316,7 @@ __device__ void integrate_all(const KArgs& a) {
       const double rem = tf - t;
       double h = dt;
       bool last = false;
-      if (h * (1.0 + 1e-10) >= rem) {
+      if (ord_bits(h * (1.0 + 1e-10)) >= ord_bits(rem)) {
         h = rem;
         last = true;
       }
@@ -324,8 +334,12 @@ __device__ void integrate_all(const KArgs& a) {
           tnew = tf;
           tlo = 0.0;
         } else if (MIXED) {
-          double s, e;
-          two_sum(t, h, s, e);
+          // Fast2Sum on the operands ordered by magnitude (integer compare):
+          // the same exact (s, e) as TwoSum with half the FP64 additions
+          const bool tb = mag_bits(t) >= mag_bits(h);
+          const double big = tb ? t : h, small = tb ? h : t;
+          const double s = big + small;
+          double e = small - (s - big);
           e += tlo;
           tnew = s + e;
           tlo = e - (tnew - s);
@@ -342,7 +356,7 @@ __device__ void integrate_all(const KArgs& a) {
             store_state<N>(a, i, js, alg.unew());
           } else {
             T tmp[N];
-            alg.interp(((ts - t) - tlo) / h, h, tmp, p, nfev);
+            alg.interp(((ts - t) - tlo) * rcp64(h), h, tmp, p, nfev);
             store_state<N>(a, i, js, tmp);
           }
           ++js;
@@ -356,14 +370,14 @@ __device__ void integrate_all(const KArgs& a) {
         for (int c = 0; c < N; ++c) fin &= val_finite(alg.u()[c]);
         if (!fin) ret = GBDE_RET_UNSTABLE;
         else if (last) ret = GBDE_RET_SUCCESS;
-        dt = a.dtmax > 0.0 ? fmin(dtnew, a.dtmax) : dtnew;
+        dt = a.dtmax > 0.0 && ord_bits(dtnew) > ord_bits(a.dtmax) ? a.dtmax : dtnew;
       } else {
         ++nrej;
         dt = h * f2d_bits(ctl_reject(a.ctl, ms));
       }
       if (ret == GBDE_RET_DEFAULT) {
         if (iters >= a.maxiters) ret = GBDE_RET_MAXITERS;
-        else if (a.adaptive && (dt < a.dtmin || dt <= 4.0 * 2.220446049250313e-16 * fabs(t)))
+        else if (a.adaptive && dt_too_small(dt, a.dtmin, t))
           ret = GBDE_RET_DTLESSTHANMIN;
         else if (a.timeout_ns && (iters & 31) == 0 && global_ns() - t_start > a.timeout_ns) {
           ret = GBDE_RET_TIMEOUT;
