@@ -60,7 +60,8 @@ def parse():
     ap.add_argument("--alg", default="rodas5", choices=["rodas5", "rosenbrock23"])
     ap.add_argument("--trajectories", type=int, default=100000)
     ap.add_argument("--chosen", default="persistent-f32x2",
-                    help="chosen form: persistent-f32x2 | plain-f32x2 | persistent | plain | "
+                    help="chosen form: persistent-f32x2 | persistent-f32x2-learned | plain-f32x2 | "
+                         "persistent | plain | "
                          "persistent-mixed | plain-mixed")
     ap.add_argument("--cpu-sample", type=int, default=100000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -363,7 +364,8 @@ def run_learned(args, de):
     else:
         lab, cost = np.zeros(n_train, np.float32), None
     x = de.learned.features(model, *tr[1:5])
-    y = np.c_[np.log10(dt1), lab].astype(np.float32)
+    y = np.c_[np.log10(dt1), lab,
+              de.learned.cost_targets(r["naccept"], r["nreject"])].astype(np.float32)
     logs_s = time.perf_counter() - t
     t = time.perf_counter()
     net, hist = de.learned.train(x, y, epochs=8, batch=4096, lr=2e-3, seed=SEED)
@@ -414,7 +416,7 @@ def run_learned(args, de):
                            nthreads=oracle.hardware_threads(),
                            noise_f32=(base == "lv_sosri"))["u"]
     w = lambda u: (np.abs(u - ref) / (chosen.abstol + chosen.reltol * np.abs(ref))).max(axis=(1, 2))
-    pred_dt, pred_st = de.learned.predict(net, de.learned.features(model, *host[:4]))
+    pred_dt, pred_st, _ = de.learned.predict(net, de.learned.features(model, *host[:4]))
     st_l = rl["naccept"] + rl["nreject"]
     st_b = rb["naccept"] + rb["nreject"]
     line = {"metric": "trajectories/sec at <=10x reltol error vs FP64 oracle; learned vs plain",
@@ -423,7 +425,7 @@ def run_learned(args, de):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "data": "synthetic (seeded, config distributions); held-out seed",
             "config": {"workload": "learned_" + base + "_N%d" % N, "train_pairs": n_train,
-                       "net": "8-64-64-64-2 GELU, BF16 weights, FP32 accumulation",
+                       "net": "8-64-64-64-3 GELU, BF16 weights, FP32 accumulation",
                        "train": "8 epochs, batch 4096, AdamW lr 2e-3 (GPU, own kernels)",
                        "form": "same launch (%s) with and without learned=1" % (
                            "persistent" if chosen.batching else "plain")},
@@ -511,15 +513,41 @@ def main():
 
     forms = {"plain": ("plain", "fp64"), "persistent": ("persistent", "fp64"),
              "persistent-mixed": ("persistent", "mixed"), "plain-mixed": ("plain", "mixed"),
-             "persistent-f32x2": ("persistent", "f32x2"), "plain-f32x2": ("plain", "f32x2")}
+             "persistent-f32x2": ("persistent", "f32x2"), "plain-f32x2": ("plain", "f32x2"),
+             "persistent-f32x2-learned": ("persistent", "f32x2", capi.LEARN_ORDER)}
 
     def opts_for(form):
-        b, prec = forms[form]
+        b, prec = forms[form][:2]
         o = capi.opts_default(alg_id)
         o.reltol, o.abstol = 1e-6, 1e-10
         o.batching = capi.BATCH_PERSISTENT if b == "persistent" else capi.BATCH_PLAIN
         o.precision = {"mixed": capi.PREC_MIXED, "f32x2": capi.PREC_F32X2}.get(prec, capi.PREC_FP64)
+        o.learned = forms[form][2] if len(forms[form]) > 2 else 0
         return o
+
+    learn_info = None
+    if len(forms[args.chosen]) > 2:
+        # the learned queue order: train the cost head on the attempted-step
+        # log of a solve of a separate training ensemble (another seed), on
+        # the GPU with the library's kernels; untimed
+        t_l = time.perf_counter()
+        trp = workload(N, SEED + 104729 + 7919 * rank)
+        trd = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in trp]
+        o_log = opts_for(args.chosen)
+        o_log.learned = 0
+        rlog = de.solve_arrays(de.models.robertson, o_log, *trd, capi.SAVE_PER_TRAJ)
+        x = de.learned.features(de.models.robertson, *trp[:4], device=local)
+        y = np.c_[np.full(N, np.nan), np.full(N, np.nan),
+                  de.learned.cost_targets(rlog["naccept"], rlog["nreject"])].astype(np.float32)
+        t_t = time.perf_counter()
+        net, hist = de.learned.train(x, y, epochs=20, batch=4096, lr=2e-3, seed=SEED, device=local)
+        train_s = time.perf_counter() - t_t
+        de.learned.load(de.models.robertson, net, device=local)
+        learn_info = {"train_trajectories": N, "epochs": 20, "batch": 4096,
+                      "train_s": train_s, "log_and_train_s": time.perf_counter() - t_l,
+                      "final_loss": float(hist[-1]),
+                      "net": "8-64-64-64-3 GELU, BF16 weights, FP32 accumulation; cost head "
+                             "= log2 attempted steps"}
 
     def out_dtype(form):
         return "f32" if forms[form][1] == "mixed" else "f64"
@@ -660,6 +688,7 @@ def main():
         "config": dict(config, chosen_form=args.chosen, l2="flushed between timed steps (256 MB write)",
                        parallelism="trajectory shards, no collective" if world > 1 else "single GPU"),
         "chosen_form": args.chosen,
+        "learned": learn_info,
         "plain": {"value": total / (plain_ms * 1e-3), "ms_per_step": plain_ms,
                   "kernel_ms": plain_kern, "error_vs_oracle": errs["plain"]},
         "speedup_vs_plain": plain_ms / chosen_ms,
@@ -684,7 +713,9 @@ def main():
         # per timed step: the initial-dt pre-pass and the solve kernel, plus
         # histogram / scan / scatter of the longest-span-first queue order for
         # persistent forms
-        "gpu_launches": args.steps * (5 if forms[args.chosen][0] == "persistent" else 2),
+        # learned forms add the network's prediction kernel
+        "gpu_launches": args.steps * ((5 if forms[args.chosen][0] == "persistent" else 2) +
+                                      (1 if learn_info else 0)),
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
     }

@@ -76,7 +76,8 @@ class MlpTrainOpts(C.Structure):
                 ("weight_decay", C.c_float), ("seed", C.c_uint64)]
 
 
-MLP_IN, MLP_PARAMS, MLP_NET_FLOATS = 8, 9026, 9044
+MLP_IN, MLP_OUT, MLP_PARAMS, MLP_NET_FLOATS = 8, 3, 9091, 9111
+LEARN_START, LEARN_ORDER = 1, 2  # gbde_opts.learned flags
 
 
 class TuneEntry(C.Structure):

@@ -174,21 +174,42 @@ class SOSRI(_Alg):
 class EnsembleGB300:
     """Ensemble algorithm that solves every trajectory on one GB300 GPU.
 
-    precision: "fp64" or "mixed" (FP32 state/stages; FP64 compensated time,
-    error norm and W-matrix LU).  batching: "plain" (one launch, a thread per
-    trajectory) or "persistent" (threads refill from a device work queue).
+    precision: "fp64", "mixed" (FP32 state/stages; FP64 compensated time,
+    error norm and W-matrix LU) or "f32x2" (state, stages and right-hand sides
+    as FP32 pairs of ~48 bits; FP64 Jacobian, LU, error norm and compensated
+    time).  batching: "plain" (one launch, a thread per trajectory) or
+    "persistent" (threads refill from a device work queue).  learned: False;
+    True or "start" (the loaded predictor's first dt and AUTO method choice);
+    "order" (the persistent queue ordered by the predicted cost); or a tuple
+    of both names.
     """
 
     def __init__(self, device=0, precision="fp64", batching="plain", learned=False,
                  block_size=0, ctas_per_sm=0, chunk=0, out_dtype=None, timeout_s=0.0):
-        if precision not in ("fp64", "mixed"):
-            raise ValueError("precision must be 'fp64' or 'mixed'")
+        if precision not in ("fp64", "mixed", "f32x2"):
+            raise ValueError("precision must be 'fp64', 'mixed' or 'f32x2'")
         if batching not in ("plain", "persistent"):
             raise ValueError("batching must be 'plain' or 'persistent'")
         self.device, self.precision, self.batching = device, precision, batching
         self.learned, self.block_size, self.ctas_per_sm = learned, block_size, ctas_per_sm
+        self.learned_flags = learned_flags(learned)
         self.chunk, self.timeout_s = chunk, timeout_s
-        self.out_dtype = out_dtype or ("f64" if precision == "fp64" else "f32")
+        self.out_dtype = out_dtype or ("f32" if precision == "mixed" else "f64")
+
+
+def learned_flags(learned):
+    """gbde_opts.learned from EnsembleGB300's `learned` argument."""
+    if learned is False or learned is None:
+        return 0
+    if learned is True:
+        return capi.LEARN_START
+    names = (learned,) if isinstance(learned, str) else tuple(learned)
+    flags = 0
+    for n in names:
+        if n not in ("start", "order"):
+            raise ValueError("learned takes True/False, 'start', 'order' or a tuple of them")
+        flags |= capi.LEARN_START if n == "start" else capi.LEARN_ORDER
+    return flags
 
 
 class EnsembleThreads:
@@ -408,7 +429,8 @@ def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start
             save_kind = capi.SAVE_PER_TRAJ
 
     opts = capi.opts_default(alg.alg_id)
-    opts.precision = capi.PREC_MIXED if ensemblealg.precision == "mixed" else capi.PREC_FP64
+    opts.precision = {"mixed": capi.PREC_MIXED, "f32x2": capi.PREC_F32X2}.get(
+        ensemblealg.precision, capi.PREC_FP64)
     opts.batching = (capi.BATCH_PERSISTENT if ensemblealg.batching == "persistent"
                      else capi.BATCH_PLAIN)
     if reltol is not None:
@@ -430,7 +452,7 @@ def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start
         if k in kwargs:
             setattr(opts, k, float(kwargs[k]))
     opts.seed = int(seed)
-    opts.learned = int(bool(ensemblealg.learned))
+    opts.learned = ensemblealg.learned_flags
     opts.block_size = int(ensemblealg.block_size)
     opts.ctas_per_sm = int(ensemblealg.ctas_per_sm)
     opts.chunk = int(ensemblealg.chunk)

@@ -51,9 +51,10 @@ struct DevBuf {
 // AUTO lists; the learned predictions.  A context keeps one set for its
 // solves; a captured graph keeps its own.
 struct Scratch {
-  DevBuf work, order, part, pred_dt, pred_stiff, dt_init;
+  DevBuf work, order, part, pred_dt, pred_stiff, pred_cost, dt_init;
   void release() {
-    for (DevBuf* b : {&work, &order, &part, &pred_dt, &pred_stiff, &dt_init}) b->release();
+    for (DevBuf* b : {&work, &order, &part, &pred_dt, &pred_stiff, &pred_cost, &dt_init})
+      b->release();
   }
 };
 
@@ -275,7 +276,8 @@ static int solve_auto(gbde_ctx* ctx, Scratch& sc, const LaunchCfg& cfg, const KA
   unsigned long long* work = (unsigned long long*)sc.work.ptr;
   unsigned* counters = reinterpret_cast<unsigned*>(work + 3);
   int32_t *nonstiff = nullptr, *stiff = nullptr;
-  const int8_t* pred = opts->learned ? (const int8_t*)sc.pred_stiff.ptr : nullptr;
+  const int8_t* pred =
+      (opts->learned & GBDE_LEARN_START) ? (const int8_t*)sc.pred_stiff.ptr : nullptr;
   GBDE_CUDA(ctx, build_partition(a.p, np, opts->stiff_threshold, pred, N, sc.part.ptr,
                                  counters, ctx->num_sms, s, &nonstiff, &stiff));
   unsigned cnt[2] = {0, 0};
@@ -362,9 +364,12 @@ static int check_solve_args(gbde_ctx* ctx, const gbde_problem* prob, const gbde_
   if (opts->maxiters <= 0) return set_err(ctx, GBDE_ERR_INVALID, "maxiters must be > 0");
   if (opts->adaptive && !(opts->qmin > 0.0 && opts->qmax >= 1.0 && opts->gamma > 0.0))
     return set_err(ctx, GBDE_ERR_INVALID, "controller needs qmin > 0, qmax >= 1, gamma > 0");
+  if (opts->learned & ~(GBDE_LEARN_START | GBDE_LEARN_ORDER))
+    return set_err(ctx, GBDE_ERR_INVALID, "unknown learned flags %d", opts->learned);
   if (opts->learned && ctx->mlp_model != prob->model)
     return set_err(ctx, GBDE_ERR_STATE,
-                   "learned=1 needs a predictor for model %d (gbde_mlp_load)", prob->model);
+                   "learned=%d needs a predictor for model %d (gbde_mlp_load)", opts->learned,
+                   prob->model);
   if (alg == GBDE_ALG_ROSENBROCK23 && prob->model == GBDE_MODEL_VDP_RING8)
     return set_err(ctx, GBDE_ERR_UNSUPPORTED,
                    "Rosenbrock23 is built for n_state <= 3 (use Rodas5 / Rodas5P for the ring)");
@@ -461,7 +466,7 @@ static bool uses_dt_prepass(const gbde_opts* o, int model) {
   const bool team = model == GBDE_MODEL_VDP_RING8 &&
                     (a == GBDE_ALG_RODAS5 || a == GBDE_ALG_RODAS5P ||
                      (a == GBDE_ALG_TSIT5 && o->threads_per_traj != 1));
-  return ode && !team && o->adaptive && !(o->dt > 0.0) && !o->learned;
+  return ode && !team && o->adaptive && !(o->dt > 0.0) && !(o->learned & GBDE_LEARN_START);
 }
 
 static int reserve_scratch(gbde_ctx* ctx, Scratch& sc, int64_t N, const gbde_opts* opts,
@@ -470,6 +475,7 @@ static int reserve_scratch(gbde_ctx* ctx, Scratch& sc, int64_t N, const gbde_opt
   if (opts->learned && N > 0) {
     GBDE_CUDA(ctx, sc.pred_dt.ensure((size_t)N * sizeof(float)));
     GBDE_CUDA(ctx, sc.pred_stiff.ensure((size_t)N));
+    GBDE_CUDA(ctx, sc.pred_cost.ensure((size_t)N * sizeof(float)));
   }
   if (opts->alg == GBDE_ALG_AUTO && N > 0)
     GBDE_CUDA(ctx, sc.part.ensure(partition_scratch_bytes(N)));
@@ -492,17 +498,23 @@ static int enqueue_solve(gbde_ctx* ctx, Scratch& sc, KArgs& a, const LaunchCfg& 
   a.queue = cfg.persistent ? work : nullptr;
   a.flag = (int32_t*)(work + 1);
   if (opts->learned && N > 0) {
-    // learned predictions: first dt (all methods) and stiff label (AUTO)
+    // learned predictions: first dt (all methods), stiff label (AUTO) and
+    // cost (queue order)
     GBDE_CUDA(ctx, mlp_predict(cfg.model, (const float*)ctx->mlp_net.ptr, a,
-                               (float*)sc.pred_dt.ptr, (int8_t*)sc.pred_stiff.ptr, ctx->num_sms,
-                               s));
-    a.pred_dt = (const float*)sc.pred_dt.ptr;
+                               (float*)sc.pred_dt.ptr, (int8_t*)sc.pred_stiff.ptr,
+                               (float*)sc.pred_cost.ptr, ctx->num_sms, s));
+    if (opts->learned & GBDE_LEARN_START) a.pred_dt = (const float*)sc.pred_dt.ptr;
   }
   if (alg == GBDE_ALG_AUTO) return solve_auto(ctx, sc, cfg, a, np, opts, s);
   if (cfg.persistent && N > 1 && N <= INT32_MAX) {
-    // queue order: longest spans first (order.cu)
+    // queue order (order.cu): highest learned cost first, else longest span
+    // first
     const int32_t* ord = nullptr;
-    GBDE_CUDA(ctx, build_span_order(a.t0, a.tf, N, sc.order.ptr, ctx->num_sms, s, &ord));
+    if (opts->learned & GBDE_LEARN_ORDER)
+      GBDE_CUDA(ctx, build_cost_order((const float*)sc.pred_cost.ptr, N, sc.order.ptr,
+                                      ctx->num_sms, s, &ord));
+    else
+      GBDE_CUDA(ctx, build_span_order(a.t0, a.tf, N, sc.order.ptr, ctx->num_sms, s, &ord));
     a.order = ord;
   }
   if (N > 0) {

@@ -22,10 +22,14 @@ cudaError_t launch_explicit(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s
 cudaError_t launch_rosenbrock(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
 cudaError_t launch_sde(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
 
-// Longest-span-first order of the persistent queue (order.cu).
+// Order of the persistent queue (order.cu): longest span first, or, with a
+// learned cost per trajectory (log2 of its predicted attempted steps), most
+// expensive first.
 size_t span_order_scratch_bytes(int64_t n);
 cudaError_t build_span_order(const double* t0, const double* tf, int64_t n, void* scratch,
                              int num_sms, cudaStream_t s, const int32_t** order_out);
+cudaError_t build_cost_order(const float* log2_cost, int64_t n, void* scratch, int num_sms,
+                             cudaStream_t s, const int32_t** order_out);
 
 // Launch geometry helper shared by the translation units.
 template <class K>
@@ -59,9 +63,10 @@ cudaError_t build_partition(const double* p, int np, double thr, const int8_t* p
                             void* scratch, unsigned* counters, int num_sms, cudaStream_t s,
                             int32_t** nonstiff, int32_t** stiff);
 
-// Learned predictions for a solve (mlp.cu): pred_dt[N] and pred_stiff[N].
+// Learned predictions for a solve (mlp.cu): pred_dt[N], pred_stiff[N] and
+// pred_cost[N] (log2 of the attempted steps).
 cudaError_t mlp_predict(int model, const float* net, const KArgs& a, float* pred_dt,
-                        int8_t* pred_stiff, int num_sms, cudaStream_t s);
+                        int8_t* pred_stiff, float* pred_cost, int num_sms, cudaStream_t s);
 
 // One-thread-per-trajectory step kernel, preceded by the initial-dt pre-pass
 // (k_init_dt) when cfg.dt_init is set.

@@ -48,7 +48,7 @@ struct WarpBuf {
 struct Shared {
   __nv_bfloat16 W1[KIN * HID], W2[HID * HID], W3[HID * HID], W4[HID * K4];
   float b1[HID], b2[HID], b3[HID], b4[NOUT];
-  float xmean[IN], xscale[IN], ymean, yscale, pad_[2];
+  float xmean[IN], xscale[IN], ymean, yscale, cmean, cscale;
   WarpBuf w[WARPS];
 };
 struct SharedGrad {
@@ -82,6 +82,8 @@ GBDE_D void stage_weights(Shared& S, const float* net) {
   if (threadIdx.x == 0) {
     S.ymean = net[OFF_YMEAN];
     S.yscale = net[OFF_YSCALE];
+    S.cmean = net[OFF_CMEAN];
+    S.cscale = net[OFF_CSCALE];
   }
 }
 
@@ -172,13 +174,14 @@ GBDE_D void gelu_back(const float* Z, WarpBuf& W) {
 
 // Loss of one tile and dY: y[0] regression on the normalised log10 of the
 // first accepted step (squared error), y[1] logit of the stiff label (binary
-// cross-entropy); NaN targets carry no loss.  Scaled by 1 / batch.
+// cross-entropy), y[2] regression on the normalised log2 of the attempted
+// steps (squared error); NaN targets carry no loss.  Scaled by 1 / batch.
 GBDE_D void loss_grad(const Shared& S, WarpBuf& W, int lane, bool valid, const float* tgt,
                       float inv_batch) {
-  float l = 0.0f, d0 = 0.0f, d1 = 0.0f;
+  float l = 0.0f, d0 = 0.0f, d1 = 0.0f, d2 = 0.0f;
   if (lane < 16 && valid) {
-    const float y0 = W.Y[lane * NOUT], y1 = W.Y[lane * NOUT + 1];
-    const float t0 = tgt[0], t1 = tgt[1];
+    const float y0 = W.Y[lane * NOUT], y1 = W.Y[lane * NOUT + 1], y2 = W.Y[lane * NOUT + 2];
+    const float t0 = tgt[0], t1 = tgt[1], t2 = tgt[2];
     if (!isnan(t0)) {
       const float tn = (t0 - S.ymean) / S.yscale;
       l += (y0 - tn) * (y0 - tn);
@@ -190,11 +193,17 @@ GBDE_D void loss_grad(const Shared& S, WarpBuf& W, int lane, bool valid, const f
       l += fmaxf(y1, 0.0f) + log1pf(expf(-fabsf(y1))) - t1 * y1;
       d1 = pr - t1;
     }
+    if (!isnan(t2)) {
+      const float tn = (t2 - S.cmean) / S.cscale;
+      l += (y2 - tn) * (y2 - tn);
+      d2 = 2.0f * (y2 - tn);
+    }
   }
   if (lane < 16) {
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
-      const float v = c == 0 ? d0 * inv_batch : (c == 1 ? d1 * inv_batch : 0.0f);
+      const float v = c == 0 ? d0 * inv_batch
+                             : (c == 1 ? d1 * inv_batch : (c == 2 ? d2 * inv_batch : 0.0f));
       W.Db[lane * 16 + c] = __float2bfloat16(v);
       if (c < NOUT) W.D[lane * NOUT + c] = v;
     }
@@ -232,7 +241,8 @@ GBDE_D void backward_tile(const Shared& S, WarpBuf& W, float* g) {
 }
 
 // ------------------------------------------------------------- kernels
-// y[n][2] = raw network outputs (normalised log10 dt, stiff logit)
+// y[n][3] = raw network outputs (normalised log10 dt, stiff logit,
+// normalised log2 steps)
 __global__ void __launch_bounds__(WARPS * 32) k_mlp_forward(const float* __restrict__ net,
                                                           const float* __restrict__ x, int64_t n,
                                                           float* __restrict__ y) {
@@ -248,8 +258,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_mlp_forward(const float* __restr
     fill_input(S, W, lane, i < n, x + (i < n ? i : 0) * IN);
     forward_tile(S, W);
     if (lane < 16 && i < n) {
-      y[i * OUT] = W.Y[lane * NOUT];
-      y[i * OUT + 1] = W.Y[lane * NOUT + 1];
+#pragma unroll
+      for (int c = 0; c < OUT; ++c) y[i * OUT + c] = W.Y[lane * NOUT + c];
     }
     __syncwarp();
   }
@@ -312,8 +322,8 @@ __global__ void k_adamw(float* __restrict__ net, const float* __restrict__ grad,
 
 __global__ void k_step(unsigned* step) { *step += 1; }
 
-// Learned predictions for a solve: features -> network -> first dt and
-// stiff label per trajectory.
+// Learned predictions for a solve: features -> network -> first dt, stiff
+// label and log2 of the attempted steps per trajectory.
 template <class M>
 __global__ void __launch_bounds__(WARPS * 32) k_mlp_predict(const float* __restrict__ net,
                                                           const double* __restrict__ p,
@@ -321,7 +331,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_mlp_predict(const float* __restr
                                                           const double* __restrict__ t0,
                                                           const double* __restrict__ tf, int64_t n,
                                                           float* __restrict__ pred_dt,
-                                                          int8_t* __restrict__ pred_stiff) {
+                                                          int8_t* __restrict__ pred_stiff,
+                                                          float* __restrict__ pred_cost) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Shared& S = *reinterpret_cast<Shared*>(smem_raw);
   stage_weights(S, net);
@@ -340,6 +351,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_mlp_predict(const float* __restr
       const float l10 = W.Y[lane * NOUT] * S.yscale + S.ymean;
       pred_dt[i] = exp10f(fminf(fmaxf(l10, -30.0f), 30.0f));
       pred_stiff[i] = W.Y[lane * NOUT + 1] > 0.0f ? 1 : 0;
+      pred_cost[i] = W.Y[lane * NOUT + 2] * S.cscale + S.cmean;
     }
     __syncwarp();
   }
@@ -392,7 +404,7 @@ int grid_for(int64_t n, int num_sms) {
 namespace gbde {
 // Launch the learned predictions for model `model` (used by capi.cu).
 cudaError_t mlp_predict(int model, const float* net, const KArgs& a, float* pred_dt,
-                        int8_t* pred_stiff, int num_sms, cudaStream_t s) {
+                        int8_t* pred_stiff, float* pred_cost, int num_sms, cudaStream_t s) {
   const int grid = grid_for(a.N, num_sms);
   switch (model) {
 #define GBDE_PRED(ID, M)                                                                  \
@@ -400,7 +412,8 @@ cudaError_t mlp_predict(int model, const float* net, const KArgs& a, float* pred
     cudaError_t e = set_smem(k_mlp_predict<M>, sizeof(Shared));                           \
     if (e != cudaSuccess) return e;                                                       \
     k_mlp_predict<M><<<grid, WARPS * 32, sizeof(Shared), s>>>(net, a.p, a.u0, a.t0, a.tf, \
-                                                               a.N, pred_dt, pred_stiff); \
+                                                               a.N, pred_dt, pred_stiff,  \
+                                                               pred_cost);                \
     return cudaGetLastError();                                                            \
   }
     GBDE_PRED(GBDE_MODEL_LINEAR, Linear)
@@ -431,6 +444,7 @@ int gbde_mlp_init(uint64_t seed, float* net) {
   fill(OFF_W4, HID, HID * OUT);
   for (int k = 0; k < IN; ++k) net[OFF_XSCALE + k] = 1.0f;
   net[OFF_YSCALE] = 1.0f;
+  net[OFF_CSCALE] = 1.0f;
   return GBDE_OK;
 }
 
@@ -527,19 +541,22 @@ int gbde_mlp_train(gbde_ctx* ctx, const float* x, const float* y, int64_t n,
   ctx_device(ctx, &dev, &sms, &s);
   MLP_CUDA(cudaSetDevice(dev));
   // normalisation from the data: features to zero mean / unit scale, the
-  // log10-dt target likewise
+  // log10-dt and log2-steps targets likewise
   std::vector<double> mean(IN, 0.0), sq(IN, 0.0);
-  double ym = 0.0, ysq = 0.0;
-  int64_t ny = 0;
+  double ym[2] = {0.0, 0.0}, ysq[2] = {0.0, 0.0};
+  int64_t ny[2] = {0, 0};
   for (int64_t i = 0; i < n; ++i) {
     for (int k = 0; k < IN; ++k) {
       mean[k] += x[i * IN + k];
       sq[k] += (double)x[i * IN + k] * x[i * IN + k];
     }
-    if (!std::isnan(y[i * OUT])) {
-      ym += y[i * OUT];
-      ysq += (double)y[i * OUT] * y[i * OUT];
-      ++ny;
+    for (int r = 0; r < 2; ++r) {
+      const float v = y[i * OUT + (r == 0 ? 0 : 2)];
+      if (!std::isnan(v)) {
+        ym[r] += v;
+        ysq[r] += (double)v * v;
+        ++ny[r];
+      }
     }
   }
   for (int k = 0; k < IN; ++k) {
@@ -547,10 +564,11 @@ int gbde_mlp_train(gbde_ctx* ctx, const float* x, const float* y, int64_t n,
     net[OFF_XMEAN + k] = (float)m;
     net[OFF_XSCALE + k] = (float)(1.0 / std::sqrt(var > 1e-12 ? var : 1e-12));
   }
-  if (ny > 0) {
-    const double m = ym / ny, var = ysq / ny - m * m;
-    net[OFF_YMEAN] = (float)m;
-    net[OFF_YSCALE] = (float)std::sqrt(var > 1e-12 ? var : 1e-12);
+  for (int r = 0; r < 2; ++r) {
+    if (ny[r] == 0) continue;
+    const double m = ym[r] / ny[r], var = ysq[r] / ny[r] - m * m;
+    net[r == 0 ? OFF_YMEAN : OFF_CMEAN] = (float)m;
+    net[r == 0 ? OFF_YSCALE : OFF_CSCALE] = (float)std::sqrt(var > 1e-12 ? var : 1e-12);
   }
   Dev dnet, dx, dy, dg, dm, dv, dperm, dstep, dloss;
   MLP_CUDA(dnet.alloc(sizeof(float) * NET_FLOATS));

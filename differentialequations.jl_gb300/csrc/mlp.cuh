@@ -1,15 +1,17 @@
-// mlp.cuh -- the learned step-size / stiffness predictor: a 4-layer MLP
-// 8 -> 64 -> 64 -> 64 -> 2 with GELU, BF16 weights and activations as matrix
-// operands, FP32 accumulation, on the tensor cores through warp-level
+// mlp.cuh -- the learned step-size / stiffness / cost predictor: a 4-layer
+// MLP 8 -> 64 -> 64 -> 64 -> 3 with GELU, BF16 weights and activations as
+// matrix operands, FP32 accumulation, on the tensor cores through warp-level
 // mma.sync m16n8k16 (bf16 x bf16 -> f32).
 //
 // Inputs: 8 features of a trajectory (parameters, initial state, time span;
 // models.cuh).  Outputs: y0 = normalised log10 of the first accepted step,
-// y1 = logit of "Rosenbrock is cheaper than the explicit method".
+// y1 = logit of "Rosenbrock is cheaper than the explicit method", y2 =
+// normalised log2 of the attempted steps (the trajectory's cost, which orders
+// the persistent queue).
 //
 // Network blob (GBDE_MLP_NET_FLOATS floats, FP32 master copy):
-//   W1[8][64] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[64][2] b4[2]
-//   x_mean[8] x_scale[8] y_mean y_scale
+//   W1[8][64] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[64][3] b4[3]
+//   x_mean[8] x_scale[8] y_mean y_scale c_mean c_scale
 // Matrices are [in][out]: z = x W + b.
 #pragma once
 #include <cuda_bf16.h>
@@ -20,15 +22,16 @@
 namespace gbde {
 namespace mlp {
 
-constexpr int IN = 8, HID = 64, OUT = 2;
+constexpr int IN = 8, HID = 64, OUT = 3;
 constexpr int KIN = 16;   // IN padded to one k16 tile
 constexpr int NOUT = 8;   // OUT padded to one n8 tile
 constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + IN * HID, OFF_W2 = OFF_B1 + HID,
               OFF_B2 = OFF_W2 + HID * HID, OFF_W3 = OFF_B2 + HID, OFF_B3 = OFF_W3 + HID * HID,
               OFF_W4 = OFF_B3 + HID, OFF_B4 = OFF_W4 + HID * OUT, NPARAM = OFF_B4 + OUT;
 constexpr int OFF_XMEAN = NPARAM, OFF_XSCALE = OFF_XMEAN + IN, OFF_YMEAN = OFF_XSCALE + IN,
-              OFF_YSCALE = OFF_YMEAN + 1, NET_FLOATS = OFF_YSCALE + 1;
-static_assert(NPARAM == 9026, "parameter count");
+              OFF_YSCALE = OFF_YMEAN + 1, OFF_CMEAN = OFF_YSCALE + 1, OFF_CSCALE = OFF_CMEAN + 1,
+              NET_FLOATS = OFF_CSCALE + 1;
+static_assert(NPARAM == 9091 && NET_FLOATS == 9111, "parameter count");
 
 // GELU, tanh form: 0.5 z (1 + tanh(c (z + 0.044715 z^3))), c = sqrt(2/pi)
 GBDE_D float gelu(float z) {

@@ -158,7 +158,7 @@ extern "C" int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_
   if (opts->adaptive && !(opts->qmin > 0.0 && opts->qmax >= 1.0 && opts->gamma > 0.0))
     return fail(GBDE_ERR_INVALID, "controller needs qmin > 0, qmax >= 1, gamma > 0");
   if (opts->learned)
-    return fail(GBDE_ERR_STATE, "gbde_ensemble_solve_noalloc has no learned predictor (learned=1)");
+    return fail(GBDE_ERR_STATE, "gbde_ensemble_solve_noalloc has no learned predictor (learned != 0)");
   if (alg == GBDE_ALG_ROSENBROCK23 && prob->model == GBDE_MODEL_VDP_RING8)
     return fail(GBDE_ERR_UNSUPPORTED,
                 "Rosenbrock23 is built for n_state <= 3 (use Rodas5 / Rodas5P for the ring)");

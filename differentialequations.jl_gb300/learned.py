@@ -1,4 +1,4 @@
-"""The learned step-size / stiffness predictor, host side.
+"""The learned step-size / stiffness / cost predictor, host side.
 
 The network (a 4-layer BF16 MLP, include/gbde.h "learned") is trained on the
 GPU by the library's own kernels (gbde_mlp_train) on step logs that the
@@ -10,11 +10,15 @@ solver itself writes:
   * target 1: stiff label -- 1 where the Rosenbrock method (Rodas5, FP64) is
     cheaper than the explicit one (Tsit5) on that trajectory, measured as
     steps x the measured device time per step of each kernel; NaN where
-    the model has no stiff regime worth predicting.
-A solve with EnsembleGB300(learned=True) (opts.learned = 1) then starts every
-trajectory at the predicted dt and, for GBDE_ALG_AUTO, uses the predicted
-label instead of the threshold.  The error controller still accepts or
-rejects every step, and the plain method is the fallback.
+    the model has no stiff regime worth predicting;
+  * target 2: log2 of the attempted steps (naccept + nreject step logs) of
+    the method the predictor will order the queue for; NaN where not logged.
+A solve with EnsembleGB300(learned=True) (opts.learned = LEARN_START) then
+starts every trajectory at the predicted dt and, for GBDE_ALG_AUTO, uses the
+predicted label instead of the threshold; learned="order" (LEARN_ORDER) has
+the persistent queue hand out trajectories by predicted cost.  The error
+controller still accepts or rejects every step, and the plain method is the
+fallback.
 """
 import ctypes as C
 
@@ -75,7 +79,7 @@ def train(x, y, epochs=20, batch=4096, lr=2e-3, weight_decay=1e-4, seed=0, devic
 
 def forward(net, x, device=0):
     x = np.ascontiguousarray(x, np.float32)
-    y = np.empty((x.shape[0], 2), np.float32)
+    y = np.empty((x.shape[0], capi.MLP_OUT), np.float32)
     ctx = capi.context(device)
     capi.check(capi.lib().gbde_mlp_forward(ctx.handle, np.ascontiguousarray(net, np.float32)
                                            .ctypes.data, x.ctypes.data, x.shape[0],
@@ -104,10 +108,19 @@ def load(model, net, device=0):
 
 
 def predict(net, x, device=0):
-    """(predicted first dt, stiff label) from features, as the solve uses them."""
+    """(predicted first dt, stiff label, predicted attempted steps) from
+    features, as the solve uses them."""
     y = forward(net, x, device)
-    ym, ys = float(net[capi.MLP_NET_FLOATS - 2]), float(net[capi.MLP_NET_FLOATS - 1])
-    return 10.0 ** (y[:, 0] * ys + ym), (y[:, 1] > 0).astype(np.int8)
+    off = capi.MLP_PARAMS + 2 * capi.MLP_IN  # y_mean, y_scale, c_mean, c_scale
+    ym, ys, cm, cs = (float(v) for v in net[off:off + 4])
+    return (10.0 ** (y[:, 0] * ys + ym), (y[:, 1] > 0).astype(np.int8),
+            2.0 ** (y[:, 2] * cs + cm))
+
+
+def cost_targets(naccept, nreject):
+    """Target 2 from a solve's step log: log2 of the attempted steps."""
+    steps = np.asarray(_np(naccept), np.float64) + np.asarray(_np(nreject), np.float64)
+    return np.log2(np.maximum(steps, 1.0)).astype(np.float32)
 
 
 def stiff_labels(solve_arrays, model, p, u0, t0, tf, saveat, save_kind, reltol, abstol,

@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define GBDE_ABI_VERSION 1
+#define GBDE_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define GBDE_API __attribute__((visibility("default")))
@@ -164,7 +164,7 @@ typedef struct {
   int64_t maxiters;    /* attempted steps per trajectory                  */
   double qmin, qmax, gamma, beta1, beta2, qsteady_min, qsteady_max, qoldinit;
   uint64_t seed;       /* Philox key for SDE noise                        */
-  int32_t learned;     /* 1 = the loaded MLP predicts first dt / method   */
+  int32_t learned;     /* GBDE_LEARN_* flags (0 = no learned predictor)   */
   int32_t block_size;  /* threads per CTA (0 = tuned default)             */
   int32_t chunk;       /* persistent-queue trajectories per fetch (0 = default) */
   int32_t ctas_per_sm; /* persistent CTAs per SM (0 = tuned default)      */
@@ -285,7 +285,7 @@ GBDE_API int gbde_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
  *     call's contents (each call clears what it needs in stream order).
  *     Calls that overlap on the GPU race: serialise them on one stream or
  *     with events;
- *   - learned=1 is rejected (GBDE_ERR_STATE); device_ms is not measured (0).
+ *   - learned != 0 is rejected (GBDE_ERR_STATE); device_ms is not measured (0).
  * Blocks until the kernels have finished. */
 #define GBDE_NOALLOC_SCRATCH_BYTES 256
 GBDE_API int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_opts* opts,
@@ -295,22 +295,30 @@ GBDE_API int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_op
  * with a dependent-chain-free FMA loop; kind 0 = FP64, 1 = FP32. */
 GBDE_API int gbde_measure_fma_peak(gbde_ctx* ctx, int32_t kind, double* tflops);
 
-/* ---- learned step-size / stiffness predictor ----------------------------
+/* ---- learned step-size / stiffness / cost predictor ----------------------
  * No counterpart in the reference (its nearest relative is the runtime
  * stiffness switching of AutoTsit5(Rosenbrock23()), test/qa/qa.jl:15).
- * A 4-layer MLP 8 -> 64 -> 64 -> 64 -> 2 with GELU, BF16 weights and FP32
+ * A 4-layer MLP 8 -> 64 -> 64 -> 64 -> 3 with GELU, BF16 weights and FP32
  * accumulation maps 8 features of a trajectory (its parameters, initial state
  * and time span; gbde_mlp_features) to (log10 of the first accepted dt,
- * logit of "stiff").  With opts.learned = 1 a solve runs the loaded network
- * first: the prediction replaces the Hairer-Wanner starting step, and
- * GBDE_ALG_AUTO uses the stiff label instead of the threshold.  The error
- * controller still accepts or rejects every step.
+ * logit of "stiff", log2 of the attempted steps).  A solve with opts.learned
+ * != 0 runs the loaded network first:
+ *   GBDE_LEARN_START: the predicted dt replaces the Hairer-Wanner starting
+ *     step, and GBDE_ALG_AUTO uses the stiff label instead of the threshold;
+ *   GBDE_LEARN_ORDER: the persistent queue hands out trajectories by
+ *     predicted cost, highest first, instead of longest span first -- the
+ *     lanes of a warp then carry trajectories of similar step counts.  Each
+ *     trajectory's result does not depend on the order.
+ * The error controller still accepts or rejects every step.
  * Network blob: GBDE_MLP_NET_FLOATS floats, FP32:
- *   W1[8][64] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[64][2] b4[2]
- *   x_mean[8] x_scale[8] y_mean y_scale                                   */
+ *   W1[8][64] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[64][3] b4[3]
+ *   x_mean[8] x_scale[8] y_mean y_scale c_mean c_scale                    */
 #define GBDE_MLP_IN 8
-#define GBDE_MLP_PARAMS 9026
-#define GBDE_MLP_NET_FLOATS 9044
+#define GBDE_MLP_OUT 3
+#define GBDE_MLP_PARAMS 9091
+#define GBDE_MLP_NET_FLOATS 9111
+#define GBDE_LEARN_START 1 /* learned first dt and AUTO method choice          */
+#define GBDE_LEARN_ORDER 2 /* persistent queue ordered by the learned cost     */
 
 typedef struct {
   int32_t epochs;      /* passes over the data                              */
@@ -325,21 +333,21 @@ GBDE_API int gbde_mlp_init(uint64_t seed, float* net);
 /* features[N][8] (device memory) of every trajectory of a device-memory
  * problem. */
 GBDE_API int gbde_mlp_features(gbde_ctx* ctx, const gbde_problem* prob, float* features);
-/* Train on the GPU: x[n][8] features, y[n][2] targets (log10 first accepted
- * dt, stiff label 0/1; NaN = no label), host memory.  `net` holds the initial
+/* Train on the GPU: x[n][8] features, y[n][3] targets (log10 first accepted
+ * dt, stiff label 0/1, log2 attempted steps; NaN = no label), host memory.  `net` holds the initial
  * weights on entry and the trained network on return (the normalisation
  * fields are set from the data); loss_history[epochs] may be NULL. */
 GBDE_API int gbde_mlp_train(gbde_ctx* ctx, const float* x, const float* y, int64_t n,
                    const gbde_mlp_train_opts* opts, float* net, float* loss_history);
-/* Raw outputs y[n][2] (normalised log10 dt, stiff logit) for x[n][8]; host
- * memory. */
+/* Raw outputs y[n][3] (normalised log10 dt, stiff logit, normalised log2
+ * steps) for x[n][8]; host memory. */
 GBDE_API int gbde_mlp_forward(gbde_ctx* ctx, const float* net, const float* x, int64_t n,
                      float* y);
 /* Gradient of the mean training loss over (x, y) w.r.t. the GBDE_MLP_PARAMS
  * weights, and the loss; host memory. */
 GBDE_API int gbde_mlp_grad(gbde_ctx* ctx, const float* net, const float* x, const float* y,
                   int64_t n, float* grad, float* loss);
-/* Make `net` (host) the network that learned=1 solves of `model` use. */
+/* Make `net` (host) the network that learned solves of `model` use. */
 GBDE_API int gbde_mlp_load(gbde_ctx* ctx, int32_t model, const float* net);
 
 /* Self-check (no counterpart in the reference): the largest relative

@@ -1,6 +1,6 @@
 """CPU oracle of the learned predictor's network (TEST INFRASTRUCTURE ONLY).
 
-A numpy restatement of the 8 -> 64 -> 64 -> 64 -> 2 GELU MLP of the library
+A numpy restatement of the 8 -> 64 -> 64 -> 64 -> 3 GELU MLP of the library
 (csrc/mlp.cuh): forward pass, training loss and its gradient.  Two modes:
   * bf16=True mirrors where the GPU kernels round to BF16 (weights, the
     normalised input, every hidden activation, and the output / hidden
@@ -11,7 +11,7 @@ Only tests/ use this module; the product never imports it.
 """
 import numpy as np
 
-IN, HID, OUT = 8, 64, 2
+IN, HID, OUT = 8, 64, 3
 OFF_W1 = 0
 OFF_B1 = OFF_W1 + IN * HID
 OFF_W2 = OFF_B1 + HID
@@ -23,7 +23,8 @@ OFF_B4 = OFF_W4 + HID * OUT
 NPARAM = OFF_B4 + OUT
 OFF_XMEAN, OFF_XSCALE = NPARAM, NPARAM + IN
 OFF_YMEAN, OFF_YSCALE = NPARAM + 2 * IN, NPARAM + 2 * IN + 1
-NET_FLOATS = OFF_YSCALE + 1
+OFF_CMEAN, OFF_CSCALE = OFF_YSCALE + 1, OFF_YSCALE + 2
+NET_FLOATS = OFF_CSCALE + 1
 C_GELU = 0.7978845608028654  # sqrt(2 / pi)
 
 
@@ -51,11 +52,12 @@ def unpack(net):
                 W3=net[OFF_W3:OFF_B3].reshape(HID, HID), b3=net[OFF_B3:OFF_W4],
                 W4=net[OFF_W4:OFF_B4].reshape(HID, OUT), b4=net[OFF_B4:NPARAM],
                 xmean=net[OFF_XMEAN:OFF_XSCALE], xscale=net[OFF_XSCALE:OFF_YMEAN],
-                ymean=net[OFF_YMEAN], yscale=net[OFF_YSCALE])
+                ymean=net[OFF_YMEAN], yscale=net[OFF_YSCALE],
+                cmean=net[OFF_CMEAN], cscale=net[OFF_CSCALE])
 
 
 def forward(net, x, bf=True):
-    """Returns y[n][2] and the saved activations."""
+    """Returns y[n][3] and the saved activations."""
     P = unpack(net)
     r = bf16 if bf else (lambda a: np.asarray(a, np.float64))
     xn = r((np.asarray(x, np.float32) - P["xmean"].astype(np.float32)) *
@@ -73,23 +75,27 @@ def forward(net, x, bf=True):
 
 def loss_and_grad(net, x, t, bf=True):
     """Mean loss over the batch and its gradient w.r.t. the NPARAM weights.
-    t[n][2]: log10 first accepted dt (squared error on the normalised value),
-    stiff label (binary cross-entropy on the logit); NaN = no label."""
+    t[n][3]: log10 first accepted dt (squared error on the normalised value),
+    stiff label (binary cross-entropy on the logit), log2 attempted steps
+    (squared error on the normalised value); NaN = no label."""
     P = unpack(net)
     r = bf16 if bf else (lambda a: np.asarray(a, np.float64))
     y, S = forward(net, x, bf)
     n = y.shape[0]
     t = np.asarray(t, np.float64)
-    m0, m1 = ~np.isnan(t[:, 0]), ~np.isnan(t[:, 1])
+    m0, m1, m2 = ~np.isnan(t[:, 0]), ~np.isnan(t[:, 1]), ~np.isnan(t[:, 2])
     tn = np.where(m0, (t[:, 0] - P["ymean"]) / P["yscale"], 0.0)
     t1 = np.where(m1, t[:, 1], 0.0)
-    y0, y1 = y[:, 0], y[:, 1]
+    cn = np.where(m2, (t[:, 2] - P["cmean"]) / P["cscale"], 0.0)
+    y0, y1, y2 = y[:, 0], y[:, 1], y[:, 2]
     loss = np.sum(np.where(m0, (y0 - tn) ** 2, 0.0))
     loss += np.sum(np.where(m1, np.maximum(y1, 0) + np.log1p(np.exp(-np.abs(y1))) - t1 * y1, 0.0))
+    loss += np.sum(np.where(m2, (y2 - cn) ** 2, 0.0))
     loss /= n
     dy = np.zeros_like(y)
     dy[:, 0] = np.where(m0, 2 * (y0 - tn), 0.0) / n
     dy[:, 1] = np.where(m1, 1 / (1 + np.exp(-y1)) - t1, 0.0) / n
+    dy[:, 2] = np.where(m2, 2 * (y2 - cn), 0.0) / n
     g = np.zeros(NPARAM)
     dyb = r(dy).astype(np.float64)
     z1, z2, z3 = S["z"]

@@ -36,7 +36,7 @@ def test_header_struct_layout_matches_ctypes(capi):
 
 
 def test_version_and_model_info(capi):
-    assert capi.lib().gbde_version() == 1
+    assert capi.lib().gbde_version() == 2
     assert capi.model_info(capi.MODEL_LORENZ) == (3, 3)
     assert capi.model_info(capi.MODEL_VDP_RING8) == (16, 2)
     with pytest.raises(capi.GBDEError):

@@ -13,18 +13,21 @@ def random_net(capi, de, seed):
     net = de.learned.init(seed)
     rng = np.random.default_rng(seed)
     net[M.OFF_B1:M.OFF_W2] = rng.normal(0, 0.1, M.HID)
-    net[M.OFF_B4:M.NPARAM] = rng.normal(0, 0.1, 2)
+    net[M.OFF_B4:M.NPARAM] = rng.normal(0, 0.1, M.OUT)
     net[M.OFF_XMEAN:M.OFF_XSCALE] = rng.normal(0, 1, M.IN)
     net[M.OFF_XSCALE:M.OFF_YMEAN] = rng.uniform(0.5, 2, M.IN)
     net[M.OFF_YMEAN], net[M.OFF_YSCALE] = -2.0, 1.5
+    net[M.OFF_CMEAN], net[M.OFF_CSCALE] = 6.0, 0.8
     return net
 
 
 def batch(rng, n):
     x = rng.normal(0, 1.5, (n, M.IN)).astype(np.float32)
-    y = np.c_[rng.normal(-2, 1.5, n), (rng.uniform(size=n) < 0.4)].astype(np.float32)
+    y = np.c_[rng.normal(-2, 1.5, n), (rng.uniform(size=n) < 0.4),
+              rng.normal(6, 1, n)].astype(np.float32)
     y[rng.uniform(size=n) < 0.1, 0] = np.nan  # unlabelled dt
     y[rng.uniform(size=n) < 0.2, 1] = np.nan  # unlabelled stiffness
+    y[rng.uniform(size=n) < 0.15, 2] = np.nan  # unlogged cost
     return x, y
 
 
@@ -50,7 +53,7 @@ def test_oracle_gradient_finite_differences(capi, de):
     net = random_net(capi, de, 3).astype(np.float64)
     x, y = batch(rng, 64)
     _, g = M.loss_and_grad(net, x, y, bf=False)
-    idx = np.r_[rng.choice(M.NPARAM, 60, replace=False), M.OFF_B4, M.OFF_B4 + 1]
+    idx = np.r_[rng.choice(M.NPARAM, 60, replace=False), M.OFF_B4, M.OFF_B4 + 1, M.OFF_B4 + 2]
     for i in idx:
         h = 1e-6 * max(1.0, abs(net[i]))
         a, b = net.copy(), net.copy()
@@ -88,18 +91,24 @@ def test_gpu_gradient_vs_oracle(capi, de):
 
 @pytest.mark.gpu
 def test_gpu_training_fits(capi, de):
-    """Training on the GPU fits a smooth synthetic target and a label."""
+    """Training on the GPU fits two smooth synthetic targets and a label."""
     rng = np.random.default_rng(6)
     n = 40000
+
+    def targets(x):
+        return (np.sin(2 * x[:, 0]) + x[:, 1] * x[:, 2] - 3.0, (x[:, 3] + x[:, 4] > 0),
+                5.0 + x[:, 5] - 0.5 * x[:, 6] ** 2)
+
     x = rng.uniform(-1, 1, (n, M.IN)).astype(np.float32)
-    y = np.c_[np.sin(2 * x[:, 0]) + x[:, 1] * x[:, 2] - 3.0, (x[:, 3] + x[:, 4] > 0)].astype(np.float32)
+    y = np.stack(targets(x), 1).astype(np.float32)
     net, hist = de.learned.train(x, y, epochs=30, batch=1024, lr=2e-3, seed=1)
     assert hist[-1] < 0.25 * hist[0], hist
     xt = rng.uniform(-1, 1, (5000, M.IN)).astype(np.float32)
-    dt, st = de.learned.predict(net, xt)
-    t0 = np.sin(2 * xt[:, 0]) + xt[:, 1] * xt[:, 2] - 3.0
+    dt, st, cost = de.learned.predict(net, xt)
+    t0, t1, t2 = targets(xt)
     assert np.median(np.abs(np.log10(dt) - t0)) < 0.1
-    assert np.mean(st == (xt[:, 3] + xt[:, 4] > 0)) > 0.9
+    assert np.mean(st == t1) > 0.9
+    assert np.median(np.abs(np.log2(cost) - t2)) < 0.1
 
 
 def _lorenz(de, N, seed):
@@ -121,7 +130,8 @@ def test_learned_first_dt_lorenz(capi, de, oracle):
     p, u0, t0, tf = _lorenz(de, 20000, 1)
     r = de.solve_arrays(model, o, p, u0, t0, tf, grid, capi.SAVE_GRID)
     x = de.learned.features(model, p, u0, t0, tf)
-    y = np.c_[np.log10(r["dt_first"]), np.zeros(len(p))].astype(np.float32)
+    y = np.c_[np.log10(r["dt_first"]), np.zeros(len(p)),
+              de.learned.cost_targets(r["naccept"], r["nreject"])].astype(np.float32)
     net, hist = de.learned.train(x, y, epochs=20, batch=1024, seed=2)
     de.learned.load(model, net)
     p, u0, t0, tf = _lorenz(de, 5000, 99)  # held out
@@ -132,7 +142,7 @@ def test_learned_first_dt_lorenz(capi, de, oracle):
     ref = oracle.solve(capi, model, _o(capi, 1e-8),
                        p, u0, t0, tf, grid, capi.SAVE_GRID, nthreads=8)
     assert oracle.weighted_error(lr["u"], ref["u"], 1e-8, 1e-8) <= 10.0
-    pred, _ = de.learned.predict(net, de.learned.features(model, p, u0, t0, tf))
+    pred, _, _ = de.learned.predict(net, de.learned.features(model, p, u0, t0, tf))
     assert np.median(np.abs(np.log10(pred / plain["dt_first"]))) < 0.15
     assert lr["nf"].sum() < plain["nf"].sum()
 
@@ -164,7 +174,7 @@ def test_learned_stiffness_vdp(capi, de):
     o.maxiters = 10 ** 6
     r = de.solve_arrays(model, o, p, u0, t0, tf, grid, capi.SAVE_GRID)
     x = de.learned.features(model, p, u0, t0, tf)
-    y = np.c_[np.log10(r["dt_first"]), lab].astype(np.float32)
+    y = np.c_[np.log10(r["dt_first"]), lab, np.full(len(p), np.nan)].astype(np.float32)
     net, _ = de.learned.train(x, y, epochs=40, batch=1024, seed=4)
     de.learned.load(model, net)
     p, u0, t0, tf = inputs(8000, 77)  # held out
@@ -186,3 +196,43 @@ def test_learned_stiffness_vdp(capi, de):
     chosen = (runs["learned"]["method"] == capi.ALG_RODAS5).astype(np.float32)
     assert np.mean(chosen == lab_t) > 0.85
     assert units(runs["learned"]) < units(runs["threshold"])
+
+
+def _robertson(N, seed):
+    rng = np.random.default_rng(seed)
+    p = np.array([0.04, 3e7, 1e4]) * 10 ** rng.uniform(-1, 1, (N, 3))
+    tf = 10 ** rng.uniform(1, 5, N)
+    saveat = tf[:, None] * 10 ** (-5 + 5 * np.arange(20) / 19)
+    return p, np.tile([1.0, 0.0, 0.0], (N, 1)), np.zeros(N), tf, np.ascontiguousarray(saveat)
+
+
+@pytest.mark.gpu
+def test_learned_queue_order_robertson(capi, de):
+    """Trained on the attempted-step logs of a Rodas5 solve, the cost head
+    predicts held-out step counts closely (R^2 > 0.9), and a persistent solve
+    whose queue is ordered by the predicted cost (learned = LEARN_ORDER)
+    gives bit-identical results to the span-ordered one: the order decides
+    only which lane runs a trajectory when."""
+    model = de.models.robertson
+    o = capi.opts_default(capi.ALG_RODAS5)
+    o.reltol, o.abstol = 1e-6, 1e-10
+    o.batching = capi.BATCH_PERSISTENT
+    o.precision = capi.PREC_F32X2
+    p, u0, t0, tf, sv = _robertson(20000, 11)
+    r = de.solve_arrays(model, o, p, u0, t0, tf, sv, capi.SAVE_PER_TRAJ)
+    x = de.learned.features(model, p, u0, t0, tf)
+    y = np.c_[np.full(len(p), np.nan), np.full(len(p), np.nan),
+              de.learned.cost_targets(r["naccept"], r["nreject"])].astype(np.float32)
+    net, _ = de.learned.train(x, y, epochs=20, batch=1024, seed=5)
+    de.learned.load(model, net)
+    p, u0, t0, tf, sv = _robertson(8000, 12)  # held out
+    base = de.solve_arrays(model, o, p, u0, t0, tf, sv, capi.SAVE_PER_TRAJ)
+    steps = (base["naccept"] + base["nreject"]).astype(np.float64)
+    _, _, pred = de.learned.predict(net, de.learned.features(model, p, u0, t0, tf))
+    r2 = 1 - np.sum((np.log2(steps) - np.log2(pred)) ** 2) / np.sum(
+        (np.log2(steps) - np.log2(steps).mean()) ** 2)
+    assert r2 > 0.9, r2
+    o.learned = capi.LEARN_ORDER
+    lo = de.solve_arrays(model, o, p, u0, t0, tf, sv, capi.SAVE_PER_TRAJ)
+    for k in ("u", "retcode", "naccept", "nreject", "nf", "t_end"):
+        assert np.array_equal(lo[k], base[k], equal_nan=(k == "u")), k
