@@ -10,9 +10,11 @@ per second of the chosen form with inputs resident in HBM (device pointers,
 one gbde_ensemble_solve); `e2e` is the same through the C ABI with pinned
 host buffers (H2D + solve + D2H inside the timed region).  `plain` is the
 plain one-thread-per-trajectory FP64 launch for comparison.  The chosen form
-(default: the persistent longest-span-first queue with state, stages and
-right-hand sides in FP32 pairs, FP64 Jacobian / LU / error norm / compensated
-time) is checked against the CPU FP64 oracle on a sample before timing.
+(default: the persistent queue ordered by the learned cost predictor, with
+state, stages and right-hand sides in FP32 pairs and an FP64 Jacobian / LU /
+error norm / compensated time) is checked against the CPU FP64 oracle on a
+sample before timing.  The learned form first trains the predictor's cost
+head on the step log of a separate training ensemble (untimed).
 
 --impl reference times the CPU FP64 restatement (EnsembleThreads-equivalent
 std::thread pool over all host cores) on the same workload.
@@ -46,9 +48,11 @@ FLOPS = {
 # DRAM bytes (read + write) per trajectory of the Rodas5 solve kernel, from one
 # ncu capture each, scaled by trajectories.  FP64 stepper: 20,000 trajectories,
 # 4.587 MB read + 8.2 KB written (the saved states stay in L2 until after the
-# kernel).  FP32-pair stepper: 100,000 trajectories, persistent launch.
+# kernel).  FP32-pair stepper: 100,000 trajectories, persistent launch in
+# longest-span-first and in learned-cost order.
 TRAFFIC_PER_TRAJ = {"fp64": (4.586752e6 + 8192.0) / 20000.0,
-                    "f32x2": (28.150272e6 + 6.957824e6) / 100000.0}
+                    "f32x2": (31.265536e6 + 9.635328e6) / 100000.0,
+                    "f32x2-learned": (30.901504e6 + 8.447488e6) / 100000.0}
 
 
 def parse():
@@ -59,7 +63,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--alg", default="rodas5", choices=["rodas5", "rosenbrock23"])
     ap.add_argument("--trajectories", type=int, default=100000)
-    ap.add_argument("--chosen", default="persistent-f32x2",
+    ap.add_argument("--chosen", default="persistent-f32x2-learned",
                     help="chosen form: persistent-f32x2 | persistent-f32x2-learned | plain-f32x2 | "
                          "persistent | plain | "
                          "persistent-mixed | plain-mixed")
@@ -588,6 +592,7 @@ def main():
             de.solve_arrays(de.models.robertson, o, *dptr, capi.SAVE_PER_TRAJ,
                             u_dtype=out_dtype(form), out=outs)
         tot, kern = 0.0, 0.0
+        per = step_log.setdefault(form, [])
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
@@ -601,6 +606,7 @@ def main():
             e1.record(stream)
             torch.cuda.synchronize()
             tot += e0.elapsed_time(e1)
+            per.append(e0.elapsed_time(e1))
             kern += r["device_ms"]
         if world > 1:
             dist.barrier()
@@ -628,9 +634,12 @@ def main():
             de.solve_arrays(de.models.robertson, o, *hp, capi.SAVE_PER_TRAJ,
                             u_dtype=out_dtype(form), out=outs)
             ts.append(time.perf_counter() - t)
+            step_log.setdefault("e2e", []).append(ts[-1] * 1e3)
         h2d = sum(a.nbytes for a in hp)
         d2h = outs["u"].nbytes + outs["retcode"].nbytes
         return float(np.mean(ts)) * 1e3, h2d, d2h
+
+    step_log = {}  # per-step times (ms) of each timed loop, for the spread
 
     with ClockSampler(local) as clk:
         chosen_ms, chosen_kern = timed_device(args.chosen, args.steps, args.warmup)
@@ -701,7 +710,8 @@ def main():
                               "peak" + ("; this form executes them as FP32-pair arithmetic with an "
                                         "FP64 Jacobian, LU, error norm and time, so the fraction "
                                         "is FP64-equivalent and is not capped at 1" if pairs else ""),
-                     "traffic": (TRAFFIC_PER_TRAJ["f32x2" if pairs else "fp64"] * N
+                     "traffic": (TRAFFIC_PER_TRAJ[("f32x2-learned" if learn_info else "f32x2")
+                                                  if pairs else "fp64"] * N
                                  if args.alg == "rodas5" else None),
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
                                        "launch (%s trajectories), scaled by trajectories"
@@ -717,6 +727,8 @@ def main():
         "gpu_launches": args.steps * ((5 if forms[args.chosen][0] == "persistent" else 2) +
                                       (1 if learn_info else 0)),
         "clocks": clk.summary(),
+        "step_ms_spread": {k: {"min": float(np.min(v)), "median": float(np.median(v)),
+                               "max": float(np.max(v))} for k, v in step_log.items()},
         "cpu_baseline": cpu,
     }
     print(json.dumps(line))
