@@ -26,6 +26,7 @@ RET_DEFAULT, RET_SUCCESS, RET_MAXITERS, RET_DTLESSTHANMIN, RET_UNSTABLE = 0, 1, 
 RET_INITIALFAILURE, RET_TIMEOUT = 5, 6
 
 MODEL_LINEAR, MODEL_LORENZ, MODEL_ROBERTSON, MODEL_VDP_RING8, MODEL_LOTKA_VOLTERRA = 1, 2, 3, 4, 5
+MODEL_USER_BASE, USER_MAX_STATE, USER_MAX_PARAM = 1000, 8, 32
 
 ALG_TSIT5, ALG_VERN7, ALG_ROSENBROCK23, ALG_RODAS5, ALG_RODAS5P = 1, 2, 3, 4, 5
 ALG_EM, ALG_SOSRI, ALG_AUTO = 6, 7, 8
@@ -85,6 +86,11 @@ class TuneEntry(C.Structure):
                 ("chunk", C.c_int32), ("threads_per_traj", C.c_int32), ("device_ms", C.c_float)]
 
 
+class UserModel(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("n_state", C.c_int32), ("n_param", C.c_int32),
+                ("f_body", C.c_char_p), ("jac_body", C.c_char_p)]
+
+
 # Every function gbde.h declares, with its ctypes signature.
 SIGNATURES = {
     "gbde_version": (C.c_int, []),
@@ -115,6 +121,8 @@ SIGNATURES = {
                                     C.POINTER(Outputs), C.POINTER(C.c_void_p)]),
     "gbde_graph_launch": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "gbde_graph_destroy": (C.c_int, [C.c_void_p]),
+    "gbde_model_register": (C.c_int, [C.POINTER(UserModel), C.POINTER(C.c_int32)]),
+    "gbde_model_compile": (C.c_int, [C.c_int32, C.c_int32, C.c_int32]),
     "gbde_autotune": (C.c_int, [C.c_void_p, C.POINTER(Problem), C.POINTER(Opts),
                                 C.POINTER(Outputs), C.c_int32, C.POINTER(Opts),
                                 C.POINTER(TuneEntry), C.c_int32, C.POINTER(C.c_int32)]),

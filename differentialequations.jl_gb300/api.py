@@ -64,16 +64,48 @@ class models:
                                "p=[alpha, beta, gamma, delta, sigma]")
 
 
+def ODEFunction(f, n_state, n_param, jac=None, name="user_model"):
+    """A user right-hand side (the reference's ODEFunction, qa.jl:84), given
+    as CUDA C++ source and compiled at run time for the GPU (NVRTC).
+
+    f: statements that fill du[0..n_state) from u[0..n_state) and
+    p[0..n_param) in a function template over the scalar type T, e.g.
+        "du[0] = p[0] * (u[1] - u[0]);  du[1] = ..."
+    jac: optional statements filling J[r][c] = d du_r / d u_c; without it the
+    Rosenbrock methods differentiate f with forward-mode dual numbers.
+    The system is autonomous (carry t as an extra state if f depends on it).
+    Registration copies the source; the first solve with an algorithm and a
+    precision compiles the kernels (under a second) and caches them.
+    Returns a Model usable as ODEProblem's f.
+    """
+    import ctypes as C
+    d = capi.UserModel(name=name.encode(), n_state=int(n_state), n_param=int(n_param),
+                       f_body=f.encode(), jac_body=jac.encode() if jac else None)
+    mid = C.c_int32()
+    capi.check(capi.lib().gbde_model_register(C.byref(d), C.byref(mid)))
+    m = Model(name, mid.value, int(n_state), int(n_param), doc="user model (runtime-compiled)")
+    m.f_source, m.jac_source = f, jac
+    return m
+
+
+def compile_model(model, alg, precision="fp64"):
+    """Compile a user model's kernels for one algorithm and precision ahead of
+    the first solve (no GPU needed); raises GBDEError with NVRTC's log."""
+    prec = {"fp64": capi.PREC_FP64, "mixed": capi.PREC_MIXED, "f32x2": capi.PREC_F32X2}[precision]
+    capi.check(capi.lib().gbde_model_compile(model.id, alg.alg_id, prec))
+
+
 # -------------------------------------------------------------- problems
 class ODEProblem:
-    """ODEProblem(f, u0, tspan, p; kwargs...) with a built-in model as f."""
+    """ODEProblem(f, u0, tspan, p; kwargs...) with a built-in model or a
+    user model (ODEFunction) as f."""
 
     is_sde = False
 
     def __init__(self, f, u0, tspan, p=None, **kwargs):
         if not isinstance(f, Model):
-            raise TypeError("f must be a built-in Model (models.lorenz, ...); user RHS "
-                            "functions are not compiled by this library")
+            raise TypeError("f must be a Model: a built-in one (models.lorenz, ...) or a "
+                            "user right-hand side from ODEFunction(source, n_state, n_param)")
         self.f = f
         self.u0 = np.atleast_1d(np.asarray(u0, dtype=np.float64)).copy()
         self.tspan = (float(tspan[0]), float(tspan[1]))

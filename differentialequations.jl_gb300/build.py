@@ -38,6 +38,31 @@ def sources():
     return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
 
 
+# Headers that runtime-compiled user models include (rtc.cu), embedded into
+# the library as {include name, text}; gbde.h under the name models.cuh uses.
+RTC_HEADERS = ["common.cuh", "controller.h", "solver.cuh", "models.cuh", "ff.cuh", "tableaus.h",
+               "dense_coeffs.h", "explicit_rk.cuh", "rosenbrock.cuh", "rodas_ff.cuh", "dual.cuh"]
+
+
+def write_rtc_headers():
+    """Write _build/rtc_headers.inc (only when its content changes)."""
+    items = [(h, os.path.join(CSRC, h)) for h in RTC_HEADERS]
+    items.append(("../../include/gbde.h", os.path.join(HERE, "..", "include", "gbde.h")))
+    out = ["// generated by build.py from the library's headers; do not edit",
+           "static const RtcHeader kRtcHeaders[] = {"]
+    for name, path in items:
+        text = open(path).read()
+        if ")GBDE_RTC_\"" in text:
+            raise RuntimeError("%s contains the raw-string delimiter" % name)
+        out.append('  {"%s", R"GBDE_RTC_(%s)GBDE_RTC_"},' % (name, text))
+    out.append("};")
+    content = "\n".join(out) + "\n"
+    path = os.path.join(OBJDIR, "rtc_headers.inc")
+    if not os.path.exists(path) or open(path).read() != content:
+        with open(path, "w") as f:
+            f.write(content)
+
+
 def _deps():
     return sources() + glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(
         os.path.join(CSRC, "*.cuh")) + [os.path.join(HERE, "..", "include", "gbde.h"), __file__]
@@ -56,11 +81,12 @@ def build(force=False, jobs=None, verbose=False):
         return LIB
     nvcc = _nvcc()
     os.makedirs(OBJDIR, exist_ok=True)
+    write_rtc_headers()
     srcs = sources()
 
     def compile_one(src):
         obj = os.path.join(OBJDIR, os.path.basename(src) + ".o")
-        cmd = [nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj]
+        cmd = [nvcc] + NVCC_FLAGS + ["-I", OBJDIR, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))
@@ -72,7 +98,7 @@ def build(force=False, jobs=None, verbose=False):
     with cf.ThreadPoolExecutor(jobs) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB + ".tmp"
-    cmd = [nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", tmp] + objs
+    cmd = [nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", tmp] + objs + ["-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

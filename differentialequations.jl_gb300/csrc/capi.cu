@@ -77,7 +77,7 @@ struct gbde_ctx {
 };
 
 static int set_err(gbde_ctx* ctx, int code, const char* fmt, ...) {
-  char buf[512];
+  char buf[4096];  // room for a user model's compile log
   va_list ap;
   va_start(ap, fmt);
   vsnprintf(buf, sizeof(buf), fmt, ap);
@@ -107,6 +107,7 @@ int set_thread_error(int code, const char* msg) {
 // one thread per trajectory otherwise.
 cudaError_t launch_alg(int alg, LaunchCfg cfg, const KArgs& a, cudaStream_t s) {
   cfg.alg = alg;
+  if (cfg.model >= GBDE_MODEL_USER_BASE) return launch_rtc(cfg, a, s);
   if (cfg.model == GBDE_MODEL_VDP_RING8 &&
       (alg == GBDE_ALG_RODAS5 || alg == GBDE_ALG_RODAS5P ||
        (alg == GBDE_ALG_TSIT5 && cfg.tpt != 1)))
@@ -141,7 +142,9 @@ int gbde_model_info(int32_t model, int32_t* n_state, int32_t* n_param) {
     case GBDE_MODEL_ROBERTSON: ns = Robertson::N; np = Robertson::NP; break;
     case GBDE_MODEL_VDP_RING8: ns = VdpRing8::N; np = VdpRing8::NP; break;
     case GBDE_MODEL_LOTKA_VOLTERRA: ns = LotkaVolterra::N; np = LotkaVolterra::NP; break;
-    default: return set_err(nullptr, GBDE_ERR_INVALID, "unknown model id %d", model);
+    default:
+      if (rtc_model_info(model, &ns, &np)) break;
+      return set_err(nullptr, GBDE_ERR_INVALID, "unknown model id %d", model);
   }
   if (n_state) *n_state = ns;
   if (n_param) *n_param = np;
@@ -385,6 +388,17 @@ static int check_solve_args(gbde_ctx* ctx, const gbde_problem* prob, const gbde_
     return set_err(ctx, GBDE_ERR_UNSUPPORTED,
                    "Rosenbrock methods on the 16-state ring run as 16-lane teams only");
   if (opts->chunk < 0) return set_err(ctx, GBDE_ERR_INVALID, "chunk must be >= 0");
+  if (prob->model >= GBDE_MODEL_USER_BASE) {
+    // a user model: compile (once per algorithm and precision) and load its
+    // kernels now, before anything is enqueued or captured
+    if (alg == GBDE_ALG_AUTO || opts->learned)
+      return set_err(ctx, GBDE_ERR_UNSUPPORTED,
+                     "user models run without GBDE_ALG_AUTO and without the learned predictor");
+    std::string why;
+    GBDE_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int rc = rtc_prepare(prob->model, alg, opts->precision, &why);
+    if (rc != GBDE_OK) return set_err(ctx, rc, "%s", why.c_str());
+  }
   if (opts->block_size != 0 && (opts->block_size > 128 || opts->block_size < 32 ||
                                 (opts->block_size & 31)))
     return set_err(ctx, GBDE_ERR_INVALID, "block_size must be a multiple of 32 and <= 128");

@@ -1,8 +1,13 @@
 // common.cuh -- host/device helpers shared by every solver kernel.
 #pragma once
+// Under NVRTC (runtime-compiled user models, rtc.cu) there are no C library
+// headers: the runtime-compiled source defines the fixed-width integer types
+// itself, and the math functions are NVRTC built-ins.
+#ifndef __CUDACC_RTC__
 #include <stdint.h>
 #include <string.h>
 #include <math.h>
+#endif
 
 #if defined(__CUDACC__)
 #define GBDE_HD __host__ __device__ __forceinline__

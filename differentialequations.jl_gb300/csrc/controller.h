@@ -21,7 +21,9 @@
 //   2^y    = 2^k * exp(f ln 2),  k = rint(y), |f| <= 1/2 (Taylor series, degree 7).
 // Host code that includes this header must be compiled with -ffp-contract=off.
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <math.h>
+#endif
 #include "common.cuh"
 
 namespace gbde {

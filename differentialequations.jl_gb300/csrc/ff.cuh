@@ -16,7 +16,9 @@
 // TwoSum / Fast2Sum chains contain no products, so FMA contraction cannot
 // change them.
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <math.h>
+#endif
 
 #include "common.cuh"
 

@@ -2,6 +2,7 @@
 // translation units.  Not part of the public ABI.
 #pragma once
 #include <cuda_runtime.h>
+#include <string>
 #include "solver.cuh"
 
 namespace gbde {
@@ -80,6 +81,11 @@ cudaError_t launch_step_kernel(K kern, const LaunchCfg& cfg, const KArgs& a, cud
   b.dt_init = cfg.dt_init;
   return launch_kernel(kern, cfg, b, s);
 }
+
+// User models compiled at run time (rtc.cu): ids >= GBDE_MODEL_USER_BASE.
+bool rtc_model_info(int id, int32_t* n_state, int32_t* n_param);
+int rtc_prepare(int id, int alg, int precision, std::string* err);
+cudaError_t launch_rtc(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
 
 // Team kernels (team.cuh): 16 threads per trajectory.
 cudaError_t launch_team(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);

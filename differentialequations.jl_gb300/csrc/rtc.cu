@@ -1,0 +1,362 @@
+// rtc.cu -- user right-hand sides compiled at run time with NVRTC.
+//
+// The reference's problems take any Julia function f!(du, u, p, t)
+// (ODEFunction, test/qa/qa.jl:84); a precompiled kernel library can only
+// offer built-in models.  This file closes the gap: a caller registers the
+// body of f (and optionally of its Jacobian) as CUDA C++ source
+// (gbde_model_register), and the first solve of that model with a given
+// algorithm and precision compiles the library's own step kernels around it --
+// the same headers as the precompiled kernels (integrate_all, the steppers,
+// the controller, the dense output) -- with NVRTC for sm_103a, loads the cubin
+// as a context-independent library and launches it like a built-in kernel.
+// Without a user Jacobian, Rosenbrock methods differentiate f by forward-mode
+// dual numbers (dual.cuh), the counterpart of the reference's ForwardDiff
+// default (AutoForwardDiff, qa.jl:12).
+//
+// NVRTC is opened with dlopen at the first compile, so the library loads
+// (and every built-in model works) where NVRTC is absent.
+#include <dlfcn.h>
+#include <nvrtc.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/gbde.h"
+#include "launch.h"
+
+namespace gbde {
+int set_thread_error(int code, const char* msg);
+}
+
+using namespace gbde;
+
+namespace {
+
+// kRtcHeaders[]: {include name, text} of every header the runtime-compiled
+// source includes, embedded at build time (build.py writes rtc_headers.inc).
+struct RtcHeader {
+  const char* name;
+  const char* text;
+};
+#include "rtc_headers.inc"
+
+// ------------------------------------------------------------------ NVRTC
+struct Nvrtc {
+  bool ok = false;
+  std::string why;
+  nvrtcResult (*create)(nvrtcProgram*, const char*, const char*, int, const char* const*,
+                        const char* const*) = nullptr;
+  nvrtcResult (*compile)(nvrtcProgram, int, const char* const*) = nullptr;
+  nvrtcResult (*log_size)(nvrtcProgram, size_t*) = nullptr;
+  nvrtcResult (*log)(nvrtcProgram, char*) = nullptr;
+  nvrtcResult (*cubin_size)(nvrtcProgram, size_t*) = nullptr;
+  nvrtcResult (*cubin)(nvrtcProgram, char*) = nullptr;
+  nvrtcResult (*destroy)(nvrtcProgram*) = nullptr;
+  const char* (*err_str)(nvrtcResult) = nullptr;
+};
+
+Nvrtc load_nvrtc() {
+  Nvrtc n;
+  void* h = nullptr;
+  std::vector<std::string> names = {"libnvrtc.so.13", "libnvrtc.so"};
+  if (const char* home = std::getenv("CUDA_HOME")) {
+    names.push_back(std::string(home) + "/lib64/libnvrtc.so.13");
+    names.push_back(std::string(home) + "/lib64/libnvrtc.so");
+  }
+  for (const auto& nm : names)
+    if ((h = dlopen(nm.c_str(), RTLD_NOW | RTLD_LOCAL)) != nullptr) break;
+  if (!h) {
+    n.why = "NVRTC (libnvrtc.so.13) not found: user models need the CUDA toolkit's NVRTC";
+    return n;
+  }
+#define GBDE_SYM(field, name)                                            \
+  n.field = reinterpret_cast<decltype(n.field)>(dlsym(h, name));         \
+  if (!n.field) {                                                        \
+    n.why = std::string("NVRTC symbol ") + name + " missing";            \
+    return n;                                                            \
+  }
+  GBDE_SYM(create, "nvrtcCreateProgram")
+  GBDE_SYM(compile, "nvrtcCompileProgram")
+  GBDE_SYM(log_size, "nvrtcGetProgramLogSize")
+  GBDE_SYM(log, "nvrtcGetProgramLog")
+  GBDE_SYM(cubin_size, "nvrtcGetCUBINSize")
+  GBDE_SYM(cubin, "nvrtcGetCUBIN")
+  GBDE_SYM(destroy, "nvrtcDestroyProgram")
+  GBDE_SYM(err_str, "nvrtcGetErrorString")
+#undef GBDE_SYM
+  n.ok = true;
+  return n;
+}
+
+Nvrtc& nvrtc() {
+  static Nvrtc n = load_nvrtc();
+  return n;
+}
+
+// --------------------------------------------------------------- registry
+struct UserModelDef {
+  std::string name, f_body, jac_body;
+  int n, np;
+};
+
+struct Compiled {
+  std::vector<char> cubin;
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t step = nullptr, init = nullptr;
+};
+
+std::mutex g_mu;
+std::vector<UserModelDef> g_models;                       // id = GBDE_MODEL_USER_BASE + index
+std::map<std::tuple<int, int, int>, Compiled> g_compiled;  // (model, alg, precision)
+
+const UserModelDef* find_model(int id) {
+  const int k = id - GBDE_MODEL_USER_BASE;
+  return (k >= 0 && k < (int)g_models.size()) ? &g_models[k] : nullptr;
+}
+
+const char* prec_type(int precision) {
+  return precision == GBDE_PREC_MIXED ? "float" : (precision == GBDE_PREC_F32X2 ? "ff" : "double");
+}
+
+// The stepper type the precompiled dispatch (k_explicit.cu, k_rosenbrock.cu)
+// uses for this algorithm and precision.
+std::string alg_type(int alg, int precision) {
+  const std::string T = prec_type(precision);
+  switch (alg) {
+    case GBDE_ALG_TSIT5: return "Tsit5Alg<UserModel, " + T + ">";
+    case GBDE_ALG_VERN7: return "Vern7Alg<UserModel, " + T + ">";
+    case GBDE_ALG_ROSENBROCK23: return "Ros23Alg<UserModel, " + T + ">";
+    case GBDE_ALG_RODAS5:
+      return precision == GBDE_PREC_F32X2 ? "RodasFF<UserModel, Rodas5Tag>"
+                                          : "RodasAlg<UserModel, " + T + ", Rodas5Tag>";
+    case GBDE_ALG_RODAS5P:
+      return precision == GBDE_PREC_F32X2 ? "RodasFF<UserModel, Rodas5PTag>"
+                                          : "RodasAlg<UserModel, " + T + ", Rodas5PTag>";
+  }
+  return "";
+}
+
+// The runtime-compiled translation unit: fixed-width types (no C library
+// under NVRTC), the library's headers, the user model, and two extern "C"
+// kernels -- the step kernel and the initial-dt pre-pass -- instantiated as
+// the precompiled ones are.
+std::string make_source(const UserModelDef& m, int id, int alg, int precision) {
+  const bool mixed = precision != GBDE_PREC_FP64;
+  std::string s;
+  s += "typedef signed char int8_t; typedef short int16_t; typedef int int32_t;\n"
+       "typedef long long int64_t; typedef unsigned char uint8_t;\n"
+       "typedef unsigned short uint16_t; typedef unsigned int uint32_t;\n"
+       "typedef unsigned long long uint64_t; typedef unsigned long size_t;\n"
+       "#include \"solver.cuh\"\n#include \"explicit_rk.cuh\"\n#include \"rosenbrock.cuh\"\n"
+       "#include \"rodas_ff.cuh\"\n#include \"dual.cuh\"\n"
+       "namespace gbde {\nstruct UserModel {\n";
+  char buf[256];
+  std::snprintf(buf, sizeof(buf),
+                "  static constexpr int N = %d, NP = %d, ID = %d, F_FLOPS = 0;\n", m.n, m.np, id);
+  s += buf;
+  s += "  template <class T> __device__ static void f(T* du, const T* u, const T* p) {\n";
+  s += "#line 1 \"" + m.name + ":f\"\n";
+  s += m.f_body;
+  s += "\n  }\n  template <class T> __device__ static void jac(T (*J)[N], const T* u, const T* p) {\n";
+  if (m.jac_body.empty()) {
+    s += "    dual_jacobian<UserModel, T>(J, u, p);\n";
+  } else {
+    s += "#line 1 \"" + m.name + ":jac\"\n";
+    s += m.jac_body;
+    s += "\n";
+  }
+  s += "  }\n"
+       "  __device__ static void features(const double*, const double*, double, float* f) {\n"
+       "    for (int i = 0; i < 8; ++i) f[i] = 0.0f;\n  }\n};\n}  // namespace gbde\n"
+       "using namespace gbde;\n";
+  s += "typedef " + alg_type(alg, precision) + " GbdeRtcAlg;\n";
+  s += std::string("typedef ") + prec_type(precision) + " GbdeRtcT;\n";
+  s += "extern \"C\" __global__ void __launch_bounds__(128) gbde_rtc_step(const KArgs a) {\n"
+       "  integrate_all<GbdeRtcAlg, UserModel, GbdeRtcT, ";
+  s += mixed ? "true" : "false";
+  s += ">(a);\n}\n"
+       "extern \"C\" __global__ void __launch_bounds__(128) gbde_rtc_init_dt(const KArgs a, "
+       "double* out) {\n  init_dt_all<GbdeRtcAlg, UserModel, GbdeRtcT>(a, out);\n}\n";
+  return s;
+}
+
+int fail(int code, const std::string& msg) { return set_thread_error(code, msg.c_str()); }
+
+// NVRTC compile of one (model, algorithm, precision); g_mu held.
+int compile_locked(int id, int alg, int precision, Compiled** out) {
+  auto key = std::make_tuple(id, alg, precision);
+  auto it = g_compiled.find(key);
+  if (it != g_compiled.end()) {
+    *out = &it->second;
+    return GBDE_OK;
+  }
+  const UserModelDef* m = find_model(id);
+  if (!m) return fail(GBDE_ERR_INVALID, "unknown user model id " + std::to_string(id));
+  if (alg_type(alg, precision).empty())
+    return fail(GBDE_ERR_UNSUPPORTED,
+                "user models run Tsit5, Vern7, Rosenbrock23, Rodas5 and Rodas5P");
+  Nvrtc& nv = nvrtc();
+  if (!nv.ok) return fail(GBDE_ERR_UNSUPPORTED, nv.why);
+  const std::string src = make_source(*m, id, alg, precision);
+  std::vector<const char*> hnames, htexts;
+  for (const RtcHeader& h : kRtcHeaders) {
+    hnames.push_back(h.name);
+    htexts.push_back(h.text);
+  }
+  nvrtcProgram prog = nullptr;
+  nvrtcResult r = nv.create(&prog, src.c_str(), (m->name + ".cu").c_str(), (int)hnames.size(),
+                            htexts.data(), hnames.data());
+  if (r != NVRTC_SUCCESS) return fail(GBDE_ERR_INVALID, std::string("nvrtcCreateProgram: ") + nv.err_str(r));
+  const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17",
+                        "-default-device", "-lineinfo"};
+  r = nv.compile(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
+  if (r != NVRTC_SUCCESS) {
+    size_t n = 0;
+    nv.log_size(prog, &n);
+    std::string log(n, '\0');
+    if (n) nv.log(prog, &log[0]);
+    nv.destroy(&prog);
+    if (log.size() > 3000) log = log.substr(0, 3000) + "\n...";
+    return fail(GBDE_ERR_INVALID, "model '" + m->name + "' does not compile for " +
+                                      alg_type(alg, precision) + ":\n" + log);
+  }
+  size_t n = 0;
+  nv.cubin_size(prog, &n);
+  Compiled c;
+  c.cubin.resize(n);
+  nv.cubin(prog, c.cubin.data());
+  nv.destroy(&prog);
+  *out = &(g_compiled[key] = std::move(c));
+  return GBDE_OK;
+}
+
+}  // namespace
+
+namespace gbde {
+
+bool rtc_model_info(int id, int32_t* n_state, int32_t* n_param) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  const UserModelDef* m = find_model(id);
+  if (!m) return false;
+  if (n_state) *n_state = m->n;
+  if (n_param) *n_param = m->np;
+  return true;
+}
+
+// Compile (if not cached) and load the kernels of (model, alg, precision).
+// Called before any work is enqueued, so never inside a stream capture.
+int rtc_prepare(int id, int alg, int precision, std::string* err) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Compiled* c = nullptr;
+  int rc = compile_locked(id, alg, precision, &c);
+  if (rc != GBDE_OK) {
+    if (err) *err = gbde_last_error(nullptr);
+    return rc;
+  }
+  if (c->lib == nullptr) {
+    cudaError_t e = cudaLibraryLoadData(&c->lib, c->cubin.data(), nullptr, nullptr, 0, nullptr,
+                                        nullptr, 0);
+    if (e == cudaSuccess) e = cudaLibraryGetKernel(&c->step, c->lib, "gbde_rtc_step");
+    if (e == cudaSuccess) e = cudaLibraryGetKernel(&c->init, c->lib, "gbde_rtc_init_dt");
+    if (e != cudaSuccess) {
+      if (c->lib) cudaLibraryUnload(c->lib);
+      c->lib = nullptr;
+      if (err) *err = std::string("loading the compiled model failed: ") + cudaGetErrorString(e);
+      return GBDE_ERR_CUDA;
+    }
+  }
+  // load both kernels into the current device's context now (a library
+  // loads lazily on first use, which must not happen inside a stream capture)
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, (const void*)c->step);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)c->init);
+  if (e != cudaSuccess) {
+    if (err) *err = std::string("loading the compiled model failed: ") + cudaGetErrorString(e);
+    return GBDE_ERR_CUDA;
+  }
+  return GBDE_OK;
+}
+
+// Launch a prepared user-model solve: the initial-dt pre-pass when
+// cfg.dt_init is set, then the step kernel (plain or persistent geometry as
+// launch_kernel).
+cudaError_t launch_rtc(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
+  cudaKernel_t step = nullptr, init = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_compiled.find(std::make_tuple(cfg.model, cfg.alg, cfg.precision));
+    if (it == g_compiled.end() || it->second.lib == nullptr) return cudaErrorInvalidResourceHandle;
+    step = it->second.step;
+    init = it->second.init;
+  }
+  KArgs b = a;
+  if (cfg.dt_init != nullptr) {
+    const long long want = (a.N + 127) / 128, cap = 8LL * cfg.num_sms;
+    const int g = (int)(want < cap ? (want > 0 ? want : 1) : cap);
+    double* out = cfg.dt_init;
+    void* args[] = {(void*)&a, (void*)&out};
+    cudaError_t e = cudaLaunchKernel((const void*)init, dim3(g), dim3(128), args, 0, s);
+    if (e != cudaSuccess) return e;
+    b.dt_init = cfg.dt_init;
+  }
+  const int block = cfg.block > 0 ? cfg.block : 128;
+  int grid;
+  if (cfg.persistent) {
+    int per_sm = cfg.ctas_per_sm;
+    if (per_sm <= 0) {
+      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)step,
+                                                                    block, 0);
+      if (e != cudaSuccess) return e;
+      if (per_sm < 1) per_sm = 1;
+    }
+    grid = per_sm * cfg.num_sms;
+    const long long need = (b.N + block - 1) / block;
+    if (grid > need) grid = (int)(need > 0 ? need : 1);
+  } else {
+    const long long g = (b.N + block - 1) / block;
+    grid = (int)(g > 0 ? g : 1);
+  }
+  void* args[] = {(void*)&b};
+  return cudaLaunchKernel((const void*)step, dim3(grid), dim3(block), args, 0, s);
+}
+
+}  // namespace gbde
+
+extern "C" {
+
+int gbde_model_register(const gbde_user_model* def, int32_t* model_id) {
+  if (!def || !model_id || !def->f_body)
+    return fail(GBDE_ERR_INVALID, "def, def->f_body and model_id must be non-NULL");
+  if (def->n_state < 1 || def->n_state > GBDE_USER_MAX_STATE)
+    return fail(GBDE_ERR_INVALID, "user models have 1 to 8 states (one thread per trajectory)");
+  if (def->n_param < 1 || def->n_param > GBDE_USER_MAX_PARAM)
+    return fail(GBDE_ERR_INVALID, "user models have 1 to 32 parameters");
+  UserModelDef m;
+  m.name = def->name && def->name[0] ? def->name : "user_model";
+  for (char& ch : m.name)
+    if (!((ch >= 'a' && ch <= 'z') || (ch >= 'A' && ch <= 'Z') || (ch >= '0' && ch <= '9'))) ch = '_';
+  m.f_body = def->f_body;
+  m.jac_body = def->jac_body ? def->jac_body : "";
+  m.n = def->n_state;
+  m.np = def->n_param;
+  std::lock_guard<std::mutex> lk(g_mu);
+  *model_id = GBDE_MODEL_USER_BASE + (int32_t)g_models.size();
+  g_models.push_back(std::move(m));
+  return GBDE_OK;
+}
+
+int gbde_model_compile(int32_t model_id, int32_t alg, int32_t precision) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Compiled* c = nullptr;
+  return compile_locked(model_id, alg, precision, &c);
+}
+
+}  // extern "C"

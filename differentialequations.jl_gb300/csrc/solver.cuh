@@ -17,7 +17,6 @@
 // with the scaled RMS norm
 //     EEst = sqrt(mean_i (err_i / (abstol + reltol max(|u_i|, |unew_i|)))^2).
 #pragma once
-#include <cooperative_groups.h>
 #include "common.cuh"
 #include "controller.h"
 #include "models.cuh"
@@ -66,7 +65,8 @@ GBDE_D uint64_t global_ns() {
 // ----------------------------------------------------------- work source
 // Plain launch: each thread takes its own index once.  Persistent launch:
 // threads that need work take consecutive indices from a global counter
-// with one atomic per group of converged lanes (warp-aggregated).
+// with one atomic per group of converged lanes (warp-aggregated: the lowest
+// active lane adds for all of them and broadcasts the base).
 // With chunk c > 1 a thread takes c consecutive queue positions per fetch.
 struct WorkSource {
   int64_t first;
@@ -85,13 +85,15 @@ struct WorkSource {
       return a.order ? (int64_t)a.order[first] : first;
     }
     if (cur >= end) {
-      namespace cg = cooperative_groups;
       const unsigned long long c = a.chunk > 1 ? (unsigned long long)a.chunk : 1ull;
-      cg::coalesced_group g = cg::coalesced_threads();
+      const unsigned m = __activemask();
+      const int lane = (int)(threadIdx.x & 31u);
+      const int leader = __ffs((int)m) - 1;
+      const unsigned rank = (unsigned)__popc(m & ((1u << lane) - 1u));
       unsigned long long base = 0;
-      if (g.thread_rank() == 0) base = atomicAdd(a.queue, (unsigned long long)g.size() * c);
-      base = g.shfl(base, 0);
-      cur = base + g.thread_rank() * c;
+      if (lane == leader) base = atomicAdd(a.queue, (unsigned long long)__popc(m) * c);
+      base = __shfl_sync(m, base, leader);
+      cur = base + rank * c;
       end = cur + c;
     }
     const unsigned long long idx = cur++;
@@ -214,7 +216,7 @@ GBDE_D double initial_dt(const T* u0, const T* f0, const T* p, double tspan, int
 // each, all lanes converged.  Same loads, Alg::init and initial_dt as the
 // step kernel, so the step kernel starts from the identical value.
 template <class Alg, class M, class T>
-__global__ void __launch_bounds__(128) k_init_dt(const KArgs a, double* __restrict__ out) {
+__device__ void init_dt_all(const KArgs& a, double* __restrict__ out) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.N;
        i += (int64_t)gridDim.x * blockDim.x) {
     T p[M::NP], u0[M::N];
@@ -235,6 +237,10 @@ __global__ void __launch_bounds__(128) k_init_dt(const KArgs a, double* __restri
     }
     out[i] = dt;
   }
+}
+template <class Alg, class M, class T>
+__global__ void __launch_bounds__(128) k_init_dt(const KArgs a, double* __restrict__ out) {
+  init_dt_all<Alg, M, T>(a, out);
 }
 
 // ------------------------------------------------------------- driver

@@ -35,8 +35,10 @@
 #ifndef GBDE_H
 #define GBDE_H
 
+#ifndef __CUDACC_RTC__ /* runtime-compiled device code (rtc.cu) defines these types */
 #include <stddef.h>
 #include <stdint.h>
+#endif
 
 #ifdef __cplusplus
 extern "C" {
@@ -77,6 +79,10 @@ extern "C" {
 #define GBDE_MODEL_LOTKA_VOLTERRA 5 /* n=2, p=[alpha,beta,gamma,delta,sigma]:
                                        drift [a x - b x y, d x y - g y],
                                        diagonal noise sigma*u (SDE)            */
+/* User models (gbde_model_register) get ids from GBDE_MODEL_USER_BASE up. */
+#define GBDE_MODEL_USER_BASE 1000
+#define GBDE_USER_MAX_STATE 8
+#define GBDE_USER_MAX_PARAM 32
 
 /* ---- algorithms ------------------------------------------------------- */
 #define GBDE_ALG_TSIT5 1        /* Tsitouras 5(4), FSAL, free 4th-order interpolant */
@@ -349,6 +355,41 @@ GBDE_API int gbde_mlp_grad(gbde_ctx* ctx, const float* net, const float* x, cons
                   int64_t n, float* grad, float* loss);
 /* Make `net` (host) the network that learned solves of `model` use. */
 GBDE_API int gbde_mlp_load(gbde_ctx* ctx, int32_t model, const float* net);
+
+/* ---- user right-hand sides, compiled at run time ------------------------
+ * Replaces passing a Julia function to ODEFunction (ODEFunction, qa.jl:84;
+ * the problem's f!(du, u, p, t), test/core.jl:22-31,39-46).  f_body is the body
+ * of a CUDA C++ function template
+ *     template <class T> void f(T* du, const T* u, const T* p)
+ * that fills du[0..n_state) from u and the parameters p (autonomous: a
+ * time-dependent system carries t as an extra state with dt/dt = 1).  T is
+ * double, float (GBDE_PREC_MIXED) or the FP32-pair type (GBDE_PREC_F32X2,
+ * which has +, - and * only).  jac_body, if not NULL, is the body of
+ *     template <class T> void jac(T (*J)[n_state], const T* u, const T* p)
+ * filling J[r][c] = d du_r / d u_c; if NULL, Rosenbrock methods take the
+ * Jacobian from forward-mode dual numbers over f_body (the reference's
+ * AutoForwardDiff default, qa.jl:12), which also needs T(x) constructions and
+ * the operators +, -, *, / and exp, log, sqrt, sin, cos, tanh, fabs, pow.
+ * The first solve (or gbde_model_compile) of a model with an algorithm and a
+ * precision compiles the library's step kernels around f with NVRTC for
+ * sm_103a (seconds); later solves reuse the cached cubin.  User models run
+ * Tsit5, Vern7, Rosenbrock23, Rodas5 and Rodas5P, one thread per trajectory,
+ * in every batching mode; not GBDE_ALG_AUTO, SDE methods or learned=1.     */
+typedef struct {
+  const char* name;     /* label used in compile messages (may be NULL)    */
+  int32_t n_state;      /* 1 .. GBDE_USER_MAX_STATE                        */
+  int32_t n_param;      /* 1 .. GBDE_USER_MAX_PARAM                        */
+  const char* f_body;   /* CUDA C++ statements: du[i] = ... (required)     */
+  const char* jac_body; /* CUDA C++ statements: J[r][c] = ..., or NULL     */
+} gbde_user_model;
+
+/* Register a user model; *model_id receives its id (>= GBDE_MODEL_USER_BASE).
+ * Source is copied; nothing is compiled yet.  Process-wide, thread-safe. */
+GBDE_API int gbde_model_register(const gbde_user_model* def, int32_t* model_id);
+/* Compile (and cache) a user model's kernels for one algorithm and precision
+ * without a GPU; GBDE_ERR_INVALID with NVRTC's log in gbde_last_error(NULL)
+ * when the source does not compile, GBDE_ERR_UNSUPPORTED without NVRTC. */
+GBDE_API int gbde_model_compile(int32_t model_id, int32_t alg, int32_t precision);
 
 /* Self-check (no counterpart in the reference): the largest relative
  * difference, over n pseudo-random x with |x| in [2^-60, 2^61), between the
