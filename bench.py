@@ -67,6 +67,11 @@ def parse():
                     help="chosen form: persistent-f32x2 | persistent-f32x2-learned | plain-f32x2 | "
                          "persistent | plain | "
                          "persistent-mixed | plain-mixed")
+    ap.add_argument("--user-model", default="none", choices=["none", "analytic", "dual"],
+                    help="solve through a user right-hand side compiled at run time (the "
+                         "Robertson formulas as source; Jacobian given or by dual numbers) "
+                         "instead of the built-in model; chosen forms without the learned "
+                         "predictor")
     ap.add_argument("--cpu-sample", type=int, default=100000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="robertson",
@@ -529,6 +534,20 @@ def main():
         o.learned = forms[form][2] if len(forms[form]) > 2 else 0
         return o
 
+    solve_model = de.models.robertson
+    if args.user_model != "none":
+        # the same Robertson formulas (test/core.jl:39-45) as runtime-compiled user source
+        solve_model = de.ODEFunction(
+            "T r1 = p[0] * u[0]; T r2 = p[1] * u[1] * u[1]; T r3 = p[2] * u[1] * u[2];\n"
+            "du[0] = -r1 + r3; du[1] = r1 - r2 - r3; du[2] = r2;", 3, 3,
+            jac=None if args.user_model == "dual" else
+            "J[0][0] = -p[0]; J[0][1] = p[2] * u[2]; J[0][2] = p[2] * u[1];\n"
+            "J[1][0] = p[0]; J[1][1] = T(-2) * p[1] * u[1] - p[2] * u[2];\n"
+            "J[1][2] = -p[2] * u[1]; J[2][0] = T(0); J[2][1] = T(2) * p[1] * u[1];\n"
+            "J[2][2] = T(0);", name="robertson_user")
+        if len(forms[args.chosen]) > 2:
+            raise SystemExit("bench: user models run without the learned predictor; "
+                             "pick --chosen persistent-f32x2")
     learn_info = None
     if len(forms[args.chosen]) > 2:
         # the learned queue order: train the cost head on the attempted-step
@@ -567,7 +586,7 @@ def main():
                        saveat[idx], capi.SAVE_PER_TRAJ, nthreads=oracle.hardware_threads())
     stats = {}
     for form in ("plain", args.chosen):
-        r = de.solve_arrays(de.models.robertson, opts_for(form), *dptr, capi.SAVE_PER_TRAJ,
+        r = de.solve_arrays(solve_model, opts_for(form), *dptr, capi.SAVE_PER_TRAJ,
                             u_dtype=out_dtype(form))
         torch.cuda.synchronize()
         u = r["u"].double().cpu().numpy()
@@ -589,7 +608,7 @@ def main():
                                  device=dev),
                 "retcode": torch.empty(N, dtype=torch.int32, device=dev)}
         for _ in range(W):
-            de.solve_arrays(de.models.robertson, o, *dptr, capi.SAVE_PER_TRAJ,
+            de.solve_arrays(solve_model, o, *dptr, capi.SAVE_PER_TRAJ,
                             u_dtype=out_dtype(form), out=outs)
         tot, kern = 0.0, 0.0
         per = step_log.setdefault(form, [])
@@ -601,7 +620,7 @@ def main():
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            r = de.solve_arrays(de.models.robertson, o, *dptr, capi.SAVE_PER_TRAJ,
+            r = de.solve_arrays(solve_model, o, *dptr, capi.SAVE_PER_TRAJ,
                                 u_dtype=out_dtype(form), out=outs)
             e1.record(stream)
             torch.cuda.synchronize()
@@ -621,7 +640,7 @@ def main():
                                  ).pin_memory().numpy(),
                 "retcode": torch.empty(N, dtype=torch.int32).pin_memory().numpy()}
         for _ in range(W):
-            de.solve_arrays(de.models.robertson, o, *hp, capi.SAVE_PER_TRAJ,
+            de.solve_arrays(solve_model, o, *hp, capi.SAVE_PER_TRAJ,
                             u_dtype=out_dtype(form), out=outs)
         if world > 1:
             dist.barrier()
@@ -631,7 +650,7 @@ def main():
             flush.zero_()
             torch.cuda.synchronize()
             t = time.perf_counter()
-            de.solve_arrays(de.models.robertson, o, *hp, capi.SAVE_PER_TRAJ,
+            de.solve_arrays(solve_model, o, *hp, capi.SAVE_PER_TRAJ,
                             u_dtype=out_dtype(form), out=outs)
             ts.append(time.perf_counter() - t)
             step_log.setdefault("e2e", []).append(ts[-1] * 1e3)
@@ -698,6 +717,7 @@ def main():
                        parallelism="trajectory shards, no collective" if world > 1 else "single GPU"),
         "chosen_form": args.chosen,
         "learned": learn_info,
+        "user_model": args.user_model,
         "plain": {"value": total / (plain_ms * 1e-3), "ms_per_step": plain_ms,
                   "kernel_ms": plain_kern, "error_vs_oracle": errs["plain"]},
         "speedup_vs_plain": plain_ms / chosen_ms,
