@@ -86,6 +86,14 @@ class TuneEntry(C.Structure):
                 ("chunk", C.c_int32), ("threads_per_traj", C.c_int32), ("device_ms", C.c_float)]
 
 
+SUMMARY_MAX_Q = 8
+
+
+class Summary(C.Structure):
+    _fields_ = [("n_quantiles", C.c_int32), ("quantiles", C.c_double * SUMMARY_MAX_Q),
+                ("mean", C.c_void_p), ("var", C.c_void_p), ("qvals", C.c_void_p)]
+
+
 class UserModel(C.Structure):
     _fields_ = [("name", C.c_char_p), ("n_state", C.c_int32), ("n_param", C.c_int32),
                 ("f_body", C.c_char_p), ("jac_body", C.c_char_p)]
@@ -121,6 +129,8 @@ SIGNATURES = {
                                     C.POINTER(Outputs), C.POINTER(C.c_void_p)]),
     "gbde_graph_launch": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "gbde_graph_destroy": (C.c_int, [C.c_void_p]),
+    "gbde_ensemble_summary": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int64,
+                                        C.c_int32, C.c_int32, C.POINTER(Summary)]),
     "gbde_model_register": (C.c_int, [C.POINTER(UserModel), C.POINTER(C.c_int32)]),
     "gbde_model_compile": (C.c_int, [C.c_int32, C.c_int32, C.c_int32]),
     "gbde_autotune": (C.c_int, [C.c_void_p, C.POINTER(Problem), C.POINTER(Opts),

@@ -317,6 +317,73 @@ class EnsembleSolution:
         return bool(np.all(self.retcode == capi.RET_SUCCESS))
 
 
+# ------------------------------------------------------ ensemble statistics
+def ensemble_summary(u, quantiles=(), device=0):
+    """Mean, variance (N - 1) and quantiles across trajectories of
+    u[N][n_save][n_state], computed on the GPU (gbde_ensemble_summary).
+    u: a CUDA tensor (statistics stay on its device and come back as CUDA
+    tensors) or a host array (staged).  Returns (mean, var, qvals) with
+    qvals[j] for quantiles[j]."""
+    import ctypes as C
+    q = [float(x) for x in quantiles]
+    if len(q) > capi.SUMMARY_MAX_Q:
+        raise ValueError("at most %d quantiles" % capi.SUMMARY_MAX_Q)
+    if u.ndim != 3:
+        raise ValueError("u must be [N][n_save][n_state]")
+    N, ns, nst = (int(x) for x in u.shape)
+    sm = capi.Summary()
+    sm.n_quantiles = len(q)
+    for j, v in enumerate(q):
+        sm.quantiles[j] = v
+    on_device = not isinstance(u, np.ndarray)
+    if on_device:
+        import torch
+        if u.dtype not in (torch.float32, torch.float64):
+            raise TypeError("u must be float32 or float64")
+        u = u.contiguous()
+        mean = torch.empty((ns, nst), dtype=torch.float64, device=u.device)
+        var = torch.empty_like(mean)
+        qv = torch.empty((max(len(q), 1), ns, nst), dtype=torch.float64, device=u.device)
+        ctx = capi.context(u.device.index or 0)
+        ctx.set_stream(torch.cuda.current_stream(u.device).cuda_stream)
+        dt = capi.F32 if u.dtype == torch.float32 else capi.F64
+        mem = capi.MEM_DEVICE
+    else:
+        if u.dtype not in (np.float32, np.float64):
+            u = u.astype(np.float64)
+        u = np.ascontiguousarray(u)
+        mean = np.empty((ns, nst))
+        var = np.empty((ns, nst))
+        qv = np.empty((max(len(q), 1), ns, nst))
+        ctx = capi.context(device)
+        ctx.set_stream(0)
+        dt = capi.F32 if u.dtype == np.float32 else capi.F64
+        mem = capi.MEM_HOST
+    sm.mean, sm.var = capi.ptr(mean), capi.ptr(var)
+    sm.qvals = capi.ptr(qv) if q else None
+    capi.check(capi.lib().gbde_ensemble_summary(ctx.handle, capi.ptr(u), dt, mem, N, ns, nst,
+                                                C.byref(sm)), ctx.handle)
+    return mean, var, qv[:len(q)]
+
+
+class EnsembleSummary:
+    """EnsembleSummary (qa.jl:54) of an ensemble solution at its save times:
+    `t`, `u` (mean), `v` (variance), `med`, `qlow`, `qhigh` as
+    [n_save][n_state] arrays, computed on the GPU.  Like the reference, the
+    statistics are taken per time point across trajectories; with per-
+    trajectory save times they are per save index."""
+
+    def __init__(self, sim, quantiles=(0.05, 0.95), device=0):
+        U = sim.U if isinstance(sim, EnsembleSolution) else sim
+        mean, var, qv = ensemble_summary(U, (0.5, float(quantiles[0]), float(quantiles[1])),
+                                         device)
+        self.t = sim.t if isinstance(sim, EnsembleSolution) else None
+        self.u, self.v = mean, var
+        self.med, self.qlow, self.qhigh = qv[0], qv[1], qv[2]
+        self.num_monte = int(U.shape[0])
+        self.converged = bool(sim.converged) if isinstance(sim, EnsembleSolution) else None
+
+
 # ----------------------------------------------------------- save times
 def _dec(x):
     """Exact rational of the shortest decimal that round-trips x (so that

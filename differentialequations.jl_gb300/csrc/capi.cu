@@ -73,6 +73,7 @@ struct gbde_ctx {
   Scratch scratch;    // device scratch of ensemble solves (queue, order, lists, predictions)
   DevBuf dt1;         // staging of the first-accepted-step log (host calls)
   DevBuf mlp_net;     // learned predictor (GBDE_MLP_NET_FLOATS floats)
+  DevBuf summary, summary_io;  // gbde_ensemble_summary: scratch; staged outputs (host mode)
   int mlp_model = 0;  // model the loaded predictor belongs to (0 = none)
 };
 
@@ -184,7 +185,7 @@ int gbde_ctx_destroy(gbde_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf* b : {&ctx->p, &ctx->u0, &ctx->t0, &ctx->tf, &ctx->saveat, &ctx->u, &ctx->ret,
                     &ctx->nacc, &ctx->nrej, &ctx->nf, &ctx->tend, &ctx->method, &ctx->dt1,
-                    &ctx->mlp_net})
+                    &ctx->mlp_net, &ctx->summary, &ctx->summary_io})
     b->release();
   ctx->scratch.release();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -769,6 +770,59 @@ int gbde_autotune(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts* opts
   if (best_i < 0) return set_err(ctx, GBDE_ERR_INVALID, "no launch configuration ran");
   *best = cand[best_i];
   return gbde_ensemble_solve(ctx, prob, best, out);
+}
+
+int gbde_ensemble_summary(gbde_ctx* ctx, const void* u, int32_t u_dtype, int32_t mem,
+                          int64_t n_traj, int32_t n_save, int32_t n_state, gbde_summary* out) {
+  if (!ctx || !out) return set_err(ctx, GBDE_ERR_INVALID, "ctx and out must be non-NULL");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (n_traj < 1 || n_save < 1 || n_state < 1 || !u)
+    return set_err(ctx, GBDE_ERR_INVALID, "need u, n_traj >= 1, n_save >= 1, n_state >= 1");
+  if (u_dtype != GBDE_F64 && u_dtype != GBDE_F32)
+    return set_err(ctx, GBDE_ERR_INVALID, "u_dtype must be GBDE_F64 or GBDE_F32");
+  if (mem != GBDE_MEM_HOST && mem != GBDE_MEM_DEVICE)
+    return set_err(ctx, GBDE_ERR_INVALID, "mem must be GBDE_MEM_HOST or GBDE_MEM_DEVICE");
+  const int nq = out->n_quantiles;
+  if (nq < 0 || nq > GBDE_SUMMARY_MAX_Q)
+    return set_err(ctx, GBDE_ERR_INVALID, "n_quantiles must be in [0, %d]", GBDE_SUMMARY_MAX_Q);
+  for (int j = 0; j < nq; ++j)
+    if (!(out->quantiles[j] >= 0.0 && out->quantiles[j] <= 1.0))
+      return set_err(ctx, GBDE_ERR_INVALID, "quantiles must lie in [0, 1]");
+  const int64_t C64 = (int64_t)n_save * n_state;
+  if (C64 > 65535) return set_err(ctx, GBDE_ERR_UNSUPPORTED, "n_save * n_state must be <= 65535");
+  const int C = (int)C64;
+  const int f32 = u_dtype == GBDE_F32;
+  const size_t ubytes = (size_t)n_traj * C * (f32 ? 4 : 8);
+  GBDE_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const int qn = out->qvals ? nq : 0;
+  GBDE_CUDA(ctx, ctx->summary.ensure(
+                     summary_scratch_bytes(n_traj, C, f32, qn, summary_sum_blocks(C, ctx->num_sms))));
+  const void* ud = u;
+  double *mean = out->mean, *var = out->var, *qv = out->qvals;
+  if (mem == GBDE_MEM_HOST) {
+    GBDE_CUDA(ctx, ctx->u.ensure(ubytes));
+    GBDE_CUDA(ctx, cudaMemcpyAsync(ctx->u.ptr, u, ubytes, cudaMemcpyHostToDevice, s));
+    ud = ctx->u.ptr;
+    GBDE_CUDA(ctx, ctx->summary_io.ensure((size_t)C * (2 + nq) * sizeof(double)));
+    double* io = (double*)ctx->summary_io.ptr;
+    mean = out->mean ? io : nullptr;
+    var = out->var ? io + C : nullptr;
+    qv = out->qvals ? io + 2 * C : nullptr;
+  }
+  GBDE_CUDA(ctx, enqueue_summary(ud, f32, n_traj, C, qn, out->quantiles, mean, var, qv,
+                                 ctx->summary.ptr, ctx->num_sms, s));
+  if (mem == GBDE_MEM_HOST) {
+    if (out->mean)
+      GBDE_CUDA(ctx, cudaMemcpyAsync(out->mean, mean, C * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (out->var)
+      GBDE_CUDA(ctx, cudaMemcpyAsync(out->var, var, C * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (out->qvals && nq)
+      GBDE_CUDA(ctx, cudaMemcpyAsync(out->qvals, qv, (size_t)nq * C * sizeof(double),
+                                     cudaMemcpyDeviceToHost, s));
+  }
+  GBDE_CUDA(ctx, cudaStreamSynchronize(s));
+  return GBDE_OK;
 }
 
 int gbde_mlp_load(gbde_ctx* ctx, int32_t model, const float* net) {

@@ -87,6 +87,13 @@ bool rtc_model_info(int id, int32_t* n_state, int32_t* n_param);
 int rtc_prepare(int id, int alg, int precision, std::string* err);
 cudaError_t launch_rtc(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
 
+// Ensemble statistics over u[N][C] in device memory (summary.cu).
+int summary_sum_blocks(int C, int num_sms);
+size_t summary_scratch_bytes(int64_t N, int C, int u_f32, int nq, int sum_blocks);
+cudaError_t enqueue_summary(const void* u, int u_f32, int64_t N, int C, int nq,
+                            const double* q_host, double* mean, double* var, double* qv,
+                            void* scratch, int num_sms, cudaStream_t s);
+
 // Team kernels (team.cuh): 16 threads per trajectory.
 cudaError_t launch_team(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
 

@@ -356,6 +356,30 @@ GBDE_API int gbde_mlp_grad(gbde_ctx* ctx, const float* net, const float* x, cons
 /* Make `net` (host) the network that learned solves of `model` use. */
 GBDE_API int gbde_mlp_load(gbde_ctx* ctx, int32_t model, const float* net);
 
+/* ---- ensemble statistics on the device -----------------------------------
+ * Replaces EnsembleSummary / EnsembleAnalysis (timepoint_meanvar,
+ * timepoint_quantile; qa.jl:54,211): per save point and state component,
+ * across the N trajectories of u[N][n_save][n_state] (a solve's output),
+ *   mean, variance (N - 1 in the denominator; NaN for N = 1) and the
+ *   quantiles q_j by linear interpolation between order statistics
+ *   ((N-1) q_j, the default of Julia's Statistics.quantile and numpy).
+ * A column holding a NaN (the unreached save slots of a failed trajectory)
+ * gives NaN statistics.  Quantiles are exact (radix selection on the
+ * values' bits).  mem = GBDE_MEM_DEVICE: u and the outputs are device memory
+ * of the context's device, and the kernels run on its stream;
+ * GBDE_MEM_HOST: host memory, staged by the call.  Outputs may be NULL. */
+#define GBDE_SUMMARY_MAX_Q 8
+typedef struct {
+  int32_t n_quantiles;                     /* 0 .. GBDE_SUMMARY_MAX_Q     */
+  double quantiles[GBDE_SUMMARY_MAX_Q];    /* each in [0, 1]              */
+  double* mean;                            /* [n_save][n_state] or NULL   */
+  double* var;                             /* [n_save][n_state] or NULL   */
+  double* qvals;                           /* [n_quantiles][n_save][n_state] or NULL */
+} gbde_summary;
+GBDE_API int gbde_ensemble_summary(gbde_ctx* ctx, const void* u, int32_t u_dtype, int32_t mem,
+                                   int64_t n_traj, int32_t n_save, int32_t n_state,
+                                   gbde_summary* out);
+
 /* ---- user right-hand sides, compiled at run time ------------------------
  * Replaces passing a Julia function to ODEFunction (ODEFunction, qa.jl:84;
  * the problem's f!(du, u, p, t), test/core.jl:22-31,39-46).  f_body is the body
