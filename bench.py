@@ -75,7 +75,7 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=100000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="robertson",
-                    choices=["robertson", "lorenz", "lv_em", "lv_sosri", "vdp_auto",
+                    choices=["robertson", "lorenz", "lv_em", "lv_sosri", "vdp_auto", "summary",
                              "learned_lorenz", "learned_lv", "learned_vdp"],
                     help="robertson = the headline (default); the others print the line of "
                          "another configuration")
@@ -454,6 +454,92 @@ def run_learned(args, de):
     print(json.dumps(line))
 
 
+def hbm_peak():
+    """Measured HBM copy bandwidth (GB/s) of the GB300s, else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback 6.8 TB/s"
+
+
+def run_summary(args, de):
+    """Ensemble statistics on the device: mean, variance and the 5 / 50 / 95 %
+    quantiles per save point and component of a 1M x 21 x 16 FP32 ensemble
+    output (the 16-state ring's output size; seeded normal values), against
+    copying that output to the host and computing the same with numpy."""
+    import torch
+    capi = de._capi
+    N, ns, nst = args.trajectories, 21, 16
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev).manual_seed(SEED)
+    u = torch.randn((N, ns, nst), generator=g, device=dev, dtype=torch.float32)
+    u.mul_(torch.linspace(0.1, 3.0, nst, device=dev)).add_(torch.linspace(-1, 1, ns, device=dev)[:, None])
+    qs = (0.05, 0.5, 0.95)
+    mean, var, qv = de.ensemble_summary(u, qs)  # correctness and warm-up
+    ref_mean = u.double().mean(0)
+    ok = bool(torch.allclose(mean, ref_mean, rtol=1e-9, atol=1e-9)) and bool(
+        torch.equal(de.ensemble_summary(u, (0.0,))[2][0], u.amin(0).double()))
+    if not ok:
+        raise SystemExit("bench: device summary disagrees with torch's reductions")
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+
+    def timed(fn, K, W):
+        for _ in range(W):
+            fn()
+        ts = []
+        for _ in range(K):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.mean(ts)), ts
+
+    with ClockSampler(0) as clk:
+        full_ms, full_ts = timed(lambda: de.ensemble_summary(u, qs), args.steps, args.warmup)
+        mv_ms, _ = timed(lambda: de.ensemble_summary(u, ()), args.steps, args.warmup)
+    # the alternative: copy the ensemble to pinned host memory, reduce with numpy
+    host = torch.empty((N, ns, nst), dtype=torch.float32).pin_memory()
+    t = time.perf_counter()
+    host.copy_(u)
+    torch.cuda.synchronize()
+    d2h_ms = (time.perf_counter() - t) * 1e3
+    hn = host.numpy()
+    t = time.perf_counter()
+    hn.mean(0)
+    hn.var(0, ddof=1)
+    np.quantile(hn, qs, axis=0)
+    cpu_ms = (time.perf_counter() - t) * 1e3
+    ubytes = N * ns * nst * 4
+    peak, src = hbm_peak()
+    achieved = ubytes / (mv_ms * 1e-3) / 1e9
+    line = {"metric": "ensemble statistics: trajectories summarised per second",
+            "value": N / (full_ms * 1e-3), "unit": "trajectories/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": full_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded normal values in the ring's output shape)",
+            "config": {"workload": "summary_N%d_21x16_f32" % N, "quantiles": list(qs),
+                       "l2": "flushed between timed steps (256 MB write)"},
+            "mean_var_only_ms": mv_ms,
+            "roofline": {"bound": "hbm", "kernel": "mean/var pass (k_sum)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": src,
+                         "algorithmic_bytes": ubytes},
+            "quantile_passes": "1 key transpose (read + write) + 4 digit passes over the keys",
+            "alternative": {"d2h_ms": d2h_ms, "numpy_ms_1_thread": cpu_ms,
+                            "what": "copy u to pinned host memory, numpy mean/var/quantile"},
+            "speedup_vs_alternative": (d2h_ms + cpu_ms) / full_ms,
+            "gpu_launches": args.steps * (2 + 1 + 1 + 4 * 3 + 1),
+            "clocks": clk.summary(),
+            "step_ms_spread": {"min": min(full_ts), "median": float(np.median(full_ts)),
+                               "max": max(full_ts)}}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
@@ -468,6 +554,8 @@ def main():
             args.trajectories = {"lorenz": 10000}.get(args.workload, 1000000)
         if args.workload.startswith("learned_"):
             return run_learned(args, de)
+        if args.workload == "summary":
+            return run_summary(args, de)
         return run_other(args, de)
     alg_id = capi.ALG_RODAS5 if args.alg == "rodas5" else capi.ALG_ROSENBROCK23
     config = {"workload": "robertson_%s_fp64_N%d" % (args.alg, args.trajectories),
