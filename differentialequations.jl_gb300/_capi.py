@@ -23,7 +23,7 @@ GBDE_ERR_NOMEM = -5
 GBDE_ERR_STATE = -6
 
 RET_DEFAULT, RET_SUCCESS, RET_MAXITERS, RET_DTLESSTHANMIN, RET_UNSTABLE = 0, 1, 2, 3, 4
-RET_INITIALFAILURE, RET_TIMEOUT = 5, 6
+RET_INITIALFAILURE, RET_TIMEOUT, RET_TERMINATED = 5, 6, 7
 
 MODEL_LINEAR, MODEL_LORENZ, MODEL_ROBERTSON, MODEL_VDP_RING8, MODEL_LOTKA_VOLTERRA = 1, 2, 3, 4, 5
 MODEL_USER_BASE, USER_MAX_STATE, USER_MAX_PARAM = 1000, 8, 32
@@ -59,7 +59,7 @@ class Opts(C.Structure):
         ("seed", C.c_uint64), ("learned", C.c_int32), ("block_size", C.c_int32),
         ("chunk", C.c_int32), ("ctas_per_sm", C.c_int32),
         ("stiff_threshold", C.c_double), ("timeout_s", C.c_double),
-        ("threads_per_traj", C.c_int32), ("reserved_", C.c_int32),
+        ("threads_per_traj", C.c_int32), ("callback", C.c_int32),
     ]
 
 
@@ -92,6 +92,14 @@ SUMMARY_MAX_Q = 8
 class Summary(C.Structure):
     _fields_ = [("n_quantiles", C.c_int32), ("quantiles", C.c_double * SUMMARY_MAX_Q),
                 ("mean", C.c_void_p), ("var", C.c_void_p), ("qvals", C.c_void_p)]
+
+
+CB_CONTINUOUS, CB_DISCRETE = 1, 2
+
+
+class Callback(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("condition", C.c_char_p), ("affect", C.c_char_p),
+                ("terminate", C.c_int32)]
 
 
 class UserModel(C.Structure):
@@ -133,6 +141,8 @@ SIGNATURES = {
                                         C.c_int32, C.c_int32, C.POINTER(Summary)]),
     "gbde_model_register": (C.c_int, [C.POINTER(UserModel), C.POINTER(C.c_int32)]),
     "gbde_model_compile": (C.c_int, [C.c_int32, C.c_int32, C.c_int32]),
+    "gbde_callback_register": (C.c_int, [C.POINTER(Callback), C.POINTER(C.c_int32)]),
+    "gbde_callback_compile": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "gbde_autotune": (C.c_int, [C.c_void_p, C.POINTER(Problem), C.POINTER(Opts),
                                 C.POINTER(Outputs), C.c_int32, C.POINTER(Opts),
                                 C.POINTER(TuneEntry), C.c_int32, C.POINTER(C.c_int32)]),

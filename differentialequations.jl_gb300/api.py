@@ -13,8 +13,10 @@ Semantics kept from the reference's pinned tests (test/core.jl):
   * the first stored state equals u0 exactly (core.jl:34);
   * remake(prob; u0=...) changes u0 (core.jl:81-88);
   * a Robertson solve with Rodas5P to t=1e5 returns Success (core.jl:38-49).
-Unsupported solve keywords (callback, dense=True, save_everystep=True) raise
-instead of silently changing behaviour.
+Callbacks (ContinuousCallback / DiscreteCallback, core.jl:60-79) take their
+condition and affect as CUDA C++ source compiled into the kernels.
+Unsupported solve keywords (dense=True, save_everystep=True, tstops,
+save_idxs) raise instead of silently changing behaviour.
 """
 import copy
 import enum
@@ -34,6 +36,7 @@ class ReturnCode(enum.IntEnum):
     Unstable = capi.RET_UNSTABLE
     InitialFailure = capi.RET_INITIALFAILURE
     Timeout = capi.RET_TIMEOUT
+    Terminated = capi.RET_TERMINATED
 
 
 # ---------------------------------------------------------------- models
@@ -93,6 +96,40 @@ def compile_model(model, alg, precision="fp64"):
     the first solve (no GPU needed); raises GBDEError with NVRTC's log."""
     prec = {"fp64": capi.PREC_FP64, "mixed": capi.PREC_MIXED, "f32x2": capi.PREC_F32X2}[precision]
     capi.check(capi.lib().gbde_model_compile(model.id, alg.alg_id, prec))
+
+
+class _Callback:
+    def __init__(self, kind, condition, affect, terminate):
+        import ctypes as C
+        d = capi.Callback(kind=kind, condition=condition.encode(),
+                          affect=affect.encode() if affect else None,
+                          terminate=int(bool(terminate)))
+        cid = C.c_int32()
+        capi.check(capi.lib().gbde_callback_register(C.byref(d), C.byref(cid)))
+        self.id, self.kind = cid.value, kind
+        self.condition, self.affect, self.terminate = condition, affect, terminate
+
+
+class ContinuousCallback(_Callback):
+    """ContinuousCallback(condition, affect=None; terminate=False) (qa.jl:24).
+
+    condition: CUDA C++ statements setting `g` (double) from `u` (the state,
+    const double*), `t` and `p`; an event is a sign change of g, located on
+    the method's dense output, where the trajectory stops (left of the root),
+    runs affect (statements modifying `u[i]`, may set `terminate = true`) and
+    restarts.  Example: ContinuousCallback("g = t - 0.5;")."""
+
+    def __init__(self, condition, affect=None, terminate=False):
+        super().__init__(capi.CB_CONTINUOUS, condition, affect, terminate)
+
+
+class DiscreteCallback(_Callback):
+    """DiscreteCallback(condition, affect=None; terminate=False) (qa.jl:36):
+    after every accepted step, g != 0 runs affect.
+    Example: DiscreteCallback("g = t >= 0.5;")."""
+
+    def __init__(self, condition, affect=None, terminate=False):
+        super().__init__(capi.CB_DISCRETE, condition, affect, terminate)
 
 
 # -------------------------------------------------------------- problems
@@ -422,7 +459,7 @@ def save_grid(t0, tf, saveat, save_start=None, save_end=None):
 
 
 # ----------------------------------------------------------------- solve
-_UNSUPPORTED = ("callback", "dense", "save_everystep", "tstops", "save_idxs")
+_UNSUPPORTED = ("dense", "save_everystep", "tstops", "save_idxs")
 
 
 def _gather_inputs(ens, N):
@@ -469,7 +506,8 @@ def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start
         if k in kwargs and kwargs[k] not in (None, False):
             raise NotImplementedError("solve keyword %r is not supported by EnsembleGB300" % k)
     extra = set(kwargs) - set(_UNSUPPORTED) - {"qmin", "qmax", "gamma", "beta1", "beta2",
-                                               "qsteady_min", "qsteady_max", "qoldinit"}
+                                               "qsteady_min", "qsteady_max", "qoldinit",
+                                               "callback"}
     if extra:
         raise TypeError("unknown solve keywords: %s" % sorted(extra))
     single = not isinstance(ens, EnsembleProblem)
@@ -552,6 +590,11 @@ def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start
             setattr(opts, k, float(kwargs[k]))
     opts.seed = int(seed)
     opts.learned = ensemblealg.learned_flags
+    cb = kwargs.get("callback")
+    if cb is not None:
+        if not isinstance(cb, _Callback):
+            raise TypeError("callback must be a ContinuousCallback or a DiscreteCallback")
+        opts.callback = cb.id
     opts.block_size = int(ensemblealg.block_size)
     opts.ctas_per_sm = int(ensemblealg.ctas_per_sm)
     opts.chunk = int(ensemblealg.chunk)
@@ -560,6 +603,11 @@ def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start
     res = solve_arrays(prob.f, opts, p, u0, t0, tf, save_arr, save_kind,
                        u_dtype=ensemblealg.out_dtype, device=ensemblealg.device)
     t_out = save_arr
+    term = res["retcode"] == capi.RET_TERMINATED
+    if np.any(term):
+        # a terminated trajectory ends at its event: keep the saves up to t_end
+        ts = t_out if t_out.ndim == 2 else np.broadcast_to(t_out, (N, t_out.shape[-1]))
+        lengths = np.where(term, np.sum(ts <= res["t_end"][:, None], axis=1), lengths)
     sol = EnsembleSolution(res["u"], t_out, res["retcode"], lengths,
                            {k: res[k] for k in ("naccept", "nreject", "nf", "t_end")},
                            res["total_ms"], res["device_ms"], probs=probs)

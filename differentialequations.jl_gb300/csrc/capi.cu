@@ -108,7 +108,7 @@ int set_thread_error(int code, const char* msg) {
 // one thread per trajectory otherwise.
 cudaError_t launch_alg(int alg, LaunchCfg cfg, const KArgs& a, cudaStream_t s) {
   cfg.alg = alg;
-  if (cfg.model >= GBDE_MODEL_USER_BASE) return launch_rtc(cfg, a, s);
+  if (cfg.model >= GBDE_MODEL_USER_BASE || cfg.callback) return launch_rtc(cfg, a, s);
   if (cfg.model == GBDE_MODEL_VDP_RING8 &&
       (alg == GBDE_ALG_RODAS5 || alg == GBDE_ALG_RODAS5P ||
        (alg == GBDE_ALG_TSIT5 && cfg.tpt != 1)))
@@ -389,15 +389,19 @@ static int check_solve_args(gbde_ctx* ctx, const gbde_problem* prob, const gbde_
     return set_err(ctx, GBDE_ERR_UNSUPPORTED,
                    "Rosenbrock methods on the 16-state ring run as 16-lane teams only");
   if (opts->chunk < 0) return set_err(ctx, GBDE_ERR_INVALID, "chunk must be >= 0");
-  if (prob->model >= GBDE_MODEL_USER_BASE) {
-    // a user model: compile (once per algorithm and precision) and load its
-    // kernels now, before anything is enqueued or captured
-    if (alg == GBDE_ALG_AUTO || opts->learned)
+  if (prob->model >= GBDE_MODEL_USER_BASE || opts->callback != 0) {
+    // a user model or a callback: compile (once per model, algorithm,
+    // precision and callback) and load the kernels now, before anything is
+    // enqueued or captured
+    if (alg == GBDE_ALG_AUTO || is_sde_alg(alg) || opts->learned)
       return set_err(ctx, GBDE_ERR_UNSUPPORTED,
-                     "user models run without GBDE_ALG_AUTO and without the learned predictor");
+                     "user models and callbacks run the one-thread ODE methods, without "
+                     "GBDE_ALG_AUTO and without the learned predictor");
+    if (prob->model == GBDE_MODEL_VDP_RING8)
+      return set_err(ctx, GBDE_ERR_UNSUPPORTED, "callbacks are not built for the 16-lane ring");
     std::string why;
     GBDE_CUDA(ctx, cudaSetDevice(ctx->device));
-    const int rc = rtc_prepare(prob->model, alg, opts->precision, &why);
+    const int rc = rtc_prepare(prob->model, alg, opts->precision, opts->callback, &why);
     if (rc != GBDE_OK) return set_err(ctx, rc, "%s", why.c_str());
   }
   if (opts->block_size != 0 && (opts->block_size > 128 || opts->block_size < 32 ||
@@ -465,6 +469,7 @@ static LaunchCfg make_cfg(const gbde_ctx* ctx, const gbde_problem* prob, const g
   cfg.ctas_per_sm = opts->ctas_per_sm;
   cfg.num_sms = ctx->num_sms;
   cfg.tpt = opts->threads_per_traj;
+  cfg.callback = opts->callback;
   return cfg;
 }
 

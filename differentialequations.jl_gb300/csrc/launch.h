@@ -16,6 +16,7 @@ struct LaunchCfg {
   int num_sms;
   int tpt = 0;        // threads per trajectory (0 = model default, 1, 16)
   double* dt_init = nullptr;  // scratch [N]: run the initial-dt pre-pass into it
+  int callback = 0;   // gbde_callback_register id (runtime-compiled kernels)
 };
 
 // Returns cudaSuccess, or cudaErrorNotSupported for an unknown combination.
@@ -84,7 +85,7 @@ cudaError_t launch_step_kernel(K kern, const LaunchCfg& cfg, const KArgs& a, cud
 
 // User models compiled at run time (rtc.cu): ids >= GBDE_MODEL_USER_BASE.
 bool rtc_model_info(int id, int32_t* n_state, int32_t* n_param);
-int rtc_prepare(int id, int alg, int precision, std::string* err);
+int rtc_prepare(int id, int alg, int precision, int callback, std::string* err);
 cudaError_t launch_rtc(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
 
 // Ensemble statistics over u[N][C] in device memory (summary.cu).

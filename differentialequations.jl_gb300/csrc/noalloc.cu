@@ -157,6 +157,8 @@ extern "C" int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_
   if (opts->maxiters <= 0) return fail(GBDE_ERR_INVALID, "maxiters must be > 0");
   if (opts->adaptive && !(opts->qmin > 0.0 && opts->qmax >= 1.0 && opts->gamma > 0.0))
     return fail(GBDE_ERR_INVALID, "controller needs qmin > 0, qmax >= 1, gamma > 0");
+  if (opts->callback != 0)
+    return fail(GBDE_ERR_UNSUPPORTED, "gbde_ensemble_solve_noalloc runs no callbacks");
   if (opts->learned)
     return fail(GBDE_ERR_STATE, "gbde_ensemble_solve_noalloc has no learned predictor (learned != 0)");
   if (alg == GBDE_ALG_ROSENBROCK23 && prob->model == GBDE_MODEL_VDP_RING8)

@@ -107,15 +107,38 @@ struct UserModelDef {
   int n, np;
 };
 
+struct CallbackDef {
+  int kind;
+  std::string condition, affect;
+};
+
 struct Compiled {
   std::vector<char> cubin;
   cudaLibrary_t lib = nullptr;
   cudaKernel_t step = nullptr, init = nullptr;
 };
 
+using Key = std::tuple<int, int, int, int>;  // (model, alg, precision, callback)
+
 std::mutex g_mu;
-std::vector<UserModelDef> g_models;                       // id = GBDE_MODEL_USER_BASE + index
-std::map<std::tuple<int, int, int>, Compiled> g_compiled;  // (model, alg, precision)
+std::vector<UserModelDef> g_models;        // id = GBDE_MODEL_USER_BASE + index
+std::vector<CallbackDef> g_callbacks;      // id = index + 1
+std::map<Key, Compiled> g_compiled;
+
+const CallbackDef* find_callback(int id) {
+  return (id >= 1 && id <= (int)g_callbacks.size()) ? &g_callbacks[id - 1] : nullptr;
+}
+
+// Built-in models a runtime-compiled kernel (with a callback) can use.
+const char* builtin_model(int id) {
+  switch (id) {
+    case GBDE_MODEL_LINEAR: return "Linear";
+    case GBDE_MODEL_LORENZ: return "Lorenz";
+    case GBDE_MODEL_ROBERTSON: return "Robertson";
+    case GBDE_MODEL_LOTKA_VOLTERRA: return "LotkaVolterra";
+  }
+  return nullptr;
+}
 
 const UserModelDef* find_model(int id) {
   const int k = id - GBDE_MODEL_USER_BASE;
@@ -131,24 +154,26 @@ const char* prec_type(int precision) {
 std::string alg_type(int alg, int precision) {
   const std::string T = prec_type(precision);
   switch (alg) {
-    case GBDE_ALG_TSIT5: return "Tsit5Alg<UserModel, " + T + ">";
-    case GBDE_ALG_VERN7: return "Vern7Alg<UserModel, " + T + ">";
-    case GBDE_ALG_ROSENBROCK23: return "Ros23Alg<UserModel, " + T + ">";
+    case GBDE_ALG_TSIT5: return "Tsit5Alg<GbdeRtcModel, " + T + ">";
+    case GBDE_ALG_VERN7: return "Vern7Alg<GbdeRtcModel, " + T + ">";
+    case GBDE_ALG_ROSENBROCK23: return "Ros23Alg<GbdeRtcModel, " + T + ">";
     case GBDE_ALG_RODAS5:
-      return precision == GBDE_PREC_F32X2 ? "RodasFF<UserModel, Rodas5Tag>"
-                                          : "RodasAlg<UserModel, " + T + ", Rodas5Tag>";
+      return precision == GBDE_PREC_F32X2 ? "RodasFF<GbdeRtcModel, Rodas5Tag>"
+                                          : "RodasAlg<GbdeRtcModel, " + T + ", Rodas5Tag>";
     case GBDE_ALG_RODAS5P:
-      return precision == GBDE_PREC_F32X2 ? "RodasFF<UserModel, Rodas5PTag>"
-                                          : "RodasAlg<UserModel, " + T + ", Rodas5PTag>";
+      return precision == GBDE_PREC_F32X2 ? "RodasFF<GbdeRtcModel, Rodas5PTag>"
+                                          : "RodasAlg<GbdeRtcModel, " + T + ", Rodas5PTag>";
   }
   return "";
 }
 
 // The runtime-compiled translation unit: fixed-width types (no C library
-// under NVRTC), the library's headers, the user model, and two extern "C"
-// kernels -- the step kernel and the initial-dt pre-pass -- instantiated as
-// the precompiled ones are.
-std::string make_source(const UserModelDef& m, int id, int alg, int precision) {
+// under NVRTC), the library's headers, the model (the user's, or a built-in
+// one when only the callback is user source), the callback, and two
+// extern "C" kernels -- the step kernel and the initial-dt pre-pass --
+// instantiated as the precompiled ones are.
+std::string make_source(const UserModelDef* m, int model, const CallbackDef* cb, int alg,
+                        int precision) {
   const bool mixed = precision != GBDE_PREC_FP64;
   std::string s;
   s += "typedef signed char int8_t; typedef short int16_t; typedef int int32_t;\n"
@@ -156,63 +181,91 @@ std::string make_source(const UserModelDef& m, int id, int alg, int precision) {
        "typedef unsigned short uint16_t; typedef unsigned int uint32_t;\n"
        "typedef unsigned long long uint64_t; typedef unsigned long size_t;\n"
        "#include \"solver.cuh\"\n#include \"explicit_rk.cuh\"\n#include \"rosenbrock.cuh\"\n"
-       "#include \"rodas_ff.cuh\"\n#include \"dual.cuh\"\n"
-       "namespace gbde {\nstruct UserModel {\n";
+       "#include \"rodas_ff.cuh\"\n#include \"dual.cuh\"\nnamespace gbde {\n";
   char buf[256];
-  std::snprintf(buf, sizeof(buf),
-                "  static constexpr int N = %d, NP = %d, ID = %d, F_FLOPS = 0;\n", m.n, m.np, id);
-  s += buf;
-  s += "  template <class T> __device__ static void f(T* du, const T* u, const T* p) {\n";
-  s += "#line 1 \"" + m.name + ":f\"\n";
-  s += m.f_body;
-  s += "\n  }\n  template <class T> __device__ static void jac(T (*J)[N], const T* u, const T* p) {\n";
-  if (m.jac_body.empty()) {
-    s += "    dual_jacobian<UserModel, T>(J, u, p);\n";
+  if (m) {
+    s += "struct UserModel {\n";
+    std::snprintf(buf, sizeof(buf),
+                  "  static constexpr int N = %d, NP = %d, ID = %d, F_FLOPS = 0;\n", m->n, m->np,
+                  model);
+    s += buf;
+    s += "  template <class T> __device__ static void f(T* du, const T* u, const T* p) {\n";
+    s += "#line 1 \"" + m->name + ":f\"\n";
+    s += m->f_body;
+    s += "\n  }\n  template <class T> __device__ static void jac(T (*J)[N], const T* u, const T* p) {\n";
+    if (m->jac_body.empty()) {
+      s += "    dual_jacobian<UserModel, T>(J, u, p);\n";
+    } else {
+      s += "#line 1 \"" + m->name + ":jac\"\n";
+      s += m->jac_body;
+      s += "\n";
+    }
+    s += "  }\n"
+         "  __device__ static void features(const double*, const double*, double, float* f) {\n"
+         "    for (int i = 0; i < 8; ++i) f[i] = 0.0f;\n  }\n};\n"
+         "typedef UserModel GbdeRtcModel;\n";
   } else {
-    s += "#line 1 \"" + m.name + ":jac\"\n";
-    s += m.jac_body;
-    s += "\n";
+    s += std::string("typedef ") + builtin_model(model) + " GbdeRtcModel;\n";
   }
-  s += "  }\n"
-       "  __device__ static void features(const double*, const double*, double, float* f) {\n"
-       "    for (int i = 0; i < 8; ++i) f[i] = 0.0f;\n  }\n};\n}  // namespace gbde\n"
-       "using namespace gbde;\n";
+  if (cb) {
+    std::snprintf(buf, sizeof(buf), "struct UserCallback {\n  static constexpr int KIND = %d;\n",
+                  cb->kind);
+    s += buf;
+    s += "  __device__ static double condition(const double* u, double t, const double* p) {\n"
+         "    double g = 0.0;\n#line 1 \"callback:condition\"\n";
+    s += cb->condition;
+    s += "\n    return g;\n  }\n"
+         "  __device__ static void affect(double* u, double t, const double* p, bool& terminate) {\n"
+         "#line 1 \"callback:affect\"\n";
+    s += cb->affect;
+    s += "\n  }\n};\ntypedef UserCallback GbdeRtcCallback;\n";
+  } else {
+    s += "typedef NoCallback GbdeRtcCallback;\n";
+  }
+  s += "}  // namespace gbde\nusing namespace gbde;\n";
   s += "typedef " + alg_type(alg, precision) + " GbdeRtcAlg;\n";
   s += std::string("typedef ") + prec_type(precision) + " GbdeRtcT;\n";
   s += "extern \"C\" __global__ void __launch_bounds__(128) gbde_rtc_step(const KArgs a) {\n"
-       "  integrate_all<GbdeRtcAlg, UserModel, GbdeRtcT, ";
+       "  integrate_all<GbdeRtcAlg, GbdeRtcModel, GbdeRtcT, ";
   s += mixed ? "true" : "false";
-  s += ">(a);\n}\n"
+  s += ", GbdeRtcCallback>(a);\n}\n"
        "extern \"C\" __global__ void __launch_bounds__(128) gbde_rtc_init_dt(const KArgs a, "
-       "double* out) {\n  init_dt_all<GbdeRtcAlg, UserModel, GbdeRtcT>(a, out);\n}\n";
+       "double* out) {\n  init_dt_all<GbdeRtcAlg, GbdeRtcModel, GbdeRtcT>(a, out);\n}\n";
   return s;
 }
 
 int fail(int code, const std::string& msg) { return set_thread_error(code, msg.c_str()); }
 
-// NVRTC compile of one (model, algorithm, precision); g_mu held.
-int compile_locked(int id, int alg, int precision, Compiled** out) {
-  auto key = std::make_tuple(id, alg, precision);
+// NVRTC compile of one (model, algorithm, precision, callback); g_mu held.
+int compile_locked(int id, int alg, int precision, int callback, Compiled** out) {
+  const Key key = std::make_tuple(id, alg, precision, callback);
   auto it = g_compiled.find(key);
   if (it != g_compiled.end()) {
     *out = &it->second;
     return GBDE_OK;
   }
   const UserModelDef* m = find_model(id);
-  if (!m) return fail(GBDE_ERR_INVALID, "unknown user model id " + std::to_string(id));
+  if (!m && !builtin_model(id))
+    return fail(GBDE_ERR_INVALID, "model " + std::to_string(id) +
+                                      " cannot be compiled at run time (unknown user model, or a "
+                                      "built-in model without one-thread kernels)");
+  const CallbackDef* cb = nullptr;
+  if (callback != 0 && !(cb = find_callback(callback)))
+    return fail(GBDE_ERR_INVALID, "unknown callback id " + std::to_string(callback));
   if (alg_type(alg, precision).empty())
     return fail(GBDE_ERR_UNSUPPORTED,
-                "user models run Tsit5, Vern7, Rosenbrock23, Rodas5 and Rodas5P");
+                "runtime-compiled kernels run Tsit5, Vern7, Rosenbrock23, Rodas5 and Rodas5P");
   Nvrtc& nv = nvrtc();
   if (!nv.ok) return fail(GBDE_ERR_UNSUPPORTED, nv.why);
-  const std::string src = make_source(*m, id, alg, precision);
+  const std::string src = make_source(m, id, cb, alg, precision);
+  const std::string label = m ? m->name : std::string(builtin_model(id));
   std::vector<const char*> hnames, htexts;
   for (const RtcHeader& h : kRtcHeaders) {
     hnames.push_back(h.name);
     htexts.push_back(h.text);
   }
   nvrtcProgram prog = nullptr;
-  nvrtcResult r = nv.create(&prog, src.c_str(), (m->name + ".cu").c_str(), (int)hnames.size(),
+  nvrtcResult r = nv.create(&prog, src.c_str(), (label + ".cu").c_str(), (int)hnames.size(),
                             htexts.data(), hnames.data());
   if (r != NVRTC_SUCCESS) return fail(GBDE_ERR_INVALID, std::string("nvrtcCreateProgram: ") + nv.err_str(r));
   const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17",
@@ -225,8 +278,9 @@ int compile_locked(int id, int alg, int precision, Compiled** out) {
     if (n) nv.log(prog, &log[0]);
     nv.destroy(&prog);
     if (log.size() > 3000) log = log.substr(0, 3000) + "\n...";
-    return fail(GBDE_ERR_INVALID, "model '" + m->name + "' does not compile for " +
-                                      alg_type(alg, precision) + ":\n" + log);
+    return fail(GBDE_ERR_INVALID, "model '" + label + "'" + (cb ? " with its callback" : "") +
+                                      " does not compile for " + alg_type(alg, precision) +
+                                      ":\n" + log);
   }
   size_t n = 0;
   nv.cubin_size(prog, &n);
@@ -253,10 +307,10 @@ bool rtc_model_info(int id, int32_t* n_state, int32_t* n_param) {
 
 // Compile (if not cached) and load the kernels of (model, alg, precision).
 // Called before any work is enqueued, so never inside a stream capture.
-int rtc_prepare(int id, int alg, int precision, std::string* err) {
+int rtc_prepare(int id, int alg, int precision, int callback, std::string* err) {
   std::lock_guard<std::mutex> lk(g_mu);
   Compiled* c = nullptr;
-  int rc = compile_locked(id, alg, precision, &c);
+  int rc = compile_locked(id, alg, precision, callback, &c);
   if (rc != GBDE_OK) {
     if (err) *err = gbde_last_error(nullptr);
     return rc;
@@ -292,7 +346,7 @@ cudaError_t launch_rtc(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
   cudaKernel_t step = nullptr, init = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_mu);
-    auto it = g_compiled.find(std::make_tuple(cfg.model, cfg.alg, cfg.precision));
+    auto it = g_compiled.find(std::make_tuple(cfg.model, cfg.alg, cfg.precision, cfg.callback));
     if (it == g_compiled.end() || it->second.lib == nullptr) return cudaErrorInvalidResourceHandle;
     step = it->second.step;
     init = it->second.init;
@@ -356,7 +410,29 @@ int gbde_model_register(const gbde_user_model* def, int32_t* model_id) {
 int gbde_model_compile(int32_t model_id, int32_t alg, int32_t precision) {
   std::lock_guard<std::mutex> lk(g_mu);
   Compiled* c = nullptr;
-  return compile_locked(model_id, alg, precision, &c);
+  return compile_locked(model_id, alg, precision, 0, &c);
+}
+
+int gbde_callback_register(const gbde_callback* def, int32_t* callback_id) {
+  if (!def || !callback_id || !def->condition)
+    return fail(GBDE_ERR_INVALID, "def, def->condition and callback_id must be non-NULL");
+  if (def->kind != GBDE_CB_CONTINUOUS && def->kind != GBDE_CB_DISCRETE)
+    return fail(GBDE_ERR_INVALID, "kind must be GBDE_CB_CONTINUOUS or GBDE_CB_DISCRETE");
+  CallbackDef c;
+  c.kind = def->kind;
+  c.condition = def->condition;
+  c.affect = def->affect ? def->affect : "";
+  if (def->terminate) c.affect += "\nterminate = true;";
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_callbacks.push_back(std::move(c));
+  *callback_id = (int32_t)g_callbacks.size();
+  return GBDE_OK;
+}
+
+int gbde_callback_compile(int32_t model, int32_t alg, int32_t precision, int32_t callback_id) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Compiled* c = nullptr;
+  return compile_locked(model, alg, precision, callback_id, &c);
 }
 
 }  // extern "C"

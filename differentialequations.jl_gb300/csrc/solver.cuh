@@ -243,6 +243,57 @@ __global__ void __launch_bounds__(128) k_init_dt(const KArgs a, double* __restri
   init_dt_all<Alg, M, T>(a, out);
 }
 
+// ----------------------------------------------------------- callbacks
+// Event handling of the reference's ContinuousCallback / DiscreteCallback
+// (qa.jl:24,36; exercised by test/core.jl:60-79).  The precompiled kernels use
+// NoCallback and compile none of it.  A callback type (runtime-compiled from
+// user source, rtc.cu) provides
+//   static constexpr int KIND;   GBDE_CB_CONTINUOUS or GBDE_CB_DISCRETE
+//   static double condition(const double* u, double t, const double* p);
+//   static void affect(double* u, double t, const double* p, bool& terminate);
+// on FP64 copies of the state and parameters, whatever the precision.
+// Continuous: a sign change of condition over an accepted step is located on
+// the method's dense output by Illinois regula falsi; the integrator moves to
+// the left side of the root (the reference's LeftRootFind default), applies
+// affect and restarts the method there.  Save points up to the event use the
+// step's dense output.  The next step looks for crossings only after 1% of
+// its length (the reference's repeat_nudge), so a root is not found twice.
+// Discrete: condition != 0 after an accepted step applies affect.
+struct NoCallback {
+  static constexpr int KIND = 0;
+  GBDE_D static double condition(const double*, double, const double*) { return 0.0; }
+  GBDE_D static void affect(double*, double, const double*, bool&) {}
+};
+
+template <class CB, int N, int NP, class T>
+GBDE_D double cb_condition(const T* u, double t, const T* p) {
+  double ud[N], pd[NP];
+#pragma unroll
+  for (int c = 0; c < N; ++c) ud[c] = (double)u[c];
+#pragma unroll
+  for (int k = 0; k < NP; ++k) pd[k] = (double)p[k];
+  return CB::condition(ud, t, pd);
+}
+
+// affect on an FP64 copy of u; returns terminate
+template <class CB, int N, int NP, class T>
+GBDE_D bool cb_affect(T* u, double t, const T* p) {
+  double ud[N], pd[NP];
+#pragma unroll
+  for (int c = 0; c < N; ++c) ud[c] = (double)u[c];
+#pragma unroll
+  for (int k = 0; k < NP; ++k) pd[k] = (double)p[k];
+  bool term = false;
+  CB::affect(ud, t, pd, term);
+#pragma unroll
+  for (int c = 0; c < N; ++c) u[c] = (T)ud[c];
+  return term;
+}
+
+GBDE_D bool cb_crossed(double g0, double g1) {
+  return (g0 < 0.0 && g1 >= 0.0) || (g0 > 0.0 && g1 <= 0.0);
+}
+
 // ------------------------------------------------------------- driver
 // Alg provides:  static constexpr int ORDER (for beta defaults / init dt),
 //   void init(const T* u0, const T* p, int& nf)       -- u = u0, f(u) cache
@@ -252,9 +303,11 @@ __global__ void __launch_bounds__(128) k_init_dt(const KArgs a, double* __restri
 //                                                       -- dense output
 //   void accept(const T* p, int& nf)                    -- u = unew, caches
 //   const T* u() / unew() / f0()
-template <class Alg, class M, class T, bool MIXED>
+template <class Alg, class M, class T, bool MIXED, class CB = NoCallback>
 __device__ void integrate_all(const KArgs& a) {
   constexpr int N = M::N;
+  double gprev = 0.0;     // continuous callback: condition at the current point
+  bool nudge = false;     // an event ended the previous step (repeat nudge)
   WorkSource src;
   src.init();
   Alg alg;
@@ -313,6 +366,10 @@ __device__ void integrate_all(const KArgs& a) {
         if (a.dtmax > 0.0) dt = fmin(dt, a.dtmax);
         if (!(t < tf)) ret = GBDE_RET_SUCCESS;
         else if (!(dt > 0.0)) ret = GBDE_RET_DTLESSTHANMIN;
+        if constexpr (CB::KIND == GBDE_CB_CONTINUOUS) {
+          gprev = cb_condition<CB, N, M::NP>(alg.u(), t, p);
+          nudge = false;
+        }
       }
       active = true;
     }
@@ -335,6 +392,7 @@ __device__ void integrate_all(const KArgs& a) {
         double dtnew = h;
         if (a.adaptive) dtnew = h * f2d_bits(ctl_accept(a.ctl, ms, lqold));
         // time update (compensated in the mixed-precision path)
+        const double tlo0 = tlo;
         double tnew;
         if (last) {
           tnew = tf;
@@ -352,13 +410,63 @@ __device__ void integrate_all(const KArgs& a) {
         } else {
           tnew = t + h;
         }
-        // saveat: dense output at every save time in (t, tnew]
-        const uint64_t tnew_o = ord_bits(tnew);
+        // continuous callback: a crossing of the condition in (t, tnew]
+        // (after the repeat nudge when the previous step ended at an event)
+        bool event = false;
+        double th_e = 1.0;
+        if constexpr (CB::KIND == GBDE_CB_CONTINUOUS) {
+          double ga = gprev, lo = 0.0;
+          if (nudge) {
+            T un[N];
+            lo = 0.01;
+            alg.interp(lo, h, un, p, nfev);
+            ga = cb_condition<CB, N, M::NP>(un, t + lo * h, p);
+            nudge = false;
+          }
+          const double gb = cb_condition<CB, N, M::NP>(alg.unew(), tnew, p);
+          if (cb_crossed(ga, gb)) {
+            // Illinois regula falsi on theta in [lo, 1]; the left end keeps
+            // the sign before the crossing
+            double a0 = lo, b0 = 1.0, fa = ga, fb = gb;
+            int side = 0;
+            for (int it = 0; it < 100; ++it) {
+              if ((b0 - a0) * fabs(h) <= 8.9e-16 * fmax(fabs(t), fabs(tnew))) break;
+              double m = b0 - fb * (b0 - a0) / (fb - fa);
+              if (!(m > a0 && m < b0)) m = 0.5 * (a0 + b0);
+              T um[N];
+              alg.interp(m, h, um, p, nfev);
+              const double fm = cb_condition<CB, N, M::NP>(um, t + m * h, p);
+              if (fm == 0.0) {
+                a0 = m;
+                break;
+              }
+              if (cb_crossed(fa, fm)) {  // root in (a0, m]
+                b0 = m;
+                fb = fm;
+                if (side == -1) fa *= 0.5;
+                side = -1;
+              } else {
+                a0 = m;
+                fa = fm;
+                if (side == 1) fb *= 0.5;
+                side = 1;
+              }
+            }
+            th_e = a0;
+            event = true;
+          } else {
+            gprev = gb;
+          }
+        }
+        // saveat: dense output at every save time in (t, tnew], or up to the
+        // event
+        const double te = event ? t + (tlo0 + th_e * h) : tnew;
+        const uint64_t tnew_o = ord_bits(tnew), lim_o = ord_bits(te);
         while (js < a.n_save) {
           const double ts = save_time(a, i, js);
           const uint64_t ts_o = ord_bits(ts);
-          if (ts_o > tnew_o) break;
-          if (ts_o == tnew_o) {
+          if (ts_o > lim_o) break;
+          if (!event && ts_o == tnew_o) {
             store_state<N>(a, i, js, alg.unew());
           } else {
             T tmp[N];
@@ -367,16 +475,45 @@ __device__ void integrate_all(const KArgs& a) {
           }
           ++js;
         }
-        alg.accept(p, nfev);
-        t = tnew;
-        if (nacc == 0) dt1 = h;
-        ++nacc;
-        bool fin = true;
+        if (event) {
+          // move to the event, apply affect, restart the method there
+          T ue[N];
+          alg.interp(th_e, h, ue, p, nfev);
+          const bool term = cb_affect<CB, N, M::NP>(ue, te, p);
+          alg.init(ue, p, nfev);
+          t = te;
+          tlo = 0.0;
+          nudge = true;
+          if (nacc == 0) dt1 = th_e * h;
+          ++nacc;
+          bool fin = true;
 #pragma unroll
-        for (int c = 0; c < N; ++c) fin &= val_finite(alg.u()[c]);
-        if (!fin) ret = GBDE_RET_UNSTABLE;
-        else if (last) ret = GBDE_RET_SUCCESS;
-        dt = a.dtmax > 0.0 && ord_bits(dtnew) > ord_bits(a.dtmax) ? a.dtmax : dtnew;
+          for (int c = 0; c < N; ++c) fin &= val_finite(alg.u()[c]);
+          if (!fin) ret = GBDE_RET_UNSTABLE;
+          else if (term) ret = GBDE_RET_TERMINATED;
+          dt = a.dtmax > 0.0 && ord_bits(dtnew) > ord_bits(a.dtmax) ? a.dtmax : dtnew;
+        } else {
+          alg.accept(p, nfev);
+          t = tnew;
+          if (nacc == 0) dt1 = h;
+          ++nacc;
+          bool fin = true;
+#pragma unroll
+          for (int c = 0; c < N; ++c) fin &= val_finite(alg.u()[c]);
+          if (!fin) ret = GBDE_RET_UNSTABLE;
+          else if (last) ret = GBDE_RET_SUCCESS;
+          if constexpr (CB::KIND == GBDE_CB_DISCRETE) {
+            if (fin && cb_condition<CB, N, M::NP>(alg.u(), t, p) != 0.0) {
+              T uc[N];
+#pragma unroll
+              for (int c = 0; c < N; ++c) uc[c] = alg.u()[c];
+              const bool term = cb_affect<CB, N, M::NP>(uc, t, p);
+              alg.init(uc, p, nfev);
+              if (term) ret = GBDE_RET_TERMINATED;
+            }
+          }
+          dt = a.dtmax > 0.0 && ord_bits(dtnew) > ord_bits(a.dtmax) ? a.dtmax : dtnew;
+        }
       } else {
         ++nrej;
         dt = h * f2d_bits(ctl_reject(a.ctl, ms));

@@ -69,6 +69,11 @@ extern "C" {
 #define GBDE_RET_UNSTABLE 4       /* ReturnCode.Unstable (non-finite state)*/
 #define GBDE_RET_INITIALFAILURE 5 /* ReturnCode.InitialFailure (bad input) */
 #define GBDE_RET_TIMEOUT 6        /* device deadline hit (no Julia analog) */
+#define GBDE_RET_TERMINATED 7     /* ReturnCode.Terminated (a callback ended it) */
+
+/* callback kinds (gbde_callback.kind) */
+#define GBDE_CB_CONTINUOUS 1      /* ContinuousCallback (qa.jl:24)         */
+#define GBDE_CB_DISCRETE 2        /* DiscreteCallback (qa.jl:36)           */
 
 /* ---- built-in right-hand sides (ODEFunction f!(du,u,p,t), qa.jl:84) ---- */
 #define GBDE_MODEL_LINEAR 1    /* n=1, p=[a]:           du = a*u (test/core.jl:10) */
@@ -178,7 +183,7 @@ typedef struct {
   double timeout_s;    /* device deadline per call (0 = none)             */
   int32_t threads_per_traj; /* 0 = model default; 1 = one thread per trajectory;
                           16 = a 16-lane team (16-state models)            */
-  int32_t reserved_;   /* zero                                            */
+  int32_t callback;    /* 0, or an id from gbde_callback_register          */
 } gbde_opts;
 
 /* Results.  u is [N][n_save][n_state] of u_dtype; retcode [N]; the step
@@ -414,6 +419,37 @@ GBDE_API int gbde_model_register(const gbde_user_model* def, int32_t* model_id);
  * without a GPU; GBDE_ERR_INVALID with NVRTC's log in gbde_last_error(NULL)
  * when the source does not compile, GBDE_ERR_UNSUPPORTED without NVRTC. */
 GBDE_API int gbde_model_compile(int32_t model_id, int32_t alg, int32_t precision);
+
+/* ---- callbacks ----------------------------------------------------------
+ * Replace ContinuousCallback / DiscreteCallback (qa.jl:24,36; the reference's
+ * own tests solve with both, test/core.jl:60-79).  condition is CUDA C++
+ * statements that set `double g` from `const double* u` (the state), `double
+ * t` and `const double* p`; affect (may be NULL) modifies `double* u` and may
+ * set `bool terminate`.
+ *   GBDE_CB_CONTINUOUS: a sign change of g over an accepted step is located
+ *     on the method's dense output (Illinois regula falsi to ~1 ulp of t);
+ *     the trajectory moves to the left side of the root (LeftRootFind),
+ *     applies affect and restarts the method there.  Save points up to the
+ *     event use the step's dense output; the next step ignores crossings in
+ *     its first 1% (repeat_nudge), so a root is found once.
+ *   GBDE_CB_DISCRETE: g != 0 after an accepted step applies affect.
+ * terminate ends the trajectory with GBDE_RET_TERMINATED (later save slots
+ * hold NaN; t_end is the event time).  A solve with opts.callback compiles
+ * its kernels at run time (NVRTC, as user models), for built-in one-thread
+ * models and user models; not GBDE_ALG_AUTO, SDE methods or learned=1.
+ * Callback saves (save_positions) are not made: only the saveat points.   */
+typedef struct {
+  int32_t kind;          /* GBDE_CB_CONTINUOUS or GBDE_CB_DISCRETE         */
+  const char* condition; /* statements: g = ...   (required)               */
+  const char* affect;    /* statements on u[] / terminate, or NULL         */
+  int32_t terminate;     /* 1: terminate after affect at every event       */
+} gbde_callback;
+/* Register a callback; *callback_id (>= 1) goes into gbde_opts.callback. */
+GBDE_API int gbde_callback_register(const gbde_callback* def, int32_t* callback_id);
+/* Compile (and cache) the kernels of a model with a callback for one
+ * algorithm and precision, without a GPU; errors as gbde_model_compile. */
+GBDE_API int gbde_callback_compile(int32_t model, int32_t alg, int32_t precision,
+                                   int32_t callback_id);
 
 /* Self-check (no counterpart in the reference): the largest relative
  * difference, over n pseudo-random x with |x| in [2^-60, 2^61), between the
