@@ -323,37 +323,171 @@ __global__ void k_adamw(float* __restrict__ net, const float* __restrict__ grad,
 __global__ void k_step(unsigned* step) { *step += 1; }
 
 // Learned predictions for a solve: features -> network -> first dt, stiff
-// label and log2 of the attempted steps per trajectory.
+// label and log2 of the attempted steps per trajectory.  A forward-only
+// kernel with the activations in registers: the m16n8 accumulators of one
+// layer, after bias and GELU, are packed to BF16 pairs that are exactly the
+// A fragments of the next layer's k16 tiles (n-tiles 2k, 2k+1 -> k-tile k).
+// The weights sit transposed in shared memory ([out][in]) so every B
+// fragment is one 32-bit load; each warp runs 16 trajectories.
+struct PredShared {
+  __nv_bfloat16 W1t[HID * KIN], W2t[HID * HID], W3t[HID * HID], W4t[NOUT * HID];
+  float b1[HID], b2[HID], b3[HID], b4[NOUT];
+  float xmean[IN], xscale[IN], ymean, yscale, cmean, cscale;
+};
+
+GBDE_D uint32_t ld_pair(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+GBDE_D uint32_t pack_f2(float lo, float hi) {
+  return pack_bf16(__float2bfloat16(lo), __float2bfloat16(hi));
+}
+
+GBDE_D void mma16816(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                     uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// One hidden layer (K inputs as KT k-tiles of A fragments, 64 outputs):
+// h_out[nt][0..1] = BF16 pairs of gelu(A W + b) for rows g and g + 8.
+template <int KT>
+GBDE_D void pred_layer(const uint32_t (*A)[4], const __nv_bfloat16* Wt, int ldw, const float* b,
+                       uint32_t (*H)[2], int g, int t) {
+#pragma unroll
+  for (int nt = 0; nt < HID / 8; ++nt) {
+    float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const __nv_bfloat16* w = Wt + (nt * 8 + g) * ldw + 2 * t;
+#pragma unroll
+    for (int kt = 0; kt < KT; ++kt)
+      mma16816(c, A[kt][0], A[kt][1], A[kt][2], A[kt][3], ld_pair(w + kt * 16),
+               ld_pair(w + kt * 16 + 8));
+    const float b0 = b[nt * 8 + 2 * t], b1 = b[nt * 8 + 2 * t + 1];
+    H[nt][0] = pack_f2(gelu(c[0] + b0), gelu(c[1] + b1));  // row g
+    H[nt][1] = pack_f2(gelu(c[2] + b0), gelu(c[3] + b1));  // row g + 8
+  }
+}
+
 template <class M>
-__global__ void __launch_bounds__(WARPS * 32) k_mlp_predict(const float* __restrict__ net,
-                                                          const double* __restrict__ p,
-                                                          const double* __restrict__ u0,
-                                                          const double* __restrict__ t0,
-                                                          const double* __restrict__ tf, int64_t n,
-                                                          float* __restrict__ pred_dt,
-                                                          int8_t* __restrict__ pred_stiff,
-                                                          float* __restrict__ pred_cost) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  Shared& S = *reinterpret_cast<Shared*>(smem_raw);
-  stage_weights(S, net);
+__global__ void __launch_bounds__(256) k_mlp_predict(const float* __restrict__ net,
+                                                     const double* __restrict__ p,
+                                                     const double* __restrict__ u0,
+                                                     const double* __restrict__ t0,
+                                                     const double* __restrict__ tf, int64_t n,
+                                                     float* __restrict__ pred_dt,
+                                                     int8_t* __restrict__ pred_stiff,
+                                                     float* __restrict__ pred_cost) {
+  __shared__ PredShared S;
+  for (int i = threadIdx.x; i < HID * KIN; i += blockDim.x) {
+    const int o = i / KIN, k = i % KIN;
+    S.W1t[i] = __float2bfloat16(k < IN ? net[OFF_W1 + k * HID + o] : 0.0f);
+  }
+  for (int i = threadIdx.x; i < HID * HID; i += blockDim.x) {
+    const int o = i / HID, k = i % HID;
+    S.W2t[i] = __float2bfloat16(net[OFF_W2 + k * HID + o]);
+    S.W3t[i] = __float2bfloat16(net[OFF_W3 + k * HID + o]);
+  }
+  for (int i = threadIdx.x; i < NOUT * HID; i += blockDim.x) {
+    const int o = i / HID, k = i % HID;
+    S.W4t[i] = __float2bfloat16(o < OUT ? net[OFF_W4 + k * OUT + o] : 0.0f);
+  }
+  for (int i = threadIdx.x; i < HID; i += blockDim.x) {
+    S.b1[i] = net[OFF_B1 + i];
+    S.b2[i] = net[OFF_B2 + i];
+    S.b3[i] = net[OFF_B3 + i];
+  }
+  if (threadIdx.x < NOUT) S.b4[threadIdx.x] = threadIdx.x < OUT ? net[OFF_B4 + threadIdx.x] : 0.0f;
+  if (threadIdx.x < IN) {
+    S.xmean[threadIdx.x] = net[OFF_XMEAN + threadIdx.x];
+    S.xscale[threadIdx.x] = net[OFF_XSCALE + threadIdx.x];
+  }
+  if (threadIdx.x == 0) {
+    S.ymean = net[OFF_YMEAN];
+    S.yscale = net[OFF_YSCALE];
+    S.cmean = net[OFF_CMEAN];
+    S.cscale = net[OFF_CSCALE];
+  }
   __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  WarpBuf& W = S.w[warp];
-  for (int64_t b0 = ((int64_t)blockIdx.x * WARPS + warp) * 16; b0 < n;
-       b0 += (int64_t)gridDim.x * WARPS * 16) {
-    const int64_t i = b0 + (lane & 15);
-    float f[IN];
-    const bool valid = i < n;
-    if (valid) M::features(p + i * M::NP, u0 + i * M::N, tf[i] - t0[i], f);
-    fill_input(S, W, lane, valid, f);
-    forward_tile(S, W);
-    if (lane < 16 && valid) {
-      const float l10 = W.Y[lane * NOUT] * S.yscale + S.ymean;
-      pred_dt[i] = exp10f(fminf(fmaxf(l10, -30.0f), 30.0f));
-      pred_stiff[i] = W.Y[lane * NOUT + 1] > 0.0f ? 1 : 0;
-      pred_cost[i] = W.Y[lane * NOUT + 2] * S.cscale + S.cmean;
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t b0 = wid * 16; b0 < n; b0 += nw * 16) {
+    // lanes 0..15: normalised features of trajectory b0 + lane
+    float x[IN];
+    {
+      const int64_t i = b0 + (lane & 15);
+      float f[IN];
+#pragma unroll
+      for (int k = 0; k < IN; ++k) f[k] = 0.0f;
+      if (lane < 16 && i < n) M::features(p + i * M::NP, u0 + i * M::N, tf[i] - t0[i], f);
+#pragma unroll
+      for (int k = 0; k < IN; ++k) x[k] = lane < 16 && i < n ? (f[k] - S.xmean[k]) * S.xscale[k] : 0.0f;
     }
-    __syncwarp();
+    // layer 1 A fragment (K = 16, inputs 8..15 zero): rows g and g + 8, k = 2t, 2t + 1
+    uint32_t A1[1][4];
+    {
+      float r0[2], r1[2];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        float v0 = 0.0f, v1 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < IN; ++k) {
+          const float a = __shfl_sync(0xffffffffu, x[k], g);
+          const float bq = __shfl_sync(0xffffffffu, x[k], g + 8);
+          if (k == 2 * t + q) {
+            v0 = a;
+            v1 = bq;
+          }
+        }
+        r0[q] = v0;
+        r1[q] = v1;
+      }
+      A1[0][0] = pack_f2(r0[0], r0[1]);
+      A1[0][1] = pack_f2(r1[0], r1[1]);
+      A1[0][2] = 0u;
+      A1[0][3] = 0u;
+    }
+    uint32_t H[HID / 8][2], A[HID / 16][4];
+    pred_layer<1>(A1, S.W1t, KIN, S.b1, H, g, t);
+#pragma unroll
+    for (int kt = 0; kt < HID / 16; ++kt) {
+      A[kt][0] = H[2 * kt][0];
+      A[kt][1] = H[2 * kt][1];
+      A[kt][2] = H[2 * kt + 1][0];
+      A[kt][3] = H[2 * kt + 1][1];
+    }
+    pred_layer<HID / 16>(A, S.W2t, HID, S.b2, H, g, t);
+#pragma unroll
+    for (int kt = 0; kt < HID / 16; ++kt) {
+      A[kt][0] = H[2 * kt][0];
+      A[kt][1] = H[2 * kt][1];
+      A[kt][2] = H[2 * kt + 1][0];
+      A[kt][3] = H[2 * kt + 1][1];
+    }
+    pred_layer<HID / 16>(A, S.W3t, HID, S.b3, H, g, t);
+    // output layer: one n8 tile; lane (g, t) holds outputs 2t, 2t + 1 of rows g, g + 8
+    float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const __nv_bfloat16* w = S.W4t + g * HID + 2 * t;
+#pragma unroll
+    for (int kt = 0; kt < HID / 16; ++kt)
+      mma16816(c, H[2 * kt][0], H[2 * kt][1], H[2 * kt + 1][0], H[2 * kt + 1][1],
+               ld_pair(w + kt * 16), ld_pair(w + kt * 16 + 8));
+    const float o0 = S.b4[2 * t], o1 = S.b4[2 * t + 1];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int64_t i = b0 + g + 8 * r;
+      const float ya = c[2 * r] + o0, yb = c[2 * r + 1] + o1;
+      if (i < n) {
+        if (t == 0) {
+          const float l10 = ya * S.yscale + S.ymean;
+          pred_dt[i] = exp10f(fminf(fmaxf(l10, -30.0f), 30.0f));
+          pred_stiff[i] = yb > 0.0f ? 1 : 0;
+        } else if (t == 1) {
+          pred_cost[i] = ya * S.cscale + S.cmean;
+        }
+      }
+    }
   }
 }
 
@@ -405,13 +539,13 @@ namespace gbde {
 // Launch the learned predictions for model `model` (used by capi.cu).
 cudaError_t mlp_predict(int model, const float* net, const KArgs& a, float* pred_dt,
                         int8_t* pred_stiff, float* pred_cost, int num_sms, cudaStream_t s) {
-  const int grid = grid_for(a.N, num_sms);
+  // 8 warps of 16 trajectories per CTA, one wave where possible
+  const long long want = (a.N + 127) / 128, cap = 8LL * num_sms;
+  const int grid = (int)(want < cap ? (want > 0 ? want : 1) : cap);
   switch (model) {
 #define GBDE_PRED(ID, M)                                                                  \
   case ID: {                                                                              \
-    cudaError_t e = set_smem(k_mlp_predict<M>, sizeof(Shared));                           \
-    if (e != cudaSuccess) return e;                                                       \
-    k_mlp_predict<M><<<grid, WARPS * 32, sizeof(Shared), s>>>(net, a.p, a.u0, a.t0, a.tf, \
+    k_mlp_predict<M><<<grid, 256, 0, s>>>(net, a.p, a.u0, a.t0, a.tf,                     \
                                                                a.N, pred_dt, pred_stiff,  \
                                                                pred_cost);                \
     return cudaGetLastError();                                                            \
