@@ -250,20 +250,26 @@ def run_other(args, de):
     peak64, peak32 = ctx.fma_peak(0), ctx.fma_peak(1)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
 
-    def timed(o, dt, K, W):
+    def timed(o, dt, K, W, **kw):
         for _ in range(W):
-            de.solve_arrays(model, o, *dptr, kind, u_dtype=dt)
+            de.solve_arrays(model, o, *dptr, kind, u_dtype=dt, **kw)
         ts, r = [], None
         for _ in range(K):
             flush.zero_()
             torch.cuda.synchronize()
-            r = de.solve_arrays(model, o, *dptr, kind, u_dtype=dt)
+            r = de.solve_arrays(model, o, *dptr, kind, u_dtype=dt, **kw)
             ts.append(r["device_ms"])
         return float(np.median(ts)), r
 
+    reduce_ms = None
     with ClockSampler(0) as clk:
         plain_ms, rp = timed(plain, dts[0], args.steps, args.warmup)
         chosen_ms, rc = timed(chosen, dts[1], args.steps, args.warmup)
+        if ekind == "sde":
+            # the chosen form reducing in the kernel (E[u], Var[u] per save
+            # point) without storing the paths
+            reduce_ms, _ = timed(chosen, dts[1], args.steps, args.warmup, reduce=True,
+                                 store_u=False)
     res = {k: {kk: (v.cpu().numpy() if v is not None else None) for kk, v in r.items()
                if kk in ("u", "retcode", "naccept", "nreject")}
            for k, r in (("plain", rp), ("chosen", rc))}
@@ -340,6 +346,7 @@ def run_other(args, de):
             "config": dict(cfg, trajectories=N, l2="flushed between timed steps (256 MB write)"),
             "plain": {"value": N / (plain_ms * 1e-3), "ms_per_step": plain_ms},
             "speedup_vs_plain": plain_ms / chosen_ms, "accuracy": acc,
+            "chosen_reduce_only_ms": reduce_ms,
             "steps_per_traj_mean": float((res["chosen"]["naccept"] + res["chosen"]["nreject"]).mean()),
             "all_success": bool(np.all(res["chosen"]["retcode"] == capi.RET_SUCCESS)),
             "fp64_peak_tflops": peak64, "fp32_peak_tflops": peak32,

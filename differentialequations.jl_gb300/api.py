@@ -623,8 +623,13 @@ def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start
 
 
 def solve_arrays(model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", device=0,
-                 out=None, stats=True):
+                 out=None, stats=True, reduce=False, store_u=True):
     """Low-level entry: arrays in, arrays out, one gbde_ensemble_solve call.
+
+    reduce=True accumulates, inside the step kernels, the sums over
+    trajectories of every saved state and of its square (gbde_outputs.reduce),
+    returned as res["reduce"] [2][n_save][n_state] with res["mean"] and
+    res["var"] (N - 1); store_u=False then skips storing the ensemble.
 
     Host numpy arrays -> GBDE_MEM_HOST (the call stages the copies).
     CUDA torch tensors -> GBDE_MEM_DEVICE on the tensors' device and the
@@ -648,9 +653,13 @@ def solve_arrays(model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", d
         dev = u0.device
         tdt = torch.float32 if u_dtype == "f32" else torch.float64
         res = out or {
-            "u": torch.empty((N, n_save, model.n_state), dtype=tdt, device=dev),
+            "u": (torch.empty((N, n_save, model.n_state), dtype=tdt, device=dev)
+                  if store_u else None),
             "retcode": torch.empty(N, dtype=torch.int32, device=dev),
         }
+        if reduce:
+            res["reduce"] = torch.empty((2, n_save, model.n_state), dtype=torch.float64,
+                                        device=dev)
         if stats and out is None:
             for k in ("naccept", "nreject", "nf", "method"):
                 res[k] = torch.empty(N, dtype=torch.int32, device=dev)
@@ -663,10 +672,12 @@ def solve_arrays(model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", d
         arrs = tuple(np.ascontiguousarray(a, np.float64) if a is not None else None
                      for a in (p, u0, t0, tf, saveat))
         res = out or {
-            "u": np.empty((N, n_save, model.n_state),
-                          np.float32 if u_dtype == "f32" else np.float64),
+            "u": (np.empty((N, n_save, model.n_state),
+                           np.float32 if u_dtype == "f32" else np.float64) if store_u else None),
             "retcode": np.empty(N, np.int32),
         }
+        if reduce:
+            res["reduce"] = np.empty((2, n_save, model.n_state))
         if stats and out is None:
             for k in ("naccept", "nreject", "nf", "method"):
                 res[k] = np.empty(N, np.int32)
@@ -676,6 +687,8 @@ def solve_arrays(model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", d
     prob.p, prob.u0, prob.t0, prob.tf, prob.saveat = [capi.ptr(a) for a in arrs]
     outs.u = capi.ptr(res["u"])
     outs.retcode = capi.ptr(res["retcode"])
+    if reduce:
+        outs.reduce = capi.ptr(res["reduce"])
     for k in ("naccept", "nreject", "nf", "t_end", "method", "dt_first"):
         if k in res:
             setattr(outs, k, capi.ptr(res[k]))
@@ -684,4 +697,8 @@ def solve_arrays(model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", d
     ctx.solve(prob, opts, outs)
     res["device_ms"] = outs.device_ms
     res["total_ms"] = outs.total_ms
+    if reduce:
+        s1, s2 = res["reduce"][0], res["reduce"][1]
+        res["mean"] = s1 / N
+        res["var"] = (s2 - s1 * s1 / N) / (N - 1) if N > 1 else s1 * float("nan")
     return res

@@ -74,6 +74,7 @@ struct gbde_ctx {
   DevBuf dt1;         // staging of the first-accepted-step log (host calls)
   DevBuf mlp_net;     // learned predictor (GBDE_MLP_NET_FLOATS floats)
   DevBuf summary, summary_io;  // gbde_ensemble_summary: scratch; staged outputs (host mode)
+  DevBuf red;         // staged in-kernel reduction (host mode)
   int mlp_model = 0;  // model the loaded predictor belongs to (0 = none)
 };
 
@@ -185,7 +186,7 @@ int gbde_ctx_destroy(gbde_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf* b : {&ctx->p, &ctx->u0, &ctx->t0, &ctx->tf, &ctx->saveat, &ctx->u, &ctx->ret,
                     &ctx->nacc, &ctx->nrej, &ctx->nf, &ctx->tend, &ctx->method, &ctx->dt1,
-                    &ctx->mlp_net, &ctx->summary, &ctx->summary_io})
+                    &ctx->mlp_net, &ctx->summary, &ctx->summary_io, &ctx->red})
     b->release();
   ctx->scratch.release();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -343,8 +344,9 @@ static int check_solve_args(gbde_ctx* ctx, const gbde_problem* prob, const gbde_
     return set_err(ctx, GBDE_ERR_INVALID, "p, u0, t0 and tf must be non-NULL");
   if (prob->n_save > 0 && !prob->saveat)
     return set_err(ctx, GBDE_ERR_INVALID, "saveat must be non-NULL when n_save > 0");
-  if (N > 0 && (!out->retcode || (prob->n_save > 0 && !out->u)))
-    return set_err(ctx, GBDE_ERR_INVALID, "out->u and out->retcode must be non-NULL");
+  if (N > 0 && (!out->retcode || (prob->n_save > 0 && !out->u && !out->reduce)))
+    return set_err(ctx, GBDE_ERR_INVALID,
+                   "out->retcode must be non-NULL, and out->u or out->reduce");
   if (out->u_dtype != GBDE_F64 && out->u_dtype != GBDE_F32)
     return set_err(ctx, GBDE_ERR_INVALID, "u_dtype must be GBDE_F64 or GBDE_F32");
   const int alg = opts->alg;
@@ -456,6 +458,7 @@ static void fill_device_ptrs(KArgs& a, const gbde_problem* prob, const gbde_outp
   a.t_end = out->t_end;
   a.method_out = out->method;
   a.dt_first = out->dt_first;
+  a.red = out->reduce;
 }
 
 static LaunchCfg make_cfg(const gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts* opts) {
@@ -510,11 +513,13 @@ static int reserve_scratch(gbde_ctx* ctx, Scratch& sc, int64_t N, const gbde_opt
 // words, learned predictions, queue order (or AUTO's lists), the step kernels.
 // No host synchronisation except GBDE_ALG_AUTO's list sizes.
 static int enqueue_solve(gbde_ctx* ctx, Scratch& sc, KArgs& a, const LaunchCfg& cfg,
-                         const gbde_opts* opts, int np, cudaStream_t s) {
+                         const gbde_opts* opts, int np, int ns, cudaStream_t s) {
   const int64_t N = a.N;
   const int alg = opts->alg;
   unsigned long long* work = (unsigned long long*)sc.work.ptr;
   GBDE_CUDA(ctx, cudaMemsetAsync(work, 0, 256, s));
+  if (a.red && a.n_save > 0)  // the in-kernel reduction starts from zero sums
+    GBDE_CUDA(ctx, cudaMemsetAsync(a.red, 0, 2 * (size_t)a.n_save * ns * sizeof(double), s));
   a.queue = cfg.persistent ? work : nullptr;
   a.flag = (int32_t*)(work + 1);
   if (opts->learned && N > 0) {
@@ -575,7 +580,7 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
     GBDE_CUDA(ctx, ctx->t0.ensure((size_t)N * 8));
     GBDE_CUDA(ctx, ctx->tf.ensure((size_t)N * 8));
     GBDE_CUDA(ctx, ctx->saveat.ensure(save_elems * 8));
-    GBDE_CUDA(ctx, ctx->u.ensure(u_bytes));
+    if (out->u) GBDE_CUDA(ctx, ctx->u.ensure(u_bytes));
     GBDE_CUDA(ctx, ctx->ret.ensure((size_t)N * 4));
     if (N > 0) {
       GBDE_CUDA(ctx, cudaMemcpyAsync(ctx->p.ptr, prob->p, (size_t)N * np * 8, cudaMemcpyHostToDevice, s));
@@ -590,8 +595,12 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
     a.t0 = (const double*)ctx->t0.ptr;
     a.tf = (const double*)ctx->tf.ptr;
     a.saveat = (const double*)ctx->saveat.ptr;
-    a.u_out = ctx->u.ptr;
+    a.u_out = out->u ? ctx->u.ptr : nullptr;
     a.retcode = (int32_t*)ctx->ret.ptr;
+    if (out->reduce) {
+      GBDE_CUDA(ctx, ctx->red.ensure(2 * n_save * (size_t)ns * 8));
+      a.red = (double*)ctx->red.ptr;
+    }
     if (out->naccept) { GBDE_CUDA(ctx, ctx->nacc.ensure((size_t)N * 4)); a.naccept = (int32_t*)ctx->nacc.ptr; }
     if (out->nreject) { GBDE_CUDA(ctx, ctx->nrej.ensure((size_t)N * 4)); a.nreject = (int32_t*)ctx->nrej.ptr; }
     if (out->nf) { GBDE_CUDA(ctx, ctx->nf.ensure((size_t)N * 4)); a.nf = (int32_t*)ctx->nf.ptr; }
@@ -604,12 +613,16 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
   const LaunchCfg cfg = make_cfg(ctx, prob, opts);
   { const int rc = reserve_scratch(ctx, ctx->scratch, N, opts, prob->model); if (rc != GBDE_OK) return rc; }
   GBDE_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
-  { const int rc = enqueue_solve(ctx, ctx->scratch, a, cfg, opts, np, s); if (rc != GBDE_OK) return rc; }
+  { const int rc = enqueue_solve(ctx, ctx->scratch, a, cfg, opts, np, ns, s); if (rc != GBDE_OK) return rc; }
   GBDE_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
 
   int32_t flag = 0;
   if (host) {
-    if (u_bytes) GBDE_CUDA(ctx, cudaMemcpyAsync(out->u, ctx->u.ptr, u_bytes, cudaMemcpyDeviceToHost, s));
+    if (u_bytes && out->u)
+      GBDE_CUDA(ctx, cudaMemcpyAsync(out->u, ctx->u.ptr, u_bytes, cudaMemcpyDeviceToHost, s));
+    if (out->reduce && n_save)
+      GBDE_CUDA(ctx, cudaMemcpyAsync(out->reduce, a.red, 2 * n_save * (size_t)ns * 8,
+                                     cudaMemcpyDeviceToHost, s));
     if (N > 0) {
       GBDE_CUDA(ctx, cudaMemcpyAsync(out->retcode, ctx->ret.ptr, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
       if (out->naccept) GBDE_CUDA(ctx, cudaMemcpyAsync(out->naccept, a.naccept, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
@@ -671,7 +684,7 @@ int gbde_graph_create(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts* 
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    rc = enqueue_solve(ctx, G->scratch, a, cfg, opts, np, s);
+    rc = enqueue_solve(ctx, G->scratch, a, cfg, opts, np, ns, s);
     e = cudaStreamEndCapture(s, &g);
   }
   if (e == cudaSuccess && rc == GBDE_OK) e = cudaGraphInstantiate(&G->exec, g, 0);

@@ -129,6 +129,8 @@ extern "C" int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_
     return fail(GBDE_ERR_INVALID, "p, u0, t0 and tf must be non-NULL");
   if (prob->n_save > 0 && !prob->saveat)
     return fail(GBDE_ERR_INVALID, "saveat must be non-NULL when n_save > 0");
+  if (out->reduce)
+    return fail(GBDE_ERR_UNSUPPORTED, "gbde_ensemble_solve_noalloc has no in-kernel reduction");
   if (N > 0 && (!out->retcode || (prob->n_save > 0 && !out->u)))
     return fail(GBDE_ERR_INVALID, "out->u and out->retcode must be non-NULL");
   if (out->u_dtype != GBDE_F64 && out->u_dtype != GBDE_F32)

@@ -54,6 +54,8 @@ struct KArgs {
   double* dt_first;           // optional: size of the first accepted step
   int32_t chunk;              // persistent queue positions per fetch (>= 1)
   const double* dt_init;      // optional: starting step per trajectory (k_init_dt)
+  double* red;                // optional: [2][n_save][N] sums and sums of squares of the
+                              // saved states over trajectories (u_out may then be NULL)
 };
 
 GBDE_D uint64_t global_ns() {
@@ -121,8 +123,21 @@ GBDE_D double save_time(const KArgs& a, int64_t i, int j) {
                                        : __ldg(a.saveat + (size_t)i * a.n_save + j);
 }
 
+// In-kernel reduction of a saved state: FP64 atomics into the sums of save
+// point j (the order of the additions is not fixed, so sums agree with a
+// sequential sum to FP64 rounding).
+GBDE_D void reduce_add(const KArgs& a, int j, int c, int n_state, double x) {
+  atomicAdd(&a.red[(size_t)j * n_state + c], x);
+  atomicAdd(&a.red[((size_t)a.n_save + j) * n_state + c], x * x);
+}
+
 template <int N, class T>
 GBDE_D void store_state(const KArgs& a, int64_t i, int j, const T* v) {
+  if (a.red) {
+#pragma unroll
+    for (int c = 0; c < N; ++c) reduce_add(a, j, c, N, (double)v[c]);
+  }
+  if (a.u_out == nullptr) return;
   const size_t base = ((size_t)i * a.n_save + j) * N;
   if (a.out_f32) {
     float* o = (float*)a.u_out + base;

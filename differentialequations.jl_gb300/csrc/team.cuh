@@ -303,6 +303,8 @@ __device__ void integrate_team(const KArgs& a) {
     const bool bad = !(tf >= t) || !isfinite(t) || !isfinite(tf) ||
                      __any_sync(tm.mask, bad_lane);
     auto store = [&](int j, T v) {
+      if (a.red) reduce_add(a, j, tm.lane, TEAM, (double)v);
+      if (a.u_out == nullptr) return;
       const size_t o = ((size_t)i * a.n_save + j) * TEAM + tm.lane;
       if (a.out_f32) ((float*)a.u_out)[o] = (float)v;
       else ((double*)a.u_out)[o] = (double)v;

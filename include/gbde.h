@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define GBDE_ABI_VERSION 2
+#define GBDE_ABI_VERSION 3
 
 #if defined(__GNUC__)
 #define GBDE_API __attribute__((visibility("default")))
@@ -201,6 +201,13 @@ typedef struct {
   float total_ms;      /* out: wall time of the whole call                */
   double* dt_first;    /* [N] or NULL: size of the first accepted step (the
                           step log the learned predictor is trained on)   */
+  double* reduce;      /* [2][n_save][n_state] or NULL: the sums over
+                          trajectories of each saved state and of its
+                          square, accumulated inside the step kernels
+                          (EnsembleProblem's reduction, qa.jl:50: moments
+                          without storing the ensemble).  With u = NULL
+                          the ensemble is not stored at all.  Additions
+                          run in no fixed order (FP64 atomics).          */
 } gbde_outputs;
 
 /* ABI version of the loaded library (GBDE_ABI_VERSION). */

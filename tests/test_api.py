@@ -36,7 +36,7 @@ def test_header_struct_layout_matches_ctypes(capi):
 
 
 def test_version_and_model_info(capi):
-    assert capi.lib().gbde_version() == 2
+    assert capi.lib().gbde_version() == 3
     assert capi.model_info(capi.MODEL_LORENZ) == (3, 3)
     assert capi.model_info(capi.MODEL_VDP_RING8) == (16, 2)
     with pytest.raises(capi.GBDEError):
@@ -92,6 +92,9 @@ def test_solve_rejects_unsupported(de):
     prob = de.ODEProblem(de.models.linear, 0.5, (0.0, 1.0), [1.01])
     ens = de.EnsembleProblem(prob)
     with pytest.raises(NotImplementedError):
+        de.solve(ens, de.Tsit5(), de.EnsembleGB300(), trajectories=2, saveat=0.1,
+                 dense=True)
+    with pytest.raises(TypeError):  # callbacks are ContinuousCallback / DiscreteCallback objects
         de.solve(ens, de.Tsit5(), de.EnsembleGB300(), trajectories=2, saveat=0.1,
                  callback=object())
     with pytest.raises(NotImplementedError):
