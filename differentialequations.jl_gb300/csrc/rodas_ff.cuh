@@ -81,6 +81,131 @@ struct FfAcc {
   }
 };
 
+// ---- two state components per instruction
+// Blackwell's paired FP32 arithmetic (add / sub / mul / fma .rn.f32x2) takes
+// two FP32 values in one 64-bit register and rounds each exactly as the scalar
+// instruction would, so pairing state components (0,1), (2,3), ... halves the
+// issue slots of the pair sums while giving bit-identical results.  The
+// product is carried negated (pn = -p) because there is no paired negation.
+struct F2 {
+  unsigned long long v;
+};
+GBDE_D F2 f2_pack(float lo, float hi) {
+  F2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(lo), "f"(hi));
+  return r;
+}
+GBDE_D void f2_unpack(F2 a, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
+}
+GBDE_D F2 f2_add(F2 a, F2 b) {
+  F2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+GBDE_D F2 f2_sub(F2 a, F2 b) {
+  F2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+GBDE_D F2 f2_mul(F2 a, F2 b) {
+  F2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+GBDE_D F2 f2_fma(F2 a, F2 b, F2 c) {  // a b + c
+  F2 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+  return r;
+}
+
+// FfAcc for two components at once: (s, e) hold components c and c + 1.
+struct FfAcc2 {
+  F2 s, e;
+  GBDE_D void set(F2 h, F2 l) {
+    s = h;
+    e = l;
+  }
+  // += a (one pair coefficient for both) * b (hi parts bh, lo parts bl);
+  // ah = (a.hi, a.hi), al = (a.lo, a.lo), ahn = (-a.hi, -a.hi)
+  GBDE_D void fma(F2 ah, F2 al, F2 ahn, F2 bh, F2 bl) {
+    const F2 pn = f2_mul(ahn, bh);                       // -p
+    F2 pe = f2_fma(ah, bh, pn);                          // a.hi b.hi - p, exactly
+    pe = f2_fma(ah, bl, f2_fma(al, bh, pe));
+    const F2 t = f2_sub(s, pn);                          // s + p
+    const F2 bb = f2_sub(t, s);
+    const F2 err = f2_sub(f2_sub(s, f2_sub(t, bb)), f2_add(pn, bb));  // (s-(t-bb)) + (p-bb)
+    s = t;
+    e = f2_add(e, f2_add(err, pe));
+  }
+  GBDE_D void add(F2 xh, F2 xl) {  // += x
+    const F2 t = f2_add(s, xh);
+    const F2 bb = f2_sub(t, s);
+    const F2 err = f2_add(f2_sub(s, f2_sub(t, bb)), f2_sub(xh, bb));
+    s = t;
+    e = f2_add(e, f2_add(err, xl));
+  }
+  GBDE_D void get(ff& x0, ff& x1) const {  // TwoSum renormalisation, as FfAcc::get
+    const F2 t = f2_add(s, e);
+    const F2 bb = f2_sub(t, s);
+    const F2 err = f2_add(f2_sub(s, f2_sub(t, bb)), f2_sub(e, bb));
+    f2_unpack(t, x0.hi, x1.hi);
+    f2_unpack(err, x0.lo, x1.lo);
+  }
+};
+
+// A vector of N pairs as Q = N/2 paired halves (hi of c, c+1; lo of c, c+1)
+// plus the odd last component.
+template <int N>
+struct FfVec {
+  static constexpr int Q = N / 2;
+  F2 h[Q > 0 ? Q : 1], l[Q > 0 ? Q : 1];
+  ff o;
+  GBDE_D void from(const ff* x) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      h[q] = f2_pack(x[2 * q].hi, x[2 * q + 1].hi);
+      l[q] = f2_pack(x[2 * q].lo, x[2 * q + 1].lo);
+    }
+    if constexpr (N % 2) o = x[N - 1];
+  }
+};
+
+// Accumulator over a whole vector: FfAcc2 for the pairs, FfAcc for the odd one.
+template <int N>
+struct FfVecAcc {
+  static constexpr int Q = N / 2;
+  FfAcc2 v[Q > 0 ? Q : 1];
+  FfAcc w;
+  GBDE_D void set(const FfVec<N>& x) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) v[q].set(x.h[q], x.l[q]);
+    if constexpr (N % 2) w.set(x.o);
+  }
+  GBDE_D void zero() {
+    const F2 z = f2_pack(0.0f, 0.0f);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) v[q].set(z, z);
+    if constexpr (N % 2) w.set(ff(0.0f, 0.0f));
+  }
+  GBDE_D void fma(ff a, const FfVec<N>& b) {
+    const F2 ah = f2_pack(a.hi, a.hi), al = f2_pack(a.lo, a.lo), ahn = f2_pack(-a.hi, -a.hi);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) v[q].fma(ah, al, ahn, b.h[q], b.l[q]);
+    if constexpr (N % 2) w.fma(a, b.o);
+  }
+  GBDE_D void add(const FfVec<N>& b) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) v[q].add(b.h[q], b.l[q]);
+    if constexpr (N % 2) w.add(b.o);
+  }
+  GBDE_D void get(ff* out) const {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) v[q].get(out[2 * q], out[2 * q + 1]);
+    if constexpr (N % 2) out[N - 1] = w.get();
+  }
+};
+
 // The FP64 LU factors as pairs, negated so that the substitutions are sums of
 // products: nL (strictly lower), nU (strictly upper), inv (reciprocal pivots).
 // The row swaps recorded in piv are applied to the right-hand side first (the
@@ -188,17 +313,43 @@ struct RodasFF {
   GBDE_D const ff* unew() const { return un; }
   GBDE_D const ff* f0() const { return F0; }
 
-  // Transformed stages u_1..u_7 of the current step, pair (hi, lo) per
-  // component: slot (i N + c) of this thread at stride kFfStageThreads.
-  GBDE_D static float2* stages() {
-    __shared__ float2 buf[7 * N * kFfStageThreads];
+  // Transformed stages u_1..u_7 of the current step in shared memory, per
+  // thread at stride kFfStageThreads: for each component pair (2q, 2q+1) one
+  // 16-byte (hi pair, lo pair) slot -- loaded straight into paired registers --
+  // and for an odd last component one 8-byte (hi, lo) slot.
+  static constexpr int Q = N / 2;
+  GBDE_D static ulonglong2* pair_stages() {
+    __shared__ ulonglong2 buf[7 * (Q > 0 ? Q : 1) * kFfStageThreads];
     return buf + threadIdx.x;
   }
-  GBDE_D static ff ld(const float2* st, int slot) {
-    const float2 v = st[slot * kFfStageThreads];
-    return ff(v.x, v.y);
+  GBDE_D static float2* odd_stages() {
+    __shared__ float2 buf[7 * (N % 2 ? 1 : 0) * kFfStageThreads + 1];
+    return buf + threadIdx.x;
   }
-  GBDE_D static void st(float2* st, int slot, ff x) { st[slot * kFfStageThreads] = make_float2(x.hi, x.lo); }
+  GBDE_D static FfVec<N> ld(int j) {
+    FfVec<N> v;
+    const ulonglong2* sp = pair_stages();
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const ulonglong2 x = sp[(j * Q + q) * kFfStageThreads];
+      v.h[q].v = x.x;
+      v.l[q].v = x.y;
+    }
+    if constexpr (N % 2) {
+      const float2 x = odd_stages()[j * kFfStageThreads];
+      v.o = ff(x.x, x.y);
+    }
+    return v;
+  }
+  GBDE_D static void st(int j, const ff* x) {
+    ulonglong2* sp = pair_stages();
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+      sp[(j * Q + q) * kFfStageThreads] =
+          make_ulonglong2(f2_pack(x[2 * q].hi, x[2 * q + 1].hi).v,
+                          f2_pack(x[2 * q].lo, x[2 * q + 1].lo).v);
+    if constexpr (N % 2) odd_stages()[j * kFfStageThreads] = make_float2(x[N - 1].hi, x[N - 1].lo);
+  }
 
   GBDE_D void init(const ff* u0, const ff* p, int& nf) {
 #pragma unroll
@@ -238,48 +389,53 @@ struct RodasFF {
     L.from(W);
     const ff iht = ff_split(rcp64(dt));
     const RodasFfTab& tb = c_rodas_ff[RodasFfIdx<Tag>::v];
-    float2* sb = stages();
+    FfVec<N> uv;
+    uv.from(uu);
     ff y[N], s[N];
 #pragma unroll 1
     for (int i = 0; i < 8; ++i) {
       // stage argument: u0 for stage 1, a fresh combination for stages 2-6; for
       // 7 and 8 the previous argument plus the previous stage (a_7j = a_6j,
       // a_76 = 1, a_8j = a_7j, a_87 = 1)
-      FfAcc ya[N], ca[N];
+      FfVecAcc<N> ya, ca;
       const bool fresh_arg = i <= 5;
-#pragma unroll
-      for (int c = 0; c < N; ++c) {
-        ya[c].set(fresh_arg ? uu[c] : y[c]);
-        ca[c].set(ff(0.0f, 0.0f));
+      if (fresh_arg) {
+        ya.set(uv);
+      } else {
+        FfVec<N> yv;
+        yv.from(y);
+        ya.set(yv);
       }
+      ca.zero();
 #pragma unroll 1
       for (int j = 0; j < i; ++j) {
         const ff cij = tb.rc[i][j];
         const ff aij = tb.ra[fresh_arg ? i : 0][fresh_arg ? j : 0];
-        const bool last = j == i - 1;
-#pragma unroll
-        for (int c = 0; c < N; ++c) {
-          const ff sj = ld(sb, j * N + c);
-          if (fresh_arg) ya[c].fma(aij, sj);
-          else if (last) ya[c].add(sj);
-          ca[c].fma(cij, sj);
-        }
+        const FfVec<N> sj = ld(j);
+        if (fresh_arg) ya.fma(aij, sj);
+        else if (j == i - 1) ya.add(sj);
+        ca.fma(cij, sj);
       }
       ff fy[N], r[N];
-#pragma unroll
-      for (int c = 0; c < N; ++c) y[c] = ya[c].get();
+      ya.get(y);
       M::f(fy, y, p);
+      if (i > 0) {
+        ff cs[N];
+        ca.get(cs);
+        FfVec<N> fv, cv;
+        fv.from(fy);
+        cv.from(cs);
+        FfVecAcc<N> ra;
+        ra.set(fv);
+        ra.fma(iht, cv);
+        ra.get(r);
+      } else {
 #pragma unroll
-      for (int c = 0; c < N; ++c) {
-        FfAcc ra;
-        ra.set(fy[c]);
-        if (i > 0) ra.fma(iht, ca[c].get());
-        r[c] = ra.get();
+        for (int c = 0; c < N; ++c) r[c] = fy[c];
       }
       L.solve(r);
       if (i < 7) {
-#pragma unroll
-        for (int c = 0; c < N; ++c) st(sb, i * N + c, r[c]);
+        st(i, r);
       } else {
 #pragma unroll
         for (int c = 0; c < N; ++c) s[c] = r[c];
@@ -309,13 +465,15 @@ struct RodasFF {
     const RodasFfTab& tb = c_rodas_ff[RodasFfIdx<Tag>::v];
     const ff tt = ff_split(th);
     const ff w = tt * (ff(1.0f, 0.0f) - tt);
-    const float2* sb = stages();
-    FfAcc a[N];
+    ff du[N];
 #pragma unroll
-    for (int c = 0; c < N; ++c) {
-      a[c].set(uu[c]);
-      a[c].fma(tt, un[c] - uu[c]);
-    }
+    for (int c = 0; c < N; ++c) du[c] = un[c] - uu[c];
+    FfVec<N> uv, dv;
+    uv.from(uu);
+    dv.from(du);
+    FfVecAcc<N> a;
+    a.set(uv);
+    a.fma(tt, dv);
 #pragma unroll 1
     for (int j = 0; j < 7; ++j) {
       FfAcc q;
@@ -324,12 +482,9 @@ struct RodasFF {
       const ff q3 = q.get();
       q.set(tb.h2[j]);
       q.fma(tt, q3);
-      const ff e = w * q.get();
-#pragma unroll
-      for (int c = 0; c < N; ++c) a[c].fma(e, ld(sb, j * N + c));
+      a.fma(w * q.get(), ld(j));
     }
-#pragma unroll
-    for (int c = 0; c < N; ++c) out[c] = a[c].get();
+    a.get(out);
   }
 
   GBDE_D void accept(const ff*, int&) {
