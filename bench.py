@@ -189,10 +189,11 @@ def other_workload(de, name, N, seed):
         saveat = de.save_grid(0.0, 1.0, 0.1)
         base = dict(reltol=1e-8, abstol=1e-8)
         plain = opts(capi.ALG_TSIT5, **base)
-        chosen = opts(capi.ALG_TSIT5, batching=capi.BATCH_PERSISTENT, **base)
-        cfg = {"workload": "lorenz_tsit5_fp64_N%d" % N, "model": "lorenz", "alg": "tsit5",
+        chosen = opts(capi.ALG_TSIT5, precision=capi.PREC_F32X2, **base)
+        cfg = {"workload": "lorenz_tsit5_N%d" % N, "model": "lorenz", "alg": "tsit5",
                "reltol": 1e-8, "abstol": 1e-8, "saveat": "0:0.1:1 (11 points)",
-               "chosen_form": "persistent fp64"}
+               "chosen_form": "one launch, FP32-pair Tsit5 stepper (FP64 norm accumulation "
+                              "and compensated time)"}
         return (de.models.lorenz, p, u0, t0, tf, saveat, capi.SAVE_GRID, plain, chosen,
                 ("f64", "f64"), cfg, "weighted")
     if name in ("lv_em", "lv_sosri"):

@@ -376,7 +376,8 @@ def test_rcp64_accuracy(de):
 @pytest.mark.parametrize("model_name,alg,rt,at", [
     ("robertson", "RODAS5", 1e-6, 1e-10), ("robertson", "RODAS5P", 1e-6, 1e-10),
     ("robertson", "ROSENBROCK23", 1e-6, 1e-10), ("lorenz", "TSIT5", 1e-8, 1e-8),
-    ("lorenz", "VERN7", 1e-8, 1e-8), ("lorenz", "RODAS5", 1e-7, 1e-7)])
+    ("lorenz", "VERN7", 1e-8, 1e-8), ("lorenz", "RODAS5", 1e-7, 1e-7),
+    ("linear", "TSIT5", 1e-10, 1e-10)])
 def test_f32x2_vs_fp64_oracle(de, oracle, rng, model_name, alg, rt, at):
     capi = de._capi
     model = getattr(de.models, model_name)
