@@ -231,7 +231,8 @@ def other_workload(de, name, N, seed):
         cfg = {"workload": "vdp_ring8_auto_N%d" % N, "model": "vdp_ring8 (16 states)",
                "alg": "auto: tsit5 if mu <= 100 else rodas5", "reltol": 1e-5,
                "saveat": "0:1:20 (21 points)",
-               "chosen_form": "persistent; Tsit5 FP32 compensated state, Rodas5 FP64"}
+               "chosen_form": "persistent; Tsit5 FP32 compensated state, Rodas5 FP32-pair "
+                              "stages and solves on an FP64 Jacobian, LU and norm"}
         return (de.models.vdp_ring8, p, u0, t0, tf, saveat, capi.SAVE_GRID, plain, chosen,
                 ("f64", "f32"), cfg, "vdp")
     raise ValueError(name)

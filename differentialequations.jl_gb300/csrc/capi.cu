@@ -271,7 +271,9 @@ static bool is_sde_alg(int a) { return a == GBDE_ALG_EM || a == GBDE_ALG_SOSRI; 
 
 // GBDE_ALG_AUTO: classify every trajectory (stiff iff p[0] > stiff_threshold,
 // or the learned predictor's label), then run the non-stiff list with Tsit5
-// (FP32 state in mixed precision) and the stiff list with Rodas5 (FP64).
+// in the requested precision and the stiff list with Rodas5: FP64 when FP64
+// is requested, otherwise FP32-pair stages and solves on an FP64 Jacobian,
+// LU and norm (Rodas needs more than FP32 stages for its tolerances).
 // The options' controller exponents (Tsit5's by default) drive the Tsit5
 // part; the Rodas5 part uses Rodas5's default exponents.
 static int solve_auto(gbde_ctx* ctx, Scratch& sc, const LaunchCfg& cfg, const KArgs& a, int np,
@@ -294,7 +296,8 @@ static int solve_auto(gbde_ctx* ctx, Scratch& sc, const LaunchCfg& cfg, const KA
     const int32_t* list;
     unsigned long long* queue;
   } parts[2] = {{GBDE_ALG_TSIT5, cfg.precision, cnt[0], nonstiff, work},
-                {GBDE_ALG_RODAS5, GBDE_PREC_FP64, cnt[1], stiff, work + 2}};
+                {GBDE_ALG_RODAS5, cfg.precision == GBDE_PREC_FP64 ? GBDE_PREC_FP64 : GBDE_PREC_F32X2,
+                 cnt[1], stiff, work + 2}};
   for (const auto& part : parts) {
     if (part.n == 0) continue;
     KArgs b = a;
@@ -358,9 +361,11 @@ static int check_solve_args(gbde_ctx* ctx, const gbde_problem* prob, const gbde_
       opts->precision != GBDE_PREC_F32X2)
     return set_err(ctx, GBDE_ERR_INVALID, "unknown precision %d", opts->precision);
   if (opts->precision == GBDE_PREC_F32X2 &&
-      (is_sde_alg(alg) || alg == GBDE_ALG_AUTO || prob->model == GBDE_MODEL_VDP_RING8))
+      (is_sde_alg(alg) ||
+       (prob->model == GBDE_MODEL_VDP_RING8 && opts->threads_per_traj == 1)))
     return set_err(ctx, GBDE_ERR_UNSUPPORTED,
-                   "GBDE_PREC_F32X2 is built for the one-thread-per-trajectory ODE kernels");
+                   "GBDE_PREC_F32X2 is built for the ODE kernels: one thread per trajectory, "
+                   "or 16-lane teams on the 16-state ring");
   if (opts->batching != GBDE_BATCH_PLAIN && opts->batching != GBDE_BATCH_PERSISTENT)
     return set_err(ctx, GBDE_ERR_INVALID, "unknown batching %d", opts->batching);
   if (opts->adaptive && !(opts->reltol > 0.0 && opts->abstol > 0.0))

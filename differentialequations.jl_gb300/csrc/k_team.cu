@@ -6,18 +6,35 @@
 
 namespace gbde {
 
+// Resident CTAs of 128 threads per SM each team stepper is compiled for: the
+// Rodas steppers are latency-bound on their broadcast chains (LU, triangular
+// solves), so 3 CTAs (<= 168 registers) beat 2 with more registers.
+template <class Alg> struct TeamMinBlocks { static constexpr int v = 1; };
+template <class M, class T, class Tag> struct TeamMinBlocks<TeamRodas<M, T, Tag>> {
+  static constexpr int v = 3;
+};
+template <class M, class Tag> struct TeamMinBlocks<TeamRodasFF<M, Tag>> {
+  static constexpr int v = 3;
+};
+
 template <class Alg, class M, class T, bool MIXED>
-__global__ void __launch_bounds__(128) k_team(const KArgs a) {
+__global__ void __launch_bounds__(128, TeamMinBlocks<Alg>::v) k_team(const KArgs a) {
   integrate_team<Alg, M, T, MIXED>(a);
 }
 
-template <class M, class T> using TeamRodas5 = TeamRodas<M, T, Rodas5Tag>;
-template <class M, class T> using TeamRodas5P = TeamRodas<M, T, Rodas5PTag>;
+// Rodas in FP32 pairs is its own stepper (TeamRodasFF); Tsit5 takes the
+// pair type directly.
+template <class M, class T, class Tag> struct TeamRodasSel { using type = TeamRodas<M, T, Tag>; };
+template <class M, class Tag> struct TeamRodasSel<M, ff, Tag> { using type = TeamRodasFF<M, Tag>; };
+template <class M, class T> using TeamRodas5 = typename TeamRodasSel<M, T, Rodas5Tag>::type;
+template <class M, class T> using TeamRodas5P = typename TeamRodasSel<M, T, Rodas5PTag>::type;
 
 template <template <class, class> class AlgT, class M>
 static cudaError_t dispatch_prec(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
   if (cfg.precision == GBDE_PREC_MIXED)
     return launch_team_kernel(k_team<AlgT<M, float>, M, float, true>, cfg, a, s);
+  if (cfg.precision == GBDE_PREC_F32X2)
+    return launch_team_kernel(k_team<AlgT<M, ff>, M, ff, true>, cfg, a, s);
   return launch_team_kernel(k_team<AlgT<M, double>, M, double, false>, cfg, a, s);
 }
 

@@ -358,10 +358,16 @@ __device__ void integrate_all(const KArgs& a) {
       bool bad = !(tf >= t) || !isfinite(t) || !isfinite(tf);
 #pragma unroll
       for (int c = 0; c < N; ++c) bad |= !isfinite((double)u0[c]);
-      // save points at t0 store u0 exactly
-      while (js < a.n_save && save_time(a, i, js) <= t) {
-        store_state<N>(a, i, js, u0);
-        ++js;
+      // save points at t0 store u0 exactly: from the FP64 input, not from its
+      // copy in the working precision T (a pair holds ~48 bits, a float 24)
+      if (js < a.n_save && save_time(a, i, js) <= t) {
+        double u0d[N];
+#pragma unroll
+        for (int c = 0; c < N; ++c) u0d[c] = __ldg(a.u0 + (size_t)i * N + c);
+        while (js < a.n_save && save_time(a, i, js) <= t) {
+          store_state<N>(a, i, js, u0d);
+          ++js;
+        }
       }
       if (bad) {
         ret = GBDE_RET_INITIALFAILURE;

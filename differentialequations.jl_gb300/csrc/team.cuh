@@ -19,6 +19,7 @@
 #pragma once
 #include "rosenbrock.cuh"
 #include "explicit_rk.cuh"
+#include "rodas_ff.cuh"
 
 namespace gbde {
 
@@ -33,6 +34,9 @@ struct Team {
     mask = 0xFFFFu << (l & TEAM);
   }
   template <class T> GBDE_D T bcast(T v, int src) const { return __shfl_sync(mask, v, src, TEAM); }
+  GBDE_D ff bcast(ff v, int src) const {
+    return ff(__shfl_sync(mask, v.hi, src, TEAM), __shfl_sync(mask, v.lo, src, TEAM));
+  }
   GBDE_D double sum(double v) const {
 #pragma unroll
     for (int o = TEAM / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o, TEAM);
@@ -106,6 +110,45 @@ struct TeamLU {
   }
 };
 
+// The factors of a TeamLU as pairs for the FP32-pair stepper: this lane's
+// row negated (multipliers and U entries) and its pivot reciprocal, split on
+// the integer pipe.  The substitutions run in pair arithmetic in the same
+// order as TeamLU::solve; the value each step broadcasts is renormalised
+// first, the lane's own row sum is carried unnormalised (FfAcc).
+struct TeamLUFF {
+  ff na[TEAM];
+  ff invp;
+  int step;
+  uint64_t piv;
+
+  GBDE_D void from(const TeamLU& W) {
+#pragma unroll
+    for (int c = 0; c < TEAM; ++c) na[c] = ff_split(-W.a[c]);
+    invp = ff_split(W.invp);
+    step = W.step;
+    piv = W.piv;
+  }
+  GBDE_D int pivot_lane(int k) const { return (int)((piv >> (4 * k)) & 15u); }
+
+  GBDE_D ff solve(ff b, const Team& tm) const {
+    FfAcc acc;
+    acc.set(b);
+#pragma unroll
+    for (int k = 0; k < TEAM; ++k) {  // forward: L z = P b
+      const ff z = tm.bcast(acc.get(), pivot_lane(k));
+      if (step > k) acc.fma(na[k], z);
+    }
+    ff x(0.0f, 0.0f);
+#pragma unroll
+    for (int k = TEAM - 1; k >= 0; --k) {  // backward: U x = z
+      const ff xk = tm.bcast(acc.get() * invp, pivot_lane(k));
+      if (step < k) acc.fma(na[k], xk);
+      if (tm.lane == k) x = xk;
+    }
+    return x;
+  }
+};
+
 // ------------------------------------------------ team Rodas5 / Rodas5P
 // Same transformed form as RodasAlg (rosenbrock.cuh), one component per lane.
 template <class M, class T, class Tag>
@@ -114,7 +157,6 @@ struct TeamRodas {
   static constexpr int ORDER = 4, ALG_ID = K::ALG_ID;
   static_assert(M::N == TEAM, "team kernels are for 16-state models");
   T uu, un, F0, s1, s2, s3, s4, s5, s6, s7;
-  T Jr[TEAM];  // row r of the Jacobian at uu
   bool fresh;
 
   GBDE_D T u() const { return uu; }
@@ -125,7 +167,6 @@ struct TeamRodas {
 
   GBDE_D void refresh(const T* p, const Team& tm) {
     F0 = M::f_lane(tm.lane, uu, p, tm);
-    M::jac_lane(tm.lane, uu, p, tm, Jr);
     fresh = true;
   }
 
@@ -141,11 +182,17 @@ struct TeamRodas {
       refresh(p, tm);
       ++nf;
     }
+    // row r of the Jacobian at uu, built afresh on every attempt: a copy
+    // kept across attempts would hold 16 more registers through the stages
     TeamLU W;
     const double ih = rcp64(dt);
     const double dg = ih * (1.0 / K::g);
+    {
+      T Jr[TEAM];
+      M::jac_lane(tm.lane, uu, p, tm, Jr);
 #pragma unroll
-    for (int c = 0; c < TEAM; ++c) W.a[c] = c == tm.lane ? dg - (double)Jr[c] : -(double)Jr[c];
+      for (int c = 0; c < TEAM; ++c) W.a[c] = c == tm.lane ? dg - (double)Jr[c] : -(double)Jr[c];
+    }
     W.factor(tm);
     const T iht = (T)ih;  // r_i = f(y_i) + (1/h) sum_j C_ij u_j
     s1 = (T)W.solve((double)F0, tm);
@@ -184,6 +231,139 @@ struct TeamRodas {
 #undef GBDE_RODAS_E
     return uu + (T)th * (un - uu) + (e[0] * s1 + e[1] * s2 + e[2] * s3 + e[3] * s4 + e[4] * s5 +
                                      e[5] * s6 + e[6] * s7);
+  }
+
+  GBDE_D void accept() {
+    uu = un;
+    fresh = false;
+  }
+};
+
+// ------------------------------------ team Rodas5 / Rodas5P in FP32 pairs
+// TeamRodas with the F32X2 split of work (as RodasFF, rodas_ff.cuh): the
+// Jacobian row, W and its row-distributed LU, and the error norm stay FP64;
+// the state, the stages, the right-hand sides, the stage combinations, the
+// eight triangular solves (TeamLUFF) and the dense output run in FP32 pairs.
+// As in RodasFF the step body is compact: the stage loop is not unrolled, so
+// the pair solve (32 unrolled broadcast-and-update steps) has one call site,
+// the transformed stages live in shared memory and the coefficients come from
+// the constant table.  With the eight solves inlined the kernel's top stall
+// was an empty instruction cache.
+template <class M, class Tag>
+struct TeamRodasFF {
+  using K = RodasCoef<Tag>;
+  using T = ff;
+  static constexpr int ORDER = 4, ALG_ID = K::ALG_ID;
+  static_assert(M::N == TEAM, "team kernels are for 16-state models");
+  ff uu, un, F0;
+  double pd[M::NP];
+  bool fresh;
+
+  GBDE_D ff u() const { return uu; }
+  GBDE_D ff unew() const { return un; }
+  GBDE_D ff f0() const { return F0; }
+
+  // stages u_1..u_7 of this lane's component, at stride kFfStageThreads
+  GBDE_D static float2* stage_buf() {
+    __shared__ float2 buf[7 * kFfStageThreads];
+    return buf + threadIdx.x;
+  }
+  GBDE_D static ff ld(int j) {
+    const float2 v = stage_buf()[j * kFfStageThreads];
+    return ff(v.x, v.y);
+  }
+  GBDE_D static void st(int j, ff x) { stage_buf()[j * kFfStageThreads] = make_float2(x.hi, x.lo); }
+
+  GBDE_D ff rhs(ff y, const ff* p, const Team& tm) const { return M::f_lane(tm.lane, y, p, tm); }
+
+  GBDE_D void refresh(const ff* p, const Team& tm) {
+    F0 = M::f_lane(tm.lane, uu, p, tm);
+    fresh = true;
+  }
+
+  GBDE_D void init(ff u0, const ff* p, const Team& tm, int& nf) {
+#pragma unroll
+    for (int k = 0; k < M::NP; ++k) pd[k] = (double)p[k];
+    uu = u0;
+    refresh(p, tm);
+    ++nf;
+  }
+
+  GBDE_D double attempt(double dt, const ff* p, double abstol, double reltol, const Team& tm,
+                        int& nf) {
+    if (!fresh) {
+      refresh(p, tm);
+      ++nf;
+    }
+    TeamLUFF L;
+    const double ih = rcp64(dt);
+    {
+      TeamLU W;
+      const double dg = ih * (1.0 / K::g);
+      double Jr[TEAM];  // FP64 Jacobian row at uu, built on every attempt (as TeamRodas)
+      M::jac_lane(tm.lane, f2d_bits(uu.hi) + f2d_bits(uu.lo), pd, tm, Jr);
+#pragma unroll
+      for (int c = 0; c < TEAM; ++c) W.a[c] = c == tm.lane ? dg - Jr[c] : -Jr[c];
+      W.factor(tm);
+      L.from(W);
+    }
+    const ff iht = ff_split(ih);  // r_i = f(y_i) + (1/h) sum_j C_ij u_j
+    const RodasFfTab& tb = c_rodas_ff[RodasFfIdx<Tag>::v];
+    ff y = uu, s8;
+#pragma unroll 1
+    for (int i = 0; i < 8; ++i) {
+      ff r = F0;
+      if (i > 0) {
+        // stage argument: a fresh combination for stages 2-6; for 7 and 8 the
+        // previous argument plus the previous stage (a_7j = a_6j, a_76 = 1,
+        // a_8j = a_7j, a_87 = 1)
+        const bool fresh_arg = i <= 5;
+        FfAcc ya, ca;
+        ya.set(fresh_arg ? uu : y);
+        ca.set(ff(0.0f, 0.0f));
+#pragma unroll 1
+        for (int j = 0; j < i; ++j) {
+          const ff sj = ld(j);
+          if (fresh_arg) ya.fma(tb.ra[fresh_arg ? i : 0][j], sj);
+          else if (j == i - 1) ya.add(sj);
+          ca.fma(tb.rc[i][j], sj);
+        }
+        y = ya.get();
+        FfAcc ra;
+        ra.set(rhs(y, p, tm));
+        ra.fma(iht, ca.get());
+        r = ra.get();
+      }
+      const ff x = L.solve(r, tm);
+      if (i < 7) st(i, x);
+      else s8 = x;
+    }
+    nf += 7;
+    un = y + s8;
+    const float m = fmaxf(fabsf(uu.hi), fabsf(un.hi));
+    const double e = f2d_bits(s8.hi) * rcp64(abstol + reltol * f2d_bits(m));
+    return tm.sum(e * e) * (1.0 / TEAM);
+  }
+
+  // as RodasFF::interp, one component per lane
+  GBDE_D ff interp(double th, double) const {
+    const RodasFfTab& tb = c_rodas_ff[RodasFfIdx<Tag>::v];
+    const ff tt = ff_split(th);
+    const ff w = tt * (ff(1.0f, 0.0f) - tt);
+    FfAcc a;
+    a.set(uu);
+    a.fma(tt, un - uu);
+#pragma unroll 1
+    for (int j = 0; j < 7; ++j) {
+      FfAcc q;
+      q.set(tb.h3[j]);
+      q.fma(tt, tb.h4[j]);
+      const ff q3 = q.get();
+      q.set(tb.h2[j]);
+      q.fma(tt, q3);
+      a.fma(w * q.get(), ld(j));
+    }
+    return a.get();
   }
 
   GBDE_D void accept() {
@@ -291,7 +471,8 @@ __device__ void integrate_team(const KArgs& a) {
     if (i < 0) break;
 #pragma unroll
     for (int k = 0; k < M::NP; ++k) p[k] = (T)__ldg(a.p + (size_t)i * M::NP + k);
-    const T u0 = (T)__ldg(a.u0 + (size_t)i * TEAM + tm.lane);
+    const double u0d = __ldg(a.u0 + (size_t)i * TEAM + tm.lane);
+    const T u0 = (T)u0d;
     double t = __ldg(a.t0 + i), tlo = 0.0;
     const double tf = __ldg(a.tf + i);
     int js = 0, nacc = 0, nrej = 0, nfev = 0;
@@ -302,14 +483,15 @@ __device__ void integrate_team(const KArgs& a) {
     const bool bad_lane = !isfinite((double)u0);
     const bool bad = !(tf >= t) || !isfinite(t) || !isfinite(tf) ||
                      __any_sync(tm.mask, bad_lane);
-    auto store = [&](int j, T v) {
-      if (a.red) reduce_add(a, j, tm.lane, TEAM, (double)v);
+    auto store = [&](int j, double v) {  // v: FP64 value of this lane's component
+      if (a.red) reduce_add(a, j, tm.lane, TEAM, v);
       if (a.u_out == nullptr) return;
       const size_t o = ((size_t)i * a.n_save + j) * TEAM + tm.lane;
       if (a.out_f32) ((float*)a.u_out)[o] = (float)v;
-      else ((double*)a.u_out)[o] = (double)v;
+      else ((double*)a.u_out)[o] = v;
     };
-    while (js < a.n_save && save_time(a, i, js) <= t) store(js++, u0);
+    // save points at t0 store u0 exactly (the FP64 input, whatever T)
+    while (js < a.n_save && save_time(a, i, js) <= t) store(js++, u0d);
     double dt = 0.0;
     if (bad) {
       ret = GBDE_RET_INITIALFAILURE;
@@ -365,7 +547,7 @@ __device__ void integrate_team(const KArgs& a) {
           const double ts = save_time(a, i, js);
           const uint64_t ts_o = ord_bits(ts);
           if (ts_o > tnew_o) break;
-          store(js, ts_o == tnew_o ? alg.unew() : alg.interp(((ts - t) - tlo) / h, h));
+          store(js, (double)(ts_o == tnew_o ? alg.unew() : alg.interp(((ts - t) - tlo) / h, h)));
           ++js;
         }
         alg.accept();
@@ -393,8 +575,7 @@ __device__ void integrate_team(const KArgs& a) {
         }
       }
     }
-    const T nanv = (T)__longlong_as_double(0x7ff8000000000000ll);
-    for (; js < a.n_save; ++js) store(js, nanv);
+    for (; js < a.n_save; ++js) store(js, __longlong_as_double(0x7ff8000000000000ll));
     if (tm.lane == 0) {
       a.retcode[i] = ret;
       if (a.naccept) a.naccept[i] = nacc;

@@ -39,16 +39,23 @@ def weighted(u, ref, rt=RT):
     return (np.abs(u - ref) / (rt + rt * np.abs(ref))).max(axis=(1, 2))
 
 
+def _prec(capi, precision):
+    return {"fp64": capi.PREC_FP64, "f32x2": capi.PREC_F32X2, "mixed": capi.PREC_MIXED}[precision]
+
+
 @pytest.mark.parametrize("alg", ["TSIT5", "RODAS5", "RODAS5P"])
 @pytest.mark.parametrize("batching", ["plain", "persistent"])
-def test_team_fp64_lockstep_nonstiff(de, oracle, alg, batching):
+@pytest.mark.parametrize("precision", ["fp64", "f32x2"])
+def test_team_lockstep_nonstiff(de, oracle, alg, batching, precision):
+    """FP64 and FP32-pair team kernels take the FP64 oracle's steps."""
     capi = de._capi
     M = de.models.vdp_ring8
     p, u0, t0, tf = ring_inputs(300, 11, -1, 0.5)
     saveat = de.save_grid(0.0, 20.0, 1.0)
     a = getattr(capi, "ALG_" + alg)
     b = capi.BATCH_PERSISTENT if batching == "persistent" else capi.BATCH_PLAIN
-    g = de.solve_arrays(M, opts_for(capi, a, batching=b), p, u0, t0, tf, saveat, capi.SAVE_GRID)
+    g = de.solve_arrays(M, opts_for(capi, a, batching=b, precision=_prec(capi, precision)), p, u0,
+                        t0, tf, saveat, capi.SAVE_GRID)
     r = oracle.solve(capi, M, opts_for(capi, a), p, u0, t0, tf, saveat, capi.SAVE_GRID,
                      nthreads=8)
     assert np.all(g["retcode"] == capi.RET_SUCCESS)
@@ -59,13 +66,15 @@ def test_team_fp64_lockstep_nonstiff(de, oracle, alg, batching):
 
 
 @pytest.mark.parametrize("alg", ["RODAS5", "RODAS5P"])
-def test_team_rodas_stiff_vs_truth(de, oracle, alg):
+@pytest.mark.parametrize("precision", ["fp64", "f32x2"])
+def test_team_rodas_stiff_vs_truth(de, oracle, alg, precision):
     capi = de._capi
     M = de.models.vdp_ring8
     p, u0, t0, tf = ring_inputs(192, 12, 1, 3)  # mu in [10, 1000]
     saveat = de.save_grid(0.0, 20.0, 1.0)
     a = getattr(capi, "ALG_" + alg)
-    g = de.solve_arrays(M, opts_for(capi, a), p, u0, t0, tf, saveat, capi.SAVE_GRID)
+    g = de.solve_arrays(M, opts_for(capi, a, precision=_prec(capi, precision)), p, u0, t0, tf,
+                        saveat, capi.SAVE_GRID)
     assert np.all(g["retcode"] == capi.RET_SUCCESS)
     r = oracle.solve(capi, M, opts_for(capi, a), p, u0, t0, tf, saveat, capi.SAVE_GRID,
                      nthreads=8)
@@ -81,7 +90,8 @@ def test_team_rodas_stiff_vs_truth(de, oracle, alg):
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_auto_partition(de, oracle, precision):
     """AUTO: stiff iff mu > stiff_threshold; non-stiff trajectories run Tsit5
-    (FP32 state in mixed precision), stiff ones Rodas5 in FP64."""
+    (FP32 state in mixed precision), stiff ones Rodas5 (FP64, or FP32-pair
+    stages on an FP64 LU in mixed precision)."""
     capi = de._capi
     M = de.models.vdp_ring8
     p, u0, t0, tf = ring_inputs(400, 13, -1, 2)
@@ -95,9 +105,10 @@ def test_auto_partition(de, oracle, precision):
     assert np.all(g["retcode"] == capi.RET_SUCCESS)
     assert np.array_equal(g["method"][st], np.full(st.sum(), capi.ALG_RODAS5))
     assert np.array_equal(g["method"][~st], np.full((~st).sum(), capi.ALG_TSIT5))
-    # stiff trajectories: FP64 Rodas5 in both precisions, same steps as alone
-    alone = de.solve_arrays(M, opts_for(capi, capi.ALG_RODAS5), p[st], u0[st], t0[st], tf[st],
-                            saveat, capi.SAVE_GRID)
+    # stiff trajectories: the same steps as Rodas5 alone in the stiff precision
+    stiff_prec = capi.PREC_F32X2 if precision == "mixed" else capi.PREC_FP64
+    alone = de.solve_arrays(M, opts_for(capi, capi.ALG_RODAS5, precision=stiff_prec), p[st],
+                            u0[st], t0[st], tf[st], saveat, capi.SAVE_GRID)
     assert np.array_equal(g["naccept"][st], alone["naccept"])
     if precision == "fp64":
         r = oracle.solve(capi, M, opts_for(capi, capi.ALG_TSIT5), p[~st], u0[~st], t0[~st],
