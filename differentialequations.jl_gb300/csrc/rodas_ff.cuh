@@ -262,7 +262,11 @@ struct RodasFF {
       }
     }
     nf += 7;
-    // y1 = U_7 + u_8; error estimate u_8, norm in FP64
+    // y1 = U_7 + u_8; error estimate u_8.  The norm's ratios
+    // u_8 / (abstol + reltol max(|u0|, |y1|)) are FP32 on the leading parts
+    // (as Tsit5FF); their squares accumulate in FP64.
+    const ff as = ff_split(abstol), rs = ff_split(reltol);
+    const float atf = xadd(as.hi, as.lo), rtf = xadd(rs.hi, rs.lo);
     double ms = 0.0;
 #pragma unroll
     for (int c = 0; c < N; ++c) {
@@ -271,7 +275,7 @@ struct RodasFF {
       a.add(s[c]);
       un[c] = a.get();
       const float m = fmaxf(fabsf(uu[c].hi), fabsf(un[c].hi));
-      const double e = f2d_bits(s[c].hi) * rcp64(abstol + reltol * f2d_bits(m));
+      const double e = f2d_bits(__fdiv_rn(s[c].hi, fmaf(rtf, m, atf)));
       ms = fma(e, e, ms);
     }
     return ms * (1.0 / N);
