@@ -2,6 +2,7 @@
 #include "explicit_rk.cuh"
 #include "ff.cuh"
 #include "tsit5_ff.cuh"
+#include "vern7_ff.cuh"
 #include "launch.h"
 
 namespace gbde {
@@ -40,7 +41,7 @@ static cudaError_t dispatch_model(const LaunchCfg& cfg, const KArgs& a, cudaStre
 
 cudaError_t launch_explicit(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
   if (cfg.alg == GBDE_ALG_TSIT5) return dispatch_model<Tsit5A>(cfg, a, s);
-  if (cfg.alg == GBDE_ALG_VERN7) return dispatch_model<Vern7Alg>(cfg, a, s);
+  if (cfg.alg == GBDE_ALG_VERN7) return dispatch_model<Vern7A>(cfg, a, s);
   return cudaErrorNotSupported;
 }
 

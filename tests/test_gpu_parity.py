@@ -372,12 +372,17 @@ def test_rcp64_accuracy(de):
 
 # F32X2: state, stages and right-hand sides as FP32 pairs (~48 bits), FP64 LU,
 # norm and time.  Near-FP64 accuracy: the steps follow the FP64 oracle's and
-# the saved states agree to well inside the tolerance.
+# the saved states agree to well inside the tolerance.  The limit is the
+# error estimate, a sum whose terms cancel to ~reltol: at reltol 1e-10 Vern7's
+# cancels ~10 digits, leaving ~4 in 48-bit pairs (~5.5 in FP64), and about 1%
+# of the linear model's trajectories then take another step sequence than the
+# oracle (measured on GB300: 99th percentile 8x tolerance) -- so the lockstep
+# cases stop at 1e-8 for Vern7.
 @pytest.mark.parametrize("model_name,alg,rt,at", [
     ("robertson", "RODAS5", 1e-6, 1e-10), ("robertson", "RODAS5P", 1e-6, 1e-10),
     ("robertson", "ROSENBROCK23", 1e-6, 1e-10), ("lorenz", "TSIT5", 1e-8, 1e-8),
     ("lorenz", "VERN7", 1e-8, 1e-8), ("lorenz", "RODAS5", 1e-7, 1e-7),
-    ("linear", "TSIT5", 1e-10, 1e-10)])
+    ("linear", "TSIT5", 1e-10, 1e-10), ("linear", "VERN7", 1e-8, 1e-8)])
 def test_f32x2_vs_fp64_oracle(de, oracle, rng, model_name, alg, rt, at):
     capi = de._capi
     model = getattr(de.models, model_name)
