@@ -1,9 +1,10 @@
 // k_rosenbrock.cu -- Rosenbrock23 / Rodas5 / Rodas5P ensemble kernels
 // (one trajectory per thread, W-matrix LU in registers; models with n <= 3).
 // In the F32X2 precision Rodas5 / Rodas5P run the compact pair stepper of
-// rodas_ff.cuh.
+// rodas_ff.cuh and Rosenbrock23 the one of ros23_ff.cuh.
 #include "rosenbrock.cuh"
 #include "rodas_ff.cuh"
+#include "ros23_ff.cuh"
 #include "ff.cuh"
 #include "launch.h"
 
@@ -43,7 +44,7 @@ static cudaError_t dispatch_model(const LaunchCfg& cfg, const KArgs& a, cudaStre
 }
 
 cudaError_t launch_rosenbrock(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
-  if (cfg.alg == GBDE_ALG_ROSENBROCK23) return dispatch_model<Ros23Alg>(cfg, a, s);
+  if (cfg.alg == GBDE_ALG_ROSENBROCK23) return dispatch_model<Ros23A>(cfg, a, s);
   if (cfg.alg == GBDE_ALG_RODAS5) return dispatch_model<Rodas5A>(cfg, a, s);
   if (cfg.alg == GBDE_ALG_RODAS5P) return dispatch_model<Rodas5PA>(cfg, a, s);
   return cudaErrorNotSupported;

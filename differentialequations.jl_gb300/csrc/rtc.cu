@@ -156,7 +156,7 @@ std::string alg_type(int alg, int precision) {
   switch (alg) {
     case GBDE_ALG_TSIT5: return "Tsit5A<GbdeRtcModel, " + T + ">";
     case GBDE_ALG_VERN7: return "Vern7A<GbdeRtcModel, " + T + ">";
-    case GBDE_ALG_ROSENBROCK23: return "Ros23Alg<GbdeRtcModel, " + T + ">";
+    case GBDE_ALG_ROSENBROCK23: return "Ros23A<GbdeRtcModel, " + T + ">";
     case GBDE_ALG_RODAS5:
       return precision == GBDE_PREC_F32X2 ? "RodasFF<GbdeRtcModel, Rodas5Tag>"
                                           : "RodasAlg<GbdeRtcModel, " + T + ", Rodas5Tag>";
@@ -181,7 +181,7 @@ std::string make_source(const UserModelDef* m, int model, const CallbackDef* cb,
        "typedef unsigned short uint16_t; typedef unsigned int uint32_t;\n"
        "typedef unsigned long long uint64_t; typedef unsigned long size_t;\n"
        "#include \"solver.cuh\"\n#include \"explicit_rk.cuh\"\n#include \"rosenbrock.cuh\"\n"
-       "#include \"rodas_ff.cuh\"\n#include \"tsit5_ff.cuh\"\n#include \"vern7_ff.cuh\"\n#include \"dual.cuh\"\nnamespace gbde {\n";
+       "#include \"rodas_ff.cuh\"\n#include \"tsit5_ff.cuh\"\n#include \"vern7_ff.cuh\"\n#include \"ros23_ff.cuh\"\n#include \"dual.cuh\"\nnamespace gbde {\n";
   char buf[256];
   if (m) {
     s += "struct UserModel {\n";
