@@ -96,6 +96,8 @@ template <class T>
 GBDE_HD bool val_finite(T x) {
   return isfinite((double)x);
 }
+// FP32 values test directly: no conversion on the FP64 pipe
+GBDE_HD bool val_finite(float x) { return isfinite(x); }
 
 // Error-free sum (Knuth TwoSum): s + e == a + b exactly.  Used for the
 // compensated time accumulation of the mixed-precision path.

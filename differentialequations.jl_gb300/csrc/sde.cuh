@@ -83,6 +83,107 @@ GBDE_D void finish_sde(const KArgs& a, int64_t i, int ret, int js, int nacc, int
 // ------------------------------------------------------------------ EM
 // Step n covers [t0 + n h, min(t0 + (n+1) h, tf)]; the normal for
 // component c of step n is draw n*N + c of the trajectory's stream.
+
+// End of EM step n in FP64 (as the FP64 loop of em_all computes it): the
+// step is the last one when this test holds.
+GBDE_D bool em_last_step(double t0, double tf, double h, int64_t n) {
+  const double tn1 = t0 + (double)(n + 1) * h;
+  return tn1 * (1.0 + 1e-14) >= tf || tn1 > tf;
+}
+
+// The EM steps of one trajectory with FP32 state (GBDE_PREC_MIXED).  The loop
+// runs on a step counter with no FP64 arithmetic: h and sqrt(h) are FP32
+// constants for every step but the last, whose length tf - t_n is computed
+// once, and the step in which each save point falls is found (a few FP64
+// operations per save point) before the loop reaches it.  The FP64 loop spends
+// ~20 FP64-pipe instructions per step on the same bookkeeping, which bounds it
+// on GB300's narrow FP64 pipe; this one is bound by the normal stream (Philox on
+// the integer pipe, Box-Muller on the MUFU pipe).  Step boundaries are the FP64
+// loop's t0 + n h: a step's length differs from h only by the rounding of
+// those boundaries, below FP32 resolution.
+template <class M>
+__device__ void em_steps_f32(const KArgs& a, int64_t i, double t0, double tf, double h, float* u,
+                             const float* p, int js, NormalStream<float>& ns) {
+  constexpr int N = M::N;
+  constexpr int64_t kNever = 0x7fffffffffffffffll;
+  // index of the last step (-1: no step)
+  int64_t nl = -1;
+  if (t0 < tf) {
+    const double m = (tf - t0) / h;
+    if (!(m <= (double)a.maxiters + 2.0)) {
+      nl = kNever - 1;  // more steps than maxiters: the loop stops at maxiters
+    } else {
+      nl = m > 1.0 ? (int64_t)m - 1 : 0;
+      for (int it = 0; it < 8 && nl > 0 && em_last_step(t0, tf, h, nl - 1); ++it) --nl;
+      for (int it = 0; it < 8 && !em_last_step(t0, tf, h, nl); ++it) ++nl;
+    }
+  }
+  const int64_t nrun = nl + 1 < a.maxiters ? nl + 1 : a.maxiters;
+  // end of step n in FP64, and the step in which save point j falls
+  auto t_end = [&](int64_t n) { return n >= nl ? tf : t0 + (double)(n + 1) * h; };
+  auto save_step = [&](int j) -> int64_t {
+    if (j >= a.n_save) return kNever;
+    const double ts = save_time(a, i, j);
+    if (!(ts <= tf) || nl < 0) return kNever;
+    const double kd = (ts - t0) / h;
+    int64_t k = kd < (double)nl ? (int64_t)kd - 1 : nl;
+    k = k < 0 ? 0 : k;
+    // the estimate is within a step or two; the bounds only matter where h is
+    // below the FP64 resolution of t (the step boundaries then repeat)
+    for (int it = 0; it < 64 && k > 0 && t_end(k - 1) >= ts; ++it) --k;
+    for (int it = 0; it < 64 && k < nl && t_end(k) < ts; ++it) ++k;
+    return k;
+  };
+  const float hT = (float)h, sq = (float)sqrt(h);
+  float hTl = hT, sql = sq;
+  if (nl >= 0 && nl < kNever - 1) {
+    const double hl = tf - (nl > 0 ? t0 + (double)nl * h : t0);
+    hTl = (float)hl;
+    sql = (float)sqrt(hl);
+  }
+  int64_t ks = save_step(js);
+  int ret = GBDE_RET_SUCCESS;
+  int64_t n = 0;
+  for (; n < nrun; ++n) {
+    const bool lastn = n == nl;
+    const float hs = lastn ? hTl : hT, sh = lastn ? sql : sq;
+    float fu[N], gu[N], un[N];
+    M::f(fu, u, p);
+    M::g(gu, u, p);
+#pragma unroll
+    for (int c = 0; c < N; ++c) un[c] = u[c] + fu[c] * hs + gu[c] * (sh * ns.next());
+    while (n == ks) {  // save points in (t_n, t_{n+1}]
+      const double ts = save_time(a, i, js), tn1 = t_end(n);
+      const double tn = n > 0 ? t0 + (double)n * h : t0;
+      if (ts >= tn1) {
+        store_state<N>(a, i, js, un);
+      } else {
+        const float th = (float)((ts - tn) / (tn1 - tn));
+        float tmp[N];
+#pragma unroll
+        for (int c = 0; c < N; ++c) tmp[c] = u[c] + th * (un[c] - u[c]);
+        store_state<N>(a, i, js, tmp);
+      }
+      ++js;
+      ks = save_step(js);
+    }
+    bool fin = true;
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      u[c] = un[c];
+      fin &= isfinite(un[c]);
+    }
+    if (!fin) {
+      ret = GBDE_RET_UNSTABLE;
+      ++n;
+      break;
+    }
+  }
+  if (ret == GBDE_RET_SUCCESS && n < nl + 1) ret = GBDE_RET_MAXITERS;
+  const double t = n == 0 ? t0 : t_end(n - 1);
+  finish_sde<N, float>(a, i, ret, js, (int)n, 0, (int)(2 * n), t, GBDE_ALG_EM, h);
+}
+
 template <class M, class T>
 __device__ void em_all(const KArgs& a) {
   constexpr int N = M::N;
@@ -112,6 +213,10 @@ __device__ void em_all(const KArgs& a) {
     }
     NormalStream<T> ns;
     ns.init(a.seed, (uint64_t)i);
+    if constexpr (sizeof(T) == 4) {
+      em_steps_f32<M>(a, i, t0, tf, h, u, p, js, ns);
+      continue;
+    }
     int ret = GBDE_RET_SUCCESS;
     int64_t n = 0;
     double t = t0;
@@ -232,7 +337,11 @@ struct NoiseStack {
           acc = hs;
         }
       } else {
-        const T sq = (T)sqrt(r);
+        // FP32 state: the square root on the FP32 pipe (GB300's FP64 pipe is
+        // 1/61 of its rate); FP64 state keeps the FP64 square root
+        T sq;
+        if constexpr (sizeof(T) == 4) sq = __fsqrt_rn((float)r);
+        else sq = (T)sqrt(r);
 #pragma unroll
         for (int c = 0; c < N; ++c) {
           w[c] += sq * ns.next();
@@ -292,6 +401,7 @@ __device__ void sri_all(const KArgs& a) {
     int ret = GBDE_RET_DEFAULT;
     int64_t iters = 0;
     float lqold = a.ctl.lqoldinit;
+    const float atf = (float)a.abstol, rtf = (float)a.reltol;
     if (!(t < tf)) ret = GBDE_RET_SUCCESS;
     while (ret == GBDE_RET_DEFAULT) {
       const double rem = tf - t;
@@ -303,8 +413,19 @@ __device__ void sri_all(const KArgs& a) {
       }
       T dW[N], dZ[N];
       stk.take(hs, dW, dZ, ns);
-      // ---- SRIW1 step
-      const T hT = (T)hs, sqh = (T)sqrt(hs), ih = (T)(1.0 / hs), isqh = (T)(1.0 / sqrt(hs));
+      // ---- SRIW1 step (with FP32 state the step's powers are FP32 operations)
+      T hT, sqh, ih, isqh;
+      if constexpr (sizeof(T) == 4) {
+        hT = (float)hs;
+        sqh = __fsqrt_rn(hT);
+        ih = __frcp_rn(hT);
+        isqh = __frcp_rn(sqh);
+      } else {
+        hT = (T)hs;
+        sqh = (T)sqrt(hs);
+        ih = (T)(1.0 / hs);
+        isqh = (T)(1.0 / sqrt(hs));
+      }
       T F1[N], F2[N], G1[N], G2[N], G3[N], G4[N], Y[N], un[N], err[N];
       M::f(F1, u, p);
       M::g(G1, u, p);
@@ -343,7 +464,9 @@ __device__ void sri_all(const KArgs& a) {
                      (T(b4_1) * G1[c] + T(b4_2) * G2[c] + T(b4_3) * G3[c] + T(b4_4) * G4[c]) * I111[c] * ih;
         err[c] = (ed < T(0) ? -ed : ed) + (en < T(0) ? -en : en);
       }
-      const double ms = err_ms<N>(err, u, un, a.abstol, a.reltol);  // EEst^2
+      double ms;  // EEst^2
+      if constexpr (sizeof(T) == 4) ms = err_ms_f32<N>(err, u, un, atf, rtf);
+      else ms = err_ms<N>(err, u, un, a.abstol, a.reltol);
       ++iters;
       if (!a.adaptive || ms <= 1.0) {
         double tnew;
@@ -377,7 +500,7 @@ __device__ void sri_all(const KArgs& a) {
 #pragma unroll
         for (int c = 0; c < N; ++c) {
           u[c] = un[c];
-          fin &= isfinite((double)un[c]);
+          fin &= val_finite(un[c]);
         }
         t = tnew;
         if (nacc == 0) dt1 = hs;

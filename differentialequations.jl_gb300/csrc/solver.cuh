@@ -183,6 +183,21 @@ GBDE_HD double err_ms(const T* err, const T* u, const T* unew, double abstol, do
   return s * (1.0 / N);
 }
 
+// err_ms with FP32 state: the ratios err_c / (abstol + reltol max(|u_c|,
+// |u1_c|)) are FP32 operations, their squares accumulate in FP64.
+template <int N>
+GBDE_D double err_ms_f32(const float* err, const float* u, const float* unew, float atf,
+                         float rtf) {
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    const float m = fmaxf(fabsf(u[c]), fabsf(unew[c]));
+    const double e = f2d_bits(__fdiv_rn(err[c], fmaf(rtf, m, atf)));
+    s = fma(e, e, s);
+  }
+  return s * (1.0 / N);
+}
+
 template <int N, class T>
 GBDE_HD double err_norm(const T* err, const T* u, const T* unew, double abstol, double reltol) {
   double s = 0.0;

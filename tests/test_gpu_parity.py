@@ -181,6 +181,32 @@ def test_em_fp32_on_fp32_stream(de, oracle, rng):
     assert rel <= 1e-4, rel
 
 
+def test_em_fp32_step_bookkeeping(de, oracle, rng):
+    """The FP32 EM loop counts steps instead of accumulating FP64 time: the
+    step count, the partial last step, save points between step boundaries
+    and the maxiters exit must be the FP64 loop's (the oracle's)."""
+    capi = de._capi
+    model = de.models.lotka_volterra
+    N = 600
+    p, u0, _, _ = make_inputs(de, model, N, rng)
+    t0 = rng.uniform(-0.5, 0.5, N)
+    tf = t0 + rng.uniform(0.05, 1.5, N)
+    frac = np.sort(rng.uniform(0.0, 1.0, (N, 9)), axis=1)
+    saveat = np.c_[t0, t0[:, None] + frac * (tf - t0)[:, None], tf]
+    for maxiters in (10 ** 6, 60):
+        g, r, _ = run_both(de, oracle, model, capi.ALG_EM, p, u0, t0, tf, saveat,
+                           capi.SAVE_PER_TRAJ, precision="mixed", noise_f32=True, u_dtype="f32",
+                           dt=1e-2, seed=5, maxiters=maxiters)
+        assert np.array_equal(g["retcode"], r["retcode"])
+        assert np.array_equal(g["naccept"], r["naccept"])
+        np.testing.assert_allclose(g["t_end"], r["t_end"], rtol=1e-15, atol=0)
+        ok = ~np.isnan(r["u"])
+        assert np.array_equal(np.isnan(g["u"]), ~ok)
+        rel = np.max(np.abs(g["u"][ok] - r["u"][ok]) / np.abs(r["u"][ok]))
+        assert rel <= 1e-4, rel
+    assert np.any(r["retcode"] == capi.RET_MAXITERS) and np.any(r["retcode"] == capi.RET_SUCCESS)
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_sosri_parity(de, oracle, rng, precision):
     capi = de._capi
