@@ -171,18 +171,6 @@ GBDE_D void store_state(const KArgs& a, int64_t i, int j, const T* v) {
 // Mean square of the scaled error, ms = EEst^2 (the accept test is ms <= 1).
 // Each err_c / sc_c uses the Newton-refined reciprocal of controller.h
 // instead of an IEEE division.
-template <int N, class T>
-GBDE_HD double err_ms(const T* err, const T* u, const T* unew, double abstol, double reltol) {
-  double s = 0.0;
-#pragma unroll
-  for (int c = 0; c < N; ++c) {
-    const double sc = abstol + reltol * fmax(fabs((double)u[c]), fabs((double)unew[c]));
-    const double e = (double)err[c] * rcp64(sc);
-    s += e * e;
-  }
-  return s * (1.0 / N);
-}
-
 // err_ms with FP32 state: the ratios err_c / (abstol + reltol max(|u_c|,
 // |u1_c|)) are FP32 operations, their squares accumulate in FP64.
 template <int N>
@@ -194,6 +182,22 @@ GBDE_D double err_ms_f32(const float* err, const float* u, const float* unew, fl
     const float m = fmaxf(fabsf(u[c]), fabsf(unew[c]));
     const double e = f2d_bits(__fdiv_rn(err[c], fmaf(rtf, m, atf)));
     s = fma(e, e, s);
+  }
+  return s * (1.0 / N);
+}
+
+template <int N, class T>
+GBDE_HD double err_ms(const T* err, const T* u, const T* unew, double abstol, double reltol) {
+#if defined(__CUDA_ARCH__)
+  if constexpr (sizeof(T) == 4)  // FP32 state
+    return err_ms_f32<N>(err, u, unew, (float)abstol, (float)reltol);
+#endif
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    const double sc = abstol + reltol * fmax(fabs((double)u[c]), fabs((double)unew[c]));
+    const double e = (double)err[c] * rcp64(sc);
+    s += e * e;
   }
   return s * (1.0 / N);
 }

@@ -44,6 +44,22 @@ struct Team {
   }
 };
 
+// This lane's squared scaled error (the team sums them): the ratio
+// err / (abstol + reltol max(|u|, |u1|)) is FP32 for FP32 state (the square is
+// formed and summed in FP64), FP64 otherwise.
+template <class T>
+GBDE_D double lane_err2(T err, T u, T un, double abstol, double reltol) {
+  if constexpr (sizeof(T) == 4) {
+    const float m = fmaxf(fabsf(u), fabsf(un));
+    const double e = f2d_bits(__fdiv_rn(err, fmaf((float)reltol, m, (float)abstol)));
+    return e * e;
+  } else {
+    const double sc = abstol + reltol * fmax(fabs((double)u), fabs((double)un));
+    const double e = (double)err * rcp64(sc);
+    return e * e;
+  }
+}
+
 // ------------------------------------------------------------- team LU
 // Row-distributed LU of W (16 x 16) with partial pivoting.  Lane r keeps its
 // row in a[]: after factor(), a[c] for c < step holds the multipliers (L) and
@@ -213,9 +229,7 @@ struct TeamRodas {
     const T s8 = (T)W.solve((double)(rhs(y, p, tm) + iht * (T(K::C81) * s1 + T(K::C82) * s2 + T(K::C83) * s3 + T(K::C84) * s4 + T(K::C85) * s5 + T(K::C86) * s6 + T(K::C87) * s7)), tm);
     nf += 7;
     un = y + s8;
-    const double sc = abstol + reltol * fmax(fabs((double)uu), fabs((double)un));
-    const double e = (double)s8 * rcp64(sc);
-    return tm.sum(e * e) * (1.0 / TEAM);
+    return tm.sum(lane_err2(s8, uu, un, abstol, reltol)) * (1.0 / TEAM);
   }
 
   GBDE_D T interp(double th, double) const {  // as RodasAlg::interp
@@ -417,9 +431,7 @@ struct TeamTsit5 {
     nf += 6;
     const T err = h * (T(bt1) * k1 + T(bt2) * k2 + T(bt3) * k3 + T(bt4) * k4 + T(bt5) * k5 +
                        T(bt6) * k6 + T(bt7) * k7);
-    const double sc = abstol + reltol * fmax(fabs((double)uu), fabs((double)un));
-    const double e = (double)err * rcp64(sc);
-    return tm.sum(e * e) * (1.0 / TEAM);
+    return tm.sum(lane_err2(err, uu, un, abstol, reltol)) * (1.0 / TEAM);
   }
 
   GBDE_D T interp(double th, double dt) const {
@@ -520,7 +532,7 @@ __device__ void integrate_team(const KArgs& a) {
       const double rem = tf - t;
       double h = dt;
       bool last = false;
-      if (h * (1.0 + 1e-10) >= rem) {
+      if (ord_bits(h * (1.0 + 1e-10)) >= ord_bits(rem)) {
         h = rem;
         last = true;
       }
@@ -528,14 +540,18 @@ __device__ void integrate_team(const KArgs& a) {
       ++iters;
       if (!a.adaptive || mag_bits(ms) <= 0x3FF0000000000000ull) {  // ms <= 1 (integer pipe)
         double dtnew = h;
-        if (a.adaptive) dtnew = h * (double)ctl_accept(a.ctl, ms, lqold);
+        if (a.adaptive) dtnew = h * f2d_bits(ctl_accept(a.ctl, ms, lqold));
         double tnew;
         if (last) {
           tnew = tf;
           tlo = 0.0;
         } else if (MIXED) {
-          double s, e;
-          two_sum(t, h, s, e);
+          // Fast2Sum on the operands ordered by magnitude (integer compare),
+          // as integrate_all
+          const bool tb = mag_bits(t) >= mag_bits(h);
+          const double big = tb ? t : h, small = tb ? h : t;
+          const double s = big + small;
+          double e = small - (s - big);
           e += tlo;
           tnew = s + e;
           tlo = e - (tnew - s);
@@ -554,16 +570,16 @@ __device__ void integrate_team(const KArgs& a) {
         t = tnew;
         if (nacc == 0) dt1 = h;
         ++nacc;
-        if (__any_sync(tm.mask, !isfinite((double)alg.u()))) ret = GBDE_RET_UNSTABLE;
+        if (__any_sync(tm.mask, !val_finite(alg.u()))) ret = GBDE_RET_UNSTABLE;
         else if (last) ret = GBDE_RET_SUCCESS;
-        dt = a.dtmax > 0.0 ? fmin(dtnew, a.dtmax) : dtnew;
+        dt = a.dtmax > 0.0 && ord_bits(dtnew) > ord_bits(a.dtmax) ? a.dtmax : dtnew;
       } else {
         ++nrej;
-        dt = h * (double)ctl_reject(a.ctl, ms);
+        dt = h * f2d_bits(ctl_reject(a.ctl, ms));
       }
       if (ret == GBDE_RET_DEFAULT) {
         if (iters >= a.maxiters) ret = GBDE_RET_MAXITERS;
-        else if (a.adaptive && (dt < a.dtmin || dt <= 4.0 * 2.220446049250313e-16 * fabs(t)))
+        else if (a.adaptive && dt_too_small(dt, a.dtmin, t))
           ret = GBDE_RET_DTLESSTHANMIN;
         else if (a.timeout_ns && (iters & 31) == 0) {
           // lane 0's clock decides for the team
