@@ -407,7 +407,7 @@ __device__ void sri_all(const KArgs& a) {
       const double rem = tf - t;
       double hs = h;
       bool last = false;
-      if (hs * (1.0 + 1e-10) >= rem) {
+      if (ord_bits(hs * (1.0 + 1e-10)) >= ord_bits(rem)) {
         hs = rem;
         last = true;
       }
@@ -468,24 +468,31 @@ __device__ void sri_all(const KArgs& a) {
       if constexpr (sizeof(T) == 4) ms = err_ms_f32<N>(err, u, un, atf, rtf);
       else ms = err_ms<N>(err, u, un, a.abstol, a.reltol);
       ++iters;
-      if (!a.adaptive || ms <= 1.0) {
+      // ms <= 1 (ms >= 0; NaN rejects) and the other bookkeeping compares on
+      // the integer pipe, as integrate_all
+      if (!a.adaptive || mag_bits(ms) <= 0x3FF0000000000000ull) {
         double tnew;
         if (last) {
           tnew = tf;
           tlo = 0.0;
         } else if (MIXED) {
-          double s, e;
-          two_sum(t, hs, s, e);
+          // Fast2Sum on the operands ordered by magnitude
+          const bool tb = mag_bits(t) >= mag_bits(hs);
+          const double big = tb ? t : hs, small = tb ? hs : t;
+          const double s = big + small;
+          double e = small - (s - big);
           e += tlo;
           tnew = s + e;
           tlo = e - (tnew - s);
         } else {
           tnew = t + hs;
         }
+        const uint64_t tnew_o = ord_bits(tnew);
         while (js < a.n_save) {
           const double ts = save_time(a, i, js);
-          if (!(ts <= tnew)) break;
-          if (ts >= tnew) {
+          const uint64_t ts_o = ord_bits(ts);
+          if (ts_o > tnew_o) break;
+          if (ts_o == tnew_o) {
             store_state<N>(a, i, js, un);
           } else {
             const T th = (T)(((ts - t) - tlo) / hs);
@@ -507,16 +514,16 @@ __device__ void sri_all(const KArgs& a) {
         ++nacc;
         if (!fin) ret = GBDE_RET_UNSTABLE;
         else if (last) ret = GBDE_RET_SUCCESS;
-        if (a.adaptive) h = hs * (double)ctl_accept(a.ctl, ms, lqold);
+        if (a.adaptive) h = hs * f2d_bits(ctl_accept(a.ctl, ms, lqold));
       } else {
         ++nrej;
         stk.push(hs, dW, dZ);
-        h = hs * (double)ctl_reject(a.ctl, ms);
+        h = hs * f2d_bits(ctl_reject(a.ctl, ms));
       }
-      if (a.dtmax > 0.0) h = fmin(h, a.dtmax);
+      if (a.dtmax > 0.0 && ord_bits(h) > ord_bits(a.dtmax)) h = a.dtmax;
       if (ret == GBDE_RET_DEFAULT) {
         if (iters >= a.maxiters) ret = GBDE_RET_MAXITERS;
-        else if (a.adaptive && (h < a.dtmin || h <= 4.0 * 2.220446049250313e-16 * fabs(t)))
+        else if (a.adaptive && dt_too_small(h, a.dtmin, t))
           ret = GBDE_RET_DTLESSTHANMIN;
       }
     }
