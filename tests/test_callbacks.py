@@ -103,20 +103,24 @@ def _ball_truth(h0, g, e, ts):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("alg", ["Tsit5", "Vern7"])
-def test_bouncing_ball_events_exact(capi, de, alg):
+@pytest.mark.parametrize("precision", ["fp64", "f32x2"])
+def test_bouncing_ball_events_exact(capi, de, alg, precision):
     """Impacts located on the dense output: the saved states follow the
     analytic piecewise-quadratic solution through several bounces (the span
-    ends well before the impacts accumulate: t1 (1 + 2e/(1-e)) >= 2.3)."""
+    ends well before the impacts accumulate: t1 (1 + 2e/(1-e)) >= 2.3), with
+    the FP64 steppers and with the compact FP32-pair ones (their dense output
+    at arbitrary theta and their restart after each affect)."""
     rng = np.random.default_rng(3)
     N = 512
     g = rng.uniform(5.0, 15.0, N)
     e = rng.uniform(0.8, 0.9, N)
     h0 = rng.uniform(0.5, 2.0, N)
-    ball = de.ODEFunction(BALL_F, 2, 2, name="ball_" + alg)
+    ball = de.ODEFunction(BALL_F, 2, 2, name="ball_%s_%s" % (alg, precision))
     cb = de.ContinuousCallback("g = u[0];", BOUNCE)
     ens = de.EnsembleProblem(de.ODEProblem(ball, [1.0, 0.0], (0.0, 1.0), [9.8, 0.8]),
                              batch=lambda prob, n: {"p": np.c_[g, e], "u0": np.c_[h0, np.zeros(N)]})
-    sol = de.solve(ens, getattr(de, alg)(), de.EnsembleGB300(batching="persistent"),
+    sol = de.solve(ens, getattr(de, alg)(),
+                   de.EnsembleGB300(batching="persistent", precision=precision),
                    trajectories=N, saveat=0.05, reltol=1e-10, abstol=1e-10, callback=cb)
     assert sol.converged
     ts = de.save_grid(0.0, 1.0, 0.05)

@@ -146,6 +146,33 @@ def test_user_lorenz_tsit5_matches_builtin(capi, de, oracle):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("alg", ["TSIT5", "VERN7", "ROSENBROCK23"])
+def test_user_model_f32x2_steppers(capi, de, oracle, alg):
+    """The compact FP32-pair steppers compiled at run time around a user f
+    (Rosenbrock23 with the dual-number Jacobian) take the FP64 oracle's steps."""
+    N = 2000
+    if alg == "ROSENBROCK23":
+        m = de.ODEFunction(ROBERTSON_F, 3, 3, name="robertson_user_ros23_ff")
+        model, (p, u0, t0, tf, sv), kind = de.models.robertson, _robertson(N, 9), capi.SAVE_PER_TRAJ
+        rt, at = 1e-6, 1e-10
+    else:
+        m = de.ODEFunction(LORENZ_F, 3, 3, name="lorenz_user_ff_" + alg.lower())
+        rng = np.random.default_rng(6)
+        p = np.array([10.0, 28.0, 8.0 / 3.0]) * rng.uniform(0.9, 1.1, (N, 3))
+        u0, t0, tf = np.tile([1.0, 0.0, 0.0], (N, 1)), np.zeros(N), np.ones(N)
+        model, sv, kind = de.models.lorenz, de.save_grid(0.0, 1.0, 0.1), capi.SAVE_GRID
+        rt, at = 1e-8, 1e-8
+    a = getattr(capi, "ALG_" + alg)
+    r = de.solve_arrays(m, _opts(capi, a, rt, at, precision=capi.PREC_F32X2), p, u0, t0, tf, sv,
+                        kind)
+    assert np.all(r["retcode"] == capi.RET_SUCCESS)
+    ref = oracle.solve(capi, model, _opts(capi, a, rt, at), p, u0, t0, tf, sv, kind, nthreads=8)
+    e = (np.abs(r["u"] - ref["u"]) / (at + rt * np.abs(ref["u"]))).max(axis=(1, 2))
+    assert np.percentile(e, 99) <= 0.1 and e.max() <= 10.0, (np.percentile(e, 99), e.max())
+    assert np.mean(r["naccept"] == ref["naccept"]) >= 0.99
+
+
+@pytest.mark.gpu
 def test_user_pendulum_vs_scipy(capi, de):
     """A model the library does not build in (damped pendulum with sin):
     Tsit5 and Rodas5 with the dual-number Jacobian (chain rule through sin),
