@@ -238,7 +238,7 @@ GBDE_API int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob,
  * as a CUDA graph; gbde_graph_launch replays it on the context's stream.
  * The graph keeps the problem's and outputs' device pointers: refill the
  * input arrays in place between launches.  No counterpart in the reference
- * (the spec batching: repeated ensembles at launch-free cost).
+ * (batching of repeated ensembles at launch-free cost).
  * GBDE_ALG_AUTO cannot be captured (it sizes its launches on the host). */
 typedef struct gbde_graph gbde_graph;
 GBDE_API int gbde_graph_create(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts* opts,
