@@ -8,13 +8,14 @@ namespace gbde {
 
 // Resident CTAs of 128 threads per SM each team stepper is compiled for: the
 // Rodas steppers are latency-bound on their broadcast chains (LU, triangular
-// solves), so 3 CTAs (<= 168 registers) beat 2 with more registers.
+// solves), so more resident warps beat more registers -- 3 CTAs (<= 168
+// registers) for the FP64 stepper, 4 (<= 128, no spills) for the pair one.
 template <class Alg> struct TeamMinBlocks { static constexpr int v = 1; };
 template <class M, class T, class Tag> struct TeamMinBlocks<TeamRodas<M, T, Tag>> {
   static constexpr int v = 3;
 };
 template <class M, class Tag> struct TeamMinBlocks<TeamRodasFF<M, Tag>> {
-  static constexpr int v = 3;
+  static constexpr int v = 4;
 };
 
 template <class Alg, class M, class T, bool MIXED>
