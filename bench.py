@@ -250,6 +250,8 @@ def run_other(args, de):
     dptr = [torch.from_numpy(a).to(dev) for a in host]
     ctx = capi.context(0)
     peak64, peak32 = ctx.fma_peak(0), ctx.fma_peak(1)
+    # the SDE kernels' bound: the FP32 normal stream (Philox + Box-Muller)
+    normal_peak = ctx.fma_peak(2) * 1e12 if ekind == "sde" else None
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
 
     def timed(o, dt, K, W, **kw):
@@ -353,6 +355,17 @@ def run_other(args, de):
             "all_success": bool(np.all(res["chosen"]["retcode"] == capi.RET_SUCCESS)),
             "fp64_peak_tflops": peak64, "fp32_peak_tflops": peak32,
             "clocks": clk.summary(), "cpu_baseline": cpu}
+    if args.workload == "lv_em":
+        # EM draws one normal per state component per step: exact count
+        normals = float(res["chosen"]["naccept"].astype(np.float64).sum()) * 2.0
+        achieved = normals / (chosen_ms * 1e-3)
+        line["roofline"] = {"bound": "FP32 normal stream (Philox4x32-10 on the integer pipe, "
+                                     "Box-Muller on the MUFU pipe)",
+                            "achieved": achieved, "peak": normal_peak, "unit": "normals/s",
+                            "frac": achieved / normal_peak,
+                            "peak_source": "in-run normal-stream microbenchmark "
+                                           "(gbde_measure_fma_peak kind 2)",
+                            "traffic": None}
     print(json.dumps(line))
 
 

@@ -1,10 +1,13 @@
-// peaks.cu -- FMA-pipe throughput microbenchmark (the roofline denominator
-// for the FP64 / FP32 solver kernels).  Each thread runs 16 independent FMA
-// chains so that the pipe, not the dependency latency, is the limit.
+// peaks.cu -- throughput microbenchmarks, the roofline denominators of the
+// solver kernels: the FP64 / FP32 FMA pipes (each thread runs 16 independent
+// FMA chains, so that the pipe, not the dependency latency, is the limit) and
+// the rate of the SDE kernels' normal stream (Philox4x32-10 on the integer
+// pipe, Box-Muller on the MUFU pipe), generated exactly as the kernels do.
 #include <cstring>
 #include <cuda_runtime.h>
 #include "../../include/gbde.h"
 #include "controller.h"
+#include "philox.h"
 
 namespace gbde {
 
@@ -23,6 +26,19 @@ __global__ void __launch_bounds__(256) k_fma_peak(T* out, int iters, T a, T b) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// Each thread draws `iters` blocks of four FP32 normals from its own stream
+// (the layout of NormalStream<float> in sde.cuh) and keeps their sum.
+__global__ void __launch_bounds__(256) k_normal_peak(float* out, int iters, uint64_t seed) {
+  const uint64_t tr = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float acc = 0.0f;
+  for (int b = 0; b < iters; ++b) {
+    float z[4];
+    philox_normal_quad_f32(seed, tr, (uint64_t)b, z);
+    acc += (z[0] + z[1]) + (z[2] + z[3]);
+  }
+  out[tr] = acc;
+}
+
 }  // namespace gbde
 
 namespace gbde {
@@ -30,14 +46,15 @@ namespace gbde {
 int ctx_device(const gbde_ctx* ctx, int* device, int* num_sms, cudaStream_t* stream);
 }  // namespace gbde
 
+// kind: 0 = FP64 FMA, 1 = FP32 FMA (T the FMA type), 2 = FP32 normals (T = float)
 template <class T>
-static int run_peak(gbde_ctx* ctx, double* tflops) {
+static int run_peak(gbde_ctx* ctx, double* tflops, int kind) {
   int dev = 0, sms = 0;
   cudaStream_t s = nullptr;
   if (gbde::ctx_device(ctx, &dev, &sms, &s) != GBDE_OK) return GBDE_ERR_INVALID;
   cudaSetDevice(dev);
   const int block = 256, grid = sms * 8;
-  const int iters = sizeof(T) == 8 ? 2048 : 16384;
+  const int iters = kind == 2 ? 256 : (sizeof(T) == 8 ? 2048 : 16384);
   T* out = nullptr;
   if (cudaMalloc(&out, (size_t)grid * block * sizeof(T)) != cudaSuccess) return GBDE_ERR_NOMEM;
   cudaEvent_t e0, e1;
@@ -46,7 +63,10 @@ static int run_peak(gbde_ctx* ctx, double* tflops) {
   float best = 1e30f;
   for (int rep = 0; rep < 5; ++rep) {
     cudaEventRecord(e0, s);
-    gbde::k_fma_peak<T><<<grid, block, 0, s>>>(out, iters, (T)0.999999, (T)1e-7);
+    if (kind == 2)
+      gbde::k_normal_peak<<<grid, block, 0, s>>>((float*)out, iters, 20261204ull + rep);
+    else
+      gbde::k_fma_peak<T><<<grid, block, 0, s>>>(out, iters, (T)0.999999, (T)1e-7);
     cudaEventRecord(e1, s);
     cudaEventSynchronize(e1);
     float ms = 0.f;
@@ -58,14 +78,16 @@ static int run_peak(gbde_ctx* ctx, double* tflops) {
   cudaEventDestroy(e1);
   cudaFree(out);
   if (err != cudaSuccess) return GBDE_ERR_CUDA;
-  const double flops = 2.0 * 16.0 * (double)iters * grid * block;
-  *tflops = flops / (best * 1e-3) / 1e12;
+  // FMA = 2 flops; a normal counts as one unit
+  const double work = (kind == 2 ? 4.0 : 2.0 * 16.0) * (double)iters * grid * block;
+  *tflops = work / (best * 1e-3) / 1e12;
   return GBDE_OK;
 }
 
 extern "C" int gbde_measure_fma_peak(gbde_ctx* ctx, int32_t kind, double* tflops) {
-  if (!ctx || !tflops || (kind != 0 && kind != 1)) return GBDE_ERR_INVALID;
-  return kind == 0 ? run_peak<double>(ctx, tflops) : run_peak<float>(ctx, tflops);
+  if (!ctx || !tflops || kind < 0 || kind > 2) return GBDE_ERR_INVALID;
+  if (kind == 0) return run_peak<double>(ctx, tflops, 0);
+  return run_peak<float>(ctx, tflops, kind);
 }
 
 // ---- self-check of rcp64 (controller.h) against the IEEE division

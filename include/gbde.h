@@ -310,7 +310,10 @@ GBDE_API int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_op
                                 gbde_outputs* out, void* stream);
 
 /* Measure the device's FP64 / FP32 FMA throughput (TFLOP/s, FMA = 2 flops)
- * with a dependent-chain-free FMA loop; kind 0 = FP64, 1 = FP32. */
+ * with a dependent-chain-free FMA loop; kind 0 = FP64, 1 = FP32.  kind 2
+ * measures the rate of the SDE kernels' FP32 normal stream (Philox4x32-10 and
+ * Box-Muller, as gbde_philox_normals defines it) in 10^12 normals/s.  No
+ * counterpart in the reference (roofline denominators for this library). */
 GBDE_API int gbde_measure_fma_peak(gbde_ctx* ctx, int32_t kind, double* tflops);
 
 /* ---- learned step-size / stiffness / cost predictor ----------------------
