@@ -144,14 +144,44 @@ __device__ void em_steps_f32(const KArgs& a, int64_t i, double t0, double tf, do
   int64_t ks = save_step(js);
   int ret = GBDE_RET_SUCCESS;
   int64_t n = 0;
+  // The stream's draws in NormalStream order (draw d is normal d % 4 of Philox
+  // block d / 4), held in registers: z0 is the next draw and the rest shift
+  // down, so no run-time index puts the block in local memory.  The state and
+  // parameters are register copies for the same reason.
+  (void)ns;
+  float z0 = 0.0f, z1 = 0.0f, z2 = 0.0f, z3 = 0.0f;
+  int left = 0;
+  uint64_t blk = 0;
+  auto draw = [&]() -> float {
+    if (left == 0) {
+      float q[4];
+      philox_normal_quad_f32(a.seed, (uint64_t)i, blk++, q);
+      z0 = q[0];
+      z1 = q[1];
+      z2 = q[2];
+      z3 = q[3];
+      left = 4;
+    }
+    const float z = z0;
+    z0 = z1;
+    z1 = z2;
+    z2 = z3;
+    --left;
+    return z;
+  };
+  float ur[N], pr[M::NP];
+#pragma unroll
+  for (int c = 0; c < N; ++c) ur[c] = u[c];
+#pragma unroll
+  for (int k = 0; k < M::NP; ++k) pr[k] = p[k];
   for (; n < nrun; ++n) {
     const bool lastn = n == nl;
     const float hs = lastn ? hTl : hT, sh = lastn ? sql : sq;
     float fu[N], gu[N], un[N];
-    M::f(fu, u, p);
-    M::g(gu, u, p);
+    M::f(fu, ur, pr);
+    M::g(gu, ur, pr);
 #pragma unroll
-    for (int c = 0; c < N; ++c) un[c] = u[c] + fu[c] * hs + gu[c] * (sh * ns.next());
+    for (int c = 0; c < N; ++c) un[c] = ur[c] + fu[c] * hs + gu[c] * (sh * draw());
     while (n == ks) {  // save points in (t_n, t_{n+1}]
       const double ts = save_time(a, i, js), tn1 = t_end(n);
       const double tn = n > 0 ? t0 + (double)n * h : t0;
@@ -161,7 +191,7 @@ __device__ void em_steps_f32(const KArgs& a, int64_t i, double t0, double tf, do
         const float th = (float)((ts - tn) / (tn1 - tn));
         float tmp[N];
 #pragma unroll
-        for (int c = 0; c < N; ++c) tmp[c] = u[c] + th * (un[c] - u[c]);
+        for (int c = 0; c < N; ++c) tmp[c] = ur[c] + th * (un[c] - ur[c]);
         store_state<N>(a, i, js, tmp);
       }
       ++js;
@@ -170,7 +200,7 @@ __device__ void em_steps_f32(const KArgs& a, int64_t i, double t0, double tf, do
     bool fin = true;
 #pragma unroll
     for (int c = 0; c < N; ++c) {
-      u[c] = un[c];
+      ur[c] = un[c];
       fin &= isfinite(un[c]);
     }
     if (!fin) {
