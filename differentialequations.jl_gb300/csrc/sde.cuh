@@ -29,35 +29,47 @@
 namespace gbde {
 
 
-// Cached reader of one trajectory's normal stream.
+// Reader of one trajectory's normal stream: draw d is normal d % PER of
+// Philox block d / PER (PER = 4 FP32 or 2 FP64 normals per block).  The
+// unused normals of the current block sit in registers with the next one
+// first and shift down on each draw, so no run-time index puts them in local
+// memory.
 template <class T>
 struct NormalStream {
-  uint64_t seed, traj, d, blk;
-  T buf[4];
+  uint64_t seed, traj, blk;  // blk: the next block to generate
+  T z0, z1, z2, z3;
+  int left;                  // unused normals of the current block
   GBDE_D void init(uint64_t s, uint64_t tr) {
     seed = s;
     traj = tr;
-    d = 0;
-    blk = ~0ull;
+    blk = 0;
+    left = 0;
   }
   GBDE_D T next() {
-    constexpr int PER = sizeof(T) == 8 ? 2 : 4;
-    const uint64_t b = d / PER;
-    if (b != blk) {
+    if (left == 0) {
       if constexpr (sizeof(T) == 8) {
-        double z0, z1;
-        philox_normal_pair_f64(seed, traj, b, z0, z1);
-        buf[0] = (T)z0;
-        buf[1] = (T)z1;
+        double a, b;
+        philox_normal_pair_f64(seed, traj, blk, a, b);
+        z0 = (T)a;
+        z1 = (T)b;
+        z2 = z3 = T(0);
+        left = 2;
       } else {
-        float z[4];
-        philox_normal_quad_f32(seed, traj, b, z);
-        buf[0] = z[0]; buf[1] = z[1]; buf[2] = z[2]; buf[3] = z[3];
+        float q[4];
+        philox_normal_quad_f32(seed, traj, blk, q);
+        z0 = q[0];
+        z1 = q[1];
+        z2 = q[2];
+        z3 = q[3];
+        left = 4;
       }
-      blk = b;
+      ++blk;
     }
-    const T z = buf[d % PER];
-    ++d;
+    const T z = z0;
+    z0 = z1;
+    z1 = z2;
+    z2 = z3;
+    --left;
     return z;
   }
 };
@@ -144,31 +156,8 @@ __device__ void em_steps_f32(const KArgs& a, int64_t i, double t0, double tf, do
   int64_t ks = save_step(js);
   int ret = GBDE_RET_SUCCESS;
   int64_t n = 0;
-  // The stream's draws in NormalStream order (draw d is normal d % 4 of Philox
-  // block d / 4), held in registers: z0 is the next draw and the rest shift
-  // down, so no run-time index puts the block in local memory.  The state and
-  // parameters are register copies for the same reason.
-  (void)ns;
-  float z0 = 0.0f, z1 = 0.0f, z2 = 0.0f, z3 = 0.0f;
-  int left = 0;
-  uint64_t blk = 0;
-  auto draw = [&]() -> float {
-    if (left == 0) {
-      float q[4];
-      philox_normal_quad_f32(a.seed, (uint64_t)i, blk++, q);
-      z0 = q[0];
-      z1 = q[1];
-      z2 = q[2];
-      z3 = q[3];
-      left = 4;
-    }
-    const float z = z0;
-    z0 = z1;
-    z1 = z2;
-    z2 = z3;
-    --left;
-    return z;
-  };
+  // register copies of the state and parameters (no pointer into the
+  // caller's arrays inside the loop)
   float ur[N], pr[M::NP];
 #pragma unroll
   for (int c = 0; c < N; ++c) ur[c] = u[c];
@@ -181,7 +170,7 @@ __device__ void em_steps_f32(const KArgs& a, int64_t i, double t0, double tf, do
     M::f(fu, ur, pr);
     M::g(gu, ur, pr);
 #pragma unroll
-    for (int c = 0; c < N; ++c) un[c] = ur[c] + fu[c] * hs + gu[c] * (sh * draw());
+    for (int c = 0; c < N; ++c) un[c] = ur[c] + fu[c] * hs + gu[c] * (sh * ns.next());
     while (n == ks) {  // save points in (t_n, t_{n+1}]
       const double ts = save_time(a, i, js), tn1 = t_end(n);
       const double tn = n > 0 ? t0 + (double)n * h : t0;
