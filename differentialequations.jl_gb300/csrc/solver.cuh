@@ -328,6 +328,16 @@ GBDE_D bool cb_crossed(double g0, double g1) {
   return (g0 < 0.0 && g1 >= 0.0) || (g0 > 0.0 && g1 <= 0.0);
 }
 
+// early_time<Alg>::v: the stepper's static constexpr bool EARLY_TIME, or false
+template <class A, class = void>
+struct early_time {
+  static constexpr bool v = false;
+};
+template <class A>
+struct early_time<A, decltype(void(A::EARLY_TIME))> {
+  static constexpr bool v = A::EARLY_TIME;
+};
+
 // ------------------------------------------------------------- driver
 // Alg provides:  static constexpr int ORDER (for beta defaults / init dt),
 //   void init(const T* u0, const T* p, int& nf)       -- u = u0, f(u) cache
@@ -423,20 +433,12 @@ __device__ void integrate_all(const KArgs& a) {
         h = rem;
         last = true;
       }
-      const double ms = alg.attempt(h, p, a.abstol, a.reltol, nfev);  // EEst^2
-      ++iters;
-      // ms <= 1 (ms >= 0; NaN rejects), compared on the integer pipe
-      const bool ok = !a.adaptive || mag_bits(ms) <= 0x3FF0000000000000ull;
-      if (ok) {
-        // controller proposal for the next step
-        double dtnew = h;
-        if (a.adaptive) dtnew = h * f2d_bits(ctl_accept(a.ctl, ms, lqold));
-        // time update (compensated in the mixed-precision path)
-        const double tlo0 = tlo;
-        double tnew;
+      // the step's end if the attempt is accepted (compensated in the
+      // mixed-precision path)
+      auto step_end = [&](double& tn, double& tl) {
         if (last) {
-          tnew = tf;
-          tlo = 0.0;
+          tn = tf;
+          tl = 0.0;
         } else if (MIXED) {
           // Fast2Sum on the operands ordered by magnitude (integer compare):
           // the same exact (s, e) as TwoSum with half the FP64 additions
@@ -445,10 +447,34 @@ __device__ void integrate_all(const KArgs& a) {
           const double s = big + small;
           double e = small - (s - big);
           e += tlo;
-          tnew = s + e;
-          tlo = e - (tnew - s);
+          tn = s + e;
+          tl = e - (tn - s);
         } else {
-          tnew = t + h;
+          tn = t + h;
+          tl = tlo;
+        }
+      };
+      // Steppers that declare EARLY_TIME get it before the attempt, so that
+      // its dependent FP64 additions overlap the attempt's work: worth it
+      // where one warp runs alone on its SM sub-partition (small ensembles),
+      // at the cost of two registers live through the attempt.
+      double tnew_e = 0.0, tlo_e = 0.0;
+      if constexpr (early_time<Alg>::v) step_end(tnew_e, tlo_e);
+      const double ms = alg.attempt(h, p, a.abstol, a.reltol, nfev);  // EEst^2
+      ++iters;
+      // ms <= 1 (ms >= 0; NaN rejects), compared on the integer pipe
+      const bool ok = !a.adaptive || mag_bits(ms) <= 0x3FF0000000000000ull;
+      if (ok) {
+        // controller proposal for the next step
+        double dtnew = h;
+        if (a.adaptive) dtnew = h * f2d_bits(ctl_accept(a.ctl, ms, lqold));
+        const double tlo0 = tlo;
+        double tnew;
+        if constexpr (early_time<Alg>::v) {
+          tnew = tnew_e;
+          tlo = tlo_e;
+        } else {
+          step_end(tnew, tlo);
         }
         // continuous callback: a crossing of the condition in (t, tnew]
         // (after the repeat nudge when the previous step ended at an event)

@@ -30,6 +30,9 @@ template <class M>
 struct Tsit5FF {
   using T = ff;
   static constexpr int ORDER = 5, ALG_ID = GBDE_ALG_TSIT5, N = M::N;
+  // the driver computes a step's end before the attempt (small ensembles run
+  // one warp per SM sub-partition, where step latency is the time)
+  static constexpr bool EARLY_TIME = true;
   ff uu[N], un[N];
   ff k1[N], k7[N];  // f at the step's start and at its end (first-same-as-last)
   FfVec<N> hk[7];   // h k_j of the current attempt

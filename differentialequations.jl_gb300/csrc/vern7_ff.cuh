@@ -19,6 +19,9 @@ template <class M>
 struct Vern7FF {
   using T = ff;
   static constexpr int ORDER = 7, ALG_ID = GBDE_ALG_VERN7, N = M::N;
+  // the driver computes a step's end before the attempt (small ensembles run
+  // one warp per SM sub-partition, where step latency is the time)
+  static constexpr bool EARLY_TIME = true;
   ff uu[N], un[N];
   ff k1[N];        // f(uu)
   ff k11[N];       // f(un), evaluated for the dense output only
