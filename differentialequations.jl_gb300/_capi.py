@@ -79,7 +79,7 @@ class MlpTrainOpts(C.Structure):
 
 
 MLP_IN, MLP_OUT, MLP_PARAMS, MLP_NET_FLOATS = 8, 3, 9091, 9111
-LEARN_START, LEARN_ORDER = 1, 2  # gbde_opts.learned flags
+LEARN_START, LEARN_ORDER, LEARN_STIFF = 1, 2, 4  # gbde_opts.learned flags
 
 
 class TuneEntry(C.Structure):

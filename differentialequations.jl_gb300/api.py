@@ -274,10 +274,12 @@ def learned_flags(learned):
         return capi.LEARN_START
     names = (learned,) if isinstance(learned, str) else tuple(learned)
     flags = 0
+    table = {"start": capi.LEARN_START, "order": capi.LEARN_ORDER, "stiff": capi.LEARN_STIFF}
     for n in names:
-        if n not in ("start", "order"):
-            raise ValueError("learned takes True/False, 'start', 'order' or a tuple of them")
-        flags |= capi.LEARN_START if n == "start" else capi.LEARN_ORDER
+        if n not in table:
+            raise ValueError("learned takes True/False, 'start', 'order', 'stiff' or a tuple "
+                             "of them")
+        flags |= table[n]
     return flags
 
 

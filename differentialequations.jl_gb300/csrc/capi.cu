@@ -284,7 +284,8 @@ static int solve_auto(gbde_ctx* ctx, Scratch& sc, const LaunchCfg& cfg, const KA
   unsigned* counters = reinterpret_cast<unsigned*>(work + 3);
   int32_t *nonstiff = nullptr, *stiff = nullptr;
   const int8_t* pred =
-      (opts->learned & GBDE_LEARN_START) ? (const int8_t*)sc.pred_stiff.ptr : nullptr;
+      (opts->learned & (GBDE_LEARN_START | GBDE_LEARN_STIFF)) ? (const int8_t*)sc.pred_stiff.ptr
+                                                               : nullptr;
   GBDE_CUDA(ctx, build_partition(a.p, np, opts->stiff_threshold, pred, N, sc.part.ptr,
                                  counters, ctx->num_sms, s, &nonstiff, &stiff));
   unsigned cnt[2] = {0, 0};
@@ -375,7 +376,7 @@ static int check_solve_args(gbde_ctx* ctx, const gbde_problem* prob, const gbde_
   if (opts->maxiters <= 0) return set_err(ctx, GBDE_ERR_INVALID, "maxiters must be > 0");
   if (opts->adaptive && !(opts->qmin > 0.0 && opts->qmax >= 1.0 && opts->gamma > 0.0))
     return set_err(ctx, GBDE_ERR_INVALID, "controller needs qmin > 0, qmax >= 1, gamma > 0");
-  if (opts->learned & ~(GBDE_LEARN_START | GBDE_LEARN_ORDER))
+  if (opts->learned & ~(GBDE_LEARN_START | GBDE_LEARN_ORDER | GBDE_LEARN_STIFF))
     return set_err(ctx, GBDE_ERR_INVALID, "unknown learned flags %d", opts->learned);
   if (opts->learned && ctx->mlp_model != prob->model)
     return set_err(ctx, GBDE_ERR_STATE,

@@ -76,9 +76,18 @@ struct TeamLU {
     step = -1;
     piv = 0;
     invp = 0.0;
+    // Row position of this lane's row in a row-swapping LU (LAPACK getrf,
+    // the reference's dense LU): swapping pivot row p with the row at
+    // position k moves that row to p's old position.  Ties in |a_k| go to the
+    // lowest position, as getrf's first-maximum search does; the pivot
+    // sequence, and with it the factors' rounding, is then the row-swapping
+    // LU's.  (On the stiff ring ties between equal entries are frequent, and
+    // another tie rule changes the rounding enough to move most step
+    // sequences.)
+    unsigned pos = (unsigned)tm.lane;
 #pragma unroll
     for (int k = 0; k < TEAM; ++k) {
-      // pivot: unpivoted lane with the largest |a_k| (ties: lowest lane)
+      // pivot: unpivoted lane with the largest |a_k|, ties: lowest position
       const uint64_t key = step < 0 ? mag_bits(a[k]) + 1ull : 0ull;
       uint64_t m = key;
 #pragma unroll
@@ -86,8 +95,12 @@ struct TeamLU {
         const uint64_t x = __shfl_xor_sync(tm.mask, m, o, TEAM);
         m = x > m ? x : m;
       }
-      const unsigned bal = __ballot_sync(tm.mask, key == m) >> ((threadIdx.x & 31) & TEAM);
+      const bool cand = key == m;
+      const unsigned ppos = __reduce_min_sync(tm.mask, cand ? pos : 0xFFFFFFFFu);
+      const unsigned bal =
+          __ballot_sync(tm.mask, cand && pos == ppos) >> ((threadIdx.x & 31) & TEAM);
       const int p = __ffs(bal) - 1;
+      if (step < 0 && pos == (unsigned)k && tm.lane != p) pos = ppos;  // swapped out
       piv |= (uint64_t)p << (4 * k);
       double prow[TEAM];
 #pragma unroll

@@ -326,6 +326,9 @@ GBDE_API int gbde_measure_fma_peak(gbde_ctx* ctx, int32_t kind, double* tflops);
  * != 0 runs the loaded network first:
  *   GBDE_LEARN_START: the predicted dt replaces the Hairer-Wanner starting
  *     step, and GBDE_ALG_AUTO uses the stiff label instead of the threshold;
+ *   GBDE_LEARN_STIFF: GBDE_ALG_AUTO uses the stiff label; every trajectory
+ *     starts from the Hairer-Wanner step, so it takes the steps the method
+ *     takes without the predictor;
  *   GBDE_LEARN_ORDER: the persistent queue hands out trajectories by
  *     predicted cost, highest first, instead of longest span first -- the
  *     lanes of a warp then carry trajectories of similar step counts.  Each
@@ -340,6 +343,7 @@ GBDE_API int gbde_measure_fma_peak(gbde_ctx* ctx, int32_t kind, double* tflops);
 #define GBDE_MLP_NET_FLOATS 9111
 #define GBDE_LEARN_START 1 /* learned first dt and AUTO method choice          */
 #define GBDE_LEARN_ORDER 2 /* persistent queue ordered by the learned cost     */
+#define GBDE_LEARN_STIFF 4 /* AUTO method choice only (Hairer-Wanner start)    */
 
 typedef struct {
   int32_t epochs;      /* passes over the data                              */

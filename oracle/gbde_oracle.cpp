@@ -171,6 +171,39 @@ double wrms(int n, const double* e, const double* u, const double* un, double at
   return s / n;
 }
 
+// Controller arithmetic.  Mode 0 (the default) evaluates the step-size factor
+// and the starting-step powers with the FP32 series of controller.h, the
+// kernels' own arithmetic, so that the oracle takes the kernels' steps.  Mode 1
+// (oracle_set_controller(1)) is the textbook FP64 form with pow() and sqrt()
+// -- the PI controller of Hairer-Norsett-Wanner I, Sec. II.4 as OrdinaryDiffEq
+// evaluates it -- used to measure how far the FP32 series moves the step
+// sequence.  Process-wide; set it before a solve, not during one.
+int g_ctl_pow64 = 0;
+
+double hw_h0_pow64(double s0, double s1, double tspan) {
+  double h0 = 1e-6;
+  if (s0 >= 1e-10 && s1 >= 1e-10 && std::isfinite(s0) && std::isfinite(s1))
+    h0 = 0.01 * (std::sqrt(s0) / std::sqrt(s1));
+  return std::fmin(h0, tspan);
+}
+
+double hw_dt_pow64(double h0, double s1, double s2, double tspan, int order) {
+  const double d1 = std::sqrt(s1), d2 = std::sqrt(s2) / h0;
+  const double m = std::fmax(d1, d2);
+  double h1;
+  if (!(m * m > 1e-30)) h1 = std::fmax(1e-6, h0 * 1e-3);
+  else if (!std::isfinite(m)) h1 = 0.0;
+  else h1 = std::pow(0.01 / m, 1.0 / (order + 1));
+  return std::fmin(std::fmin(100.0 * h0, h1), tspan);
+}
+
+// Per-trajectory controller memory: log2(qold) for the FP32 series, qold for
+// the FP64 form.
+struct CtlMem {
+  float lqold;
+  double qold;
+};
+
 // Hairer-Norsett-Wanner I, Sec. II.4 starting step: mean squares of the
 // scaled u0, f0 and f(u0 + h0 f0) - f0; the powers go through the shared
 // hw_h0 / hw_dt (controller.h), as in the kernels.
@@ -185,7 +218,7 @@ double init_dt(const Model& m, const double* u0, const double* f0, const double*
   }
   s0 /= n;
   s1 /= n;
-  const double h0 = gbde::hw_h0(s0, s1, tspan);
+  const double h0 = g_ctl_pow64 ? hw_h0_pow64(s0, s1, tspan) : gbde::hw_h0(s0, s1, tspan);
   Vec u1, f1;
   for (int c = 0; c < n; ++c) u1[c] = u0[c] + h0 * f0[c];
   rhs(m.id, u1, p, f1);
@@ -195,7 +228,8 @@ double init_dt(const Model& m, const double* u0, const double* f0, const double*
     const double sc = at + std::fabs(u0[c]) * rt;
     s2 += ((f1[c] - f0[c]) / sc) * ((f1[c] - f0[c]) / sc);
   }
-  return gbde::hw_dt(h0, s1, s2 / n, tspan, order);
+  return g_ctl_pow64 ? hw_dt_pow64(h0, s1, s2 / n, tspan, order)
+                     : gbde::hw_dt(h0, s1, s2 / n, tspan, order);
 }
 
 struct Ctl {  // controller constants (gbde_opts)
@@ -204,6 +238,27 @@ struct Ctl {  // controller constants (gbde_opts)
   int adaptive;
   gbde::CtlK k;  // step-size factor constants (controller.h, shared with the kernels)
 };
+
+CtlMem ctl_start(const Ctl& C) { return CtlMem{C.k.lqoldinit, C.qoldinit}; }
+
+// Accepted step with EEst^2 = E: the factor r of dt_new = h r.
+double ctl_accept_r(const Ctl& C, double E, CtlMem& m) {
+  if (!g_ctl_pow64) return (double)gbde::ctl_accept(C.k, E, m.lqold);
+  const double eest = std::sqrt(E);
+  double q = std::pow(eest, C.beta1) / std::pow(m.qold, C.beta2) / C.gamma;
+  q = std::fmax(1.0 / C.qmax, std::fmin(1.0 / C.qmin, q));
+  if (q >= C.qsmin && q <= C.qsmax) q = 1.0;
+  m.qold = std::fmax(eest, C.qoldinit);
+  return 1.0 / q;
+}
+
+// Rejected step: the factor r of dt_new = h r.
+double ctl_reject_r(const Ctl& C, double E) {
+  if (!g_ctl_pow64) return (double)gbde::ctl_reject(C.k, E);
+  if (!std::isfinite(E)) return C.qmin;
+  const double q = std::fmin(1.0 / C.qmin, std::pow(std::sqrt(E), C.beta1) / C.gamma);
+  return 1.0 / q;
+}
 
 // ---------------------------------------------------------- one trajectory
 struct Out {
@@ -564,7 +619,7 @@ void solve_ode_traj(const Model& m, int alg, const Ctl& C, Out& o) {
   S.id = m.id;
   S.p = p;
   double dt = 0.0;
-  float lqold = C.k.lqoldinit;
+  CtlMem cm = ctl_start(C);
   if (bad) {
     ret = GBDE_RET_INITIALFAILURE;
   } else {
@@ -587,7 +642,7 @@ void solve_ode_traj(const Model& m, int alg, const Ctl& C, Out& o) {
     ++iters;
     if (!C.adaptive || E <= 1.0) {
       double dtnew = h;
-      if (C.adaptive) dtnew = h * (double)gbde::ctl_accept(C.k, E, lqold);
+      if (C.adaptive) dtnew = h * ctl_accept_r(C, E, cm);
       const double tnew = last ? tf : t + h;
       while (js < P->n_save) {
         const double ts = o.ts(js);
@@ -611,7 +666,7 @@ void solve_ode_traj(const Model& m, int alg, const Ctl& C, Out& o) {
       dt = C.dtmax > 0.0 ? std::fmin(dtnew, C.dtmax) : dtnew;
     } else {
       ++nrej;
-      dt = h * (double)gbde::ctl_reject(C.k, E);
+      dt = h * ctl_reject_r(C, E);
     }
     if (ret == GBDE_RET_DEFAULT) {
       if (iters >= C.maxiters) ret = GBDE_RET_MAXITERS;
@@ -862,7 +917,7 @@ void solve_sri_traj(const Model& m, const Ctl& C, uint64_t seed, int f32, Out& o
   if (C.dtmax > 0.0) h = std::fmin(h, C.dtmax);
   int ret = t < tf ? GBDE_RET_DEFAULT : GBDE_RET_SUCCESS;
   int64_t iters = 0;
-  float lqold = C.k.lqoldinit;
+  CtlMem cm = ctl_start(C);
   while (ret == GBDE_RET_DEFAULT) {
     const double rem = tf - t;
     double hs = h;
@@ -953,7 +1008,7 @@ void solve_sri_traj(const Model& m, const Ctl& C, uint64_t seed, int f32, Out& o
       ++nacc;
       if (!fin) ret = GBDE_RET_UNSTABLE;
       else if (last) ret = GBDE_RET_SUCCESS;
-      if (C.adaptive) h = hs * (double)gbde::ctl_accept(C.k, E, lqold);
+      if (C.adaptive) h = hs * ctl_accept_r(C, E, cm);
     } else {
       ++nrej;
       if (sp == 8) {  // merge the two farthest pieces
@@ -965,7 +1020,7 @@ void solve_sri_traj(const Model& m, const Ctl& C, uint64_t seed, int f32, Out& o
       stk[sp].dt = hs;
       for (int c = 0; c < n; ++c) { stk[sp].W[c] = dW[c]; stk[sp].Z[c] = dZ[c]; }
       ++sp;
-      h = hs * (double)gbde::ctl_reject(C.k, E);
+      h = hs * ctl_reject_r(C, E);
     }
     if (C.dtmax > 0.0) h = std::fmin(h, C.dtmax);
     if (ret == GBDE_RET_DEFAULT) {
@@ -1034,6 +1089,10 @@ void oracle_normals(uint64_t seed, uint64_t traj, uint64_t counter, int64_t n, i
   z.d = counter;
   for (int64_t k = 0; k < n; ++k) out[k] = z.next();
 }
+
+// Controller arithmetic of later solves: 0 = the kernels' FP32 series
+// (controller.h, identical steps), 1 = FP64 pow() (see g_ctl_pow64).
+void oracle_set_controller(int mode) { g_ctl_pow64 = mode == 1; }
 
 int oracle_hardware_threads(void) {
   const unsigned h = std::thread::hardware_concurrency();

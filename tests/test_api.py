@@ -35,6 +35,32 @@ def test_header_struct_layout_matches_ctypes(capi):
         assert fields == [f[0] for f in py._fields_], cname
 
 
+def test_oracle_restates_the_abi(capi, oracle):
+    """The oracle carries its own copy of gbde.h's structs, constants and
+    option defaults (so that it never loads the product library); they must
+    equal the product's, field for field."""
+    for py, orc in ((capi.Problem, oracle.Problem), (capi.Opts, oracle.Opts),
+                    (capi.Outputs, oracle.Outputs)):
+        assert [f[0] for f in py._fields_] == [f[0] for f in orc._fields_]
+        assert C.sizeof(py) == C.sizeof(orc)
+        for (n, _), (n2, _) in zip(py._fields_, orc._fields_):
+            assert getattr(py, n).offset == getattr(orc, n2).offset, n
+    for name in ("MODEL_LINEAR", "MODEL_LORENZ", "MODEL_ROBERTSON", "MODEL_VDP_RING8",
+                 "MODEL_LOTKA_VOLTERRA", "ALG_TSIT5", "ALG_VERN7", "ALG_ROSENBROCK23",
+                 "ALG_RODAS5", "ALG_RODAS5P", "ALG_EM", "ALG_SOSRI", "ALG_AUTO", "SAVE_GRID",
+                 "SAVE_PER_TRAJ", "MEM_HOST", "F64", "F32", "RET_SUCCESS"):
+        assert getattr(capi, name) == getattr(oracle, name), name
+    for mid, size in oracle.MODEL_SIZES.items():
+        assert capi.model_info(mid) == size
+    algs = [capi.ALG_TSIT5, capi.ALG_VERN7, capi.ALG_ROSENBROCK23, capi.ALG_RODAS5,
+            capi.ALG_RODAS5P, capi.ALG_EM, capi.ALG_SOSRI, capi.ALG_AUTO]
+    algs += [capi.ALG_SRIW1] if hasattr(capi, "ALG_SRIW1") else []
+    for alg in algs:
+        a, b = capi.opts_default(alg), oracle.opts_default(alg)
+        for n, _ in capi.Opts._fields_:
+            assert getattr(a, n) == getattr(b, n), (alg, n)
+
+
 def test_version_and_model_info(capi):
     assert capi.lib().gbde_version() == 3
     assert capi.model_info(capi.MODEL_LORENZ) == (3, 3)

@@ -1,0 +1,143 @@
+"""Full-size GPU runs of the 1,000,000-trajectory configurations, each checked
+on a seeded sample against the CPU FP64 oracle (same algorithm, same
+tolerances, same noise), with the gates the benchmark line reports:
+
+  * SDE ensemble (Lotka-Volterra, diagonal noise 0.1 u, tspan (0, 10)):
+    EM at dt = 1e-3 in FP64 within 1e-12 relative of the oracle on identical
+    noise; EM with FP32 state within 1e-4 relative of the FP64 oracle driven
+    by the same FP32 normals (FP32 rounding over 10,000 steps); SOSRI at
+    reltol 1e-3 with FP32 state: >= 95 % of the sample on the oracle's
+    Brownian path (an accept/reject flip continues a trajectory on another
+    path) and weighted error <= 10 on those.
+  * 16-state Van der Pol ring, AUTO (Tsit5 / Rodas5), reltol 1e-5, in the
+    chosen FP32-pair form: lockstep with the oracle on >= 95 % of the sample
+    and weighted error <= 10 there; trajectories off lockstep are held to the
+    oracle's own accuracy against a reltol-1e-10 truth.
+  * Learned stiffness choice on held-out ring trajectories: the same gate
+    per trajectory with the method the network chose, and every trajectory
+    succeeds.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+import bench  # noqa: E402  (the benchmark's input generators and accuracy gate)
+
+N_FULL = 1000000
+SAMPLE = 2000
+
+
+def _lv(N, seed):
+    rng = np.random.default_rng(seed)
+    p = np.c_[np.array([1.5, 1.0, 3.0, 1.0]) * rng.uniform(0.8, 1.2, (N, 4)), np.full(N, 0.1)]
+    return p, np.ones((N, 2)), np.zeros(N), np.full(N, 10.0), np.arange(11.0)
+
+
+def _rel(u, r):
+    return float(np.max(np.abs(np.asarray(u, np.float64) - r) / np.abs(r)))
+
+
+def test_config3_em_full_size(de, oracle):
+    capi = de._capi
+    M = de.models.lotka_volterra
+    p, u0, t0, tf, sv = _lv(N_FULL, bench.SEED)
+    idx = np.arange(SAMPLE)  # the noise is keyed by trajectory index
+    sub = [a[idx] for a in (p, u0, t0, tf)]
+    for prec, dt_out in ((capi.PREC_FP64, "f64"), (capi.PREC_MIXED, "f32")):
+        o = capi.opts_default(capi.ALG_EM)
+        o.dt, o.seed, o.precision = 1e-3, bench.SEED, prec
+        g = de.solve_arrays(M, o, p, u0, t0, tf, sv, capi.SAVE_GRID, u_dtype=dt_out)
+        assert np.all(g["retcode"] == capi.RET_SUCCESS)
+        assert np.all(g["naccept"] == 10000)
+        r = oracle.solve(capi, M, o, *sub, sv, capi.SAVE_GRID, nthreads=oracle.hardware_threads(),
+                         noise_f32=prec == capi.PREC_MIXED)
+        rel = _rel(g["u"][idx], r["u"])
+        assert rel <= (1e-12 if prec == capi.PREC_FP64 else 1e-4), (prec, rel)
+        assert np.isfinite(g["u"]).all()
+
+
+def test_config3_sosri_full_size(de, oracle):
+    capi = de._capi
+    M = de.models.lotka_volterra
+    p, u0, t0, tf, sv = _lv(N_FULL, bench.SEED)
+    o = capi.opts_default(capi.ALG_SOSRI)
+    o.reltol = o.abstol = 1e-3
+    o.seed, o.precision, o.batching = bench.SEED, capi.PREC_MIXED, capi.BATCH_PERSISTENT
+    g = de.solve_arrays(M, o, p, u0, t0, tf, sv, capi.SAVE_GRID, u_dtype="f32")
+    assert np.all(g["retcode"] == capi.RET_SUCCESS)
+    idx = np.arange(SAMPLE)
+    r = oracle.solve(capi, M, o, *[a[idx] for a in (p, u0, t0, tf)], sv, capi.SAVE_GRID,
+                     nthreads=oracle.hardware_threads(), noise_f32=True)
+    e = oracle.weighted_errors(g["u"][idx], r["u"], 1e-3, 1e-3).max(axis=(1, 2))
+    same = (g["naccept"][idx] == r["naccept"]) & (g["nreject"][idx] == r["nreject"])
+    assert same.mean() >= 0.95, same.mean()
+    assert e[same].max() <= 10.0, e[same].max()
+
+
+def _vdp_forms(de, capi, host, forms, learned=0):
+    M = de.models.vdp_ring8
+    out = {}
+    for name, prec, batch, odt in forms:
+        o = capi.opts_default(capi.ALG_AUTO)
+        o.reltol = o.abstol = bench.VDP_RTOL
+        o.stiff_threshold = bench.VDP_STIFF_MU
+        o.maxiters = 10 ** 6
+        o.precision, o.batching, o.learned = prec, batch, learned
+        r = de.solve_arrays(M, o, *host, capi.SAVE_GRID, u_dtype=odt)
+        out[name] = {k: r[k] for k in ("u", "naccept", "nreject", "retcode", "method")}
+        assert np.all(r["retcode"] == capi.RET_SUCCESS), name
+    return out
+
+
+def test_config4_full_size(de, oracle):
+    """1M trajectories of the ring in the chosen form (persistent queue,
+    FP32-pair Tsit5 / Rodas5 on an FP64 LU, FP32 output), gated on a
+    2,000-trajectory sample as the benchmark gates it."""
+    capi = de._capi
+    host = bench.vdp_inputs(N_FULL, bench.SEED)
+    forms = _vdp_forms(de, capi, host, [("persistent-f32x2", capi.PREC_F32X2,
+                                         capi.BATCH_PERSISTENT, "f32")])
+    idx = np.sort(np.random.default_rng(1).choice(N_FULL, SAMPLE, replace=False))
+    acc, ok = bench.vdp_accuracy(forms, host, idx, oracle.hardware_threads())
+    print(acc["persistent-f32x2"])
+    assert ok, acc
+    assert np.isfinite(forms["persistent-f32x2"]["u"]).all()
+
+
+def test_config5_learned_stiffness_full_size(de, oracle):
+    """Trained from scratch on the step logs of 200,000 ring trajectories, the
+    network picks Tsit5 or Rodas5 for 1M held-out trajectories (LEARN_STIFF:
+    the method choice only, Hairer-Wanner starting steps); every one succeeds
+    and a sample matches the oracle run with the chosen method."""
+    capi = de._capi
+    M = de.models.vdp_ring8
+    grid = np.arange(21.0)
+    tr = bench.vdp_inputs(200000, bench.SEED + 1000)
+    lab, _ = de.learned.stiff_labels(de.solve_arrays, M, *tr[:4], grid, capi.SAVE_GRID,
+                                     bench.VDP_RTOL, bench.VDP_RTOL)
+    o = capi.opts_default(capi.ALG_AUTO)
+    o.reltol = o.abstol = bench.VDP_RTOL
+    o.maxiters = 10 ** 6
+    r = de.solve_arrays(M, o, *tr, capi.SAVE_GRID)
+    x = de.learned.features(M, *tr[:4])
+    y = np.c_[np.log10(r["dt_first"]), lab, np.full(len(lab), np.nan)].astype(np.float32)
+    net, hist = de.learned.train(x, y, epochs=8, batch=4096, lr=2e-3, seed=bench.SEED)
+    assert hist[-1] < hist[0]
+    de.learned.load(M, net)
+    host = bench.vdp_inputs(N_FULL, bench.SEED + 2000)  # held out
+    forms = _vdp_forms(de, capi, host, [("learned-f32x2", capi.PREC_F32X2,
+                                         capi.BATCH_PERSISTENT, "f32")],
+                       learned=capi.LEARN_STIFF)
+    m = forms["learned-f32x2"]["method"]
+    # the network moves the split away from the fixed threshold
+    assert 0.05 < np.mean(m == capi.ALG_RODAS5) < 0.6
+    idx = np.sort(np.random.default_rng(2).choice(N_FULL, SAMPLE, replace=False))
+    acc, ok = bench.vdp_accuracy(forms, host, idx, oracle.hardware_threads())
+    print(acc["learned-f32x2"])
+    assert ok, acc

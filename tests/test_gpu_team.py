@@ -87,6 +87,31 @@ def test_team_rodas_stiff_vs_truth(de, oracle, alg, precision):
     assert abs(g["naccept"].mean() / r["naccept"].mean() - 1.0) < 0.05
 
 
+@pytest.mark.parametrize("alg", ["RODAS5", "RODAS5P"])
+@pytest.mark.parametrize("precision", ["fp64", "f32x2"])
+def test_team_rodas_stiff_lockstep(de, oracle, alg, precision):
+    """On the stiff ring the team LU picks the pivots of a row-swapping LU
+    (first maximum by current row position, as LAPACK's getrf and the
+    oracle): with another tie rule the rounding of W's factors differs enough
+    to move almost every step sequence.  With the same pivots the team
+    kernels take the oracle's steps."""
+    capi = de._capi
+    M = de.models.vdp_ring8
+    p, u0, t0, tf = ring_inputs(256, 14, 2, 3)  # mu in [100, 1000]
+    saveat = de.save_grid(0.0, 20.0, 1.0)
+    a = getattr(capi, "ALG_" + alg)
+    g = de.solve_arrays(M, opts_for(capi, a, precision=_prec(capi, precision),
+                                    batching=capi.BATCH_PERSISTENT), p, u0, t0, tf, saveat,
+                        capi.SAVE_GRID)
+    r = oracle.solve(capi, M, opts_for(capi, a), p, u0, t0, tf, saveat, capi.SAVE_GRID,
+                     nthreads=8)
+    assert np.all(g["retcode"] == capi.RET_SUCCESS)
+    lock = (g["naccept"] == r["naccept"]) & (g["nreject"] == r["nreject"])
+    e = weighted(g["u"], r["u"])
+    assert lock.mean() >= 0.95, lock.mean()
+    assert e[lock].max() <= (1.0 if precision == "fp64" else 10.0), e[lock].max()
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_auto_partition(de, oracle, precision):
     """AUTO: stiff iff mu > stiff_threshold; non-stiff trajectories run Tsit5
