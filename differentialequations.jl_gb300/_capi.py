@@ -29,7 +29,7 @@ MODEL_LINEAR, MODEL_LORENZ, MODEL_ROBERTSON, MODEL_VDP_RING8, MODEL_LOTKA_VOLTER
 MODEL_USER_BASE, USER_MAX_STATE, USER_MAX_PARAM = 1000, 8, 32
 
 ALG_TSIT5, ALG_VERN7, ALG_ROSENBROCK23, ALG_RODAS5, ALG_RODAS5P = 1, 2, 3, 4, 5
-ALG_EM, ALG_SOSRI, ALG_AUTO = 6, 7, 8
+ALG_EM, ALG_SOSRI, ALG_AUTO, ALG_SRIW1 = 6, 7, 8, 9
 
 PREC_FP64, PREC_MIXED, PREC_F32X2 = 0, 1, 2
 BATCH_PLAIN, BATCH_PERSISTENT = 0, 1

@@ -236,7 +236,14 @@ class EM(_Alg):
 
 
 class SOSRI(_Alg):
+    """Rackauckas & Nie's stability-optimised SRI (strong order 1.5), adaptive."""
     alg_id = capi.ALG_SOSRI
+    sde = True
+
+
+class SRIW1(_Alg):
+    """Roessler's SRIW1 (strong order 1.5), adaptive."""
+    alg_id = capi.ALG_SRIW1
     sde = True
 
 
@@ -523,7 +530,7 @@ def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start
                                   "use EnsembleGB300()")
     if not isinstance(alg, _Alg):
         raise TypeError("alg must be one of Tsit5(), Vern7(), Rosenbrock23(), Rodas5(), "
-                        "Rodas5P(), EM(), SOSRI()")
+                        "Rodas5P(), EM(), SOSRI(), SRIW1()")
     prob = ens.prob
     if alg.sde and not prob.is_sde:
         raise TypeError("%r needs an SDEProblem" % alg)

@@ -115,7 +115,8 @@ cudaError_t launch_alg(int alg, LaunchCfg cfg, const KArgs& a, cudaStream_t s) {
        (alg == GBDE_ALG_TSIT5 && cfg.tpt != 1)))
     return launch_team(cfg, a, s);
   if (alg == GBDE_ALG_TSIT5 || alg == GBDE_ALG_VERN7) return launch_explicit(cfg, a, s);
-  if (alg == GBDE_ALG_EM || alg == GBDE_ALG_SOSRI) return launch_sde(cfg, a, s);
+  if (alg == GBDE_ALG_EM || alg == GBDE_ALG_SOSRI || alg == GBDE_ALG_SRIW1)
+    return launch_sde(cfg, a, s);
   return launch_rosenbrock(cfg, a, s);
 }
 
@@ -246,7 +247,8 @@ int gbde_opts_default(int32_t alg, gbde_opts* o) {
       o->adaptive = 0;
       o->beta1 = 0.5;
       break;
-    case GBDE_ALG_SOSRI:  // strong order 1.5 pair: error ~ h^2 (I-controller)
+    case GBDE_ALG_SOSRI:  // strong order 1.5 pairs: error ~ h^2 (I-controller)
+    case GBDE_ALG_SRIW1:
       o->beta1 = 1.0 / 2.0;
       o->beta2 = 0.0;
       o->reltol = 1e-2;
@@ -267,7 +269,9 @@ static bool is_ode_alg(int a) {
   return a == GBDE_ALG_TSIT5 || a == GBDE_ALG_VERN7 || a == GBDE_ALG_ROSENBROCK23 ||
          a == GBDE_ALG_RODAS5 || a == GBDE_ALG_RODAS5P || a == GBDE_ALG_AUTO;
 }
-static bool is_sde_alg(int a) { return a == GBDE_ALG_EM || a == GBDE_ALG_SOSRI; }
+static bool is_sde_alg(int a) {
+  return a == GBDE_ALG_EM || a == GBDE_ALG_SOSRI || a == GBDE_ALG_SRIW1;
+}
 
 // GBDE_ALG_AUTO: classify every trajectory (stiff iff p[0] > stiff_threshold,
 // or the learned predictor's label), then run the non-stiff list with Tsit5

@@ -95,7 +95,7 @@ bool is_ode(int a) {
   return a == GBDE_ALG_TSIT5 || a == GBDE_ALG_VERN7 || a == GBDE_ALG_ROSENBROCK23 ||
          a == GBDE_ALG_RODAS5 || a == GBDE_ALG_RODAS5P;
 }
-bool is_sde(int a) { return a == GBDE_ALG_EM || a == GBDE_ALG_SOSRI; }
+bool is_sde(int a) { return a == GBDE_ALG_EM || a == GBDE_ALG_SOSRI || a == GBDE_ALG_SRIW1; }
 
 #define NOALLOC_CUDA(call)                                                           \
   do {                                                                               \

@@ -62,7 +62,9 @@ struct SmallLU {
     }
   }
 
-  // x = A^{-1} b in FP64 (b and x may alias)
+  // x = A^{-1} b in FP64 (b and x may alias).  factor() swaps whole rows,
+  // multipliers included (P A = L U, as LAPACK's getrf), so every row swap is
+  // applied to b before the forward substitution (getrs's order).
   GBDE_HD void solve(double* b) const {
 #pragma unroll
     for (int k = 0; k < N; ++k) {
@@ -73,6 +75,9 @@ struct SmallLU {
         b[k] = sw ? y : x;
         b[r] = sw ? x : y;
       }
+    }
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
 #pragma unroll
       for (int r = k + 1; r < N; ++r) b[r] -= A[r][k] * b[k];
     }
@@ -117,6 +122,7 @@ struct FFLU {
     ff b[N];
 #pragma unroll
     for (int c = 0; c < N; ++c) b[c] = rhs[c];
+    // every row swap first, then the substitutions (P A = L U, as SmallLU)
 #pragma unroll
     for (int k = 0; k < N; ++k) {
 #pragma unroll
@@ -126,6 +132,9 @@ struct FFLU {
         b[k] = sw ? yr : xk;
         b[r] = sw ? xk : yr;
       }
+    }
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
 #pragma unroll
       for (int r = k + 1; r < N; ++r) b[r] -= A[r][k] * b[k];
     }

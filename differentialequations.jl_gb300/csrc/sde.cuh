@@ -22,6 +22,8 @@
 //    Every normal comes from the counter-based stream in draw order, so the
 //    host can replay a trajectory exactly.
 #pragma once
+#include <type_traits>
+
 #include "philox.h"
 #include "solver.cuh"
 #include "tableaus.h"
@@ -372,9 +374,105 @@ struct NoiseStack {
   }
 };
 
-template <class M, class T, bool MIXED>
+// Which stages of a 4-stage SRI table (tableaus.h SosriTab / Sriw1Tab) need
+// an evaluation: f at H0_i when alpha_i or a later A0 / A1 column uses it, g at
+// H1_i when a beta or a later B0 / B1 column does; a stage whose H0 (H1) row
+// is empty sits at X and reuses stage 1's f (g).
+template <class Tab>
+struct SriUse {
+  static constexpr bool row_zero(const double (&r)[4]) {
+    return r[0] == 0.0 && r[1] == 0.0 && r[2] == 0.0 && r[3] == 0.0;
+  }
+  static constexpr bool h0_at_x(int i) {
+    return i == 0 || (row_zero(Tab::A0[i]) && row_zero(Tab::B0[i]));
+  }
+  static constexpr bool h1_at_x(int i) {
+    return i == 0 || (row_zero(Tab::A1[i]) && row_zero(Tab::B1[i]));
+  }
+  static constexpr bool f_used(int i) {
+    bool u = Tab::al[i] != 0.0;
+    for (int k = i + 1; k < 4; ++k) u = u || Tab::A0[k][i] != 0.0 || Tab::A1[k][i] != 0.0;
+    return u;
+  }
+  static constexpr bool g_used(int i) {
+    bool u = false;
+    for (int q = 0; q < 4; ++q) u = u || Tab::b[q][i] != 0.0;
+    for (int k = i + 1; k < 4; ++k) u = u || Tab::B0[k][i] != 0.0 || Tab::B1[k][i] != 0.0;
+    return u;
+  }
+  // f evaluations per step
+  static constexpr int n_f() {
+    int n = 1;
+    for (int i = 1; i < 4; ++i) n += (f_used(i) && !h0_at_x(i)) ? 1 : 0;
+    return n;
+  }
+};
+
+// Compile-time loop: f(std::integral_constant<int, I>) for I = B .. E-1, so
+// that table entries are read as constants (and zero entries drop out).
+template <int B, int E, class F>
+GBDE_D void static_for(F&& f) {
+  if constexpr (B < E) {
+    f(std::integral_constant<int, B>{});
+    static_for<B + 1, E>(f);
+  }
+}
+
+// Stage argument X + h sum_j A[i][j] F[j] + s sum_j B[i][j] G[j] (s: I10/h per
+// component for H0, sqrt(h) for H1); only the nonzero entries are summed.
+template <class Tab, int I, bool H0, int N, class T>
+GBDE_D void sri_arg(T* Y, const T* u, const T (*F)[N], const T (*G)[N], T hT, const T* s0,
+                    T s1) {
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    T af = T(0), bg = T(0);
+    static_for<0, I>([&](auto jc) {
+      constexpr int j = decltype(jc)::value;
+      constexpr double a = H0 ? Tab::A0[I][j] : Tab::A1[I][j];
+      constexpr double b = H0 ? Tab::B0[I][j] : Tab::B1[I][j];
+      if constexpr (a != 0.0) af += T(a) * F[j][c];
+      if constexpr (b != 0.0) bg += T(b) * G[j][c];
+    });
+    Y[c] = u[c] + af * hT + bg * (H0 ? s0[c] : s1);
+  }
+}
+
+// The drift and diffusion stage values F[i] = f(H0_i), G[i] = g(H1_i) of one
+// SRI step (I10h = I10 / h per component).
+template <class Tab, class M, class T>
+GBDE_D void sri_stages(T (*F)[M::N], T (*G)[M::N], const T* u, const T* p, T hT, T sqh,
+                       const T* I10h) {
+  constexpr int N = M::N;
+  using U = SriUse<Tab>;
+  M::f(F[0], u, p);
+  M::g(G[0], u, p);
+  static_for<1, 4>([&](auto ic) {
+    constexpr int i = decltype(ic)::value;
+    if constexpr (U::f_used(i)) {
+      if constexpr (U::h0_at_x(i)) {
+#pragma unroll
+        for (int c = 0; c < N; ++c) F[i][c] = F[0][c];
+      } else {
+        T Y[N];
+        sri_arg<Tab, i, true, N, T>(Y, u, F, G, hT, I10h, sqh);
+        M::f(F[i], Y, p);
+      }
+    }
+    if constexpr (U::g_used(i)) {
+      if constexpr (U::h1_at_x(i)) {
+#pragma unroll
+        for (int c = 0; c < N; ++c) G[i][c] = G[0][c];
+      } else {
+        T Y[N];
+        sri_arg<Tab, i, false, N, T>(Y, u, F, G, hT, I10h, sqh);
+        M::g(G[i], Y, p);
+      }
+    }
+  });
+}
+
+template <class M, class T, bool MIXED, class Tab, int ALG>
 __device__ void sri_all(const KArgs& a) {
-  using namespace tab::sriw1;
   constexpr int N = M::N;
   WorkSource src;
   src.init();
@@ -396,7 +494,7 @@ __device__ void sri_all(const KArgs& a) {
 #pragma unroll
     for (int c = 0; c < N; ++c) bad |= !isfinite((double)u[c]);
     if (bad) {
-      finish_sde<N, T>(a, i, GBDE_RET_INITIALFAILURE, js, 0, 0, 0, t0, GBDE_ALG_SOSRI,
+      finish_sde<N, T>(a, i, GBDE_RET_INITIALFAILURE, js, 0, 0, 0, t0, ALG,
                        __longlong_as_double(0x7ff8000000000000ll));
       continue;
     }
@@ -432,7 +530,7 @@ __device__ void sri_all(const KArgs& a) {
       }
       T dW[N], dZ[N];
       stk.take(hs, dW, dZ, ns);
-      // ---- SRIW1 step (with FP32 state the step's powers are FP32 operations)
+      // ---- SRI step (with FP32 state the step's powers are FP32 operations)
       T hT, sqh, ih, isqh;
       if constexpr (sizeof(T) == 4) {
         hT = (float)hs;
@@ -445,42 +543,39 @@ __device__ void sri_all(const KArgs& a) {
         ih = (T)(1.0 / hs);
         isqh = (T)(1.0 / sqrt(hs));
       }
-      T F1[N], F2[N], G1[N], G2[N], G3[N], G4[N], Y[N], un[N], err[N];
-      M::f(F1, u, p);
-      M::g(G1, u, p);
-      T I10[N], I11[N], I111[N];
+      T I10[N], I11[N], I111[N], I10h[N];
 #pragma unroll
       for (int c = 0; c < N; ++c) {
         I10[c] = T(0.5) * hT * (dW[c] + dZ[c] * T(0.57735026918962576451));
         I11[c] = T(0.5) * (dW[c] * dW[c] - hT);
         I111[c] = (dW[c] * dW[c] * dW[c] - T(3) * hT * dW[c]) * T(1.0 / 6.0);
+        I10h[c] = I10[c] * ih;
       }
-#pragma unroll
-      for (int c = 0; c < N; ++c) Y[c] = u[c] + T(A0_21) * F1[c] * hT + T(B0_21) * G1[c] * I10[c] * ih;
-      M::f(F2, Y, p);
-#pragma unroll
-      for (int c = 0; c < N; ++c) Y[c] = u[c] + T(A1_21) * F1[c] * hT + T(B1_21) * G1[c] * sqh;
-      M::g(G2, Y, p);
-#pragma unroll
-      for (int c = 0; c < N; ++c) Y[c] = u[c] + T(A1_31) * F1[c] * hT + T(B1_31) * G1[c] * sqh;
-      M::g(G3, Y, p);
-#pragma unroll
-      for (int c = 0; c < N; ++c)
-        Y[c] = u[c] + T(A1_43) * F1[c] * hT +
-               (T(B1_41) * G1[c] + T(B1_42) * G2[c] + T(B1_43) * G3[c]) * sqh;
-      M::g(G4, Y, p);
-      nfev += 2;
+      T F[4][N], G[4][N], un[N], err[N];
+      sri_stages<Tab, M, T>(F, G, u, p, hT, sqh, I10h);
+      nfev += SriUse<Tab>::n_f();
 #pragma unroll
       for (int c = 0; c < N; ++c) {
-        const T w1 = T(b1_1) * dW[c] + T(b2_1) * I11[c] * isqh + T(b3_1) * I10[c] * ih + T(b4_1) * I111[c] * ih;
-        const T w2 = T(b1_2) * dW[c] + T(b2_2) * I11[c] * isqh + T(b3_2) * I10[c] * ih + T(b4_2) * I111[c] * ih;
-        const T w3 = T(b1_3) * dW[c] + T(b2_3) * I11[c] * isqh + T(b3_3) * I10[c] * ih + T(b4_3) * I111[c] * ih;
-        const T w4 = T(b1_4) * dW[c] + T(b2_4) * I11[c] * isqh + T(b3_4) * I10[c] * ih + T(b4_4) * I111[c] * ih;
-        un[c] = u[c] + hT * (T(al1) * F1[c] + T(al2) * F2[c]) + w1 * G1[c] + w2 * G2[c] +
-                w3 * G3[c] + w4 * G4[c];
-        const T ed = hT * (T(al1 - 1.0) * F1[c] + T(al2) * F2[c]);
-        const T en = (T(b3_1) * G1[c] + T(b3_2) * G2[c] + T(b3_3) * G3[c] + T(b3_4) * G4[c]) * I10[c] * ih +
-                     (T(b4_1) * G1[c] + T(b4_2) * G2[c] + T(b4_3) * G3[c] + T(b4_4) * G4[c]) * I111[c] * ih;
+        T drift = T(0), ed = T(0), sto = T(0), g3 = T(0), g4 = T(0);
+        static_for<0, 4>([&](auto kc) {
+          constexpr int k = decltype(kc)::value;
+          constexpr double al = Tab::al[k], ale = al - (k == 0 ? 1.0 : 0.0);
+          constexpr double b1 = Tab::b[0][k], b2 = Tab::b[1][k], b3 = Tab::b[2][k],
+                           b4 = Tab::b[3][k];
+          if constexpr (al != 0.0) drift += T(al) * F[k][c];
+          // the embedded Euler drift (alpha = e_1) for the error estimate
+          if constexpr (ale != 0.0) ed += T(ale) * F[k][c];
+          if constexpr (b1 != 0.0 || b2 != 0.0 || b3 != 0.0 || b4 != 0.0) {
+            const T w = T(b1) * dW[c] + T(b2) * I11[c] * isqh + T(b3) * I10h[c] +
+                        T(b4) * I111[c] * ih;
+            sto += w * G[k][c];
+          }
+          if constexpr (b3 != 0.0) g3 += T(b3) * G[k][c];
+          if constexpr (b4 != 0.0) g4 += T(b4) * G[k][c];
+        });
+        un[c] = u[c] + hT * drift + sto;
+        ed *= hT;
+        const T en = g3 * I10h[c] + g4 * I111[c] * ih;
         err[c] = (ed < T(0) ? -ed : ed) + (en < T(0) ? -en : en);
       }
       double ms;  // EEst^2
@@ -546,7 +641,7 @@ __device__ void sri_all(const KArgs& a) {
           ret = GBDE_RET_DTLESSTHANMIN;
       }
     }
-    finish_sde<N, T>(a, i, ret, js, nacc, nrej, nfev, t + tlo, GBDE_ALG_SOSRI, dt1);
+    finish_sde<N, T>(a, i, ret, js, nacc, nrej, nfev, t + tlo, ALG, dt1);
   }
 }
 

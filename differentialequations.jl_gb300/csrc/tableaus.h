@@ -295,6 +295,99 @@ constexpr double b4_3 = -0.6666666666666666;
 constexpr double b4_4 = 1.0;
 }  // namespace sriw1
 
+// ---------------------------------------------------------------- SOSRI
+// C. Rackauckas, Q. Nie, "Stability-optimized high order methods and
+// stiffness detection for pathwise stiff stochastic differential equations",
+// arXiv:1804.04344 (2018): the 4-stage SRI of strong order 1.5 for diagonal
+// noise whose free coefficients were chosen to enlarge the stability region
+// (SOSRI).  Same stage structure as SRIW1 (Roessler's SRI):
+//   H0_i = X + sum_j A0_ij f(H0_j) h + sum_j B0_ij g(H1_j) I10/h
+//   H1_i = X + sum_j A1_ij f(H0_j) h + sum_j B1_ij g(H1_j) sqrt(h)
+// with every strictly lower entry in use.  The values are the published ones;
+// they satisfy the strong-order-1.5 conditions to ~1e-16 except
+// al . B0 e = 1 and al . (B0 e)^2 = 3/2, which they meet to ~7e-11.
+namespace sosri {
+constexpr double A0_21 = -0.04199224421316468;
+constexpr double A0_31 = 2.842612915017106;
+constexpr double A0_32 = -2.0527723684000727;
+constexpr double A0_41 = 4.338237071435815;
+constexpr double A0_42 = -2.8895936137439793;
+constexpr double A0_43 = 2.3017575594644466;
+constexpr double A1_21 = 0.26204282091330466;
+constexpr double A1_31 = 0.20903646383505375;
+constexpr double A1_32 = -0.1502377115150361;
+constexpr double A1_41 = 0.05836595312746999;
+constexpr double A1_42 = 0.6149440396332373;
+constexpr double A1_43 = 0.08535117634046772;
+constexpr double B0_21 = -0.21641093549612528;
+constexpr double B0_31 = 1.5336352863679572;
+constexpr double B0_32 = 0.26066223492647056;
+constexpr double B0_41 = -1.0536037558179159;
+constexpr double B0_42 = 1.7015284721089472;
+constexpr double B0_43 = -0.20725685514492662;
+constexpr double B1_21 = -0.5119011827621657;
+constexpr double B1_31 = 2.67767339866713;
+constexpr double B1_32 = -4.9395031322250995;
+constexpr double B1_41 = 0.15580956238299215;
+constexpr double B1_42 = 3.2361551006624674;
+constexpr double B1_43 = -1.4223118283355949;
+constexpr double al1 = 1.140099274172029;
+constexpr double al2 = -0.6401334255743456;
+constexpr double al3 = 0.4736296532772559;
+constexpr double al4 = 0.026404498125060714;
+constexpr double b1_1 = -1.8453464565104432;
+constexpr double b1_2 = 2.688764531100726;
+constexpr double b1_3 = -0.2523866501071323;
+constexpr double b1_4 = 0.40896857551684956;
+constexpr double b2_1 = 0.4969658141589478;
+constexpr double b2_2 = -0.5771202869753592;
+constexpr double b2_3 = -0.12919702470322217;
+constexpr double b2_4 = 0.2093514975196336;
+constexpr double b3_1 = 2.8453464565104425;
+constexpr double b3_2 = -2.688764531100725;
+constexpr double b3_3 = 0.2523866501071322;
+constexpr double b3_4 = -0.40896857551684945;
+constexpr double b4_1 = 0.11522663875443433;
+constexpr double b4_2 = -0.57877086147738;
+constexpr double b4_3 = 0.2857851028163886;
+constexpr double b4_4 = 0.17775911990655704;
+}  // namespace sosri
+
+// Both SRI tables as full 4 x 4 arrays (entries not listed are zero), for the
+// stage loops of the kernels and of the oracle; b[q] holds beta^(q+1).
+#define GBDE_SRI_ARRAYS(NS, A0_3, A0_4, A1_3, A1_4, B0_3, B0_4, B1_3, B1_4, AL)               \
+  static constexpr double A0[4][4] = {{0, 0, 0, 0}, {NS::A0_21, 0, 0, 0}, A0_3, A0_4};        \
+  static constexpr double B0[4][4] = {{0, 0, 0, 0}, {NS::B0_21, 0, 0, 0}, B0_3, B0_4};        \
+  static constexpr double A1[4][4] = {{0, 0, 0, 0}, {NS::A1_21, 0, 0, 0}, A1_3, A1_4};        \
+  static constexpr double B1[4][4] = {{0, 0, 0, 0}, {NS::B1_21, 0, 0, 0}, B1_3, B1_4};        \
+  static constexpr double al[4] = AL;                                                       \
+  static constexpr double b[4][4] = {{NS::b1_1, NS::b1_2, NS::b1_3, NS::b1_4},               \
+                                     {NS::b2_1, NS::b2_2, NS::b2_3, NS::b2_4},               \
+                                     {NS::b3_1, NS::b3_2, NS::b3_3, NS::b3_4},               \
+                                     {NS::b4_1, NS::b4_2, NS::b4_3, NS::b4_4}};
+#define GBDE_ROW(...) {__VA_ARGS__}
+struct SosriTab {
+  GBDE_SRI_ARRAYS(sosri, GBDE_ROW(sosri::A0_31, sosri::A0_32, 0, 0),
+                  GBDE_ROW(sosri::A0_41, sosri::A0_42, sosri::A0_43, 0),
+                  GBDE_ROW(sosri::A1_31, sosri::A1_32, 0, 0),
+                  GBDE_ROW(sosri::A1_41, sosri::A1_42, sosri::A1_43, 0),
+                  GBDE_ROW(sosri::B0_31, sosri::B0_32, 0, 0),
+                  GBDE_ROW(sosri::B0_41, sosri::B0_42, sosri::B0_43, 0),
+                  GBDE_ROW(sosri::B1_31, sosri::B1_32, 0, 0),
+                  GBDE_ROW(sosri::B1_41, sosri::B1_42, sosri::B1_43, 0),
+                  GBDE_ROW(sosri::al1, sosri::al2, sosri::al3, sosri::al4))
+};
+struct Sriw1Tab {
+  GBDE_SRI_ARRAYS(sriw1, GBDE_ROW(0, 0, 0, 0), GBDE_ROW(0, 0, 0, 0),
+                  GBDE_ROW(sriw1::A1_31, 0, 0, 0), GBDE_ROW(0, 0, sriw1::A1_43, 0),
+                  GBDE_ROW(0, 0, 0, 0), GBDE_ROW(0, 0, 0, 0),
+                  GBDE_ROW(sriw1::B1_31, 0, 0, 0),
+                  GBDE_ROW(sriw1::B1_41, sriw1::B1_42, sriw1::B1_43, 0),
+                  GBDE_ROW(sriw1::al1, sriw1::al2, 0, 0))
+};
+#undef GBDE_ROW
+#undef GBDE_SRI_ARRAYS
+
 }  // namespace tab
 }  // namespace gbde
 

@@ -79,11 +79,8 @@ struct TeamLU {
     // Row position of this lane's row in a row-swapping LU (LAPACK getrf,
     // the reference's dense LU): swapping pivot row p with the row at
     // position k moves that row to p's old position.  Ties in |a_k| go to the
-    // lowest position, as getrf's first-maximum search does; the pivot
-    // sequence, and with it the factors' rounding, is then the row-swapping
-    // LU's.  (On the stiff ring ties between equal entries are frequent, and
-    // another tie rule changes the rounding enough to move most step
-    // sequences.)
+    // lowest position, as getrf's first-maximum search does, so the pivot
+    // sequence is the row-swapping LU's even when entries tie.
     unsigned pos = (unsigned)tm.lane;
 #pragma unroll
     for (int k = 0; k < TEAM; ++k) {

@@ -96,8 +96,9 @@ extern "C" {
 #define GBDE_ALG_RODAS5 4       /* Di Marzo 5(4) Rosenbrock, stiffly accurate       */
 #define GBDE_ALG_RODAS5P 5      /* Steinebach 5(4) Rosenbrock                       */
 #define GBDE_ALG_EM 6           /* Euler-Maruyama, fixed step                       */
-#define GBDE_ALG_SOSRI 7        /* SRI strong 1.5, adaptive with rejection sampling
-                                   with memory                                      */
+#define GBDE_ALG_SOSRI 7        /* SOSRI (Rackauckas & Nie 2018): stability-optimised
+                                   SRI of strong order 1.5, adaptive with rejection
+                                   sampling with memory (SOSRI, SDEProblem qa.jl:103) */
 #define GBDE_ALG_AUTO 8         /* per-trajectory Tsit5 / Rodas5 choice, made once
                                    before integration: stiff iff p[0] >
                                    stiff_threshold (or the learned predictor's label);
@@ -105,6 +106,9 @@ extern "C" {
                                    test/qa/qa.jl:15.  Stiff trajectories always run
                                    Rodas5 in FP64; with GBDE_PREC_MIXED the others run
                                    Tsit5 with FP32 state.                             */
+
+#define GBDE_ALG_SRIW1 9        /* SRIW1 (Roessler 2010): SRI of strong order 1.5,
+                                   adaptive with rejection sampling with memory      */
 
 /* ---- precision -------------------------------------------------------- */
 #define GBDE_PREC_FP64 0  /* everything in FP64                                  */

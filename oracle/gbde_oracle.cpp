@@ -146,12 +146,15 @@ struct LU {
       }
     }
   }
+  // factor() swaps whole rows, multipliers included (P A = L U, LAPACK's
+  // getrf), so the solve applies every row swap to b first and then
+  // substitutes (getrs's order).
   void solve(const double* b, double* x) const {
     for (int c = 0; c < n; ++c) x[c] = b[c];
-    for (int k = 0; k < n; ++k) {
+    for (int k = 0; k < n; ++k)
       if (piv[k] != k) std::swap(x[k], x[piv[k]]);
+    for (int k = 0; k < n; ++k)
       for (int r = k + 1; r < n; ++r) x[r] -= A[r * n + k] * x[k];
-    }
     for (int k = n - 1; k >= 0; --k) {
       double s = x[k];
       for (int c = k + 1; c < n; ++c) s -= A[k * n + c] * x[c];
@@ -882,13 +885,17 @@ struct Piece {
   double dt, W[NMAX], Z[NMAX];
 };
 
-void solve_sri_traj(const Model& m, const Ctl& C, uint64_t seed, int f32, Out& o) {
-  using namespace gbde::tab::sriw1;
-  const double al[2] = {al1, al2};
-  const double b1[4] = {b1_1, b1_2, b1_3, b1_4};
-  const double b2[4] = {b2_1, b2_2, b2_3, b2_4};
-  const double b3[4] = {b3_1, b3_2, b3_3, b3_4};
-  const double b4[4] = {b4_1, b4_2, b4_3, b4_4};
+// One trajectory of a 4-stage SRI (Roessler's form; Tab = SosriTab or
+// Sriw1Tab, tableaus.h):
+//   H0_i = X + sum_j A0_ij f(H0_j) h + sum_j B0_ij g(H1_j) I10/h
+//   H1_i = X + sum_j A1_ij f(H0_j) h + sum_j B1_ij g(H1_j) sqrt(h)
+//   X'   = X + h sum_i al_i f(H0_i)
+//            + sum_i (b1_i dW + b2_i I11/sqrt(h) + b3_i I10/h + b4_i I111/h) g(H1_i)
+// Error estimate (Rackauckas & Nie, DCDS-B 22 (2017)): the embedded Euler
+// drift and the terms of strong order 1.5,
+//   E = h |sum_i al_i f(H0_i) - f(X)| + |sum_i (b3_i I10/h + b4_i I111/h) g(H1_i)|.
+template <class Tab>
+void solve_sri_traj(const Model& m, const Ctl& C, uint64_t seed, int f32, Out& o, int alg) {
   const gbde_problem* P = o.P;
   const int64_t i = o.i;
   const int n = m.n;
@@ -900,7 +907,7 @@ void solve_sri_traj(const Model& m, const Ctl& C, uint64_t seed, int f32, Out& o
   while (js < P->n_save && o.ts(js) <= t0) o.save(js++, u, n);
   bool bad = !(tf >= t0) || !std::isfinite(t0) || !std::isfinite(tf);
   for (int c = 0; c < n; ++c) bad |= !std::isfinite(u[c]);
-  if (bad) return finish(o, n, js, GBDE_RET_INITIALFAILURE, 0, 0, 0, t0, GBDE_ALG_SOSRI);
+  if (bad) return finish(o, n, js, GBDE_RET_INITIALFAILURE, 0, 0, 0, t0, alg);
   Normals z{seed, (uint64_t)i};
   z.f32 = f32;
   Piece stk[8];
@@ -961,30 +968,63 @@ void solve_sri_traj(const Model& m, const Ctl& C, uint64_t seed, int f32, Out& o
       I11[c] = 0.5 * (dW[c] * dW[c] - hs);
       I111[c] = (dW[c] * dW[c] * dW[c] - 3.0 * hs * dW[c]) * (1.0 / 6.0);
     }
-    double F1[NMAX], F2[NMAX], G[4][NMAX], Y[NMAX], un[NMAX], err[NMAX];
-    rhs(m.id, u, p, F1);
+    // stage values: f at H0_i, g at H1_i, in stage order; a stage whose H0
+    // (H1) row is empty sits at X
+    double F[4][NMAX], G[4][NMAX], Y[NMAX], un[NMAX], err[NMAX];
+    rhs(m.id, u, p, F[0]);
     noise(m.id, u, p, G[0]);
-    for (int c = 0; c < n; ++c) Y[c] = u[c] + A0_21 * F1[c] * hs + B0_21 * G[0][c] * I10[c] * ih;
-    rhs(m.id, Y, p, F2);
-    for (int c = 0; c < n; ++c) Y[c] = u[c] + A1_21 * F1[c] * hs + B1_21 * G[0][c] * sqh;
-    noise(m.id, Y, p, G[1]);
-    for (int c = 0; c < n; ++c) Y[c] = u[c] + A1_31 * F1[c] * hs + B1_31 * G[0][c] * sqh;
-    noise(m.id, Y, p, G[2]);
-    for (int c = 0; c < n; ++c)
-      Y[c] = u[c] + A1_43 * F1[c] * hs + (B1_41 * G[0][c] + B1_42 * G[1][c] + B1_43 * G[2][c]) * sqh;
-    noise(m.id, Y, p, G[3]);
-    nf += 2;
-    for (int c = 0; c < n; ++c) {
-      double sto = 0.0, en3 = 0.0, en4 = 0.0;
-      for (int s = 0; s < 4; ++s) {
-        sto += (b1[s] * dW[c] + b2[s] * I11[c] * isqh + b3[s] * I10[c] * ih + b4[s] * I111[c] * ih) * G[s][c];
-        en3 += b3[s] * G[s][c];
-        en4 += b4[s] * G[s][c];
+    int nfs = 1;
+    for (int s = 1; s < 4; ++s) {
+      bool h0x = true, h1x = true;
+      for (int j = 0; j < s; ++j) {
+        h0x = h0x && Tab::A0[s][j] == 0.0 && Tab::B0[s][j] == 0.0;
+        h1x = h1x && Tab::A1[s][j] == 0.0 && Tab::B1[s][j] == 0.0;
       }
-      un[c] = u[c] + hs * (al[0] * F1[c] + al[1] * F2[c]) + sto;
-      const double ed = hs * ((al[0] - 1.0) * F1[c] + al[1] * F2[c]);
+      if (h0x) {
+        for (int c = 0; c < n; ++c) F[s][c] = F[0][c];
+      } else {
+        for (int c = 0; c < n; ++c) {
+          double af = 0.0, bg = 0.0;
+          for (int j = 0; j < s; ++j) {
+            af += Tab::A0[s][j] * F[j][c];
+            bg += Tab::B0[s][j] * G[j][c];
+          }
+          Y[c] = u[c] + af * hs + bg * I10[c] * ih;
+        }
+        rhs(m.id, Y, p, F[s]);
+        // counted when the method uses it (alpha or a later A0 / A1 column)
+        bool used = Tab::al[s] != 0.0;
+        for (int k = s + 1; k < 4; ++k) used = used || Tab::A0[k][s] != 0.0 || Tab::A1[k][s] != 0.0;
+        nfs += used ? 1 : 0;
+      }
+      if (h1x) {
+        for (int c = 0; c < n; ++c) G[s][c] = G[0][c];
+      } else {
+        for (int c = 0; c < n; ++c) {
+          double af = 0.0, bg = 0.0;
+          for (int j = 0; j < s; ++j) {
+            af += Tab::A1[s][j] * F[j][c];
+            bg += Tab::B1[s][j] * G[j][c];
+          }
+          Y[c] = u[c] + af * hs + bg * sqh;
+        }
+        noise(m.id, Y, p, G[s]);
+      }
+    }
+    nf += nfs;
+    for (int c = 0; c < n; ++c) {
+      double drift = 0.0, sto = 0.0, en3 = 0.0, en4 = 0.0, ed = 0.0;
+      for (int s = 0; s < 4; ++s) {
+        drift += Tab::al[s] * F[s][c];
+        ed += (Tab::al[s] - (s == 0 ? 1.0 : 0.0)) * F[s][c];
+        sto += (Tab::b[0][s] * dW[c] + Tab::b[1][s] * I11[c] * isqh + Tab::b[2][s] * I10[c] * ih +
+                Tab::b[3][s] * I111[c] * ih) * G[s][c];
+        en3 += Tab::b[2][s] * G[s][c];
+        en4 += Tab::b[3][s] * G[s][c];
+      }
+      un[c] = u[c] + hs * drift + sto;
       const double en = en3 * I10[c] * ih + en4 * I111[c] * ih;
-      err[c] = std::fabs(ed) + std::fabs(en);
+      err[c] = std::fabs(hs * ed) + std::fabs(en);
     }
     const double E = wrms(n, err, u, un, C.at, C.rt);
     ++iters;
@@ -1029,7 +1069,7 @@ void solve_sri_traj(const Model& m, const Ctl& C, uint64_t seed, int f32, Out& o
         ret = GBDE_RET_DTLESSTHANMIN;
     }
   }
-  finish(o, n, js, ret, nacc, nrej, nf, t, GBDE_ALG_SOSRI);
+  finish(o, n, js, ret, nacc, nrej, nf, t, alg);
 }
 
 }  // namespace
@@ -1063,7 +1103,10 @@ int oracle_ensemble_solve(const gbde_problem* P, const gbde_opts* O, gbde_output
       for (int64_t i = b; i < e; ++i) {
         Out o{P, out, i};
         if (alg == GBDE_ALG_EM) solve_em_traj(m, C, O->seed, noise_f32, o);
-        else if (alg == GBDE_ALG_SOSRI) solve_sri_traj(m, C, O->seed, noise_f32, o);
+        else if (alg == GBDE_ALG_SOSRI)
+          solve_sri_traj<gbde::tab::SosriTab>(m, C, O->seed, noise_f32, o, alg);
+        else if (alg == GBDE_ALG_SRIW1)
+          solve_sri_traj<gbde::tab::Sriw1Tab>(m, C, O->seed, noise_f32, o, alg);
         else solve_ode_traj(m, alg, C, o);
       }
     }
@@ -1088,6 +1131,18 @@ void oracle_normals(uint64_t seed, uint64_t traj, uint64_t counter, int64_t n, i
   z.f32 = f32;
   z.d = counter;
   for (int64_t k = 0; k < n; ++k) out[k] = z.next();
+}
+
+// x = A^{-1} b by the oracle's partial-pivot LU (A row-major n x n, n <= 16):
+// the linear solve of its Rosenbrock steppers, exposed for its own tests.
+int oracle_lu_solve(int n, const double* A, const double* b, double* x) {
+  if (n < 1 || n > NMAX) return GBDE_ERR_INVALID;
+  LU W;
+  W.n = n;
+  for (int k = 0; k < n * n; ++k) W.A[k] = A[k];
+  W.factor();
+  W.solve(b, x);
+  return GBDE_OK;
 }
 
 // Controller arithmetic of later solves: 0 = the kernels' FP32 series

@@ -128,6 +128,8 @@ def lib():
         L.oracle_normals.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, C.c_int64, C.c_int,
                                      C.c_void_p]
         L.oracle_hardware_threads.restype = C.c_int
+        L.oracle_lu_solve.restype = C.c_int
+        L.oracle_lu_solve.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_set_controller.restype = None
         L.oracle_set_controller.argtypes = [C.c_int]
         _lib = L
@@ -142,6 +144,16 @@ def set_controller(mode):
     """0: the kernels' FP32-series step-size factor (identical steps; the
     default); 1: the FP64 pow() form of the same PI controller."""
     lib().oracle_set_controller(int(mode))
+
+
+def lu_solve(A, b):
+    """x = A^{-1} b with the oracle's partial-pivot LU (its Rosenbrock solve)."""
+    A = np.ascontiguousarray(A, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    x = np.empty_like(b)
+    if lib().oracle_lu_solve(len(b), A.ctypes.data, b.ctypes.data, x.ctypes.data) != 0:
+        raise ValueError("lu_solve: n must be 1..16")
+    return x
 
 
 def solve(capi, model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", nthreads=1,

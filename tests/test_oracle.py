@@ -233,3 +233,19 @@ def test_sri_adaptive_statistics(oracle, capi, de):
     assert abs(x.mean() - 1.0) < 4 * x.std() / np.sqrt(N)
     lx = np.log(x)
     assert abs(lx.var() - 0.25) < 0.05
+
+
+@pytest.mark.parametrize("n", [2, 3, 5, 16])
+def test_oracle_lu_solve_with_row_swaps(oracle, n):
+    """The Rosenbrock steppers' partial-pivot LU solves W x = b to rounding
+    when rows are swapped at every elimination step (the factorisation swaps
+    whole rows, P W = L U, so the solve applies every swap before the
+    substitutions).  Rows are ordered by increasing magnitude of their
+    leading entries so that every step swaps."""
+    rng = np.random.default_rng(n)
+    for _ in range(200):
+        A = rng.normal(size=(n, n))
+        A[:, 0] = np.arange(1, n + 1) * rng.choice([-1.0, 1.0], n)
+        b = rng.normal(size=n)
+        x = oracle.lu_solve(A, b)
+        assert np.max(np.abs(A @ x - b)) <= 1e-10 * (1 + np.abs(A).sum(1).max() * np.abs(x).max())

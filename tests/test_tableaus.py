@@ -139,24 +139,72 @@ def test_ros23_constants():
     assert abs(v["e32"] - (6.0 + np.sqrt(2.0))) < 1e-15
 
 
-def test_sriw1_strong_order_gbm():
-    """SRIW1 (tableaus.h) has strong order ~1.5 on geometric Brownian motion
-    dX = mu X dt + s X dW, whose exact solution is known given W."""
-    v = TB["sriw1"]
+def sri_table(name):
+    """Full 4 x 4 arrays of an SRI table parsed from tableaus.h (entries not
+    listed are zero)."""
+    v = TB[name]
+    M = {k: np.zeros((4, 4)) for k in ("A0", "B0", "A1", "B1")}
+    for key, val in v.items():
+        if key[:2] in M and "_" in key:
+            i, j = int(key[3]) - 1, int(key[4]) - 1
+            M[key[:2]][i, j] = val
+    al = np.array([v.get("al%d" % i, 0.0) for i in range(1, 5)])
+    b = np.array([[v["b%d_%d" % (q, i)] for i in range(1, 5)] for q in range(1, 5)])
+    return M["A0"], M["B0"], M["A1"], M["B1"], al, b
+
+
+def sri_conditions(A0, B0, A1, B1, al, b):
+    """Roessler's conditions for strong order 1.5 of an SRI method with
+    diagonal noise (SIAM J. Numer. Anal. 48 (2010)), as residuals."""
+    e = np.ones(4)
+    b1, b2, b3, b4 = b
+    B1e, B0e, A1e = B1 @ e, B0 @ e, A1 @ e
+    return {
+        "a.e=1": al @ e - 1, "b1.e=1": b1 @ e - 1, "b2.e=0": b2 @ e, "b3.e=0": b3 @ e,
+        "b4.e=0": b4 @ e,
+        "b1.B1e=0": b1 @ B1e, "b2.B1e=1": b2 @ B1e - 1, "b3.B1e=0": b3 @ B1e, "b4.B1e=0": b4 @ B1e,
+        "a.A0e=1/2": al @ A0 @ e - 0.5, "a.B0e=1": al @ B0e - 1, "a.(B0e)^2=3/2": al @ B0e ** 2 - 1.5,
+        "b1.A1e=1": b1 @ A1e - 1, "b2.A1e=0": b2 @ A1e, "b3.A1e=-1": b3 @ A1e + 1, "b4.A1e=0": b4 @ A1e,
+        "b1.(B1e)^2=1": b1 @ B1e ** 2 - 1, "b2.(B1e)^2=0": b2 @ B1e ** 2,
+        "b3.(B1e)^2=-1": b3 @ B1e ** 2 + 1, "b4.(B1e)^2=2": b4 @ B1e ** 2 - 2,
+        "b1.B1B1e=0": b1 @ B1 @ B1e, "b2.B1B1e=0": b2 @ B1 @ B1e, "b3.B1B1e=0": b3 @ B1 @ B1e,
+        "b4.B1B1e=1": b4 @ B1 @ B1e - 1,
+        "b1.A1B0e/2+b3.A1B0e/3=0": 0.5 * b1 @ A1 @ B0e + b3 @ A1 @ B0e / 3.0,
+    }
+
+
+@pytest.mark.parametrize("name", ["sriw1", "sosri"])
+def test_sri_order_conditions(name):
+    """SRIW1 (Roessler 2010) and SOSRI (Rackauckas & Nie 2018) satisfy the
+    strong-order-1.5 conditions.  SOSRI's published coefficients come from a
+    numerical optimisation: the two conditions on B0 hold to ~7e-11, the rest
+    to rounding."""
+    res = sri_conditions(*sri_table(name))
+    for k, r in res.items():
+        tol = 1e-9 if (name == "sosri" and "B0e" in k and "A1" not in k) else 1e-14
+        assert abs(r) < tol, (name, k, r)
+
+
+def test_sosri_is_not_sriw1():
+    """The SOSRI slot holds the stability-optimised table (all stages used),
+    not SRIW1's."""
+    A0, B0, A1, B1, al, b = sri_table("sosri")
+    assert np.all(al != 0) and np.count_nonzero(A0) == 6 and np.count_nonzero(B1) == 6
+    assert not np.allclose(al, sri_table("sriw1")[4])
+
+
+@pytest.mark.parametrize("name", ["sriw1", "sosri"])
+def test_sri_strong_order_gbm(name):
+    """SRIW1 and SOSRI (tableaus.h) have strong order ~1.5 on geometric
+    Brownian motion dX = mu X dt + s X dW, whose exact solution is known
+    given W."""
+    A0, B0, A1, B1, al, bb = sri_table(name)
     rng = np.random.default_rng(1)
     mu, sig, T, M, nfine = 1.5, 1.0, 1.0, 2000, 2 ** 11
     dtf = T / nfine
     W = np.concatenate([np.zeros((M, 1)),
                         np.cumsum(rng.normal(0, np.sqrt(dtf), (M, nfine)), 1)], 1)
     exact = np.exp((mu - sig ** 2 / 2) * T + sig * W[:, -1])
-    A0 = np.zeros((4, 4)); A0[1, 0] = v["A0_21"]
-    B0 = np.zeros((4, 4)); B0[1, 0] = v["B0_21"]
-    A1 = np.zeros((4, 4)); A1[1, 0] = v["A1_21"]; A1[2, 0] = v["A1_31"]; A1[3, 2] = v["A1_43"]
-    B1 = np.zeros((4, 4))
-    B1[1, 0], B1[2, 0], B1[3, 0], B1[3, 1], B1[3, 2] = (v["B1_21"], v["B1_31"], v["B1_41"],
-                                                        v["B1_42"], v["B1_43"])
-    al = [v["al1"], v["al2"], 0, 0]
-    bb = [[v["b%d_%d" % (q, i)] for i in range(1, 5)] for q in range(1, 5)]
 
     def run(n):
         h, k, x = T / n, nfine // n, np.ones(M)
@@ -165,11 +213,11 @@ def test_sriw1_strong_order_gbm():
             I1 = Wi[:, -1]
             I10 = np.trapezoid(Wi, dx=dtf, axis=1)
             I11, I111 = (I1 ** 2 - h) / 2, (I1 ** 3 - 3 * h * I1) / 6
-            F, G, H0, H1 = [None] * 4, [None] * 4, [None] * 4, [None] * 4
+            F, G = [None] * 4, [None] * 4
             for i in range(4):
-                H0[i] = x + sum(A0[i, j] * F[j] * h + B0[i, j] * G[j] * I10 / h for j in range(i))
-                H1[i] = x + sum(A1[i, j] * F[j] * h + B1[i, j] * G[j] * np.sqrt(h) for j in range(i))
-                F[i], G[i] = mu * H0[i], sig * H1[i]
+                H0 = x + sum(A0[i, j] * F[j] * h + B0[i, j] * G[j] * I10 / h for j in range(i))
+                H1 = x + sum(A1[i, j] * F[j] * h + B1[i, j] * G[j] * np.sqrt(h) for j in range(i))
+                F[i], G[i] = mu * H0, sig * H1
             x = x + sum(al[i] * F[i] * h for i in range(4)) + sum(
                 (bb[0][i] * I1 + bb[1][i] * I11 / np.sqrt(h) + bb[2][i] * I10 / h +
                  bb[3][i] * I111 / h) * G[i] for i in range(4))

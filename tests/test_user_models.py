@@ -212,3 +212,48 @@ def test_user_model_rejects_auto_and_learned(capi, de):
             de.solve_arrays(m, o, p, u0, np.zeros(1), np.ones(1), np.array([1.0]),
                             capi.SAVE_GRID)
         assert e.value.code in (capi.GBDE_ERR_UNSUPPORTED, capi.GBDE_ERR_STATE)
+
+
+# a linear system whose W = I/(gamma h) - A needs a row swap after the first
+# elimination step once the fast modes have decayed and the steps grow
+# (eigenvalues -1.09 and -20.6 +- 78.6i)
+LIN3_A = np.array([[-1.1, 0.0, 0.2], [-9.9, 25.3, -77.0], [-54.7, 107.3, -66.4]])
+LIN3_F = """
+du[0] = p[0] * u[0] + p[1] * u[1] + p[2] * u[2];
+du[1] = p[3] * u[0] + p[4] * u[1] + p[5] * u[2];
+du[2] = p[6] * u[0] + p[7] * u[1] + p[8] * u[2];
+"""
+LIN3_J = """
+J[0][0] = p[0]; J[0][1] = p[1]; J[0][2] = p[2];
+J[1][0] = p[3]; J[1][1] = p[4]; J[1][2] = p[5];
+J[2][0] = p[6]; J[2][1] = p[7]; J[2][2] = p[8];
+"""
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("alg", ["ROSENBROCK23", "RODAS5", "RODAS5P"])
+@pytest.mark.parametrize("precision", ["fp64", "f32x2"])
+def test_rosenbrock_w_solve_with_row_swaps(capi, de, alg, precision):
+    """Rosenbrock steps whose W-matrix LU swaps rows after its first step
+    (P W = L U with whole-row swaps: every swap must reach the right-hand side
+    before the substitutions): the solution of u' = A u matches exp(A t) u0
+    within the metric's bar, and every trajectory succeeds."""
+    from scipy.linalg import expm
+    a = getattr(capi, "ALG_" + alg)
+    m = de.ODEFunction(LIN3_F, 3, 9, jac=LIN3_J, name="lin3")
+    _compile_or_skip(de, capi, m, {"ROSENBROCK23": de.Rosenbrock23(), "RODAS5": de.Rodas5(),
+                                   "RODAS5P": de.Rodas5P()}[alg], precision)
+    N = 64
+    rng = np.random.default_rng(9)
+    p = np.tile(LIN3_A.ravel(), (N, 1))
+    u0 = rng.uniform(-1, 1, (N, 3))
+    grid = de.save_grid(0.0, 5.0, 0.5)
+    o = capi.opts_default(a)
+    o.reltol, o.abstol = 1e-6, 1e-8
+    o.precision = capi.PREC_F32X2 if precision == "f32x2" else capi.PREC_FP64
+    g = de.solve_arrays(m, o, p, u0, np.zeros(N), np.full(N, 5.0), grid, capi.SAVE_GRID)
+    assert np.all(g["retcode"] == capi.RET_SUCCESS)
+    exact = np.stack([u0 @ expm(LIN3_A * t).T for t in grid], axis=1)
+    err = np.abs(g["u"] - exact) / (1e-8 + 1e-6 * np.abs(exact))
+    # Rosenbrock23 is order 2: its global error runs to tens of tolerances
+    assert err.max() <= (100.0 if alg == "ROSENBROCK23" else 10.0), err.max()
