@@ -11,13 +11,14 @@ SciMLBase interface over that ABI.
 from . import _capi, learned, tuning
 from .api import (EM, SOSRI, SRIW1, ContinuousCallback, DiscreteCallback, EnsembleGB300, EnsembleProblem, EnsembleSerial,
                   EnsembleSolution, EnsembleThreads, ODEFunction, ODEProblem, ODESolution,
+                  SDEFunction,
                   ReturnCode, EnsembleSummary, compile_model, ensemble_summary,
                   Rodas5, Rodas5P, Rosenbrock23, SDEProblem, Tsit5, Vern7, models, remake,
                   save_grid, solve, solve_arrays)
 
 __all__ = [
     "EM", "SOSRI", "SRIW1", "ContinuousCallback", "DiscreteCallback", "EnsembleGB300", "EnsembleProblem", "EnsembleSerial", "EnsembleSolution",
-    "EnsembleThreads", "ODEFunction", "ODEProblem", "ODESolution", "compile_model", "EnsembleSummary", "ensemble_summary",
+    "EnsembleThreads", "ODEFunction", "SDEFunction", "ODEProblem", "ODESolution", "compile_model", "EnsembleSummary", "ensemble_summary",
     "ReturnCode", "Rodas5", "Rodas5P",
     "Rosenbrock23", "SDEProblem", "Tsit5", "Vern7", "models", "remake", "save_grid", "solve",
     "solve_arrays",

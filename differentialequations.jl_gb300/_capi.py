@@ -141,6 +141,7 @@ SIGNATURES = {
     "gbde_ensemble_summary": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int64,
                                         C.c_int32, C.c_int32, C.POINTER(Summary)]),
     "gbde_model_register": (C.c_int, [C.POINTER(UserModel), C.POINTER(C.c_int32)]),
+    "gbde_sde_model_register": (C.c_int, [C.POINTER(UserModel), C.c_char_p, C.POINTER(C.c_int32)]),
     "gbde_model_compile": (C.c_int, [C.c_int32, C.c_int32, C.c_int32]),
     "gbde_callback_register": (C.c_int, [C.POINTER(Callback), C.POINTER(C.c_int32)]),
     "gbde_callback_compile": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32]),

@@ -91,6 +91,25 @@ def ODEFunction(f, n_state, n_param, jac=None, name="user_model"):
     return m
 
 
+def SDEFunction(f, g, n_state, n_param, jac=None, name="user_sde"):
+    """A user SDE with diagonal noise (the reference's SDEFunction(f, g),
+    qa.jl:102): du_i = f_i(u, p) dt + g_i(u, p) dW_i, both given as CUDA C++
+    statements over the scalar type T -- f fills du[0..n_state), g fills
+    g[0..n_state).  Compiled at run time for EM, SOSRI and SRIW1 (and for the
+    ODE methods on f alone); the noise is the library's counter-based stream,
+    the same as for the built-in models.  Returns a Model usable as
+    SDEProblem's f (pass g=None or the same model as g)."""
+    import ctypes as C
+    d = capi.UserModel(name=name.encode(), n_state=int(n_state), n_param=int(n_param),
+                       f_body=f.encode(), jac_body=jac.encode() if jac else None)
+    mid = C.c_int32()
+    capi.check(capi.lib().gbde_sde_model_register(C.byref(d), g.encode(), C.byref(mid)))
+    m = Model(name, mid.value, int(n_state), int(n_param), noise=True,
+              doc="user SDE model (runtime-compiled)")
+    m.f_source, m.g_source, m.jac_source = f, g, jac
+    return m
+
+
 def compile_model(model, alg, precision="fp64"):
     """Compile a user model's kernels for one algorithm and precision ahead of
     the first solve (no GPU needed); raises GBDEError with NVRTC's log."""
@@ -162,9 +181,10 @@ class SDEProblem(ODEProblem):
 
     def __init__(self, f, g, u0, tspan, p=None, **kwargs):
         if not (isinstance(f, Model) and f.noise):
-            raise TypeError("SDEProblem needs a built-in model with a noise term")
+            raise TypeError("SDEProblem needs a model with a noise term (a built-in one, or "
+                            "SDEFunction(f, g, ...))")
         if g is not None and g is not f:
-            raise TypeError("the noise term is part of the built-in model; pass g=None or g=f")
+            raise TypeError("the noise term is part of the model; pass g=None or g=f")
         super().__init__(f, u0, tspan, p, **kwargs)
 
 
@@ -256,12 +276,15 @@ class EnsembleGB300:
     time).  batching: "plain" (one launch, a thread per trajectory) or
     "persistent" (threads refill from a device work queue).  learned: False;
     True or "start" (the loaded predictor's first dt and AUTO method choice);
-    "order" (the persistent queue ordered by the predicted cost); or a tuple
-    of both names.
+    "order" (the persistent queue ordered by the predicted cost); "stiff" (the
+    AUTO method choice only); or a tuple of names.  devices: a list of GPU
+    indices to split the trajectories over in one call (contiguous slices, one
+    host thread and context per GPU, no collective); default: `device` alone.
     """
 
     def __init__(self, device=0, precision="fp64", batching="plain", learned=False,
-                 block_size=0, ctas_per_sm=0, chunk=0, out_dtype=None, timeout_s=0.0):
+                 block_size=0, ctas_per_sm=0, chunk=0, out_dtype=None, timeout_s=0.0,
+                 devices=None):
         if precision not in ("fp64", "mixed", "f32x2"):
             raise ValueError("precision must be 'fp64', 'mixed' or 'f32x2'")
         if batching not in ("plain", "persistent"):
@@ -271,6 +294,9 @@ class EnsembleGB300:
         self.learned_flags = learned_flags(learned)
         self.chunk, self.timeout_s = chunk, timeout_s
         self.out_dtype = out_dtype or ("f32" if precision == "mixed" else "f64")
+        self.devices = [int(d) for d in devices] if devices else [int(device)]
+        if not self.devices:
+            raise ValueError("devices must name at least one GPU")
 
 
 def learned_flags(learned):
@@ -609,8 +635,14 @@ def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start
     opts.chunk = int(ensemblealg.chunk)
     opts.timeout_s = float(ensemblealg.timeout_s)
 
-    res = solve_arrays(prob.f, opts, p, u0, t0, tf, save_arr, save_kind,
-                       u_dtype=ensemblealg.out_dtype, device=ensemblealg.device)
+    if len(ensemblealg.devices) > 1:
+        from . import distributed
+        res = distributed.solve_sharded(solve_arrays, ensemblealg.devices, prob.f, opts, p, u0,
+                                        t0, tf, save_arr, save_kind,
+                                        u_dtype=ensemblealg.out_dtype)
+    else:
+        res = solve_arrays(prob.f, opts, p, u0, t0, tf, save_arr, save_kind,
+                           u_dtype=ensemblealg.out_dtype, device=ensemblealg.devices[0])
     t_out = save_arr
     term = res["retcode"] == capi.RET_TERMINATED
     if np.any(term):

@@ -360,8 +360,11 @@ static int check_solve_args(gbde_ctx* ctx, const gbde_problem* prob, const gbde_
   const int alg = opts->alg;
   if (!is_ode_alg(alg) && !is_sde_alg(alg))
     return set_err(ctx, GBDE_ERR_INVALID, "unknown algorithm id %d", alg);
-  if (is_sde_alg(alg) && prob->model != GBDE_MODEL_LOTKA_VOLTERRA)
-    return set_err(ctx, GBDE_ERR_UNSUPPORTED, "SDE algorithms need a model with a noise term");
+  if (is_sde_alg(alg) && prob->model != GBDE_MODEL_LOTKA_VOLTERRA &&
+      !(prob->model >= GBDE_MODEL_USER_BASE && rtc_model_has_noise(prob->model)))
+    return set_err(ctx, GBDE_ERR_UNSUPPORTED,
+                   "SDE algorithms need a model with a noise term (the built-in Lotka-Volterra "
+                   "model, or a user model from gbde_sde_model_register)");
   if (opts->precision != GBDE_PREC_FP64 && opts->precision != GBDE_PREC_MIXED &&
       opts->precision != GBDE_PREC_F32X2)
     return set_err(ctx, GBDE_ERR_INVALID, "unknown precision %d", opts->precision);
@@ -405,10 +408,10 @@ static int check_solve_args(gbde_ctx* ctx, const gbde_problem* prob, const gbde_
     // a user model or a callback: compile (once per model, algorithm,
     // precision and callback) and load the kernels now, before anything is
     // enqueued or captured
-    if (alg == GBDE_ALG_AUTO || is_sde_alg(alg) || opts->learned)
+    if (alg == GBDE_ALG_AUTO || opts->learned || (is_sde_alg(alg) && opts->callback != 0))
       return set_err(ctx, GBDE_ERR_UNSUPPORTED,
-                     "user models and callbacks run the one-thread ODE methods, without "
-                     "GBDE_ALG_AUTO and without the learned predictor");
+                     "user models run the one-thread ODE and SDE methods and callbacks the ODE "
+                     "methods, without GBDE_ALG_AUTO and without the learned predictor");
     if (prob->model == GBDE_MODEL_VDP_RING8)
       return set_err(ctx, GBDE_ERR_UNSUPPORTED, "callbacks are not built for the 16-lane ring");
     std::string why;

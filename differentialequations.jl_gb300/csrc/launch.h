@@ -85,6 +85,7 @@ cudaError_t launch_step_kernel(K kern, const LaunchCfg& cfg, const KArgs& a, cud
 
 // User models compiled at run time (rtc.cu): ids >= GBDE_MODEL_USER_BASE.
 bool rtc_model_info(int id, int32_t* n_state, int32_t* n_param);
+bool rtc_model_has_noise(int id);
 int rtc_prepare(int id, int alg, int precision, int callback, std::string* err);
 cudaError_t launch_rtc(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
 

@@ -117,6 +117,10 @@ extern "C" int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_
   int32_t ns = 0, np = 0;
   if (gbde_model_info(prob->model, &ns, &np) != GBDE_OK)
     return fail(GBDE_ERR_INVALID, "unknown model id %d", prob->model);
+  if (prob->model >= GBDE_MODEL_USER_BASE)
+    return fail(GBDE_ERR_UNSUPPORTED,
+                "gbde_ensemble_solve_noalloc runs the built-in models only: a user model's "
+                "kernels are compiled and loaded by gbde_ensemble_solve");
   if (prob->n_state != ns || prob->n_param != np)
     return fail(GBDE_ERR_INVALID, "model %d has n_state=%d n_param=%d; got n_state=%d n_param=%d",
                 prob->model, ns, np, prob->n_state, prob->n_param);
@@ -166,6 +170,15 @@ extern "C" int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_
   if (alg == GBDE_ALG_ROSENBROCK23 && prob->model == GBDE_MODEL_VDP_RING8)
     return fail(GBDE_ERR_UNSUPPORTED,
                 "Rosenbrock23 is built for n_state <= 3 (use Rodas5 / Rodas5P for the ring)");
+  if (opts->threads_per_traj != 0 && opts->threads_per_traj != 1 && opts->threads_per_traj != 16)
+    return fail(GBDE_ERR_INVALID, "threads_per_traj must be 0, 1 or 16");
+  if (opts->threads_per_traj == 16 && prob->model != GBDE_MODEL_VDP_RING8)
+    return fail(GBDE_ERR_UNSUPPORTED, "16-lane teams are built for the 16-state ring");
+  if (opts->threads_per_traj == 1 && prob->model == GBDE_MODEL_VDP_RING8 &&
+      alg != GBDE_ALG_TSIT5 && alg != GBDE_ALG_VERN7)
+    return fail(GBDE_ERR_UNSUPPORTED,
+                "Rosenbrock methods on the 16-state ring run as 16-lane teams only");
+  if (opts->chunk < 0) return fail(GBDE_ERR_INVALID, "chunk must be >= 0");
   const int block = opts->block_size > 0 ? opts->block_size : 128;
   if (block > 128 || (block & 31))
     return fail(GBDE_ERR_INVALID, "block_size must be a multiple of 32 and <= 128");

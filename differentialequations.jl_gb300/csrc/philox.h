@@ -24,8 +24,10 @@
 // Host code that includes this header must be compiled with
 // -ffp-contract=off.
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <stdint.h>
 #include <math.h>
+#endif
 #include "common.cuh"
 
 namespace gbde {

@@ -103,7 +103,7 @@ Nvrtc& nvrtc() {
 
 // --------------------------------------------------------------- registry
 struct UserModelDef {
-  std::string name, f_body, jac_body;
+  std::string name, f_body, jac_body, g_body;  // g_body: diagonal noise (SDE models)
   int n, np;
 };
 
@@ -153,7 +153,13 @@ const char* prec_type(int precision) {
 // uses for this algorithm and precision.
 std::string alg_type(int alg, int precision) {
   const std::string T = prec_type(precision);
+  if ((alg == GBDE_ALG_EM || alg == GBDE_ALG_SOSRI || alg == GBDE_ALG_SRIW1) &&
+      precision == GBDE_PREC_F32X2)
+    return "";
   switch (alg) {
+    case GBDE_ALG_EM: return "em";
+    case GBDE_ALG_SOSRI: return "sri<tab::SosriTab, GBDE_ALG_SOSRI>";
+    case GBDE_ALG_SRIW1: return "sri<tab::Sriw1Tab, GBDE_ALG_SRIW1>";
     case GBDE_ALG_TSIT5: return "Tsit5A<GbdeRtcModel, " + T + ">";
     case GBDE_ALG_VERN7: return "Vern7A<GbdeRtcModel, " + T + ">";
     case GBDE_ALG_ROSENBROCK23: return "Ros23A<GbdeRtcModel, " + T + ">";
@@ -181,7 +187,7 @@ std::string make_source(const UserModelDef* m, int model, const CallbackDef* cb,
        "typedef unsigned short uint16_t; typedef unsigned int uint32_t;\n"
        "typedef unsigned long long uint64_t; typedef unsigned long size_t;\n"
        "#include \"solver.cuh\"\n#include \"explicit_rk.cuh\"\n#include \"rosenbrock.cuh\"\n"
-       "#include \"rodas_ff.cuh\"\n#include \"tsit5_ff.cuh\"\n#include \"vern7_ff.cuh\"\n#include \"ros23_ff.cuh\"\n#include \"dual.cuh\"\nnamespace gbde {\n";
+       "#include \"rodas_ff.cuh\"\n#include \"tsit5_ff.cuh\"\n#include \"vern7_ff.cuh\"\n#include \"ros23_ff.cuh\"\n#include \"dual.cuh\"\n#include \"sde.cuh\"\nnamespace gbde {\n";
   char buf[256];
   if (m) {
     s += "struct UserModel {\n";
@@ -200,8 +206,14 @@ std::string make_source(const UserModelDef* m, int model, const CallbackDef* cb,
       s += m->jac_body;
       s += "\n";
     }
-    s += "  }\n"
-         "  __device__ static void features(const double*, const double*, double, float* f) {\n"
+    s += "  }\n";
+    if (!m->g_body.empty()) {
+      s += "  template <class T> __device__ static void g(T* g, const T* u, const T* p) {\n";
+      s += "#line 1 \"" + m->name + ":g\"\n";
+      s += m->g_body;
+      s += "\n  }\n";
+    }
+    s += "  __device__ static void features(const double*, const double*, double, float* f) {\n"
          "    for (int i = 0; i < 8; ++i) f[i] = 0.0f;\n  }\n};\n"
          "typedef UserModel GbdeRtcModel;\n";
   } else {
@@ -223,8 +235,21 @@ std::string make_source(const UserModelDef* m, int model, const CallbackDef* cb,
     s += "typedef NoCallback GbdeRtcCallback;\n";
   }
   s += "}  // namespace gbde\nusing namespace gbde;\n";
-  s += "typedef " + alg_type(alg, precision) + " GbdeRtcAlg;\n";
+  const std::string at = alg_type(alg, precision);
   s += std::string("typedef ") + prec_type(precision) + " GbdeRtcT;\n";
+  if (at == "em" || at.rfind("sri<", 0) == 0) {
+    // SDE methods: the library's EM / SRI drivers around the user's f and g;
+    // no initial-dt pre-pass (an empty kernel keeps the loader's interface)
+    const std::string body =
+        at == "em" ? std::string("em_all<GbdeRtcModel, GbdeRtcT>(a);")
+                   : "sri_all<GbdeRtcModel, GbdeRtcT, " + std::string(mixed ? "true" : "false") +
+                         ", " + at.substr(4, at.size() - 5) + ">(a);";
+    s += "extern \"C\" __global__ void __launch_bounds__(128) gbde_rtc_step(const KArgs a) {\n  " +
+         body + "\n}\n"
+         "extern \"C\" __global__ void gbde_rtc_init_dt(const KArgs, double*) {}\n";
+    return s;
+  }
+  s += "typedef " + at + " GbdeRtcAlg;\n";
   s += "extern \"C\" __global__ void __launch_bounds__(128) gbde_rtc_step(const KArgs a) {\n"
        "  integrate_all<GbdeRtcAlg, GbdeRtcModel, GbdeRtcT, ";
   s += mixed ? "true" : "false";
@@ -254,7 +279,13 @@ int compile_locked(int id, int alg, int precision, int callback, Compiled** out)
     return fail(GBDE_ERR_INVALID, "unknown callback id " + std::to_string(callback));
   if (alg_type(alg, precision).empty())
     return fail(GBDE_ERR_UNSUPPORTED,
-                "runtime-compiled kernels run Tsit5, Vern7, Rosenbrock23, Rodas5 and Rodas5P");
+                "runtime-compiled kernels run Tsit5, Vern7, Rosenbrock23, Rodas5 and Rodas5P, "
+                "and EM, SOSRI and SRIW1 in FP64 or mixed precision");
+  const bool sde = alg == GBDE_ALG_EM || alg == GBDE_ALG_SOSRI || alg == GBDE_ALG_SRIW1;
+  if (sde && (cb || !m || m->g_body.empty()))
+    return fail(GBDE_ERR_UNSUPPORTED,
+                "SDE methods need a user model registered with its noise term "
+                "(gbde_sde_model_register), without a callback");
   Nvrtc& nv = nvrtc();
   if (!nv.ok) return fail(GBDE_ERR_UNSUPPORTED, nv.why);
   const std::string src = make_source(m, id, cb, alg, precision);
@@ -303,6 +334,12 @@ bool rtc_model_info(int id, int32_t* n_state, int32_t* n_param) {
   if (n_state) *n_state = m->n;
   if (n_param) *n_param = m->np;
   return true;
+}
+
+bool rtc_model_has_noise(int id) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  const UserModelDef* m = find_model(id);
+  return m && !m->g_body.empty();
 }
 
 // Compile (if not cached) and load the kernels of (model, alg, precision).
@@ -386,7 +423,7 @@ cudaError_t launch_rtc(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
 
 extern "C" {
 
-int gbde_model_register(const gbde_user_model* def, int32_t* model_id) {
+static int register_model(const gbde_user_model* def, const char* g_body, int32_t* model_id) {
   if (!def || !model_id || !def->f_body)
     return fail(GBDE_ERR_INVALID, "def, def->f_body and model_id must be non-NULL");
   if (def->n_state < 1 || def->n_state > GBDE_USER_MAX_STATE)
@@ -399,12 +436,23 @@ int gbde_model_register(const gbde_user_model* def, int32_t* model_id) {
     if (!((ch >= 'a' && ch <= 'z') || (ch >= 'A' && ch <= 'Z') || (ch >= '0' && ch <= '9'))) ch = '_';
   m.f_body = def->f_body;
   m.jac_body = def->jac_body ? def->jac_body : "";
+  m.g_body = g_body ? g_body : "";
   m.n = def->n_state;
   m.np = def->n_param;
   std::lock_guard<std::mutex> lk(g_mu);
   *model_id = GBDE_MODEL_USER_BASE + (int32_t)g_models.size();
   g_models.push_back(std::move(m));
   return GBDE_OK;
+}
+
+int gbde_model_register(const gbde_user_model* def, int32_t* model_id) {
+  return register_model(def, nullptr, model_id);
+}
+
+int gbde_sde_model_register(const gbde_user_model* def, const char* g_body, int32_t* model_id) {
+  if (!g_body || !g_body[0])
+    return fail(GBDE_ERR_INVALID, "g_body (the diagonal noise) must be non-empty");
+  return register_model(def, g_body, model_id);
 }
 
 int gbde_model_compile(int32_t model_id, int32_t alg, int32_t precision) {

@@ -22,8 +22,6 @@
 //    Every normal comes from the counter-based stream in draw order, so the
 //    host can replay a trajectory exactly.
 #pragma once
-#include <type_traits>
-
 #include "philox.h"
 #include "solver.cuh"
 #include "tableaus.h"
@@ -117,7 +115,7 @@ GBDE_D bool em_last_step(double t0, double tf, double h, int64_t n) {
 // those boundaries, below FP32 resolution.
 template <class M>
 __device__ void em_steps_f32(const KArgs& a, int64_t i, double t0, double tf, double h, float* u,
-                             const float* p, int js, NormalStream<float>& ns) {
+                             const float* p, int js, NormalStream<float>& ns, uint64_t t_start) {
   constexpr int N = M::N;
   constexpr int64_t kNever = 0x7fffffffffffffffll;
   // index of the last step (-1: no step)
@@ -166,6 +164,12 @@ __device__ void em_steps_f32(const KArgs& a, int64_t i, double t0, double tf, do
 #pragma unroll
   for (int k = 0; k < M::NP; ++k) pr[k] = p[k];
   for (; n < nrun; ++n) {
+    // the optional device deadline, every 1024 steps
+    if (a.timeout_ns && (n & 1023) == 0 && n > 0 && global_ns() - t_start > a.timeout_ns) {
+      ret = GBDE_RET_TIMEOUT;
+      atomicOr(a.flag, 1);
+      break;
+    }
     const bool lastn = n == nl;
     const float hs = lastn ? hTl : hT, sh = lastn ? sql : sq;
     float fu[N], gu[N], un[N];
@@ -201,6 +205,7 @@ __device__ void em_steps_f32(const KArgs& a, int64_t i, double t0, double tf, do
     }
   }
   if (ret == GBDE_RET_SUCCESS && n < nl + 1) ret = GBDE_RET_MAXITERS;
+  // (a timed-out trajectory keeps GBDE_RET_TIMEOUT; its unreached saves are NaN)
   const double t = n == 0 ? t0 : t_end(n - 1);
   finish_sde<N, float>(a, i, ret, js, (int)n, 0, (int)(2 * n), t, GBDE_ALG_EM, h);
 }
@@ -210,6 +215,7 @@ __device__ void em_all(const KArgs& a) {
   constexpr int N = M::N;
   WorkSource src;
   src.init();
+  const uint64_t t_start = a.timeout_ns ? global_ns() : 0;
   int64_t i;
   while ((i = src.next(a)) >= 0) {
     T p[M::NP], u[N];
@@ -235,7 +241,7 @@ __device__ void em_all(const KArgs& a) {
     NormalStream<T> ns;
     ns.init(a.seed, (uint64_t)i);
     if constexpr (sizeof(T) == 4) {
-      em_steps_f32<M>(a, i, t0, tf, h, u, p, js, ns);
+      em_steps_f32<M>(a, i, t0, tf, h, u, p, js, ns, t_start);
       continue;
     }
     int ret = GBDE_RET_SUCCESS;
@@ -244,6 +250,11 @@ __device__ void em_all(const KArgs& a) {
     while (t < tf) {
       if (n >= a.maxiters) {
         ret = GBDE_RET_MAXITERS;
+        break;
+      }
+      if (a.timeout_ns && (n & 1023) == 0 && n > 0 && global_ns() - t_start > a.timeout_ns) {
+        ret = GBDE_RET_TIMEOUT;
+        atomicOr(a.flag, 1);
         break;
       }
       double tn1 = t0 + (double)(n + 1) * h;
@@ -408,12 +419,17 @@ struct SriUse {
   }
 };
 
-// Compile-time loop: f(std::integral_constant<int, I>) for I = B .. E-1, so
-// that table entries are read as constants (and zero entries drop out).
+// Compile-time loop: f(IntC<I>) for I = B .. E-1, so that table entries are
+// read as constants (and zero entries drop out).  (No <type_traits>: the
+// runtime-compiled kernels include this header under NVRTC.)
+template <int I>
+struct IntC {
+  static constexpr int value = I;
+};
 template <int B, int E, class F>
 GBDE_D void static_for(F&& f) {
   if constexpr (B < E) {
-    f(std::integral_constant<int, B>{});
+    f(IntC<B>{});
     static_for<B + 1, E>(f);
   }
 }
@@ -476,6 +492,7 @@ __device__ void sri_all(const KArgs& a) {
   constexpr int N = M::N;
   WorkSource src;
   src.init();
+  const uint64_t t_start = a.timeout_ns ? global_ns() : 0;
   int64_t i;
   NoiseStack<N, T> stk;
   while ((i = src.next(a)) >= 0) {
@@ -639,6 +656,10 @@ __device__ void sri_all(const KArgs& a) {
         if (iters >= a.maxiters) ret = GBDE_RET_MAXITERS;
         else if (a.adaptive && dt_too_small(h, a.dtmin, t))
           ret = GBDE_RET_DTLESSTHANMIN;
+        else if (a.timeout_ns && (iters & 31) == 0 && global_ns() - t_start > a.timeout_ns) {
+          ret = GBDE_RET_TIMEOUT;
+          atomicOr(a.flag, 1);
+        }
       }
     }
     finish_sde<N, T>(a, i, ret, js, nacc, nrej, nfev, t + tlo, ALG, dt1);

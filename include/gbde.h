@@ -307,7 +307,19 @@ GBDE_API int gbde_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
  *     call's contents (each call clears what it needs in stream order).
  *     Calls that overlap on the GPU race: serialise them on one stream or
  *     with events;
- *   - learned != 0 is rejected (GBDE_ERR_STATE); device_ms is not measured (0).
+ *   - options and sizes are checked as gbde_ensemble_solve checks them; in
+ *     addition these are rejected: learned != 0 (GBDE_ERR_STATE: no
+ *     predictor), GBDE_ALG_AUTO (GBDE_ERR_UNSUPPORTED: its per-trajectory lists
+ *     grow with n_traj), callback != 0 and user models (GBDE_ERR_UNSUPPORTED:
+ *     their kernels are compiled and loaded by gbde_ensemble_solve),
+ *     out->reduce (GBDE_ERR_UNSUPPORTED), GBDE_PREC_F32X2 on the 16-state ring
+ *     (GBDE_ERR_UNSUPPORTED);
+ *   - the device deadline (timeout_s) works as in gbde_ensemble_solve: the
+ *     status word in the static array reports it (GBDE_ERR_TIMEOUT);
+ *   - device_ms is not measured (0);
+ *   - the device address of the array is looked up once per device and kept
+ *     for the process: after a cudaDeviceReset the entry point must not be
+ *     called again in that process.
  * Blocks until the kernels have finished. */
 #define GBDE_NOALLOC_SCRATCH_BYTES 256
 GBDE_API int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_opts* opts,
@@ -421,7 +433,9 @@ GBDE_API int gbde_ensemble_summary(gbde_ctx* ctx, const void* u, int32_t u_dtype
  * precision compiles the library's step kernels around f with NVRTC for
  * sm_103a (seconds); later solves reuse the cached cubin.  User models run
  * Tsit5, Vern7, Rosenbrock23, Rodas5 and Rodas5P, one thread per trajectory,
- * in every batching mode; not GBDE_ALG_AUTO, SDE methods or learned=1.     */
+ * in every batching mode; models registered with a noise term
+ * (gbde_sde_model_register) also run EM, SOSRI and SRIW1 in FP64 or mixed
+ * precision; not GBDE_ALG_AUTO or learned=1.                               */
 typedef struct {
   const char* name;     /* label used in compile messages (may be NULL)    */
   int32_t n_state;      /* 1 .. GBDE_USER_MAX_STATE                        */
@@ -433,6 +447,15 @@ typedef struct {
 /* Register a user model; *model_id receives its id (>= GBDE_MODEL_USER_BASE).
  * Source is copied; nothing is compiled yet.  Process-wide, thread-safe. */
 GBDE_API int gbde_model_register(const gbde_user_model* def, int32_t* model_id);
+/* Register a user SDE model (replaces SDEFunction(f, g), qa.jl:102, with
+ * diagonal noise): def as for gbde_model_register (f is the drift), and
+ * g_body the body of
+ *     template <class T> void g(T* g, const T* u, const T* p)
+ * filling g[0..n_state), the diagonal noise: du_i = f_i dt + g_i dW_i.  The
+ * SDE methods draw the same counter-based normal stream as for built-in models
+ * (gbde_philox_normals regenerates it).  The id also runs the ODE methods on f. */
+GBDE_API int gbde_sde_model_register(const gbde_user_model* def, const char* g_body,
+                                     int32_t* model_id);
 /* Compile (and cache) a user model's kernels for one algorithm and precision
  * without a GPU; GBDE_ERR_INVALID with NVRTC's log in gbde_last_error(NULL)
  * when the source does not compile, GBDE_ERR_UNSUPPORTED without NVRTC. */

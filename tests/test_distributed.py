@@ -72,3 +72,50 @@ def test_two_rank_sharded_solve(tmp_path, oracle, de):
                        de.save_grid(0.0, 1.0, 0.1), capi.SAVE_GRID)
     assert np.array_equal(g["u"], ref["u"])
     assert np.array_equal(g["retcode"], ref["retcode"])
+
+
+def _oracle_solver(oracle, calls):
+    """Stand-in for api.solve_arrays on the CPU (same signature; writes into
+    `out`), recording which device each slice was given."""
+    def solver(model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", device=0, out=None,
+               reduce=False):
+        r = oracle.solve(None, model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype=u_dtype)
+        for k in ("u", "retcode", "naccept", "nreject", "nf", "t_end"):
+            out[k][...] = r[k]
+        calls.append((device, len(p)))
+        res = dict(out, device_ms=1.0, total_ms=2.0)
+        if reduce:
+            u = np.asarray(r["u"], np.float64)
+            res["reduce"] = np.stack([u.sum(0), (u * u).sum(0)])
+        return res
+    return solver
+
+
+@pytest.mark.parametrize("ndev", [1, 2, 3, 5])
+def test_solve_sharded_reassembles_bitwise(oracle, de, ndev):
+    """One-call sharding over several GPUs (EnsembleGB300(devices=...)):
+    contiguous slices, each written into its rows of the full outputs, equal
+    a single solve bitwise; per-trajectory save times are sliced with their
+    trajectories; reduction sums add up across slices."""
+    from differentialequations_gb300 import distributed
+    rng = np.random.default_rng(8)
+    N = 41
+    p = np.array([0.04, 3e7, 1e4]) * 10 ** rng.uniform(-1, 1, (N, 3))
+    u0 = np.tile([1.0, 0.0, 0.0], (N, 1))
+    t0, tf = np.zeros(N), 10 ** rng.uniform(1, 3, N)
+    saveat = tf[:, None] * np.linspace(0.1, 1.0, 6)
+    opts = oracle.opts_default(oracle.ALG_RODAS5)
+    opts.reltol, opts.abstol = 1e-6, 1e-10
+    M = oracle.ModelRef(oracle.MODEL_ROBERTSON)
+    calls = []
+    got = distributed.solve_sharded(_oracle_solver(oracle, calls), list(range(10, 10 + ndev)), M,
+                                    opts, p, u0, t0, tf, saveat, oracle.SAVE_PER_TRAJ,
+                                    reduce=True)
+    ref = oracle.solve(None, M, opts, p, u0, t0, tf, saveat, oracle.SAVE_PER_TRAJ)
+    for k in ("u", "retcode", "naccept", "nreject", "t_end"):
+        assert np.array_equal(got[k], ref[k]), k
+    assert sorted(d for d, _ in calls) == list(range(10, 10 + ndev))
+    sizes = [b - a for a, b in got["spans"]]
+    assert sum(sizes) == N and max(sizes) - min(sizes) <= 1
+    assert [a for a, _ in got["spans"]] == [0] + list(np.cumsum(sizes)[:-1])
+    np.testing.assert_allclose(got["mean"], ref["u"].mean(0), rtol=1e-12, atol=1e-15)

@@ -207,14 +207,17 @@ def test_em_fp32_step_bookkeeping(de, oracle, rng):
     assert np.any(r["retcode"] == capi.RET_MAXITERS) and np.any(r["retcode"] == capi.RET_SUCCESS)
 
 
+@pytest.mark.parametrize("alg", ["SOSRI", "SRIW1"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_sosri_parity(de, oracle, rng, precision):
+def test_sosri_parity(de, oracle, rng, precision, alg):
+    """SOSRI (and SRIW1) on the GPU against the oracle on identical noise."""
     capi = de._capi
     model = de.models.lotka_volterra
     N = 1000
     p, u0, t0, tf = make_inputs(de, model, N, rng)
     saveat = de.save_grid(0.0, 10.0, 1.0)
-    g, r, _ = run_both(de, oracle, model, capi.ALG_SOSRI, p, u0, t0, tf, saveat, capi.SAVE_GRID,
+    g, r, _ = run_both(de, oracle, model, getattr(capi, "ALG_" + alg), p, u0, t0, tf, saveat,
+                       capi.SAVE_GRID,
                        precision=precision, noise_f32=(precision == "mixed"),
                        u_dtype="f64" if precision == "fp64" else "f32",
                        reltol=1e-3, abstol=1e-3, seed=11)
@@ -299,6 +302,31 @@ def test_device_deadline_returns_status(de, rng):
     g = de.solve_arrays(model, opts, p[:100], u0[:100], t0[:100], tf[:100], tf[:100, None],
                         capi.SAVE_PER_TRAJ)
     assert np.all(g["retcode"] == capi.RET_SUCCESS)
+
+
+@pytest.mark.parametrize("alg,precision", [("EM", "fp64"), ("EM", "mixed"), ("SOSRI", "mixed"),
+                                           ("SRIW1", "fp64")])
+def test_sde_device_deadline_returns_status(de, rng, alg, precision):
+    """The SDE loops honour the device deadline as the ODE loops do: a solve
+    whose deadline expires returns GBDE_ERR_TIMEOUT (no fault, no hang)."""
+    capi = de._capi
+    model = de.models.lotka_volterra
+    N = 20000
+    p, u0, t0, tf = make_inputs(de, model, N, rng)
+    opts = capi.opts_default(getattr(capi, "ALG_" + alg))
+    opts.precision = capi.PREC_MIXED if precision == "mixed" else capi.PREC_FP64
+    opts.seed = 3
+    if alg == "EM":
+        opts.dt = 1e-5
+        opts.maxiters = 10 ** 8
+    else:
+        opts.reltol = opts.abstol = 1e-7
+        opts.maxiters = 10 ** 8
+    opts.timeout_s = 1e-6
+    with pytest.raises(capi.GBDEError) as e:
+        de.solve_arrays(model, opts, p, u0, t0, tf, de.save_grid(0.0, 10.0, 1.0), capi.SAVE_GRID,
+                        u_dtype="f32" if precision == "mixed" else "f64")
+    assert e.value.code == capi.GBDE_ERR_TIMEOUT
 
 
 def test_device_mode_matches_host_mode(de, rng):
@@ -448,3 +476,22 @@ def test_f32x2_rejected_where_not_built(de, rng):
     with pytest.raises(capi.GBDEError) as e:
         de.solve_arrays(de.models.lotka_volterra, o, p, u0, t0, tf, np.array([0.0]), capi.SAVE_GRID)
     assert e.value.code == capi.GBDE_ERR_UNSUPPORTED
+
+
+def test_one_call_sharding_matches_single_device(de):
+    """EnsembleGB300(devices=[...]) splits the ensemble into contiguous
+    slices solved concurrently (one host thread and context per entry; here
+    both on GPU 0) and reassembles them in place: bitwise the single-device
+    solve."""
+    N = 5001
+    rng = np.random.default_rng(31)
+    p = np.array([10.0, 28.0, 8.0 / 3.0]) * rng.uniform(0.9, 1.1, (N, 3))
+    ens = de.EnsembleProblem(de.ODEProblem(de.models.lorenz, [1.0, 0.0, 0.0], (0.0, 1.0),
+                                           p[0]), batch=lambda prob, n: {"p": p})
+    one = de.solve(ens, de.Tsit5(), de.EnsembleGB300(device=0), trajectories=N, saveat=0.1,
+                   reltol=1e-8, abstol=1e-8)
+    two = de.solve(ens, de.Tsit5(), de.EnsembleGB300(devices=[0, 0]), trajectories=N,
+                   saveat=0.1, reltol=1e-8, abstol=1e-8)
+    assert one.converged and two.converged
+    assert np.array_equal(one.U, two.U)
+    assert np.array_equal(one.retcode, two.retcode)

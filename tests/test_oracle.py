@@ -203,13 +203,14 @@ def test_em_uses_the_stream(oracle, capi, de):
     assert np.allclose(r["u"][0, -1], u, rtol=1e-13, atol=0)
 
 
-def test_sri_reduces_to_rk2_without_noise(oracle, capi, de):
-    """SRIW1 with sigma = 0 is its deterministic 2-stage part: an adaptive
-    solve at tight tolerance matches the ODE truth."""
+@pytest.mark.parametrize("alg", ["SOSRI", "SRIW1"])
+def test_sri_reduces_to_rk2_without_noise(oracle, capi, de, alg):
+    """SOSRI and SRIW1 with sigma = 0 are their deterministic parts (order 2):
+    an adaptive solve at tight tolerance matches the ODE truth."""
     model = de.models.lotka_volterra
     p = [1.5, 1.0, 3.0, 1.0, 0.0]
     grid = np.linspace(0, 2, 5)
-    r = run(oracle, capi, model, "SOSRI", p, [1.0, 1.0], (0.0, 2.0), grid, reltol=1e-7,
+    r = run(oracle, capi, model, alg, p, [1.0, 1.0], (0.0, 2.0), grid, reltol=1e-7,
             abstol=1e-7, seed=1)
     assert r["retcode"][0] == capi.RET_SUCCESS
     ref = solve_ivp(lambda t, u: [p[0] * u[0] - p[1] * u[0] * u[1], p[3] * u[0] * u[1] - p[2] * u[1]],
@@ -217,7 +218,8 @@ def test_sri_reduces_to_rk2_without_noise(oracle, capi, de):
     assert np.max(np.abs(r["u"][0] - ref)) < 1e-4
 
 
-def test_sri_adaptive_statistics(oracle, capi, de):
+@pytest.mark.parametrize("alg", ["SOSRI", "SRIW1"])
+def test_sri_adaptive_statistics(oracle, capi, de, alg):
     """Adaptive SRI with rejection sampling with memory keeps the Brownian
     path a Brownian path: on dX = sigma X dW (mean-zero drift) E[X_T] = X0,
     Var[log X_T] = sigma^2 T."""
@@ -225,7 +227,7 @@ def test_sri_adaptive_statistics(oracle, capi, de):
     N = 4000
     # alpha = beta = gamma = delta = 0: pure multiplicative noise
     p = np.tile([0.0, 0.0, 0.0, 0.0, 0.5], (N, 1))
-    r = run(oracle, capi, model, "SOSRI", p, np.ones((N, 2)), (0.0, 1.0), np.array([1.0]),
+    r = run(oracle, capi, model, alg, p, np.ones((N, 2)), (0.0, 1.0), np.array([1.0]),
             reltol=1e-2, abstol=1e-2, seed=3)
     assert np.all(r["retcode"] == capi.RET_SUCCESS)
     assert r["nreject"].sum() > 0  # the rejection path was exercised

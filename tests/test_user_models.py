@@ -257,3 +257,103 @@ def test_rosenbrock_w_solve_with_row_swaps(capi, de, alg, precision):
     err = np.abs(g["u"] - exact) / (1e-8 + 1e-6 * np.abs(exact))
     # Rosenbrock23 is order 2: its global error runs to tens of tolerances
     assert err.max() <= (100.0 if alg == "ROSENBROCK23" else 10.0), err.max()
+
+
+# the built-in Lotka-Volterra SDE (drift and diagonal noise sigma u) restated
+LV_F = """
+du[0] = p[0] * u[0] - p[1] * u[0] * u[1];
+du[1] = p[3] * u[0] * u[1] - p[2] * u[1];
+"""
+LV_G = """
+g[0] = p[4] * u[0];
+g[1] = p[4] * u[1];
+"""
+
+
+@pytest.mark.parametrize("alg", ["EM", "SOSRI", "SRIW1"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_user_sde_compiles(capi, de, alg, precision):
+    """A user SDE (SDEFunction: drift and diagonal noise as source) compiles
+    into the library's EM / SRI drivers without a GPU."""
+    m = de.SDEFunction(LV_F, LV_G, 2, 5, name="lv_user")
+    assert m.noise and capi.model_info(m.id) == (2, 5)
+    _compile_or_skip(de, capi, m, getattr(de, alg)(), precision)
+
+
+def test_user_sde_rejections(capi, de):
+    m = de.SDEFunction(LV_F, LV_G, 2, 5, name="lv_user")
+    with pytest.raises(capi.GBDEError) as e:  # no FP32-pair SDE kernels
+        de.compile_model(m, de.EM(), "f32x2")
+    assert e.value.code == capi.GBDE_ERR_UNSUPPORTED
+    ode = de.ODEFunction(LV_F, 2, 5, name="lv_drift_only")
+    with pytest.raises(capi.GBDEError) as e:  # an ODE model has no noise term
+        de.compile_model(ode, de.EM(), "fp64")
+    assert e.value.code == capi.GBDE_ERR_UNSUPPORTED
+    with pytest.raises(TypeError):
+        de.SDEProblem(ode, None, [1.0, 1.0], (0.0, 1.0), np.ones(5))
+    import ctypes as C
+    d = capi.UserModel(name=b"x", n_state=2, n_param=5, f_body=LV_F.encode(), jac_body=None)
+    mid = C.c_int32()
+    assert capi.lib().gbde_sde_model_register(C.byref(d), b"", C.byref(mid)) == \
+        capi.GBDE_ERR_INVALID
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("alg,precision", [("EM", "fp64"), ("EM", "mixed"), ("SOSRI", "fp64"),
+                                           ("SOSRI", "mixed"), ("SRIW1", "fp64")])
+def test_user_sde_matches_builtin_oracle(capi, de, oracle, alg, precision):
+    """The user restatement of the Lotka-Volterra SDE, compiled at run time,
+    against the CPU oracle's built-in model on the same counter-based noise:
+    EM in FP64 within 1e-12 relative; with FP32 state within 1e-3 of the
+    oracle driven by the same FP32 normals; adaptive SRI on the oracle's
+    Brownian path for >= 95 % of trajectories (an FMA-contracted accept /
+    reject flip continues a trajectory on another path) with weighted error
+    <= 10 on those."""
+    m = de.SDEFunction(LV_F, LV_G, 2, 5, name="lv_user")
+    N = 1000
+    rng = np.random.default_rng(12)
+    p = np.c_[np.array([1.5, 1.0, 3.0, 1.0]) * rng.uniform(0.8, 1.2, (N, 4)), np.full(N, 0.1)]
+    u0, t0, tf = np.ones((N, 2)), np.zeros(N), np.full(N, 5.0)
+    grid = de.save_grid(0.0, 5.0, 0.5)
+    o = capi.opts_default(getattr(capi, "ALG_" + alg))
+    o.seed = 21
+    if alg == "EM":
+        o.dt = 1e-3
+    else:
+        o.reltol = o.abstol = 1e-3
+    o.precision = capi.PREC_MIXED if precision == "mixed" else capi.PREC_FP64
+    g = de.solve_arrays(m, o, p, u0, t0, tf, grid, capi.SAVE_GRID,
+                        u_dtype="f32" if precision == "mixed" else "f64")
+    assert np.all(g["retcode"] == capi.RET_SUCCESS)
+    r = oracle.solve(capi, de.models.lotka_volterra, o, p, u0, t0, tf, grid, capi.SAVE_GRID,
+                     nthreads=8, noise_f32=precision == "mixed")
+    u = np.asarray(g["u"], np.float64)
+    if alg == "EM":
+        rel = np.max(np.abs(u - r["u"]) / np.abs(r["u"]))
+        assert rel <= (1e-12 if precision == "fp64" else 1e-3), rel
+    else:
+        same = (g["naccept"] == r["naccept"]) & (g["nreject"] == r["nreject"])
+        e = oracle.weighted_errors(u, r["u"], 1e-3, 1e-3).max(axis=(1, 2))
+        assert same.mean() >= 0.95, same.mean()
+        assert e[same].max() <= 10.0
+
+
+@pytest.mark.gpu
+def test_user_sde_gbm_strong_error(capi, de, oracle):
+    """Geometric Brownian motion dX = mu X dt + s X dW as a user SDE: EM at
+    dt = 1e-3 against the exact solution X0 exp((mu - s^2/2) t + s W_t) on
+    the Brownian path regenerated on the host from the same counter-based
+    stream (gbde_philox_normals): the mean strong error is of order sqrt(dt)."""
+    m = de.SDEFunction("du[0] = p[0] * u[0];", "g[0] = p[1] * u[0];", 1, 2, name="gbm")
+    N, dt, T = 256, 1e-3, 1.0
+    p = np.tile([0.5, 0.4], (N, 1))
+    o = capi.opts_default(capi.ALG_EM)
+    o.dt, o.seed = dt, 77
+    g = de.solve_arrays(m, o, p, np.ones((N, 1)), np.zeros(N), np.full(N, T), np.array([T]),
+                        capi.SAVE_GRID)
+    assert np.all(g["retcode"] == capi.RET_SUCCESS)
+    nsteps = int(round(T / dt))
+    W = np.array([np.sqrt(dt) * oracle.normals(77, i, 0, nsteps).sum() for i in range(N)])
+    exact = np.exp((0.5 - 0.08) * T + 0.4 * W)
+    err = np.abs(g["u"][:, 0, 0] - exact)
+    assert err.mean() < 5 * np.sqrt(dt) * 0.4 * exact.mean(), err.mean()
