@@ -10,7 +10,13 @@ Writes ``dense_coeffs.h`` beside this file.  Run: ``python derive_dense_output.p
    as polynomial identities, plus b_j(1) = b_j (the interpolant ends at y1);
    minimum-norm solution.
 
-2. Rodas5 / Rodas5P 4th-order continuous extension in transformed variables
+2. Vern7 7th-order continuous extension by bootstrapping (Enright, Jackson,
+   Norsett, Thomsen, ACM TOMS 12 (1986)): three extra stages on the 5th-order
+   extension, a degree-6 Hermite-Birkhoff interpolant through y0, y1, f0, f1
+   and their values, four more stages on it and the degree-7 interpolant;
+   checked here against the order-7 conditions over all 18 stages.
+
+3. Rodas5 / Rodas5P 4th-order continuous extension in transformed variables
        y(theta) = (1-theta) y0 + theta y1
                   + theta (1-theta) sum_j (H2_j + theta H3_j + theta^2 H4_j) u_j
    over stages 1..7: the continuous order conditions up to order 4
@@ -179,6 +185,68 @@ def derive_vern7(tb, q=5):
     return B, resid
 
 
+# -------------------------------------------- Vern7, 7th-order interpolant
+# Level-1 and level-2 abscissae of the bootstrapped interpolant (chosen for a
+# small order-8 defect and moderate coefficients; the Hermite-Birkhoff systems
+# are nonsingular for them).
+V7_THETA1 = (0.12, 0.25, 0.78)
+V7_THETA2 = (0.11, 0.22, 0.55, 0.75)
+
+
+def _hermite_birkhoff(nstage, nodes, node_stages, b, deg):
+    """Coefficients of u(theta) = y0 + h sum_{m=1..deg} c_m theta^m with
+    u(1) = y1 = y0 + h b.K, u'(0) = h K_1, u'(1) = h K_11 (= f(y1)) and
+    u'(theta_i) = h K_{node_stages[i]}: returns C (deg x nstage) with
+    c_m = sum_j C[m-1, j] K_j."""
+    V, R = [], []
+    V.append(np.ones(deg))
+    r = np.zeros(nstage)
+    r[:len(b)] = b
+    R.append(r)
+    v = np.zeros(deg)
+    v[0] = 1.0
+    V.append(v)
+    r = np.zeros(nstage)
+    r[0] = 1.0
+    R.append(r)
+    V.append(np.arange(1, deg + 1, dtype=float))
+    r = np.zeros(nstage)
+    r[10] = 1.0
+    R.append(r)
+    for th, j in zip(nodes, node_stages):
+        V.append(np.arange(1, deg + 1) * th ** np.arange(0, deg))
+        r = np.zeros(nstage)
+        r[j] = 1.0
+        R.append(r)
+    V = np.array(V)
+    assert V.shape == (deg, deg)
+    return np.linalg.solve(V, np.array(R))
+
+
+def derive_vern7_lazy(tb, B5):
+    """7th-order continuous extension of Vern7 by bootstrapping (W.H. Enright,
+    K.R. Jackson, S.P. Norsett, P.G. Thomsen, "Interpolants for Runge-Kutta
+    formulas", ACM TOMS 12 (1986) 193-218): stages 1-10 of Vern7 and
+    K11 = f(y1); three stages at theta in V7_THETA1 on the 5th-order
+    extension (local error O(h^6)) feed a degree-6 Hermite-Birkhoff
+    interpolant (y0, y1, f0, f1 and their derivatives: O(h^7)); four stages at
+    theta in V7_THETA2 on that one feed the degree-7 interpolant (O(h^8),
+    order 7).  The seven extra stages are evaluated only on steps that save.
+    Returns (AA: 18 x 18 stage matrix, W1 3 x 11, W2 4 x 14, C7 7 x 18)."""
+    A, b, _ = vern7_tableau(tb)
+    S = 18
+    AA = np.zeros((S, S))
+    AA[:10, :10] = A
+    AA[10, :10] = b
+    W1 = np.array([B5 @ (th ** np.arange(1, 6)) for th in V7_THETA1])
+    AA[11:14, :11] = W1
+    C6 = _hermite_birkhoff(14, V7_THETA1, (11, 12, 13), b, 6)
+    W2 = np.array([(th ** np.arange(1, 7)) @ C6 for th in V7_THETA2])
+    AA[14:18, :14] = W2
+    C7 = _hermite_birkhoff(S, V7_THETA2, (14, 15, 16, 17), b, 7)
+    return AA, W1, W2, C7
+
+
 # ---------------------------------------------------------------- Rodas
 def derive_rodas(tb, name):
     """4th-order continuous extension over stages u_1..u_7:
@@ -249,6 +317,36 @@ def main():
         for k in range(B.shape[1]):
             lines.append("constexpr double B%d_%d = %s;" % (j + 1, k + 1, fmt(B[j, k])))
     lines.append("}  // namespace vern7d")
+    AA, W1, W2, C7 = derive_vern7_lazy(tb, B)
+    T7 = trees(7)
+    r7l = max(abs(((th ** np.arange(1, 8)) @ C7) @ rk_phi(t, AA) - th ** rho(t) / tree_gamma(t))
+              for th in (0.1, 0.5, 0.9) for n in range(1, 8) for t in T7[n])
+    assert r7l < 1e-11, r7l
+    lines += [
+        "// Vern7 7th-order continuous extension by bootstrapping (derive_vern7_lazy):",
+        "// stages K12..K14 at y0 + h sum_j L1_i_j K_j (i = 1..3, j = 1..11, the 5th-order",
+        "// extension's weights at theta = %s), K15..K18 at y0 + h sum_j L2_i_j K_j"
+        % ", ".join("%g" % t for t in V7_THETA1),
+        "// (i = 1..4, j = 1..14, theta = %s); output"
+        % ", ".join("%g" % t for t in V7_THETA2),
+        "// u(theta) = y0 + h sum_j (sum_m D_j_m theta^m) K_j, j = 1..18, m = 1..7.",
+        "// max residual of the order-7 conditions: %.3e" % r7l,
+        "namespace vern7l {",
+    ]
+    for i in range(3):
+        lines.append("constexpr double TH1_%d = %s;" % (i + 1, fmt(V7_THETA1[i])))
+    for i in range(4):
+        lines.append("constexpr double TH2_%d = %s;" % (i + 1, fmt(V7_THETA2[i])))
+    for i in range(3):
+        for j in range(11):
+            lines.append("constexpr double L1_%d_%d = %s;" % (i + 1, j + 1, fmt(W1[i, j])))
+    for i in range(4):
+        for j in range(14):
+            lines.append("constexpr double L2_%d_%d = %s;" % (i + 1, j + 1, fmt(W2[i, j])))
+    for j in range(18):
+        for m in range(7):
+            lines.append("constexpr double D%d_%d = %s;" % (j + 1, m + 1, fmt(C7[m, j])))
+    lines.append("}  // namespace vern7l")
     for name in ("rodas5", "rodas5p"):
         h2, h3, h4, rr = derive_rodas(tb, name)
         lines.append("// %s 4th-order continuous extension (transformed stages u_1..u_7),"

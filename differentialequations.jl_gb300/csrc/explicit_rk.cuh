@@ -193,23 +193,71 @@ struct Vern7Alg {
     return err_ms<N>(err, uu, un, abstol, reltol);
   }
 
+  // 7th-order dense output u(theta) = y0 + h sum_j D_j(theta) K_j
+  // (dense_coeffs.h, vern7l) over K1, K4..K9, K11 = f(t+h, y1) and four lazy
+  // stages: K12..K14 on the 5th-order extension at theta = 0.12, 0.25, 0.78,
+  // then K15..K18 on the degree-6 interpolant through them at theta = 0.11,
+  // 0.22, 0.55, 0.75.  The lazy stages are evaluated for each save point and
+  // each of K15..K18 is folded into the sum as soon as it exists, so that few
+  // stage vectors are live at once (the kernel's register count is set by its
+  // peak).
   GBDE_D void interp(double th, double dt, T* out, const T* p, int& nf) {
-    using namespace tab::vern7d;
+    using namespace tab::vern7l;
     if (!have11) {
       M::f(k11, un, p);
       ++nf;
       have11 = true;
     }
-#define GBDE_V7B(j) (T)(th * (B##j##_1 + th * (B##j##_2 + th * (B##j##_3 + th * (B##j##_4 + th * B##j##_5)))))
-    const T w1 = GBDE_V7B(1), w4 = GBDE_V7B(4), w5 = GBDE_V7B(5), w6 = GBDE_V7B(6);
-    const T w7 = GBDE_V7B(7), w8 = GBDE_V7B(8), w9 = GBDE_V7B(9), w10 = GBDE_V7B(10);
-    const T w11 = GBDE_V7B(11);
-#undef GBDE_V7B
     const T h = (T)dt;
+#define GBDE_V7D(j)                                                                          \
+  (T)(th * (D##j##_1 + th * (D##j##_2 + th * (D##j##_3 + th * (D##j##_4 +                    \
+      th * (D##j##_5 + th * (D##j##_6 + th * D##j##_7)))))))
+    T acc[N];
+    {
+      const T w1 = GBDE_V7D(1), w4 = GBDE_V7D(4), w5 = GBDE_V7D(5), w6 = GBDE_V7D(6);
+      const T w7 = GBDE_V7D(7), w8 = GBDE_V7D(8), w9 = GBDE_V7D(9), w11 = GBDE_V7D(11);
 #pragma unroll
-    for (int c = 0; c < N; ++c)
-      out[c] = at(c, h * (w1 * k1[c] + w4 * k4[c] + w5 * k5[c] + w6 * k6[c] + w7 * k7[c] +
-                          w8 * k8[c] + w9 * k9[c] + w10 * k10[c] + w11 * k11[c]));
+      for (int c = 0; c < N; ++c)
+        acc[c] = w1 * k1[c] + w4 * k4[c] + w5 * k5[c] + w6 * k6[c] + w7 * k7[c] + w8 * k8[c] +
+                 w9 * k9[c] + w11 * k11[c];
+    }
+    T k12[N], k13[N], k14[N], y[N], k[N];
+#define GBDE_V7L1(i, c)                                                                         \
+  (T(L1_##i##_1) * k1[c] + T(L1_##i##_4) * k4[c] + T(L1_##i##_5) * k5[c] +                      \
+   T(L1_##i##_6) * k6[c] + T(L1_##i##_7) * k7[c] + T(L1_##i##_8) * k8[c] +                      \
+   T(L1_##i##_9) * k9[c] + T(L1_##i##_10) * k10[c] + T(L1_##i##_11) * k11[c])
+#define GBDE_V7L2(i, c)                                                                         \
+  (T(L2_##i##_1) * k1[c] + T(L2_##i##_4) * k4[c] + T(L2_##i##_5) * k5[c] +                      \
+   T(L2_##i##_6) * k6[c] + T(L2_##i##_7) * k7[c] + T(L2_##i##_8) * k8[c] +                      \
+   T(L2_##i##_9) * k9[c] + T(L2_##i##_11) * k11[c] + T(L2_##i##_12) * k12[c] +                  \
+   T(L2_##i##_13) * k13[c] + T(L2_##i##_14) * k14[c])
+#pragma unroll
+    for (int c = 0; c < N; ++c) y[c] = at(c, h * GBDE_V7L1(1, c));
+    M::f(k12, y, p);
+#pragma unroll
+    for (int c = 0; c < N; ++c) y[c] = at(c, h * GBDE_V7L1(2, c));
+    M::f(k13, y, p);
+#pragma unroll
+    for (int c = 0; c < N; ++c) y[c] = at(c, h * GBDE_V7L1(3, c));
+    M::f(k14, y, p);
+#define GBDE_V7LAZY2(i, j)                                                                      \
+  _Pragma("unroll") for (int c = 0; c < N; ++c) y[c] = at(c, h * GBDE_V7L2(i, c));              \
+  M::f(k, y, p);                                                                                \
+  {                                                                                             \
+    const T w = GBDE_V7D(j);                                                                    \
+    _Pragma("unroll") for (int c = 0; c < N; ++c) acc[c] += w * k[c];                           \
+  }
+    GBDE_V7LAZY2(1, 15)
+    GBDE_V7LAZY2(2, 16)
+    GBDE_V7LAZY2(3, 17)
+    GBDE_V7LAZY2(4, 18)
+#undef GBDE_V7LAZY2
+#undef GBDE_V7L1
+#undef GBDE_V7L2
+#undef GBDE_V7D
+    nf += 7;
+#pragma unroll
+    for (int c = 0; c < N; ++c) out[c] = at(c, h * acc[c]);
   }
 
   GBDE_D void accept(const T* p, int& nf) {

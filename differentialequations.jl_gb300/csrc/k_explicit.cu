@@ -7,8 +7,20 @@
 
 namespace gbde {
 
+// Resident CTAs of 128 threads per SM the kernel is compiled for.  Vern7's
+// 7th-order dense output (seven lazy stages on saving steps) needs more
+// registers than its steps: capping the kernel at the steps' need moves the
+// excess to local memory on the saving path instead of costing occupancy on
+// every step -- 128 registers (4 CTAs) for FP64 / FP32 state, 168 (3 CTAs)
+// for FP32 pairs on up to three states.
+template <class Alg> struct ErkMinBlocks { static constexpr int v = 1; };
+template <class M, class T> struct ErkMinBlocks<Vern7Alg<M, T>> {
+  static constexpr int v = M::N <= 3 ? 4 : 1;
+};
+template <class M> struct ErkMinBlocks<Vern7FF<M>> { static constexpr int v = 3; };
+
 template <class Alg, class M, class T, bool MIXED>
-__global__ void __launch_bounds__(128) k_erk(const KArgs a) {
+__global__ void __launch_bounds__(128, ErkMinBlocks<Alg>::v) k_erk(const KArgs a) {
   integrate_all<Alg, M, T, MIXED>(a);
 }
 

@@ -11,10 +11,12 @@
 //    4th-order continuous extension b_i(theta).
 //  * Vern7: J.H. Verner, "Numerically optimal Runge-Kutta pairs with
 //    interpolants", Numer. Algorithms 53 (2010) 383-396, "most efficient"
-//    7(6) pair.  The dense output is this library's own 5th-order continuous
-//    extension over the 10 stages plus f(t+h, y1) (derived by
-//    derive_dense_output.py beside this file); Verner's 7th-order lazy
-//    interpolant needs six extra stages whose coefficients are not restated.
+//    7(6) pair.  Its dense output is 7th order: a 5th-order continuous
+//    extension over the 10 stages plus f(t+h, y1), bootstrapped to order 7 by
+//    seven lazy stages on steps that save (Enright, Jackson, Norsett and
+//    Thomsen, ACM TOMS 12 (1986); derived by derive_dense_output.py beside
+//    this file).  Verner's own lazy interpolant (six extra stages) is not
+//    restated: its coefficients are not in a source this build can cite.
 //  * Rosenbrock23: L.F. Shampine, M.W. Reichelt, "The MATLAB ODE suite",
 //    SIAM J. Sci. Comput. 18 (1997) 1-22, the ode23s W-method and its
 //    continuous extension.

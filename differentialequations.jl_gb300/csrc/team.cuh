@@ -25,6 +25,14 @@ namespace gbde {
 
 constexpr int TEAM = 16;
 
+// A double step length or weight as the stepper's scalar type: FP32 pairs are
+// split on the integer pipe (ff_split), not by FP64 subtraction.
+template <class T>
+GBDE_D T team_scalar(double d) {
+  if constexpr (is_ff<T>::value) return ff_split(d);
+  else return (T)d;
+}
+
 struct Team {
   unsigned mask;  // the team's 16 lanes within the warp
   int lane;       // 0..15
@@ -45,11 +53,18 @@ struct Team {
 };
 
 // This lane's squared scaled error (the team sums them): the ratio
-// err / (abstol + reltol max(|u|, |u1|)) is FP32 for FP32 state (the square is
-// formed and summed in FP64), FP64 otherwise.
+// err / (abstol + reltol max(|u|, |u1|)) is FP32 for FP32 state and for FP32
+// pairs (on the leading parts, as the one-thread pair steppers), the square
+// formed and summed in FP64; FP64 otherwise.  (GB300 issues FP64 at 1/64 of
+// the FP32 rate: with the ratio in FP64 the pair Tsit5 team kernel was bound
+// by its FP64 pipe.)
 template <class T>
 GBDE_D double lane_err2(T err, T u, T un, double abstol, double reltol) {
-  if constexpr (sizeof(T) == 4) {
+  if constexpr (is_ff<T>::value) {
+    const float m = fmaxf(fabsf(u.hi), fabsf(un.hi));
+    const double e = f2d_bits(__fdiv_rn(err.hi, fmaf((float)reltol, m, (float)abstol)));
+    return e * e;
+  } else if constexpr (sizeof(T) == 4) {
     const float m = fmaxf(fabsf(u), fabsf(un));
     const double e = f2d_bits(__fdiv_rn(err, fmaf((float)reltol, m, (float)abstol)));
     return e * e;
@@ -426,7 +441,7 @@ struct TeamTsit5 {
   GBDE_D double attempt(double dt, const T* p, double abstol, double reltol, const Team& tm,
                         int& nf) {
     using namespace tab::tsit5;
-    const T h = (T)dt;
+    const T h = team_scalar<T>(dt);
     k2 = rhs(at(h * (T(a21) * k1)), p, tm);
     k3 = rhs(at(h * (T(a31) * k1 + T(a32) * k2)), p, tm);
     k4 = rhs(at(h * (T(a41) * k1 + T(a42) * k2 + T(a43) * k3)), p, tm);
@@ -454,7 +469,7 @@ struct TeamTsit5 {
     const T b5 = (T)(r51 * (th - r52) * (th - r53) * t2);
     const T b6 = (T)(r61 * (th - r62) * (th - r63) * t2);
     const T b7 = (T)(r71 * (th - r72) * (th - r73) * t2);
-    const T h = (T)dt;
+    const T h = team_scalar<T>(dt);
     return at(h * (b1 * k1 + b2 * k2 + b3 * k3 + b4 * k4 + b5 * k5 + b6 * k6 + b7 * k7));
   }
 

@@ -3,7 +3,8 @@
 //
 // Same method as Vern7Alg (explicit_rk.cuh; OrdinaryDiffEq's Vern7,
 // test/qa/qa.jl:126): Verner's 10-stage 7(6) pair and this library's
-// 5th-order dense output with the lazily evaluated f(u1).  The work is placed
+// 7th-order dense output with the lazily evaluated f(u1) and seven lazy
+// stages.  The work is placed
 // as in Tsit5FF (tsit5_ff.cuh): the stage derivatives are kept pre-scaled,
 // hk_j = h k_j, in paired FP32 registers; every stage argument, the new state,
 // the error estimate and the dense output is one unnormalised accumulation
@@ -157,21 +158,78 @@ struct Vern7FF {
     return ms * (1.0 / N);
   }
 
-  // y(theta) = y0 + sum_j w_j(theta) h k_j with w_j(theta) = theta (B_j1 +
-  // theta (B_j2 + ... + theta B_j5)) (as Vern7Alg::interp), in pair arithmetic;
-  // f(u1) is evaluated on the first call of a step.
+  // The interpolant's seven lazy stages (as Vern7Alg::lazy_stages), in pair
+  // arithmetic: K12..K14 on the 5th-order extension, K15..K18 on the degree-6
+  // interpolant through them (per save point, as in Vern7Alg).
+  GBDE_D void lazy_stages(double dt, const ff* p, int& nf, FfVec<N>* hl) {
+    using namespace tab::vern7l;
+    const ff h = ff_split(dt);
+    FfVec<N> uv, l1[3];
+    uv.from(uu);
+    FfVecAcc<N> a;
+    ff y[N], k[N];
+#define GBDE_V7FF_L1(i)                                                                          \
+  a.set(uv);                                                                                     \
+  a.fma(ff(L1_##i##_1), hk[0]);                                                                  \
+  a.fma(ff(L1_##i##_4), hk[3]);                                                                  \
+  a.fma(ff(L1_##i##_5), hk[4]);                                                                  \
+  a.fma(ff(L1_##i##_6), hk[5]);                                                                  \
+  a.fma(ff(L1_##i##_7), hk[6]);                                                                  \
+  a.fma(ff(L1_##i##_8), hk[7]);                                                                  \
+  a.fma(ff(L1_##i##_9), hk[8]);                                                                  \
+  a.fma(ff(L1_##i##_10), hk[9]);                                                                 \
+  a.fma(ff(L1_##i##_11), hk[10]);                                                                \
+  a.get(y);                                                                                      \
+  M::f(k, y, p);                                                                                 \
+  l1[i - 1] = ff_scale<N>(h, k);
+    GBDE_V7FF_L1(1)
+    GBDE_V7FF_L1(2)
+    GBDE_V7FF_L1(3)
+#undef GBDE_V7FF_L1
+#define GBDE_V7FF_L2(i)                                                                          \
+  a.set(uv);                                                                                     \
+  a.fma(ff(L2_##i##_1), hk[0]);                                                                  \
+  a.fma(ff(L2_##i##_4), hk[3]);                                                                  \
+  a.fma(ff(L2_##i##_5), hk[4]);                                                                  \
+  a.fma(ff(L2_##i##_6), hk[5]);                                                                  \
+  a.fma(ff(L2_##i##_7), hk[6]);                                                                  \
+  a.fma(ff(L2_##i##_8), hk[7]);                                                                  \
+  a.fma(ff(L2_##i##_9), hk[8]);                                                                  \
+  a.fma(ff(L2_##i##_11), hk[10]);                                                                \
+  a.fma(ff(L2_##i##_12), l1[0]);                                                                 \
+  a.fma(ff(L2_##i##_13), l1[1]);                                                                 \
+  a.fma(ff(L2_##i##_14), l1[2]);                                                                 \
+  a.get(y);                                                                                      \
+  M::f(k, y, p);                                                                                 \
+  hl[i - 1] = ff_scale<N>(h, k);
+    GBDE_V7FF_L2(1)
+    GBDE_V7FF_L2(2)
+    GBDE_V7FF_L2(3)
+    GBDE_V7FF_L2(4)
+#undef GBDE_V7FF_L2
+    nf += 7;
+  }
+
+  // y(theta) = y0 + sum_j w_j(theta) h k_j with w_j(theta) = theta (D_j1 +
+  // theta (D_j2 + ... + theta D_j7)) (as Vern7Alg::interp), in pair arithmetic;
+  // f(u1) is evaluated on the first call of a step, the lazy stages on each.
   GBDE_D void interp(double th, double dt, ff* out, const ff* p, int& nf) {
-    using namespace tab::vern7d;
+    using namespace tab::vern7l;
     if (!have11) {
       M::f(k11, un, p);
       ++nf;
       hk[10] = ff_scale<N>(ff_split(dt), k11);
       have11 = true;
     }
+    FfVec<N> hl[4];
+    lazy_stages(dt, p, nf, hl);
     const ff t = ff_split(th);
 #define GBDE_V7FF_W(j)                                                                           \
-  (t * (ff(B##j##_1) +                                                                           \
-        t * (ff(B##j##_2) + t * (ff(B##j##_3) + t * (ff(B##j##_4) + t * ff(B##j##_5))))))
+  (t * (ff(D##j##_1) +                                                                           \
+        t * (ff(D##j##_2) +                                                                      \
+             t * (ff(D##j##_3) +                                                                 \
+                  t * (ff(D##j##_4) +                                                            \
+                       t * (ff(D##j##_5) + t * (ff(D##j##_6) + t * ff(D##j##_7))))))))
     FfVec<N> uv;
     uv.from(uu);
     FfVecAcc<N> a;
@@ -183,8 +241,11 @@ struct Vern7FF {
     a.fma(GBDE_V7FF_W(7), hk[6]);
     a.fma(GBDE_V7FF_W(8), hk[7]);
     a.fma(GBDE_V7FF_W(9), hk[8]);
-    a.fma(GBDE_V7FF_W(10), hk[9]);
     a.fma(GBDE_V7FF_W(11), hk[10]);
+    a.fma(GBDE_V7FF_W(15), hl[0]);
+    a.fma(GBDE_V7FF_W(16), hl[1]);
+    a.fma(GBDE_V7FF_W(17), hl[2]);
+    a.fma(GBDE_V7FF_W(18), hl[3]);
 #undef GBDE_V7FF_W
     a.get(out);
   }

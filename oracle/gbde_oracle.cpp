@@ -391,31 +391,62 @@ struct Stepper {
     have11 = false;
     return wrms(n, e, u, un, C.at, C.rt);
   }
+  // Vern7's 7th-order dense output (dense_coeffs.h, vern7l; Enright, Jackson,
+  // Norsett, Thomsen, ACM TOMS 12 (1986) bootstrapping): f(t+h, y1) once per
+  // step, then per save point three stages on the 5th-order extension and
+  // four on the degree-6 interpolant through them;
+  //   u(theta) = y0 + h sum_j (sum_m D_j_m theta^m) K_j,  j = 1..18.
   void vern7_interp(double th, double h, double* out, int& nf) {
-    using namespace gbde::tab::vern7d;
+    using namespace gbde::tab::vern7l;
     if (!have11) {
       rhs(id, un, p, k[10]);
       ++nf;
       have11 = true;
     }
-    const double B[11][5] = {{B1_1, B1_2, B1_3, B1_4, B1_5},      {B2_1, B2_2, B2_3, B2_4, B2_5},
-                             {B3_1, B3_2, B3_3, B3_4, B3_5},      {B4_1, B4_2, B4_3, B4_4, B4_5},
-                             {B5_1, B5_2, B5_3, B5_4, B5_5},      {B6_1, B6_2, B6_3, B6_4, B6_5},
-                             {B7_1, B7_2, B7_3, B7_4, B7_5},      {B8_1, B8_2, B8_3, B8_4, B8_5},
-                             {B9_1, B9_2, B9_3, B9_4, B9_5},      {B10_1, B10_2, B10_3, B10_4, B10_5},
-                             {B11_1, B11_2, B11_3, B11_4, B11_5}};
-    double w[11];
-    for (int j = 0; j < 11; ++j) {
-      double pw = th, acc = 0.0;
-      for (int q = 0; q < 5; ++q) {
-        acc += B[j][q] * pw;
-        pw *= th;
+#define GBDE_O_ROW11(P, i) {P##i##_1, P##i##_2, P##i##_3, P##i##_4, P##i##_5, P##i##_6, \
+                            P##i##_7, P##i##_8, P##i##_9, P##i##_10, P##i##_11}
+    const double L1[3][11] = {GBDE_O_ROW11(L1_, 1), GBDE_O_ROW11(L1_, 2), GBDE_O_ROW11(L1_, 3)};
+#undef GBDE_O_ROW11
+#define GBDE_O_ROW14(i) {L2_##i##_1, L2_##i##_2, L2_##i##_3, L2_##i##_4, L2_##i##_5, L2_##i##_6, \
+                         L2_##i##_7, L2_##i##_8, L2_##i##_9, L2_##i##_10, L2_##i##_11,           \
+                         L2_##i##_12, L2_##i##_13, L2_##i##_14}
+    const double L2[4][14] = {GBDE_O_ROW14(1), GBDE_O_ROW14(2), GBDE_O_ROW14(3), GBDE_O_ROW14(4)};
+#undef GBDE_O_ROW14
+#define GBDE_O_D(j) {D##j##_1, D##j##_2, D##j##_3, D##j##_4, D##j##_5, D##j##_6, D##j##_7}
+    const double D[18][7] = {GBDE_O_D(1),  GBDE_O_D(2),  GBDE_O_D(3),  GBDE_O_D(4),  GBDE_O_D(5),
+                             GBDE_O_D(6),  GBDE_O_D(7),  GBDE_O_D(8),  GBDE_O_D(9),  GBDE_O_D(10),
+                             GBDE_O_D(11), GBDE_O_D(12), GBDE_O_D(13), GBDE_O_D(14), GBDE_O_D(15),
+                             GBDE_O_D(16), GBDE_O_D(17), GBDE_O_D(18)};
+#undef GBDE_O_D
+    double K[18][NMAX], y[NMAX];
+    for (int j = 0; j < 11; ++j)
+      for (int c = 0; c < n; ++c) K[j][c] = k[j][c];
+    for (int i = 0; i < 3; ++i) {
+      for (int c = 0; c < n; ++c) {
+        double acc = 0.0;
+        for (int j = 0; j < 11; ++j) acc += L1[i][j] * K[j][c];
+        y[c] = u[c] + h * acc;
       }
-      w[j] = acc;
+      rhs(id, y, p, K[11 + i]);
+    }
+    for (int i = 0; i < 4; ++i) {
+      for (int c = 0; c < n; ++c) {
+        double acc = 0.0;
+        for (int j = 0; j < 14; ++j) acc += L2[i][j] * K[j][c];
+        y[c] = u[c] + h * acc;
+      }
+      rhs(id, y, p, K[14 + i]);
+    }
+    nf += 7;
+    double w[18];
+    for (int j = 0; j < 18; ++j) {
+      double acc = 0.0;
+      for (int m = 6; m >= 0; --m) acc = acc * th + D[j][m];
+      w[j] = acc * th;
     }
     for (int c = 0; c < n; ++c) {
       double acc = 0.0;
-      for (int j = 0; j < 11; ++j) acc += w[j] * k[j][c];
+      for (int j = 0; j < 18; ++j) acc += w[j] * K[j][c];
       out[c] = u[c] + h * acc;
     }
   }

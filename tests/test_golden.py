@@ -5,7 +5,10 @@ solve_ivp at rtol <= 1e-12).
 Each bound is the method's own global error at the given tolerance on that
 problem (weighted: |u - u*| / (abstol + reltol |u*|)), as measured for the
 oracle when the fixtures were made, times ~2.5: a pin on the accuracy of the
-restated methods, not a lockstep check (that is test_gpu_parity.py)."""
+restated methods, not a lockstep check (that is test_gpu_parity.py).  Vern7's
+bounds are those of its 7th-order dense output: the 5th-order extension it
+replaced left Lorenz at 2 x tolerance, interpolation error dominating the
+7th-order steps (now 0.02)."""
 import json
 import os
 
@@ -18,18 +21,18 @@ BY_NAME = {c["name"]: c for c in CASES}
 
 # (case, algorithm, reltol, abstol, bound)
 RUNS = [
-    ("linear_1.01", "TSIT5", 1e-8, 1e-8, 0.5), ("linear_1.01", "VERN7", 1e-8, 1e-8, 0.5),
+    ("linear_1.01", "TSIT5", 1e-8, 1e-8, 0.5), ("linear_1.01", "VERN7", 1e-8, 1e-8, 0.001),
     ("linear_1.01", "ROSENBROCK23", 1e-8, 1e-8, 330), ("linear_1.01", "RODAS5", 1e-8, 1e-8, 1.5),
     ("linear_1.01", "RODAS5P", 1e-8, 1e-8, 1.5),
-    ("lorenz_core", "TSIT5", 1e-8, 1e-8, 6), ("lorenz_core", "VERN7", 1e-8, 1e-8, 5),
-    ("lorenz_scaled", "TSIT5", 1e-8, 1e-8, 6), ("lorenz_scaled", "VERN7", 1e-8, 1e-8, 5),
+    ("lorenz_core", "TSIT5", 1e-8, 1e-8, 6), ("lorenz_core", "VERN7", 1e-8, 1e-8, 0.05),
+    ("lorenz_scaled", "TSIT5", 1e-8, 1e-8, 6), ("lorenz_scaled", "VERN7", 1e-8, 1e-8, 0.05),
     ("robertson_core", "ROSENBROCK23", 1e-6, 1e-10, 110), ("robertson_core", "RODAS5", 1e-6, 1e-10, 17),
     ("robertson_core", "RODAS5P", 1e-6, 1e-10, 31), ("robertson_scaled", "ROSENBROCK23", 1e-6, 1e-10, 70),
     ("robertson_scaled", "RODAS5", 1e-6, 1e-10, 20), ("robertson_scaled", "RODAS5P", 1e-6, 1e-10, 37),
-    ("vdp_ring8_mu1", "TSIT5", 1e-6, 1e-6, 34), ("vdp_ring8_mu1", "VERN7", 1e-6, 1e-6, 9),
+    ("vdp_ring8_mu1", "TSIT5", 1e-6, 1e-6, 34), ("vdp_ring8_mu1", "VERN7", 1e-6, 1e-6, 4),
     ("vdp_ring8_mu1", "RODAS5", 1e-6, 1e-6, 32), ("vdp_ring8_mu1", "RODAS5P", 1e-6, 1e-6, 36),
     ("vdp_ring8_mu30", "RODAS5", 1e-6, 1e-6, 800), ("vdp_ring8_mu30", "RODAS5P", 1e-6, 1e-6, 1100),
-    ("lotka_volterra_drift", "TSIT5", 1e-8, 1e-8, 10), ("lotka_volterra_drift", "VERN7", 1e-8, 1e-8, 8),
+    ("lotka_volterra_drift", "TSIT5", 1e-8, 1e-8, 10), ("lotka_volterra_drift", "VERN7", 1e-8, 1e-8, 2),
     ("lotka_volterra_drift", "RODAS5", 1e-8, 1e-8, 26), ("lotka_volterra_drift", "RODAS5P", 1e-8, 1e-8, 53),
 ]
 

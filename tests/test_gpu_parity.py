@@ -58,7 +58,7 @@ ODE_CASES = [
     ("linear", "TSIT5", 1e-8, 1e-8), ("linear", "VERN7", 1e-10, 1e-10),
     ("robertson", "ROSENBROCK23", 1e-6, 1e-10), ("robertson", "RODAS5", 1e-6, 1e-10),
     ("robertson", "RODAS5P", 1e-6, 1e-10), ("lorenz", "RODAS5", 1e-7, 1e-7),
-    ("linear", "RODAS5P", 1e-8, 1e-8),
+    ("linear", "RODAS5P", 1e-8, 1e-8), ("lorenz", "VERN7", 1e-10, 1e-10),
 ]
 
 
@@ -495,3 +495,28 @@ def test_one_call_sharding_matches_single_device(de):
     assert one.converged and two.converged
     assert np.array_equal(one.U, two.U)
     assert np.array_equal(one.retcode, two.retcode)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "f32x2"])
+def test_vern7_dense_output_is_7th_order(de, precision):
+    """Save points inside Vern7's steps carry the method's own accuracy: on
+    u' = a u with saves at every 0.01 (most inside a step), the error against
+    exp(a t) at reltol 1e-10 stays within the bar of the step endpoints (a
+    lower-order interpolant would dominate the 7th-order steps here)."""
+    capi = de._capi
+    N = 256
+    rng = np.random.default_rng(17)
+    p = rng.uniform(0.5, 1.5, (N, 1))
+    u0 = rng.uniform(0.1, 1.0, (N, 1))
+    grid = np.linspace(0.0, 1.0, 101)
+    o = capi.opts_default(capi.ALG_VERN7)
+    o.reltol = o.abstol = 1e-10
+    o.precision = capi.PREC_F32X2 if precision == "f32x2" else capi.PREC_FP64
+    g = de.solve_arrays(de.models.linear, o, p, u0, np.zeros(N), np.ones(N), grid,
+                        capi.SAVE_GRID)
+    assert np.all(g["retcode"] == capi.RET_SUCCESS)
+    exact = u0 * np.exp(p * grid[None, :])
+    err = np.abs(g["u"][:, :, 0] - exact) / (1e-10 + 1e-10 * np.abs(exact))
+    assert err.max() <= 2.0, err.max()
+    # most save points fall inside steps: the steps are far longer than 0.01
+    assert g["naccept"].mean() < 30

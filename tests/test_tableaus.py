@@ -238,3 +238,34 @@ def test_dense_coeffs_regenerate(tmp_path):
     shutil.copytree(CSRC, work, ignore=shutil.ignore_patterns("*.o"))
     subprocess.check_call([sys.executable, str(work / "derive_dense_output.py")])
     assert (work / "dense_coeffs.h").read_text() == open(os.path.join(CSRC, "dense_coeffs.h")).read()
+
+
+@pytest.mark.parametrize("theta", [0.1, 0.37, 0.5, 0.9, 1.0])
+def test_vern7_dense_output_order7(theta):
+    """Vern7's dense output (dense_coeffs.h, vern7l) is a 7th-order continuous
+    extension: over the 18 stages (Vern7's 10, f(t+h, y1), three lazy stages
+    on the 5th-order extension, four on the degree-6 interpolant) its weights
+    satisfy every order condition up to order 7 at each theta, and not all of
+    order 8."""
+    A, b, _ = dd.vern7_tableau(TB)
+    v = DENSE["vern7l"]
+    S = 18
+    AA = np.zeros((S, S))
+    AA[:10, :10] = A
+    AA[10, :10] = b
+    for i in range(3):
+        AA[11 + i, :11] = [v["L1_%d_%d" % (i + 1, j + 1)] for j in range(11)]
+    for i in range(4):
+        AA[14 + i, :14] = [v["L2_%d_%d" % (i + 1, j + 1)] for j in range(14)]
+    w = np.array([sum(v["D%d_%d" % (j + 1, m)] * theta ** m for m in range(1, 8))
+                  for j in range(S)])
+    for n in range(1, 8):
+        for t in TREES[n]:
+            assert abs(w @ dd.rk_phi(t, AA) - theta ** n / dd.tree_gamma(t)) < 1e-11, (n, t)
+    assert max(abs(w @ dd.rk_phi(t, AA) - theta ** 8 / dd.tree_gamma(t)) for t in TREES[8]) > 1e-7
+    # the extra stages sit where their abscissae say
+    c = AA.sum(1)
+    assert np.allclose(c[11:14], [v["TH1_%d" % i] for i in (1, 2, 3)], atol=1e-12)
+    assert np.allclose(c[14:18], [v["TH2_%d" % i] for i in (1, 2, 3, 4)], atol=1e-12)
+    if theta == 1.0:
+        assert np.allclose(w[:10], b, atol=1e-12)  # the interpolant ends at y1
