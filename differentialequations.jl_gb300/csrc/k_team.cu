@@ -8,14 +8,18 @@ namespace gbde {
 
 // Resident CTAs of 128 threads per SM each team stepper is compiled for: the
 // Rodas steppers are latency-bound on their broadcast chains (LU, triangular
-// solves), so more resident warps beat more registers -- 3 CTAs (<= 168
-// registers) for the FP64 stepper, 4 (<= 128, no spills) for the pair one.
+// solves), so more resident warps beat more registers.  With W's rows in
+// shared memory (team.cuh, 17 KB per CTA, 24 KB with the pair stages) both fit
+// 6 CTAs (<= 80 registers, no spills in the Rodas5 steppers).
 template <class Alg> struct TeamMinBlocks { static constexpr int v = 1; };
 template <class M, class T, class Tag> struct TeamMinBlocks<TeamRodas<M, T, Tag>> {
-  static constexpr int v = 3;
+  static constexpr int v = 6;
 };
 template <class M, class Tag> struct TeamMinBlocks<TeamRodasFF<M, Tag>> {
-  static constexpr int v = 4;
+  static constexpr int v = 6;
+};
+template <class M, class T> struct TeamMinBlocks<TeamTsit5<M, T>> {
+  static constexpr int v = 1;
 };
 
 template <class Alg, class M, class T, bool MIXED>

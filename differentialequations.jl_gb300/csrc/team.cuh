@@ -10,10 +10,11 @@
 //     few components that row depends on from the other lanes by shuffles.
 //   * Error norm: a butterfly sum over the team; every lane then takes the
 //     same accept/reject decision, so control flow stays team-uniform.
-//   * LU with partial pivoting, distributed by rows without moving rows: at
-//     step k the team picks the unpivoted row with the largest |a_k| (shuffle
-//     max on the magnitude bits + ballot), broadcasts that row and every
-//     unpivoted lane eliminates.  Triangular solves run in pivot order.
+//   * LU with partial pivoting, distributed by rows without moving rows (the
+//     rows in shared memory): at step k the team picks the unpivoted row with
+//     the largest |a_k| (shuffle max on the magnitude bits + ballot), every
+//     unpivoted lane reads that row and eliminates.  Triangular solves run in
+//     pivot order.
 //   * Saves: the 16 lanes store the 16 components of a save point as one
 //     contiguous, coalesced 128-byte (FP64) or 64-byte (FP32) segment.
 #pragma once
@@ -76,18 +77,36 @@ GBDE_D double lane_err2(T err, T u, T un, double abstol, double reltol) {
 }
 
 // ------------------------------------------------------------- team LU
-// Row-distributed LU of W (16 x 16) with partial pivoting.  Lane r keeps its
-// row in a[]: after factor(), a[c] for c < step holds the multipliers (L) and
-// a[c] for c >= step the U entries, where `step` is the elimination step at
-// which row r was the pivot.  piv packs the pivot lane of step k in bits
-// [4k, 4k+4).
+// Row-distributed LU of W (16 x 16) with partial pivoting.  Lane r's row lives
+// in shared memory (team_lu_row(), 17 doubles at a stride that keeps a warp's
+// row accesses conflict-free): the pivot row is read there by the 16 lanes of
+// the team (one broadcast address), the elimination and the substitutions run
+// as loops with run-time bounds (compact code: the fully unrolled form was the
+// kernel's largest piece of code and its top stall an empty instruction
+// cache), and no row sits in registers.  After factor(), row r holds the
+// multipliers (L) in c < step and the U entries in c >= step, where `step` is
+// the elimination step at which row r was the pivot.  piv packs the pivot lane
+// of step k in bits [4k, 4k+4).  The caller writes row r of W with
+// team_lu_row() before factor().
+constexpr int kTeamLuStride = TEAM + 1;
+constexpr int kTeamLuThreads = 128;  // team kernels run CTAs of up to 128 threads
+
+GBDE_D double* team_lu_row() {
+  __shared__ double buf[kTeamLuThreads * kTeamLuStride];
+  return buf + threadIdx.x * kTeamLuStride;
+}
+// the row of lane `lane` of this thread's team
+GBDE_D double* team_lu_row_of(int lane) {
+  return team_lu_row() + (lane - (int)(threadIdx.x & (TEAM - 1))) * kTeamLuStride;
+}
+
 struct TeamLU {
-  double a[TEAM];
   double invp;   // 1 / pivot of this lane's step
   int step;
   uint64_t piv;
 
   GBDE_D void factor(const Team& tm) {
+    double* a = team_lu_row();
     step = -1;
     piv = 0;
     invp = 0.0;
@@ -97,10 +116,12 @@ struct TeamLU {
     // lowest position, as getrf's first-maximum search does, so the pivot
     // sequence is the row-swapping LU's even when entries tie.
     unsigned pos = (unsigned)tm.lane;
-#pragma unroll
+    __syncwarp(tm.mask);  // every lane's row is written
+#pragma unroll 1
     for (int k = 0; k < TEAM; ++k) {
+      const double ak = a[k];
       // pivot: unpivoted lane with the largest |a_k|, ties: lowest position
-      const uint64_t key = step < 0 ? mag_bits(a[k]) + 1ull : 0ull;
+      const uint64_t key = step < 0 ? mag_bits(ak) + 1ull : 0ull;
       uint64_t m = key;
 #pragma unroll
       for (int o = TEAM / 2; o > 0; o >>= 1) {
@@ -114,19 +135,18 @@ struct TeamLU {
       const int p = __ffs(bal) - 1;
       if (step < 0 && pos == (unsigned)k && tm.lane != p) pos = ppos;  // swapped out
       piv |= (uint64_t)p << (4 * k);
-      double prow[TEAM];
-#pragma unroll
-      for (int c = k; c < TEAM; ++c) prow[c] = tm.bcast(a[c], p);
+      const double* prow = team_lu_row_of(p);
       const double inv = rcp64(prow[k]);
       if (tm.lane == p) {
         step = k;
         invp = inv;
       } else if (step < 0) {
-        const double l = a[k] * inv;
+        const double l = ak * inv;
         a[k] = l;
-#pragma unroll
+#pragma unroll 3
         for (int c = k + 1; c < TEAM; ++c) a[c] = fma(-l, prow[c], a[c]);
       }
+      __syncwarp(tm.mask);  // step k's updates land before step k+1 reads them
     }
   }
 
@@ -135,13 +155,14 @@ struct TeamLU {
   // Solve W x = b; b is this lane's right-hand side component, the return
   // value this lane's component of x.
   GBDE_D double solve(double b, const Team& tm) const {
-#pragma unroll
+    const double* a = team_lu_row();
+#pragma unroll 4
     for (int k = 0; k < TEAM; ++k) {  // forward: L z = P b
       const double z = tm.bcast(b, pivot_lane(k));
       if (step > k) b = fma(-a[k], z, b);
     }
     double x = 0.0;
-#pragma unroll
+#pragma unroll 4
     for (int k = TEAM - 1; k >= 0; --k) {  // backward: U x = z
       const double xk = tm.bcast(b * invp, pivot_lane(k));
       if (step < k) b = fma(-a[k], xk, b);
@@ -152,19 +173,26 @@ struct TeamLU {
 };
 
 // The factors of a TeamLU as pairs for the FP32-pair stepper: this lane's
-// row negated (multipliers and U entries) and its pivot reciprocal, split on
-// the integer pipe.  The substitutions run in pair arithmetic in the same
+// row negated (multipliers and U entries), written as pairs over the FP64 row
+// in shared memory (same 8 bytes per entry), and its pivot reciprocal, split
+// on the integer pipe.  The substitutions run in pair arithmetic in the same
 // order as TeamLU::solve; the value each step broadcasts is renormalised
 // first, the lane's own row sum is carried unnormalised (FfAcc).
 struct TeamLUFF {
-  ff na[TEAM];
   ff invp;
   int step;
   uint64_t piv;
 
+  GBDE_D static float2* rowp() { return reinterpret_cast<float2*>(team_lu_row()); }
+
   GBDE_D void from(const TeamLU& W) {
-#pragma unroll
-    for (int c = 0; c < TEAM; ++c) na[c] = ff_split(-W.a[c]);
+    double* a = team_lu_row();
+    float2* na = rowp();
+#pragma unroll 4
+    for (int c = 0; c < TEAM; ++c) {
+      const ff x = ff_split(-a[c]);
+      na[c] = make_float2(x.hi, x.lo);
+    }
     invp = ff_split(W.invp);
     step = W.step;
     piv = W.piv;
@@ -172,18 +200,21 @@ struct TeamLUFF {
   GBDE_D int pivot_lane(int k) const { return (int)((piv >> (4 * k)) & 15u); }
 
   GBDE_D ff solve(ff b, const Team& tm) const {
+    const float2* na = rowp();
     FfAcc acc;
     acc.set(b);
-#pragma unroll
+#pragma unroll 4
     for (int k = 0; k < TEAM; ++k) {  // forward: L z = P b
       const ff z = tm.bcast(acc.get(), pivot_lane(k));
-      if (step > k) acc.fma(na[k], z);
+      const float2 v = na[k];
+      if (step > k) acc.fma(ff(v.x, v.y), z);
     }
     ff x(0.0f, 0.0f);
-#pragma unroll
+#pragma unroll 4
     for (int k = TEAM - 1; k >= 0; --k) {  // backward: U x = z
       const ff xk = tm.bcast(acc.get() * invp, pivot_lane(k));
-      if (step < k) acc.fma(na[k], xk);
+      const float2 v = na[k];
+      if (step < k) acc.fma(ff(v.x, v.y), xk);
       if (tm.lane == k) x = xk;
     }
     return x;
@@ -231,8 +262,9 @@ struct TeamRodas {
     {
       T Jr[TEAM];
       M::jac_lane(tm.lane, uu, p, tm, Jr);
+      double* wr = team_lu_row();
 #pragma unroll
-      for (int c = 0; c < TEAM; ++c) W.a[c] = c == tm.lane ? dg - (double)Jr[c] : -(double)Jr[c];
+      for (int c = 0; c < TEAM; ++c) wr[c] = c == tm.lane ? dg - (double)Jr[c] : -(double)Jr[c];
     }
     W.factor(tm);
     const T iht = (T)ih;  // r_i = f(y_i) + (1/h) sum_j C_ij u_j
@@ -341,8 +373,9 @@ struct TeamRodasFF {
       const double dg = ih * (1.0 / K::g);
       double Jr[TEAM];  // FP64 Jacobian row at uu, built on every attempt (as TeamRodas)
       M::jac_lane(tm.lane, f2d_bits(uu.hi) + f2d_bits(uu.lo), pd, tm, Jr);
+      double* wr = team_lu_row();
 #pragma unroll
-      for (int c = 0; c < TEAM; ++c) W.a[c] = c == tm.lane ? dg - Jr[c] : -Jr[c];
+      for (int c = 0; c < TEAM; ++c) wr[c] = c == tm.lane ? dg - Jr[c] : -Jr[c];
       W.factor(tm);
       L.from(W);
     }
