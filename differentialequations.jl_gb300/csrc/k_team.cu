@@ -10,7 +10,9 @@ namespace gbde {
 // Rodas steppers are latency-bound on their broadcast chains (LU, triangular
 // solves), so more resident warps beat more registers.  With W's rows in
 // shared memory (team.cuh, 17 KB per CTA, 24 KB with the pair stages) both fit
-// 6 CTAs (<= 80 registers, no spills in the Rodas5 steppers).
+// 6 CTAs (<= 80 registers, no spills in the Rodas5 steppers): 914 -> 625 ms on
+// the 250k stiff trajectories of the 1M ring workload.  The Tsit5 team kernel
+// (no LU) gains 3 % from 6 CTAs over its natural 95-110 registers.
 template <class Alg> struct TeamMinBlocks { static constexpr int v = 1; };
 template <class M, class T, class Tag> struct TeamMinBlocks<TeamRodas<M, T, Tag>> {
   static constexpr int v = 6;
@@ -19,7 +21,7 @@ template <class M, class Tag> struct TeamMinBlocks<TeamRodasFF<M, Tag>> {
   static constexpr int v = 6;
 };
 template <class M, class T> struct TeamMinBlocks<TeamTsit5<M, T>> {
-  static constexpr int v = 1;
+  static constexpr int v = 6;
 };
 
 template <class Alg, class M, class T, bool MIXED>
