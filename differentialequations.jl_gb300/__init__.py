@@ -9,7 +9,8 @@ include/gbde.h); this package is the host-side mirror of the reference's
 SciMLBase interface over that ABI.
 """
 from . import _capi, learned, tuning
-from .api import (EM, SOSRI, SRIW1, ContinuousCallback, DiscreteCallback, EnsembleGB300, EnsembleProblem, EnsembleSerial,
+from .api import (EM, SOSRI, SRIW1, CallbackSet, ContinuousCallback, DiscreteCallback,
+                  VectorContinuousCallback, EnsembleGB300, EnsembleProblem, EnsembleSerial,
                   EnsembleSolution, EnsembleThreads, ODEFunction, ODEProblem, ODESolution,
                   SDEFunction,
                   ReturnCode, EnsembleSummary, compile_model, ensemble_summary,
@@ -17,7 +18,8 @@ from .api import (EM, SOSRI, SRIW1, ContinuousCallback, DiscreteCallback, Ensemb
                   save_grid, solve, solve_arrays)
 
 __all__ = [
-    "EM", "SOSRI", "SRIW1", "ContinuousCallback", "DiscreteCallback", "EnsembleGB300", "EnsembleProblem", "EnsembleSerial", "EnsembleSolution",
+    "EM", "SOSRI", "SRIW1", "CallbackSet", "ContinuousCallback", "DiscreteCallback",
+    "VectorContinuousCallback", "EnsembleGB300", "EnsembleProblem", "EnsembleSerial", "EnsembleSolution",
     "EnsembleThreads", "ODEFunction", "SDEFunction", "ODEProblem", "ODESolution", "compile_model", "EnsembleSummary", "ensemble_summary",
     "ReturnCode", "Rodas5", "Rodas5P",
     "Rosenbrock23", "SDEProblem", "Tsit5", "Vern7", "models", "remake", "save_grid", "solve",

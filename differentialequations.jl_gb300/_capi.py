@@ -95,7 +95,8 @@ class Summary(C.Structure):
                 ("mean", C.c_void_p), ("var", C.c_void_p), ("qvals", C.c_void_p)]
 
 
-CB_CONTINUOUS, CB_DISCRETE = 1, 2
+CB_CONTINUOUS, CB_DISCRETE, CB_VECTOR = 1, 2, 3
+MAX_CB_CONDITIONS = 64
 
 
 class Callback(C.Structure):
@@ -144,6 +145,10 @@ SIGNATURES = {
     "gbde_sde_model_register": (C.c_int, [C.POINTER(UserModel), C.c_char_p, C.POINTER(C.c_int32)]),
     "gbde_model_compile": (C.c_int, [C.c_int32, C.c_int32, C.c_int32]),
     "gbde_callback_register": (C.c_int, [C.POINTER(Callback), C.POINTER(C.c_int32)]),
+    "gbde_vector_callback_register": (C.c_int, [C.POINTER(Callback), C.c_int32,
+                                                C.POINTER(C.c_int32)]),
+    "gbde_callback_set_register": (C.c_int, [C.POINTER(C.c_int32), C.c_int32,
+                                             C.POINTER(C.c_int32)]),
     "gbde_callback_compile": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "gbde_autotune": (C.c_int, [C.c_void_p, C.POINTER(Problem), C.POINTER(Opts),
                                 C.POINTER(Outputs), C.c_int32, C.POINTER(Opts),

@@ -118,14 +118,18 @@ def compile_model(model, alg, precision="fp64"):
 
 
 class _Callback:
-    def __init__(self, kind, condition, affect, terminate):
+    def __init__(self, kind, condition, affect, terminate, len=1):
         import ctypes as C
         d = capi.Callback(kind=kind, condition=condition.encode(),
                           affect=affect.encode() if affect else None,
                           terminate=int(bool(terminate)))
         cid = C.c_int32()
-        capi.check(capi.lib().gbde_callback_register(C.byref(d), C.byref(cid)))
-        self.id, self.kind = cid.value, kind
+        if kind == capi.CB_VECTOR:
+            capi.check(capi.lib().gbde_vector_callback_register(C.byref(d), int(len),
+                                                                C.byref(cid)))
+        else:
+            capi.check(capi.lib().gbde_callback_register(C.byref(d), C.byref(cid)))
+        self.id, self.kind, self.len = cid.value, kind, int(len)
         self.condition, self.affect, self.terminate = condition, affect, terminate
 
 
@@ -149,6 +153,40 @@ class DiscreteCallback(_Callback):
 
     def __init__(self, condition, affect=None, terminate=False):
         super().__init__(capi.CB_DISCRETE, condition, affect, terminate)
+
+
+class VectorContinuousCallback(_Callback):
+    """VectorContinuousCallback(condition, affect, len; terminate=False)
+    (qa.jl:124): len continuous conditions in one callback.
+
+    condition: CUDA C++ statements setting `out[0..len-1]` (double*) from
+    `u`, `t` and `p`; the earliest sign change among them is the event, and
+    affect runs with `idx` (int, 0-based: the reference's event_index - 1)
+    naming the condition that fired.  Example, two balls bouncing:
+    VectorContinuousCallback("out[0] = u[0]; out[1] = u[2];",
+                             "u[2 * idx + 1] = -0.9 * u[2 * idx + 1];", 2)."""
+
+    def __init__(self, condition, affect=None, len=1, terminate=False):
+        super().__init__(capi.CB_VECTOR, condition, affect, terminate, len)
+
+
+class CallbackSet:
+    """CallbackSet(cb1, cb2, ...) (qa.jl:26): continuous conditions of every
+    member compete for the earliest root of a step (the first member on a
+    tie); after each accepted step or event the discrete members run in
+    order.  Members may be sets."""
+
+    def __init__(self, *callbacks):
+        import ctypes as C
+        if not callbacks:
+            raise ValueError("CallbackSet needs at least one callback")
+        for cb in callbacks:
+            if not isinstance(cb, (_Callback, CallbackSet)):
+                raise TypeError("CallbackSet members are callbacks or callback sets")
+        ids = (C.c_int32 * len(callbacks))(*[cb.id for cb in callbacks])
+        sid = C.c_int32()
+        capi.check(capi.lib().gbde_callback_set_register(ids, len(callbacks), C.byref(sid)))
+        self.id, self.callbacks = sid.value, tuple(callbacks)
 
 
 # -------------------------------------------------------------- problems
@@ -329,12 +367,13 @@ class EnsembleSerial(EnsembleThreads):
 class ODESolution:
     """One trajectory's solution: views into the ensemble arrays."""
 
-    def __init__(self, t, u, retcode, prob=None, stats=None):
+    def __init__(self, t, u, retcode, prob=None, stats=None, dense=None):
         self.t = t
         self._u = u
         self.retcode = ReturnCode(int(retcode))
         self.prob = prob
         self.stats = stats or {}
+        self._dense = dense  # callable(times) -> (len(times), n_state), or None
 
     @property
     def u(self):
@@ -347,8 +386,22 @@ class ODESolution:
         return self._u.shape[0]
 
     def __call__(self, t):
-        """Linear interpolation between the stored points."""
-        return np.array([np.interp(t, self.t, self._u[:, c]) for c in range(self._u.shape[1])])
+        """The solution at time(s) t.  A solve with dense=True evaluates the
+        method's own dense output (the interpolant the kernels save with) at t:
+        the trajectory is solved again on the GPU with t as its save times --
+        save points never change a trajectory's steps, so the values are
+        exactly those a saveat containing t would have stored.  Without
+        dense=True: linear interpolation between the stored points."""
+        scalar = np.ndim(t) == 0
+        ts = np.atleast_1d(np.asarray(t, np.float64))
+        if self._dense is not None:
+            order = np.argsort(ts, kind="stable")
+            vals = np.empty((len(ts), self._u.shape[1]))
+            vals[order] = self._dense(ts[order])
+        else:
+            vals = np.stack([np.interp(ts, self.t, self._u[:, c])
+                             for c in range(self._u.shape[1])], axis=1)
+        return vals[0] if scalar else vals
 
 
 class EnsembleSolution:
@@ -356,7 +409,7 @@ class EnsembleSolution:
     solutions; `U`, `t`, `retcode` expose the underlying arrays."""
 
     def __init__(self, U, t, retcode, lengths, stats, elapsed_ms, device_ms, output_func=None,
-                 reduction=None, probs=None):
+                 reduction=None, probs=None, dense=None):
         self.U = U                  # (N, n_save, n_state)
         self.t = t                  # (n_save,) or (N, n_save)
         self.retcode = retcode      # (N,) int32
@@ -366,6 +419,7 @@ class EnsembleSolution:
         self.device_ms = device_ms
         self._output_func = output_func
         self._probs = probs
+        self._dense = dense  # callable(i, times), or None
 
     def __len__(self):
         return self.U.shape[0]
@@ -374,8 +428,11 @@ class EnsembleSolution:
         n = int(self.lengths[i])
         t = self.t[:n] if self.t.ndim == 1 else self.t[i, :n]
         st = {k: v[i] for k, v in self.stats.items()}
+        dense = None
+        if self._dense is not None:
+            dense = (lambda ts, i=i: self._dense(i, ts))
         return ODESolution(t, self.U[i, :n], self.retcode[i],
-                           None if self._probs is None else self._probs[i], st)
+                           None if self._probs is None else self._probs[i], st, dense)
 
     def __getitem__(self, i):
         return self.solution(i)
@@ -494,7 +551,7 @@ def save_grid(t0, tf, saveat, save_start=None, save_end=None):
 
 
 # ----------------------------------------------------------------- solve
-_UNSUPPORTED = ("dense", "save_everystep", "tstops", "save_idxs")
+_UNSUPPORTED = ("save_everystep", "tstops", "save_idxs")
 
 
 def _gather_inputs(ens, N):
@@ -542,7 +599,7 @@ def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start
             raise NotImplementedError("solve keyword %r is not supported by EnsembleGB300" % k)
     extra = set(kwargs) - set(_UNSUPPORTED) - {"qmin", "qmax", "gamma", "beta1", "beta2",
                                                "qsteady_min", "qsteady_max", "qoldinit",
-                                               "callback"}
+                                               "callback", "dense"}
     if extra:
         raise TypeError("unknown solve keywords: %s" % sorted(extra))
     single = not isinstance(ens, EnsembleProblem)
@@ -577,12 +634,18 @@ def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start
         per = None
         if isinstance(saves, list):
             per = [s if s is not None else saveat for s in saves]
+        if per is None and saveat is None and kwargs.get("dense"):
+            # dense=True without saveat: store the end points; sol(t) evaluates
+            # the method's interpolant anywhere in between
+            saveat = []
+            save_start = True if save_start is None else save_start
+            save_end = True if save_end is None else save_end
         if per is None and saveat is None:
             if save_end is False and save_start is False:
                 raise ValueError("nothing to save")
             raise NotImplementedError(
-                "EnsembleGB300 stores fixed save grids: pass saveat (a step or a vector) "
-                "(saving every step is not supported)")
+                "EnsembleGB300 stores fixed save grids: pass saveat (a step or a vector), or "
+                "dense=True (saving every step is not supported)")
         uniform = per is None and (N == 0 or (np.all(t0 == t0[0]) and np.all(tf == tf[0])))
         if uniform:
             grid = save_grid(t0[0] if N else prob.tspan[0], tf[0] if N else prob.tspan[1],
@@ -627,8 +690,9 @@ def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start
     opts.learned = ensemblealg.learned_flags
     cb = kwargs.get("callback")
     if cb is not None:
-        if not isinstance(cb, _Callback):
-            raise TypeError("callback must be a ContinuousCallback or a DiscreteCallback")
+        if not isinstance(cb, (_Callback, CallbackSet)):
+            raise TypeError("callback must be a ContinuousCallback, DiscreteCallback, "
+                            "VectorContinuousCallback or CallbackSet")
         opts.callback = cb.id
     opts.block_size = int(ensemblealg.block_size)
     opts.ctas_per_sm = int(ensemblealg.ctas_per_sm)
@@ -649,9 +713,21 @@ def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start
         # a terminated trajectory ends at its event: keep the saves up to t_end
         ts = t_out if t_out.ndim == 2 else np.broadcast_to(t_out, (N, t_out.shape[-1]))
         lengths = np.where(term, np.sum(ts <= res["t_end"][:, None], axis=1), lengths)
+    dense = None
+    if kwargs.get("dense"):
+        dev = ensemblealg.devices[0]
+
+        def dense(i, ts, opts=opts, model=prob.f):
+            ts = np.asarray(ts, np.float64)
+            if np.any(ts < t0[i]) or np.any(ts > tf[i]):
+                raise ValueError("dense output is defined on [t0, tf] = [%g, %g]" % (t0[i], tf[i]))
+            r = solve_arrays(model, opts, p[i:i + 1], u0[i:i + 1], t0[i:i + 1], tf[i:i + 1], ts,
+                             capi.SAVE_GRID, u_dtype=ensemblealg.out_dtype, device=dev)
+            return np.asarray(r["u"][0], np.float64)
+
     sol = EnsembleSolution(res["u"], t_out, res["retcode"], lengths,
                            {k: res[k] for k in ("naccept", "nreject", "nf", "t_end")},
-                           res["total_ms"], res["device_ms"], probs=probs)
+                           res["total_ms"], res["device_ms"], probs=probs, dense=dense)
     if ens.output_func is not None:
         outs = []
         for i in range(N):

@@ -100,9 +100,10 @@ cudaError_t enqueue_summary(const void* u, int u_f32, int64_t N, int C, int nq,
 cudaError_t launch_team(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
 
 template <class K>
-cudaError_t launch_team_kernel(K kern, const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
+cudaError_t launch_team_kernel(K kern, const LaunchCfg& cfg, const KArgs& a, cudaStream_t s,
+                               int lanes = 16) {
   const int block = cfg.block > 0 ? cfg.block : 128;
-  const long long need = (a.N * 16 + block - 1) / block;
+  const long long need = (a.N * lanes + block - 1) / block;
   int grid;
   if (cfg.persistent) {
     int per_sm = cfg.ctas_per_sm;

@@ -124,6 +124,16 @@ struct VdpRing8 {
     const T dv = p[0] * (T(1) - x * x) * v - x + p[1] * (xl - T(2) * x + xr);
     return (r & 1) ? dv : v;
   }
+  // 8-lane teams (one oscillator per lane): lane l holds (x_l, v_l) in y[0],
+  // y[1]; only the neighbours' positions are fetched.  Same arithmetic as
+  // f_lane and f.
+  template <class T, class Sh>
+  GBDE_D static void f_osc(int l, const T* y, const T* p, const Sh& sh, T* dy) {
+    const T x = y[0], v = y[1];
+    const T xl = sh.bcast(x, (l + 7) & 7), xr = sh.bcast(x, (l + 1) & 7);
+    dy[0] = v;
+    dy[1] = p[0] * (T(1) - x * x) * v - x + p[1] * (xl - T(2) * x + xr);
+  }
   template <class T, class Sh>
   GBDE_D static void jac_lane(int r, T y, const T* p, const Sh& sh, T* Jr) {
     T x, v, xl, xr;

@@ -107,9 +107,12 @@ struct UserModelDef {
   int n, np;
 };
 
+// A registered callback: a leaf (GBDE_CB_CONTINUOUS / _DISCRETE / _VECTOR,
+// len conditions for a vector one) or a set (kind 0) of earlier ids.
 struct CallbackDef {
-  int kind;
+  int kind = 0, len = 1;
   std::string condition, affect;
+  std::vector<int> members;
 };
 
 struct Compiled {
@@ -127,6 +130,62 @@ std::map<Key, Compiled> g_compiled;
 
 const CallbackDef* find_callback(int id) {
   return (id >= 1 && id <= (int)g_callbacks.size()) ? &g_callbacks[id - 1] : nullptr;
+}
+
+// The leaves of a callback in order, sets expanded (members always have
+// smaller ids than their set, so this ends).
+void flatten_callback(const CallbackDef* cb, std::vector<const CallbackDef*>& out) {
+  if (cb->kind != 0) {
+    out.push_back(cb);
+    return;
+  }
+  for (int id : cb->members) flatten_callback(find_callback(id), out);
+}
+
+// UserCallback for the driver's interface (solver.cuh): the continuous
+// conditions of every ContinuousCallback (one) and VectorContinuousCallback
+// (len) in order, and the discrete callbacks in order.
+std::string callback_source(const CallbackDef* cb) {
+  std::vector<const CallbackDef*> leaves;
+  flatten_callback(cb, leaves);
+  const std::string args = "const double* u, double t, const double* p";
+  const std::string margs = "double* u, double t, const double* p, bool& terminate";
+  std::string s, conds, aff_c, cond_d, aff_d;
+  int nc = 0, nd = 0;
+  for (size_t q = 0; q < leaves.size(); ++q) {
+    const CallbackDef* l = leaves[q];
+    const std::string tag = std::to_string(q);
+    const std::string cond_line = "#line 1 \"callback" + tag + ":condition\"\n";
+    const std::string aff_line = "#line 1 \"callback" + tag + ":affect\"\n";
+    if (l->kind == GBDE_CB_DISCRETE) {
+      s += "  __device__ static bool cond_d" + tag + "(" + args + ") {\n    double g = 0.0;\n" +
+           cond_line + l->condition + "\n    return g != 0.0;\n  }\n";
+      s += "  __device__ static void aff_d" + tag + "(" + margs + ") {\n" + aff_line + l->affect +
+           "\n  }\n";
+      cond_d += "    case " + std::to_string(nd) + ": return cond_d" + tag + "(u, t, p);\n";
+      aff_d += "    case " + std::to_string(nd) + ": aff_d" + tag + "(u, t, p, terminate); return;\n";
+      ++nd;
+      continue;
+    }
+    const bool vec = l->kind == GBDE_CB_VECTOR;
+    s += "  __device__ static void cond_c" + tag + "(" + args + ", double* out) {\n" +
+         (vec ? "" : "    double g = 0.0;\n") + cond_line + l->condition +
+         (vec ? "\n  }\n" : "\n    out[0] = g;\n  }\n");
+    s += "  __device__ static void aff_c" + tag + "(int idx, " + margs + ") {\n    (void)idx;\n" +
+         aff_line + l->affect + "\n  }\n";
+    conds += "    cond_c" + tag + "(u, t, p, g + " + std::to_string(nc) + ");\n";
+    aff_c += "    if (idx < " + std::to_string(nc + l->len) + ") { aff_c" + tag + "(idx - " +
+             std::to_string(nc) + ", u, t, p, terminate); return; }\n";
+    nc += l->len;
+  }
+  return "struct UserCallback {\n  static constexpr int NC = " + std::to_string(nc) +
+         ", ND = " + std::to_string(nd) + ";\n" + s +
+         "  __device__ static void conditions(" + args + ", double* g) {\n" + conds + "  }\n" +
+         "  __device__ static void affect_c(int idx, " + margs + ") {\n" + aff_c + "  }\n" +
+         "  __device__ static bool condition_d(int k, " + args + ") {\n    switch (k) {\n" +
+         cond_d + "    }\n    return false;\n  }\n" +
+         "  __device__ static void affect_d(int k, " + margs + ") {\n    switch (k) {\n" + aff_d +
+         "    }\n  }\n};\ntypedef UserCallback GbdeRtcCallback;\n";
 }
 
 // Built-in models a runtime-compiled kernel (with a callback) can use.
@@ -220,17 +279,7 @@ std::string make_source(const UserModelDef* m, int model, const CallbackDef* cb,
     s += std::string("typedef ") + builtin_model(model) + " GbdeRtcModel;\n";
   }
   if (cb) {
-    std::snprintf(buf, sizeof(buf), "struct UserCallback {\n  static constexpr int KIND = %d;\n",
-                  cb->kind);
-    s += buf;
-    s += "  __device__ static double condition(const double* u, double t, const double* p) {\n"
-         "    double g = 0.0;\n#line 1 \"callback:condition\"\n";
-    s += cb->condition;
-    s += "\n    return g;\n  }\n"
-         "  __device__ static void affect(double* u, double t, const double* p, bool& terminate) {\n"
-         "#line 1 \"callback:affect\"\n";
-    s += cb->affect;
-    s += "\n  }\n};\ntypedef UserCallback GbdeRtcCallback;\n";
+    s += callback_source(cb);
   } else {
     s += "typedef NoCallback GbdeRtcCallback;\n";
   }
@@ -277,6 +326,16 @@ int compile_locked(int id, int alg, int precision, int callback, Compiled** out)
   const CallbackDef* cb = nullptr;
   if (callback != 0 && !(cb = find_callback(callback)))
     return fail(GBDE_ERR_INVALID, "unknown callback id " + std::to_string(callback));
+  if (cb) {
+    std::vector<const CallbackDef*> leaves;
+    flatten_callback(cb, leaves);
+    int nc = 0;
+    for (const CallbackDef* l : leaves) nc += l->kind == GBDE_CB_DISCRETE ? 0 : l->len;
+    if (nc > GBDE_MAX_CB_CONDITIONS)
+      return fail(GBDE_ERR_INVALID, "the callback set carries " + std::to_string(nc) +
+                                        " continuous conditions (at most " +
+                                        std::to_string(GBDE_MAX_CB_CONDITIONS) + ")");
+  }
   if (alg_type(alg, precision).empty())
     return fail(GBDE_ERR_UNSUPPORTED,
                 "runtime-compiled kernels run Tsit5, Vern7, Rosenbrock23, Rodas5 and Rodas5P, "
@@ -461,20 +520,48 @@ int gbde_model_compile(int32_t model_id, int32_t alg, int32_t precision) {
   return compile_locked(model_id, alg, precision, 0, &c);
 }
 
-int gbde_callback_register(const gbde_callback* def, int32_t* callback_id) {
-  if (!def || !callback_id || !def->condition)
-    return fail(GBDE_ERR_INVALID, "def, def->condition and callback_id must be non-NULL");
-  if (def->kind != GBDE_CB_CONTINUOUS && def->kind != GBDE_CB_DISCRETE)
-    return fail(GBDE_ERR_INVALID, "kind must be GBDE_CB_CONTINUOUS or GBDE_CB_DISCRETE");
-  CallbackDef c;
-  c.kind = def->kind;
-  c.condition = def->condition;
-  c.affect = def->affect ? def->affect : "";
-  if (def->terminate) c.affect += "\nterminate = true;";
+static int push_callback(CallbackDef&& c, int32_t* callback_id) {
   std::lock_guard<std::mutex> lk(g_mu);
+  for (int id : c.members)
+    if (!find_callback(id))
+      return fail(GBDE_ERR_INVALID, "unknown callback id " + std::to_string(id) + " in the set");
   g_callbacks.push_back(std::move(c));
   *callback_id = (int32_t)g_callbacks.size();
   return GBDE_OK;
+}
+
+static int leaf_callback(const gbde_callback* def, int kind, int len, int32_t* callback_id) {
+  if (!def || !callback_id || !def->condition)
+    return fail(GBDE_ERR_INVALID, "def, def->condition and callback_id must be non-NULL");
+  CallbackDef c;
+  c.kind = kind;
+  c.len = len;
+  c.condition = def->condition;
+  c.affect = def->affect ? def->affect : "";
+  if (def->terminate) c.affect += "\nterminate = true;";
+  return push_callback(std::move(c), callback_id);
+}
+
+int gbde_callback_register(const gbde_callback* def, int32_t* callback_id) {
+  if (def && def->kind != GBDE_CB_CONTINUOUS && def->kind != GBDE_CB_DISCRETE)
+    return fail(GBDE_ERR_INVALID, "kind must be GBDE_CB_CONTINUOUS or GBDE_CB_DISCRETE");
+  return leaf_callback(def, def ? def->kind : 0, 1, callback_id);
+}
+
+int gbde_vector_callback_register(const gbde_callback* def, int32_t len, int32_t* callback_id) {
+  if (len < 1 || len > GBDE_MAX_CB_CONDITIONS)
+    return fail(GBDE_ERR_INVALID, "len must be in [1, " + std::to_string(GBDE_MAX_CB_CONDITIONS) + "]");
+  if (def && def->kind != GBDE_CB_VECTOR)
+    return fail(GBDE_ERR_INVALID, "kind must be GBDE_CB_VECTOR");
+  return leaf_callback(def, GBDE_CB_VECTOR, len, callback_id);
+}
+
+int gbde_callback_set_register(const int32_t* ids, int32_t n, int32_t* set_id) {
+  if (!ids || !set_id || n < 1)
+    return fail(GBDE_ERR_INVALID, "ids and set_id must be non-NULL and n >= 1");
+  CallbackDef c;
+  c.members.assign(ids, ids + n);
+  return push_callback(std::move(c), set_id);
 }
 
 int gbde_callback_compile(int32_t model, int32_t alg, int32_t precision, int32_t callback_id) {

@@ -278,50 +278,81 @@ __global__ void __launch_bounds__(128) k_init_dt(const KArgs a, double* __restri
 }
 
 // ----------------------------------------------------------- callbacks
-// Event handling of the reference's ContinuousCallback / DiscreteCallback
-// (qa.jl:24,36; exercised by test/core.jl:60-79).  The precompiled kernels use
-// NoCallback and compile none of it.  A callback type (runtime-compiled from
-// user source, rtc.cu) provides
-//   static constexpr int KIND;   GBDE_CB_CONTINUOUS or GBDE_CB_DISCRETE
-//   static double condition(const double* u, double t, const double* p);
-//   static void affect(double* u, double t, const double* p, bool& terminate);
+// Event handling of the reference's ContinuousCallback, DiscreteCallback,
+// VectorContinuousCallback and CallbackSet (qa.jl:24,36,124,26; exercised by
+// test/core.jl:60-79).  The precompiled kernels use NoCallback and compile none
+// of it.  A callback type (runtime-compiled from user source, rtc.cu) provides
+//   static constexpr int NC;   continuous conditions: 1 per ContinuousCallback,
+//                              len per VectorContinuousCallback, summed over a set
+//   static constexpr int ND;   discrete callbacks
+//   static void conditions(const double* u, double t, const double* p, double* g);
+//   static void affect_c(int idx, double* u, double t, const double* p, bool& terminate);
+//   static bool condition_d(int k, const double* u, double t, const double* p);
+//   static void affect_d(int k, double* u, double t, const double* p, bool& terminate);
 // on FP64 copies of the state and parameters, whatever the precision.
-// Continuous: a sign change of condition over an accepted step is located on
-// the method's dense output by Illinois regula falsi; the integrator moves to
-// the left side of the root (the reference's LeftRootFind default), applies
-// affect and restarts the method there.  Save points up to the event use the
-// step's dense output.  The next step looks for crossings only after 1% of
-// its length (the reference's repeat_nudge), so a root is not found twice.
-// Discrete: condition != 0 after an accepted step applies affect.
+// Continuous: a sign change of condition idx over an accepted step is located
+// on the method's dense output by Illinois regula falsi; of several, the
+// earliest root is the event.  The integrator moves to the left side of the
+// root (the reference's LeftRootFind default), applies affect idx and restarts
+// the method there.  Save points up to the event use the step's dense output.
+// The next step looks for crossings only after 1% of its length (the
+// reference's repeat_nudge), so a root is not found twice.
+// Discrete: after an accepted step each condition k that is true applies its
+// affect, in order, on the state the previous ones left.
 struct NoCallback {
-  static constexpr int KIND = 0;
-  GBDE_D static double condition(const double*, double, const double*) { return 0.0; }
-  GBDE_D static void affect(double*, double, const double*, bool&) {}
+  static constexpr int NC = 0, ND = 0;
+  GBDE_D static void conditions(const double*, double, const double*, double*) {}
+  GBDE_D static void affect_c(int, double*, double, const double*, bool&) {}
+  GBDE_D static bool condition_d(int, const double*, double, const double*) { return false; }
+  GBDE_D static void affect_d(int, double*, double, const double*, bool&) {}
 };
 
 template <class CB, int N, int NP, class T>
-GBDE_D double cb_condition(const T* u, double t, const T* p) {
+GBDE_D void cb_conditions(const T* u, double t, const T* p, double* g) {
   double ud[N], pd[NP];
 #pragma unroll
   for (int c = 0; c < N; ++c) ud[c] = (double)u[c];
 #pragma unroll
   for (int k = 0; k < NP; ++k) pd[k] = (double)p[k];
-  return CB::condition(ud, t, pd);
+  CB::conditions(ud, t, pd, g);
 }
 
-// affect on an FP64 copy of u; returns terminate
+// continuous affect idx on an FP64 copy of u; returns terminate
 template <class CB, int N, int NP, class T>
-GBDE_D bool cb_affect(T* u, double t, const T* p) {
+GBDE_D bool cb_affect_c(int idx, T* u, double t, const T* p) {
   double ud[N], pd[NP];
 #pragma unroll
   for (int c = 0; c < N; ++c) ud[c] = (double)u[c];
 #pragma unroll
   for (int k = 0; k < NP; ++k) pd[k] = (double)p[k];
   bool term = false;
-  CB::affect(ud, t, pd, term);
+  CB::affect_c(idx, ud, t, pd, term);
 #pragma unroll
   for (int c = 0; c < N; ++c) u[c] = (T)ud[c];
   return term;
+}
+
+// every discrete callback in order on u; returns (any fired, terminate)
+template <class CB, int N, int NP, class T>
+GBDE_D bool cb_discrete(T* u, double t, const T* p, bool& term) {
+  double ud[N], pd[NP];
+#pragma unroll
+  for (int c = 0; c < N; ++c) ud[c] = (double)u[c];
+#pragma unroll
+  for (int k = 0; k < NP; ++k) pd[k] = (double)p[k];
+  bool any = false;
+#pragma unroll
+  for (int k = 0; k < CB::ND; ++k) {
+    if (CB::condition_d(k, ud, t, pd)) {
+      CB::affect_d(k, ud, t, pd, term);
+      any = true;
+    }
+  }
+  if (any) {
+#pragma unroll
+    for (int c = 0; c < N; ++c) u[c] = (T)ud[c];
+  }
+  return any;
 }
 
 GBDE_D bool cb_crossed(double g0, double g1) {
@@ -350,7 +381,7 @@ struct early_time<A, decltype(void(A::EARLY_TIME))> {
 template <class Alg, class M, class T, bool MIXED, class CB = NoCallback>
 __device__ void integrate_all(const KArgs& a) {
   constexpr int N = M::N;
-  double gprev = 0.0;     // continuous callback: condition at the current point
+  double gprev[CB::NC > 0 ? CB::NC : 1];  // continuous conditions at the current point
   bool nudge = false;     // an event ended the previous step (repeat nudge)
   WorkSource src;
   src.init();
@@ -416,8 +447,8 @@ __device__ void integrate_all(const KArgs& a) {
         if (a.dtmax > 0.0) dt = fmin(dt, a.dtmax);
         if (!(t < tf)) ret = GBDE_RET_SUCCESS;
         else if (!(dt > 0.0)) ret = GBDE_RET_DTLESSTHANMIN;
-        if constexpr (CB::KIND == GBDE_CB_CONTINUOUS) {
-          gprev = cb_condition<CB, N, M::NP>(alg.u(), t, p);
+        if constexpr (CB::NC > 0) {
+          cb_conditions<CB, N, M::NP>(alg.u(), t, p, gprev);
           nudge = false;
         }
       }
@@ -476,24 +507,30 @@ __device__ void integrate_all(const KArgs& a) {
         } else {
           step_end(tnew, tlo);
         }
-        // continuous callback: a crossing of the condition in (t, tnew]
-        // (after the repeat nudge when the previous step ended at an event)
+        // continuous callbacks: crossings of the conditions in (t, tnew]
+        // (after the repeat nudge when the previous step ended at an event);
+        // the earliest located root is the event
         bool event = false;
         double th_e = 1.0;
-        if constexpr (CB::KIND == GBDE_CB_CONTINUOUS) {
-          double ga = gprev, lo = 0.0;
+        int idx_e = 0;
+        if constexpr (CB::NC > 0) {
+          double ga[CB::NC], gb[CB::NC], lo = 0.0;
+#pragma unroll
+          for (int c = 0; c < CB::NC; ++c) ga[c] = gprev[c];
           if (nudge) {
             T un[N];
             lo = 0.01;
             alg.interp(lo, h, un, p, nfev);
-            ga = cb_condition<CB, N, M::NP>(un, t + lo * h, p);
+            cb_conditions<CB, N, M::NP>(un, t + lo * h, p, ga);
             nudge = false;
           }
-          const double gb = cb_condition<CB, N, M::NP>(alg.unew(), tnew, p);
-          if (cb_crossed(ga, gb)) {
-            // Illinois regula falsi on theta in [lo, 1]; the left end keeps
-            // the sign before the crossing
-            double a0 = lo, b0 = 1.0, fa = ga, fb = gb;
+          cb_conditions<CB, N, M::NP>(alg.unew(), tnew, p, gb);
+#pragma unroll 1
+          for (int ci = 0; ci < CB::NC; ++ci) {
+            if (!cb_crossed(ga[ci], gb[ci])) continue;
+            // Illinois regula falsi on theta in [lo, 1] for condition ci; the
+            // left end keeps the sign before the crossing
+            double a0 = lo, b0 = 1.0, fa = ga[ci], fb = gb[ci];
             int side = 0;
             for (int it = 0; it < 100; ++it) {
               if ((b0 - a0) * fabs(h) <= 8.9e-16 * fmax(fabs(t), fabs(tnew))) break;
@@ -501,7 +538,9 @@ __device__ void integrate_all(const KArgs& a) {
               if (!(m > a0 && m < b0)) m = 0.5 * (a0 + b0);
               T um[N];
               alg.interp(m, h, um, p, nfev);
-              const double fm = cb_condition<CB, N, M::NP>(um, t + m * h, p);
+              double gm[CB::NC];
+              cb_conditions<CB, N, M::NP>(um, t + m * h, p, gm);
+              const double fm = gm[ci];
               if (fm == 0.0) {
                 a0 = m;
                 break;
@@ -518,10 +557,15 @@ __device__ void integrate_all(const KArgs& a) {
                 side = 1;
               }
             }
-            th_e = a0;
+            if (!event || a0 < th_e) {
+              th_e = a0;
+              idx_e = ci;
+            }
             event = true;
-          } else {
-            gprev = gb;
+          }
+          if (!event) {
+#pragma unroll
+            for (int c = 0; c < CB::NC; ++c) gprev[c] = gb[c];
           }
         }
         // saveat: dense output at every save time in (t, tnew], or up to the
@@ -545,7 +589,8 @@ __device__ void integrate_all(const KArgs& a) {
           // move to the event, apply affect, restart the method there
           T ue[N];
           alg.interp(th_e, h, ue, p, nfev);
-          const bool term = cb_affect<CB, N, M::NP>(ue, te, p);
+          bool term = cb_affect_c<CB, N, M::NP>(idx_e, ue, te, p);
+          if constexpr (CB::ND > 0) cb_discrete<CB, N, M::NP>(ue, te, p, term);
           alg.init(ue, p, nfev);
           t = te;
           tlo = 0.0;
@@ -568,12 +613,12 @@ __device__ void integrate_all(const KArgs& a) {
           for (int c = 0; c < N; ++c) fin &= val_finite(alg.u()[c]);
           if (!fin) ret = GBDE_RET_UNSTABLE;
           else if (last) ret = GBDE_RET_SUCCESS;
-          if constexpr (CB::KIND == GBDE_CB_DISCRETE) {
-            if (fin && cb_condition<CB, N, M::NP>(alg.u(), t, p) != 0.0) {
-              T uc[N];
+          if constexpr (CB::ND > 0) {
+            T uc[N];
 #pragma unroll
-              for (int c = 0; c < N; ++c) uc[c] = alg.u()[c];
-              const bool term = cb_affect<CB, N, M::NP>(uc, t, p);
+            for (int c = 0; c < N; ++c) uc[c] = alg.u()[c];
+            bool term = false;
+            if (fin && cb_discrete<CB, N, M::NP>(uc, t, p, term)) {
               alg.init(uc, p, nfev);
               if (term) ret = GBDE_RET_TERMINATED;
             }

@@ -444,75 +444,6 @@ struct TeamRodasFF {
   }
 };
 
-// ------------------------------------------------------------ team Tsit5
-// Tsit5Alg (explicit_rk.cuh) with one component per lane; the FP32 path keeps
-// the compensated state uu + lo.
-template <class M, class T>
-struct TeamTsit5 {
-  static constexpr int ORDER = 5, ALG_ID = GBDE_ALG_TSIT5;
-  static constexpr bool CMP = sizeof(T) == 4;
-  static_assert(M::N == TEAM, "team kernels are for 16-state models");
-  T uu, un, lo, lon, k1, k2, k3, k4, k5, k6, k7;
-
-  GBDE_D T u() const { return uu; }
-  GBDE_D T unew() const { return un; }
-  GBDE_D T f0() const { return k1; }
-
-  GBDE_D T at(T inc) const {
-    if constexpr (CMP) return uu + (lo + inc);
-    else return uu + inc;
-  }
-  GBDE_D T rhs(T y, const T* p, const Team& tm) const { return M::f_lane(tm.lane, y, p, tm); }
-
-  GBDE_D void init(T u0, const T* p, const Team& tm, int& nf) {
-    uu = u0;
-    lo = T(0);
-    k1 = rhs(uu, p, tm);
-    ++nf;
-  }
-
-  GBDE_D double attempt(double dt, const T* p, double abstol, double reltol, const Team& tm,
-                        int& nf) {
-    using namespace tab::tsit5;
-    const T h = team_scalar<T>(dt);
-    k2 = rhs(at(h * (T(a21) * k1)), p, tm);
-    k3 = rhs(at(h * (T(a31) * k1 + T(a32) * k2)), p, tm);
-    k4 = rhs(at(h * (T(a41) * k1 + T(a42) * k2 + T(a43) * k3)), p, tm);
-    k5 = rhs(at(h * (T(a51) * k1 + T(a52) * k2 + T(a53) * k3 + T(a54) * k4)), p, tm);
-    k6 = rhs(at(h * (T(a61) * k1 + T(a62) * k2 + T(a63) * k3 + T(a64) * k4 + T(a65) * k5)), p,
-             tm);
-    const T inc = h * (T(a71) * k1 + T(a72) * k2 + T(a73) * k3 + T(a74) * k4 + T(a75) * k5 +
-                       T(a76) * k6);
-    if constexpr (CMP) two_sum_t(uu, lo + inc, un, lon);
-    else un = uu + inc;
-    k7 = rhs(un, p, tm);
-    nf += 6;
-    const T err = h * (T(bt1) * k1 + T(bt2) * k2 + T(bt3) * k3 + T(bt4) * k4 + T(bt5) * k5 +
-                       T(bt6) * k6 + T(bt7) * k7);
-    return tm.sum(lane_err2(err, uu, un, abstol, reltol)) * (1.0 / TEAM);
-  }
-
-  GBDE_D T interp(double th, double dt) const {
-    using namespace tab::tsit5;
-    const double t2 = th * th;
-    const T b1 = (T)(r11 * th * (th - r12) * (t2 - r13 * th + r14));
-    const T b2 = (T)(r21 * t2 * (t2 - r22 * th + r23));
-    const T b3 = (T)(r31 * t2 * (t2 - r32 * th + r33));
-    const T b4 = (T)(r41 * (th - r42) * (th - r43) * t2);
-    const T b5 = (T)(r51 * (th - r52) * (th - r53) * t2);
-    const T b6 = (T)(r61 * (th - r62) * (th - r63) * t2);
-    const T b7 = (T)(r71 * (th - r72) * (th - r73) * t2);
-    const T h = team_scalar<T>(dt);
-    return at(h * (b1 * k1 + b2 * k2 + b3 * k3 + b4 * k4 + b5 * k5 + b6 * k6 + b7 * k7));
-  }
-
-  GBDE_D void accept() {
-    uu = un;
-    if constexpr (CMP) lo = lon;
-    k1 = k7;
-  }
-};
-
 // ----------------------------------------------------------- team driver
 // integrate_all (solver.cuh) for teams: the same controller, saves, return
 // codes and deadline; every scalar decision is team-uniform.
@@ -650,6 +581,310 @@ __device__ void integrate_team(const KArgs& a) {
       }
     }
     for (; js < a.n_save; ++js) store(js, __longlong_as_double(0x7ff8000000000000ll));
+    if (tm.lane == 0) {
+      a.retcode[i] = ret;
+      if (a.naccept) a.naccept[i] = nacc;
+      if (a.nreject) a.nreject[i] = nrej;
+      if (a.nf) a.nf[i] = nfev;
+      if (a.t_end) a.t_end[i] = t + tlo;
+      if (a.method_out) a.method_out[i] = Alg::ALG_ID;
+      if (a.dt_first) a.dt_first[i] = dt1;
+    }
+  }
+}
+
+// ------------------------------------------ 8-lane Tsit5 (two components per lane)
+// The explicit method needs no W-matrix, so a team of 8 lanes carries a
+// trajectory of the 16-state ring with one oscillator (two components) per
+// lane: 4 trajectories per warp instead of 2.  Every per-trajectory scalar
+// operation of the driver (error-norm sum, step-size products, compensated
+// time) runs once per team, and on GB300's narrow FP64 pipe those bound the
+// 16-lane pair kernel; the right-hand side fetches two neighbours per
+// oscillator instead of four per component.  Same method and arithmetic per
+// component as Tsit5Alg (explicit_rk.cuh); the FP32 path keeps the compensated
+// state uu + lo.
+constexpr int TEAM8 = 8;
+
+struct Team8 {
+  unsigned mask;  // the team's 8 lanes within the warp
+  int lane;       // 0..7: components 2 lane, 2 lane + 1
+  GBDE_D void init() {
+    const int l = threadIdx.x & 31;
+    lane = l & (TEAM8 - 1);
+    mask = 0xFFu << (l & 24);
+  }
+  template <class T> GBDE_D T bcast(T v, int src) const { return __shfl_sync(mask, v, src, TEAM8); }
+  GBDE_D ff bcast(ff v, int src) const {
+    return ff(__shfl_sync(mask, v.hi, src, TEAM8), __shfl_sync(mask, v.lo, src, TEAM8));
+  }
+  GBDE_D double sum(double v) const {
+#pragma unroll
+    for (int o = TEAM8 / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o, TEAM8);
+    return v;
+  }
+};
+
+template <class M, class T>
+struct TeamTsit5P {
+  static constexpr int ORDER = 5, ALG_ID = GBDE_ALG_TSIT5;
+  static constexpr bool CMP = sizeof(T) == 4;
+  static_assert(M::N == 2 * TEAM8, "8-lane teams are for 16-state models");
+  T uu[2], un[2], lo[2], lon[2], k1[2], k2[2], k3[2], k4[2], k5[2], k6[2], k7[2];
+
+  GBDE_D const T* u() const { return uu; }
+  GBDE_D const T* unew() const { return un; }
+  GBDE_D const T* f0() const { return k1; }
+
+  GBDE_D T at(int c, T inc) const {
+    if constexpr (CMP) return uu[c] + (lo[c] + inc);
+    else return uu[c] + inc;
+  }
+  GBDE_D void rhs(const T* y, const T* p, const Team8& tm, T* dy) const {
+    M::f_osc(tm.lane, y, p, tm, dy);
+  }
+
+  GBDE_D void init(const T* u0, const T* p, const Team8& tm, int& nf) {
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      uu[c] = u0[c];
+      lo[c] = T(0);
+    }
+    rhs(uu, p, tm, k1);
+    ++nf;
+  }
+
+  GBDE_D double attempt(double dt, const T* p, double abstol, double reltol, const Team8& tm,
+                        int& nf) {
+    using namespace tab::tsit5;
+    const T h = team_scalar<T>(dt);
+    T y[2];
+#define GBDE_T8_STAGE(dst, expr)               \
+  _Pragma("unroll") for (int c = 0; c < 2; ++c) \
+    y[c] = at(c, h * (expr));                    \
+  rhs(y, p, tm, dst);
+    GBDE_T8_STAGE(k2, T(a21) * k1[c])
+    GBDE_T8_STAGE(k3, T(a31) * k1[c] + T(a32) * k2[c])
+    GBDE_T8_STAGE(k4, T(a41) * k1[c] + T(a42) * k2[c] + T(a43) * k3[c])
+    GBDE_T8_STAGE(k5, T(a51) * k1[c] + T(a52) * k2[c] + T(a53) * k3[c] + T(a54) * k4[c])
+    GBDE_T8_STAGE(k6, T(a61) * k1[c] + T(a62) * k2[c] + T(a63) * k3[c] + T(a64) * k4[c] +
+                          T(a65) * k5[c])
+#undef GBDE_T8_STAGE
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const T inc = h * (T(a71) * k1[c] + T(a72) * k2[c] + T(a73) * k3[c] + T(a74) * k4[c] +
+                         T(a75) * k5[c] + T(a76) * k6[c]);
+      if constexpr (CMP) two_sum_t(uu[c], lo[c] + inc, un[c], lon[c]);
+      else un[c] = uu[c] + inc;
+    }
+    rhs(un, p, tm, k7);
+    nf += 6;
+    double e2 = 0.0;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const T err = h * (T(bt1) * k1[c] + T(bt2) * k2[c] + T(bt3) * k3[c] + T(bt4) * k4[c] +
+                         T(bt5) * k5[c] + T(bt6) * k6[c] + T(bt7) * k7[c]);
+      e2 += lane_err2(err, uu[c], un[c], abstol, reltol);
+    }
+    return tm.sum(e2) * (1.0 / M::N);
+  }
+
+  GBDE_D void interp(double th, double dt, T* out) const {
+    using namespace tab::tsit5;
+    const double t2 = th * th;
+    const T b1 = team_scalar<T>(r11 * th * (th - r12) * (t2 - r13 * th + r14));
+    const T b2 = team_scalar<T>(r21 * t2 * (t2 - r22 * th + r23));
+    const T b3 = team_scalar<T>(r31 * t2 * (t2 - r32 * th + r33));
+    const T b4 = team_scalar<T>(r41 * (th - r42) * (th - r43) * t2);
+    const T b5 = team_scalar<T>(r51 * (th - r52) * (th - r53) * t2);
+    const T b6 = team_scalar<T>(r61 * (th - r62) * (th - r63) * t2);
+    const T b7 = team_scalar<T>(r71 * (th - r72) * (th - r73) * t2);
+    const T h = team_scalar<T>(dt);
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+      out[c] = at(c, h * (b1 * k1[c] + b2 * k2[c] + b3 * k3[c] + b4 * k4[c] + b5 * k5[c] +
+                          b6 * k6[c] + b7 * k7[c]));
+  }
+
+  GBDE_D void accept() {
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      uu[c] = un[c];
+      if constexpr (CMP) lo[c] = lon[c];
+      k1[c] = k7[c];
+    }
+  }
+};
+
+// integrate_team for 8-lane teams with two components per lane: the same
+// controller, saves, return codes and deadline.
+template <class Alg, class M, class T, bool MIXED>
+__device__ void integrate_team8(const KArgs& a) {
+  Team8 tm;
+  tm.init();
+  const int64_t team_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / TEAM8;
+  const uint64_t t_start = a.timeout_ns ? global_ns() : 0;
+  bool first = true;
+  Alg alg;
+  T p[M::NP];
+  const int c0 = 2 * tm.lane;  // this lane's first component
+  while (true) {
+    // ---- next trajectory (team-uniform)
+    int64_t i;
+    if (a.queue == nullptr) {
+      if (!first) break;
+      i = team_id < a.N ? (a.order ? (int64_t)a.order[team_id] : team_id) : -1;
+    } else {
+      unsigned long long idx = 0;
+      if (tm.lane == 0) idx = atomicAdd(a.queue, 1ull);
+      idx = tm.bcast(idx, 0);
+      i = idx < (unsigned long long)a.N ? (a.order ? (int64_t)a.order[idx] : (int64_t)idx) : -1;
+    }
+    first = false;
+    if (i < 0) break;
+#pragma unroll
+    for (int k = 0; k < M::NP; ++k) p[k] = (T)__ldg(a.p + (size_t)i * M::NP + k);
+    // scalar loads and stores: the caller's arrays need only element alignment
+    const double u0x = __ldg(a.u0 + (size_t)i * M::N + c0);
+    const double u0y = __ldg(a.u0 + (size_t)i * M::N + c0 + 1);
+    const T u0[2] = {(T)u0x, (T)u0y};
+    double t = __ldg(a.t0 + i), tlo = 0.0;
+    const double tf = __ldg(a.tf + i);
+    int js = 0, nacc = 0, nrej = 0, nfev = 0;
+    int64_t iters = 0;
+    float lqold = a.ctl.lqoldinit;
+    double dt1 = __longlong_as_double(0x7ff8000000000000ll);
+    int ret = GBDE_RET_DEFAULT;
+    const bool bad_lane = !isfinite(u0x) || !isfinite(u0y);
+    const bool bad = !(tf >= t) || !isfinite(t) || !isfinite(tf) ||
+                     __any_sync(tm.mask, bad_lane);
+    auto store = [&](int j, double v0, double v1) {  // FP64 values of this lane's components
+      if (a.red) {
+        reduce_add(a, j, c0, M::N, v0);
+        reduce_add(a, j, c0 + 1, M::N, v1);
+      }
+      if (a.u_out == nullptr) return;
+      const size_t o = ((size_t)i * a.n_save + j) * M::N + c0;
+      if (a.out_f32) {
+        ((float*)a.u_out)[o] = (float)v0;
+        ((float*)a.u_out)[o + 1] = (float)v1;
+      } else {
+        ((double*)a.u_out)[o] = v0;
+        ((double*)a.u_out)[o + 1] = v1;
+      }
+    };
+    // save points at t0 store u0 exactly (the FP64 input, whatever T)
+    while (js < a.n_save && save_time(a, i, js) <= t) store(js++, u0x, u0y);
+    double dt = 0.0;
+    if (bad) {
+      ret = GBDE_RET_INITIALFAILURE;
+    } else {
+      alg.init(u0, p, tm, nfev);
+      if (a.pred_dt != nullptr && a.pred_dt[i] > 0.f) {
+        dt = fmin((double)a.pred_dt[i], tf - t);
+      } else if (a.dt0 > 0.0 || !a.adaptive) {
+        dt = a.dt0;
+      } else {
+        // Hairer-Wanner starting step (hw_h0 / hw_dt, controller.h)
+        double r[2], s0 = 0.0, s1 = 0.0;
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          r[c] = rcp64(a.abstol + fabs((double)alg.u()[c]) * a.reltol);
+          const double x = (double)alg.u()[c] * r[c], y = (double)alg.f0()[c] * r[c];
+          s0 += x * x;
+          s1 += y * y;
+        }
+        s0 = tm.sum(s0) * (1.0 / M::N);
+        s1 = tm.sum(s1) * (1.0 / M::N);
+        const double h0 = hw_h0(s0, s1, tf - t);
+        T y[2], f1[2];
+#pragma unroll
+        for (int c = 0; c < 2; ++c) y[c] = alg.u()[c] + T(h0) * alg.f0()[c];
+        alg.rhs(y, p, tm, f1);
+        ++nfev;
+        double s2 = 0.0;
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const double z = ((double)f1[c] - (double)alg.f0()[c]) * r[c];
+          s2 += z * z;
+        }
+        dt = hw_dt(h0, s1, tm.sum(s2) * (1.0 / M::N), tf - t, Alg::ORDER);
+      }
+      if (a.dtmax > 0.0) dt = fmin(dt, a.dtmax);
+      if (!(t < tf)) ret = GBDE_RET_SUCCESS;
+      else if (!(dt > 0.0)) ret = GBDE_RET_DTLESSTHANMIN;
+    }
+    while (ret == GBDE_RET_DEFAULT) {
+      const double rem = tf - t;
+      double h = dt;
+      bool last = false;
+      if (ord_bits(h * (1.0 + 1e-10)) >= ord_bits(rem)) {
+        h = rem;
+        last = true;
+      }
+      const double ms = alg.attempt(h, p, a.abstol, a.reltol, tm, nfev);
+      ++iters;
+      if (!a.adaptive || mag_bits(ms) <= 0x3FF0000000000000ull) {  // ms <= 1 (integer pipe)
+        double dtnew = h;
+        if (a.adaptive) dtnew = h * f2d_bits(ctl_accept(a.ctl, ms, lqold));
+        double tnew;
+        if (last) {
+          tnew = tf;
+          tlo = 0.0;
+        } else if (MIXED) {
+          // Fast2Sum on the operands ordered by magnitude (integer compare),
+          // as integrate_all
+          const bool tb = mag_bits(t) >= mag_bits(h);
+          const double big = tb ? t : h, small = tb ? h : t;
+          const double s = big + small;
+          double e = small - (s - big);
+          e += tlo;
+          tnew = s + e;
+          tlo = e - (tnew - s);
+        } else {
+          tnew = t + h;
+        }
+        const uint64_t tnew_o = ord_bits(tnew);
+        while (js < a.n_save) {
+          const double ts = save_time(a, i, js);
+          const uint64_t ts_o = ord_bits(ts);
+          if (ts_o > tnew_o) break;
+          if (ts_o == tnew_o) {
+            store(js, (double)alg.unew()[0], (double)alg.unew()[1]);
+          } else {
+            T v[2];
+            alg.interp(((ts - t) - tlo) / h, h, v);
+            store(js, (double)v[0], (double)v[1]);
+          }
+          ++js;
+        }
+        alg.accept();
+        t = tnew;
+        if (nacc == 0) dt1 = h;
+        ++nacc;
+        if (__any_sync(tm.mask, !val_finite(alg.u()[0]) || !val_finite(alg.u()[1])))
+          ret = GBDE_RET_UNSTABLE;
+        else if (last) ret = GBDE_RET_SUCCESS;
+        dt = a.dtmax > 0.0 && ord_bits(dtnew) > ord_bits(a.dtmax) ? a.dtmax : dtnew;
+      } else {
+        ++nrej;
+        dt = h * f2d_bits(ctl_reject(a.ctl, ms));
+      }
+      if (ret == GBDE_RET_DEFAULT) {
+        if (iters >= a.maxiters) ret = GBDE_RET_MAXITERS;
+        else if (a.adaptive && dt_too_small(dt, a.dtmin, t))
+          ret = GBDE_RET_DTLESSTHANMIN;
+        else if (a.timeout_ns && (iters & 31) == 0) {
+          // lane 0's clock decides for the team
+          const int late = tm.bcast((int)(global_ns() - t_start > a.timeout_ns), 0);
+          if (late) {
+            ret = GBDE_RET_TIMEOUT;
+            if (tm.lane == 0) atomicOr(a.flag, 1);
+          }
+        }
+      }
+    }
+    const double nanv = __longlong_as_double(0x7ff8000000000000ll);
+    for (; js < a.n_save; ++js) store(js, nanv, nanv);
     if (tm.lane == 0) {
       a.retcode[i] = ret;
       if (a.naccept) a.naccept[i] = nacc;

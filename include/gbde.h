@@ -74,6 +74,9 @@ extern "C" {
 /* callback kinds (gbde_callback.kind) */
 #define GBDE_CB_CONTINUOUS 1      /* ContinuousCallback (qa.jl:24)         */
 #define GBDE_CB_DISCRETE 2        /* DiscreteCallback (qa.jl:36)           */
+#define GBDE_CB_VECTOR 3          /* VectorContinuousCallback (qa.jl:124)  */
+/* most continuous conditions one solve's callback (set) may carry */
+#define GBDE_MAX_CB_CONDITIONS 64
 
 /* ---- built-in right-hand sides (ODEFunction f!(du,u,p,t), qa.jl:84) ---- */
 #define GBDE_MODEL_LINEAR 1    /* n=1, p=[a]:           du = a*u (test/core.jl:10) */
@@ -462,31 +465,46 @@ GBDE_API int gbde_sde_model_register(const gbde_user_model* def, const char* g_b
 GBDE_API int gbde_model_compile(int32_t model_id, int32_t alg, int32_t precision);
 
 /* ---- callbacks ----------------------------------------------------------
- * Replace ContinuousCallback / DiscreteCallback (qa.jl:24,36; the reference's
- * own tests solve with both, test/core.jl:60-79).  condition is CUDA C++
- * statements that set `double g` from `const double* u` (the state), `double
- * t` and `const double* p`; affect (may be NULL) modifies `double* u` and may
- * set `bool terminate`.
- *   GBDE_CB_CONTINUOUS: a sign change of g over an accepted step is located
- *     on the method's dense output (Illinois regula falsi to ~1 ulp of t);
- *     the trajectory moves to the left side of the root (LeftRootFind),
- *     applies affect and restarts the method there.  Save points up to the
- *     event use the step's dense output; the next step ignores crossings in
- *     its first 1% (repeat_nudge), so a root is found once.
- *   GBDE_CB_DISCRETE: g != 0 after an accepted step applies affect.
+ * Replace ContinuousCallback / DiscreteCallback / VectorContinuousCallback /
+ * CallbackSet (qa.jl:24,36,124,26; the reference's own tests solve with the
+ * first two, test/core.jl:60-79).  condition is CUDA C++ statements that set
+ * `double g` from `const double* u` (the state), `double t` and `const
+ * double* p` (GBDE_CB_VECTOR: that set `out[0..len-1]`, `double* out`);
+ * affect (may be NULL) modifies `double* u` and may set `bool terminate`
+ * (GBDE_CB_VECTOR: `int idx` in [0, len) names the condition that fired).
+ *   GBDE_CB_CONTINUOUS / GBDE_CB_VECTOR: a sign change of a condition over an
+ *     accepted step is located on the method's dense output (Illinois regula
+ *     falsi to ~1 ulp of t); of several, the earliest root (the first
+ *     condition on a tie) is the event.  The trajectory moves to the left
+ *     side of the root (LeftRootFind), applies that affect and restarts the
+ *     method there.  Save points up to the event use the step's dense output;
+ *     the next step ignores crossings in its first 1% (repeat_nudge), so a
+ *     root is found once.
+ *   GBDE_CB_DISCRETE: g != 0 after an accepted step (or an event) applies
+ *     affect.
+ * A set (gbde_callback_set_register) holds earlier ids, sets included, in
+ * order: its continuous conditions compete for the earliest root; after each
+ * accepted step or event its discrete callbacks run in order.
  * terminate ends the trajectory with GBDE_RET_TERMINATED (later save slots
  * hold NaN; t_end is the event time).  A solve with opts.callback compiles
  * its kernels at run time (NVRTC, as user models), for built-in one-thread
  * models and user models; not GBDE_ALG_AUTO, SDE methods or learned=1.
  * Callback saves (save_positions) are not made: only the saveat points.   */
 typedef struct {
-  int32_t kind;          /* GBDE_CB_CONTINUOUS or GBDE_CB_DISCRETE         */
+  int32_t kind;          /* GBDE_CB_CONTINUOUS, GBDE_CB_DISCRETE, _VECTOR  */
   const char* condition; /* statements: g = ...   (required)               */
   const char* affect;    /* statements on u[] / terminate, or NULL         */
   int32_t terminate;     /* 1: terminate after affect at every event       */
 } gbde_callback;
 /* Register a callback; *callback_id (>= 1) goes into gbde_opts.callback. */
 GBDE_API int gbde_callback_register(const gbde_callback* def, int32_t* callback_id);
+/* Register a VectorContinuousCallback of len conditions (def->kind ==
+ * GBDE_CB_VECTOR, 1 <= len <= GBDE_MAX_CB_CONDITIONS). */
+GBDE_API int gbde_vector_callback_register(const gbde_callback* def, int32_t len,
+                                           int32_t* callback_id);
+/* Register a CallbackSet of n earlier callback ids (leaves or sets); a solve
+ * with it carries at most GBDE_MAX_CB_CONDITIONS continuous conditions. */
+GBDE_API int gbde_callback_set_register(const int32_t* ids, int32_t n, int32_t* set_id);
 /* Compile (and cache) the kernels of a model with a callback for one
  * algorithm and precision, without a GPU; errors as gbde_model_compile. */
 GBDE_API int gbde_callback_compile(int32_t model, int32_t alg, int32_t precision,

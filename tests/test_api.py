@@ -117,10 +117,11 @@ def test_problem_and_remake(de):
 def test_solve_rejects_unsupported(de):
     prob = de.ODEProblem(de.models.linear, 0.5, (0.0, 1.0), [1.01])
     ens = de.EnsembleProblem(prob)
-    with pytest.raises(NotImplementedError):
-        de.solve(ens, de.Tsit5(), de.EnsembleGB300(), trajectories=2, saveat=0.1,
-                 dense=True)
-    with pytest.raises(TypeError):  # callbacks are ContinuousCallback / DiscreteCallback objects
+    for key in ("save_everystep", "tstops", "save_idxs"):
+        with pytest.raises(NotImplementedError):
+            de.solve(ens, de.Tsit5(), de.EnsembleGB300(), trajectories=2, saveat=0.1,
+                     **{key: True})
+    with pytest.raises(TypeError):  # callbacks are the callback classes and sets of them
         de.solve(ens, de.Tsit5(), de.EnsembleGB300(), trajectories=2, saveat=0.1,
                  callback=object())
     with pytest.raises(NotImplementedError):

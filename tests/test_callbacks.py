@@ -183,3 +183,112 @@ def test_rodas5_event_on_robertson(capi, de, prec):
     t_lin = fine[k - 1] + (y[np.arange(N), k - 1] - 0.8) / (
         y[np.arange(N), k - 1] - y[np.arange(N), k]) * (fine[k] - fine[k - 1])
     np.testing.assert_allclose(r["t_end"], t_lin, rtol=1e-5)
+
+
+# ------------------------------------------- vector callbacks and sets
+BALLS_F = "du[0] = u[1]; du[1] = -p[0]; du[2] = u[3]; du[3] = -p[1];"  # p = [g1, g2, e1, e2]
+BOUNCE_IDX = "u[2 * idx + 1] = -p[2 + idx] * u[2 * idx + 1];"
+
+
+def test_vector_callback_and_set_compile(capi, de):
+    """VectorContinuousCallback / CallbackSet (qa.jl:124,26) compile for the
+    one-thread methods and both precisions; sets nest; a set over the
+    condition limit, an unknown member and a bad length are refused."""
+    balls = de.ODEFunction(BALLS_F, 4, 4, name="balls_compile")
+    vc = de.VectorContinuousCallback("out[0] = u[0]; out[1] = u[2];", BOUNCE_IDX, 2)
+    c0 = de.ContinuousCallback("g = u[0];", "u[1] = -p[2] * u[1];")
+    c1 = de.ContinuousCallback("g = u[2];", "u[3] = -p[3] * u[3];")
+    d = de.DiscreteCallback("g = t > 0.5;", "u[1] += 0.0;")
+    nested = de.CallbackSet(de.CallbackSet(c0, d), c1, vc)
+    L = capi.lib()
+    for cb in (vc, de.CallbackSet(c0, c1, d), nested):
+        for alg, prec in ((capi.ALG_TSIT5, capi.PREC_FP64), (capi.ALG_VERN7, capi.PREC_F32X2),
+                          (capi.ALG_RODAS5, capi.PREC_FP64)):
+            _skip_without_nvrtc(capi, lambda: capi.check(
+                L.gbde_callback_compile(balls.id, alg, prec, cb.id)))
+    with pytest.raises(capi.GBDEError):
+        de.VectorContinuousCallback("out[0] = u[0];", None, 0)
+    with pytest.raises(capi.GBDEError):
+        de.VectorContinuousCallback("out[0] = u[0];", None, capi.MAX_CB_CONDITIONS + 1)
+    import ctypes as C
+    ids, sid = (C.c_int32 * 1)(10 ** 6), C.c_int32()
+    with pytest.raises(capi.GBDEError):
+        capi.check(L.gbde_callback_set_register(ids, 1, C.byref(sid)))
+    big = de.VectorContinuousCallback("out[0] = u[0];", None, capi.MAX_CB_CONDITIONS)
+    over = de.CallbackSet(big, c0)
+    with pytest.raises(capi.GBDEError) as e:
+        _skip_without_nvrtc(capi, lambda: capi.check(
+            L.gbde_callback_compile(balls.id, capi.ALG_TSIT5, capi.PREC_FP64, over.id)))
+    assert "continuous conditions" in str(e.value)
+    with pytest.raises(TypeError):
+        de.CallbackSet(c0, "g = t;")
+
+
+def _two_balls(de, N, seed):
+    rng = np.random.default_rng(seed)
+    g = rng.uniform(5.0, 15.0, (N, 2))
+    e = rng.uniform(0.8, 0.9, (N, 2))
+    h0 = rng.uniform(0.5, 2.0, (N, 2))
+    u0 = np.c_[h0[:, 0], np.zeros(N), h0[:, 1], np.zeros(N)]
+    return g, e, h0, u0, np.c_[g, e]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", ["vector", "set"])
+@pytest.mark.parametrize("precision", ["fp64", "f32x2"])
+def test_two_balls_vector_callback_exact(capi, de, form, precision):
+    """Two independent balls in one state, their impacts as one
+    VectorContinuousCallback (idx picks the ball) or as a CallbackSet of two
+    ContinuousCallbacks plus a no-op DiscreteCallback: every save follows the
+    analytic solution of each ball through its own bounces, so the earliest
+    root of the two conditions is taken each time and the affect gets the
+    right index."""
+    N = 384
+    g, e, h0, u0, p = _two_balls(de, N, 6)
+    balls = de.ODEFunction(BALLS_F, 4, 4, name="balls_%s_%s" % (form, precision))
+    if form == "vector":
+        cb = de.VectorContinuousCallback("out[0] = u[0]; out[1] = u[2];", BOUNCE_IDX, 2)
+    else:
+        cb = de.CallbackSet(de.ContinuousCallback("g = u[0];", "u[1] = -p[2] * u[1];"),
+                            de.DiscreteCallback("g = 1.0;"),
+                            de.ContinuousCallback("g = u[2];", "u[3] = -p[3] * u[3];"))
+    ens = de.EnsembleProblem(de.ODEProblem(balls, u0[0], (0.0, 1.0), p[0]),
+                             batch=lambda prob, n: {"p": p, "u0": u0})
+    sol = de.solve(ens, de.Tsit5(), de.EnsembleGB300(precision=precision), trajectories=N,
+                   saveat=0.05, reltol=1e-10, abstol=1e-10, callback=cb)
+    assert sol.converged
+    ts = de.save_grid(0.0, 1.0, 0.05)
+    err = 0.0
+    for i in range(N):
+        for b in range(2):
+            x, v = _ball_truth(h0[i, b], g[i, b], e[i, b], ts)
+            err = max(err, np.abs(sol.U[i, :, 2 * b] - x).max(),
+                      np.abs(sol.U[i, :, 2 * b + 1] - v).max() / g[i, b])
+    assert err <= 1e-8, err
+
+
+@pytest.mark.gpu
+def test_discrete_callbacks_in_order_after_events(capi, de):
+    """Discrete members of a set run in order after every accepted step and
+    after every event: the first counts (u[4] += 1), the second doubles the
+    count's copy (u[5] = 2 u[4]), so u[5] == 2 u[4] at every save only if
+    the order holds.  naccept counts accepted steps, event-truncated ones
+    included, and the save at the final time holds the state before that
+    step's discrete affects (as the reference's saveat with the callbacks'
+    default save_positions), so the last saved count is naccept - 1."""
+    N = 64
+    g, e, h0, u0, p = _two_balls(de, N, 7)
+    f = BALLS_F + " du[4] = 0.0; du[5] = 0.0;"
+    balls = de.ODEFunction(f, 6, 4, name="balls_counted")
+    cb = de.CallbackSet(de.ContinuousCallback("g = u[0];", "u[1] = -p[2] * u[1];"),
+                        de.DiscreteCallback("g = 1.0;", "u[4] += 1.0;"),
+                        de.DiscreteCallback("g = 1.0;", "u[5] = 2.0 * u[4];"))
+    o = capi.opts_default(capi.ALG_TSIT5)
+    o.reltol = o.abstol = 1e-9
+    o.callback = cb.id
+    grid = de.save_grid(0.0, 1.0, 0.1)
+    r = de.solve_arrays(balls, o, p, np.c_[u0, np.zeros((N, 2))], np.zeros(N), np.ones(N),
+                        grid, capi.SAVE_GRID)
+    assert np.all(r["retcode"] == capi.RET_SUCCESS)
+    np.testing.assert_array_equal(r["u"][:, :, 5], 2.0 * r["u"][:, :, 4])
+    np.testing.assert_array_equal(r["u"][:, -1, 4], r["naccept"] - 1)

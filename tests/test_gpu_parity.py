@@ -520,3 +520,31 @@ def test_vern7_dense_output_is_7th_order(de, precision):
     assert err.max() <= 2.0, err.max()
     # most save points fall inside steps: the steps are far longer than 0.01
     assert g["naccept"].mean() < 30
+
+
+@pytest.mark.parametrize("alg", ["Tsit5", "Vern7", "Rodas5P"])
+def test_dense_solution_evaluation(de, alg):
+    """sol(t) on a dense solve (test/core.jl:51-58: u' = 1.01 u, u0 = 0.5,
+    sol(0.5) is a number > 0.5) is the method's own dense output: exactly the
+    value a saveat containing t stores (save points never change the steps),
+    within the tolerance of the exact solution."""
+    prob = de.ODEProblem(de.models.linear, 0.5, (0.0, 1.0), [1.01])
+    a = getattr(de, alg)()
+    sol = de.solve(prob, a, de.EnsembleGB300(), dense=True, reltol=1e-8, abstol=1e-8)
+    assert sol.retcode == de.ReturnCode.Success
+    assert list(sol.t) == [0.0, 1.0]  # the end points are stored
+    v = sol(0.5)
+    assert v.shape == (1,) and v[0] > 0.5
+    ts = np.array([0.73, 0.1, 0.5])
+    vs = sol(ts)
+    ref = de.solve(prob, a, de.EnsembleGB300(), saveat=np.sort(ts), reltol=1e-8, abstol=1e-8)
+    order = np.argsort(ts)
+    assert np.array_equal(vs[order, 0], np.array([u[0] for u in ref.u]))
+    assert np.allclose(vs[:, 0], 0.5 * np.exp(1.01 * ts), rtol=1e-6, atol=0)
+    with pytest.raises(ValueError):
+        sol(1.5)
+    # an ensemble member's dense output
+    ens = de.EnsembleProblem(prob, prob_func=lambda pr, i, rep: de.remake(pr, u0=0.5 + 0.1 * i))
+    es = de.solve(ens, a, de.EnsembleGB300(), trajectories=4, dense=True, reltol=1e-8,
+                  abstol=1e-8)
+    assert np.allclose(es[3](0.25), 0.8 * np.exp(1.01 * 0.25), rtol=1e-6)
