@@ -295,8 +295,9 @@ __global__ void __launch_bounds__(128) k_init_dt(const KArgs a, double* __restri
 // earliest root is the event.  The integrator moves to the left side of the
 // root (the reference's LeftRootFind default), applies affect idx and restarts
 // the method there.  Save points up to the event use the step's dense output.
-// The next step looks for crossings only after 1% of its length (the
-// reference's repeat_nudge), so a root is not found twice.
+// For the condition that fired, the next step looks for crossings only after
+// 1% of its length (the reference's repeat_nudge), so a root is not found
+// twice; the other conditions start from their values after the affect.
 // Discrete: after an accepted step each condition k that is true applies its
 // affect, in order, on the state the previous ones left.
 struct NoCallback {
@@ -382,7 +383,7 @@ template <class Alg, class M, class T, bool MIXED, class CB = NoCallback>
 __device__ void integrate_all(const KArgs& a) {
   constexpr int N = M::N;
   double gprev[CB::NC > 0 ? CB::NC : 1];  // continuous conditions at the current point
-  bool nudge = false;     // an event ended the previous step (repeat nudge)
+  int nudge = -1;  // condition whose event ended the previous step (repeat nudge), or -1
   WorkSource src;
   src.init();
   Alg alg;
@@ -449,7 +450,7 @@ __device__ void integrate_all(const KArgs& a) {
         else if (!(dt > 0.0)) ret = GBDE_RET_DTLESSTHANMIN;
         if constexpr (CB::NC > 0) {
           cb_conditions<CB, N, M::NP>(alg.u(), t, p, gprev);
-          nudge = false;
+          nudge = -1;
         }
       }
       active = true;
@@ -508,21 +509,25 @@ __device__ void integrate_all(const KArgs& a) {
           step_end(tnew, tlo);
         }
         // continuous callbacks: crossings of the conditions in (t, tnew]
-        // (after the repeat nudge when the previous step ended at an event);
-        // the earliest located root is the event
+        // (for the condition that fired at t, in (t + h/100, tnew]: the
+        // repeat nudge); the earliest located root is the event
         bool event = false;
         double th_e = 1.0;
         int idx_e = 0;
         if constexpr (CB::NC > 0) {
-          double ga[CB::NC], gb[CB::NC], lo = 0.0;
+          double ga[CB::NC], gb[CB::NC];
 #pragma unroll
           for (int c = 0; c < CB::NC; ++c) ga[c] = gprev[c];
-          if (nudge) {
+          const int nudged = nudge;
+          if (nudged >= 0) {
             T un[N];
-            lo = 0.01;
-            alg.interp(lo, h, un, p, nfev);
-            cb_conditions<CB, N, M::NP>(un, t + lo * h, p, ga);
-            nudge = false;
+            double gn[CB::NC];
+            alg.interp(0.01, h, un, p, nfev);
+            cb_conditions<CB, N, M::NP>(un, t + 0.01 * h, p, gn);
+#pragma unroll
+            for (int c = 0; c < CB::NC; ++c)
+              if (c == nudged) ga[c] = gn[c];
+            nudge = -1;
           }
           cb_conditions<CB, N, M::NP>(alg.unew(), tnew, p, gb);
 #pragma unroll 1
@@ -530,6 +535,7 @@ __device__ void integrate_all(const KArgs& a) {
             if (!cb_crossed(ga[ci], gb[ci])) continue;
             // Illinois regula falsi on theta in [lo, 1] for condition ci; the
             // left end keeps the sign before the crossing
+            const double lo = ci == nudged ? 0.01 : 0.0;
             double a0 = lo, b0 = 1.0, fa = ga[ci], fb = gb[ci];
             int side = 0;
             for (int it = 0; it < 100; ++it) {
@@ -594,7 +600,8 @@ __device__ void integrate_all(const KArgs& a) {
           alg.init(ue, p, nfev);
           t = te;
           tlo = 0.0;
-          nudge = true;
+          nudge = idx_e;
+          cb_conditions<CB, N, M::NP>(alg.u(), t, p, gprev);
           if (nacc == 0) dt1 = th_e * h;
           ++nacc;
           bool fin = true;
@@ -620,6 +627,7 @@ __device__ void integrate_all(const KArgs& a) {
             bool term = false;
             if (fin && cb_discrete<CB, N, M::NP>(uc, t, p, term)) {
               alg.init(uc, p, nfev);
+              if constexpr (CB::NC > 0) cb_conditions<CB, N, M::NP>(alg.u(), t, p, gprev);
               if (term) ret = GBDE_RET_TERMINATED;
             }
           }

@@ -137,14 +137,28 @@ struct TeamLU {
       piv |= (uint64_t)p << (4 * k);
       const double* prow = team_lu_row_of(p);
       const double inv = rcp64(prow[k]);
+      bool upd = false;
       if (tm.lane == p) {
         step = k;
         invp = inv;
       } else if (step < 0) {
         const double l = ak * inv;
         a[k] = l;
-#pragma unroll 3
-        for (int c = k + 1; c < TEAM; ++c) a[c] = fma(-l, prow[c], a[c]);
+        upd = l != 0.0;
+      }
+      // Rank-1 update of the rows with a nonzero multiplier (on the ring's W,
+      // 2-3 of up to 15 per step), column-parallel: lane c updates entry c
+      // of each such row.  Every updated entry gets the same fma as a
+      // row-by-row update; the skipped rows would add -0 * prow[c], which
+      // leaves a finite entry unchanged.
+      unsigned rows = __ballot_sync(tm.mask, upd) >> ((threadIdx.x & 31) & TEAM);
+      rows &= 0xFFFFu;
+      __syncwarp(tm.mask);  // the multipliers are in shared memory
+      const double pc = prow[tm.lane];
+#pragma unroll 1
+      for (; rows != 0u; rows &= rows - 1u) {
+        double* ar = team_lu_row_of(__ffs(rows) - 1);
+        if (tm.lane > k) ar[tm.lane] = fma(-ar[k], pc, ar[tm.lane]);
       }
       __syncwarp(tm.mask);  // step k's updates land before step k+1 reads them
     }
