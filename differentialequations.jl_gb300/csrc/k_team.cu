@@ -24,6 +24,9 @@ template <class M, class Tag> struct TeamMinBlocks<TeamRodasFF<M, Tag>> {
 template <class M, class T> struct TeamMinBlocks<TeamTsit5P<M, T>> {
   static constexpr int v = 6;
 };
+template <class M> struct TeamMinBlocks<TeamTsit5FF<M>> {
+  static constexpr int v = 6;
+};
 
 template <class Alg, class M, class T, bool MIXED>
 __global__ void __launch_bounds__(128, TeamMinBlocks<Alg>::v) k_team(const KArgs a) {
@@ -61,7 +64,7 @@ cudaError_t launch_team(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
       if (cfg.precision == GBDE_PREC_MIXED)
         return launch_team_kernel(k_team8<TeamTsit5P<M, float>, M, float, true>, cfg, a, s, 8);
       if (cfg.precision == GBDE_PREC_F32X2)
-        return launch_team_kernel(k_team8<TeamTsit5P<M, ff>, M, ff, true>, cfg, a, s, 8);
+        return launch_team_kernel(k_team8<TeamTsit5FF<M>, M, ff, true>, cfg, a, s, 8);
       return launch_team_kernel(k_team8<TeamTsit5P<M, double>, M, double, false>, cfg, a, s, 8);
     case GBDE_ALG_RODAS5: return dispatch_prec<TeamRodas5, M>(cfg, a, s);
     case GBDE_ALG_RODAS5P: return dispatch_prec<TeamRodas5P, M>(cfg, a, s);

@@ -21,6 +21,7 @@
 #include "rosenbrock.cuh"
 #include "explicit_rk.cuh"
 #include "rodas_ff.cuh"
+#include "tsit5_ff.cuh"
 
 namespace gbde {
 
@@ -724,6 +725,153 @@ struct TeamTsit5P {
     for (int c = 0; c < 2; ++c) {
       uu[c] = un[c];
       if constexpr (CMP) lo[c] = lon[c];
+      k1[c] = k7[c];
+    }
+  }
+};
+
+// The FP32-pair form of TeamTsit5P: a lane's two components are one paired
+// FP32 register (FfVec<2>), so every stage argument, the new state, the error
+// estimate and the dense output are one unnormalised accumulation of paired
+// instructions over the pre-scaled stages h k_j (as Tsit5FF, tsit5_ff.cuh);
+// the norm's ratios are FP32 on the leading parts, their squares FP64.
+template <class M>
+struct TeamTsit5FF {
+  using T = ff;
+  static constexpr int ORDER = 5, ALG_ID = GBDE_ALG_TSIT5;
+  static_assert(M::N == 2 * TEAM8, "8-lane teams are for 16-state models");
+  ff uu[2], un[2], k1[2], k7[2];
+  FfVec<2> hk[7];  // h k_j of the current attempt
+
+  GBDE_D const ff* u() const { return uu; }
+  GBDE_D const ff* unew() const { return un; }
+  GBDE_D const ff* f0() const { return k1; }
+  GBDE_D void rhs(const ff* y, const ff* p, const Team8& tm, ff* dy) const {
+    M::f_osc(tm.lane, y, p, tm, dy);
+  }
+
+  GBDE_D void init(const ff* u0, const ff* p, const Team8& tm, int& nf) {
+    uu[0] = u0[0];
+    uu[1] = u0[1];
+    rhs(uu, p, tm, k1);
+    ++nf;
+  }
+
+  GBDE_D double attempt(double dt, const ff* p, double abstol, double reltol, const Team8& tm,
+                        int& nf) {
+    using namespace tab::tsit5;
+    constexpr ff A21 = ff(a21);
+    constexpr ff A31 = ff(a31), A32 = ff(a32);
+    constexpr ff A41 = ff(a41), A42 = ff(a42), A43 = ff(a43);
+    constexpr ff A51 = ff(a51), A52 = ff(a52), A53 = ff(a53), A54 = ff(a54);
+    constexpr ff A61 = ff(a61), A62 = ff(a62), A63 = ff(a63), A64 = ff(a64), A65 = ff(a65);
+    constexpr ff A71 = ff(a71), A72 = ff(a72), A73 = ff(a73), A74 = ff(a74), A75 = ff(a75),
+                 A76 = ff(a76);
+    constexpr ff E1 = ff(bt1), E2 = ff(bt2), E3 = ff(bt3), E4 = ff(bt4), E5 = ff(bt5),
+                 E6 = ff(bt6), E7 = ff(bt7);
+    const ff h = ff_split(dt);
+    FfVec<2> uv;
+    uv.from(uu);
+    ff y[2], k[2];
+    FfVecAcc<2> a;
+    hk[0] = ff_scale<2>(h, k1);
+    a.set(uv);
+    a.fma(A21, hk[0]);
+    a.get(y);
+    rhs(y, p, tm, k);
+    hk[1] = ff_scale<2>(h, k);
+    a.set(uv);
+    a.fma(A31, hk[0]);
+    a.fma(A32, hk[1]);
+    a.get(y);
+    rhs(y, p, tm, k);
+    hk[2] = ff_scale<2>(h, k);
+    a.set(uv);
+    a.fma(A41, hk[0]);
+    a.fma(A42, hk[1]);
+    a.fma(A43, hk[2]);
+    a.get(y);
+    rhs(y, p, tm, k);
+    hk[3] = ff_scale<2>(h, k);
+    a.set(uv);
+    a.fma(A51, hk[0]);
+    a.fma(A52, hk[1]);
+    a.fma(A53, hk[2]);
+    a.fma(A54, hk[3]);
+    a.get(y);
+    rhs(y, p, tm, k);
+    hk[4] = ff_scale<2>(h, k);
+    a.set(uv);
+    a.fma(A61, hk[0]);
+    a.fma(A62, hk[1]);
+    a.fma(A63, hk[2]);
+    a.fma(A64, hk[3]);
+    a.fma(A65, hk[4]);
+    a.get(y);
+    rhs(y, p, tm, k);
+    hk[5] = ff_scale<2>(h, k);
+    a.set(uv);
+    a.fma(A71, hk[0]);
+    a.fma(A72, hk[1]);
+    a.fma(A73, hk[2]);
+    a.fma(A74, hk[3]);
+    a.fma(A75, hk[4]);
+    a.fma(A76, hk[5]);
+    a.get(un);
+    rhs(un, p, tm, k7);
+    hk[6] = ff_scale<2>(h, k7);
+    nf += 6;
+    ff err[2];
+    a.zero();
+    a.fma(E1, hk[0]);
+    a.fma(E2, hk[1]);
+    a.fma(E3, hk[2]);
+    a.fma(E4, hk[3]);
+    a.fma(E5, hk[4]);
+    a.fma(E6, hk[5]);
+    a.fma(E7, hk[6]);
+    a.get(err);
+    const ff as = ff_split(abstol), rs = ff_split(reltol);
+    const float atf = xadd(as.hi, as.lo), rtf = xadd(rs.hi, rs.lo);
+    double e2 = 0.0;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const float m = fmaxf(fabsf(uu[c].hi), fabsf(un[c].hi));
+      const double ed = f2d_bits(__fdiv_rn(err[c].hi, fmaf(rtf, m, atf)));
+      e2 = fma(ed, ed, e2);
+    }
+    return tm.sum(e2) * (1.0 / M::N);
+  }
+
+  // Tsit5's interpolation polynomials in pair arithmetic (as Tsit5FF::interp)
+  GBDE_D void interp(double th, double, ff* out) const {
+    using namespace tab::tsit5;
+    constexpr ff R11 = ff(r11), R12 = ff(r12), R13 = ff(r13), R14 = ff(r14);
+    constexpr ff R21 = ff(r21), R22 = ff(r22), R23 = ff(r23);
+    constexpr ff R31 = ff(r31), R32 = ff(r32), R33 = ff(r33);
+    constexpr ff R41 = ff(r41), R42 = ff(r42), R43 = ff(r43);
+    constexpr ff R51 = ff(r51), R52 = ff(r52), R53 = ff(r53);
+    constexpr ff R61 = ff(r61), R62 = ff(r62), R63 = ff(r63);
+    constexpr ff R71 = ff(r71), R72 = ff(r72), R73 = ff(r73);
+    const ff t = ff_split(th), t2 = t * t;
+    FfVec<2> uv;
+    uv.from(uu);
+    FfVecAcc<2> a;
+    a.set(uv);
+    a.fma(R11 * t * (t - R12) * (t2 - R13 * t + R14), hk[0]);
+    a.fma(R21 * t2 * (t2 - R22 * t + R23), hk[1]);
+    a.fma(R31 * t2 * (t2 - R32 * t + R33), hk[2]);
+    a.fma(R41 * (t - R42) * (t - R43) * t2, hk[3]);
+    a.fma(R51 * (t - R52) * (t - R53) * t2, hk[4]);
+    a.fma(R61 * (t - R62) * (t - R63) * t2, hk[5]);
+    a.fma(R71 * (t - R72) * (t - R73) * t2, hk[6]);
+    a.get(out);
+  }
+
+  GBDE_D void accept() {
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      uu[c] = un[c];
       k1[c] = k7[c];
     }
   }
