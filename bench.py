@@ -47,12 +47,15 @@ FLOPS = {
     ("tsit5", "lorenz"): (272.0, 0.0, 85.0),
 }
 
-# FP64 work of one attempted step of the 16-lane Rodas5 on the 16-state ring
-# that stays FP64 in every precision (FMA = 2 flops): the LU of W with partial
-# pivoting, sum over k < 16 of (15 - k) (1 + 2 (15 - k)) = 2,600 flops; W's
-# diagonal 1/(gamma h) - J_rr, 16; the Jacobian rows, 8 x 6 = 48; the error
-# norm's scales, ratios and squares, 16 x 6 = 96.
-TEAM_RODAS_FP64_PER_ATTEMPT = 2600.0 + 16.0 + 48.0 + 96.0
+# FP64 work of one attempted step of Rodas5 on the 16-state ring that stays
+# FP64 in every precision (FMA = 2 flops).  The LU of W with partial pivoting:
+# on the ring's W the elimination has 34 nonzero multipliers and 297 updated
+# row entries whatever the values (a structural constant, checked on 3,000
+# random ring matrices), so 34 + 2 x 297 + 16 pivot reciprocals = 644 flops
+# (the dense count, 2,600, multiplies mostly zeros); W's diagonal
+# 1/(gamma h) - J_rr, 16; the Jacobian rows, 8 x 9 = 72; the error norm's
+# squares, 16 x 2 = 32.
+TEAM_RODAS_FP64_PER_ATTEMPT = 644.0 + 16.0 + 72.0 + 32.0
 
 # DRAM bytes (read + write) per trajectory of the Rodas5 solve kernel, from one
 # ncu capture each, scaled by trajectories.  FP64 stepper: 20,000 trajectories,
@@ -406,7 +409,7 @@ def run_vdp(args, de):
     host_out = {"u": torch.empty((N, S, 16), dtype=torch.float32 if odt(chosen) == "f32"
                                  else torch.float64).pin_memory().numpy(),
                 "retcode": torch.empty(N, dtype=torch.int32).pin_memory().numpy()}
-    # the dominant kernel alone: the stiff trajectories' 16-lane Rodas5
+    # the dominant kernel alone: the stiff trajectories' Rodas5
     st_prec = capi.PREC_FP64 if VDP_FORMS[chosen][0] == "PREC_FP64" else capi.PREC_F32X2
     o_st = opts(chosen, capi.ALG_RODAS5)
     o_st.precision = st_prec
@@ -497,9 +500,9 @@ def run_vdp(args, de):
                    "l2": "flushed between timed steps (256 MB write); output 1.34 GB > L2",
                    "parallelism": "trajectory shards, no collective" if world > 1
                    else "single GPU"},
-        "chosen_form": {"persistent-f32x2": "persistent queue; 16-lane Tsit5 and Rodas5 in FP32 "
-                        "pairs with an FP64 Jacobian, LU, error norm and compensated time; FP32 "
-                        "output",
+        "chosen_form": {"persistent-f32x2": "persistent queue; Tsit5 and Rodas5 on 8-lane teams "
+                        "in FP32 pairs (paired FP32 instructions) with an FP64 Jacobian, LU, "
+                        "error-norm accumulation and compensated time; FP32 output",
                         "persistent-mixed": "persistent queue; Tsit5 FP32 compensated state, "
                         "Rodas5 FP32 pairs on an FP64 LU; FP32 output",
                         "persistent": "persistent queue, FP64", "plain": "one launch, FP64"}[chosen],
@@ -510,15 +513,15 @@ def run_vdp(args, de):
         "accuracy": acc,
         "e2e": {"value": total / (e2e_ms * 1e-3), "unit": "trajectories/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "fp64", "kernel": "k_team<TeamRodasFF<VdpRing8,Rodas5>> (stiff "
+        "roofline": {"bound": "fp64", "kernel": "k_team8<TeamRodasFF8<VdpRing8,Rodas5>> (stiff "
                      "trajectories)" if st_prec == capi.PREC_F32X2 else
                      "k_team<TeamRodas<VdpRing8,double,Rodas5>> (stiff trajectories)",
                      "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
                      "frac": achieved / peak64,
-                     "basis": "FP64 work that stays FP64 in every precision (LU of W, W's "
-                              "diagonal, Jacobian rows, error norm: %d flops per attempted "
-                              "step) x the oracle's attempted steps, over the kernel's time on "
-                              "the stiff trajectories alone (CUDA events, median)"
+                     "basis": "FP64 work that stays FP64 in every precision (sparse LU of W, "
+                              "W's diagonal, Jacobian rows, error-norm squares: %d flops per "
+                              "attempted step) x the oracle's attempted steps, over the kernel's "
+                              "time on the stiff trajectories alone (CUDA events, median)"
                               % TEAM_RODAS_FP64_PER_ATTEMPT,
                      "kernel_ms": stiff_ms, "stiff_trajectories": int(len(st_idx)),
                      "share_of_step": stiff_ms / chosen_ms,

@@ -134,6 +134,27 @@ struct VdpRing8 {
     dy[0] = v;
     dy[1] = p[0] * (T(1) - x * x) * v - x + p[1] * (xl - T(2) * x + xr);
   }
+  // 8-lane teams: rows 2l and 2l + 1 of W = dg I - J at lane l's oscillator
+  // (x, v) = (y[0], y[1]), written to w0[0..16), w1[0..16): the nonzeros of
+  // jac_lane's rows 2l (x_l' = v_l) and 2l + 1 (v_l'), same arithmetic,
+  // negated, dg added on the diagonal; every other entry 0.
+  template <class T>
+  GBDE_D static void w_osc(int l, const T* y, const T* p, T dg, T* w0, T* w1) {
+    const T mu = p[0], ka = p[1], x = y[0], v = y[1];
+    const int e = 2 * l;
+    const T dx = T(-2) * mu * x * v - T(1) - T(2) * ka, dvv = mu * (T(1) - x * x);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      w0[c] = T(0);
+      w1[c] = T(0);
+    }
+    w0[e] = dg;
+    w0[e + 1] = T(-1);
+    w1[e] = -dx;
+    w1[e + 1] = dg - dvv;
+    w1[(e + 14) & 15] = -ka;
+    w1[(e + 2) & 15] = -ka;
+  }
   template <class T, class Sh>
   GBDE_D static void jac_lane(int r, T y, const T* p, const Sh& sh, T* Jr) {
     T x, v, xl, xr;

@@ -187,55 +187,6 @@ struct TeamLU {
   }
 };
 
-// The factors of a TeamLU as pairs for the FP32-pair stepper: this lane's
-// row negated (multipliers and U entries), written as pairs over the FP64 row
-// in shared memory (same 8 bytes per entry), and its pivot reciprocal, split
-// on the integer pipe.  The substitutions run in pair arithmetic in the same
-// order as TeamLU::solve; the value each step broadcasts is renormalised
-// first, the lane's own row sum is carried unnormalised (FfAcc).
-struct TeamLUFF {
-  ff invp;
-  int step;
-  uint64_t piv;
-
-  GBDE_D static float2* rowp() { return reinterpret_cast<float2*>(team_lu_row()); }
-
-  GBDE_D void from(const TeamLU& W) {
-    double* a = team_lu_row();
-    float2* na = rowp();
-#pragma unroll 4
-    for (int c = 0; c < TEAM; ++c) {
-      const ff x = ff_split(-a[c]);
-      na[c] = make_float2(x.hi, x.lo);
-    }
-    invp = ff_split(W.invp);
-    step = W.step;
-    piv = W.piv;
-  }
-  GBDE_D int pivot_lane(int k) const { return (int)((piv >> (4 * k)) & 15u); }
-
-  GBDE_D ff solve(ff b, const Team& tm) const {
-    const float2* na = rowp();
-    FfAcc acc;
-    acc.set(b);
-#pragma unroll 4
-    for (int k = 0; k < TEAM; ++k) {  // forward: L z = P b
-      const ff z = tm.bcast(acc.get(), pivot_lane(k));
-      const float2 v = na[k];
-      if (step > k) acc.fma(ff(v.x, v.y), z);
-    }
-    ff x(0.0f, 0.0f);
-#pragma unroll 4
-    for (int k = TEAM - 1; k >= 0; --k) {  // backward: U x = z
-      const ff xk = tm.bcast(acc.get() * invp, pivot_lane(k));
-      const float2 v = na[k];
-      if (step < k) acc.fma(ff(v.x, v.y), xk);
-      if (tm.lane == k) x = xk;
-    }
-    return x;
-  }
-};
-
 // ------------------------------------------------ team Rodas5 / Rodas5P
 // Same transformed form as RodasAlg (rosenbrock.cuh), one component per lane.
 template <class M, class T, class Tag>
@@ -317,140 +268,6 @@ struct TeamRodas {
 #undef GBDE_RODAS_E
     return uu + (T)th * (un - uu) + (e[0] * s1 + e[1] * s2 + e[2] * s3 + e[3] * s4 + e[4] * s5 +
                                      e[5] * s6 + e[6] * s7);
-  }
-
-  GBDE_D void accept() {
-    uu = un;
-    fresh = false;
-  }
-};
-
-// ------------------------------------ team Rodas5 / Rodas5P in FP32 pairs
-// TeamRodas with the F32X2 split of work (as RodasFF, rodas_ff.cuh): the
-// Jacobian row, W and its row-distributed LU, and the error norm stay FP64;
-// the state, the stages, the right-hand sides, the stage combinations, the
-// eight triangular solves (TeamLUFF) and the dense output run in FP32 pairs.
-// As in RodasFF the step body is compact: the stage loop is not unrolled, so
-// the pair solve (32 unrolled broadcast-and-update steps) has one call site,
-// the transformed stages live in shared memory and the coefficients come from
-// the constant table.  With the eight solves inlined the kernel's top stall
-// was an empty instruction cache.
-template <class M, class Tag>
-struct TeamRodasFF {
-  using K = RodasCoef<Tag>;
-  using T = ff;
-  static constexpr int ORDER = 4, ALG_ID = K::ALG_ID;
-  static_assert(M::N == TEAM, "team kernels are for 16-state models");
-  ff uu, un, F0;
-  double pd[M::NP];
-  bool fresh;
-
-  GBDE_D ff u() const { return uu; }
-  GBDE_D ff unew() const { return un; }
-  GBDE_D ff f0() const { return F0; }
-
-  // stages u_1..u_7 of this lane's component, at stride kFfStageThreads
-  GBDE_D static float2* stage_buf() {
-    __shared__ float2 buf[7 * kFfStageThreads];
-    return buf + threadIdx.x;
-  }
-  GBDE_D static ff ld(int j) {
-    const float2 v = stage_buf()[j * kFfStageThreads];
-    return ff(v.x, v.y);
-  }
-  GBDE_D static void st(int j, ff x) { stage_buf()[j * kFfStageThreads] = make_float2(x.hi, x.lo); }
-
-  GBDE_D ff rhs(ff y, const ff* p, const Team& tm) const { return M::f_lane(tm.lane, y, p, tm); }
-
-  GBDE_D void refresh(const ff* p, const Team& tm) {
-    F0 = M::f_lane(tm.lane, uu, p, tm);
-    fresh = true;
-  }
-
-  GBDE_D void init(ff u0, const ff* p, const Team& tm, int& nf) {
-#pragma unroll
-    for (int k = 0; k < M::NP; ++k) pd[k] = (double)p[k];
-    uu = u0;
-    refresh(p, tm);
-    ++nf;
-  }
-
-  GBDE_D double attempt(double dt, const ff* p, double abstol, double reltol, const Team& tm,
-                        int& nf) {
-    if (!fresh) {
-      refresh(p, tm);
-      ++nf;
-    }
-    TeamLUFF L;
-    const double ih = rcp64(dt);
-    {
-      TeamLU W;
-      const double dg = ih * (1.0 / K::g);
-      double Jr[TEAM];  // FP64 Jacobian row at uu, built on every attempt (as TeamRodas)
-      M::jac_lane(tm.lane, f2d_bits(uu.hi) + f2d_bits(uu.lo), pd, tm, Jr);
-      double* wr = team_lu_row();
-#pragma unroll
-      for (int c = 0; c < TEAM; ++c) wr[c] = c == tm.lane ? dg - Jr[c] : -Jr[c];
-      W.factor(tm);
-      L.from(W);
-    }
-    const ff iht = ff_split(ih);  // r_i = f(y_i) + (1/h) sum_j C_ij u_j
-    const RodasFfTab& tb = c_rodas_ff[RodasFfIdx<Tag>::v];
-    ff y = uu, s8;
-#pragma unroll 1
-    for (int i = 0; i < 8; ++i) {
-      ff r = F0;
-      if (i > 0) {
-        // stage argument: a fresh combination for stages 2-6; for 7 and 8 the
-        // previous argument plus the previous stage (a_7j = a_6j, a_76 = 1,
-        // a_8j = a_7j, a_87 = 1)
-        const bool fresh_arg = i <= 5;
-        FfAcc ya, ca;
-        ya.set(fresh_arg ? uu : y);
-        ca.set(ff(0.0f, 0.0f));
-#pragma unroll 1
-        for (int j = 0; j < i; ++j) {
-          const ff sj = ld(j);
-          if (fresh_arg) ya.fma(tb.ra[fresh_arg ? i : 0][j], sj);
-          else if (j == i - 1) ya.add(sj);
-          ca.fma(tb.rc[i][j], sj);
-        }
-        y = ya.get();
-        FfAcc ra;
-        ra.set(rhs(y, p, tm));
-        ra.fma(iht, ca.get());
-        r = ra.get();
-      }
-      const ff x = L.solve(r, tm);
-      if (i < 7) st(i, x);
-      else s8 = x;
-    }
-    nf += 7;
-    un = y + s8;
-    const float m = fmaxf(fabsf(uu.hi), fabsf(un.hi));
-    const double e = f2d_bits(s8.hi) * rcp64(abstol + reltol * f2d_bits(m));
-    return tm.sum(e * e) * (1.0 / TEAM);
-  }
-
-  // as RodasFF::interp, one component per lane
-  GBDE_D ff interp(double th, double) const {
-    const RodasFfTab& tb = c_rodas_ff[RodasFfIdx<Tag>::v];
-    const ff tt = ff_split(th);
-    const ff w = tt * (ff(1.0f, 0.0f) - tt);
-    FfAcc a;
-    a.set(uu);
-    a.fma(tt, un - uu);
-#pragma unroll 1
-    for (int j = 0; j < 7; ++j) {
-      FfAcc q;
-      q.set(tb.h3[j]);
-      q.fma(tt, tb.h4[j]);
-      const ff q3 = q.get();
-      q.set(tb.h2[j]);
-      q.fma(tt, q3);
-      a.fma(w * q.get(), ld(j));
-    }
-    return a.get();
   }
 
   GBDE_D void accept() {
@@ -874,6 +691,349 @@ struct TeamTsit5FF {
       uu[c] = un[c];
       k1[c] = k7[c];
     }
+  }
+};
+
+// ---------------------------------------- 8-lane Rodas (two rows per lane)
+// The 16-state ring's stiff trajectories on teams of 8 lanes: lane l owns rows
+// 2l and 2l + 1 of W (its oscillator's x and v rows) and components 2l, 2l + 1
+// of every stage, so a warp carries 4 trajectories and the pair arithmetic of
+// a lane's two components runs on paired FP32 instructions (FfAcc2, FfVec<2>).
+// Same method, pivot order and FP64 factorisation as TeamLU / TeamRodas.
+constexpr int kTeam8Threads = 128;  // CTA size the shared arrays are sized for
+
+// W of this team: 16 rows of 17 doubles (the stride keeps a team's row
+// accesses conflict-free).  16 teams per CTA: 34,816 bytes.  Row i sits in
+// slot i at even team positions and in slot i + 1 (mod 16) at odd ones: the
+// two teams of a half-warp then read their rows at the same column through
+// disjoint banks (an even team at word offsets 4l + 2k (mod 32) for lane l,
+// column k; an odd one at 4l + 2k + 2).
+GBDE_D double* team8_row(int i) {
+  __shared__ double rows[kTeam8Threads / TEAM8 * TEAM * kTeamLuStride];
+  const int t = threadIdx.x / TEAM8;
+  return rows + (t * TEAM + ((i + (t & 1)) & (TEAM - 1))) * kTeamLuStride;
+}
+
+struct TeamLU8 {
+  double invp[2];  // 1 / pivot of this lane's rows
+  int step[2];     // elimination step at which each of them was the pivot
+  uint64_t piv;    // pivot row of step k in bits [4k, 4k+4)
+
+  // LU with partial pivoting of the W written into team8_row(): the
+  // pivot of step k is the unpivoted row with the largest |a_k|, ties to the
+  // lowest row position of the row-swapping LU (LAPACK getrf's order, as
+  // TeamLU); the rank-1 update runs column-parallel over the rows with a
+  // nonzero multiplier (lane l updates columns l and l + 8).
+  GBDE_D void factor(const Team8& tm) {
+    const int r0 = 2 * tm.lane, r1 = r0 + 1;
+    double* a0 = team8_row(r0);
+    double* a1 = team8_row(r1);
+    step[0] = step[1] = -1;
+    invp[0] = invp[1] = 0.0;
+    piv = 0;
+    unsigned pos0 = (unsigned)r0, pos1 = (unsigned)r1;
+    const unsigned sh = (threadIdx.x & 31) & 24;  // the team's first lane in the warp
+    __syncwarp(tm.mask);  // every lane's rows are written
+#pragma unroll 1
+    for (int k = 0; k < TEAM; ++k) {
+      const double ak0 = a0[k], ak1 = a1[k];
+      const uint64_t key0 = step[0] < 0 ? mag_bits(ak0) + 1ull : 0ull;
+      const uint64_t key1 = step[1] < 0 ? mag_bits(ak1) + 1ull : 0ull;
+      uint64_t m = key0 > key1 ? key0 : key1;
+#pragma unroll
+      for (int o = TEAM8 / 2; o > 0; o >>= 1) {
+        const uint64_t x = __shfl_xor_sync(tm.mask, m, o, TEAM8);
+        m = x > m ? x : m;
+      }
+      // ties: the lowest position; (position, row) packed, positions unique
+      unsigned pk = min(key0 == m ? (pos0 << 4) | (unsigned)r0 : 0xFFFFFFFFu,
+                        key1 == m ? (pos1 << 4) | (unsigned)r1 : 0xFFFFFFFFu);
+#pragma unroll
+      for (int o = TEAM8 / 2; o > 0; o >>= 1) pk = min(pk, __shfl_xor_sync(tm.mask, pk, o, TEAM8));
+      const unsigned ppos = pk >> 4;
+      const int p = (int)(pk & 15u);
+      if (step[0] < 0 && pos0 == (unsigned)k && r0 != p) pos0 = ppos;  // swapped out
+      if (step[1] < 0 && pos1 == (unsigned)k && r1 != p) pos1 = ppos;
+      piv |= (uint64_t)p << (4 * k);
+      const double* prow = team8_row(p);
+      const double inv = rcp64(prow[k]);
+      bool u0 = false, u1 = false;
+      if (r0 == p) {
+        step[0] = k;
+        invp[0] = inv;
+      } else if (step[0] < 0) {
+        const double l = ak0 * inv;
+        a0[k] = l;
+        u0 = l != 0.0;
+      }
+      if (r1 == p) {
+        step[1] = k;
+        invp[1] = inv;
+      } else if (step[1] < 0) {
+        const double l = ak1 * inv;
+        a1[k] = l;
+        u1 = l != 0.0;
+      }
+      const unsigned b0 = (__ballot_sync(tm.mask, u0) >> sh) & 0xFFu;  // rows 2j
+      const unsigned b1 = (__ballot_sync(tm.mask, u1) >> sh) & 0xFFu;  // rows 2j + 1
+      __syncwarp(tm.mask);  // the multipliers are in shared memory
+      const int ca = tm.lane, cb = tm.lane + TEAM8;
+      const double pa = prow[ca], pb = prow[cb];
+#pragma unroll 1
+      for (unsigned rows = b0 | (b1 << 8); rows != 0u; rows &= rows - 1u) {
+        const int j = __ffs(rows) - 1;
+        double* ar = team8_row(j < 8 ? 2 * j : 2 * (j - 8) + 1);
+        const double l = ar[k];
+        if (ca > k) ar[ca] = fma(-l, pa, ar[ca]);
+        if (cb > k) ar[cb] = fma(-l, pb, ar[cb]);
+      }
+      __syncwarp(tm.mask);  // step k's updates land before step k+1 reads them
+    }
+  }
+};
+
+// The factors of a TeamLU8 as pairs for the solves: each lane's two rows
+// written as pairs over their FP64 entries in shared memory, and the pivot
+// reciprocals split on the integer pipe.  Forward and back substitution keep
+// a lane's two right-hand-side components in one paired accumulator and
+// subtract (broadcast value) x (factor entry).
+struct TeamLUFF8 {
+  ff invp[2];
+  int step[2];
+  uint64_t piv;
+
+  GBDE_D static float2* row_ff(int i) { return reinterpret_cast<float2*>(team8_row(i)); }
+  GBDE_D void from(const TeamLU8& W, const Team8& tm) {
+    double* a0 = team8_row(2 * tm.lane);
+    double* a1 = team8_row(2 * tm.lane + 1);
+    float2* n0 = reinterpret_cast<float2*>(a0);
+    float2* n1 = reinterpret_cast<float2*>(a1);
+#pragma unroll 4
+    for (int c = 0; c < TEAM; ++c) {
+      const ff x0 = ff_split(a0[c]), x1 = ff_split(a1[c]);
+      n0[c] = make_float2(x0.hi, x0.lo);
+      n1[c] = make_float2(x1.hi, x1.lo);
+    }
+    invp[0] = ff_split(W.invp[0]);
+    invp[1] = ff_split(W.invp[1]);
+    step[0] = W.step[0];
+    step[1] = W.step[1];
+    piv = W.piv;
+  }
+  // W x = b for this lane's components b[0], b[1] (rows 2l, 2l + 1); x[0],
+  // x[1] are unknowns 2l, 2l + 1.  A row that takes no update at step k
+  // (k outside its L or U part) adds a zero product.  The pivot rows are read
+  // off a running copy of piv (constant shifts).
+  GBDE_D void solve(const ff* b, ff* x, const Team8& tm) const {
+    const float2* n0 = row_ff(2 * tm.lane);
+    const float2* n1 = row_ff(2 * tm.lane + 1);
+    FfAcc2 acc;
+    acc.set(f2_pack(b[0].hi, b[1].hi), f2_pack(b[0].lo, b[1].lo));
+    uint64_t pv = piv;
+#pragma unroll 4
+    for (int k = 0; k < TEAM; ++k) {  // forward: L z = P b
+      const int p = (int)(pv & 15u);
+      pv >>= 4;
+      ff g0, g1;
+      acc.get(g0, g1);
+      const ff z = tm.bcast((p & 1) ? g1 : g0, p >> 1);
+      const float2 v0 = n0[k], v1 = n1[k];
+      const bool e0 = step[0] > k, e1 = step[1] > k;
+      acc.fma(f2_pack(-z.hi, -z.hi), f2_pack(-z.lo, -z.lo), f2_pack(z.hi, z.hi),
+              f2_pack(e0 ? v0.x : 0.0f, e1 ? v1.x : 0.0f),
+              f2_pack(e0 ? v0.y : 0.0f, e1 ? v1.y : 0.0f));
+    }
+    pv = piv;
+#pragma unroll 4
+    for (int k = TEAM - 1; k >= 0; --k) {  // backward: U x = z
+      const int p = (int)(pv >> 60);
+      pv <<= 4;
+      ff g0, g1;
+      acc.get(g0, g1);
+      const ff xk = tm.bcast(((p & 1) ? g1 : g0) * ((p & 1) ? invp[1] : invp[0]), p >> 1);
+      const float2 v0 = n0[k], v1 = n1[k];
+      const bool e0 = step[0] < k, e1 = step[1] < k;
+      acc.fma(f2_pack(-xk.hi, -xk.hi), f2_pack(-xk.lo, -xk.lo), f2_pack(xk.hi, xk.hi),
+              f2_pack(e0 ? v0.x : 0.0f, e1 ? v1.x : 0.0f),
+              f2_pack(e0 ? v0.y : 0.0f, e1 ? v1.y : 0.0f));
+      if (k == 2 * tm.lane) x[0] = xk;
+      if (k == 2 * tm.lane + 1) x[1] = xk;
+    }
+  }
+};
+
+// Rodas5 / Rodas5P in FP32 pairs on 8-lane teams (the method and arithmetic of
+// RodasFF, rodas_ff.cuh, for a lane's two components): FP64 Jacobian rows, W
+// and its LU (TeamLU8), pair solves (TeamLUFF8), stage sums and dense output
+// on paired FP32 instructions, the norm's ratios FP32, their squares FP64.
+template <class M, class Tag>
+struct TeamRodasFF8 {
+  using K = RodasCoef<Tag>;
+  using T = ff;
+  static constexpr int ORDER = 4, ALG_ID = K::ALG_ID;
+  static_assert(M::N == 2 * TEAM8, "8-lane teams are for 16-state models");
+  ff uu[2], un[2];
+  ff F0[2];  // f(u0): read only by the Hairer-Wanner starting step after init()
+  double pd[M::NP];
+  bool fresh;  // uu's f evaluation already counted
+
+  GBDE_D const ff* u() const { return uu; }
+  GBDE_D const ff* unew() const { return un; }
+  GBDE_D const ff* f0() const { return F0; }
+  GBDE_D void rhs(const ff* y, const ff* p, const Team8& tm, ff* dy) const {
+    M::f_osc(tm.lane, y, p, tm, dy);
+  }
+
+  // stages u_1..u_7 of this lane's two components: one 16-byte (hi pair, lo
+  // pair) slot per stage at stride kTeam8Threads (14,336 bytes per CTA)
+  GBDE_D static ulonglong2* stages() {
+    __shared__ ulonglong2 buf[7 * kTeam8Threads];
+    return buf + threadIdx.x;
+  }
+  GBDE_D static FfVec<2> ld(int j) {
+    const ulonglong2 x = stages()[j * kTeam8Threads];
+    FfVec<2> v;
+    v.h[0].v = x.x;
+    v.l[0].v = x.y;
+    return v;
+  }
+  GBDE_D static void st(int j, const ff* x) {
+    stages()[j * kTeam8Threads] =
+        make_ulonglong2(f2_pack(x[0].hi, x[1].hi).v, f2_pack(x[0].lo, x[1].lo).v);
+  }
+
+  GBDE_D void init(const ff* u0, const ff* p, const Team8& tm, int& nf) {
+#pragma unroll
+    for (int k = 0; k < M::NP; ++k) pd[k] = (double)p[k];
+    uu[0] = u0[0];
+    uu[1] = u0[1];
+    rhs(uu, p, tm, F0);
+    ++nf;
+    fresh = true;
+  }
+
+  GBDE_D double attempt(double dt, const ff* p, double abstol, double reltol, const Team8& tm,
+                        int& nf) {
+    if (!fresh) {
+      ++nf;
+      fresh = true;
+    }
+    TeamLUFF8 L;
+    {
+      // rows 2l, 2l + 1 of W = I/(h gamma) - J(uu), FP64
+      TeamLU8 W;
+      double ud[2];
+      ud[0] = f2d_bits(uu[0].hi) + f2d_bits(uu[0].lo);
+      ud[1] = f2d_bits(uu[1].hi) + f2d_bits(uu[1].lo);
+      M::w_osc(tm.lane, ud, pd, rcp64(dt) * (1.0 / K::g), team8_row(2 * tm.lane),
+               team8_row(2 * tm.lane + 1));
+      W.factor(tm);
+      L.from(W, tm);
+    }
+    const ff iht = ff_split(rcp64(dt));
+    const RodasFfTab& tb = c_rodas_ff[RodasFfIdx<Tag>::v];
+    FfVec<2> uv;
+    uv.from(uu);
+    ff y[2], s[2];
+#pragma unroll 1
+    for (int i = 0; i < 8; ++i) {
+      // stage argument: u0 for stage 1, a fresh combination for stages 2-6;
+      // for 7 and 8 the previous argument plus the previous stage
+      FfVecAcc<2> ya, ca;
+      const bool fresh_arg = i <= 5;
+      if (fresh_arg) {
+        ya.set(uv);
+      } else {
+        FfVec<2> yv;
+        yv.from(y);
+        ya.set(yv);
+      }
+      ca.zero();
+#pragma unroll 1
+      for (int j = 0; j < i; ++j) {
+        const ff cij = tb.rc[i][j];
+        const ff aij = tb.ra[fresh_arg ? i : 0][fresh_arg ? j : 0];
+        const FfVec<2> sj = ld(j);
+        if (fresh_arg) ya.fma(aij, sj);
+        else if (j == i - 1) ya.add(sj);
+        ca.fma(cij, sj);
+      }
+      ff fy[2], r[2];
+      ya.get(y);
+      rhs(y, p, tm, fy);
+      if (i > 0) {
+        ff cs[2];
+        ca.get(cs);
+        FfVec<2> fv, cv;
+        fv.from(fy);
+        cv.from(cs);
+        FfVecAcc<2> ra;
+        ra.set(fv);
+        ra.fma(iht, cv);
+        ra.get(r);
+      } else {
+        r[0] = fy[0];
+        r[1] = fy[1];
+      }
+      ff x[2];
+      L.solve(r, x, tm);
+      if (i < 7) {
+        st(i, x);
+      } else {
+        s[0] = x[0];
+        s[1] = x[1];
+      }
+    }
+    nf += 7;
+    // y1 = U_7 + u_8; error estimate u_8 (ratios FP32 on the leading parts,
+    // squares FP64, as RodasFF)
+    const ff as = ff_split(abstol), rs = ff_split(reltol);
+    const float atf = xadd(as.hi, as.lo), rtf = xadd(rs.hi, rs.lo);
+    double e2 = 0.0;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      FfAcc a;
+      a.set(y[c]);
+      a.add(s[c]);
+      un[c] = a.get();
+      const float m = fmaxf(fabsf(uu[c].hi), fabsf(un[c].hi));
+      const double e = f2d_bits(__fdiv_rn(s[c].hi, fmaf(rtf, m, atf)));
+      e2 = fma(e, e, e2);
+    }
+    return tm.sum(e2) * (1.0 / M::N);
+  }
+
+  // dense output as RodasFF::interp for the lane's two components
+  GBDE_D void interp(double th, double, ff* out) const {
+    const RodasFfTab& tb = c_rodas_ff[RodasFfIdx<Tag>::v];
+    const ff tt = ff_split(th);
+    const ff w = tt * (ff(1.0f, 0.0f) - tt);
+    ff du[2];
+    du[0] = un[0] - uu[0];
+    du[1] = un[1] - uu[1];
+    FfVec<2> uv, dv;
+    uv.from(uu);
+    dv.from(du);
+    FfVecAcc<2> a;
+    a.set(uv);
+    a.fma(tt, dv);
+#pragma unroll 1
+    for (int j = 0; j < 7; ++j) {
+      FfAcc q;
+      q.set(tb.h3[j]);
+      q.fma(tt, tb.h4[j]);
+      const ff q3 = q.get();
+      q.set(tb.h2[j]);
+      q.fma(tt, q3);
+      a.fma(w * q.get(), ld(j));
+    }
+    a.get(out);
+  }
+
+  GBDE_D void accept() {
+    uu[0] = un[0];
+    uu[1] = un[1];
+    fresh = false;
   }
 };
 
