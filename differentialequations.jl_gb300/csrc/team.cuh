@@ -758,13 +758,14 @@ struct TeamLU8 {
       const double* prow = team8_row(p);
       const double inv = rcp64(prow[k]);
       bool u0 = false, u1 = false;
+      // l != 0 tested on the integer pipe (magnitude bits)
       if (r0 == p) {
         step[0] = k;
         invp[0] = inv;
       } else if (step[0] < 0) {
         const double l = ak0 * inv;
         a0[k] = l;
-        u0 = l != 0.0;
+        u0 = mag_bits(l) != 0ull;
       }
       if (r1 == p) {
         step[1] = k;
@@ -772,7 +773,7 @@ struct TeamLU8 {
       } else if (step[1] < 0) {
         const double l = ak1 * inv;
         a1[k] = l;
-        u1 = l != 0.0;
+        u1 = mag_bits(l) != 0ull;
       }
       const unsigned b0 = (__ballot_sync(tm.mask, u0) >> sh) & 0xFFu;  // rows 2j
       const unsigned b1 = (__ballot_sync(tm.mask, u1) >> sh) & 0xFFu;  // rows 2j + 1
@@ -793,10 +794,9 @@ struct TeamLU8 {
 };
 
 // The factors of a TeamLU8 as pairs for the solves: each lane's two rows
-// written as pairs over their FP64 entries in shared memory, and the pivot
-// reciprocals split on the integer pipe.  Forward and back substitution keep
-// a lane's two right-hand-side components in one paired accumulator and
-// subtract (broadcast value) x (factor entry).
+// negated, written as pairs over their FP64 entries in shared memory, and the
+// pivot reciprocals split on the integer pipe.  Forward and back substitution
+// keep a lane's two right-hand-side components in one paired accumulator.
 struct TeamLUFF8 {
   ff invp[2];
   int step[2];
@@ -811,8 +811,8 @@ struct TeamLUFF8 {
 #pragma unroll 4
     for (int c = 0; c < TEAM; ++c) {
       const ff x0 = ff_split(a0[c]), x1 = ff_split(a1[c]);
-      n0[c] = make_float2(x0.hi, x0.lo);
-      n1[c] = make_float2(x1.hi, x1.lo);
+      n0[c] = make_float2(-x0.hi, -x0.lo);
+      n1[c] = make_float2(-x1.hi, -x1.lo);
     }
     invp[0] = ff_split(W.invp[0]);
     invp[1] = ff_split(W.invp[1]);
@@ -830,7 +830,7 @@ struct TeamLUFF8 {
     FfAcc2 acc;
     acc.set(f2_pack(b[0].hi, b[1].hi), f2_pack(b[0].lo, b[1].lo));
     uint64_t pv = piv;
-#pragma unroll 4
+#pragma unroll 4  // pair solve
     for (int k = 0; k < TEAM; ++k) {  // forward: L z = P b
       const int p = (int)(pv & 15u);
       pv >>= 4;
@@ -839,12 +839,12 @@ struct TeamLUFF8 {
       const ff z = tm.bcast((p & 1) ? g1 : g0, p >> 1);
       const float2 v0 = n0[k], v1 = n1[k];
       const bool e0 = step[0] > k, e1 = step[1] > k;
-      acc.fma(f2_pack(-z.hi, -z.hi), f2_pack(-z.lo, -z.lo), f2_pack(z.hi, z.hi),
+      acc.fma(f2_pack(z.hi, z.hi), f2_pack(z.lo, z.lo), f2_pack(-z.hi, -z.hi),
               f2_pack(e0 ? v0.x : 0.0f, e1 ? v1.x : 0.0f),
               f2_pack(e0 ? v0.y : 0.0f, e1 ? v1.y : 0.0f));
     }
     pv = piv;
-#pragma unroll 4
+#pragma unroll 4  // pair solve
     for (int k = TEAM - 1; k >= 0; --k) {  // backward: U x = z
       const int p = (int)(pv >> 60);
       pv <<= 4;
@@ -853,7 +853,7 @@ struct TeamLUFF8 {
       const ff xk = tm.bcast(((p & 1) ? g1 : g0) * ((p & 1) ? invp[1] : invp[0]), p >> 1);
       const float2 v0 = n0[k], v1 = n1[k];
       const bool e0 = step[0] < k, e1 = step[1] < k;
-      acc.fma(f2_pack(-xk.hi, -xk.hi), f2_pack(-xk.lo, -xk.lo), f2_pack(xk.hi, xk.hi),
+      acc.fma(f2_pack(xk.hi, xk.hi), f2_pack(xk.lo, xk.lo), f2_pack(-xk.hi, -xk.hi),
               f2_pack(e0 ? v0.x : 0.0f, e1 ? v1.x : 0.0f),
               f2_pack(e0 ? v0.y : 0.0f, e1 ? v1.y : 0.0f));
       if (k == 2 * tm.lane) x[0] = xk;
