@@ -66,6 +66,13 @@ TRAFFIC_PER_TRAJ = {"fp64": (4.586752e6 + 8192.0) / 20000.0,
                     "f32x2": (31.265536e6 + 9.635328e6) / 100000.0,
                     "f32x2-learned": (30.901504e6 + 8.447488e6) / 100000.0}
 
+# DRAM bytes (read + write) per stiff trajectory of the ring's Rodas5 kernel in
+# FP32 pairs (k_team8<TeamRodasFF8>), from one ncu capture at 400,000
+# trajectories of the ring workload (100,078 stiff; 1,263 bytes each against
+# ~1,536 bytes of inputs and outputs: the last saves are still in L2 when the
+# kernel ends), scaled by the launch's stiff trajectories.
+RING_STIFF_TRAFFIC_PER_TRAJ = (37.643264e6 + 88.761088e6) / 100078.0
+
 WORKLOADS = ["vdp_auto", "robertson", "lorenz", "lv_em", "lv_sosri", "summary",
              "learned_lorenz", "learned_lv", "learned_vdp"]
 DEFAULT_N = {"vdp_auto": 1000000, "robertson": 100000, "lorenz": 10000, "lv_em": 1000000,
@@ -526,7 +533,12 @@ def run_vdp(args, de):
                      "kernel_ms": stiff_ms, "stiff_trajectories": int(len(st_idx)),
                      "share_of_step": stiff_ms / chosen_ms,
                      "peak_source": "in-run FP64 FMA microbenchmark (gbde_measure_fma_peak)",
-                     "fp32_peak_tflops": peak32, "traffic": None},
+                     "fp32_peak_tflops": peak32,
+                     "traffic": RING_STIFF_TRAFFIC_PER_TRAJ * len(st_idx)
+                     if st_prec == capi.PREC_F32X2 else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
+                                       "k_team8<TeamRodasFF8> at 400,000 trajectories (100,078 "
+                                       "stiff), per stiff trajectory x this launch's"},
         "gpu_launches": K * 3,
         "clocks": clk.summary(),
         "step_ms_spread": {"chosen": spread(chosen_ts), "plain": spread(plain_ts),

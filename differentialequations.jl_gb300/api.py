@@ -13,10 +13,12 @@ Semantics kept from the reference's pinned tests (test/core.jl):
   * the first stored state equals u0 exactly (core.jl:34);
   * remake(prob; u0=...) changes u0 (core.jl:81-88);
   * a Robertson solve with Rodas5P to t=1e5 returns Success (core.jl:38-49).
-Callbacks (ContinuousCallback / DiscreteCallback, core.jl:60-79) take their
-condition and affect as CUDA C++ source compiled into the kernels.
-Unsupported solve keywords (dense=True, save_everystep=True, tstops,
-save_idxs) raise instead of silently changing behaviour.
+Callbacks (ContinuousCallback / DiscreteCallback, core.jl:60-79, and
+VectorContinuousCallback / CallbackSet, qa.jl:124,26) take their condition
+and affect as CUDA C++ source compiled into the kernels.  dense=True gives
+solutions callable at any t (sol(0.5), core.jl:51-58).  Unsupported solve
+keywords (save_everystep=True, tstops, save_idxs) raise instead of silently
+changing behaviour.
 """
 import copy
 import enum
