@@ -9,7 +9,7 @@ include/gbde.h); this package is the host-side mirror of the reference's
 SciMLBase interface over that ABI.
 """
 from . import _capi, learned, tuning
-from .api import (EM, SOSRI, SRIW1, CallbackSet, ContinuousCallback, DiscreteCallback,
+from .api import (EM, SOSRI, SRIW1, AutoTsit5, CallbackSet, ContinuousCallback, DiscreteCallback,
                   VectorContinuousCallback, EnsembleGB300, EnsembleProblem, EnsembleSerial,
                   EnsembleSolution, EnsembleThreads, ODEFunction, ODEProblem, ODESolution,
                   SDEFunction,
@@ -18,7 +18,7 @@ from .api import (EM, SOSRI, SRIW1, CallbackSet, ContinuousCallback, DiscreteCal
                   save_grid, solve, solve_arrays)
 
 __all__ = [
-    "EM", "SOSRI", "SRIW1", "CallbackSet", "ContinuousCallback", "DiscreteCallback",
+    "EM", "SOSRI", "SRIW1", "AutoTsit5", "CallbackSet", "ContinuousCallback", "DiscreteCallback",
     "VectorContinuousCallback", "EnsembleGB300", "EnsembleProblem", "EnsembleSerial", "EnsembleSolution",
     "EnsembleThreads", "ODEFunction", "SDEFunction", "ODEProblem", "ODESolution", "compile_model", "EnsembleSummary", "ensemble_summary",
     "ReturnCode", "Rodas5", "Rodas5P",

@@ -30,6 +30,7 @@ MODEL_USER_BASE, USER_MAX_STATE, USER_MAX_PARAM = 1000, 8, 32
 
 ALG_TSIT5, ALG_VERN7, ALG_ROSENBROCK23, ALG_RODAS5, ALG_RODAS5P = 1, 2, 3, 4, 5
 ALG_EM, ALG_SOSRI, ALG_AUTO, ALG_SRIW1 = 6, 7, 8, 9
+ALG_AUTOTSIT5_ROSENBROCK23, ALG_AUTOTSIT5_RODAS5 = 10, 11
 
 PREC_FP64, PREC_MIXED, PREC_F32X2 = 0, 1, 2
 BATCH_PLAIN, BATCH_PERSISTENT = 0, 1

@@ -290,6 +290,27 @@ class Rodas5P(_Alg):
     alg_id = capi.ALG_RODAS5P
 
 
+class AutoTsit5(_Alg):
+    """AutoTsit5(stiff_alg) (qa.jl:15): per trajectory, Tsit5 with a run-time
+    stiffness estimate that switches to stiff_alg (Rosenbrock23() or
+    Rodas5()) and back, with OrdinaryDiffEq's AutoSwitch defaults (10
+    successive stiff estimates to switch, 3 non-stiff ones to switch back,
+    tolerance 9/10, dt doubled / halved at a switch).  FP64 or "mixed"."""
+
+    def __init__(self, stiff_alg=None):
+        stiff_alg = Rosenbrock23() if stiff_alg is None else stiff_alg
+        if isinstance(stiff_alg, Rosenbrock23):
+            self.alg_id = capi.ALG_AUTOTSIT5_ROSENBROCK23
+        elif isinstance(stiff_alg, Rodas5) and not isinstance(stiff_alg, Rodas5P):
+            self.alg_id = capi.ALG_AUTOTSIT5_RODAS5
+        else:
+            raise TypeError("AutoTsit5 takes Rosenbrock23() or Rodas5()")
+        self.stiff_alg = stiff_alg
+
+    def __repr__(self):
+        return "AutoTsit5(%r)" % (self.stiff_alg,)
+
+
 class EM(_Alg):
     alg_id = capi.ALG_EM
     sde = True

@@ -42,7 +42,8 @@ def sources():
 # the library as {include name, text}; gbde.h under the name models.cuh uses.
 RTC_HEADERS = ["common.cuh", "controller.h", "solver.cuh", "models.cuh", "ff.cuh", "tableaus.h",
                "dense_coeffs.h", "explicit_rk.cuh", "rosenbrock.cuh", "ff_vec.cuh", "rodas_ff.cuh",
-               "tsit5_ff.cuh", "vern7_ff.cuh", "ros23_ff.cuh", "dual.cuh", "philox.h", "sde.cuh"]
+               "tsit5_ff.cuh", "vern7_ff.cuh", "ros23_ff.cuh", "dual.cuh", "philox.h", "sde.cuh",
+               "autoswitch.cuh"]
 
 
 def write_rtc_headers():

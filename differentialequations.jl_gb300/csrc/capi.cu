@@ -115,6 +115,8 @@ cudaError_t launch_alg(int alg, LaunchCfg cfg, const KArgs& a, cudaStream_t s) {
        (alg == GBDE_ALG_TSIT5 && cfg.tpt != 1)))
     return launch_team(cfg, a, s);
   if (alg == GBDE_ALG_TSIT5 || alg == GBDE_ALG_VERN7) return launch_explicit(cfg, a, s);
+  if (alg == GBDE_ALG_AUTOTSIT5_ROSENBROCK23 || alg == GBDE_ALG_AUTOTSIT5_RODAS5)
+    return launch_autoswitch(cfg, a, s);
   if (alg == GBDE_ALG_EM || alg == GBDE_ALG_SOSRI || alg == GBDE_ALG_SRIW1)
     return launch_sde(cfg, a, s);
   return launch_rosenbrock(cfg, a, s);
@@ -259,15 +261,27 @@ int gbde_opts_default(int32_t alg, gbde_opts* o) {
       o->beta1 = 0.2 - 0.75 * 0.04;
       o->stiff_threshold = 30.0;
       break;
+    case GBDE_ALG_AUTOTSIT5_ROSENBROCK23:  // Tsit5's; the stiff method's own defaults
+    case GBDE_ALG_AUTOTSIT5_RODAS5:        // are taken when it steps
+      o->beta2 = 0.04;
+      o->beta1 = 0.2 - 0.75 * 0.04;
+      break;
     default:
       return set_err(nullptr, GBDE_ERR_INVALID, "unknown algorithm id %d", alg);
   }
   return GBDE_OK;
 }
 
+static bool is_switch_alg(int a) {
+  return a == GBDE_ALG_AUTOTSIT5_ROSENBROCK23 || a == GBDE_ALG_AUTOTSIT5_RODAS5;
+}
 static bool is_ode_alg(int a) {
   return a == GBDE_ALG_TSIT5 || a == GBDE_ALG_VERN7 || a == GBDE_ALG_ROSENBROCK23 ||
-         a == GBDE_ALG_RODAS5 || a == GBDE_ALG_RODAS5P || a == GBDE_ALG_AUTO;
+         a == GBDE_ALG_RODAS5 || a == GBDE_ALG_RODAS5P || a == GBDE_ALG_AUTO || is_switch_alg(a);
+}
+// the stiff method of a switching composite
+static int switch_stiff_alg(int a) {
+  return a == GBDE_ALG_AUTOTSIT5_RODAS5 ? GBDE_ALG_RODAS5 : GBDE_ALG_ROSENBROCK23;
 }
 static bool is_sde_alg(int a) {
   return a == GBDE_ALG_EM || a == GBDE_ALG_SOSRI || a == GBDE_ALG_SRIW1;
@@ -408,10 +422,12 @@ static int check_solve_args(gbde_ctx* ctx, const gbde_problem* prob, const gbde_
     // a user model or a callback: compile (once per model, algorithm,
     // precision and callback) and load the kernels now, before anything is
     // enqueued or captured
-    if (alg == GBDE_ALG_AUTO || opts->learned || (is_sde_alg(alg) && opts->callback != 0))
+    if (alg == GBDE_ALG_AUTO || opts->learned || (is_sde_alg(alg) && opts->callback != 0) ||
+        (is_switch_alg(alg) && opts->callback != 0))
       return set_err(ctx, GBDE_ERR_UNSUPPORTED,
                      "user models run the one-thread ODE and SDE methods and callbacks the ODE "
-                     "methods, without GBDE_ALG_AUTO and without the learned predictor");
+                     "methods but the AutoTsit5 composites, without GBDE_ALG_AUTO and without "
+                     "the learned predictor");
     if (prob->model == GBDE_MODEL_VDP_RING8)
       return set_err(ctx, GBDE_ERR_UNSUPPORTED, "callbacks are not built for the 16-lane ring");
     std::string why;
@@ -419,6 +435,14 @@ static int check_solve_args(gbde_ctx* ctx, const gbde_problem* prob, const gbde_
     const int rc = rtc_prepare(prob->model, alg, opts->precision, opts->callback, &why);
     if (rc != GBDE_OK) return set_err(ctx, rc, "%s", why.c_str());
   }
+  if (is_switch_alg(alg) && (opts->precision == GBDE_PREC_F32X2 || opts->learned))
+    return set_err(ctx, GBDE_ERR_UNSUPPORTED,
+                   "the AutoTsit5 composites run in FP64 or GBDE_PREC_MIXED, without the "
+                   "learned predictor");
+  if (is_switch_alg(alg) && prob->model == GBDE_MODEL_VDP_RING8)
+    return set_err(ctx, GBDE_ERR_UNSUPPORTED,
+                   "the AutoTsit5 composites are built for one-thread models (n <= 3) and "
+                   "user models; the 16-state ring has GBDE_ALG_AUTO");
   if (opts->block_size != 0 && (opts->block_size > 128 || opts->block_size < 32 ||
                                 (opts->block_size & 31)))
     return set_err(ctx, GBDE_ERR_INVALID, "block_size must be a multiple of 32 and <= 128");
@@ -454,6 +478,13 @@ static void fill_common(KArgs& a, const gbde_problem* prob, const gbde_opts* opt
   a.timeout_ns = opts->timeout_s > 0 ? (uint64_t)(opts->timeout_s * 1e9) : 0;
   a.ctl = ctl_consts(opts->beta1, opts->beta2, opts->gamma, opts->qmin, opts->qmax,
                      opts->qsteady_min, opts->qsteady_max, opts->qoldinit);
+  a.ctl_stiff = a.ctl;
+  if (is_switch_alg(opts->alg)) {  // the stiff method steps with its own exponents
+    gbde_opts r;
+    gbde_opts_default(switch_stiff_alg(opts->alg), &r);
+    a.ctl_stiff = ctl_consts(r.beta1, r.beta2, opts->gamma, opts->qmin, opts->qmax,
+                             opts->qsteady_min, opts->qsteady_max, opts->qoldinit);
+  }
   a.chunk = opts->chunk > 0 ? opts->chunk : 1;
 }
 
@@ -498,7 +529,7 @@ static LaunchCfg make_cfg(const gbde_ctx* ctx, const gbde_problem* prob, const g
 static bool uses_dt_prepass(const gbde_opts* o, int model) {
   const int a = o->alg;
   const bool ode = a == GBDE_ALG_TSIT5 || a == GBDE_ALG_VERN7 || a == GBDE_ALG_ROSENBROCK23 ||
-                   a == GBDE_ALG_RODAS5 || a == GBDE_ALG_RODAS5P;
+                   a == GBDE_ALG_RODAS5 || a == GBDE_ALG_RODAS5P || is_switch_alg(a);
   const bool team = model == GBDE_MODEL_VDP_RING8 &&
                     (a == GBDE_ALG_RODAS5 || a == GBDE_ALG_RODAS5P ||
                      (a == GBDE_ALG_TSIT5 && o->threads_per_traj != 1));

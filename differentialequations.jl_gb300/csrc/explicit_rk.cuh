@@ -9,9 +9,15 @@
 
 namespace gbde {
 
-template <class M, class T>
+// EIG: also estimate the spectral radius of the Jacobian along the step for
+// run-time stiffness detection (AutoSwitchAlg, autoswitch.cuh): Hairer &
+// Wanner II (IV.2) with the infinity norm, from the last two stages and their
+// arguments, eig = max_c |(k7_c - k6_c) / (y1_c - g6_c)| (NaN if any ratio is
+// NaN, as a maximum over a vector with a NaN).
+template <class M, class T, bool EIG = false>
 struct Tsit5Alg {
   static constexpr int ORDER = 5, ALG_ID = GBDE_ALG_TSIT5, N = M::N;
+  double eig;  // written by attempt() when EIG
   // FP32 path: the state is the unevaluated sum uu + lo (compensated), so
   // the per-step rounding of u + h*sum(b k) does not accumulate.
   static constexpr bool CMP = sizeof(T) == 4;
@@ -70,12 +76,34 @@ struct Tsit5Alg {
                       T(a75) * k5[c] + T(a76) * k6[c]));
     M::f(k7, un, p);
     nf += 6;
+    if constexpr (EIG) {  // y holds the 6th stage's argument
+      double mx = 0.0;
+      bool nan = false;
+#pragma unroll
+      for (int c = 0; c < N; ++c) {
+        const double r =
+            fabs(((double)k7[c] - (double)k6[c]) / ((double)un[c] - (double)y[c]));
+        nan |= r != r;
+        mx = fmax(mx, r);
+      }
+      eig = nan ? __longlong_as_double(0x7ff8000000000000ll) : mx;
+    }
     T err[N];
 #pragma unroll
     for (int c = 0; c < N; ++c)
       err[c] = h * (T(bt1) * k1[c] + T(bt2) * k2[c] + T(bt3) * k3[c] + T(bt4) * k4[c] +
                     T(bt5) * k5[c] + T(bt6) * k6[c] + T(bt7) * k7[c]);
     return err_ms<N>(err, uu, un, abstol, reltol);
+  }
+
+  // continue at u0 with f(u0) = f0 already known (a switch of methods)
+  GBDE_D void init_from(const T* u0, const T* f0, const T*) {
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      uu[c] = u0[c];
+      lo[c] = T(0);
+      k1[c] = f0[c];
+    }
   }
 
   GBDE_D void interp(double th, double dt, T* out, const T*, int&) {

@@ -23,6 +23,7 @@ struct LaunchCfg {
 cudaError_t launch_explicit(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
 cudaError_t launch_rosenbrock(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
 cudaError_t launch_sde(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
+cudaError_t launch_autoswitch(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s);
 
 // Order of the persistent queue (order.cu): longest span first, or, with a
 // learned cost per trajectory (log2 of its predicted attempted steps), most

@@ -15,6 +15,23 @@
 
 namespace gbde {
 
+// max over rows of sum_c |J_rc| in FP64, columns in order (the stiffness
+// estimate of the Rosenbrock methods in a composite: Hairer & Wanner II, IV.2)
+template <int N, class T>
+GBDE_D double jac_inf_norm(const T (*J)[N]) {
+  double mx = 0.0;
+  bool nan = false;
+#pragma unroll
+  for (int r = 0; r < N; ++r) {
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < N; ++c) s += fabs((double)J[r][c]);
+    nan |= s != s;
+    mx = fmax(mx, s);
+  }
+  return nan ? __longlong_as_double(0x7ff8000000000000ll) : mx;
+}
+
 // ---------------------------------------------------------------- LU
 // Partial-pivot LU of an N x N matrix held in registers.  Row swaps are done
 // with compile-time indices and selects so that nothing spills to local
@@ -187,6 +204,18 @@ struct Ros23Alg {
     ++nf;
     fresh = false;
   }
+  // continue at u0 with f(u0) = f0 already known (a switch of methods)
+  GBDE_D void init_from(const T* u0, const T* f0, const T*) {
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      uu[c] = u0[c];
+      F0[c] = f0[c];
+    }
+    fresh = false;
+  }
+  // ||J||_inf of the Jacobian the last attempt used (stiffness estimate)
+  GBDE_D double jac_norm() const { return jac_inf_norm<N>(J); }
+  GBDE_D bool f0_valid() const { return true; }  // F0 = f(uu) after accept (F2)
 
   GBDE_D double attempt(double dt, const T* p, double abstol, double reltol, int& nf) {
     using namespace tab::ros23;
@@ -319,6 +348,19 @@ struct RodasAlg {
     M::jac(J, uu, p);
     fresh = true;
   }
+  // continue at u0 with f(u0) = f0 already known (a switch of methods)
+  GBDE_D void init_from(const T* u0, const T* f0, const T* p) {
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      uu[c] = u0[c];
+      F0[c] = f0[c];
+    }
+    M::jac(J, uu, p);
+    fresh = true;
+  }
+  // ||J||_inf of the Jacobian the last attempt used (stiffness estimate)
+  GBDE_D double jac_norm() const { return jac_inf_norm<N>(J); }
+  GBDE_D bool f0_valid() const { return fresh; }  // F0 is re-evaluated after an accept
 
   GBDE_D double attempt(double dt, const T* p, double abstol, double reltol, int& nf) {
     if (!fresh) {

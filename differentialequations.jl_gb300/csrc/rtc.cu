@@ -228,6 +228,13 @@ std::string alg_type(int alg, int precision) {
     case GBDE_ALG_RODAS5P:
       return precision == GBDE_PREC_F32X2 ? "RodasFF<GbdeRtcModel, Rodas5PTag>"
                                           : "RodasAlg<GbdeRtcModel, " + T + ", Rodas5PTag>";
+    case GBDE_ALG_AUTOTSIT5_ROSENBROCK23:
+      if (precision == GBDE_PREC_F32X2) return "";
+      return "AutoSwitchAlg<GbdeRtcModel, " + T + ", Ros23Alg<GbdeRtcModel, " + T + ">>";
+    case GBDE_ALG_AUTOTSIT5_RODAS5:
+      if (precision == GBDE_PREC_F32X2) return "";
+      return "AutoSwitchAlg<GbdeRtcModel, " + T + ", RodasAlg<GbdeRtcModel, " + T +
+             ", Rodas5Tag>>";
   }
   return "";
 }
@@ -246,7 +253,7 @@ std::string make_source(const UserModelDef* m, int model, const CallbackDef* cb,
        "typedef unsigned short uint16_t; typedef unsigned int uint32_t;\n"
        "typedef unsigned long long uint64_t; typedef unsigned long size_t;\n"
        "#include \"solver.cuh\"\n#include \"explicit_rk.cuh\"\n#include \"rosenbrock.cuh\"\n"
-       "#include \"rodas_ff.cuh\"\n#include \"tsit5_ff.cuh\"\n#include \"vern7_ff.cuh\"\n#include \"ros23_ff.cuh\"\n#include \"dual.cuh\"\n#include \"sde.cuh\"\nnamespace gbde {\n";
+       "#include \"rodas_ff.cuh\"\n#include \"tsit5_ff.cuh\"\n#include \"vern7_ff.cuh\"\n#include \"ros23_ff.cuh\"\n#include \"dual.cuh\"\n#include \"sde.cuh\"\n#include \"autoswitch.cuh\"\nnamespace gbde {\n";
   char buf[256];
   if (m) {
     s += "struct UserModel {\n";
@@ -339,7 +346,8 @@ int compile_locked(int id, int alg, int precision, int callback, Compiled** out)
   if (alg_type(alg, precision).empty())
     return fail(GBDE_ERR_UNSUPPORTED,
                 "runtime-compiled kernels run Tsit5, Vern7, Rosenbrock23, Rodas5 and Rodas5P, "
-                "and EM, SOSRI and SRIW1 in FP64 or mixed precision");
+                "the AutoTsit5 composites in FP64 or mixed precision, and EM, SOSRI and SRIW1 "
+                "in FP64 or mixed precision");
   const bool sde = alg == GBDE_ALG_EM || alg == GBDE_ALG_SOSRI || alg == GBDE_ALG_SRIW1;
   if (sde && (cb || !m || m->g_body.empty()))
     return fail(GBDE_ERR_UNSUPPORTED,

@@ -51,6 +51,7 @@ struct KArgs {
   int32_t* flag;              // device status word (bit 0: deadline hit)
   const float* pred_dt;       // optional predicted first dt per trajectory
   CtlK ctl;                   // step-size controller constants (controller.h)
+  CtlK ctl_stiff;             // the stiff method's, in a switching composite (autoswitch.cuh)
   double* dt_first;           // optional: size of the first accepted step
   int32_t chunk;              // persistent queue positions per fetch (>= 1)
   const double* dt_init;      // optional: starting step per trajectory (k_init_dt)
@@ -370,6 +371,27 @@ struct early_time<A, decltype(void(A::EARLY_TIME))> {
   static constexpr bool v = A::EARLY_TIME;
 };
 
+// switching<Alg>::v: a composite that may change its method before an attempt
+// (AutoSwitchAlg, autoswitch.cuh, specialises it); it provides
+//   double choose(double dt, const T* p, int& nf)   -- the step size to attempt
+//   bool stiff                                       -- the stiff method is current
+//   int method() const                               -- GBDE_ALG_* of the current method
+template <class A>
+struct switching {
+  static constexpr bool v = false;
+};
+// the controller constants of the stepper's current method
+template <class A>
+GBDE_D const CtlK& ctl_of(const A& alg, const KArgs& a) {
+  if constexpr (switching<A>::v) return alg.stiff ? a.ctl_stiff : a.ctl;
+  else return a.ctl;
+}
+template <class A>
+GBDE_D int method_of(const A& alg) {
+  if constexpr (switching<A>::v) return alg.method();
+  else return A::ALG_ID;
+}
+
 // ------------------------------------------------------------- driver
 // Alg provides:  static constexpr int ORDER (for beta defaults / init dt),
 //   void init(const T* u0, const T* p, int& nf)       -- u = u0, f(u) cache
@@ -458,6 +480,12 @@ __device__ void integrate_all(const KArgs& a) {
 
     if (ret == GBDE_RET_DEFAULT) {
       // ---- one attempted step
+      if constexpr (switching<Alg>::v) {
+        if (iters > 0) {  // the method for this attempt, from the last one's estimate
+          dt = alg.choose(dt, p, nfev);
+          if (a.dtmax > 0.0 && ord_bits(dt) > ord_bits(a.dtmax)) dt = a.dtmax;
+        }
+      }
       const double rem = tf - t;
       double h = dt;
       bool last = false;
@@ -499,7 +527,7 @@ __device__ void integrate_all(const KArgs& a) {
       if (ok) {
         // controller proposal for the next step
         double dtnew = h;
-        if (a.adaptive) dtnew = h * f2d_bits(ctl_accept(a.ctl, ms, lqold));
+        if (a.adaptive) dtnew = h * f2d_bits(ctl_accept(ctl_of(alg, a), ms, lqold));
         const double tlo0 = tlo;
         double tnew;
         if constexpr (early_time<Alg>::v) {
@@ -635,7 +663,7 @@ __device__ void integrate_all(const KArgs& a) {
         }
       } else {
         ++nrej;
-        dt = h * f2d_bits(ctl_reject(a.ctl, ms));
+        dt = h * f2d_bits(ctl_reject(ctl_of(alg, a), ms));
       }
       if (ret == GBDE_RET_DEFAULT) {
         if (iters >= a.maxiters) ret = GBDE_RET_MAXITERS;
@@ -661,7 +689,7 @@ __device__ void integrate_all(const KArgs& a) {
       if (a.nreject) a.nreject[i] = nrej;
       if (a.nf) a.nf[i] = nfev;
       if (a.t_end) a.t_end[i] = t + tlo;
-      if (a.method_out) a.method_out[i] = Alg::ALG_ID;
+      if (a.method_out) a.method_out[i] = method_of(alg);
       if (a.dt_first) a.dt_first[i] = dt1;
       active = false;
     }

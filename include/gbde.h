@@ -112,6 +112,18 @@ extern "C" {
 
 #define GBDE_ALG_SRIW1 9        /* SRIW1 (Roessler 2010): SRI of strong order 1.5,
                                    adaptive with rejection sampling with memory      */
+/* AutoTsit5(Rosenbrock23()) / AutoTsit5(Rodas5()) (test/qa/qa.jl:15): per
+ * trajectory, run-time switching.  Tsit5 estimates the Jacobian's spectral
+ * radius from its last two stages, the stiff method takes ||J||_inf; before
+ * every attempt after the first, stiffness = |eig dt / 3.5068| > 0.9 counts
+ * towards a switch: more than 10 successive stiff estimates switch Tsit5 to
+ * the stiff method (dt * 2), more than 3 successive non-stiff ones switch
+ * back (dt / 2) -- OrdinaryDiffEq's AutoSwitch with its defaults.  Each method
+ * steps with its own PI exponents (Tsit5's are the options', the stiff
+ * method's its defaults).  outputs.method: the method of the last step.
+ * Built-in models with n <= 3 and user models; FP64 or GBDE_PREC_MIXED. */
+#define GBDE_ALG_AUTOTSIT5_ROSENBROCK23 10
+#define GBDE_ALG_AUTOTSIT5_RODAS5 11
 
 /* ---- precision -------------------------------------------------------- */
 #define GBDE_PREC_FP64 0  /* everything in FP64                                  */

@@ -288,6 +288,7 @@ struct Stepper {
   double k[11][NMAX];  // stages (RK) or transformed stages (Rodas)
   double J[NMAX * NMAX];
   bool fresh, have11;
+  double eig = 0.0;  // the last attempt's stiffness estimate (switching composites)
 
   void init(const double* u0, int& nf) {
     for (int c = 0; c < n; ++c) u[c] = u0[c];
@@ -313,18 +314,32 @@ struct Stepper {
                             {a71, a72, a73, a74, a75, a76}};
     const double bt[7] = {bt1, bt2, bt3, bt4, bt5, bt6, bt7};
     for (int c = 0; c < n; ++c) k[0][c] = f0[c];
-    double y[NMAX];
+    double y[NMAX], g6[NMAX];
     for (int s = 1; s < 7; ++s) {
       for (int c = 0; c < n; ++c) {
         double acc = 0.0;
         for (int j = 0; j < s; ++j) acc += A[s][j] * k[j][c];
         y[c] = u[c] + h * acc;
       }
+      if (s == 5)
+        for (int c = 0; c < n; ++c) g6[c] = y[c];
       if (s == 6)
         for (int c = 0; c < n; ++c) un[c] = y[c];
       rhs(id, y, p, k[s]);
     }
     nf += 6;
+    // stiffness estimate (Hairer & Wanner II, IV.2, infinity norm): the
+    // largest |(k7 - k6) / (y1 - g6)| over components, NaN if any is NaN
+    {
+      double mx = 0.0;
+      bool nan = false;
+      for (int c = 0; c < n; ++c) {
+        const double r = std::fabs((k[6][c] - k[5][c]) / (un[c] - g6[c]));
+        nan |= r != r;
+        mx = std::fmax(mx, r);
+      }
+      eig = nan ? NAN : mx;
+    }
     double e[NMAX];
     for (int c = 0; c < n; ++c) {
       double acc = 0.0;
@@ -588,12 +603,50 @@ struct Stepper {
     }
   }
 
+  // ||J||_inf (row sums of |J| in column order): the Rosenbrock methods'
+  // stiffness estimate in a switching composite
+  double jac_norm() const {
+    double mx = 0.0;
+    bool nan = false;
+    for (int r = 0; r < n; ++r) {
+      double s = 0.0;
+      for (int c = 0; c < n; ++c) s += std::fabs(J[r * n + c]);
+      nan |= s != s;
+      mx = std::fmax(mx, s);
+    }
+    return nan ? NAN : mx;
+  }
   double attempt(double h, const Ctl& C, int& nf) {
     switch (alg) {
       case GBDE_ALG_TSIT5: return tsit5(h, C, nf);
       case GBDE_ALG_VERN7: return vern7(h, C, nf);
-      case GBDE_ALG_ROSENBROCK23: return ros23(h, C, nf);
-      default: return rodas(h, C, nf);
+      case GBDE_ALG_ROSENBROCK23: {
+        const double E = ros23(h, C, nf);
+        eig = jac_norm();
+        return E;
+      }
+      default: {
+        const double E = rodas(h, C, nf);
+        eig = jac_norm();
+        return E;
+      }
+    }
+  }
+  // Continue the trajectory at u with another method: f(u) carries over
+  // (Rodas re-evaluates it after an accept, so it is evaluated here then);
+  // Rodas gets its Jacobian at u now.
+  void switch_to(int to, int& nf) {
+    if ((alg == GBDE_ALG_RODAS5 || alg == GBDE_ALG_RODAS5P) && !fresh) {
+      rhs(id, u, p, f0);
+      ++nf;
+    }
+    alg = to;
+    have11 = false;
+    if (to == GBDE_ALG_RODAS5 || to == GBDE_ALG_RODAS5P) {
+      jacobian(id, n, u, p, J);
+      fresh = true;
+    } else {
+      fresh = false;
     }
   }
   void interp(double th, double h, double* out, int& nf) {
@@ -633,7 +686,13 @@ struct Stepper {
 // ------------------------------------------------------------ ODE driver
 // One trajectory: PI controller (HNW I, II.4; Gustafsson), scaled RMS norm,
 // HNW starting step, dense output at save times, tf snapping, return codes.
-void solve_ode_traj(const Model& m, int alg, const Ctl& C, Out& o) {
+// stiff_alg != 0: the AutoTsit5(stiff_alg) composite (AutoSwitch with its
+// published defaults: before every attempt after the first, stiffness =
+// |eig dt / 3.5068| > 9/10 counts; > 10 successive stiff estimates switch
+// Tsit5 to stiff_alg with dt * 2, > 3 successive non-stiff ones switch back
+// with dt / 2; the stiff method steps with the controller constants Cs).
+void solve_ode_traj(const Model& m, int alg, const Ctl& C, Out& o, int stiff_alg = 0,
+                    const Ctl* Cs = nullptr) {
   const gbde_problem* P = o.P;
   const int64_t i = o.i;
   const int n = m.n;
@@ -648,10 +707,12 @@ void solve_ode_traj(const Model& m, int alg, const Ctl& C, Out& o) {
   bool bad = !(tf >= t) || !std::isfinite(t) || !std::isfinite(tf);
   for (int c = 0; c < n; ++c) bad |= !std::isfinite(u0[c]);
   Stepper S;
-  S.alg = alg;
+  S.alg = stiff_alg ? GBDE_ALG_TSIT5 : alg;
   S.n = n;
   S.id = m.id;
   S.p = p;
+  bool stiff = false;
+  int count = 0;
   double dt = 0.0;
   CtlMem cm = ctl_start(C);
   if (bad) {
@@ -665,6 +726,22 @@ void solve_ode_traj(const Model& m, int alg, const Ctl& C, Out& o) {
     else if (!(dt > 0.0)) ret = GBDE_RET_DTLESSTHANMIN;
   }
   while (ret == GBDE_RET_DEFAULT) {
+    if (stiff_alg && iters > 0) {
+      const double stiffness = std::fabs(S.eig * dt / 3.5068);
+      const bool s = stiffness > 0.9;  // NaN: not stiff
+      count = s ? (count < 0 ? 1 : count + 1) : (count > 0 ? -1 : count - 1);
+      if (!stiff && count > 10) {
+        S.switch_to(stiff_alg, nf);
+        stiff = true;
+        dt = dt * 2.0;
+      } else if (stiff && count < -3) {
+        S.switch_to(GBDE_ALG_TSIT5, nf);
+        stiff = false;
+        dt = dt / 2.0;
+      }
+      if (C.dtmax > 0.0) dt = std::fmin(dt, C.dtmax);
+    }
+    const Ctl& Cc = stiff ? *Cs : C;
     const double rem = tf - t;
     double h = dt;
     bool last = false;
@@ -676,7 +753,7 @@ void solve_ode_traj(const Model& m, int alg, const Ctl& C, Out& o) {
     ++iters;
     if (!C.adaptive || E <= 1.0) {
       double dtnew = h;
-      if (C.adaptive) dtnew = h * ctl_accept_r(C, E, cm);
+      if (C.adaptive) dtnew = h * ctl_accept_r(Cc, E, cm);
       const double tnew = last ? tf : t + h;
       while (js < P->n_save) {
         const double ts = o.ts(js);
@@ -700,7 +777,7 @@ void solve_ode_traj(const Model& m, int alg, const Ctl& C, Out& o) {
       dt = C.dtmax > 0.0 ? std::fmin(dtnew, C.dtmax) : dtnew;
     } else {
       ++nrej;
-      dt = h * ctl_reject_r(C, E);
+      dt = h * ctl_reject_r(Cc, E);
     }
     if (ret == GBDE_RET_DEFAULT) {
       if (iters >= C.maxiters) ret = GBDE_RET_MAXITERS;
@@ -717,7 +794,7 @@ void solve_ode_traj(const Model& m, int alg, const Ctl& C, Out& o) {
   if (O->nreject) O->nreject[i] = nrej;
   if (O->nf) O->nf[i] = nf;
   if (O->t_end) O->t_end[i] = t;
-  if (O->method) O->method[i] = alg;
+  if (O->method) O->method[i] = S.alg;
 }
 
 // ------------------------------------------------- Philox4x32-10 + normals
@@ -1123,6 +1200,18 @@ int oracle_ensemble_solve(const gbde_problem* P, const gbde_opts* O, gbde_output
         gbde::ctl_consts(O->beta1, O->beta2, O->gamma, O->qmin, O->qmax, O->qsteady_min,
                          O->qsteady_max, O->qoldinit)};
   const int alg = O->alg;
+  // AutoTsit5 composites: the stiff method and its own PI exponents (its
+  // option defaults: Rosenbrock23 1/3, 0; Rodas5 1/5, 0)
+  const int stiff_alg = alg == GBDE_ALG_AUTOTSIT5_ROSENBROCK23 ? GBDE_ALG_ROSENBROCK23
+                        : alg == GBDE_ALG_AUTOTSIT5_RODAS5     ? GBDE_ALG_RODAS5
+                                                               : 0;
+  Ctl Cs = C;
+  if (stiff_alg) {
+    Cs.beta1 = stiff_alg == GBDE_ALG_ROSENBROCK23 ? 1.0 / 3.0 : 1.0 / 5.0;
+    Cs.beta2 = 0.0;
+    Cs.k = gbde::ctl_consts(Cs.beta1, Cs.beta2, O->gamma, O->qmin, O->qmax, O->qsteady_min,
+                            O->qsteady_max, O->qoldinit);
+  }
   const int64_t N = P->n_traj;
   std::atomic<int64_t> next{0};
   auto work = [&]() {
@@ -1138,6 +1227,7 @@ int oracle_ensemble_solve(const gbde_problem* P, const gbde_opts* O, gbde_output
           solve_sri_traj<gbde::tab::SosriTab>(m, C, O->seed, noise_f32, o, alg);
         else if (alg == GBDE_ALG_SRIW1)
           solve_sri_traj<gbde::tab::Sriw1Tab>(m, C, O->seed, noise_f32, o, alg);
+        else if (stiff_alg) solve_ode_traj(m, alg, C, o, stiff_alg, &Cs);
         else solve_ode_traj(m, alg, C, o);
       }
     }

@@ -23,6 +23,7 @@ _lib = None
 MODEL_LINEAR, MODEL_LORENZ, MODEL_ROBERTSON, MODEL_VDP_RING8, MODEL_LOTKA_VOLTERRA = 1, 2, 3, 4, 5
 ALG_TSIT5, ALG_VERN7, ALG_ROSENBROCK23, ALG_RODAS5, ALG_RODAS5P = 1, 2, 3, 4, 5
 ALG_EM, ALG_SOSRI, ALG_AUTO, ALG_SRIW1 = 6, 7, 8, 9
+ALG_AUTOTSIT5_ROSENBROCK23, ALG_AUTOTSIT5_RODAS5 = 10, 11
 SAVE_GRID, SAVE_PER_TRAJ = 0, 1
 MEM_HOST = 0
 F64, F32 = 0, 1
@@ -85,7 +86,7 @@ def opts_default(alg):
     o.reltol, o.abstol, o.maxiters = 1e-3, 1e-6, 100000
     o.qmin, o.qmax, o.gamma = 0.2, 10.0, 0.9
     o.qsteady_min, o.qsteady_max, o.qoldinit = 1.0, 1.0, 1e-4
-    if alg in (ALG_TSIT5, ALG_AUTO):
+    if alg in (ALG_TSIT5, ALG_AUTO, ALG_AUTOTSIT5_ROSENBROCK23, ALG_AUTOTSIT5_RODAS5):
         o.beta2 = 0.04
         o.beta1 = 0.2 - 0.75 * 0.04
         if alg == ALG_AUTO:
@@ -180,11 +181,12 @@ def solve(capi, model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", nt
         "nreject": np.empty(N, np.int32),
         "nf": np.empty(N, np.int32),
         "t_end": np.empty(N, np.float64),
+        "method": np.empty(N, np.int32),
     }
     outs = Outputs()
     outs.u = res["u"].ctypes.data
     outs.u_dtype = F32 if u_dtype == "f32" else F64
-    for k in ("retcode", "naccept", "nreject", "nf", "t_end"):
+    for k in ("retcode", "naccept", "nreject", "nf", "t_end", "method"):
         setattr(outs, k, res[k].ctypes.data)
     o = _as_opts(opts)
     rc = lib().oracle_ensemble_solve(C.addressof(prob), C.addressof(o), C.addressof(outs),

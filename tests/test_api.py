@@ -47,14 +47,15 @@ def test_oracle_restates_the_abi(capi, oracle):
             assert getattr(py, n).offset == getattr(orc, n2).offset, n
     for name in ("MODEL_LINEAR", "MODEL_LORENZ", "MODEL_ROBERTSON", "MODEL_VDP_RING8",
                  "MODEL_LOTKA_VOLTERRA", "ALG_TSIT5", "ALG_VERN7", "ALG_ROSENBROCK23",
-                 "ALG_RODAS5", "ALG_RODAS5P", "ALG_EM", "ALG_SOSRI", "ALG_AUTO", "SAVE_GRID",
+                 "ALG_RODAS5", "ALG_RODAS5P", "ALG_EM", "ALG_SOSRI", "ALG_AUTO", "ALG_SRIW1",
+                 "ALG_AUTOTSIT5_ROSENBROCK23", "ALG_AUTOTSIT5_RODAS5", "SAVE_GRID",
                  "SAVE_PER_TRAJ", "MEM_HOST", "F64", "F32", "RET_SUCCESS"):
         assert getattr(capi, name) == getattr(oracle, name), name
     for mid, size in oracle.MODEL_SIZES.items():
         assert capi.model_info(mid) == size
     algs = [capi.ALG_TSIT5, capi.ALG_VERN7, capi.ALG_ROSENBROCK23, capi.ALG_RODAS5,
-            capi.ALG_RODAS5P, capi.ALG_EM, capi.ALG_SOSRI, capi.ALG_AUTO]
-    algs += [capi.ALG_SRIW1] if hasattr(capi, "ALG_SRIW1") else []
+            capi.ALG_RODAS5P, capi.ALG_EM, capi.ALG_SOSRI, capi.ALG_AUTO, capi.ALG_SRIW1,
+            capi.ALG_AUTOTSIT5_ROSENBROCK23, capi.ALG_AUTOTSIT5_RODAS5]
     for alg in algs:
         a, b = capi.opts_default(alg), oracle.opts_default(alg)
         for n, _ in capi.Opts._fields_:

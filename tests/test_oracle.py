@@ -251,3 +251,51 @@ def test_oracle_lu_solve_with_row_swaps(oracle, n):
         b = rng.normal(size=n)
         x = oracle.lu_solve(A, b)
         assert np.max(np.abs(A @ x - b)) <= 1e-10 * (1 + np.abs(A).sum(1).max() * np.abs(x).max())
+
+
+# ------------------------------------------------ AutoTsit5 composites
+@pytest.mark.parametrize("stiff", ["ROSENBROCK23", "RODAS5"])
+def test_autoswitch_nonstiff_is_tsit5(oracle, capi, de, stiff):
+    """AutoTsit5(stiff) on a non-stiff problem (Lorenz at reltol 1e-8, where
+    h * eig stays far inside Tsit5's stability region) never switches: the
+    same steps and values as Tsit5 itself, bit for bit."""
+    grid = de.save_grid(0.0, 2.0, 0.1)
+    kw = dict(reltol=1e-8, abstol=1e-8)
+    p, u0 = [10.0, 28.0, 8.0 / 3.0], [1.0, 0.0, 0.0]
+    a = run(oracle, capi, de.models.lorenz, "AUTOTSIT5_" + stiff, p, u0, (0.0, 2.0), grid, **kw)
+    t = run(oracle, capi, de.models.lorenz, "TSIT5", p, u0, (0.0, 2.0), grid, **kw)
+    assert a["method"][0] == capi.ALG_TSIT5
+    assert np.array_equal(a["u"], t["u"]) and a["naccept"][0] == t["naccept"][0]
+
+
+@pytest.mark.parametrize("stiff", ["ROSENBROCK23", "RODAS5"])
+def test_autoswitch_stiff_linear_switches(oracle, capi, de, stiff):
+    """u' = a u with a = -1e4 on (0, 1): Tsit5's steps are held at its
+    stability limit (h |a| ~ 3.5), every estimate is stiff, and after 11 of
+    them the composite continues with the stiff method (the run ends in it)
+    in a small fraction of Tsit5's step count; the solution stays within
+    tolerance of exp(a t)."""
+    grid = de.save_grid(0.0, 1.0, 0.1)
+    kw = dict(reltol=1e-6, abstol=1e-8)
+    a = run(oracle, capi, de.models.linear, "AUTOTSIT5_" + stiff, [-1e4], [1.0], (0.0, 1.0),
+            grid, **kw)
+    t = run(oracle, capi, de.models.linear, "TSIT5", [-1e4], [1.0], (0.0, 1.0), grid, **kw)
+    assert a["retcode"][0] == capi.RET_SUCCESS
+    assert a["method"][0] == getattr(capi, "ALG_" + stiff)
+    assert a["naccept"][0] + a["nreject"][0] < 0.2 * (t["naccept"][0] + t["nreject"][0])
+    exact = np.exp(-1e4 * grid)
+    assert np.max(np.abs(a["u"][0, :, 0] - exact)) < 1e-6
+
+
+def test_autoswitch_robertson(oracle, capi, de):
+    """AutoTsit5(Rodas5()) on Robertson (core.jl:38-49's problem, to t = 1e5):
+    Success, ends in Rodas5, and stays within 10x tolerance of Rodas5 at a
+    tight tolerance."""
+    grid = np.array([1e-3, 1e-1, 1.0, 1e2, 1e4, 1e5])
+    kw = dict(reltol=1e-6, abstol=1e-10)
+    k, u0 = [0.04, 3e7, 1e4], [1.0, 0.0, 0.0]
+    a = run(oracle, capi, de.models.robertson, "AUTOTSIT5_RODAS5", k, u0, (0.0, 1e5), grid, **kw)
+    ref = run(oracle, capi, de.models.robertson, "RODAS5", k, u0, (0.0, 1e5), grid,
+              reltol=1e-10, abstol=1e-14)
+    assert a["retcode"][0] == capi.RET_SUCCESS and a["method"][0] == capi.ALG_RODAS5
+    assert oracle.weighted_error(a["u"][0], ref["u"][0], 1e-10, 1e-6) < 10

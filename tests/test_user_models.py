@@ -69,6 +69,21 @@ def test_compile_every_algorithm_and_precision(capi, de):
             _compile_or_skip(de, capi, m, alg, prec)
 
 
+def test_compile_autoswitch_composites(capi, de):
+    """AutoTsit5(Rosenbrock23()) / AutoTsit5(Rodas5()) build around a user f
+    (dual-number Jacobian) in FP64 and mixed precision; FP32 pairs are
+    refused with GBDE_ERR_UNSUPPORTED."""
+    m = de.ODEFunction(LORENZ_F, 3, 3, name="lorenz_autoswitch")
+    for stiff in (de.Rosenbrock23(), de.Rodas5()):
+        for prec in ("fp64", "mixed"):
+            _compile_or_skip(de, capi, m, de.AutoTsit5(stiff), prec)
+        with pytest.raises(capi.GBDEError) as e:
+            de.compile_model(m, de.AutoTsit5(stiff), "f32x2")
+        assert e.value.code == capi.GBDE_ERR_UNSUPPORTED
+    with pytest.raises(TypeError):
+        de.AutoTsit5(de.Vern7())
+
+
 def test_compile_error_carries_the_log(capi, de):
     m = de.ODEFunction("du[0] = undefined_rate * u[0];", 1, 1, name="broken")
     with pytest.raises(capi.GBDEError) as e:
