@@ -59,10 +59,14 @@ def test_julia_enums_match_header(capi):
     expect = {"Tsit5": capi.ALG_TSIT5, "Vern7": capi.ALG_VERN7,
               "Rosenbrock23": capi.ALG_ROSENBROCK23, "Rodas5": capi.ALG_RODAS5,
               "Rodas5P": capi.ALG_RODAS5P, "EM": capi.ALG_EM, "SOSRI": capi.ALG_SOSRI,
-              "AutoTsit5": capi.ALG_AUTO}
-    if hasattr(capi, "ALG_SRIW1"):
-        expect["SRIW1"] = capi.ALG_SRIW1
+              "SRIW1": capi.ALG_SRIW1}
     assert algs == expect
+    # AutoTsit5(stiff): the switching composites; the stiff_threshold option: AUTO
+    comp = re.search(r"algid\(alg::OrdinaryDiffEq\.CompositeAlgorithm\) =(.*?)error", code, re.S)
+    assert comp and re.findall(r"isa (\w+) \? (\d+)", comp.group(1)) == [
+        ("Rosenbrock23", str(capi.ALG_AUTOTSIT5_ROSENBROCK23)),
+        ("Rodas5", str(capi.ALG_AUTOTSIT5_RODAS5))]
+    assert re.search(r"solver_id\(alg, ea\) = .*: (\d+)", code).group(1) == str(capi.ALG_AUTO)
     prec = dict(re.findall(r":(\w+) => (\d+)", re.search(r"PRECISION = Dict\((.*?)\)", code).group(1)))
     assert {k: int(v) for k, v in prec.items()} == {"fp64": capi.PREC_FP64,
                                                     "mixed": capi.PREC_MIXED,
