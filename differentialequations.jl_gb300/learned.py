@@ -124,19 +124,23 @@ def cost_targets(naccept, nreject):
 
 
 def stiff_labels(solve_arrays, model, p, u0, t0, tf, saveat, save_kind, reltol, abstol,
-                 explicit_maxiters=20000):
-    """Label 1 where Rodas5 (FP64) is cheaper than Tsit5 (FP32 compensated
-    state) on a trajectory: steps x device time per step of each kernel, both
-    measured on these inputs.  Tsit5 runs that hit explicit_maxiters count as
-    stiff."""
+                 explicit_maxiters=20000, precision=None):
+    """Label 1 where Rodas5 is cheaper than Tsit5 on a trajectory: steps x
+    device time per step of each kernel, both measured on these inputs in the
+    precision the learned solves will run (GBDE_ALG_AUTO's: Tsit5 in
+    `precision`, Rodas5 in FP64 for an FP64 solve and in FP32 pairs
+    otherwise; default FP32 pairs for both).  Tsit5 runs that hit
+    explicit_maxiters count as stiff."""
+    prec = capi.PREC_F32X2 if precision is None else precision
+    stiff_prec = capi.PREC_FP64 if prec == capi.PREC_FP64 else capi.PREC_F32X2
     res = {}
-    for name, alg, prec, mi in (("tsit5", capi.ALG_TSIT5, capi.PREC_MIXED, explicit_maxiters),
-                                ("rodas5", capi.ALG_RODAS5, capi.PREC_FP64, 10 ** 6)):
+    for name, alg, pr, mi in (("tsit5", capi.ALG_TSIT5, prec, explicit_maxiters),
+                              ("rodas5", capi.ALG_RODAS5, stiff_prec, 10 ** 6)):
         o = capi.opts_default(alg)
-        o.reltol, o.abstol, o.maxiters, o.precision = reltol, abstol, mi, prec
+        o.reltol, o.abstol, o.maxiters, o.precision = reltol, abstol, mi, pr
         o.batching = capi.BATCH_PERSISTENT
         r = solve_arrays(model, o, p, u0, t0, tf, saveat, save_kind,
-                         u_dtype="f32" if prec == capi.PREC_MIXED else "f64")
+                         u_dtype="f64" if pr == capi.PREC_FP64 else "f32")
         steps = (_np(r["naccept"]) + _np(r["nreject"])).astype(np.float64)
         res[name] = (steps, r["device_ms"] / max(steps.sum(), 1.0), _np(r["retcode"]))
     (st_t, c_t, rc_t), (st_r, c_r, _) = res["tsit5"], res["rodas5"]
