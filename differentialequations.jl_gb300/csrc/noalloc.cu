@@ -91,9 +91,12 @@ int device_setup(int device, DeviceSetup* out) {
   return GBDE_OK;
 }
 
+bool is_switch(int a) {
+  return a == GBDE_ALG_AUTOTSIT5_ROSENBROCK23 || a == GBDE_ALG_AUTOTSIT5_RODAS5;
+}
 bool is_ode(int a) {
   return a == GBDE_ALG_TSIT5 || a == GBDE_ALG_VERN7 || a == GBDE_ALG_ROSENBROCK23 ||
-         a == GBDE_ALG_RODAS5 || a == GBDE_ALG_RODAS5P;
+         a == GBDE_ALG_RODAS5 || a == GBDE_ALG_RODAS5P || is_switch(a);
 }
 bool is_sde(int a) { return a == GBDE_ALG_EM || a == GBDE_ALG_SOSRI || a == GBDE_ALG_SRIW1; }
 
@@ -170,6 +173,10 @@ extern "C" int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_
   if (alg == GBDE_ALG_ROSENBROCK23 && prob->model == GBDE_MODEL_VDP_RING8)
     return fail(GBDE_ERR_UNSUPPORTED,
                 "Rosenbrock23 is built for n_state <= 3 (use Rodas5 / Rodas5P for the ring)");
+  if (is_switch(alg) &&
+      (opts->precision == GBDE_PREC_F32X2 || prob->model == GBDE_MODEL_VDP_RING8))
+    return fail(GBDE_ERR_UNSUPPORTED,
+                "the AutoTsit5 composites run one-thread models in FP64 or GBDE_PREC_MIXED");
   if (opts->threads_per_traj != 0 && opts->threads_per_traj != 1 && opts->threads_per_traj != 16)
     return fail(GBDE_ERR_INVALID, "threads_per_traj must be 0, 1 or 16");
   if (opts->threads_per_traj == 16 && prob->model != GBDE_MODEL_VDP_RING8)
@@ -241,6 +248,14 @@ extern "C" int gbde_ensemble_solve_noalloc(const gbde_problem* prob, const gbde_
   a.timeout_ns = opts->timeout_s > 0 ? (uint64_t)(opts->timeout_s * 1e9) : 0;
   a.ctl = ctl_consts(opts->beta1, opts->beta2, opts->gamma, opts->qmin, opts->qmax,
                      opts->qsteady_min, opts->qsteady_max, opts->qoldinit);
+  a.ctl_stiff = a.ctl;
+  if (is_switch(alg)) {  // the stiff method steps with its own exponents (its defaults)
+    gbde_opts r;
+    gbde_opts_default(alg == GBDE_ALG_AUTOTSIT5_RODAS5 ? GBDE_ALG_RODAS5 : GBDE_ALG_ROSENBROCK23,
+                      &r);
+    a.ctl_stiff = ctl_consts(r.beta1, r.beta2, opts->gamma, opts->qmin, opts->qmax,
+                             opts->qsteady_min, opts->qsteady_max, opts->qoldinit);
+  }
   a.chunk = opts->chunk > 0 ? opts->chunk : 1;
   a.queue = opts->batching == GBDE_BATCH_PERSISTENT ? queue : nullptr;
   a.flag = flag_dev;

@@ -108,10 +108,17 @@ def _lv_inputs(N, seed):
     return p, np.ones((N, 2)), np.zeros(N), np.full(N, 2.0), np.linspace(0.0, 2.0, 9)
 
 
-@pytest.mark.parametrize("case", ["em", "ring_rodas5"])
+def _robertson_inputs(N, seed):
+    rng = np.random.default_rng(seed)
+    p = np.array([0.04, 3e7, 1e4]) * 10 ** rng.uniform(-1, 1, (N, 3))
+    return p, np.tile([1.0, 0.0, 0.0], (N, 1)), np.zeros(N), np.full(N, 1e3), np.logspace(-3, 3, 7)
+
+
+@pytest.mark.parametrize("case", ["em", "ring_rodas5", "autotsit5_rosenbrock23"])
 def test_noalloc_matches_ensemble_solve_other_kernels(de, case):
-    """The SDE kernel (Euler-Maruyama on the Lotka-Volterra ensemble) and the
-    16-lane team kernel (Rodas5 on the 16-state ring) through the
+    """The SDE kernel (Euler-Maruyama on the Lotka-Volterra ensemble), the
+    ring's team kernel (Rodas5 on the 16-state ring) and the AutoTsit5
+    composite (Robertson: Tsit5, then Rosenbrock23) through the
     no-allocation entry point: bitwise the outputs of gbde_ensemble_solve, on
     two calls in a row."""
     import torch
@@ -120,6 +127,10 @@ def test_noalloc_matches_ensemble_solve_other_kernels(de, case):
         model, host = de.models.lotka_volterra, _lv_inputs(2000, 3)
         opts = capi.opts_default(capi.ALG_EM)
         opts.dt, opts.seed = 1e-3, 17
+    elif case == "autotsit5_rosenbrock23":
+        model, host = de.models.robertson, _robertson_inputs(1000, 5)
+        opts = capi.opts_default(capi.ALG_AUTOTSIT5_ROSENBROCK23)
+        opts.reltol, opts.abstol = 1e-6, 1e-10
     else:
         model, host = de.models.vdp_ring8, _ring_inputs(512, 4)
         opts = capi.opts_default(capi.ALG_RODAS5)
