@@ -443,14 +443,15 @@ def run_vdp(args, de):
                             out=host_out)
         if world > 1:
             dist.barrier()
-        e2e_ts = []
+        e2e_ts, e2e_call = [], []
         for _ in range(K):
             flush.zero_()
             torch.cuda.synchronize()
             t = time.perf_counter()
-            de.solve_arrays(M, opts(chosen), *hp, capi.SAVE_GRID, u_dtype=odt(chosen),
-                            out=host_out)
+            r = de.solve_arrays(M, opts(chosen), *hp, capi.SAVE_GRID, u_dtype=odt(chosen),
+                                out=host_out)
             e2e_ts.append((time.perf_counter() - t) * 1e3)
+            e2e_call.append((r["total_ms"], r["device_ms"]))
         if world > 1:
             dist.barrier()
     if not np.all(host_out["retcode"] == capi.RET_SUCCESS):
@@ -519,7 +520,12 @@ def run_vdp(args, de):
         "error_vs_oracle": acc[chosen],
         "accuracy": acc,
         "e2e": {"value": total / (e2e_ms * 1e-3), "unit": "trajectories/s", "ms_per_step": e2e_ms,
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "call_total_ms": float(np.median([c[0] for c in e2e_call])),
+                "call_device_ms": float(np.median([c[1] for c in e2e_call])),
+                "path": "gbde_ensemble_solve with GBDE_MEM_HOST: pinned inputs copied to the "
+                        "device; the saves stored by the kernels straight into the pinned host "
+                        "output over the host link while they run (no staging copy)"},
         "roofline": {"bound": "fp64", "kernel": "k_team8<TeamRodasFF8<VdpRing8,Rodas5>> (stiff "
                      "trajectories)" if st_prec == capi.PREC_F32X2 else
                      "k_team<TeamRodas<VdpRing8,double,Rodas5>> (stiff trajectories)",

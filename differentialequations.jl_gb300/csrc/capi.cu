@@ -272,6 +272,20 @@ int gbde_opts_default(int32_t alg, gbde_opts* o) {
   return GBDE_OK;
 }
 
+// The device address of a page-locked host buffer mapped into the device's
+// address space (cudaHostAlloc / cudaHostRegister memory, e.g. torch's
+// pinned tensors), or nullptr for any other pointer (pageable memory is
+// staged and copied).
+static void* mapped_host(const void* p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();  // a pointer the runtime does not know: not mapped
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 static bool is_switch_alg(int a) {
   return a == GBDE_ALG_AUTOTSIT5_ROSENBROCK23 || a == GBDE_ALG_AUTOTSIT5_RODAS5;
 }
@@ -618,13 +632,18 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
   KArgs a;
   fill_common(a, prob, opts, out);
   const bool host = prob->mem == GBDE_MEM_HOST;
+  void* u_direct = nullptr;
   if (host) {
     GBDE_CUDA(ctx, ctx->p.ensure((size_t)N * np * 8));
     GBDE_CUDA(ctx, ctx->u0.ensure((size_t)N * ns * 8));
     GBDE_CUDA(ctx, ctx->t0.ensure((size_t)N * 8));
     GBDE_CUDA(ctx, ctx->tf.ensure((size_t)N * 8));
     GBDE_CUDA(ctx, ctx->saveat.ensure(save_elems * 8));
-    if (out->u) GBDE_CUDA(ctx, ctx->u.ensure(u_bytes));
+    // saves straight into a page-locked, mapped output buffer: the kernels
+    // store them over the host link while they run (GB300's coherent C2C;
+    // ~2 GB/s of stores spread over the solve instead of a 1 GB copy after it)
+    u_direct = out->u ? mapped_host(out->u) : nullptr;
+    if (out->u && !u_direct) GBDE_CUDA(ctx, ctx->u.ensure(u_bytes));
     GBDE_CUDA(ctx, ctx->ret.ensure((size_t)N * 4));
     if (N > 0) {
       GBDE_CUDA(ctx, cudaMemcpyAsync(ctx->p.ptr, prob->p, (size_t)N * np * 8, cudaMemcpyHostToDevice, s));
@@ -639,7 +658,7 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
     a.t0 = (const double*)ctx->t0.ptr;
     a.tf = (const double*)ctx->tf.ptr;
     a.saveat = (const double*)ctx->saveat.ptr;
-    a.u_out = out->u ? ctx->u.ptr : nullptr;
+    a.u_out = out->u ? (u_direct ? u_direct : ctx->u.ptr) : nullptr;
     a.retcode = (int32_t*)ctx->ret.ptr;
     if (out->reduce) {
       GBDE_CUDA(ctx, ctx->red.ensure(2 * n_save * (size_t)ns * 8));
@@ -662,7 +681,7 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
 
   int32_t flag = 0;
   if (host) {
-    if (u_bytes && out->u)
+    if (u_bytes && out->u && !u_direct)
       GBDE_CUDA(ctx, cudaMemcpyAsync(out->u, ctx->u.ptr, u_bytes, cudaMemcpyDeviceToHost, s));
     if (out->reduce && n_save)
       GBDE_CUDA(ctx, cudaMemcpyAsync(out->reduce, a.red, 2 * n_save * (size_t)ns * 8,

@@ -146,7 +146,10 @@ extern "C" {
 #define GBDE_SAVE_PER_TRAJ 1 /* saveat[N][n_save]                             */
 
 /* ---- memory space of the problem / output pointers -------------------- */
-#define GBDE_MEM_HOST 0   /* host pointers: the call copies H2D and D2H     */
+#define GBDE_MEM_HOST 0   /* host pointers: the call copies H2D and D2H; a
+                             page-locked, device-mapped outputs.u
+                             (cudaHostAlloc / cudaHostRegister) is written
+                             by the kernels directly, without a copy      */
 #define GBDE_MEM_DEVICE 1 /* device pointers on the context's device: no copies */
 
 /* ---- output element type ---------------------------------------------- */

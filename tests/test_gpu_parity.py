@@ -548,3 +548,36 @@ def test_dense_solution_evaluation(de, alg):
     es = de.solve(ens, a, de.EnsembleGB300(), trajectories=4, dense=True, reltol=1e-8,
                   abstol=1e-8)
     assert np.allclose(es[3](0.25), 0.8 * np.exp(1.01 * 0.25), rtol=1e-6)
+
+
+@pytest.mark.parametrize("model_name,alg", [("lorenz", "TSIT5"), ("vdp_ring8", "AUTO")])
+def test_host_outputs_pinned_equal_staged(de, rng, model_name, alg):
+    """GBDE_MEM_HOST with a page-locked output buffer: the kernels store the
+    saves straight into it (no staging copy); the result is bitwise the staged
+    path's (pageable output) and the device path's."""
+    import torch
+    capi = de._capi
+    model = getattr(de.models, model_name)
+    N = 3000
+    p, u0, t0, tf = make_inputs(de, model, N, rng)
+    grid = de.save_grid(0.0, float(tf[0]), float(tf[0]) / 10)
+    o = capi.opts_default(getattr(capi, "ALG_" + alg))
+    o.reltol = o.abstol = 1e-6
+    o.maxiters = 10 ** 6
+    if alg == "AUTO":
+        o.stiff_threshold = 100.0
+        o.precision = capi.PREC_F32X2
+        o.batching = capi.BATCH_PERSISTENT
+    shape = (N, len(grid), model.n_state)
+    pinned = {"u": torch.empty(shape, dtype=torch.float32).pin_memory().numpy(),
+              "retcode": torch.empty(N, dtype=torch.int32).pin_memory().numpy()}
+    staged = {"u": np.empty(shape, np.float32), "retcode": np.empty(N, np.int32)}
+    for out in (pinned, staged):
+        out["u"][:] = -1.0
+        de.solve_arrays(model, o, p, u0, t0, tf, grid, capi.SAVE_GRID, u_dtype="f32", out=out)
+    d = de.solve_arrays(model, o, *[torch.from_numpy(np.ascontiguousarray(a)).cuda()
+                                    for a in (p, u0, t0, tf, grid)], capi.SAVE_GRID,
+                        u_dtype="f32")
+    assert np.all(pinned["retcode"] == capi.RET_SUCCESS)
+    assert np.array_equal(pinned["u"], staged["u"])
+    assert np.array_equal(pinned["u"], d["u"].cpu().numpy())
