@@ -384,7 +384,7 @@ __device__ void integrate_team(const KArgs& a) {
           const double ts = save_time(a, i, js);
           const uint64_t ts_o = ord_bits(ts);
           if (ts_o > tnew_o) break;
-          store(js, (double)(ts_o == tnew_o ? alg.unew() : alg.interp(((ts - t) - tlo) / h, h)));
+          store(js, (double)(ts_o == tnew_o ? alg.unew() : alg.interp(((ts - t) - tlo) * rcp64(h), h)));
           ++js;
         }
         alg.accept();
@@ -418,7 +418,7 @@ __device__ void integrate_team(const KArgs& a) {
       if (a.naccept) a.naccept[i] = nacc;
       if (a.nreject) a.nreject[i] = nrej;
       if (a.nf) a.nf[i] = nfev;
-      if (a.t_end) a.t_end[i] = t + tlo;
+      if (a.t_end) a.t_end[i] = t;
       if (a.method_out) a.method_out[i] = Alg::ALG_ID;
       if (a.dt_first) a.dt_first[i] = dt1;
     }
@@ -1069,7 +1069,7 @@ __device__ void integrate_team8(const KArgs& a) {
     const double u0x = __ldg(a.u0 + (size_t)i * M::N + c0);
     const double u0y = __ldg(a.u0 + (size_t)i * M::N + c0 + 1);
     const T u0[2] = {(T)u0x, (T)u0y};
-    double t = __ldg(a.t0 + i), tlo = 0.0;
+    double t = __ldg(a.t0 + i);
     const double tf = __ldg(a.tf + i);
     int js = 0, nacc = 0, nrej = 0, nfev = 0;
     int64_t iters = 0;
@@ -1148,23 +1148,10 @@ __device__ void integrate_team8(const KArgs& a) {
       if (!a.adaptive || mag_bits(ms) <= 0x3FF0000000000000ull) {  // ms <= 1 (integer pipe)
         double dtnew = h;
         if (a.adaptive) dtnew = h * f2d_bits(ctl_accept(a.ctl, ms, lqold));
-        double tnew;
-        if (last) {
-          tnew = tf;
-          tlo = 0.0;
-        } else if (MIXED) {
-          // Fast2Sum on the operands ordered by magnitude (integer compare),
-          // as integrate_all
-          const bool tb = mag_bits(t) >= mag_bits(h);
-          const double big = tb ? t : h, small = tb ? h : t;
-          const double s = big + small;
-          double e = small - (s - big);
-          e += tlo;
-          tnew = s + e;
-          tlo = e - (tnew - s);
-        } else {
-          tnew = t + h;
-        }
+        // the step's end in plain FP64, as the FP64 oracle forms it (no
+        // compensated sum: it cost 6 FP64 additions per step on a pipe that
+        // runs at 1/64 of the FP32 rate)
+        const double tnew = last ? tf : t + h;
         const uint64_t tnew_o = ord_bits(tnew);
         while (js < a.n_save) {
           const double ts = save_time(a, i, js);
@@ -1174,7 +1161,7 @@ __device__ void integrate_team8(const KArgs& a) {
             store(js, (double)alg.unew()[0], (double)alg.unew()[1]);
           } else {
             T v[2];
-            alg.interp(((ts - t) - tlo) / h, h, v);
+            alg.interp((ts - t) * rcp64(h), h, v);
             store(js, (double)v[0], (double)v[1]);
           }
           ++js;
@@ -1212,7 +1199,7 @@ __device__ void integrate_team8(const KArgs& a) {
       if (a.naccept) a.naccept[i] = nacc;
       if (a.nreject) a.nreject[i] = nrej;
       if (a.nf) a.nf[i] = nfev;
-      if (a.t_end) a.t_end[i] = t + tlo;
+      if (a.t_end) a.t_end[i] = t;
       if (a.method_out) a.method_out[i] = Alg::ALG_ID;
       if (a.dt_first) a.dt_first[i] = dt1;
     }
