@@ -65,7 +65,9 @@ struct gbde_ctx {
   int num_sms = 0;
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
+  cudaStream_t aux = nullptr;       // GBDE_ALG_AUTO's second partition
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev_join = nullptr;    // aux -> stream
   std::mutex mu;
   std::string err;
   // staging for GBDE_MEM_HOST calls
@@ -173,6 +175,8 @@ int gbde_ctx_create(int device, gbde_ctx** out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     int r = set_err(nullptr, GBDE_ERR_CUDA, "context setup failed: %s", cudaGetErrorString(e));
     delete c;
@@ -194,6 +198,11 @@ int gbde_ctx_destroy(gbde_ctx* ctx) {
   ctx->scratch.release();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->aux) {
+    cudaStreamSynchronize(ctx->aux);
+    cudaStreamDestroy(ctx->aux);
+  }
   if (ctx->own) cudaStreamDestroy(ctx->own);
   delete ctx;
   return GBDE_OK;
@@ -323,14 +332,21 @@ static int solve_auto(gbde_ctx* ctx, Scratch& sc, const LaunchCfg& cfg, const KA
   unsigned cnt[2] = {0, 0};
   GBDE_CUDA(ctx, cudaMemcpyAsync(cnt, counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
   GBDE_CUDA(ctx, cudaStreamSynchronize(s));
+  // The stiff list first on the solve's stream, the non-stiff one on the
+  // auxiliary stream: its CTAs take the SMs the first kernel's tail leaves
+  // idle (each kernel alone fills the GPU).  The solve's stream then waits for
+  // both.  (Every earlier piece of work on the stream has completed: the
+  // list sizes were read back above.)
+  const bool two = cnt[0] > 0 && cnt[1] > 0 && ctx->aux != nullptr;
   const struct {
     int alg, precision;
     unsigned n;
     const int32_t* list;
     unsigned long long* queue;
-  } parts[2] = {{GBDE_ALG_TSIT5, cfg.precision, cnt[0], nonstiff, work},
-                {GBDE_ALG_RODAS5, cfg.precision == GBDE_PREC_FP64 ? GBDE_PREC_FP64 : GBDE_PREC_F32X2,
-                 cnt[1], stiff, work + 2}};
+    cudaStream_t st;
+  } parts[2] = {{GBDE_ALG_RODAS5, cfg.precision == GBDE_PREC_FP64 ? GBDE_PREC_FP64 : GBDE_PREC_F32X2,
+                 cnt[1], stiff, work + 2, s},
+                {GBDE_ALG_TSIT5, cfg.precision, cnt[0], nonstiff, work, two ? ctx->aux : s}};
   for (const auto& part : parts) {
     if (part.n == 0) continue;
     KArgs b = a;
@@ -346,12 +362,16 @@ static int solve_auto(gbde_ctx* ctx, Scratch& sc, const LaunchCfg& cfg, const KA
     }
     LaunchCfg c = cfg;
     c.precision = part.precision;
-    const cudaError_t e = launch_alg(part.alg, c, b, s);
+    const cudaError_t e = launch_alg(part.alg, c, b, part.st);
     if (e == cudaErrorNotSupported)
       return set_err(ctx, GBDE_ERR_UNSUPPORTED, "GBDE_ALG_AUTO is not built for model %d",
                      cfg.model);
     if (e != cudaSuccess)
       return set_err(ctx, GBDE_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+  }
+  if (two) {
+    GBDE_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->aux));
+    GBDE_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join, 0));
   }
   return GBDE_OK;
 }
