@@ -510,7 +510,7 @@ def run_vdp(args, de):
                    else "single GPU"},
         "chosen_form": {"persistent-f32x2": "persistent queue; Tsit5 and Rodas5 on 8-lane teams "
                         "in FP32 pairs (paired FP32 instructions) with an FP64 Jacobian, LU, "
-                        "error-norm accumulation and compensated time; FP32 output",
+                        "error-norm accumulation and time; FP32 output",
                         "persistent-mixed": "persistent queue; Tsit5 FP32 compensated state, "
                         "Rodas5 FP32 pairs on an FP64 LU; FP32 output",
                         "persistent": "persistent queue, FP64", "plain": "one launch, FP64"}[chosen],
@@ -590,7 +590,7 @@ def other_workload(de, name, N, seed):
         cfg = {"workload": "lorenz_tsit5_N%d" % N, "model": "lorenz", "alg": "tsit5",
                "reltol": 1e-8, "abstol": 1e-8, "saveat": "0:0.1:1 (11 points)",
                "chosen_form": "one launch, FP32-pair Tsit5 stepper (FP64 norm accumulation "
-                              "and compensated time)"}
+                              "and time)"}
         return (de.models.lorenz, p, u0, t0, tf, saveat, capi.SAVE_GRID, plain, chosen,
                 ("f64", "f64"), cfg, "weighted")
     if name in ("lv_em", "lv_sosri"):

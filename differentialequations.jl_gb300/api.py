@@ -331,10 +331,9 @@ class SRIW1(_Alg):
 class EnsembleGB300:
     """Ensemble algorithm that solves every trajectory on one GB300 GPU.
 
-    precision: "fp64", "mixed" (FP32 state/stages; FP64 compensated time,
-    error norm and W-matrix LU) or "f32x2" (state, stages and right-hand sides
-    as FP32 pairs of ~48 bits; FP64 Jacobian, LU, error norm and compensated
-    time).  batching: "plain" (one launch, a thread per trajectory) or
+    precision: "fp64", "mixed" (FP32 state/stages; FP64 time, error norm and
+    W-matrix LU) or "f32x2" (state, stages and right-hand sides as FP32 pairs
+    of ~48 bits; FP64 Jacobian, LU, error norm and time).  batching: "plain" (one launch, a thread per trajectory) or
     "persistent" (threads refill from a device work queue).  learned: False;
     True or "start" (the loaded predictor's first dt and AUTO method choice);
     "order" (the persistent queue ordered by the predicted cost); "stiff" (the

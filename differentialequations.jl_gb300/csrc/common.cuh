@@ -99,14 +99,6 @@ GBDE_HD bool val_finite(T x) {
 // FP32 values test directly: no conversion on the FP64 pipe
 GBDE_HD bool val_finite(float x) { return isfinite(x); }
 
-// Error-free sum (Knuth TwoSum): s + e == a + b exactly.  Used for the
-// compensated time accumulation of the mixed-precision path.
-GBDE_HD void two_sum(double a, double b, double& s, double& e) {
-  s = a + b;
-  double bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-
 // TwoSum in the working precision T (the FP32 path keeps its state as an
 // unevaluated sum hi + lo so that rounding does not accumulate over steps).
 template <class T>
@@ -115,18 +107,5 @@ GBDE_HD void two_sum_t(T a, T b, T& s, T& e) {
   T bb = s - a;
   e = (a - (s - bb)) + (b - bb);
 }
-
-// Compensated time: t = hi + lo.
-struct CTime {
-  double hi, lo;
-  GBDE_HD double value() const { return hi + lo; }
-  GBDE_HD void add(double dt) {
-    double s, e;
-    two_sum(hi, dt, s, e);
-    e += lo;
-    hi = s + e;
-    lo = e - (hi - s);
-  }
-};
 
 }  // namespace gbde

@@ -519,7 +519,7 @@ __device__ void sri_all(const KArgs& a) {
     ns.init(a.seed, (uint64_t)i);
     stk.sp = 0;
     int nfev = 0, nacc = 0, nrej = 0;
-    double t = t0, tlo = 0.0;
+    double t = t0;
     double h, dt1 = __longlong_as_double(0x7ff8000000000000ll);
     if (a.pred_dt != nullptr && a.pred_dt[i] > 0.f) {
       h = fmin((double)a.pred_dt[i], tf - t0);
@@ -602,22 +602,8 @@ __device__ void sri_all(const KArgs& a) {
       // ms <= 1 (ms >= 0; NaN rejects) and the other bookkeeping compares on
       // the integer pipe, as integrate_all
       if (!a.adaptive || mag_bits(ms) <= 0x3FF0000000000000ull) {
-        double tnew;
-        if (last) {
-          tnew = tf;
-          tlo = 0.0;
-        } else if (MIXED) {
-          // Fast2Sum on the operands ordered by magnitude
-          const bool tb = mag_bits(t) >= mag_bits(hs);
-          const double big = tb ? t : hs, small = tb ? hs : t;
-          const double s = big + small;
-          double e = small - (s - big);
-          e += tlo;
-          tnew = s + e;
-          tlo = e - (tnew - s);
-        } else {
-          tnew = t + hs;
-        }
+        // t + h in FP64 in every precision, as the FP64 oracle forms it
+        const double tnew = last ? tf : t + hs;
         const uint64_t tnew_o = ord_bits(tnew);
         while (js < a.n_save) {
           const double ts = save_time(a, i, js);
@@ -626,7 +612,7 @@ __device__ void sri_all(const KArgs& a) {
           if (ts_o == tnew_o) {
             store_state<N>(a, i, js, un);
           } else {
-            const T th = (T)(((ts - t) - tlo) / hs);
+            const T th = (T)((ts - t) / hs);
             T tmp[N];
 #pragma unroll
             for (int c = 0; c < N; ++c) tmp[c] = u[c] + th * (un[c] - u[c]);
@@ -662,7 +648,7 @@ __device__ void sri_all(const KArgs& a) {
         }
       }
     }
-    finish_sde<N, T>(a, i, ret, js, nacc, nrej, nfev, t + tlo, ALG, dt1);
+    finish_sde<N, T>(a, i, ret, js, nacc, nrej, nfev, t, ALG, dt1);
   }
 }
 

@@ -412,7 +412,7 @@ __device__ void integrate_all(const KArgs& a) {
   T p[M::NP];
   int64_t i = -1;
   bool active = false;
-  double t = 0.0, tlo = 0.0, tf = 0.0, dt = 0.0, dt1 = 0.0;
+  double t = 0.0, tf = 0.0, dt = 0.0, dt1 = 0.0;
   float lqold = 0.0f;  // log2(qold)
   int js = 0, nacc = 0, nrej = 0, nfev = 0;
   int64_t iters = 0;
@@ -430,7 +430,6 @@ __device__ void integrate_all(const KArgs& a) {
 #pragma unroll
       for (int c = 0; c < N; ++c) u0[c] = (T)__ldg(a.u0 + (size_t)i * N + c);
       t = __ldg(a.t0 + i);
-      tlo = 0.0;
       tf = __ldg(a.tf + i);
       js = 0;
       nacc = nrej = nfev = 0;
@@ -493,33 +492,14 @@ __device__ void integrate_all(const KArgs& a) {
         h = rem;
         last = true;
       }
-      // the step's end if the attempt is accepted (compensated in the
-      // mixed-precision path)
-      auto step_end = [&](double& tn, double& tl) {
-        if (last) {
-          tn = tf;
-          tl = 0.0;
-        } else if (MIXED) {
-          // Fast2Sum on the operands ordered by magnitude (integer compare):
-          // the same exact (s, e) as TwoSum with half the FP64 additions
-          const bool tb = mag_bits(t) >= mag_bits(h);
-          const double big = tb ? t : h, small = tb ? h : t;
-          const double s = big + small;
-          double e = small - (s - big);
-          e += tlo;
-          tn = s + e;
-          tl = e - (tn - s);
-        } else {
-          tn = t + h;
-          tl = tlo;
-        }
-      };
-      // Steppers that declare EARLY_TIME get it before the attempt, so that
-      // its dependent FP64 additions overlap the attempt's work: worth it
-      // where one warp runs alone on its SM sub-partition (small ensembles),
-      // at the cost of two registers live through the attempt.
-      double tnew_e = 0.0, tlo_e = 0.0;
-      if constexpr (early_time<Alg>::v) step_end(tnew_e, tlo_e);
+      // The step's end if the attempt is accepted: t + h in FP64, in every
+      // precision, as the FP64 oracle and the reference form it.  Steppers
+      // that declare EARLY_TIME get it before the attempt, so that its FP64
+      // addition overlaps the attempt's work: worth it where one warp runs
+      // alone on its SM sub-partition (small ensembles), at the cost of a
+      // register pair live through the attempt.
+      double tnew_e = 0.0;
+      if constexpr (early_time<Alg>::v) tnew_e = last ? tf : t + h;
       const double ms = alg.attempt(h, p, a.abstol, a.reltol, nfev);  // EEst^2
       ++iters;
       // ms <= 1 (ms >= 0; NaN rejects), compared on the integer pipe
@@ -528,14 +508,9 @@ __device__ void integrate_all(const KArgs& a) {
         // controller proposal for the next step
         double dtnew = h;
         if (a.adaptive) dtnew = h * f2d_bits(ctl_accept(ctl_of(alg, a), ms, lqold));
-        const double tlo0 = tlo;
         double tnew;
-        if constexpr (early_time<Alg>::v) {
-          tnew = tnew_e;
-          tlo = tlo_e;
-        } else {
-          step_end(tnew, tlo);
-        }
+        if constexpr (early_time<Alg>::v) tnew = tnew_e;
+        else tnew = last ? tf : t + h;
         // continuous callbacks: crossings of the conditions in (t, tnew]
         // (for the condition that fired at t, in (t + h/100, tnew]: the
         // repeat nudge); the earliest located root is the event
@@ -604,7 +579,7 @@ __device__ void integrate_all(const KArgs& a) {
         }
         // saveat: dense output at every save time in (t, tnew], or up to the
         // event
-        const double te = event ? t + (tlo0 + th_e * h) : tnew;
+        const double te = event ? t + th_e * h : tnew;
         const uint64_t tnew_o = ord_bits(tnew), lim_o = ord_bits(te);
         while (js < a.n_save) {
           const double ts = save_time(a, i, js);
@@ -614,7 +589,7 @@ __device__ void integrate_all(const KArgs& a) {
             store_state<N>(a, i, js, alg.unew());
           } else {
             T tmp[N];
-            alg.interp(((ts - t) - tlo) * rcp64(h), h, tmp, p, nfev);
+            alg.interp((ts - t) * rcp64(h), h, tmp, p, nfev);
             store_state<N>(a, i, js, tmp);
           }
           ++js;
@@ -627,7 +602,6 @@ __device__ void integrate_all(const KArgs& a) {
           if constexpr (CB::ND > 0) cb_discrete<CB, N, M::NP>(ue, te, p, term);
           alg.init(ue, p, nfev);
           t = te;
-          tlo = 0.0;
           nudge = idx_e;
           cb_conditions<CB, N, M::NP>(alg.u(), t, p, gprev);
           if (nacc == 0) dt1 = th_e * h;
@@ -688,7 +662,7 @@ __device__ void integrate_all(const KArgs& a) {
       if (a.naccept) a.naccept[i] = nacc;
       if (a.nreject) a.nreject[i] = nrej;
       if (a.nf) a.nf[i] = nfev;
-      if (a.t_end) a.t_end[i] = t + tlo;
+      if (a.t_end) a.t_end[i] = t;
       if (a.method_out) a.method_out[i] = method_of(alg);
       if (a.dt_first) a.dt_first[i] = dt1;
       active = false;

@@ -306,7 +306,7 @@ __device__ void integrate_team(const KArgs& a) {
     for (int k = 0; k < M::NP; ++k) p[k] = (T)__ldg(a.p + (size_t)i * M::NP + k);
     const double u0d = __ldg(a.u0 + (size_t)i * TEAM + tm.lane);
     const T u0 = (T)u0d;
-    double t = __ldg(a.t0 + i), tlo = 0.0;
+    double t = __ldg(a.t0 + i);
     const double tf = __ldg(a.tf + i);
     int js = 0, nacc = 0, nrej = 0, nfev = 0;
     int64_t iters = 0;
@@ -362,29 +362,13 @@ __device__ void integrate_team(const KArgs& a) {
       if (!a.adaptive || mag_bits(ms) <= 0x3FF0000000000000ull) {  // ms <= 1 (integer pipe)
         double dtnew = h;
         if (a.adaptive) dtnew = h * f2d_bits(ctl_accept(a.ctl, ms, lqold));
-        double tnew;
-        if (last) {
-          tnew = tf;
-          tlo = 0.0;
-        } else if (MIXED) {
-          // Fast2Sum on the operands ordered by magnitude (integer compare),
-          // as integrate_all
-          const bool tb = mag_bits(t) >= mag_bits(h);
-          const double big = tb ? t : h, small = tb ? h : t;
-          const double s = big + small;
-          double e = small - (s - big);
-          e += tlo;
-          tnew = s + e;
-          tlo = e - (tnew - s);
-        } else {
-          tnew = t + h;
-        }
+        const double tnew = last ? tf : t + h;  // plain FP64, as the oracle
         const uint64_t tnew_o = ord_bits(tnew);
         while (js < a.n_save) {
           const double ts = save_time(a, i, js);
           const uint64_t ts_o = ord_bits(ts);
           if (ts_o > tnew_o) break;
-          store(js, (double)(ts_o == tnew_o ? alg.unew() : alg.interp(((ts - t) - tlo) * rcp64(h), h)));
+          store(js, (double)(ts_o == tnew_o ? alg.unew() : alg.interp((ts - t) * rcp64(h), h)));
           ++js;
         }
         alg.accept();
@@ -1148,10 +1132,7 @@ __device__ void integrate_team8(const KArgs& a) {
       if (!a.adaptive || mag_bits(ms) <= 0x3FF0000000000000ull) {  // ms <= 1 (integer pipe)
         double dtnew = h;
         if (a.adaptive) dtnew = h * f2d_bits(ctl_accept(a.ctl, ms, lqold));
-        // the step's end in plain FP64, as the FP64 oracle forms it (no
-        // compensated sum: it cost 6 FP64 additions per step on a pipe that
-        // runs at 1/64 of the FP32 rate)
-        const double tnew = last ? tf : t + h;
+        const double tnew = last ? tf : t + h;  // plain FP64, as the oracle
         const uint64_t tnew_o = ord_bits(tnew);
         while (js < a.n_save) {
           const double ts = save_time(a, i, js);

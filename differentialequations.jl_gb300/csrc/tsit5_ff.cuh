@@ -18,8 +18,8 @@
 // GB300 issues one FP64 warp instruction per ~64 cycles on each SM
 // sub-partition.  In a small ensemble (one warp per sub-partition) every FP64
 // instruction of a step is therefore step latency; here only the norm's
-// accumulation and the driver's compensated time and step-size products stay
-// on that pipe.
+// accumulation and the driver's time and step-size products stay on that
+// pipe.
 #pragma once
 #include "ff_vec.cuh"
 #include "explicit_rk.cuh"
