@@ -11,8 +11,11 @@ namespace gbde {
 // Rodas steppers are latency-bound on their broadcast chains (LU, triangular
 // solves), so more resident warps beat more registers.  With W's rows in
 // shared memory (team.cuh, 17 KB per CTA) the 16-lane Rodas steppers fit 6
-// CTAs (<= 80 registers, no spills).  The 8-lane pair Rodas holds 48 KB of
-// shared memory per CTA (W rows and stages of 16 trajectories), so 4 CTAs.
+// CTAs (<= 80 registers, no spills).  The 8-lane pair Rodas holds 3 KB of
+// shared memory per trajectory (W rows and stages): CTAs of 96 threads (12
+// teams, 36.9 KB), 6 per SM, 96 registers -- 374 ms on the 250k stiff
+// trajectories against 377 ms with 128-thread CTAs at 4 per SM (48 KB, 125
+// registers) and 392 ms with 96 x 5.
 // The 8-lane Tsit5 teams measured 368 / 338 / 290 / 280 ms at 1 / 4 / 5 / 6
 // CTAs per SM on the 750k non-stiff trajectories of the 1M ring workload.
 template <class Alg> struct TeamMinBlocks { static constexpr int v = 1; };
@@ -26,7 +29,13 @@ template <class M> struct TeamMinBlocks<TeamTsit5FF<M>> {
   static constexpr int v = 6;
 };
 template <class M, class Tag> struct TeamMinBlocks<TeamRodasFF8<M, Tag>> {
-  static constexpr int v = 4;
+  static constexpr int v = 6;
+};
+// Threads per CTA a team kernel is compiled for (its launch's block size
+// at most): 128, but the pair Rodas's kTeam8Threads (team.cuh)
+template <class Alg> struct TeamThreads { static constexpr int v = 128; };
+template <class M, class Tag> struct TeamThreads<TeamRodasFF8<M, Tag>> {
+  static constexpr int v = kTeam8Threads;
 };
 
 template <class Alg, class M, class T, bool MIXED>
@@ -36,7 +45,7 @@ __global__ void __launch_bounds__(128, TeamMinBlocks<Alg>::v) k_team(const KArgs
 
 // 8-lane teams, one oscillator per lane (team.cuh)
 template <class Alg, class M, class T, bool MIXED>
-__global__ void __launch_bounds__(128, TeamMinBlocks<Alg>::v) k_team8(const KArgs a) {
+__global__ void __launch_bounds__(TeamThreads<Alg>::v, TeamMinBlocks<Alg>::v) k_team8(const KArgs a) {
   integrate_team8<Alg, M, T, MIXED>(a);
 }
 
@@ -44,8 +53,11 @@ __global__ void __launch_bounds__(128, TeamMinBlocks<Alg>::v) k_team8(const KArg
 // 16-lane teams (TeamRodas).
 template <class Tag, class M>
 static cudaError_t launch_team_rodas(const LaunchCfg& cfg, const KArgs& a, cudaStream_t s) {
-  if (cfg.precision == GBDE_PREC_F32X2)
-    return launch_team_kernel(k_team8<TeamRodasFF8<M, Tag>, M, ff, true>, cfg, a, s, 8);
+  if (cfg.precision == GBDE_PREC_F32X2) {
+    LaunchCfg c = cfg;  // its shared arrays hold kTeam8Threads threads' teams
+    if (c.block <= 0 || c.block > kTeam8Threads) c.block = kTeam8Threads;
+    return launch_team_kernel(k_team8<TeamRodasFF8<M, Tag>, M, ff, true>, c, a, s, 8);
+  }
   if (cfg.precision == GBDE_PREC_MIXED)
     return launch_team_kernel(k_team<TeamRodas<M, float, Tag>, M, float, true>, cfg, a, s);
   return launch_team_kernel(k_team<TeamRodas<M, double, Tag>, M, double, false>, cfg, a, s);

@@ -684,10 +684,12 @@ struct TeamTsit5FF {
 // of every stage, so a warp carries 4 trajectories and the pair arithmetic of
 // a lane's two components runs on paired FP32 instructions (FfAcc2, FfVec<2>).
 // Same method, pivot order and FP64 factorisation as TeamLU / TeamRodas.
-constexpr int kTeam8Threads = 128;  // CTA size the shared arrays are sized for
+// CTA size of the 8-lane pair Rodas kernel, which its shared arrays are sized
+// for: 12 teams, 36.9 KB (W rows 26.1 KB, stages 10.8 KB), 6 CTAs per SM
+constexpr int kTeam8Threads = 96;
 
 // W of this team: 16 rows of 17 doubles (the stride keeps a team's row
-// accesses conflict-free).  16 teams per CTA: 34,816 bytes.  Row i sits in
+// accesses conflict-free), 2,176 bytes per team.  Row i sits in
 // slot i at even team positions and in slot i + 1 (mod 16) at odd ones: the
 // two teams of a half-warp then read their rows at the same column through
 // disjoint banks (an even team at word offsets 4l + 2k (mod 32) for lane l,
@@ -869,7 +871,7 @@ struct TeamRodasFF8 {
   }
 
   // stages u_1..u_7 of this lane's two components: one 16-byte (hi pair, lo
-  // pair) slot per stage at stride kTeam8Threads (14,336 bytes per CTA)
+  // pair) slot per stage at stride kTeam8Threads
   GBDE_D static ulonglong2* stages() {
     __shared__ ulonglong2 buf[7 * kTeam8Threads];
     return buf + threadIdx.x;
