@@ -779,71 +779,98 @@ struct TeamLU8 {
   }
 };
 
-// The factors of a TeamLU8 as pairs for the solves: each lane's two rows
-// negated, written as pairs over their FP64 entries in shared memory, and the
-// pivot reciprocals split on the integer pipe.  Forward and back substitution
-// keep a lane's two right-hand-side components in one paired accumulator.
+// The factors of a TeamLU8 as pairs for the solves, in pivot order: the row
+// that was the pivot of step k (its L part in columns < k, U in columns > k)
+// goes to slot k, i.e. lane k / 2, half k % 2 -- the row order of LAPACK's
+// row-swapping factorisation.  Each entry is negated and split to a pair on
+// the integer pipe as it moves; each slot keeps its pivot reciprocal.  With
+// the slots in step order, the source of every step of the substitutions is
+// lane k / 2, half k % 2, known from k: no pivot lookups, and the two halves'
+// selects fold at compile time.  Forward and back substitution keep a lane's
+// two slots in one paired accumulator.
 struct TeamLUFF8 {
-  ff invp[2];
-  int step[2];
-  uint64_t piv;
+  ff invs[2];  // pivot reciprocals of this lane's slots 2l, 2l + 1
+  int q[2];    // the rows in them (their right-hand-side components)
 
   GBDE_D static float2* row_ff(int i) { return reinterpret_cast<float2*>(team8_row(i)); }
   GBDE_D void from(const TeamLU8& W, const Team8& tm) {
-    double* a0 = team8_row(2 * tm.lane);
-    double* a1 = team8_row(2 * tm.lane + 1);
-    float2* n0 = reinterpret_cast<float2*>(a0);
-    float2* n1 = reinterpret_cast<float2*>(a1);
-#pragma unroll 4
-    for (int c = 0; c < TEAM; ++c) {
-      const ff x0 = ff_split(a0[c]), x1 = ff_split(a1[c]);
-      n0[c] = make_float2(-x0.hi, -x0.lo);
-      n1[c] = make_float2(-x1.hi, -x1.lo);
+    const int l = tm.lane;
+    q[0] = (int)((W.piv >> (8 * l)) & 15u);
+    q[1] = (int)((W.piv >> (8 * l + 4)) & 15u);
+    const double* r0 = team8_row(q[0]);
+    const double* r1 = team8_row(q[1]);
+    // the reciprocal of each slot's diagonal, as factor() formed it
+    invs[0] = ff_split(rcp64(r0[2 * l]));
+    invs[1] = ff_split(rcp64(r1[2 * l + 1]));
+    // slot rows 2l, 2l + 1 receive rows q0, q1, four columns at a time: every
+    // lane reads its columns before any lane overwrites them
+    float2* d0 = row_ff(2 * l);
+    float2* d1 = row_ff(2 * l + 1);
+#pragma unroll 1
+    for (int c0 = 0; c0 < TEAM; c0 += 4) {
+      double v0[4], v1[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        v0[c] = r0[c0 + c];
+        v1[c] = r1[c0 + c];
+      }
+      __syncwarp(tm.mask);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const ff x0 = ff_split(v0[c]), x1 = ff_split(v1[c]);
+        d0[c0 + c] = make_float2(-x0.hi, -x0.lo);
+        d1[c0 + c] = make_float2(-x1.hi, -x1.lo);
+      }
+      __syncwarp(tm.mask);
     }
-    invp[0] = ff_split(W.invp[0]);
-    invp[1] = ff_split(W.invp[1]);
-    step[0] = W.step[0];
-    step[1] = W.step[1];
-    piv = W.piv;
   }
-  // W x = b for this lane's components b[0], b[1] (rows 2l, 2l + 1); x[0],
-  // x[1] are unknowns 2l, 2l + 1.  A row that takes no update at step k
-  // (k outside its L or U part) adds a zero product.  The pivot rows are read
-  // off a running copy of piv (constant shifts).
+
+  // W x = b for this lane's components b[0], b[1] (x[0], x[1]: unknowns 2l,
+  // 2l + 1).  Slot s's accumulator starts from b of its row q_s.  Step k
+  // (source lane k / 2) updates the slots after k in the forward pass and
+  // those before k in the backward pass; a slot that takes no update adds a
+  // zero product.  The loops run over pairs of steps (2s, 2s + 1).
   GBDE_D void solve(const ff* b, ff* x, const Team8& tm) const {
-    const float2* n0 = row_ff(2 * tm.lane);
-    const float2* n1 = row_ff(2 * tm.lane + 1);
+    const int l = tm.lane;
+    const float2* n0 = row_ff(2 * l);
+    const float2* n1 = row_ff(2 * l + 1);
     FfAcc2 acc;
-    acc.set(f2_pack(b[0].hi, b[1].hi), f2_pack(b[0].lo, b[1].lo));
-    uint64_t pv = piv;
-#pragma unroll 4  // pair solve
-    for (int k = 0; k < TEAM; ++k) {  // forward: L z = P b
-      const int p = (int)(pv & 15u);
-      pv >>= 4;
-      ff g0, g1;
-      acc.get(g0, g1);
-      const ff z = tm.bcast((p & 1) ? g1 : g0, p >> 1);
-      const float2 v0 = n0[k], v1 = n1[k];
-      const bool e0 = step[0] > k, e1 = step[1] > k;
+    {
+      const ff a0 = tm.bcast(b[0], q[0] >> 1), a1 = tm.bcast(b[1], q[0] >> 1);
+      const ff c0 = tm.bcast(b[0], q[1] >> 1), c1 = tm.bcast(b[1], q[1] >> 1);
+      const ff s0 = (q[0] & 1) ? a1 : a0, s1 = (q[1] & 1) ? c1 : c0;
+      acc.set(f2_pack(s0.hi, s1.hi), f2_pack(s0.lo, s1.lo));
+    }
+    auto update = [&](ff z, float2 v0, float2 v1, bool e0, bool e1) {
       acc.fma(f2_pack(z.hi, z.hi), f2_pack(z.lo, z.lo), f2_pack(-z.hi, -z.hi),
               f2_pack(e0 ? v0.x : 0.0f, e1 ? v1.x : 0.0f),
               f2_pack(e0 ? v0.y : 0.0f, e1 ? v1.y : 0.0f));
-    }
-    pv = piv;
-#pragma unroll 4  // pair solve
-    for (int k = TEAM - 1; k >= 0; --k) {  // backward: U x = z
-      const int p = (int)(pv >> 60);
-      pv <<= 4;
+    };
+#pragma unroll 2  // pair solve
+    for (int sl = 0; sl < TEAM8; ++sl) {  // forward: L z = P b, steps 2 sl, 2 sl + 1
+      const bool gt = l > sl, ge = l >= sl;
       ff g0, g1;
       acc.get(g0, g1);
-      const ff xk = tm.bcast(((p & 1) ? g1 : g0) * ((p & 1) ? invp[1] : invp[0]), p >> 1);
-      const float2 v0 = n0[k], v1 = n1[k];
-      const bool e0 = step[0] < k, e1 = step[1] < k;
-      acc.fma(f2_pack(xk.hi, xk.hi), f2_pack(xk.lo, xk.lo), f2_pack(-xk.hi, -xk.hi),
-              f2_pack(e0 ? v0.x : 0.0f, e1 ? v1.x : 0.0f),
-              f2_pack(e0 ? v0.y : 0.0f, e1 ? v1.y : 0.0f));
-      if (k == 2 * tm.lane) x[0] = xk;
-      if (k == 2 * tm.lane + 1) x[1] = xk;
+      const ff za = tm.bcast(g0, sl);  // step 2 sl: slot 2 sl
+      update(za, n0[2 * sl], n1[2 * sl], gt, ge);
+      acc.get(g0, g1);
+      const ff zb = tm.bcast(g1, sl);  // step 2 sl + 1: slot 2 sl + 1
+      update(zb, n0[2 * sl + 1], n1[2 * sl + 1], gt, gt);
+    }
+#pragma unroll 2  // pair solve
+    for (int sl = TEAM8 - 1; sl >= 0; --sl) {  // backward: U x = z, steps 2 sl + 1, 2 sl
+      const bool lt = l < sl, le = l <= sl, own = l == sl;
+      ff g0, g1;
+      acc.get(g0, g1);
+      const ff xb = tm.bcast(g1 * invs[1], sl);  // step 2 sl + 1
+      update(xb, n0[2 * sl + 1], n1[2 * sl + 1], le, lt);
+      acc.get(g0, g1);
+      const ff xa = tm.bcast(g0 * invs[0], sl);  // step 2 sl
+      update(xa, n0[2 * sl], n1[2 * sl], lt, lt);
+      if (own) {
+        x[0] = xa;
+        x[1] = xb;
+      }
     }
   }
 };
