@@ -70,7 +70,8 @@ class Outputs(C.Structure):
         ("naccept", C.c_void_p), ("nreject", C.c_void_p), ("nf", C.c_void_p),
         ("t_end", C.c_void_p), ("method", C.c_void_p),
         ("device_ms", C.c_float), ("total_ms", C.c_float), ("dt_first", C.c_void_p),
-        ("reduce", C.c_void_p),
+        ("reduce", C.c_void_p), ("ev_t", C.c_void_p), ("ev_u", C.c_void_p),
+        ("ev_count", C.c_void_p), ("ev_capacity", C.c_int32),
     ]
 
 
@@ -97,12 +98,13 @@ class Summary(C.Structure):
 
 
 CB_CONTINUOUS, CB_DISCRETE, CB_VECTOR = 1, 2, 3
+SAVE_BEFORE, SAVE_AFTER = 1, 2
 MAX_CB_CONDITIONS = 64
 
 
 class Callback(C.Structure):
     _fields_ = [("kind", C.c_int32), ("condition", C.c_char_p), ("affect", C.c_char_p),
-                ("terminate", C.c_int32)]
+                ("terminate", C.c_int32), ("save_positions", C.c_int32)]
 
 
 class UserModel(C.Structure):

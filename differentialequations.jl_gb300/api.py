@@ -119,12 +119,18 @@ def compile_model(model, alg, precision="fp64"):
     capi.check(capi.lib().gbde_model_compile(model.id, alg.alg_id, prec))
 
 
+def _save_bits(save_positions):
+    before, after = save_positions
+    return (capi.SAVE_BEFORE if before else 0) | (capi.SAVE_AFTER if after else 0)
+
+
 class _Callback:
-    def __init__(self, kind, condition, affect, terminate, len=1):
+    def __init__(self, kind, condition, affect, terminate, len=1, save_positions=(True, True)):
         import ctypes as C
+        bits = _save_bits(save_positions)
         d = capi.Callback(kind=kind, condition=condition.encode(),
-                          affect=affect.encode() if affect else None,
-                          terminate=int(bool(terminate)))
+                          affect=affect.encode() if affect is not None else None,
+                          terminate=int(bool(terminate)), save_positions=bits)
         cid = C.c_int32()
         if kind == capi.CB_VECTOR:
             capi.check(capi.lib().gbde_vector_callback_register(C.byref(d), int(len),
@@ -133,33 +139,51 @@ class _Callback:
             capi.check(capi.lib().gbde_callback_register(C.byref(d), C.byref(cid)))
         self.id, self.kind, self.len = cid.value, kind, int(len)
         self.condition, self.affect, self.terminate = condition, affect, terminate
+        self.save_positions = tuple(bool(x) for x in save_positions)
+        # the saves the kernels make: a continuous callback without an affect
+        # leaves u unmodified and saves nothing after it
+        modifies = kind == capi.CB_DISCRETE or affect is not None or terminate
+        self.save_bits = bits if modifies else bits & capi.SAVE_BEFORE
 
 
 class ContinuousCallback(_Callback):
-    """ContinuousCallback(condition, affect=None; terminate=False) (qa.jl:24).
+    """ContinuousCallback(condition, affect=None; terminate=False,
+    save_positions=(True, True)) (qa.jl:24).
 
     condition: CUDA C++ statements setting `g` (double) from `u` (the state,
     const double*), `t` and `p`; an event is a sign change of g, located on
     the method's dense output, where the trajectory stops (left of the root),
     runs affect (statements modifying `u[i]`, may set `terminate = true`) and
-    restarts.  Example: ContinuousCallback("g = t - 0.5;")."""
+    restarts.  Example: ContinuousCallback("g = t - 0.5;").
 
-    def __init__(self, condition, affect=None, terminate=False):
-        super().__init__(capi.CB_CONTINUOUS, condition, affect, terminate)
+    save_positions: save (t, u) at the event before / after the affect (the
+    reference's keyword and default).  These saves join the saveat points in
+    each trajectory's solution (sol[i].t, sol[i].u; the ensemble's U array
+    holds the saveat points only).  affect=None (the reference's `nothing`)
+    leaves u unmodified and saves nothing after the event; affect="" is a
+    no-op affect, like a Julia function that does nothing."""
+
+    def __init__(self, condition, affect=None, terminate=False, save_positions=(True, True)):
+        super().__init__(capi.CB_CONTINUOUS, condition, affect, terminate,
+                         save_positions=save_positions)
 
 
 class DiscreteCallback(_Callback):
-    """DiscreteCallback(condition, affect=None; terminate=False) (qa.jl:36):
-    after every accepted step, g != 0 runs affect.
+    """DiscreteCallback(condition, affect=None; terminate=False,
+    save_positions=(True, True)) (qa.jl:36): after every accepted step, g != 0
+    runs affect, with saves of (t, u) before and after it as save_positions
+    asks (the one before is skipped when a saveat point falls on t).
     Example: DiscreteCallback("g = t >= 0.5;")."""
 
-    def __init__(self, condition, affect=None, terminate=False):
-        super().__init__(capi.CB_DISCRETE, condition, affect, terminate)
+    def __init__(self, condition, affect=None, terminate=False, save_positions=(True, True)):
+        super().__init__(capi.CB_DISCRETE, condition, affect, terminate,
+                         save_positions=save_positions)
 
 
 class VectorContinuousCallback(_Callback):
-    """VectorContinuousCallback(condition, affect, len; terminate=False)
-    (qa.jl:124): len continuous conditions in one callback.
+    """VectorContinuousCallback(condition, affect, len; terminate=False,
+    save_positions=(True, True)) (qa.jl:124): len continuous conditions in
+    one callback, with the event saves of ContinuousCallback.
 
     condition: CUDA C++ statements setting `out[0..len-1]` (double*) from
     `u`, `t` and `p`; the earliest sign change among them is the event, and
@@ -168,8 +192,9 @@ class VectorContinuousCallback(_Callback):
     VectorContinuousCallback("out[0] = u[0]; out[1] = u[2];",
                              "u[2 * idx + 1] = -0.9 * u[2 * idx + 1];", 2)."""
 
-    def __init__(self, condition, affect=None, len=1, terminate=False):
-        super().__init__(capi.CB_VECTOR, condition, affect, terminate, len)
+    def __init__(self, condition, affect=None, len=1, terminate=False,
+                 save_positions=(True, True)):
+        super().__init__(capi.CB_VECTOR, condition, affect, terminate, len, save_positions)
 
 
 class CallbackSet:
@@ -189,6 +214,9 @@ class CallbackSet:
         sid = C.c_int32()
         capi.check(capi.lib().gbde_callback_set_register(ids, len(callbacks), C.byref(sid)))
         self.id, self.callbacks = sid.value, tuple(callbacks)
+        self.save_bits = 0
+        for cb in callbacks:
+            self.save_bits |= cb.save_bits
 
 
 # -------------------------------------------------------------- problems
@@ -431,8 +459,9 @@ class EnsembleSolution:
     solutions; `U`, `t`, `retcode` expose the underlying arrays."""
 
     def __init__(self, U, t, retcode, lengths, stats, elapsed_ms, device_ms, output_func=None,
-                 reduction=None, probs=None, dense=None):
-        self.U = U                  # (N, n_save, n_state)
+                 reduction=None, probs=None, dense=None, events=None):
+        self.U = U                  # (N, n_save, n_state): the saveat points
+        self.events = events        # (ev_t, ev_u, ev_count) of the callbacks' saves, or None
         self.t = t                  # (n_save,) or (N, n_save)
         self.retcode = retcode      # (N,) int32
         self.lengths = lengths      # (N,) stored points per trajectory
@@ -449,11 +478,22 @@ class EnsembleSolution:
     def solution(self, i):
         n = int(self.lengths[i])
         t = self.t[:n] if self.t.ndim == 1 else self.t[i, :n]
+        u = self.U[i, :n]
+        if self.events is not None and int(self.events[2][i]) > 0:
+            # the saveat points and the event saves in time order; at one
+            # time the saveat points first, then the event saves as made
+            ev_t, ev_u, ev_n = self.events
+            c = int(ev_n[i])
+            tt = np.concatenate([np.asarray(t, np.float64), np.asarray(ev_t[i, :c])])
+            kind = np.r_[np.zeros(n, np.int8), np.ones(c, np.int8)]
+            order = np.lexsort((np.arange(n + c), kind, tt))
+            t = tt[order]
+            u = np.concatenate([np.asarray(u), np.asarray(ev_u[i, :c])])[order]
         st = {k: v[i] for k, v in self.stats.items()}
         dense = None
         if self._dense is not None:
             dense = (lambda ts, i=i: self._dense(i, ts))
-        return ODESolution(t, self.U[i, :n], self.retcode[i],
+        return ODESolution(t, u, self.retcode[i],
                            None if self._probs is None else self._probs[i], st, dense)
 
     def __getitem__(self, i):
@@ -610,6 +650,9 @@ def _gather_inputs(ens, N):
     return u0, p, tspan, saves, probs
 
 
+_EVENT_SAVES_GUESS = 8  # event saves per trajectory room of a callback solve's first try
+
+
 def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start=None,
           save_end=None, reltol=None, abstol=None, dt=None, adaptive=None, maxiters=None,
           dtmin=None, dtmax=None, seed=0, **kwargs):
@@ -721,14 +764,24 @@ def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start
     opts.chunk = int(ensemblealg.chunk)
     opts.timeout_s = float(ensemblealg.timeout_s)
 
-    if len(ensemblealg.devices) > 1:
-        from . import distributed
-        res = distributed.solve_sharded(solve_arrays, ensemblealg.devices, prob.f, opts, p, u0,
-                                        t0, tf, save_arr, save_kind,
-                                        u_dtype=ensemblealg.out_dtype)
-    else:
-        res = solve_arrays(prob.f, opts, p, u0, t0, tf, save_arr, save_kind,
-                           u_dtype=ensemblealg.out_dtype, device=ensemblealg.devices[0])
+    def run(events):
+        if len(ensemblealg.devices) > 1:
+            from . import distributed
+            return distributed.solve_sharded(solve_arrays, ensemblealg.devices, prob.f, opts, p,
+                                             u0, t0, tf, save_arr, save_kind,
+                                             u_dtype=ensemblealg.out_dtype, events=events)
+        return solve_arrays(prob.f, opts, p, u0, t0, tf, save_arr, save_kind,
+                            u_dtype=ensemblealg.out_dtype, device=ensemblealg.devices[0],
+                            events=events)
+
+    # saves at callback events: a first guess of their number per trajectory;
+    # a trajectory that made more has them all counted, and the ensemble is
+    # solved again with room for the largest count (same steps, same results)
+    events = _EVENT_SAVES_GUESS if cb is not None and cb.save_bits else None
+    res = run(events)
+    if events is not None and N and int(res["ev_count"].max()) > events:
+        events = int(res["ev_count"].max())
+        res = run(events)
     t_out = save_arr
     term = res["retcode"] == capi.RET_TERMINATED
     if np.any(term):
@@ -747,9 +800,11 @@ def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start
                              capi.SAVE_GRID, u_dtype=ensemblealg.out_dtype, device=dev)
             return np.asarray(r["u"][0], np.float64)
 
+    ev = None if events is None else (res["ev_t"], res["ev_u"], res["ev_count"])
     sol = EnsembleSolution(res["u"], t_out, res["retcode"], lengths,
                            {k: res[k] for k in ("naccept", "nreject", "nf", "t_end")},
-                           res["total_ms"], res["device_ms"], probs=probs, dense=dense)
+                           res["total_ms"], res["device_ms"], probs=probs, dense=dense,
+                           events=ev)
     if ens.output_func is not None:
         outs = []
         for i in range(N):
@@ -762,13 +817,18 @@ def solve(ens, alg, ensemblealg=None, trajectories=None, saveat=None, save_start
 
 
 def solve_arrays(model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", device=0,
-                 out=None, stats=True, reduce=False, store_u=True):
+                 out=None, stats=True, reduce=False, store_u=True, events=None):
     """Low-level entry: arrays in, arrays out, one gbde_ensemble_solve call.
 
     reduce=True accumulates, inside the step kernels, the sums over
     trajectories of every saved state and of its square (gbde_outputs.reduce),
     returned as res["reduce"] [2][n_save][n_state] with res["mean"] and
     res["var"] (N - 1); store_u=False then skips storing the ensemble.
+
+    events=K (a solve with opts.callback) keeps up to K saves at callback
+    events per trajectory (the callbacks' save_positions): res["ev_t"] [N][K],
+    res["ev_u"] [N][K][n_state] and res["ev_count"] [N], which counts every
+    save made, also those beyond K.
 
     Host numpy arrays -> GBDE_MEM_HOST (the call stages the copies).
     CUDA torch tensors -> GBDE_MEM_DEVICE on the tensors' device and the
@@ -823,6 +883,19 @@ def solve_arrays(model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", d
             res["t_end"] = np.empty(N, np.float64)
             res["dt_first"] = np.empty(N, np.float64)
         ctx.set_stream(0)
+    if events is not None:
+        cap = int(events)
+        if on_device:
+            res.setdefault("ev_t", torch.empty((N, cap), dtype=torch.float64, device=dev))
+            res.setdefault("ev_u", torch.empty((N, cap, model.n_state), dtype=tdt, device=dev))
+            res.setdefault("ev_count", torch.empty(N, dtype=torch.int32, device=dev))
+        else:
+            res.setdefault("ev_t", np.empty((N, cap), np.float64))
+            res.setdefault("ev_u", np.empty((N, cap, model.n_state),
+                                            np.float32 if u_dtype == "f32" else np.float64))
+            res.setdefault("ev_count", np.empty(N, np.int32))
+        outs.ev_t, outs.ev_u = capi.ptr(res["ev_t"]), capi.ptr(res["ev_u"])
+        outs.ev_count, outs.ev_capacity = capi.ptr(res["ev_count"]), cap
     prob.p, prob.u0, prob.t0, prob.tf, prob.saveat = [capi.ptr(a) for a in arrs]
     outs.u = capi.ptr(res["u"])
     outs.retcode = capi.ptr(res["retcode"])

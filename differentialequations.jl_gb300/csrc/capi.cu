@@ -77,6 +77,7 @@ struct gbde_ctx {
   DevBuf mlp_net;     // learned predictor (GBDE_MLP_NET_FLOATS floats)
   DevBuf summary, summary_io;  // gbde_ensemble_summary: scratch; staged outputs (host mode)
   DevBuf red;         // staged in-kernel reduction (host mode)
+  DevBuf evt, evu, evn;  // staged event saves (host mode)
   int mlp_model = 0;  // model the loaded predictor belongs to (0 = none)
 };
 
@@ -193,7 +194,8 @@ int gbde_ctx_destroy(gbde_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf* b : {&ctx->p, &ctx->u0, &ctx->t0, &ctx->tf, &ctx->saveat, &ctx->u, &ctx->ret,
                     &ctx->nacc, &ctx->nrej, &ctx->nf, &ctx->tend, &ctx->method, &ctx->dt1,
-                    &ctx->mlp_net, &ctx->summary, &ctx->summary_io, &ctx->red})
+                    &ctx->mlp_net, &ctx->summary, &ctx->summary_io, &ctx->red, &ctx->evt,
+                    &ctx->evu, &ctx->evn})
     b->release();
   ctx->scratch.release();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -405,6 +407,8 @@ static int check_solve_args(gbde_ctx* ctx, const gbde_problem* prob, const gbde_
                    "out->retcode must be non-NULL, and out->u or out->reduce");
   if (out->u_dtype != GBDE_F64 && out->u_dtype != GBDE_F32)
     return set_err(ctx, GBDE_ERR_INVALID, "u_dtype must be GBDE_F64 or GBDE_F32");
+  if (opts->callback != 0 && out->ev_count && out->ev_capacity < 0)
+    return set_err(ctx, GBDE_ERR_INVALID, "ev_capacity must be >= 0");
   const int alg = opts->alg;
   if (!is_ode_alg(alg) && !is_sde_alg(alg))
     return set_err(ctx, GBDE_ERR_INVALID, "unknown algorithm id %d", alg);
@@ -522,6 +526,9 @@ static void fill_common(KArgs& a, const gbde_problem* prob, const gbde_opts* opt
   a.chunk = opts->chunk > 0 ? opts->chunk : 1;
 }
 
+// the event-save outputs are in use (the kernels take them only with a callback)
+static bool event_saves(const gbde_outputs* out) { return out->ev_count != nullptr; }
+
 static void fill_device_ptrs(KArgs& a, const gbde_problem* prob, const gbde_outputs* out) {
   a.p = prob->p;
   a.u0 = prob->u0;
@@ -537,6 +544,12 @@ static void fill_device_ptrs(KArgs& a, const gbde_problem* prob, const gbde_outp
   a.method_out = out->method;
   a.dt_first = out->dt_first;
   a.red = out->reduce;
+  if (event_saves(out)) {
+    a.ev_t = out->ev_t;
+    a.ev_u = out->ev_u;
+    a.ev_n = out->ev_count;
+    a.ev_cap = out->ev_capacity;
+  }
 }
 
 static LaunchCfg make_cfg(const gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts* opts) {
@@ -652,6 +665,7 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
   KArgs a;
   fill_common(a, prob, opts, out);
   const bool host = prob->mem == GBDE_MEM_HOST;
+  const bool ev = opts->callback != 0 && event_saves(out);
   void* u_direct = nullptr;
   if (host) {
     GBDE_CUDA(ctx, ctx->p.ensure((size_t)N * np * 8));
@@ -690,6 +704,14 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
     if (out->t_end) { GBDE_CUDA(ctx, ctx->tend.ensure((size_t)N * 8)); a.t_end = (double*)ctx->tend.ptr; }
     if (out->method) { GBDE_CUDA(ctx, ctx->method.ensure((size_t)N * 4)); a.method_out = (int32_t*)ctx->method.ptr; }
     if (out->dt_first) { GBDE_CUDA(ctx, ctx->dt1.ensure((size_t)N * 8)); a.dt_first = (double*)ctx->dt1.ptr; }
+    if (ev) {
+      const size_t slots = (size_t)N * (size_t)out->ev_capacity;
+      GBDE_CUDA(ctx, ctx->evn.ensure((size_t)N * 4));
+      a.ev_n = (int32_t*)ctx->evn.ptr;
+      a.ev_cap = out->ev_capacity;
+      if (out->ev_t && slots) { GBDE_CUDA(ctx, ctx->evt.ensure(slots * 8)); a.ev_t = (double*)ctx->evt.ptr; }
+      if (out->ev_u && slots) { GBDE_CUDA(ctx, ctx->evu.ensure(slots * ns * esz)); a.ev_u = ctx->evu.ptr; }
+    }
   } else {
     fill_device_ptrs(a, prob, out);
   }
@@ -714,6 +736,12 @@ int gbde_ensemble_solve(gbde_ctx* ctx, const gbde_problem* prob, const gbde_opts
       if (out->t_end) GBDE_CUDA(ctx, cudaMemcpyAsync(out->t_end, a.t_end, (size_t)N * 8, cudaMemcpyDeviceToHost, s));
       if (out->method) GBDE_CUDA(ctx, cudaMemcpyAsync(out->method, a.method_out, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
       if (out->dt_first) GBDE_CUDA(ctx, cudaMemcpyAsync(out->dt_first, a.dt_first, (size_t)N * 8, cudaMemcpyDeviceToHost, s));
+      if (ev) {
+        const size_t slots = (size_t)N * (size_t)out->ev_capacity;
+        GBDE_CUDA(ctx, cudaMemcpyAsync(out->ev_count, a.ev_n, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
+        if (a.ev_t) GBDE_CUDA(ctx, cudaMemcpyAsync(out->ev_t, a.ev_t, slots * 8, cudaMemcpyDeviceToHost, s));
+        if (a.ev_u) GBDE_CUDA(ctx, cudaMemcpyAsync(out->ev_u, a.ev_u, slots * ns * esz, cudaMemcpyDeviceToHost, s));
+      }
     }
   }
   GBDE_CUDA(ctx, cudaMemcpyAsync(&flag, a.flag, 4, cudaMemcpyDeviceToHost, s));

@@ -111,6 +111,8 @@ struct UserModelDef {
 // len conditions for a vector one) or a set (kind 0) of earlier ids.
 struct CallbackDef {
   int kind = 0, len = 1;
+  int save = 0;             // GBDE_SAVE_BEFORE | GBDE_SAVE_AFTER
+  bool has_affect = false;  // an affect or terminate (the state is modified)
   std::string condition, affect;
   std::vector<int> members;
 };
@@ -144,14 +146,16 @@ void flatten_callback(const CallbackDef* cb, std::vector<const CallbackDef*>& ou
 
 // UserCallback for the driver's interface (solver.cuh): the continuous
 // conditions of every ContinuousCallback (one) and VectorContinuousCallback
-// (len) in order, and the discrete callbacks in order.
+// (len) in order, and the discrete callbacks in order; the event saves of
+// each (save_c / save_d: GBDE_SAVE_* bits; a continuous callback without an
+// affect saves nothing after it, as the reference saves only a modified u).
 std::string callback_source(const CallbackDef* cb) {
   std::vector<const CallbackDef*> leaves;
   flatten_callback(cb, leaves);
   const std::string args = "const double* u, double t, const double* p";
   const std::string margs = "double* u, double t, const double* p, bool& terminate";
-  std::string s, conds, aff_c, cond_d, aff_d;
-  int nc = 0, nd = 0;
+  std::string s, conds, aff_c, cond_d, aff_d, save_c, save_d;
+  int nc = 0, nd = 0, saves = 0;
   for (size_t q = 0; q < leaves.size(); ++q) {
     const CallbackDef* l = leaves[q];
     const std::string tag = std::to_string(q);
@@ -164,9 +168,14 @@ std::string callback_source(const CallbackDef* cb) {
            "\n  }\n";
       cond_d += "    case " + std::to_string(nd) + ": return cond_d" + tag + "(u, t, p);\n";
       aff_d += "    case " + std::to_string(nd) + ": aff_d" + tag + "(u, t, p, terminate); return;\n";
+      save_d += "    case " + std::to_string(nd) + ": return " + std::to_string(l->save) + ";\n";
+      saves |= l->save;
       ++nd;
       continue;
     }
+    const int sv = l->save & (l->has_affect ? (GBDE_SAVE_BEFORE | GBDE_SAVE_AFTER) : GBDE_SAVE_BEFORE);
+    save_c += "    if (idx < " + std::to_string(nc + l->len) + ") return " + std::to_string(sv) + ";\n";
+    saves |= sv;
     const bool vec = l->kind == GBDE_CB_VECTOR;
     s += "  __device__ static void cond_c" + tag + "(" + args + ", double* out) {\n" +
          (vec ? "" : "    double g = 0.0;\n") + cond_line + l->condition +
@@ -179,7 +188,10 @@ std::string callback_source(const CallbackDef* cb) {
     nc += l->len;
   }
   return "struct UserCallback {\n  static constexpr int NC = " + std::to_string(nc) +
-         ", ND = " + std::to_string(nd) + ";\n" + s +
+         ", ND = " + std::to_string(nd) + ", SAVES = " + std::to_string(saves) + ";\n" + s +
+         "  __device__ static int save_c(int idx) {\n" + save_c + "    return 0;\n  }\n" +
+         "  __device__ static int save_d(int k) {\n    switch (k) {\n" + save_d +
+         "    }\n    return 0;\n  }\n" +
          "  __device__ static void conditions(" + args + ", double* g) {\n" + conds + "  }\n" +
          "  __device__ static void affect_c(int idx, " + margs + ") {\n" + aff_c + "  }\n" +
          "  __device__ static bool condition_d(int k, " + args + ") {\n    switch (k) {\n" +
@@ -544,8 +556,12 @@ static int leaf_callback(const gbde_callback* def, int kind, int len, int32_t* c
   CallbackDef c;
   c.kind = kind;
   c.len = len;
+  if (def->save_positions & ~(GBDE_SAVE_BEFORE | GBDE_SAVE_AFTER))
+    return fail(GBDE_ERR_INVALID, "save_positions takes GBDE_SAVE_BEFORE | GBDE_SAVE_AFTER bits");
   c.condition = def->condition;
   c.affect = def->affect ? def->affect : "";
+  c.has_affect = def->affect != nullptr || def->terminate;
+  c.save = def->save_positions;
   if (def->terminate) c.affect += "\nterminate = true;";
   return push_callback(std::move(c), callback_id);
 }

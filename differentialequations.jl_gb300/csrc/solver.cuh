@@ -57,6 +57,10 @@ struct KArgs {
   const double* dt_init;      // optional: starting step per trajectory (k_init_dt)
   double* red;                // optional: [2][n_save][N] sums and sums of squares of the
                               // saved states over trajectories (u_out may then be NULL)
+  double* ev_t;               // optional: [N][ev_cap] times of the saves at callback events
+  void* ev_u;                 // optional: [N][ev_cap][n_state] their states (out_f32's type)
+  int32_t* ev_n;              // optional: [N] event saves made (callback kernels only)
+  int32_t ev_cap;             // event saves per trajectory the buffers hold
 };
 
 GBDE_D uint64_t global_ns() {
@@ -301,8 +305,14 @@ __global__ void __launch_bounds__(128) k_init_dt(const KArgs a, double* __restri
 // twice; the other conditions start from their values after the affect.
 // Discrete: after an accepted step each condition k that is true applies its
 // affect, in order, on the state the previous ones left.
+// Event saves (the reference's save_positions; save_c(idx) / save_d(k) give
+// the GBDE_SAVE_* bits of continuous condition idx / discrete callback k,
+// SAVES their union): (t, u) before an affect, unless a saveat point at
+// exactly t was stored at that moment, and (t, u) after it.
 struct NoCallback {
-  static constexpr int NC = 0, ND = 0;
+  static constexpr int NC = 0, ND = 0, SAVES = 0;
+  GBDE_D static int save_c(int) { return 0; }
+  GBDE_D static int save_d(int) { return 0; }
   GBDE_D static void conditions(const double*, double, const double*, double*) {}
   GBDE_D static void affect_c(int, double*, double, const double*, bool&) {}
   GBDE_D static bool condition_d(int, const double*, double, const double*) { return false; }
@@ -334,9 +344,12 @@ GBDE_D bool cb_affect_c(int idx, T* u, double t, const T* p) {
   return term;
 }
 
-// every discrete callback in order on u; returns (any fired, terminate)
-template <class CB, int N, int NP, class T>
-GBDE_D bool cb_discrete(T* u, double t, const T* p, bool& term) {
+// every discrete callback in order on u; returns (any fired, terminate).
+// save(t, ud) makes an event save; `exact`: a saveat point at exactly t was
+// stored just before (the first callback to fire then saves nothing before
+// its affect).
+template <class CB, int N, int NP, class T, class Save>
+GBDE_D bool cb_discrete(T* u, double t, const T* p, bool& term, bool exact, Save&& save) {
   double ud[N], pd[NP];
 #pragma unroll
   for (int c = 0; c < N; ++c) ud[c] = (double)u[c];
@@ -346,7 +359,11 @@ GBDE_D bool cb_discrete(T* u, double t, const T* p, bool& term) {
 #pragma unroll
   for (int k = 0; k < CB::ND; ++k) {
     if (CB::condition_d(k, ud, t, pd)) {
+      const int sv = CB::save_d(k);
+      if ((sv & GBDE_SAVE_BEFORE) && !exact) save(t, ud);
+      exact = false;
       CB::affect_d(k, ud, t, pd, term);
+      if (sv & GBDE_SAVE_AFTER) save(t, ud);
       any = true;
     }
   }
@@ -406,6 +423,7 @@ __device__ void integrate_all(const KArgs& a) {
   constexpr int N = M::N;
   double gprev[CB::NC > 0 ? CB::NC : 1];  // continuous conditions at the current point
   int nudge = -1;  // condition whose event ended the previous step (repeat nudge), or -1
+  int nev = 0;     // event saves made by the current trajectory
   WorkSource src;
   src.init();
   Alg alg;
@@ -432,7 +450,7 @@ __device__ void integrate_all(const KArgs& a) {
       t = __ldg(a.t0 + i);
       tf = __ldg(a.tf + i);
       js = 0;
-      nacc = nrej = nfev = 0;
+      nacc = nrej = nfev = nev = 0;
       iters = 0;
       lqold = a.ctl.lqoldinit;
       dt1 = __longlong_as_double(0x7ff8000000000000ll);
@@ -578,13 +596,15 @@ __device__ void integrate_all(const KArgs& a) {
           }
         }
         // saveat: dense output at every save time in (t, tnew], or up to the
-        // event
+        // event; `exact`: the last one stored falls on that end
         const double te = event ? t + th_e * h : tnew;
         const uint64_t tnew_o = ord_bits(tnew), lim_o = ord_bits(te);
+        bool exact = false;
         while (js < a.n_save) {
           const double ts = save_time(a, i, js);
           const uint64_t ts_o = ord_bits(ts);
           if (ts_o > lim_o) break;
+          exact = ts_o == lim_o;
           if (!event && ts_o == tnew_o) {
             store_state<N>(a, i, js, alg.unew());
           } else {
@@ -594,12 +614,45 @@ __device__ void integrate_all(const KArgs& a) {
           }
           ++js;
         }
+        // an event save: (time, state) rounded to the working precision,
+        // the state the integration holds
+        auto ev_save = [&](double ts, const double* ud) {
+          if constexpr (CB::SAVES != 0) {
+            if (a.ev_n == nullptr) return;
+            if (nev < a.ev_cap) {
+              const size_t o = (size_t)i * a.ev_cap + nev;
+              if (a.ev_t) a.ev_t[o] = ts;
+              if (a.ev_u) {
+#pragma unroll
+                for (int c = 0; c < N; ++c) {
+                  const double v = (double)(T)ud[c];
+                  if (a.out_f32) ((float*)a.ev_u)[o * N + c] = (float)v;
+                  else ((double*)a.ev_u)[o * N + c] = v;
+                }
+              }
+            }
+            ++nev;
+          }
+        };
         if (event) {
           // move to the event, apply affect, restart the method there
           T ue[N];
           alg.interp(th_e, h, ue, p, nfev);
+          const int sv = CB::save_c(idx_e);
+          if ((sv & GBDE_SAVE_BEFORE) && !exact) {
+            double ud[N];
+#pragma unroll
+            for (int c = 0; c < N; ++c) ud[c] = (double)ue[c];
+            ev_save(te, ud);
+          }
           bool term = cb_affect_c<CB, N, M::NP>(idx_e, ue, te, p);
-          if constexpr (CB::ND > 0) cb_discrete<CB, N, M::NP>(ue, te, p, term);
+          if (sv & GBDE_SAVE_AFTER) {
+            double ud[N];
+#pragma unroll
+            for (int c = 0; c < N; ++c) ud[c] = (double)ue[c];
+            ev_save(te, ud);
+          }
+          if constexpr (CB::ND > 0) cb_discrete<CB, N, M::NP>(ue, te, p, term, false, ev_save);
           alg.init(ue, p, nfev);
           t = te;
           nudge = idx_e;
@@ -627,7 +680,7 @@ __device__ void integrate_all(const KArgs& a) {
 #pragma unroll
             for (int c = 0; c < N; ++c) uc[c] = alg.u()[c];
             bool term = false;
-            if (fin && cb_discrete<CB, N, M::NP>(uc, t, p, term)) {
+            if (fin && cb_discrete<CB, N, M::NP>(uc, t, p, term, exact, ev_save)) {
               alg.init(uc, p, nfev);
               if constexpr (CB::NC > 0) cb_conditions<CB, N, M::NP>(alg.u(), t, p, gprev);
               if (term) ret = GBDE_RET_TERMINATED;
@@ -665,6 +718,9 @@ __device__ void integrate_all(const KArgs& a) {
       if (a.t_end) a.t_end[i] = t;
       if (a.method_out) a.method_out[i] = method_of(alg);
       if (a.dt_first) a.dt_first[i] = dt1;
+      if constexpr (CB::NC + CB::ND > 0) {
+        if (a.ev_n) a.ev_n[i] = nev;
+      }
       active = false;
     }
   }

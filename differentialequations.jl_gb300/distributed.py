@@ -38,7 +38,7 @@ def solve_shard(solve_fn, arrays, rank, world):
 
 
 def solve_sharded(solver, devices, model, opts, p, u0, t0, tf, saveat, save_kind,
-                  u_dtype="f64", reduce=False):
+                  u_dtype="f64", reduce=False, events=None):
     """One call, several GPUs of this process: contiguous trajectory slices
     (shard_range), one per entry of `devices`, each solved by
     `solver(model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype=,
@@ -47,7 +47,8 @@ def solve_sharded(solver, devices, model, opts, p, u0, t0, tf, saveat, save_kind
     its own context, stream and staging buffers.  Every slice writes straight
     into its rows of the full output arrays (C order, trajectory-major), so
     nothing is copied to reassemble the ensemble; per-save-point reduction
-    sums add up across slices.  No collective: trajectories never interact.
+    sums add up across slices; events=K keeps K saves at callback events per
+    trajectory.  No collective: trajectories never interact.
     The replacement of EnsembleDistributed / EnsembleSplitThreads
     (test/qa/qa.jl:49,53) within one node."""
     import threading
@@ -60,6 +61,10 @@ def solve_sharded(solver, devices, model, opts, p, u0, t0, tf, saveat, save_kind
         res[k] = np.empty(N, np.int32)
     res["t_end"] = np.empty(N, np.float64)
     res["dt_first"] = np.empty(N, np.float64)
+    if events is not None:  # saves at callback events, K per trajectory
+        res["ev_t"] = np.empty((N, int(events)), np.float64)
+        res["ev_u"] = np.empty((N, int(events), model.n_state), res["u"].dtype)
+        res["ev_count"] = np.empty(N, np.int32)
     per_traj_save = saveat is not None and saveat.ndim == 2
     spans = [shard_range(N, r, len(devices)) for r in range(len(devices))]
     parts, errors = [None] * len(devices), [None] * len(devices)
@@ -70,7 +75,8 @@ def solve_sharded(solver, devices, model, opts, p, u0, t0, tf, saveat, save_kind
             out = {k: v[a:b] for k, v in res.items()}
             parts[r] = solver(model, opts, p[a:b], u0[a:b], t0[a:b], tf[a:b],
                               saveat[a:b] if per_traj_save else saveat, save_kind,
-                              u_dtype=u_dtype, device=devices[r], out=out, reduce=reduce)
+                              u_dtype=u_dtype, device=devices[r], out=out, reduce=reduce,
+                              events=events)
         except Exception as e:  # re-raised on the calling thread
             errors[r] = e
 

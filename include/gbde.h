@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define GBDE_ABI_VERSION 3
+#define GBDE_ABI_VERSION 4
 
 #if defined(__GNUC__)
 #define GBDE_API __attribute__((visibility("default")))
@@ -230,6 +230,17 @@ typedef struct {
                           without storing the ensemble).  With u = NULL
                           the ensemble is not stored at all.  Additions
                           run in no fixed order (FP64 atomics).          */
+  /* Saves at callback events (the callbacks' save_positions; solves with
+   * opts.callback only, ignored otherwise).  Trajectory i's k-th event save
+   * is (ev_t[i][k], ev_u[i][k][:]) for k < min(ev_count[i], ev_capacity), in
+   * the order made; ev_u has u_dtype.  ev_count[i] counts every save the
+   * trajectory made, also those beyond ev_capacity (not stored): a caller
+   * that finds ev_count[i] > ev_capacity solves again with a larger one.
+   * ev_count NULL: no event saves.                                        */
+  double* ev_t;        /* [N][ev_capacity] or NULL                          */
+  void* ev_u;          /* [N][ev_capacity][n_state] or NULL                 */
+  int32_t* ev_count;   /* [N] or NULL                                       */
+  int32_t ev_capacity; /* event saves per trajectory the buffers hold       */
 } gbde_outputs;
 
 /* ABI version of the loaded library (GBDE_ABI_VERSION). */
@@ -504,12 +515,25 @@ GBDE_API int gbde_model_compile(int32_t model_id, int32_t alg, int32_t precision
  * hold NaN; t_end is the event time).  A solve with opts.callback compiles
  * its kernels at run time (NVRTC, as user models), for built-in one-thread
  * models and user models; not GBDE_ALG_AUTO, SDE methods or learned=1.
- * Callback saves (save_positions) are not made: only the saveat points.   */
+ * save_positions (the reference's keyword of every callback kind, default
+ * (true, true): GBDE_SAVE_BEFORE | GBDE_SAVE_AFTER) adds saves at the
+ * callback's events to gbde_outputs.ev_*, beside the saveat points:
+ *   GBDE_SAVE_BEFORE: (t, u) before the affect, unless a saveat point at
+ *     exactly t was stored at that moment (the first discrete callback to
+ *     fire after a step that ends on a saveat time, or an event on one);
+ *   GBDE_SAVE_AFTER: (t, u) after the affect (continuous callbacks only
+ *     when they have an affect, as the reference saves only a modified u).
+ * At one time, saveat points come first, then the event saves in the order
+ * made: the continuous event's, then each discrete callback's that fired. */
+#define GBDE_SAVE_BEFORE 1
+#define GBDE_SAVE_AFTER 2
 typedef struct {
   int32_t kind;          /* GBDE_CB_CONTINUOUS, GBDE_CB_DISCRETE, _VECTOR  */
   const char* condition; /* statements: g = ...   (required)               */
   const char* affect;    /* statements on u[] / terminate, or NULL         */
   int32_t terminate;     /* 1: terminate after affect at every event       */
+  int32_t save_positions;/* GBDE_SAVE_BEFORE | GBDE_SAVE_AFTER bits (0: no
+                            event saves; the reference's default is both) */
 } gbde_callback;
 /* Register a callback; *callback_id (>= 1) goes into gbde_opts.callback. */
 GBDE_API int gbde_callback_register(const gbde_callback* def, int32_t* callback_id);

@@ -61,7 +61,8 @@ class Outputs(C.Structure):
         ("naccept", C.c_void_p), ("nreject", C.c_void_p), ("nf", C.c_void_p),
         ("t_end", C.c_void_p), ("method", C.c_void_p),
         ("device_ms", C.c_float), ("total_ms", C.c_float), ("dt_first", C.c_void_p),
-        ("reduce", C.c_void_p),
+        ("reduce", C.c_void_p), ("ev_t", C.c_void_p), ("ev_u", C.c_void_p),
+        ("ev_count", C.c_void_p), ("ev_capacity", C.c_int32),
     ]
 
 

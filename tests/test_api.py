@@ -63,7 +63,7 @@ def test_oracle_restates_the_abi(capi, oracle):
 
 
 def test_version_and_model_info(capi):
-    assert capi.lib().gbde_version() == 3
+    assert capi.lib().gbde_version() == 4
     assert capi.model_info(capi.MODEL_LORENZ) == (3, 3)
     assert capi.model_info(capi.MODEL_VDP_RING8) == (16, 2)
     with pytest.raises(capi.GBDEError):

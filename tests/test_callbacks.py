@@ -55,17 +55,36 @@ def _lorenz_ens(de, N=64):
 @pytest.mark.gpu
 def test_reference_callbacks_lorenz(capi, de, oracle):
     """test/core.jl:60-79 on the GPU: both callbacks return Success.  The
-    no-op discrete affect restarts Tsit5 at the same state, so the solution is
-    bit-identical to the solve without callback; the continuous one cuts the
-    step at t = 0.5 and stays within tolerance of the FP64 oracle."""
+    no-op discrete affect restarts Tsit5 at the same state, so the saveat
+    points are bit-identical to the solve without callback; the continuous
+    one cuts the step at t = 0.5 and stays within tolerance of the FP64
+    oracle.  With the default save_positions the discrete callback adds
+    (t, u) before and after its affect at every step end from t = 0.5 on
+    (before: not at tf, a saveat point), the continuous one (no affect) at
+    most one save at its event, before it."""
     prob = de.ODEProblem(de.models.lorenz, [1.0, 0.0, 0.0], (0.0, 1.0), [10.0, 28.0, 8.0 / 3.0])
     kw = dict(saveat=0.1, reltol=1e-8, abstol=1e-8)
+    grid = de.save_grid(0.0, 1.0, 0.1)
     ref = de.solve(prob, de.Tsit5(), **kw)
-    cc = de.solve(prob, de.Tsit5(), callback=de.ContinuousCallback("g = t - 0.5;"), **kw)
-    dc = de.solve(prob, de.Tsit5(), callback=de.DiscreteCallback("g = t >= 0.5;"), **kw)
+    quiet = dict(save_positions=(False, False))
+    cc = de.solve(prob, de.Tsit5(), callback=de.ContinuousCallback("g = t - 0.5;", **quiet), **kw)
+    dc = de.solve(prob, de.Tsit5(), callback=de.DiscreteCallback("g = t >= 0.5;", **quiet), **kw)
     assert cc.retcode == de.ReturnCode.Success and dc.retcode == de.ReturnCode.Success
     assert len(cc.t) == 11 and np.array_equal(np.asarray(cc.u[0]), [1.0, 0.0, 0.0])
     assert np.array_equal(np.asarray(dc.u), np.asarray(ref.u))
+    # the reference's default save_positions = (true, true)
+    cc2 = de.solve(prob, de.Tsit5(), callback=de.ContinuousCallback("g = t - 0.5;"), **kw)
+    assert len(cc2.t) in (11, 12)
+    extra = ~np.isin(cc2.t, grid)
+    assert np.all(np.abs(cc2.t[extra] - 0.5) <= 1e-12)
+    dc2 = de.solve(prob, de.Tsit5(), callback=de.DiscreteCallback("g = t >= 0.5;"), **kw)
+    on_grid = np.isin(dc2.t, grid)
+    ev_t, ev_u = dc2.t[~on_grid], np.asarray(dc2.u)[~on_grid]
+    assert len(ev_t) % 2 == 0 and len(ev_t) >= 2 and np.all(ev_t >= 0.5)
+    assert np.array_equal(ev_t[0::2], ev_t[1::2]) and np.array_equal(ev_u[0::2], ev_u[1::2])
+    assert len(dc2.t) - len(ev_t) == 11 + 1  # the save after the affect at tf
+    u_grid = np.asarray(dc2.u)[on_grid]
+    assert np.array_equal(u_grid[:11], np.asarray(ref.u)) and np.array_equal(u_grid[11], u_grid[10])
     o = capi.opts_default(capi.ALG_TSIT5)
     o.reltol = o.abstol = 1e-8
     orc = oracle.solve(capi, de.models.lorenz, o, np.array([[10.0, 28.0, 8.0 / 3.0]]),
@@ -292,3 +311,161 @@ def test_discrete_callbacks_in_order_after_events(capi, de):
     assert np.all(r["retcode"] == capi.RET_SUCCESS)
     np.testing.assert_array_equal(r["u"][:, :, 5], 2.0 * r["u"][:, :, 4])
     np.testing.assert_array_equal(r["u"][:, -1, 4], r["naccept"] - 1)
+
+
+# ------------------------------------------- saves at events (save_positions)
+def _impacts(h0, g, e, t_end):
+    """Analytic impacts of a ball dropped from rest at h0 up to t_end: their
+    times, speeds before (downward) and after (upward, e times it)."""
+    t, v_in = np.sqrt(2 * h0 / g), np.sqrt(2 * h0 / g) * g
+    out = []
+    while t <= t_end:
+        out.append((t, v_in))
+        v_in *= e
+        t += 2 * v_in / g
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "f32x2"])
+def test_event_saves_bouncing_ball(capi, de, precision):
+    """save_positions=(true, true), the reference's default: every impact adds
+    (t, u) before the bounce (x = 0, v = -v_in) and after it (x = 0,
+    v = e v_in) to the trajectory's solution, between the saveat points of
+    their time; the analytic impacts pin times and states."""
+    N = 256
+    rng = np.random.default_rng(11)
+    g = rng.uniform(5.0, 15.0, N)
+    e = rng.uniform(0.8, 0.9, N)
+    h0 = rng.uniform(0.5, 2.0, N)
+    ball = de.ODEFunction(BALL_F, 2, 2, name="ball_evsave_%s" % precision)
+    cb = de.ContinuousCallback("g = u[0];", BOUNCE)
+    ens = de.EnsembleProblem(de.ODEProblem(ball, [1.0, 0.0], (0.0, 1.0), [9.8, 0.8]),
+                             batch=lambda prob, n: {"p": np.c_[g, e], "u0": np.c_[h0, np.zeros(N)]})
+    sol = de.solve(ens, de.Tsit5(), de.EnsembleGB300(precision=precision), trajectories=N,
+                   saveat=0.05, reltol=1e-10, abstol=1e-10, callback=cb)
+    assert sol.converged
+    ts = de.save_grid(0.0, 1.0, 0.05)
+    ev_t, ev_u, ev_n = sol.events
+    for i in range(N):
+        imp = _impacts(h0[i], g[i], e[i], 1.0)
+        assert ev_n[i] == 2 * len(imp), (i, ev_n[i], len(imp))
+        for k, (t_hit, v_in) in enumerate(imp):
+            for j, v in ((2 * k, -v_in), (2 * k + 1, e[i] * v_in)):
+                assert abs(ev_t[i, j] - t_hit) <= 1e-9 * t_hit, (i, k)
+                assert abs(ev_u[i, j, 0]) <= 1e-9 and abs(ev_u[i, j, 1] - v) <= 1e-8 * g[i]
+        s = sol[i]
+        assert len(s.t) == len(ts) + 2 * len(imp)
+        assert np.all(np.diff(s.t) >= 0)
+        grid_rows = np.isin(s.t, ts)
+        assert np.array_equal(np.asarray(s.u)[grid_rows], sol.U[i])
+
+
+@pytest.mark.gpu
+def test_event_save_positions_flags(capi, de):
+    """(true, false) keeps the saves before the affects, (false, true) those
+    after, (false, false) none (no event buffers at all); a continuous
+    callback without an affect saves nothing after its event."""
+    N = 64
+    rng = np.random.default_rng(12)
+    g, e, h0 = rng.uniform(5.0, 15.0, N), rng.uniform(0.8, 0.9, N), rng.uniform(0.5, 2.0, N)
+    ball = de.ODEFunction(BALL_F, 2, 2, name="ball_evflags")
+    ens = de.EnsembleProblem(de.ODEProblem(ball, [1.0, 0.0], (0.0, 1.0), [9.8, 0.8]),
+                             batch=lambda prob, n: {"p": np.c_[g, e], "u0": np.c_[h0, np.zeros(N)]})
+    kw = dict(trajectories=N, saveat=0.05, reltol=1e-10, abstol=1e-10)
+    n_imp = np.array([len(_impacts(h0[i], g[i], e[i], 1.0)) for i in range(N)])
+    for sp, sign in (((True, False), -1.0), ((False, True), 1.0)):
+        cb = de.ContinuousCallback("g = u[0];", BOUNCE, save_positions=sp)
+        sol = de.solve(ens, de.Tsit5(), de.EnsembleGB300(), callback=cb, **kw)
+        ev_t, ev_u, ev_n = sol.events
+        assert np.array_equal(ev_n, n_imp), sp
+        assert all(np.all(np.sign(ev_u[i, :ev_n[i], 1]) == sign) for i in range(N))
+    sol = de.solve(ens, de.Tsit5(), de.EnsembleGB300(),
+                   callback=de.ContinuousCallback("g = u[0];", BOUNCE,
+                                                  save_positions=(False, False)), **kw)
+    assert sol.events is None and len(sol[0].t) == 21
+    # no affect: u is not modified, only the save before the event is made
+    # (the ball then falls through zero: one crossing per trajectory)
+    sol = de.solve(ens, de.Tsit5(), de.EnsembleGB300(),
+                   callback=de.ContinuousCallback("g = u[0];"), **kw)
+    ev_t, ev_u, ev_n = sol.events
+    assert np.all(ev_n == 1)
+    np.testing.assert_allclose(ev_t[:, 0], np.sqrt(2 * h0 / g), rtol=1e-9)
+
+
+def _counting_problem(de, N, seed, name):
+    g, e, h0, u0, p = _two_balls(de, N, seed)
+    f = BALLS_F + " du[4] = 0.0; du[5] = 0.0;"
+    balls = de.ODEFunction(f, 6, 4, name=name)
+    cb = de.CallbackSet(de.ContinuousCallback("g = u[0];", "u[1] = -p[2] * u[1];"),
+                        de.DiscreteCallback("g = 1.0;", "u[4] += 1.0;"),
+                        de.DiscreteCallback("g = 1.0;", "u[5] = 2.0 * u[4];"))
+    return g, e, h0, np.c_[u0, np.zeros((N, 2))], p, balls, cb
+
+
+@pytest.mark.gpu
+def test_discrete_event_saves_count_and_order(capi, de):
+    """Two discrete callbacks firing after every accepted step and an impact
+    callback: each impact saves twice, each discrete firing twice, but the
+    first discrete callback after the last step (which ends on the saveat
+    point tf) saves nothing before its affect -- so a trajectory makes
+    2 impacts + 4 naccept - 1 saves, in time order, and the save after the
+    second affect always holds u[5] == 2 u[4].  A capacity below the count
+    stores the first saves of the same sequence and counts them all."""
+    N = 64
+    g, e, h0, u0, p, balls, cb = _counting_problem(de, N, 13, "balls_evcount")
+    o = capi.opts_default(capi.ALG_TSIT5)
+    o.reltol = o.abstol = 1e-9
+    o.callback = cb.id
+    grid = de.save_grid(0.0, 1.0, 0.1)
+    args = (balls, o, p, u0, np.zeros(N), np.ones(N), grid, capi.SAVE_GRID)
+    n_imp = np.array([len(_impacts(h0[i, 0], g[i, 0], e[i, 0], 1.0)) for i in range(N)])
+    first = de.solve_arrays(*args, events=0)
+    count = first["ev_count"]
+    assert np.all(first["retcode"] == capi.RET_SUCCESS)
+    assert np.array_equal(count, 2 * n_imp + 4 * first["naccept"] - 1)
+    cap = int(count.max())
+    full = de.solve_arrays(*args, events=cap)
+    assert np.array_equal(full["ev_count"], count)
+    for i in range(N):
+        c = count[i]
+        t, u = full["ev_t"][i, :c], full["ev_u"][i, :c]
+        assert np.all(np.diff(t) >= 0)
+        # the last save is the second discrete affect's after the final step
+        assert t[-1] == 1.0 and u[-1, 5] == 2.0 * u[-1, 4] == 2.0 * first["naccept"][i]
+    small = de.solve_arrays(*args, events=5)
+    assert np.array_equal(small["ev_count"], count)
+    assert np.array_equal(small["ev_t"], full["ev_t"][:, :5])
+    assert np.array_equal(small["ev_u"], full["ev_u"][:, :5])
+
+
+@pytest.mark.gpu
+def test_event_saves_device_memory_and_resolve(capi, de):
+    """Device-memory solves write the same event saves as host-memory ones,
+    and solve() solves again when the first guess of room was short: every
+    save of every trajectory ends up in its solution."""
+    torch = pytest.importorskip("torch")
+    N = 32
+    g, e, h0, u0, p, balls, cb = _counting_problem(de, N, 14, "balls_evdev")
+    o = capi.opts_default(capi.ALG_TSIT5)
+    o.reltol = o.abstol = 1e-9
+    o.callback = cb.id
+    grid = de.save_grid(0.0, 1.0, 0.1)
+    host = de.solve_arrays(balls, o, p, u0, np.zeros(N), np.ones(N), grid, capi.SAVE_GRID,
+                           events=16)
+    dv = [torch.from_numpy(np.ascontiguousarray(a)).cuda()
+          for a in (p, u0, np.zeros(N), np.ones(N), grid)]
+    dev = de.solve_arrays(balls, o, *dv, capi.SAVE_GRID, events=16)
+    torch.cuda.synchronize()
+    for k in ("ev_t", "ev_u", "ev_count"):
+        assert np.array_equal(dev[k].cpu().numpy(), host[k]), k
+    ens = de.EnsembleProblem(de.ODEProblem(balls, u0[0], (0.0, 1.0), p[0]),
+                             batch=lambda prob, n: {"p": p, "u0": u0})
+    sol = de.solve(ens, de.Tsit5(), de.EnsembleGB300(), trajectories=N, saveat=0.1,
+                   reltol=1e-9, abstol=1e-9, callback=cb)
+    ev_t, ev_u, ev_n = sol.events
+    assert np.array_equal(ev_n, host["ev_count"]) and ev_t.shape[1] == ev_n.max() > 16
+    for i in range(N):
+        assert len(sol[i].t) == len(grid) + ev_n[i]
+        c = min(16, int(ev_n[i]))
+        assert np.array_equal(ev_t[i, :c], host["ev_t"][i, :c])

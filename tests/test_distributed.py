@@ -78,10 +78,14 @@ def _oracle_solver(oracle, calls):
     """Stand-in for api.solve_arrays on the CPU (same signature; writes into
     `out`), recording which device each slice was given."""
     def solver(model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype="f64", device=0, out=None,
-               reduce=False):
+               reduce=False, events=None):
         r = oracle.solve(None, model, opts, p, u0, t0, tf, saveat, save_kind, u_dtype=u_dtype)
         for k in ("u", "retcode", "naccept", "nreject", "nf", "t_end"):
             out[k][...] = r[k]
+        if events is not None:  # stand-in event saves: t_end and u0, naccept times over
+            out["ev_count"][...] = r["naccept"]
+            out["ev_t"][...] = r["t_end"][:, None]
+            out["ev_u"][...] = u0[:, None, :]
         calls.append((device, len(p)))
         res = dict(out, device_ms=1.0, total_ms=2.0)
         if reduce:
@@ -110,10 +114,14 @@ def test_solve_sharded_reassembles_bitwise(oracle, de, ndev):
     calls = []
     got = distributed.solve_sharded(_oracle_solver(oracle, calls), list(range(10, 10 + ndev)), M,
                                     opts, p, u0, t0, tf, saveat, oracle.SAVE_PER_TRAJ,
-                                    reduce=True)
+                                    reduce=True, events=3)
     ref = oracle.solve(None, M, opts, p, u0, t0, tf, saveat, oracle.SAVE_PER_TRAJ)
     for k in ("u", "retcode", "naccept", "nreject", "t_end"):
         assert np.array_equal(got[k], ref[k]), k
+    # event saves (callback save_positions) land in their trajectories' rows
+    assert np.array_equal(got["ev_count"], ref["naccept"])
+    assert np.array_equal(got["ev_t"], np.repeat(ref["t_end"][:, None], 3, axis=1))
+    assert np.array_equal(got["ev_u"], np.repeat(u0[:, None, :], 3, axis=1))
     assert sorted(d for d, _ in calls) == list(range(10, 10 + ndev))
     sizes = [b - a for a, b in got["spans"]]
     assert sum(sizes) == N and max(sizes) - min(sizes) <= 1
