@@ -30,6 +30,19 @@ GBDE_D ff ff_split(double d) {
   return ff(hi, sign ? -lo : lo);
 }
 
+// 1 / x for a pair, relative error about 2^-47: the correctly rounded FP32
+// reciprocal r of the leading part, then one Newton correction on the pair,
+// 1/x ~ r + r e with e = 1 - x r.  The leading residual 1 - hi r is exact
+// with an FMA (the residual of a correctly rounded reciprocal is
+// representable); the low part enters as - lo r.  (Newton's iteration for the
+// reciprocal with an exact first residual, as in T.J. Dekker, Numer. Math. 18
+// (1971) 224-242, applied to a float-float divisor.)
+GBDE_D ff ff_rcp(ff x) {
+  const float r = __frcp_rn(x.hi);
+  const float e = xfma(-x.lo, r, xfma(-x.hi, r, 1.0f));
+  return ff_renorm(r, xmul(r, e));
+}
+
 // Unnormalised accumulator of a sum of pair products: value = s + e.  Each term
 // costs one TwoProd with cross terms and one TwoSum; get() renormalises once.
 struct FfAcc {

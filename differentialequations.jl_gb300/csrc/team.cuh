@@ -701,36 +701,36 @@ GBDE_D double* team8_row(int i) {
 }
 
 struct TeamLU8 {
-  double invp[2];  // 1 / pivot of this lane's rows
-  int step[2];     // elimination step at which each of them was the pivot
-  uint64_t piv;    // pivot row of step k in bits [4k, 4k+4)
+  uint64_t piv;  // pivot row of step k in bits [4k, 4k+4)
 
-  // LU with partial pivoting of the W written into team8_row(): the
-  // pivot of step k is the unpivoted row with the largest |a_k|, ties to the
-  // lowest row position of the row-swapping LU (LAPACK getrf's order, as
-  // TeamLU); the rank-1 update runs column-parallel over the rows with a
-  // nonzero multiplier (lane l updates columns l and l + 8).
+  GBDE_D static ff* row(int i) { return reinterpret_cast<ff*>(team8_row(i)); }
+
+  // LU with partial pivoting, in FP32 pairs, of the W written as pairs into
+  // team8_row(): the pivot of step k is the unpivoted row with the largest
+  // |leading part| of a_k, ties to the lowest row position of the
+  // row-swapping LU (LAPACK getrf's order, as TeamLU); the rank-1 update runs
+  // column-parallel over the rows with a nonzero multiplier, lane l updating
+  // columns l and l + 8 in one paired accumulation.  GB300 runs FP32 at ~60x
+  // its FP64 rate: each FP64 update here was one FP64-pipe instruction of ~64
+  // cycles per warp on the elimination's critical path.
   GBDE_D void factor(const Team8& tm) {
     const int r0 = 2 * tm.lane, r1 = r0 + 1;
-    double* a0 = team8_row(r0);
-    double* a1 = team8_row(r1);
-    step[0] = step[1] = -1;
-    invp[0] = invp[1] = 0.0;
+    ff* a0 = row(r0);
+    ff* a1 = row(r1);
+    bool open0 = true, open1 = true;  // not yet a pivot row
     piv = 0;
     unsigned pos0 = (unsigned)r0, pos1 = (unsigned)r1;
     const unsigned sh = (threadIdx.x & 31) & 24;  // the team's first lane in the warp
     __syncwarp(tm.mask);  // every lane's rows are written
 #pragma unroll 1
     for (int k = 0; k < TEAM; ++k) {
-      const double ak0 = a0[k], ak1 = a1[k];
-      const uint64_t key0 = step[0] < 0 ? mag_bits(ak0) + 1ull : 0ull;
-      const uint64_t key1 = step[1] < 0 ? mag_bits(ak1) + 1ull : 0ull;
-      uint64_t m = key0 > key1 ? key0 : key1;
+      const ff ak0 = a0[k], ak1 = a1[k];
+      // |leading part| + 1 on the integer pipe (NaN ranks above every number)
+      const unsigned key0 = open0 ? (__float_as_uint(ak0.hi) & 0x7fffffffu) + 1u : 0u;
+      const unsigned key1 = open1 ? (__float_as_uint(ak1.hi) & 0x7fffffffu) + 1u : 0u;
+      unsigned m = max(key0, key1);
 #pragma unroll
-      for (int o = TEAM8 / 2; o > 0; o >>= 1) {
-        const uint64_t x = __shfl_xor_sync(tm.mask, m, o, TEAM8);
-        m = x > m ? x : m;
-      }
+      for (int o = TEAM8 / 2; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(tm.mask, m, o, TEAM8));
       // ties: the lowest position; (position, row) packed, positions unique
       unsigned pk = min(key0 == m ? (pos0 << 4) | (unsigned)r0 : 0xFFFFFFFFu,
                         key1 == m ? (pos1 << 4) | (unsigned)r1 : 0xFFFFFFFFu);
@@ -738,52 +738,59 @@ struct TeamLU8 {
       for (int o = TEAM8 / 2; o > 0; o >>= 1) pk = min(pk, __shfl_xor_sync(tm.mask, pk, o, TEAM8));
       const unsigned ppos = pk >> 4;
       const int p = (int)(pk & 15u);
-      if (step[0] < 0 && pos0 == (unsigned)k && r0 != p) pos0 = ppos;  // swapped out
-      if (step[1] < 0 && pos1 == (unsigned)k && r1 != p) pos1 = ppos;
+      if (open0 && pos0 == (unsigned)k && r0 != p) pos0 = ppos;  // swapped out
+      if (open1 && pos1 == (unsigned)k && r1 != p) pos1 = ppos;
       piv |= (uint64_t)p << (4 * k);
-      const double* prow = team8_row(p);
-      const double inv = rcp64(prow[k]);
+      const ff* prow = row(p);
+      const ff inv = ff_rcp(prow[k]);
+      // multipliers of the open rows; l != 0 tested on the integer pipe
       bool u0 = false, u1 = false;
-      // l != 0 tested on the integer pipe (magnitude bits)
       if (r0 == p) {
-        step[0] = k;
-        invp[0] = inv;
-      } else if (step[0] < 0) {
-        const double l = ak0 * inv;
+        open0 = false;
+      } else if (open0) {
+        const ff l = ak0 * inv;
         a0[k] = l;
-        u0 = mag_bits(l) != 0ull;
+        u0 = (__float_as_uint(l.hi) << 1) != 0u;
       }
       if (r1 == p) {
-        step[1] = k;
-        invp[1] = inv;
-      } else if (step[1] < 0) {
-        const double l = ak1 * inv;
+        open1 = false;
+      } else if (open1) {
+        const ff l = ak1 * inv;
         a1[k] = l;
-        u1 = mag_bits(l) != 0ull;
+        u1 = (__float_as_uint(l.hi) << 1) != 0u;
       }
       const unsigned b0 = (__ballot_sync(tm.mask, u0) >> sh) & 0xFFu;  // rows 2j
       const unsigned b1 = (__ballot_sync(tm.mask, u1) >> sh) & 0xFFu;  // rows 2j + 1
       __syncwarp(tm.mask);  // the multipliers are in shared memory
       const int ca = tm.lane, cb = tm.lane + TEAM8;
-      const double pa = prow[ca], pb = prow[cb];
+      const ff pa = prow[ca], pb = prow[cb];
+      const F2 ph = f2_pack(pa.hi, pb.hi), pl = f2_pack(pa.lo, pb.lo);
+      const bool wa = ca > k, wb = cb > k;
 #pragma unroll 1
       for (unsigned rows = b0 | (b1 << 8); rows != 0u; rows &= rows - 1u) {
         const int j = __ffs(rows) - 1;
-        double* ar = team8_row(j < 8 ? 2 * j : 2 * (j - 8) + 1);
-        const double l = ar[k];
-        if (ca > k) ar[ca] = fma(-l, pa, ar[ca]);
-        if (cb > k) ar[cb] = fma(-l, pb, ar[cb]);
+        ff* ar = row(j < 8 ? 2 * j : 2 * (j - 8) + 1);
+        const ff l = ar[k];
+        const ff xa = ar[ca], xb = ar[cb];
+        // (a_ca, a_cb) -= l (p_ca, p_cb), one paired accumulation
+        FfAcc2 acc;
+        acc.set(f2_pack(xa.hi, xb.hi), f2_pack(xa.lo, xb.lo));
+        acc.fma(f2_pack(-l.hi, -l.hi), f2_pack(-l.lo, -l.lo), f2_pack(l.hi, l.hi), ph, pl);
+        ff ya, yb;
+        acc.get(ya, yb);
+        if (wa) ar[ca] = ya;
+        if (wb) ar[cb] = yb;
       }
       __syncwarp(tm.mask);  // step k's updates land before step k+1 reads them
     }
   }
 };
 
-// The factors of a TeamLU8 as pairs for the solves, in pivot order: the row
-// that was the pivot of step k (its L part in columns < k, U in columns > k)
-// goes to slot k, i.e. lane k / 2, half k % 2 -- the row order of LAPACK's
-// row-swapping factorisation.  Each entry is negated and split to a pair on
-// the integer pipe as it moves; each slot keeps its pivot reciprocal.  With
+// The factors of a TeamLU8 for the solves, in pivot order: the row that was
+// the pivot of step k (its L part in columns < k, U in columns > k) goes to
+// slot k, i.e. lane k / 2, half k % 2 -- the row order of LAPACK's
+// row-swapping factorisation.  Each entry is negated as it moves; each slot
+// keeps its pivot reciprocal.  With
 // the slots in step order, the source of every step of the substitutions is
 // lane k / 2, half k % 2, known from k: no pivot lookups, and the two halves'
 // selects fold at compile time.  Forward and back substitution keep a lane's
@@ -797,18 +804,18 @@ struct TeamLUFF8 {
     const int l = tm.lane;
     q[0] = (int)((W.piv >> (8 * l)) & 15u);
     q[1] = (int)((W.piv >> (8 * l + 4)) & 15u);
-    const double* r0 = team8_row(q[0]);
-    const double* r1 = team8_row(q[1]);
+    const ff* r0 = TeamLU8::row(q[0]);
+    const ff* r1 = TeamLU8::row(q[1]);
     // the reciprocal of each slot's diagonal, as factor() formed it
-    invs[0] = ff_split(rcp64(r0[2 * l]));
-    invs[1] = ff_split(rcp64(r1[2 * l + 1]));
+    invs[0] = ff_rcp(r0[2 * l]);
+    invs[1] = ff_rcp(r1[2 * l + 1]);
     // slot rows 2l, 2l + 1 receive rows q0, q1, four columns at a time: every
     // lane reads its columns before any lane overwrites them
     float2* d0 = row_ff(2 * l);
     float2* d1 = row_ff(2 * l + 1);
 #pragma unroll 1
     for (int c0 = 0; c0 < TEAM; c0 += 4) {
-      double v0[4], v1[4];
+      ff v0[4], v1[4];
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
         v0[c] = r0[c0 + c];
@@ -817,9 +824,8 @@ struct TeamLUFF8 {
       __syncwarp(tm.mask);
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        const ff x0 = ff_split(v0[c]), x1 = ff_split(v1[c]);
-        d0[c0 + c] = make_float2(-x0.hi, -x0.lo);
-        d1[c0 + c] = make_float2(-x1.hi, -x1.lo);
+        d0[c0 + c] = make_float2(-v0[c].hi, -v0[c].lo);
+        d1[c0 + c] = make_float2(-v1[c].hi, -v1[c].lo);
       }
       __syncwarp(tm.mask);
     }
@@ -875,10 +881,10 @@ struct TeamLUFF8 {
   }
 };
 
-// Rodas5 / Rodas5P in FP32 pairs on 8-lane teams (the method and arithmetic of
-// RodasFF, rodas_ff.cuh, for a lane's two components): FP64 Jacobian rows, W
-// and its LU (TeamLU8), pair solves (TeamLUFF8), stage sums and dense output
-// on paired FP32 instructions, the norm's ratios FP32, their squares FP64.
+// Rodas5 / Rodas5P in FP32 pairs on 8-lane teams (the method of RodasFF,
+// rodas_ff.cuh, for a lane's two components): Jacobian rows, W and its LU
+// (TeamLU8) in pairs, pair solves (TeamLUFF8), stage sums and dense output on
+// paired FP32 instructions, the norm's ratios FP32, their squares FP64.
 template <class M, class Tag>
 struct TeamRodasFF8 {
   using K = RodasCoef<Tag>;
@@ -887,7 +893,6 @@ struct TeamRodasFF8 {
   static_assert(M::N == 2 * TEAM8, "8-lane teams are for 16-state models");
   ff uu[2], un[2];
   ff F0[2];  // f(u0): read only by the Hairer-Wanner starting step after init()
-  double pd[M::NP];
   bool fresh;  // uu's f evaluation already counted
 
   GBDE_D const ff* u() const { return uu; }
@@ -916,8 +921,6 @@ struct TeamRodasFF8 {
   }
 
   GBDE_D void init(const ff* u0, const ff* p, const Team8& tm, int& nf) {
-#pragma unroll
-    for (int k = 0; k < M::NP; ++k) pd[k] = (double)p[k];
     uu[0] = u0[0];
     uu[1] = u0[1];
     rhs(uu, p, tm, F0);
@@ -931,19 +934,17 @@ struct TeamRodasFF8 {
       ++nf;
       fresh = true;
     }
+    const double ih = rcp64(dt);
     TeamLUFF8 L;
     {
-      // rows 2l, 2l + 1 of W = I/(h gamma) - J(uu), FP64
+      // rows 2l, 2l + 1 of W = I/(h gamma) - J(uu), in pairs
       TeamLU8 W;
-      double ud[2];
-      ud[0] = f2d_bits(uu[0].hi) + f2d_bits(uu[0].lo);
-      ud[1] = f2d_bits(uu[1].hi) + f2d_bits(uu[1].lo);
-      M::w_osc(tm.lane, ud, pd, rcp64(dt) * (1.0 / K::g), team8_row(2 * tm.lane),
-               team8_row(2 * tm.lane + 1));
+      M::w_osc(tm.lane, uu, p, ff_split(ih * (1.0 / K::g)), TeamLU8::row(2 * tm.lane),
+               TeamLU8::row(2 * tm.lane + 1));
       W.factor(tm);
       L.from(W, tm);
     }
-    const ff iht = ff_split(rcp64(dt));
+    const ff iht = ff_split(ih);
     const RodasFfTab& tb = c_rodas_ff[RodasFfIdx<Tag>::v];
     FfVec<2> uv;
     uv.from(uu);
