@@ -134,15 +134,21 @@ struct VdpRing8 {
     dy[0] = v;
     dy[1] = p[0] * (T(1) - x * x) * v - x + p[1] * (xl - T(2) * x + xr);
   }
-  // 8-lane teams: rows 2l and 2l + 1 of W = dg I - J at lane l's oscillator
-  // (x, v) = (y[0], y[1]), written to w0[0..16), w1[0..16): the nonzeros of
-  // jac_lane's rows 2l (x_l' = v_l) and 2l + 1 (v_l'), same arithmetic,
-  // negated, dg added on the diagonal; every other entry 0.
+  // 8-lane teams: rows 2l (x_l' = v_l) and 2l + 1 (v_l') of W = dg I - J at
+  // lane l's oscillator (x, v) = (y[0], y[1]) have the nonzeros
+  //   W[2l][2l] = dg, W[2l][2l + 1] = -1,
+  //   W[2l + 1][2l] = w10, W[2l + 1][2l + 1] = w11, W[2l + 1][2(l +- 1)] = -ka
+  // (jac_lane's rows negated, dg added on the diagonal).
   template <class T>
-  GBDE_D static void w_osc(int l, const T* y, const T* p, T dg, T* w0, T* w1) {
+  GBDE_D static void w_osc_nz(const T* y, const T* p, T dg, T& w10, T& w11) {
     const T mu = p[0], ka = p[1], x = y[0], v = y[1];
+    w10 = T(2) * mu * x * v + T(1) + T(2) * ka;
+    w11 = dg - mu * (T(1) - x * x);
+  }
+  // those rows written out in full to w0[0..16), w1[0..16)
+  template <class T>
+  GBDE_D static void w_osc_rows(int l, T dg, T w10, T w11, T ka, T* w0, T* w1) {
     const int e = 2 * l;
-    const T dx = T(-2) * mu * x * v - T(1) - T(2) * ka, dvv = mu * (T(1) - x * x);
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
       w0[c] = T(0);
@@ -150,10 +156,32 @@ struct VdpRing8 {
     }
     w0[e] = dg;
     w0[e + 1] = T(-1);
-    w1[e] = -dx;
-    w1[e + 1] = dg - dvv;
+    w1[e] = w10;
+    w1[e + 1] = w11;
     w1[(e + 14) & 15] = -ka;
     w1[(e + 2) & 15] = -ka;
+  }
+  // r = b - W x on rows 2l, 2l + 1 with W's nonzeros (w_osc_nz) as pairs P
+  // and x FP32 values (the lane's components; its neighbours' first
+  // components fetched), accumulated in Acc (a pair accumulator with set /
+  // fma / add / get): the residual of an FP32 solve, for a step of iterative
+  // refinement.
+  template <class Acc, class P, class Sh>
+  GBDE_D static void w_osc_residual(int l, P dg, P w10, P w11, P ka, const P* b, const float* x,
+                                    const Sh& sh, P* r) {
+    const float xl = sh.bcast(x[0], (l + 7) & 7), xr = sh.bcast(x[0], (l + 1) & 7);
+    Acc a;
+    a.set(b[0]);
+    a.fma(-dg, P(x[0], 0.0f));
+    a.add(P(x[1], 0.0f));
+    r[0] = a.get();
+    Acc c;
+    c.set(b[1]);
+    c.fma(-w10, P(x[0], 0.0f));
+    c.fma(-w11, P(x[1], 0.0f));
+    c.fma(ka, P(xl, 0.0f));
+    c.fma(ka, P(xr, 0.0f));
+    r[1] = c.get();
   }
   template <class T, class Sh>
   GBDE_D static void jac_lane(int r, T y, const T* p, const Sh& sh, T* Jr) {

@@ -688,35 +688,29 @@ struct TeamTsit5FF {
 // for: 12 teams, 36.9 KB (W rows 26.1 KB, stages 10.8 KB), 6 CTAs per SM
 constexpr int kTeam8Threads = 96;
 
-// W of this team: 16 rows of 17 doubles (the stride keeps a team's row
-// accesses conflict-free), 2,176 bytes per team.  Row i sits in
-// slot i at even team positions and in slot i + 1 (mod 16) at odd ones: the
-// two teams of a half-warp then read their rows at the same column through
-// disjoint banks (an even team at word offsets 4l + 2k (mod 32) for lane l,
-// column k; an odd one at 4l + 2k + 2).
-GBDE_D double* team8_row(int i) {
-  __shared__ double rows[kTeam8Threads / TEAM8 * TEAM * kTeamLuStride];
+// W of this team as FP32 rows: 16 rows of 17 floats, 1,088 bytes per team.
+// Row i sits in slot (i + s) mod 16, s = 1 for the third and fourth team of a
+// warp: the warp's 32 lanes then read their rows 2l + h at one column through
+// 32 distinct banks (team t: word 16 t + 17 ((2l + h + s) mod 16) + k, mod 32).
+GBDE_D float* team8_row(int i) {
+  __shared__ float rows[kTeam8Threads / TEAM8 * TEAM * kTeamLuStride];
   const int t = threadIdx.x / TEAM8;
-  return rows + (t * TEAM + ((i + (t & 1)) & (TEAM - 1))) * kTeamLuStride;
+  return rows + (t * TEAM + ((i + ((t >> 1) & 1)) & (TEAM - 1))) * kTeamLuStride;
 }
 
 struct TeamLU8 {
   uint64_t piv;  // pivot row of step k in bits [4k, 4k+4)
 
-  GBDE_D static ff* row(int i) { return reinterpret_cast<ff*>(team8_row(i)); }
-
-  // LU with partial pivoting, in FP32 pairs, of the W written as pairs into
-  // team8_row(): the pivot of step k is the unpivoted row with the largest
-  // |leading part| of a_k, ties to the lowest row position of the
-  // row-swapping LU (LAPACK getrf's order, as TeamLU); the rank-1 update runs
-  // column-parallel over the rows with a nonzero multiplier, lane l updating
-  // columns l and l + 8 in one paired accumulation.  GB300 runs FP32 at ~60x
-  // its FP64 rate: each FP64 update here was one FP64-pipe instruction of ~64
-  // cycles per warp on the elimination's critical path.
+  // LU with partial pivoting, in FP32, of the W written into team8_row(): the
+  // pivot of step k is the unpivoted row with the largest |a_k|, ties to the
+  // lowest row position of the row-swapping LU (LAPACK getrf's order, as
+  // TeamLU); the rank-1 update runs column-parallel over the rows with a
+  // nonzero multiplier (lane l updates columns l and l + 8).  The solves
+  // refine their FP32 result once against W in pairs (TeamRodasFF8).
   GBDE_D void factor(const Team8& tm) {
     const int r0 = 2 * tm.lane, r1 = r0 + 1;
-    ff* a0 = row(r0);
-    ff* a1 = row(r1);
+    float* a0 = team8_row(r0);
+    float* a1 = team8_row(r1);
     bool open0 = true, open1 = true;  // not yet a pivot row
     piv = 0;
     unsigned pos0 = (unsigned)r0, pos1 = (unsigned)r1;
@@ -724,10 +718,10 @@ struct TeamLU8 {
     __syncwarp(tm.mask);  // every lane's rows are written
 #pragma unroll 1
     for (int k = 0; k < TEAM; ++k) {
-      const ff ak0 = a0[k], ak1 = a1[k];
-      // |leading part| + 1 on the integer pipe (NaN ranks above every number)
-      const unsigned key0 = open0 ? (__float_as_uint(ak0.hi) & 0x7fffffffu) + 1u : 0u;
-      const unsigned key1 = open1 ? (__float_as_uint(ak1.hi) & 0x7fffffffu) + 1u : 0u;
+      const float ak0 = a0[k], ak1 = a1[k];
+      // |a_k| + 1 on the integer pipe (NaN ranks above every number)
+      const unsigned key0 = open0 ? (__float_as_uint(ak0) & 0x7fffffffu) + 1u : 0u;
+      const unsigned key1 = open1 ? (__float_as_uint(ak1) & 0x7fffffffu) + 1u : 0u;
       unsigned m = max(key0, key1);
 #pragma unroll
       for (int o = TEAM8 / 2; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(tm.mask, m, o, TEAM8));
@@ -741,45 +735,37 @@ struct TeamLU8 {
       if (open0 && pos0 == (unsigned)k && r0 != p) pos0 = ppos;  // swapped out
       if (open1 && pos1 == (unsigned)k && r1 != p) pos1 = ppos;
       piv |= (uint64_t)p << (4 * k);
-      const ff* prow = row(p);
-      const ff inv = ff_rcp(prow[k]);
+      const float* prow = team8_row(p);
+      const float inv = __frcp_rn(prow[k]);
       // multipliers of the open rows; l != 0 tested on the integer pipe
       bool u0 = false, u1 = false;
       if (r0 == p) {
         open0 = false;
       } else if (open0) {
-        const ff l = ak0 * inv;
+        const float l = xmul(ak0, inv);
         a0[k] = l;
-        u0 = (__float_as_uint(l.hi) << 1) != 0u;
+        u0 = (__float_as_uint(l) << 1) != 0u;
       }
       if (r1 == p) {
         open1 = false;
       } else if (open1) {
-        const ff l = ak1 * inv;
+        const float l = xmul(ak1, inv);
         a1[k] = l;
-        u1 = (__float_as_uint(l.hi) << 1) != 0u;
+        u1 = (__float_as_uint(l) << 1) != 0u;
       }
       const unsigned b0 = (__ballot_sync(tm.mask, u0) >> sh) & 0xFFu;  // rows 2j
       const unsigned b1 = (__ballot_sync(tm.mask, u1) >> sh) & 0xFFu;  // rows 2j + 1
       __syncwarp(tm.mask);  // the multipliers are in shared memory
       const int ca = tm.lane, cb = tm.lane + TEAM8;
-      const ff pa = prow[ca], pb = prow[cb];
-      const F2 ph = f2_pack(pa.hi, pb.hi), pl = f2_pack(pa.lo, pb.lo);
+      const float pa = prow[ca], pb = prow[cb];
       const bool wa = ca > k, wb = cb > k;
 #pragma unroll 1
       for (unsigned rows = b0 | (b1 << 8); rows != 0u; rows &= rows - 1u) {
         const int j = __ffs(rows) - 1;
-        ff* ar = row(j < 8 ? 2 * j : 2 * (j - 8) + 1);
-        const ff l = ar[k];
-        const ff xa = ar[ca], xb = ar[cb];
-        // (a_ca, a_cb) -= l (p_ca, p_cb), one paired accumulation
-        FfAcc2 acc;
-        acc.set(f2_pack(xa.hi, xb.hi), f2_pack(xa.lo, xb.lo));
-        acc.fma(f2_pack(-l.hi, -l.hi), f2_pack(-l.lo, -l.lo), f2_pack(l.hi, l.hi), ph, pl);
-        ff ya, yb;
-        acc.get(ya, yb);
-        if (wa) ar[ca] = ya;
-        if (wb) ar[cb] = yb;
+        float* ar = team8_row(j < 8 ? 2 * j : 2 * (j - 8) + 1);
+        const float l = ar[k];
+        if (wa) ar[ca] = xfma(-l, pa, ar[ca]);
+        if (wb) ar[cb] = xfma(-l, pb, ar[cb]);
       }
       __syncwarp(tm.mask);  // step k's updates land before step k+1 reads them
     }
@@ -790,32 +776,30 @@ struct TeamLU8 {
 // the pivot of step k (its L part in columns < k, U in columns > k) goes to
 // slot k, i.e. lane k / 2, half k % 2 -- the row order of LAPACK's
 // row-swapping factorisation.  Each entry is negated as it moves; each slot
-// keeps its pivot reciprocal.  With
-// the slots in step order, the source of every step of the substitutions is
-// lane k / 2, half k % 2, known from k: no pivot lookups, and the two halves'
-// selects fold at compile time.  Forward and back substitution keep a lane's
-// two slots in one paired accumulator.
-struct TeamLUFF8 {
-  ff invs[2];  // pivot reciprocals of this lane's slots 2l, 2l + 1
-  int q[2];    // the rows in them (their right-hand-side components)
+// keeps its pivot reciprocal.  With the slots in step order, the source of
+// every step of the substitutions is lane k / 2, half k % 2, known from k: no
+// pivot lookups, and the two halves' selects fold at compile time.  Forward
+// and back substitution keep a lane's two slots in one paired FP32 register.
+struct TeamLUF8 {
+  float invs[2];  // pivot reciprocals of this lane's slots 2l, 2l + 1
+  int q[2];       // the rows in them (their right-hand-side components)
 
-  GBDE_D static float2* row_ff(int i) { return reinterpret_cast<float2*>(team8_row(i)); }
   GBDE_D void from(const TeamLU8& W, const Team8& tm) {
     const int l = tm.lane;
     q[0] = (int)((W.piv >> (8 * l)) & 15u);
     q[1] = (int)((W.piv >> (8 * l + 4)) & 15u);
-    const ff* r0 = TeamLU8::row(q[0]);
-    const ff* r1 = TeamLU8::row(q[1]);
+    const float* r0 = team8_row(q[0]);
+    const float* r1 = team8_row(q[1]);
     // the reciprocal of each slot's diagonal, as factor() formed it
-    invs[0] = ff_rcp(r0[2 * l]);
-    invs[1] = ff_rcp(r1[2 * l + 1]);
+    invs[0] = __frcp_rn(r0[2 * l]);
+    invs[1] = __frcp_rn(r1[2 * l + 1]);
     // slot rows 2l, 2l + 1 receive rows q0, q1, four columns at a time: every
     // lane reads its columns before any lane overwrites them
-    float2* d0 = row_ff(2 * l);
-    float2* d1 = row_ff(2 * l + 1);
+    float* d0 = team8_row(2 * l);
+    float* d1 = team8_row(2 * l + 1);
 #pragma unroll 1
     for (int c0 = 0; c0 < TEAM; c0 += 4) {
-      ff v0[4], v1[4];
+      float v0[4], v1[4];
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
         v0[c] = r0[c0 + c];
@@ -824,56 +808,52 @@ struct TeamLUFF8 {
       __syncwarp(tm.mask);
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        d0[c0 + c] = make_float2(-v0[c].hi, -v0[c].lo);
-        d1[c0 + c] = make_float2(-v1[c].hi, -v1[c].lo);
+        d0[c0 + c] = -v0[c];
+        d1[c0 + c] = -v1[c];
       }
       __syncwarp(tm.mask);
     }
   }
 
-  // W x = b for this lane's components b[0], b[1] (x[0], x[1]: unknowns 2l,
-  // 2l + 1).  Slot s's accumulator starts from b of its row q_s.  Step k
-  // (source lane k / 2) updates the slots after k in the forward pass and
-  // those before k in the backward pass; a slot that takes no update adds a
-  // zero product.  The loops run over pairs of steps (2s, 2s + 1).
-  GBDE_D void solve(const ff* b, ff* x, const Team8& tm) const {
+  // W x = b in FP32 for this lane's components b[0], b[1] (x[0], x[1]:
+  // unknowns 2l, 2l + 1).  Slot s's accumulator starts from b of its row q_s.
+  // Step k (source lane k / 2) updates the slots after k in the forward pass
+  // and those before k in the backward pass; a slot that takes no update adds
+  // a zero product.  The loops run over pairs of steps (2s, 2s + 1).
+  GBDE_D void solve(const float* b, float* x, const Team8& tm) const {
     const int l = tm.lane;
-    const float2* n0 = row_ff(2 * l);
-    const float2* n1 = row_ff(2 * l + 1);
-    FfAcc2 acc;
+    const float* n0 = team8_row(2 * l);
+    const float* n1 = team8_row(2 * l + 1);
+    F2 acc;
     {
-      const ff a0 = tm.bcast(b[0], q[0] >> 1), a1 = tm.bcast(b[1], q[0] >> 1);
-      const ff c0 = tm.bcast(b[0], q[1] >> 1), c1 = tm.bcast(b[1], q[1] >> 1);
-      const ff s0 = (q[0] & 1) ? a1 : a0, s1 = (q[1] & 1) ? c1 : c0;
-      acc.set(f2_pack(s0.hi, s1.hi), f2_pack(s0.lo, s1.lo));
+      const float a0 = tm.bcast(b[0], q[0] >> 1), a1 = tm.bcast(b[1], q[0] >> 1);
+      const float c0 = tm.bcast(b[0], q[1] >> 1), c1 = tm.bcast(b[1], q[1] >> 1);
+      acc = f2_pack((q[0] & 1) ? a1 : a0, (q[1] & 1) ? c1 : c0);
     }
-    auto update = [&](ff z, float2 v0, float2 v1, bool e0, bool e1) {
-      acc.fma(f2_pack(z.hi, z.hi), f2_pack(z.lo, z.lo), f2_pack(-z.hi, -z.hi),
-              f2_pack(e0 ? v0.x : 0.0f, e1 ? v1.x : 0.0f),
-              f2_pack(e0 ? v0.y : 0.0f, e1 ? v1.y : 0.0f));
-    };
-#pragma unroll 2  // pair solve
+    float g0, g1;
+#pragma unroll 4
     for (int sl = 0; sl < TEAM8; ++sl) {  // forward: L z = P b, steps 2 sl, 2 sl + 1
       const bool gt = l > sl, ge = l >= sl;
-      ff g0, g1;
-      acc.get(g0, g1);
-      const ff za = tm.bcast(g0, sl);  // step 2 sl: slot 2 sl
-      update(za, n0[2 * sl], n1[2 * sl], gt, ge);
-      acc.get(g0, g1);
-      const ff zb = tm.bcast(g1, sl);  // step 2 sl + 1: slot 2 sl + 1
-      update(zb, n0[2 * sl + 1], n1[2 * sl + 1], gt, gt);
+      f2_unpack(acc, g0, g1);
+      const float za = tm.bcast(g0, sl);  // step 2 sl: slot 2 sl
+      acc = f2_fma(f2_pack(gt ? n0[2 * sl] : 0.0f, ge ? n1[2 * sl] : 0.0f), f2_pack(za, za), acc);
+      f2_unpack(acc, g0, g1);
+      const float zb = tm.bcast(g1, sl);  // step 2 sl + 1: slot 2 sl + 1
+      acc = f2_fma(f2_pack(gt ? n0[2 * sl + 1] : 0.0f, gt ? n1[2 * sl + 1] : 0.0f),
+                   f2_pack(zb, zb), acc);
     }
-#pragma unroll 2  // pair solve
+#pragma unroll 4
     for (int sl = TEAM8 - 1; sl >= 0; --sl) {  // backward: U x = z, steps 2 sl + 1, 2 sl
-      const bool lt = l < sl, le = l <= sl, own = l == sl;
-      ff g0, g1;
-      acc.get(g0, g1);
-      const ff xb = tm.bcast(g1 * invs[1], sl);  // step 2 sl + 1
-      update(xb, n0[2 * sl + 1], n1[2 * sl + 1], le, lt);
-      acc.get(g0, g1);
-      const ff xa = tm.bcast(g0 * invs[0], sl);  // step 2 sl
-      update(xa, n0[2 * sl], n1[2 * sl], lt, lt);
-      if (own) {
+      const bool lt = l < sl, le = l <= sl;
+      f2_unpack(acc, g0, g1);
+      const float xb = tm.bcast(xmul(g1, invs[1]), sl);  // step 2 sl + 1
+      acc = f2_fma(f2_pack(le ? n0[2 * sl + 1] : 0.0f, lt ? n1[2 * sl + 1] : 0.0f),
+                   f2_pack(xb, xb), acc);
+      f2_unpack(acc, g0, g1);
+      const float xa = tm.bcast(xmul(g0, invs[0]), sl);  // step 2 sl
+      acc = f2_fma(f2_pack(lt ? n0[2 * sl] : 0.0f, lt ? n1[2 * sl] : 0.0f), f2_pack(xa, xa),
+                   acc);
+      if (l == sl) {
         x[0] = xa;
         x[1] = xb;
       }
@@ -882,9 +862,10 @@ struct TeamLUFF8 {
 };
 
 // Rodas5 / Rodas5P in FP32 pairs on 8-lane teams (the method of RodasFF,
-// rodas_ff.cuh, for a lane's two components): Jacobian rows, W and its LU
-// (TeamLU8) in pairs, pair solves (TeamLUFF8), stage sums and dense output on
-// paired FP32 instructions, the norm's ratios FP32, their squares FP64.
+// rodas_ff.cuh, for a lane's two components): Jacobian rows and W in pairs;
+// W's LU (TeamLU8) and the substitutions (TeamLUF8) in FP32, each stage's
+// solve refined once against W in pairs; stage sums and dense output on
+// paired FP32 instructions; the norm's ratios FP32, their squares FP64.
 template <class M, class Tag>
 struct TeamRodasFF8 {
   using K = RodasCoef<Tag>;
@@ -935,12 +916,16 @@ struct TeamRodasFF8 {
       fresh = true;
     }
     const double ih = rcp64(dt);
-    TeamLUFF8 L;
+    // W = I/(h gamma) - J(uu): the nonzeros of rows 2l, 2l + 1 in pairs (for
+    // the residuals), the rows rounded to FP32 for the LU
+    const ff dg = ff_split(ih * (1.0 / K::g));
+    ff w10, w11;
+    M::w_osc_nz(uu, p, dg, w10, w11);
+    TeamLUF8 L;
     {
-      // rows 2l, 2l + 1 of W = I/(h gamma) - J(uu), in pairs
       TeamLU8 W;
-      M::w_osc(tm.lane, uu, p, ff_split(ih * (1.0 / K::g)), TeamLU8::row(2 * tm.lane),
-               TeamLU8::row(2 * tm.lane + 1));
+      M::w_osc_rows(tm.lane, (float)dg, (float)w10, (float)w11, (float)p[1],
+                    team8_row(2 * tm.lane), team8_row(2 * tm.lane + 1));
       W.factor(tm);
       L.from(W, tm);
     }
@@ -990,7 +975,21 @@ struct TeamRodasFF8 {
         r[1] = fy[1];
       }
       ff x[2];
-      L.solve(r, x, tm);
+      {
+        // W x = r: an FP32 solve and one refinement against W in pairs,
+        // x = x0 + d with W d = r - W x0 (residual in pairs).  W = I/(h gamma)
+        // - J is well conditioned here, so the refined error is about
+        // (cond(W) 2^-24)^2 of |x|, far below the tolerances.
+        float b32[2] = {(float)r[0], (float)r[1]}, x0[2], d[2];
+        L.solve(b32, x0, tm);
+        ff res[2];
+        M::template w_osc_residual<FfAcc>(tm.lane, dg, w10, w11, p[1], r, x0, tm, res);
+        b32[0] = (float)res[0];
+        b32[1] = (float)res[1];
+        L.solve(b32, d, tm);
+        x[0] = ff(x0[0], 0.0f) + ff(d[0], 0.0f);
+        x[1] = ff(x0[1], 0.0f) + ff(d[1], 0.0f);
+      }
       if (i < 7) {
         st(i, x);
       } else {
