@@ -1,7 +1,8 @@
 // k_team.cu -- team kernels for 16-state models (ring of 8 Van der Pol
 // oscillators, team.cuh): Rodas5 / Rodas5P with a row-distributed FP64 LU on
-// 16 lanes per trajectory (FP64 and FP32 state) or 8 lanes per trajectory
-// (FP32 pairs), and Tsit5 on 8 lanes per trajectory.
+// 16 lanes per trajectory (FP64 and FP32 state), or on 8 lanes per trajectory
+// in FP32 pairs with an FP32 LU, W^-1 and refined solves; Tsit5 on 8 lanes per
+// trajectory.
 #include "team.cuh"
 #include "launch.h"
 
@@ -12,10 +13,10 @@ namespace gbde {
 // solves), so more resident warps beat more registers.  With W's rows in
 // shared memory (team.cuh, 17 KB per CTA) the 16-lane Rodas steppers fit 6
 // CTAs (<= 80 registers, no spills).  The 8-lane pair Rodas holds 3 KB of
-// shared memory per trajectory (W rows and stages): CTAs of 96 threads (12
-// teams, 36.9 KB), 6 per SM, 96 registers -- 374 ms on the 250k stiff
-// trajectories against 377 ms with 128-thread CTAs at 4 per SM (48 KB, 125
-// registers) and 392 ms with 96 x 5.
+// shared memory per trajectory (FP32 W rows, W^-1 rows, stages): CTAs of 96
+// threads (12 teams, 36.1 KB), 6 per SM, 96 registers.  7 per SM caps the
+// registers at 80 and spills in the stage loop (457 against 261 ms on the
+// 250k stiff trajectories, with the refined FP32 substitutions).
 // The 8-lane Tsit5 teams measured 368 / 338 / 290 / 280 ms at 1 / 4 / 5 / 6
 // CTAs per SM on the 750k non-stiff trajectories of the 1M ring workload.
 template <class Alg> struct TeamMinBlocks { static constexpr int v = 1; };

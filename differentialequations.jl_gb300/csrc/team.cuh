@@ -735,8 +735,9 @@ struct TeamLU8 {
       if (open0 && pos0 == (unsigned)k && r0 != p) pos0 = ppos;  // swapped out
       if (open1 && pos1 == (unsigned)k && r1 != p) pos1 = ppos;
       piv |= (uint64_t)p << (4 * k);
-      const float* prow = team8_row(p);
+      float* prow = team8_row(p);
       const float inv = __frcp_rn(prow[k]);
+      if (tm.lane == (p >> 1)) prow[TEAM] = inv;  // the pivot's reciprocal, in the row's spare slot
       // multipliers of the open rows; l != 0 tested on the integer pipe
       bool u0 = false, u1 = false;
       if (r0 == p) {
@@ -772,100 +773,88 @@ struct TeamLU8 {
   }
 };
 
-// The factors of a TeamLU8 for the solves, in pivot order: the row that was
-// the pivot of step k (its L part in columns < k, U in columns > k) goes to
-// slot k, i.e. lane k / 2, half k % 2 -- the row order of LAPACK's
-// row-swapping factorisation.  Each entry is negated as it moves; each slot
-// keeps its pivot reciprocal.  With the slots in step order, the source of
-// every step of the substitutions is lane k / 2, half k % 2, known from k: no
-// pivot lookups, and the two halves' selects fold at compile time.  Forward
-// and back substitution keep a lane's two slots in one paired FP32 register.
-struct TeamLUF8 {
-  float invs[2];  // pivot reciprocals of this lane's slots 2l, 2l + 1
-  int q[2];       // the rows in them (their right-hand-side components)
+// Rows 2l, 2l + 1 of W^-1 = U^-1 L^-1 P for lane l, in FP32, from a
+// TeamLU8's factors: a solve W x = b is then the product of those rows with b
+// (every b_j broadcast), with no chain of dependent steps.
+//   row i of U^-1:  U^T a = e_i, right-looking over the slots k (U's row k is
+//                   the pivot row of step k, q_k: columns > k; the pivot's
+//                   reciprocal in its spare column 16);
+//   times L^-1:     L^T b = a, right-looking down from k = 15 (L's row k: q_k's
+//                   multipliers in columns < k);
+//   times P:        W^-1[i][q_k] = b_k.
+// The two rows share every coefficient and run as one paired FP32 register
+// per slot.  Storage: per thread 8 chunks of 16 bytes, chunk u holding
+// columns 2u, 2u + 1 of both rows, at position u ^ (lane & 7): the 8 threads
+// of a 128-byte load phase read distinct bank groups.
+struct TeamInvF8 {
+  GBDE_D static float4* rows() {
+    __shared__ float4 buf[kTeam8Threads * 8];
+    return buf + threadIdx.x * 8;
+  }
+  GBDE_D static int sw(int u) { return u ^ (int)(threadIdx.x & 7); }
 
-  GBDE_D void from(const TeamLU8& W, const Team8& tm) {
+  GBDE_D void build(const TeamLU8& W, const Team8& tm) const {
     const int l = tm.lane;
-    q[0] = (int)((W.piv >> (8 * l)) & 15u);
-    q[1] = (int)((W.piv >> (8 * l + 4)) & 15u);
-    const float* r0 = team8_row(q[0]);
-    const float* r1 = team8_row(q[1]);
-    // the reciprocal of each slot's diagonal, as factor() formed it
-    invs[0] = __frcp_rn(r0[2 * l]);
-    invs[1] = __frcp_rn(r1[2 * l + 1]);
-    // slot rows 2l, 2l + 1 receive rows q0, q1, four columns at a time: every
-    // lane reads its columns before any lane overwrites them
-    float* d0 = team8_row(2 * l);
-    float* d1 = team8_row(2 * l + 1);
-#pragma unroll 1
-    for (int c0 = 0; c0 < TEAM; c0 += 4) {
-      float v0[4], v1[4];
+    const F2 zero = f2_pack(0.0f, 0.0f);
+    F2 a[TEAM];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        v0[c] = r0[c0 + c];
-        v1[c] = r1[c0 + c];
-      }
-      __syncwarp(tm.mask);
+    for (int k = 0; k < TEAM; ++k)
+      a[k] = f2_pack(k == 2 * l ? 1.0f : 0.0f, k == 2 * l + 1 ? 1.0f : 0.0f);
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        d0[c0 + c] = -v0[c];
-        d1[c0 + c] = -v1[c];
+    for (int k = 0; k < TEAM; ++k) {  // U^T a = e_i
+      const float* r = team8_row((int)((W.piv >> (4 * k)) & 15u));
+      const float ip = r[TEAM];
+      a[k] = f2_prod(a[k], f2_pack(ip, ip));
+      const F2 na = f2_sub(zero, a[k]);
+#pragma unroll
+      for (int m = k + 1; m < TEAM; ++m) {
+        const float u = r[m];
+        a[m] = f2_fma(na, f2_pack(u, u), a[m]);
       }
-      __syncwarp(tm.mask);
+    }
+#pragma unroll
+    for (int k = TEAM - 1; k > 0; --k) {  // L^T b = a
+      const float* r = team8_row((int)((W.piv >> (4 * k)) & 15u));
+      const F2 nb = f2_sub(zero, a[k]);
+#pragma unroll
+      for (int m = 0; m < k; ++m) {
+        const float v = r[m];
+        a[m] = f2_fma(nb, f2_pack(v, v), a[m]);
+      }
+    }
+    unsigned long long* out = reinterpret_cast<unsigned long long*>(rows());
+#pragma unroll
+    for (int k = 0; k < TEAM; ++k) {  // column q_k
+      const int c = (int)((W.piv >> (4 * k)) & 15u);
+      out[2 * sw(c >> 1) + (c & 1)] = a[k].v;
     }
   }
 
-  // W x = b in FP32 for this lane's components b[0], b[1] (x[0], x[1]:
-  // unknowns 2l, 2l + 1).  Slot s's accumulator starts from b of its row q_s.
-  // Step k (source lane k / 2) updates the slots after k in the forward pass
-  // and those before k in the backward pass; a slot that takes no update adds
-  // a zero product.  The loops run over pairs of steps (2s, 2s + 1).
-  GBDE_D void solve(const float* b, float* x, const Team8& tm) const {
-    const int l = tm.lane;
-    const float* n0 = team8_row(2 * l);
-    const float* n1 = team8_row(2 * l + 1);
-    F2 acc;
-    {
-      const float a0 = tm.bcast(b[0], q[0] >> 1), a1 = tm.bcast(b[1], q[0] >> 1);
-      const float c0 = tm.bcast(b[0], q[1] >> 1), c1 = tm.bcast(b[1], q[1] >> 1);
-      acc = f2_pack((q[0] & 1) ? a1 : a0, (q[1] & 1) ? c1 : c0);
+  // x = W^-1 b for this lane's unknowns 2l, 2l + 1 (b[0], b[1] likewise)
+  GBDE_D void apply(const float* b, float* x, const Team8& tm) const {
+    const float4* w = rows();
+    const F2 bb = f2_pack(b[0], b[1]);
+    F2 acc0 = f2_pack(0.0f, 0.0f), acc1 = acc0;
+#pragma unroll
+    for (int u = 0; u < TEAM8; ++u) {
+      const float4 c = w[sw(u)];
+      F2 bu;
+      bu.v = __shfl_sync(tm.mask, bb.v, u, TEAM8);  // b_2u, b_2u+1
+      float b0, b1;
+      f2_unpack(bu, b0, b1);
+      acc0 = f2_fma(f2_pack(c.x, c.y), f2_pack(b0, b0), acc0);
+      acc1 = f2_fma(f2_pack(c.z, c.w), f2_pack(b1, b1), acc1);
     }
-    float g0, g1;
-#pragma unroll 4
-    for (int sl = 0; sl < TEAM8; ++sl) {  // forward: L z = P b, steps 2 sl, 2 sl + 1
-      const bool gt = l > sl, ge = l >= sl;
-      f2_unpack(acc, g0, g1);
-      const float za = tm.bcast(g0, sl);  // step 2 sl: slot 2 sl
-      acc = f2_fma(f2_pack(gt ? n0[2 * sl] : 0.0f, ge ? n1[2 * sl] : 0.0f), f2_pack(za, za), acc);
-      f2_unpack(acc, g0, g1);
-      const float zb = tm.bcast(g1, sl);  // step 2 sl + 1: slot 2 sl + 1
-      acc = f2_fma(f2_pack(gt ? n0[2 * sl + 1] : 0.0f, gt ? n1[2 * sl + 1] : 0.0f),
-                   f2_pack(zb, zb), acc);
-    }
-#pragma unroll 4
-    for (int sl = TEAM8 - 1; sl >= 0; --sl) {  // backward: U x = z, steps 2 sl + 1, 2 sl
-      const bool lt = l < sl, le = l <= sl;
-      f2_unpack(acc, g0, g1);
-      const float xb = tm.bcast(xmul(g1, invs[1]), sl);  // step 2 sl + 1
-      acc = f2_fma(f2_pack(le ? n0[2 * sl + 1] : 0.0f, lt ? n1[2 * sl + 1] : 0.0f),
-                   f2_pack(xb, xb), acc);
-      f2_unpack(acc, g0, g1);
-      const float xa = tm.bcast(xmul(g0, invs[0]), sl);  // step 2 sl
-      acc = f2_fma(f2_pack(lt ? n0[2 * sl] : 0.0f, lt ? n1[2 * sl] : 0.0f), f2_pack(xa, xa),
-                   acc);
-      if (l == sl) {
-        x[0] = xa;
-        x[1] = xb;
-      }
-    }
+    f2_unpack(f2_add(acc0, acc1), x[0], x[1]);
   }
 };
 
 // Rodas5 / Rodas5P in FP32 pairs on 8-lane teams (the method of RodasFF,
 // rodas_ff.cuh, for a lane's two components): Jacobian rows and W in pairs;
-// W's LU (TeamLU8) and the substitutions (TeamLUF8) in FP32, each stage's
-// solve refined once against W in pairs; stage sums and dense output on
-// paired FP32 instructions; the norm's ratios FP32, their squares FP64.
+// W's LU (TeamLU8) and the rows of W^-1 (TeamInvF8) in FP32, each stage's
+// solve a product with W^-1 refined once against W in pairs; stage sums and
+// dense output on paired FP32 instructions; the norm's ratios FP32, their
+// squares FP64.
 template <class M, class Tag>
 struct TeamRodasFF8 {
   using K = RodasCoef<Tag>;
@@ -921,13 +910,13 @@ struct TeamRodasFF8 {
     const ff dg = ff_split(ih * (1.0 / K::g));
     ff w10, w11;
     M::w_osc_nz(uu, p, dg, w10, w11);
-    TeamLUF8 L;
+    TeamInvF8 L;
     {
       TeamLU8 W;
       M::w_osc_rows(tm.lane, (float)dg, (float)w10, (float)w11, (float)p[1],
                     team8_row(2 * tm.lane), team8_row(2 * tm.lane + 1));
       W.factor(tm);
-      L.from(W, tm);
+      L.build(W, tm);
     }
     const ff iht = ff_split(ih);
     const RodasFfTab& tb = c_rodas_ff[RodasFfIdx<Tag>::v];
@@ -976,17 +965,17 @@ struct TeamRodasFF8 {
       }
       ff x[2];
       {
-        // W x = r: an FP32 solve and one refinement against W in pairs,
-        // x = x0 + d with W d = r - W x0 (residual in pairs).  W = I/(h gamma)
-        // - J is well conditioned here, so the refined error is about
-        // (cond(W) 2^-24)^2 of |x|, far below the tolerances.
+        // W x = r: an FP32 solve (x0 = W^-1 r) and one refinement against W
+        // in pairs, x = x0 + d with d = W^-1 (r - W x0) (residual in pairs).
+        // W = I/(h gamma) - J is well conditioned here, so the refined error
+        // is about (cond(W) 2^-24)^2 of |x|, far below the tolerances.
         float b32[2] = {(float)r[0], (float)r[1]}, x0[2], d[2];
-        L.solve(b32, x0, tm);
+        L.apply(b32, x0, tm);
         ff res[2];
         M::template w_osc_residual<FfAcc>(tm.lane, dg, w10, w11, p[1], r, x0, tm, res);
         b32[0] = (float)res[0];
         b32[1] = (float)res[1];
-        L.solve(b32, d, tm);
+        L.apply(b32, d, tm);
         x[0] = ff(x0[0], 0.0f) + ff(d[0], 0.0f);
         x[1] = ff(x0[1], 0.0f) + ff(d[1], 0.0f);
       }
