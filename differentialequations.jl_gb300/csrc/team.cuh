@@ -438,7 +438,23 @@ struct Team8 {
     for (int o = TEAM8 / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o, TEAM8);
     return v;
   }
+  GBDE_D float sum(float v) const {
+#pragma unroll
+    for (int o = TEAM8 / 2; o > 0; o >>= 1) v = xadd(v, __shfl_xor_sync(mask, v, o, TEAM8));
+    return v;
+  }
 };
+
+// The mean of the squared norm ratios e_c of a lane's two components over the
+// team's 16, in FP32: each ratio is already an FP32 value (relative error
+// ~2^-24), which the FP32 squares and sum leave at that order.  GB300 issues
+// one FP64 warp instruction per ~64 cycles per SM sub-partition: the FP64
+// form (2 FMAs, 3 additions, a product per attempt) was the non-stiff pair
+// kernel's FP64-pipe bottleneck.  Returned as a double (integer-pipe widening).
+GBDE_D double team8_mean_sq(const Team8& tm, float e0, float e1) {
+  const float s = tm.sum(xfma(e1, e1, xmul(e0, e0)));
+  return f2d_bits(xmul(s, 1.0f / (2 * TEAM8)));
+}
 
 template <class M, class T>
 struct TeamTsit5P {
@@ -535,7 +551,8 @@ struct TeamTsit5P {
 // FP32 register (FfVec<2>), so every stage argument, the new state, the error
 // estimate and the dense output are one unnormalised accumulation of paired
 // instructions over the pre-scaled stages h k_j (as Tsit5FF, tsit5_ff.cuh);
-// the norm's ratios are FP32 on the leading parts, their squares FP64.
+// the norm's ratios are FP32 on the leading parts, their mean square FP32
+// (team8_mean_sq).
 template <class M>
 struct TeamTsit5FF {
   using T = ff;
@@ -634,14 +651,13 @@ struct TeamTsit5FF {
     a.get(err);
     const ff as = ff_split(abstol), rs = ff_split(reltol);
     const float atf = xadd(as.hi, as.lo), rtf = xadd(rs.hi, rs.lo);
-    double e2 = 0.0;
+    float e[2];
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
       const float m = fmaxf(fabsf(uu[c].hi), fabsf(un[c].hi));
-      const double ed = f2d_bits(__fdiv_rn(err[c].hi, fmaf(rtf, m, atf)));
-      e2 = fma(ed, ed, e2);
+      e[c] = __fdiv_rn(err[c].hi, fmaf(rtf, m, atf));
     }
-    return tm.sum(e2) * (1.0 / M::N);
+    return team8_mean_sq(tm, e[0], e[1]);
   }
 
   // Tsit5's interpolation polynomials in pair arithmetic (as Tsit5FF::interp)
@@ -683,9 +699,10 @@ struct TeamTsit5FF {
 // 2l and 2l + 1 of W (its oscillator's x and v rows) and components 2l, 2l + 1
 // of every stage, so a warp carries 4 trajectories and the pair arithmetic of
 // a lane's two components runs on paired FP32 instructions (FfAcc2, FfVec<2>).
-// Same method, pivot order and FP64 factorisation as TeamLU / TeamRodas.
+// Same method and pivot rule as TeamLU / TeamRodas.
 // CTA size of the 8-lane pair Rodas kernel, which its shared arrays are sized
-// for: 12 teams, 36.9 KB (W rows 26.1 KB, stages 10.8 KB), 6 CTAs per SM
+// for: 12 teams, 36.1 KB (FP32 W rows 13.1 KB, W^-1 rows 12.3 KB, stages
+// 10.8 KB), 6 CTAs per SM
 constexpr int kTeam8Threads = 96;
 
 // W of this team as FP32 rows: 16 rows of 17 floats, 1,088 bytes per team.
@@ -853,8 +870,8 @@ struct TeamInvF8 {
 // rodas_ff.cuh, for a lane's two components): Jacobian rows and W in pairs;
 // W's LU (TeamLU8) and the rows of W^-1 (TeamInvF8) in FP32, each stage's
 // solve a product with W^-1 refined once against W in pairs; stage sums and
-// dense output on paired FP32 instructions; the norm's ratios FP32, their
-// squares FP64.
+// dense output on paired FP32 instructions; the norm's ratios and their mean
+// square FP32 (team8_mean_sq).
 template <class M, class Tag>
 struct TeamRodasFF8 {
   using K = RodasCoef<Tag>;
@@ -988,10 +1005,10 @@ struct TeamRodasFF8 {
     }
     nf += 7;
     // y1 = U_7 + u_8; error estimate u_8 (ratios FP32 on the leading parts,
-    // squares FP64, as RodasFF)
+    // their mean square in FP32)
     const ff as = ff_split(abstol), rs = ff_split(reltol);
     const float atf = xadd(as.hi, as.lo), rtf = xadd(rs.hi, rs.lo);
-    double e2 = 0.0;
+    float e[2];
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
       FfAcc a;
@@ -999,10 +1016,9 @@ struct TeamRodasFF8 {
       a.add(s[c]);
       un[c] = a.get();
       const float m = fmaxf(fabsf(uu[c].hi), fabsf(un[c].hi));
-      const double e = f2d_bits(__fdiv_rn(s[c].hi, fmaf(rtf, m, atf)));
-      e2 = fma(e, e, e2);
+      e[c] = __fdiv_rn(s[c].hi, fmaf(rtf, m, atf));
     }
-    return tm.sum(e2) * (1.0 / M::N);
+    return team8_mean_sq(tm, e[0], e[1]);
   }
 
   // dense output as RodasFF::interp for the lane's two components
