@@ -736,17 +736,22 @@ struct TeamLU8 {
 #pragma unroll 1
     for (int k = 0; k < TEAM; ++k) {
       const float ak0 = a0[k], ak1 = a1[k];
-      // |a_k| + 1 on the integer pipe (NaN ranks above every number)
-      const unsigned key0 = open0 ? (__float_as_uint(ak0) & 0x7fffffffu) + 1u : 0u;
-      const unsigned key1 = open1 ? (__float_as_uint(ak1) & 0x7fffffffu) + 1u : 0u;
-      unsigned m = max(key0, key1);
+      // one maximum over (|a_k| + 1, then the lowest (position, row), packed
+      // and inverted) on the integer pipe: the largest magnitude, ties to the
+      // lowest position (NaN ranks above every number; closed rows are 0)
+      const uint64_t key0 = open0 ? ((uint64_t)((__float_as_uint(ak0) & 0x7fffffffu) + 1u) << 32) |
+                                        (uint64_t)(~((pos0 << 4) | (unsigned)r0))
+                                  : 0ull;
+      const uint64_t key1 = open1 ? ((uint64_t)((__float_as_uint(ak1) & 0x7fffffffu) + 1u) << 32) |
+                                        (uint64_t)(~((pos1 << 4) | (unsigned)r1))
+                                  : 0ull;
+      uint64_t m = key0 > key1 ? key0 : key1;
 #pragma unroll
-      for (int o = TEAM8 / 2; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(tm.mask, m, o, TEAM8));
-      // ties: the lowest position; (position, row) packed, positions unique
-      unsigned pk = min(key0 == m ? (pos0 << 4) | (unsigned)r0 : 0xFFFFFFFFu,
-                        key1 == m ? (pos1 << 4) | (unsigned)r1 : 0xFFFFFFFFu);
-#pragma unroll
-      for (int o = TEAM8 / 2; o > 0; o >>= 1) pk = min(pk, __shfl_xor_sync(tm.mask, pk, o, TEAM8));
+      for (int o = TEAM8 / 2; o > 0; o >>= 1) {
+        const uint64_t x = __shfl_xor_sync(tm.mask, m, o, TEAM8);
+        m = x > m ? x : m;
+      }
+      const unsigned pk = ~(unsigned)m;  // (position, row) of the pivot
       const unsigned ppos = pk >> 4;
       const int p = (int)(pk & 15u);
       if (open0 && pos0 == (unsigned)k && r0 != p) pos0 = ppos;  // swapped out
@@ -777,13 +782,22 @@ struct TeamLU8 {
       const int ca = tm.lane, cb = tm.lane + TEAM8;
       const float pa = prow[ca], pb = prow[cb];
       const bool wa = ca > k, wb = cb > k;
+      // two rows per pass, their loads ahead of the updates (distinct rows)
 #pragma unroll 1
-      for (unsigned rows = b0 | (b1 << 8); rows != 0u; rows &= rows - 1u) {
-        const int j = __ffs(rows) - 1;
-        float* ar = team8_row(j < 8 ? 2 * j : 2 * (j - 8) + 1);
-        const float l = ar[k];
-        if (wa) ar[ca] = xfma(-l, pa, ar[ca]);
-        if (wb) ar[cb] = xfma(-l, pb, ar[cb]);
+      for (unsigned rows = b0 | (b1 << 8); rows != 0u;) {
+        const int j1 = __ffs(rows) - 1;
+        rows &= rows - 1u;
+        const bool two = rows != 0u;
+        const int j2 = two ? __ffs(rows) - 1 : j1;
+        rows &= rows - 1u;
+        float* ar1 = team8_row(j1 < 8 ? 2 * j1 : 2 * (j1 - 8) + 1);
+        float* ar2 = team8_row(j2 < 8 ? 2 * j2 : 2 * (j2 - 8) + 1);
+        const float l1 = ar1[k], x1a = ar1[ca], x1b = ar1[cb];
+        const float l2 = ar2[k], x2a = ar2[ca], x2b = ar2[cb];
+        if (wa) ar1[ca] = xfma(-l1, pa, x1a);
+        if (wb) ar1[cb] = xfma(-l1, pb, x1b);
+        if (two && wa) ar2[ca] = xfma(-l2, pa, x2a);
+        if (two && wb) ar2[cb] = xfma(-l2, pb, x2b);
       }
       __syncwarp(tm.mask);  // step k's updates land before step k+1 reads them
     }
