@@ -1070,7 +1070,11 @@ struct TeamRodasFF8 {
 };
 
 // integrate_team for 8-lane teams with two components per lane: the same
-// controller, saves, return codes and deadline.
+// controller, saves, return codes and deadline.  One flat loop: a team whose
+// trajectory has ended writes its results and takes the next one inside the
+// loop body, then rejoins the other teams of its warp at the attempt, so the
+// warp's four teams step together instead of waiting, trajectory by
+// trajectory, for the one with the most steps.
 template <class Alg, class M, class T, bool MIXED>
 __device__ void integrate_team8(const KArgs& a) {
   Team8 tm;
@@ -1081,156 +1085,165 @@ __device__ void integrate_team8(const KArgs& a) {
   Alg alg;
   T p[M::NP];
   const int c0 = 2 * tm.lane;  // this lane's first component
+  int64_t i = -1;              // the team's trajectory (-1: none yet)
+  double t = 0.0, tf = 0.0, dt = 0.0, dt1 = 0.0;
+  int js = 0, nacc = 0, nrej = 0, nfev = 0;
+  int64_t iters = 0;
+  float lqold = 0.0f;
+  int ret = GBDE_RET_SUCCESS;  // anything but DEFAULT: take a trajectory
+  auto store = [&](int j, double v0, double v1) {  // FP64 values of this lane's components
+    if (a.red) {
+      reduce_add(a, j, c0, M::N, v0);
+      reduce_add(a, j, c0 + 1, M::N, v1);
+    }
+    if (a.u_out == nullptr) return;
+    const size_t o = ((size_t)i * a.n_save + j) * M::N + c0;
+    if (a.out_f32) {
+      ((float*)a.u_out)[o] = (float)v0;
+      ((float*)a.u_out)[o + 1] = (float)v1;
+    } else {
+      ((double*)a.u_out)[o] = v0;
+      ((double*)a.u_out)[o + 1] = v1;
+    }
+  };
   while (true) {
-    // ---- next trajectory (team-uniform)
-    int64_t i;
-    if (a.queue == nullptr) {
-      if (!first) break;
-      i = team_id < a.N ? (a.order ? (int64_t)a.order[team_id] : team_id) : -1;
-    } else {
-      unsigned long long idx = 0;
-      if (tm.lane == 0) idx = atomicAdd(a.queue, 1ull);
-      idx = tm.bcast(idx, 0);
-      i = idx < (unsigned long long)a.N ? (a.order ? (int64_t)a.order[idx] : (int64_t)idx) : -1;
-    }
-    first = false;
-    if (i < 0) break;
-#pragma unroll
-    for (int k = 0; k < M::NP; ++k) p[k] = (T)__ldg(a.p + (size_t)i * M::NP + k);
-    // scalar loads and stores: the caller's arrays need only element alignment
-    const double u0x = __ldg(a.u0 + (size_t)i * M::N + c0);
-    const double u0y = __ldg(a.u0 + (size_t)i * M::N + c0 + 1);
-    const T u0[2] = {(T)u0x, (T)u0y};
-    double t = __ldg(a.t0 + i);
-    const double tf = __ldg(a.tf + i);
-    int js = 0, nacc = 0, nrej = 0, nfev = 0;
-    int64_t iters = 0;
-    float lqold = a.ctl.lqoldinit;
-    double dt1 = __longlong_as_double(0x7ff8000000000000ll);
-    int ret = GBDE_RET_DEFAULT;
-    const bool bad_lane = !isfinite(u0x) || !isfinite(u0y);
-    const bool bad = !(tf >= t) || !isfinite(t) || !isfinite(tf) ||
-                     __any_sync(tm.mask, bad_lane);
-    auto store = [&](int j, double v0, double v1) {  // FP64 values of this lane's components
-      if (a.red) {
-        reduce_add(a, j, c0, M::N, v0);
-        reduce_add(a, j, c0 + 1, M::N, v1);
-      }
-      if (a.u_out == nullptr) return;
-      const size_t o = ((size_t)i * a.n_save + j) * M::N + c0;
-      if (a.out_f32) {
-        ((float*)a.u_out)[o] = (float)v0;
-        ((float*)a.u_out)[o + 1] = (float)v1;
-      } else {
-        ((double*)a.u_out)[o] = v0;
-        ((double*)a.u_out)[o + 1] = v1;
-      }
-    };
-    // save points at t0 store u0 exactly (the FP64 input, whatever T)
-    while (js < a.n_save && save_time(a, i, js) <= t) store(js++, u0x, u0y);
-    double dt = 0.0;
-    if (bad) {
-      ret = GBDE_RET_INITIALFAILURE;
-    } else {
-      alg.init(u0, p, tm, nfev);
-      if (a.pred_dt != nullptr && a.pred_dt[i] > 0.f) {
-        dt = fmin((double)a.pred_dt[i], tf - t);
-      } else if (a.dt0 > 0.0 || !a.adaptive) {
-        dt = a.dt0;
-      } else {
-        // Hairer-Wanner starting step (hw_h0 / hw_dt, controller.h)
-        double r[2], s0 = 0.0, s1 = 0.0;
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-          r[c] = rcp64(a.abstol + fabs((double)alg.u()[c]) * a.reltol);
-          const double x = (double)alg.u()[c] * r[c], y = (double)alg.f0()[c] * r[c];
-          s0 += x * x;
-          s1 += y * y;
+    if (ret != GBDE_RET_DEFAULT) {
+      // ---- finish the trajectory; save slots never reached hold NaN
+      if (i >= 0) {
+        const double nanv = __longlong_as_double(0x7ff8000000000000ll);
+        for (; js < a.n_save; ++js) store(js, nanv, nanv);
+        if (tm.lane == 0) {
+          a.retcode[i] = ret;
+          if (a.naccept) a.naccept[i] = nacc;
+          if (a.nreject) a.nreject[i] = nrej;
+          if (a.nf) a.nf[i] = nfev;
+          if (a.t_end) a.t_end[i] = t;
+          if (a.method_out) a.method_out[i] = Alg::ALG_ID;
+          if (a.dt_first) a.dt_first[i] = dt1;
         }
-        s0 = tm.sum(s0) * (1.0 / M::N);
-        s1 = tm.sum(s1) * (1.0 / M::N);
-        const double h0 = hw_h0(s0, s1, tf - t);
-        T y[2], f1[2];
-#pragma unroll
-        for (int c = 0; c < 2; ++c) y[c] = alg.u()[c] + T(h0) * alg.f0()[c];
-        alg.rhs(y, p, tm, f1);
-        ++nfev;
-        double s2 = 0.0;
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-          const double z = ((double)f1[c] - (double)alg.f0()[c]) * r[c];
-          s2 += z * z;
-        }
-        dt = hw_dt(h0, s1, tm.sum(s2) * (1.0 / M::N), tf - t, Alg::ORDER);
       }
-      if (a.dtmax > 0.0) dt = fmin(dt, a.dtmax);
-      if (!(t < tf)) ret = GBDE_RET_SUCCESS;
-      else if (!(dt > 0.0)) ret = GBDE_RET_DTLESSTHANMIN;
-    }
-    while (ret == GBDE_RET_DEFAULT) {
-      const double rem = tf - t;
-      double h = dt;
-      bool last = false;
-      if (ord_bits(h * (1.0 + 1e-10)) >= ord_bits(rem)) {
-        h = rem;
-        last = true;
+      // ---- next trajectory (team-uniform)
+      if (a.queue == nullptr) {
+        i = first && team_id < a.N ? (a.order ? (int64_t)a.order[team_id] : team_id) : -1;
+      } else {
+        unsigned long long idx = 0;
+        if (tm.lane == 0) idx = atomicAdd(a.queue, 1ull);
+        idx = tm.bcast(idx, 0);
+        i = idx < (unsigned long long)a.N ? (a.order ? (int64_t)a.order[idx] : (int64_t)idx) : -1;
       }
-      const double ms = alg.attempt(h, p, a.abstol, a.reltol, tm, nfev);
-      ++iters;
-      if (!a.adaptive || mag_bits(ms) <= 0x3FF0000000000000ull) {  // ms <= 1 (integer pipe)
-        double dtnew = h;
-        if (a.adaptive) dtnew = h * f2d_bits(ctl_accept(a.ctl, ms, lqold));
-        const double tnew = last ? tf : t + h;  // plain FP64, as the oracle
-        const uint64_t tnew_o = ord_bits(tnew);
-        while (js < a.n_save) {
-          const double ts = save_time(a, i, js);
-          const uint64_t ts_o = ord_bits(ts);
-          if (ts_o > tnew_o) break;
-          if (ts_o == tnew_o) {
-            store(js, (double)alg.unew()[0], (double)alg.unew()[1]);
-          } else {
-            T v[2];
-            alg.interp((ts - t) * rcp64(h), h, v);
-            store(js, (double)v[0], (double)v[1]);
+      first = false;
+      if (i < 0) break;
+#pragma unroll
+      for (int k = 0; k < M::NP; ++k) p[k] = (T)__ldg(a.p + (size_t)i * M::NP + k);
+      // scalar loads and stores: the caller's arrays need only element alignment
+      const double u0x = __ldg(a.u0 + (size_t)i * M::N + c0);
+      const double u0y = __ldg(a.u0 + (size_t)i * M::N + c0 + 1);
+      const T u0[2] = {(T)u0x, (T)u0y};
+      t = __ldg(a.t0 + i);
+      tf = __ldg(a.tf + i);
+      js = nacc = nrej = nfev = 0;
+      iters = 0;
+      lqold = a.ctl.lqoldinit;
+      dt1 = __longlong_as_double(0x7ff8000000000000ll);
+      ret = GBDE_RET_DEFAULT;
+      const bool bad_lane = !isfinite(u0x) || !isfinite(u0y);
+      const bool bad = !(tf >= t) || !isfinite(t) || !isfinite(tf) ||
+                       __any_sync(tm.mask, bad_lane);
+      // save points at t0 store u0 exactly (the FP64 input, whatever T)
+      while (js < a.n_save && save_time(a, i, js) <= t) store(js++, u0x, u0y);
+      dt = 0.0;
+      if (bad) {
+        ret = GBDE_RET_INITIALFAILURE;
+      } else {
+        alg.init(u0, p, tm, nfev);
+        if (a.pred_dt != nullptr && a.pred_dt[i] > 0.f) {
+          dt = fmin((double)a.pred_dt[i], tf - t);
+        } else if (a.dt0 > 0.0 || !a.adaptive) {
+          dt = a.dt0;
+        } else {
+          // Hairer-Wanner starting step (hw_h0 / hw_dt, controller.h)
+          double r[2], s0 = 0.0, s1 = 0.0;
+#pragma unroll
+          for (int c = 0; c < 2; ++c) {
+            r[c] = rcp64(a.abstol + fabs((double)alg.u()[c]) * a.reltol);
+            const double x = (double)alg.u()[c] * r[c], y = (double)alg.f0()[c] * r[c];
+            s0 += x * x;
+            s1 += y * y;
           }
-          ++js;
-        }
-        alg.accept();
-        t = tnew;
-        if (nacc == 0) dt1 = h;
-        ++nacc;
-        if (__any_sync(tm.mask, !val_finite(alg.u()[0]) || !val_finite(alg.u()[1])))
-          ret = GBDE_RET_UNSTABLE;
-        else if (last) ret = GBDE_RET_SUCCESS;
-        dt = a.dtmax > 0.0 && ord_bits(dtnew) > ord_bits(a.dtmax) ? a.dtmax : dtnew;
-      } else {
-        ++nrej;
-        dt = h * f2d_bits(ctl_reject(a.ctl, ms));
-      }
-      if (ret == GBDE_RET_DEFAULT) {
-        if (iters >= a.maxiters) ret = GBDE_RET_MAXITERS;
-        else if (a.adaptive && dt_too_small(dt, a.dtmin, t))
-          ret = GBDE_RET_DTLESSTHANMIN;
-        else if (a.timeout_ns && (iters & 31) == 0) {
-          // lane 0's clock decides for the team
-          const int late = tm.bcast((int)(global_ns() - t_start > a.timeout_ns), 0);
-          if (late) {
-            ret = GBDE_RET_TIMEOUT;
-            if (tm.lane == 0) atomicOr(a.flag, 1);
+          s0 = tm.sum(s0) * (1.0 / M::N);
+          s1 = tm.sum(s1) * (1.0 / M::N);
+          const double h0 = hw_h0(s0, s1, tf - t);
+          T y[2], f1[2];
+#pragma unroll
+          for (int c = 0; c < 2; ++c) y[c] = alg.u()[c] + T(h0) * alg.f0()[c];
+          alg.rhs(y, p, tm, f1);
+          ++nfev;
+          double s2 = 0.0;
+#pragma unroll
+          for (int c = 0; c < 2; ++c) {
+            const double z = ((double)f1[c] - (double)alg.f0()[c]) * r[c];
+            s2 += z * z;
           }
+          dt = hw_dt(h0, s1, tm.sum(s2) * (1.0 / M::N), tf - t, Alg::ORDER);
+        }
+        if (a.dtmax > 0.0) dt = fmin(dt, a.dtmax);
+        if (!(t < tf)) ret = GBDE_RET_SUCCESS;
+        else if (!(dt > 0.0)) ret = GBDE_RET_DTLESSTHANMIN;
+      }
+      if (ret != GBDE_RET_DEFAULT) continue;  // ended before any step
+    }
+    // ---- one attempted step
+    const double rem = tf - t;
+    double h = dt;
+    bool last = false;
+    if (ord_bits(h * (1.0 + 1e-10)) >= ord_bits(rem)) {
+      h = rem;
+      last = true;
+    }
+    const double ms = alg.attempt(h, p, a.abstol, a.reltol, tm, nfev);
+    ++iters;
+    if (!a.adaptive || mag_bits(ms) <= 0x3FF0000000000000ull) {  // ms <= 1 (integer pipe)
+      double dtnew = h;
+      if (a.adaptive) dtnew = h * f2d_bits(ctl_accept(a.ctl, ms, lqold));
+      const double tnew = last ? tf : t + h;  // plain FP64, as the oracle
+      const uint64_t tnew_o = ord_bits(tnew);
+      while (js < a.n_save) {
+        const double ts = save_time(a, i, js);
+        const uint64_t ts_o = ord_bits(ts);
+        if (ts_o > tnew_o) break;
+        if (ts_o == tnew_o) {
+          store(js, (double)alg.unew()[0], (double)alg.unew()[1]);
+        } else {
+          T v[2];
+          alg.interp((ts - t) * rcp64(h), h, v);
+          store(js, (double)v[0], (double)v[1]);
+        }
+        ++js;
+      }
+      alg.accept();
+      t = tnew;
+      if (nacc == 0) dt1 = h;
+      ++nacc;
+      if (__any_sync(tm.mask, !val_finite(alg.u()[0]) || !val_finite(alg.u()[1])))
+        ret = GBDE_RET_UNSTABLE;
+      else if (last) ret = GBDE_RET_SUCCESS;
+      dt = a.dtmax > 0.0 && ord_bits(dtnew) > ord_bits(a.dtmax) ? a.dtmax : dtnew;
+    } else {
+      ++nrej;
+      dt = h * f2d_bits(ctl_reject(a.ctl, ms));
+    }
+    if (ret == GBDE_RET_DEFAULT) {
+      if (iters >= a.maxiters) ret = GBDE_RET_MAXITERS;
+      else if (a.adaptive && dt_too_small(dt, a.dtmin, t))
+        ret = GBDE_RET_DTLESSTHANMIN;
+      else if (a.timeout_ns && (iters & 31) == 0) {
+        // lane 0's clock decides for the team
+        const int late = tm.bcast((int)(global_ns() - t_start > a.timeout_ns), 0);
+        if (late) {
+          ret = GBDE_RET_TIMEOUT;
+          if (tm.lane == 0) atomicOr(a.flag, 1);
         }
       }
-    }
-    const double nanv = __longlong_as_double(0x7ff8000000000000ll);
-    for (; js < a.n_save; ++js) store(js, nanv, nanv);
-    if (tm.lane == 0) {
-      a.retcode[i] = ret;
-      if (a.naccept) a.naccept[i] = nacc;
-      if (a.nreject) a.nreject[i] = nrej;
-      if (a.nf) a.nf[i] = nfev;
-      if (a.t_end) a.t_end[i] = t;
-      if (a.method_out) a.method_out[i] = Alg::ALG_ID;
-      if (a.dt_first) a.dt_first[i] = dt1;
     }
   }
 }
