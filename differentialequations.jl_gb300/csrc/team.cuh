@@ -709,10 +709,13 @@ constexpr int kTeam8Threads = 96;
 // Row i sits in slot (i + s) mod 16, s = 1 for the third and fourth team of a
 // warp: the warp's 32 lanes then read their rows 2l + h at one column through
 // 32 distinct banks (team t: word 16 t + 17 ((2l + h + s) mod 16) + k, mod 32).
-GBDE_D float* team8_row(int i) {
+GBDE_D float* team8_rows() {
   __shared__ float rows[kTeam8Threads / TEAM8 * TEAM * kTeamLuStride];
-  const int t = threadIdx.x / TEAM8;
-  return rows + (t * TEAM + ((i + ((t >> 1) & 1)) & (TEAM - 1))) * kTeamLuStride;
+  return rows + (threadIdx.x / TEAM8) * TEAM * kTeamLuStride;
+}
+GBDE_D int team8_shift() { return (threadIdx.x / (2 * TEAM8)) & 1; }
+GBDE_D float* team8_row(int i) {
+  return team8_rows() + ((i + team8_shift()) & (TEAM - 1)) * kTeamLuStride;
 }
 
 struct TeamLU8 {
@@ -726,8 +729,11 @@ struct TeamLU8 {
   // refine their FP32 result once against W in pairs (TeamRodasFF8).
   GBDE_D void factor(const Team8& tm) {
     const int r0 = 2 * tm.lane, r1 = r0 + 1;
-    float* a0 = team8_row(r0);
-    float* a1 = team8_row(r1);
+    float* const base = team8_rows();
+    const int shift = team8_shift();
+    auto row = [&](int r) { return base + ((r + shift) & (TEAM - 1)) * kTeamLuStride; };
+    float* a0 = row(r0);
+    float* a1 = row(r1);
     bool open0 = true, open1 = true;  // not yet a pivot row
     piv = 0;
     unsigned pos0 = (unsigned)r0, pos1 = (unsigned)r1;
@@ -757,7 +763,7 @@ struct TeamLU8 {
       if (open0 && pos0 == (unsigned)k && r0 != p) pos0 = ppos;  // swapped out
       if (open1 && pos1 == (unsigned)k && r1 != p) pos1 = ppos;
       piv |= (uint64_t)p << (4 * k);
-      float* prow = team8_row(p);
+      float* prow = row(p);
       const float inv = __frcp_rn(prow[k]);
       if (tm.lane == (p >> 1)) prow[TEAM] = inv;  // the pivot's reciprocal, in the row's spare slot
       // multipliers of the open rows; l != 0 tested on the integer pipe
@@ -776,22 +782,31 @@ struct TeamLU8 {
         a1[k] = l;
         u1 = (__float_as_uint(l) << 1) != 0u;
       }
+      // the rows with a nonzero multiplier, bit r for row r: lane j's two
+      // ballot bits spread to bits 2j, 2j + 1
       const unsigned b0 = (__ballot_sync(tm.mask, u0) >> sh) & 0xFFu;  // rows 2j
       const unsigned b1 = (__ballot_sync(tm.mask, u1) >> sh) & 0xFFu;  // rows 2j + 1
+      unsigned e0 = b0, e1 = b1;
+      e0 = (e0 | (e0 << 4)) & 0x0F0Fu;
+      e0 = (e0 | (e0 << 2)) & 0x3333u;
+      e0 = (e0 | (e0 << 1)) & 0x5555u;
+      e1 = (e1 | (e1 << 4)) & 0x0F0Fu;
+      e1 = (e1 | (e1 << 2)) & 0x3333u;
+      e1 = (e1 | (e1 << 1)) & 0x5555u;
       __syncwarp(tm.mask);  // the multipliers are in shared memory
       const int ca = tm.lane, cb = tm.lane + TEAM8;
       const float pa = prow[ca], pb = prow[cb];
       const bool wa = ca > k, wb = cb > k;
       // two rows per pass, their loads ahead of the updates (distinct rows)
 #pragma unroll 1
-      for (unsigned rows = b0 | (b1 << 8); rows != 0u;) {
+      for (unsigned rows = e0 | (e1 << 1); rows != 0u;) {
         const int j1 = __ffs(rows) - 1;
         rows &= rows - 1u;
         const bool two = rows != 0u;
         const int j2 = two ? __ffs(rows) - 1 : j1;
         rows &= rows - 1u;
-        float* ar1 = team8_row(j1 < 8 ? 2 * j1 : 2 * (j1 - 8) + 1);
-        float* ar2 = team8_row(j2 < 8 ? 2 * j2 : 2 * (j2 - 8) + 1);
+        float* ar1 = row(j1);
+        float* ar2 = row(j2);
         const float l1 = ar1[k], x1a = ar1[ca], x1b = ar1[cb];
         const float l2 = ar2[k], x2a = ar2[ca], x2b = ar2[cb];
         if (wa) ar1[ca] = xfma(-l1, pa, x1a);
