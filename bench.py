@@ -66,12 +66,18 @@ TRAFFIC_PER_TRAJ = {"fp64": (4.586752e6 + 8192.0) / 20000.0,
                     "f32x2": (31.265536e6 + 9.635328e6) / 100000.0,
                     "f32x2-learned": (30.901504e6 + 8.447488e6) / 100000.0}
 
-# DRAM bytes (read + write) per stiff trajectory of the ring's Rodas5 kernel in
-# FP32 pairs (k_team8<TeamRodasFF8>), from one ncu capture at 400,000
-# trajectories of the ring workload (100,078 stiff; 1,263 bytes each against
-# ~1,536 bytes of inputs and outputs: the last saves are still in L2 when the
-# kernel ends), scaled by the launch's stiff trajectories.
-RING_STIFF_TRAFFIC_PER_TRAJ = (37.643264e6 + 88.761088e6) / 100078.0
+# The ring's stiff kernel in FP32 pairs (k_team8<TeamRodasFF8>), from one ncu
+# capture at 400,000 trajectories of the ring workload (100,078 stiff, 223.3
+# attempted steps each by the oracle's count; `python bench.py --trajectories
+# 400000 --steps 1 --warmup 1 --no-cpu-baseline` under ncu --metrics
+# dram__bytes_read.sum,dram__bytes_write.sum,smsp__inst_executed.sum):
+#   DRAM bytes (read + write) per stiff trajectory: 1,360 against ~1,536 bytes
+#   of inputs and outputs (the last saves are still in L2 when the kernel
+#   ends);
+#   warp instructions per trajectory and attempted step: 57.70e9 / (100,078 x
+#   223.3) = 2,582 (a warp carries 4 trajectories).
+RING_STIFF_TRAFFIC_PER_TRAJ = (36.905984e6 + 99.164672e6) / 100078.0
+RING_STIFF_INST_PER_ATTEMPT = 57.701854e9 / (100078.0 * 223.323)
 
 WORKLOADS = ["vdp_auto", "robertson", "lorenz", "lv_em", "lv_sosri", "summary",
              "learned_lorenz", "learned_lv", "learned_vdp"]
@@ -478,6 +484,13 @@ def run_vdp(args, de):
     orc_steps = acc["oracle_stiff_attempts_mean"]
     flops = TEAM_RODAS_FP64_PER_ATTEMPT * orc_steps * len(st_idx)
     achieved = flops / (stiff_ms * 1e-3) / 1e12
+    # the kernel's binding resource: instruction issue (one warp instruction per
+    # cycle per SM sub-partition, 4 per SM) at the SM clock sampled in the run
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    clocks = clk.summary()
+    sm_hz = (clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0) * 1e6
+    issue_peak = 4.0 * n_sm * sm_hz / 1e12  # warp instructions per second, x 1e12
+    issue_achieved = RING_STIFF_INST_PER_ATTEMPT * orc_steps * len(st_idx) / (stiff_ms * 1e-3) / 1e12
     cpu = None
     if not args.no_cpu_baseline:
         nc = args.cpu_sample or 50000
@@ -496,8 +509,8 @@ def run_vdp(args, de):
         "value": total / (chosen_ms * 1e-3), "unit": "trajectories/s", "n_gpus": world,
         "steps": K, "warmup": W, "ms_per_step": chosen_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": {"persistent-f32x2": "f32x2-state/f64-lu", "persistent-mixed": "f32-state/f64-lu"}
-        .get(chosen, "f64"),
+        "dtype": {"persistent-f32x2": "f32x2-state/f32-lu-refined",
+                  "persistent-mixed": "f32-state/f32-lu-refined"}.get(chosen, "f64"),
         "data": "synthetic (seeded, the configuration's distributions)",
         "config": {"workload": "vdp_ring8_auto_N%d" % N, "model": "ring of 8 Van der Pol "
                    "oscillators (16 states), kappa 0.05, mu = 10^U(-1,3), u0 ~ U[-2,2]^16",
@@ -509,10 +522,11 @@ def run_vdp(args, de):
                    "parallelism": "trajectory shards, no collective" if world > 1
                    else "single GPU"},
         "chosen_form": {"persistent-f32x2": "persistent queue; Tsit5 and Rodas5 on 8-lane teams "
-                        "in FP32 pairs (paired FP32 instructions) with an FP64 Jacobian, LU, "
-                        "error-norm accumulation and time; FP32 output",
+                        "in FP32 pairs (paired FP32 instructions); Rodas5's W in pairs, its LU "
+                        "and W^-1 in FP32, each stage solve refined once against W in pairs; "
+                        "FP64 time; FP32 output",
                         "persistent-mixed": "persistent queue; Tsit5 FP32 compensated state, "
-                        "Rodas5 FP32 pairs on an FP64 LU; FP32 output",
+                        "Rodas5 as in persistent-f32x2; FP32 output",
                         "persistent": "persistent queue, FP64", "plain": "one launch, FP64"}[chosen],
         "plain": {"value": total / (plain_ms * 1e-3), "ms_per_step": plain_ms,
                   "error_vs_oracle": acc["plain"]},
@@ -526,19 +540,26 @@ def run_vdp(args, de):
                 "path": "gbde_ensemble_solve with GBDE_MEM_HOST: pinned inputs copied to the "
                         "device; the saves stored by the kernels straight into the pinned host "
                         "output over the host link while they run (no staging copy)"},
-        "roofline": {"bound": "fp64", "kernel": "k_team8<TeamRodasFF8<VdpRing8,Rodas5>> (stiff "
+        "roofline": {"bound": "issue", "kernel": "k_team8<TeamRodasFF8<VdpRing8,Rodas5>> (stiff "
                      "trajectories)" if st_prec == capi.PREC_F32X2 else
                      "k_team<TeamRodas<VdpRing8,double,Rodas5>> (stiff trajectories)",
-                     "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
-                     "frac": achieved / peak64,
-                     "basis": "FP64 work that stays FP64 in every precision (sparse LU of W, "
-                              "W's diagonal, Jacobian rows, error-norm squares: %d flops per "
-                              "attempted step) x the oracle's attempted steps, over the kernel's "
-                              "time on the stiff trajectories alone (CUDA events, median)"
-                              % TEAM_RODAS_FP64_PER_ATTEMPT,
+                     "achieved": issue_achieved, "peak": issue_peak,
+                     "unit": "warp instructions/s x 1e12", "frac": issue_achieved / issue_peak,
+                     "basis": "the kernel's warp instructions per trajectory and attempted step "
+                              "(%d, ncu smsp__inst_executed.sum at 400,000 trajectories) x the "
+                              "oracle's attempted steps x this launch's stiff trajectories, over "
+                              "the kernel's time on them alone (CUDA events, median); peak: one "
+                              "warp instruction per cycle per SM sub-partition, 4 x %d SMs at "
+                              "the sampled SM clock" % (RING_STIFF_INST_PER_ATTEMPT, n_sm),
+                     "fp64_equivalent": {"achieved_tflops": achieved, "peak_tflops": peak64,
+                                         "frac": achieved / peak64,
+                                         "basis": "the %d FP64 flops per attempted step the "
+                                                  "FP64 form executes (sparse LU of W, W's "
+                                                  "diagonal, Jacobian rows, norm squares), now "
+                                                  "done in FP32 / FP32 pairs"
+                                                  % TEAM_RODAS_FP64_PER_ATTEMPT},
                      "kernel_ms": stiff_ms, "stiff_trajectories": int(len(st_idx)),
                      "share_of_step": stiff_ms / chosen_ms,
-                     "peak_source": "in-run FP64 FMA microbenchmark (gbde_measure_fma_peak)",
                      "fp32_peak_tflops": peak32,
                      "traffic": RING_STIFF_TRAFFIC_PER_TRAJ * len(st_idx)
                      if st_prec == capi.PREC_F32X2 else None,
@@ -546,7 +567,7 @@ def run_vdp(args, de):
                                        "k_team8<TeamRodasFF8> at 400,000 trajectories (100,078 "
                                        "stiff), per stiff trajectory x this launch's"},
         "gpu_launches": K * 3,
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "step_ms_spread": {"chosen": spread(chosen_ts), "plain": spread(plain_ts),
                            "e2e": spread(e2e_ts), "stiff_kernel": spread(stiff_ts)},
         "cpu_baseline": cpu,
@@ -609,7 +630,7 @@ def other_workload(de, name, N, seed):
             plain = opts(capi.ALG_SOSRI, **base)
             chosen = opts(capi.ALG_SOSRI, precision=capi.PREC_MIXED,
                           batching=capi.BATCH_PERSISTENT, **base)
-            cfg = {"workload": "lotka_volterra_sosri_N%d" % N, "alg": "sosri (SRIW1 + RSwM)",
+            cfg = {"workload": "lotka_volterra_sosri_N%d" % N, "alg": "sosri (RSwM rejection)",
                    "reltol": 1e-3, "abstol": 1e-3,
                    "chosen_form": "persistent, FP32 state, FP64 time"}
         cfg.update({"model": "lotka_volterra", "noise": "diagonal 0.1 u",
@@ -628,8 +649,8 @@ def other_workload(de, name, N, seed):
         cfg = {"workload": "vdp_ring8_auto_N%d" % N, "model": "vdp_ring8 (16 states)",
                "alg": "auto: tsit5 if mu <= 100 else rodas5", "reltol": 1e-5,
                "saveat": "0:1:20 (21 points)",
-               "chosen_form": "persistent; Tsit5 and Rodas5 on 8-lane teams in FP32 pairs on an "
-                              "FP64 Jacobian, LU and norm accumulation"}
+               "chosen_form": "persistent; Tsit5 and Rodas5 on 8-lane teams in FP32 pairs; "
+                              "Rodas5's LU and W^-1 in FP32 with pair-refined solves"}
         return (de.models.vdp_ring8, p, u0, t0, tf, saveat, capi.SAVE_GRID, plain, chosen,
                 ("f64", "f32"), cfg, "vdp")
     raise ValueError(name)
