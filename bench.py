@@ -71,13 +71,13 @@ TRAFFIC_PER_TRAJ = {"fp64": (4.586752e6 + 8192.0) / 20000.0,
 # attempted steps each by the oracle's count; `python bench.py --trajectories
 # 400000 --steps 1 --warmup 1 --no-cpu-baseline` under ncu --metrics
 # dram__bytes_read.sum,dram__bytes_write.sum,smsp__inst_executed.sum):
-#   DRAM bytes (read + write) per stiff trajectory: 1,360 against ~1,536 bytes
+#   DRAM bytes (read + write) per stiff trajectory: 1,212 against ~1,536 bytes
 #   of inputs and outputs (the last saves are still in L2 when the kernel
 #   ends);
-#   warp instructions per trajectory and attempted step: 57.70e9 / (100,078 x
-#   223.3) = 2,582 (a warp carries 4 trajectories).
-RING_STIFF_TRAFFIC_PER_TRAJ = (36.905984e6 + 99.164672e6) / 100078.0
-RING_STIFF_INST_PER_ATTEMPT = 57.701854e9 / (100078.0 * 223.323)
+#   warp instructions per trajectory and attempted step: 34.30e9 / (100,078 x
+#   223.3) = 1,535 (a warp carries 4 trajectories).
+RING_STIFF_TRAFFIC_PER_TRAJ = (33.384960e6 + 87.890176e6) / 100078.0
+RING_STIFF_INST_PER_ATTEMPT = 34.297503e9 / (100078.0 * 223.323)
 
 WORKLOADS = ["vdp_auto", "robertson", "lorenz", "lv_em", "lv_sosri", "summary",
              "learned_lorenz", "learned_lv", "learned_vdp"]

@@ -145,22 +145,6 @@ struct VdpRing8 {
     w10 = T(2) * mu * x * v + T(1) + T(2) * ka;
     w11 = dg - mu * (T(1) - x * x);
   }
-  // those rows written out in full to w0[0..16), w1[0..16)
-  template <class T>
-  GBDE_D static void w_osc_rows(int l, T dg, T w10, T w11, T ka, T* w0, T* w1) {
-    const int e = 2 * l;
-#pragma unroll
-    for (int c = 0; c < 16; ++c) {
-      w0[c] = T(0);
-      w1[c] = T(0);
-    }
-    w0[e] = dg;
-    w0[e + 1] = T(-1);
-    w1[e] = w10;
-    w1[e + 1] = w11;
-    w1[(e + 14) & 15] = -ka;
-    w1[(e + 2) & 15] = -ka;
-  }
   // r = b - W x on rows 2l, 2l + 1 with W's nonzeros (w_osc_nz) as pairs P
   // and x FP32 values (the lane's components; its neighbours' first
   // components fetched), accumulated in Acc (a pair accumulator with set /

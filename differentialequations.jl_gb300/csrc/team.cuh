@@ -694,213 +694,102 @@ struct TeamTsit5FF {
   }
 };
 
-// ---------------------------------------- 8-lane Rodas (two rows per lane)
-// The 16-state ring's stiff trajectories on teams of 8 lanes: lane l owns rows
-// 2l and 2l + 1 of W (its oscillator's x and v rows) and components 2l, 2l + 1
-// of every stage, so a warp carries 4 trajectories and the pair arithmetic of
-// a lane's two components runs on paired FP32 instructions (FfAcc2, FfVec<2>).
-// Same method and pivot rule as TeamLU / TeamRodas.
-// CTA size of the 8-lane pair Rodas kernel, which its shared arrays are sized
-// for: 12 teams, 36.1 KB (FP32 W rows 13.1 KB, W^-1 rows 12.3 KB, stages
-// 10.8 KB), 6 CTAs per SM
+// ----------------------------------- 8-lane Rodas (one oscillator per lane)
+// The 16-state ring's stiff trajectories on teams of 8 lanes: lane l owns
+// oscillator l (components 2l, 2l + 1 of the state and of every stage, rows
+// 2l and 2l + 1 of W), so a warp carries 4 trajectories and the pair
+// arithmetic of a lane's two components runs on paired FP32 instructions
+// (FfAcc2, FfVec<2>).
+// CTA size of the 8-lane pair Rodas kernel, which its shared stage buffer is
+// sized for: 12 teams, 10.8 KB, 6 CTAs per SM (96 registers)
 constexpr int kTeam8Threads = 96;
 
-// W of this team as FP32 rows: 16 rows of 17 floats, 1,088 bytes per team.
-// Row i sits in slot (i + s) mod 16, s = 1 for the third and fourth team of a
-// warp: the warp's 32 lanes then read their rows 2l + h at one column through
-// 32 distinct banks (team t: word 16 t + 17 ((2l + h + s) mod 16) + k, mod 32).
-GBDE_D float* team8_rows() {
-  __shared__ float rows[kTeam8Threads / TEAM8 * TEAM * kTeamLuStride];
-  return rows + (threadIdx.x / TEAM8) * TEAM * kTeamLuStride;
-}
-GBDE_D int team8_shift() { return (threadIdx.x / (2 * TEAM8)) & 1; }
-GBDE_D float* team8_row(int i) {
-  return team8_rows() + ((i + team8_shift()) & (TEAM - 1)) * kTeamLuStride;
-}
+// Solves with the ring's W = dg I - J on an 8-lane team (lane l: oscillator
+// l, unknowns x_l = 2l and v_l = 2l + 1).  W's nonzeros (VdpRing8::w_osc_nz):
+//   row 2l:      dg x_l - v_l                                   = b_2l
+//   row 2l + 1:  w10_l x_l + w11_l v_l - ka (x_{l-1} + x_{l+1}) = b_2l+1
+// v_l enters no other row, so row 2l gives it exactly, v_l = dg x_l - b_2l
+// (its pivot is -1: no choice to make), and substituting it leaves the Schur
+// complement on the positions, an 8 x 8 cyclic tridiagonal system
+//   A x = c,  A_ll = w10_l + w11_l dg,  A_l,l+-1 = -ka,  c_l = b_2l+1 + w11_l b_2l.
+// A^-1 is formed once per attempt by Gauss-Jordan elimination with partial
+// pivoting in FP32, lane l holding row l of [A | I] in registers (the pivot
+// of column k: the open row with the largest |a_k|, ties to the lowest lane);
+// a solve is then the product of A^-1 with c (every c_m broadcast), and v
+// from its formula.  A's diagonal, c and v are formed in pairs (each may
+// cancel) and rounded once.  The callers refine every solve once against W
+// in pairs.
+struct RingSchur8 {
+  float e[TEAM8];  // the row of A^-1 of the column this lane's row was the pivot of
+  int src;         // the lane holding row l of A^-1, whose product is x_l
+  ff w11, dg;
 
-struct TeamLU8 {
-  uint64_t piv;  // pivot row of step k in bits [4k, 4k+4)
-
-  // LU with partial pivoting, in FP32, of the W written into team8_row(): the
-  // pivot of step k is the unpivoted row with the largest |a_k|, ties to the
-  // lowest row position of the row-swapping LU (LAPACK getrf's order, as
-  // TeamLU); the rank-1 update runs column-parallel over the rows with a
-  // nonzero multiplier (lane l updates columns l and l + 8).  The solves
-  // refine their FP32 result once against W in pairs (TeamRodasFF8).
-  GBDE_D void factor(const Team8& tm) {
-    const int r0 = 2 * tm.lane, r1 = r0 + 1;
-    float* const base = team8_rows();
-    const int shift = team8_shift();
-    auto row = [&](int r) { return base + ((r + shift) & (TEAM - 1)) * kTeamLuStride; };
-    float* a0 = row(r0);
-    float* a1 = row(r1);
-    bool open0 = true, open1 = true;  // not yet a pivot row
-    piv = 0;
-    unsigned pos0 = (unsigned)r0, pos1 = (unsigned)r1;
-    const unsigned sh = (threadIdx.x & 31) & 24;  // the team's first lane in the warp
-    __syncwarp(tm.mask);  // every lane's rows are written
-#pragma unroll 1
-    for (int k = 0; k < TEAM; ++k) {
-      const float ak0 = a0[k], ak1 = a1[k];
-      // one maximum over (|a_k| + 1, then the lowest (position, row), packed
-      // and inverted) on the integer pipe: the largest magnitude, ties to the
-      // lowest position (NaN ranks above every number; closed rows are 0)
-      const uint64_t key0 = open0 ? ((uint64_t)((__float_as_uint(ak0) & 0x7fffffffu) + 1u) << 32) |
-                                        (uint64_t)(~((pos0 << 4) | (unsigned)r0))
-                                  : 0ull;
-      const uint64_t key1 = open1 ? ((uint64_t)((__float_as_uint(ak1) & 0x7fffffffu) + 1u) << 32) |
-                                        (uint64_t)(~((pos1 << 4) | (unsigned)r1))
-                                  : 0ull;
-      uint64_t m = key0 > key1 ? key0 : key1;
+  GBDE_D void build(ff dg_, ff w10, ff w11_, ff ka, const Team8& tm) {
+    dg = dg_;
+    w11 = w11_;
+    const int l = tm.lane;
+    const float ad = (float)(w10 + w11 * dg), nk = -(float)ka;
+    float a[TEAM8];
+#pragma unroll
+    for (int m = 0; m < TEAM8; ++m) {
+      a[m] = m == l ? ad : (m == ((l + 1) & (TEAM8 - 1)) || m == ((l + TEAM8 - 1) & (TEAM8 - 1)))
+                               ? nk
+                               : 0.0f;
+      e[m] = m == l ? 1.0f : 0.0f;
+    }
+    bool open = true;
+    unsigned piv = 0;  // pivot lane of column k in bits [3k, 3k+3)
+#pragma unroll
+    for (int k = 0; k < TEAM8; ++k) {
+      uint64_t m = open ? ((uint64_t)((__float_as_uint(a[k]) & 0x7fffffffu) + 1u) << 32) |
+                              (uint64_t)(~(unsigned)l)
+                        : 0ull;
 #pragma unroll
       for (int o = TEAM8 / 2; o > 0; o >>= 1) {
         const uint64_t x = __shfl_xor_sync(tm.mask, m, o, TEAM8);
         m = x > m ? x : m;
       }
-      const unsigned pk = ~(unsigned)m;  // (position, row) of the pivot
-      const unsigned ppos = pk >> 4;
-      const int p = (int)(pk & 15u);
-      if (open0 && pos0 == (unsigned)k && r0 != p) pos0 = ppos;  // swapped out
-      if (open1 && pos1 == (unsigned)k && r1 != p) pos1 = ppos;
-      piv |= (uint64_t)p << (4 * k);
-      float* prow = row(p);
-      const float inv = __frcp_rn(prow[k]);
-      if (tm.lane == (p >> 1)) prow[TEAM] = inv;  // the pivot's reciprocal, in the row's spare slot
-      // multipliers of the open rows; l != 0 tested on the integer pipe
-      bool u0 = false, u1 = false;
-      if (r0 == p) {
-        open0 = false;
-      } else if (open0) {
-        const float l = xmul(ak0, inv);
-        a0[k] = l;
-        u0 = (__float_as_uint(l) << 1) != 0u;
+      const int p = (int)(~(unsigned)m & (TEAM8 - 1));
+      piv |= (unsigned)p << (3 * k);
+      const bool me = l == p;
+      const float inv = __frcp_rn(tm.bcast(a[k], p));
+      const float f = me ? 0.0f : xmul(a[k], inv);  // this row's multiplier
+#pragma unroll
+      for (int c = k + 1; c < TEAM8; ++c) {
+        const float v = tm.bcast(a[c], p);
+        a[c] = me ? xmul(v, inv) : xfma(-f, v, a[c]);
       }
-      if (r1 == p) {
-        open1 = false;
-      } else if (open1) {
-        const float l = xmul(ak1, inv);
-        a1[k] = l;
-        u1 = (__float_as_uint(l) << 1) != 0u;
+#pragma unroll
+      for (int c = 0; c < TEAM8; ++c) {
+        const float v = tm.bcast(e[c], p);
+        e[c] = me ? xmul(v, inv) : xfma(-f, v, e[c]);
       }
-      // the rows with a nonzero multiplier, bit r for row r: lane j's two
-      // ballot bits spread to bits 2j, 2j + 1
-      const unsigned b0 = (__ballot_sync(tm.mask, u0) >> sh) & 0xFFu;  // rows 2j
-      const unsigned b1 = (__ballot_sync(tm.mask, u1) >> sh) & 0xFFu;  // rows 2j + 1
-      unsigned e0 = b0, e1 = b1;
-      e0 = (e0 | (e0 << 4)) & 0x0F0Fu;
-      e0 = (e0 | (e0 << 2)) & 0x3333u;
-      e0 = (e0 | (e0 << 1)) & 0x5555u;
-      e1 = (e1 | (e1 << 4)) & 0x0F0Fu;
-      e1 = (e1 | (e1 << 2)) & 0x3333u;
-      e1 = (e1 | (e1 << 1)) & 0x5555u;
-      __syncwarp(tm.mask);  // the multipliers are in shared memory
-      const int ca = tm.lane, cb = tm.lane + TEAM8;
-      const float pa = prow[ca], pb = prow[cb];
-      const bool wa = ca > k, wb = cb > k;
-      // two rows per pass, their loads ahead of the updates (distinct rows)
-#pragma unroll 1
-      for (unsigned rows = e0 | (e1 << 1); rows != 0u;) {
-        const int j1 = __ffs(rows) - 1;
-        rows &= rows - 1u;
-        const bool two = rows != 0u;
-        const int j2 = two ? __ffs(rows) - 1 : j1;
-        rows &= rows - 1u;
-        float* ar1 = row(j1);
-        float* ar2 = row(j2);
-        const float l1 = ar1[k], x1a = ar1[ca], x1b = ar1[cb];
-        const float l2 = ar2[k], x2a = ar2[ca], x2b = ar2[cb];
-        if (wa) ar1[ca] = xfma(-l1, pa, x1a);
-        if (wb) ar1[cb] = xfma(-l1, pb, x1b);
-        if (two && wa) ar2[ca] = xfma(-l2, pa, x2a);
-        if (two && wb) ar2[cb] = xfma(-l2, pb, x2b);
-      }
-      __syncwarp(tm.mask);  // step k's updates land before step k+1 reads them
+      if (me) open = false;
     }
-  }
-};
-
-// Rows 2l, 2l + 1 of W^-1 = U^-1 L^-1 P for lane l, in FP32, from a
-// TeamLU8's factors: a solve W x = b is then the product of those rows with b
-// (every b_j broadcast), with no chain of dependent steps.
-//   row i of U^-1:  U^T a = e_i, right-looking over the slots k (U's row k is
-//                   the pivot row of step k, q_k: columns > k; the pivot's
-//                   reciprocal in its spare column 16);
-//   times L^-1:     L^T b = a, right-looking down from k = 15 (L's row k: q_k's
-//                   multipliers in columns < k);
-//   times P:        W^-1[i][q_k] = b_k.
-// The two rows share every coefficient and run as one paired FP32 register
-// per slot.  Storage: per thread 8 chunks of 16 bytes, chunk u holding
-// columns 2u, 2u + 1 of both rows, at position u ^ (lane & 7): the 8 threads
-// of a 128-byte load phase read distinct bank groups.
-struct TeamInvF8 {
-  GBDE_D static float4* rows() {
-    __shared__ float4 buf[kTeam8Threads * 8];
-    return buf + threadIdx.x * 8;
-  }
-  GBDE_D static int sw(int u) { return u ^ (int)(threadIdx.x & 7); }
-
-  GBDE_D void build(const TeamLU8& W, const Team8& tm) const {
-    const int l = tm.lane;
-    const F2 zero = f2_pack(0.0f, 0.0f);
-    F2 a[TEAM];
-#pragma unroll
-    for (int k = 0; k < TEAM; ++k)
-      a[k] = f2_pack(k == 2 * l ? 1.0f : 0.0f, k == 2 * l + 1 ? 1.0f : 0.0f);
-#pragma unroll
-    for (int k = 0; k < TEAM; ++k) {  // U^T a = e_i
-      const float* r = team8_row((int)((W.piv >> (4 * k)) & 15u));
-      const float ip = r[TEAM];
-      a[k] = f2_prod(a[k], f2_pack(ip, ip));
-      const F2 na = f2_sub(zero, a[k]);
-#pragma unroll
-      for (int m = k + 1; m < TEAM; ++m) {
-        const float u = r[m];
-        a[m] = f2_fma(na, f2_pack(u, u), a[m]);
-      }
-    }
-#pragma unroll
-    for (int k = TEAM - 1; k > 0; --k) {  // L^T b = a
-      const float* r = team8_row((int)((W.piv >> (4 * k)) & 15u));
-      const F2 nb = f2_sub(zero, a[k]);
-#pragma unroll
-      for (int m = 0; m < k; ++m) {
-        const float v = r[m];
-        a[m] = f2_fma(nb, f2_pack(v, v), a[m]);
-      }
-    }
-    unsigned long long* out = reinterpret_cast<unsigned long long*>(rows());
-#pragma unroll
-    for (int k = 0; k < TEAM; ++k) {  // column q_k
-      const int c = (int)((W.piv >> (4 * k)) & 15u);
-      out[2 * sw(c >> 1) + (c & 1)] = a[k].v;
-    }
+    src = (int)((piv >> (3 * l)) & (TEAM8 - 1));
   }
 
-  // x = W^-1 b for this lane's unknowns 2l, 2l + 1 (b[0], b[1] likewise)
-  GBDE_D void apply(const float* b, float* x, const Team8& tm) const {
-    const float4* w = rows();
-    const F2 bb = f2_pack(b[0], b[1]);
-    F2 acc0 = f2_pack(0.0f, 0.0f), acc1 = acc0;
+  // (x_l, v_l) in FP32 from this lane's b_2l, b_2l+1 (b[0], b[1], pairs)
+  GBDE_D void solve(const ff* b, float* xv, const Team8& tm) const {
+    const float c = (float)(b[1] + w11 * b[0]);
+    float s0 = 0.0f, s1 = 0.0f;
 #pragma unroll
-    for (int u = 0; u < TEAM8; ++u) {
-      const float4 c = w[sw(u)];
-      F2 bu;
-      bu.v = __shfl_sync(tm.mask, bb.v, u, TEAM8);  // b_2u, b_2u+1
-      float b0, b1;
-      f2_unpack(bu, b0, b1);
-      acc0 = f2_fma(f2_pack(c.x, c.y), f2_pack(b0, b0), acc0);
-      acc1 = f2_fma(f2_pack(c.z, c.w), f2_pack(b1, b1), acc1);
+    for (int m = 0; m < TEAM8; m += 2) {
+      s0 = xfma(e[m], tm.bcast(c, m), s0);
+      s1 = xfma(e[m + 1], tm.bcast(c, m + 1), s1);
     }
-    f2_unpack(f2_add(acc0, acc1), x[0], x[1]);
+    const float x = tm.bcast(xadd(s0, s1), src);
+    xv[0] = x;
+    xv[1] = (float)(dg * ff(x, 0.0f) - b[0]);
   }
 };
 
 // Rodas5 / Rodas5P in FP32 pairs on 8-lane teams (the method of RodasFF,
-// rodas_ff.cuh, for a lane's two components): Jacobian rows and W in pairs;
-// W's LU (TeamLU8) and the rows of W^-1 (TeamInvF8) in FP32, each stage's
-// solve a product with W^-1 refined once against W in pairs; stage sums and
-// dense output on paired FP32 instructions; the norm's ratios and their mean
-// square FP32 (team8_mean_sq).
+// rodas_ff.cuh, for a lane's two components): Jacobian rows and W's nonzeros
+// in pairs; each stage's solve through W's Schur complement on the positions
+// (RingSchur8, its 8 x 8 inverse in FP32) refined once against W in pairs;
+// stage sums and dense output on paired FP32 instructions; the norm's ratios
+// and their mean square FP32 (team8_mean_sq).
 template <class M, class Tag>
 struct TeamRodasFF8 {
   using K = RodasCoef<Tag>;
@@ -956,14 +845,8 @@ struct TeamRodasFF8 {
     const ff dg = ff_split(ih * (1.0 / K::g));
     ff w10, w11;
     M::w_osc_nz(uu, p, dg, w10, w11);
-    TeamInvF8 L;
-    {
-      TeamLU8 W;
-      M::w_osc_rows(tm.lane, (float)dg, (float)w10, (float)w11, (float)p[1],
-                    team8_row(2 * tm.lane), team8_row(2 * tm.lane + 1));
-      W.factor(tm);
-      L.build(W, tm);
-    }
+    RingSchur8 L;
+    L.build(dg, w10, w11, p[1], tm);
     const ff iht = ff_split(ih);
     const RodasFfTab& tb = c_rodas_ff[RodasFfIdx<Tag>::v];
     FfVec<2> uv;
@@ -1011,17 +894,15 @@ struct TeamRodasFF8 {
       }
       ff x[2];
       {
-        // W x = r: an FP32 solve (x0 = W^-1 r) and one refinement against W
-        // in pairs, x = x0 + d with d = W^-1 (r - W x0) (residual in pairs).
-        // W = I/(h gamma) - J is well conditioned here, so the refined error
-        // is about (cond(W) 2^-24)^2 of |x|, far below the tolerances.
-        float b32[2] = {(float)r[0], (float)r[1]}, x0[2], d[2];
-        L.apply(b32, x0, tm);
+        // W x = r: an FP32 solve (RingSchur8) and one refinement against W in
+        // pairs, x = x0 + d with W d ~ r - W x0 (residual in pairs).  W =
+        // I/(h gamma) - J is well conditioned here, so the refined error is
+        // about (cond 2^-24)^2 of |x|, far below the tolerances.
+        float x0[2], d[2];
+        L.solve(r, x0, tm);
         ff res[2];
         M::template w_osc_residual<FfAcc>(tm.lane, dg, w10, w11, p[1], r, x0, tm, res);
-        b32[0] = (float)res[0];
-        b32[1] = (float)res[1];
-        L.apply(b32, d, tm);
+        L.solve(res, d, tm);
         x[0] = ff(x0[0], 0.0f) + ff(d[0], 0.0f);
         x[1] = ff(x0[1], 0.0f) + ff(d[1], 0.0f);
       }
