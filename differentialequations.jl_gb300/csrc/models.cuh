@@ -134,6 +134,26 @@ struct VdpRing8 {
     dy[0] = v;
     dy[1] = p[0] * (T(1) - x * x) * v - x + p[1] * (xl - T(2) * x + xr);
   }
+  // f_osc for FP32 pairs P as one unnormalised pair accumulation (Acc: set /
+  // add / fma / get), the same value to pair precision:
+  //   v' = mu v - (mu v x) x - x - 2 ka x + ka xl + ka xr
+  // (two pair products, five accumulated terms and one renormalisation,
+  // instead of five renormalised products and five sums).  2 ka is exact.
+  template <class Acc, class P, class Sh>
+  GBDE_D static void f_osc_acc(int l, const P* y, const P* p, const Sh& sh, P* dy) {
+    const P x = y[0], v = y[1];
+    const P xl = sh.bcast(x, (l + 7) & 7), xr = sh.bcast(x, (l + 1) & 7);
+    const P mv = p[0] * v, ka = p[1], ka2n(-2.0f * ka.hi, -2.0f * ka.lo);
+    Acc a;
+    a.set(mv);
+    a.fma(-(mv * x), x);
+    a.add(-x);
+    a.fma(ka2n, x);
+    a.fma(ka, xl);
+    a.fma(ka, xr);
+    dy[0] = v;
+    dy[1] = a.get();
+  }
   // 8-lane teams: rows 2l (x_l' = v_l) and 2l + 1 (v_l') of W = dg I - J at
   // lane l's oscillator (x, v) = (y[0], y[1]) have the nonzeros
   //   W[2l][2l] = dg, W[2l][2l + 1] = -1,

@@ -565,7 +565,7 @@ struct TeamTsit5FF {
   GBDE_D const ff* unew() const { return un; }
   GBDE_D const ff* f0() const { return k1; }
   GBDE_D void rhs(const ff* y, const ff* p, const Team8& tm, ff* dy) const {
-    M::f_osc(tm.lane, y, p, tm, dy);
+    M::template f_osc_acc<FfAcc>(tm.lane, y, p, tm, dy);
   }
 
   GBDE_D void init(const ff* u0, const ff* p, const Team8& tm, int& nf) {
@@ -804,7 +804,7 @@ struct TeamRodasFF8 {
   GBDE_D const ff* unew() const { return un; }
   GBDE_D const ff* f0() const { return F0; }
   GBDE_D void rhs(const ff* y, const ff* p, const Team8& tm, ff* dy) const {
-    M::f_osc(tm.lane, y, p, tm, dy);
+    M::template f_osc_acc<FfAcc>(tm.lane, y, p, tm, dy);
   }
 
   // stages u_1..u_7 of this lane's two components: one 16-byte (hi pair, lo
