@@ -4,7 +4,7 @@ Workload (default): the mixed-precision coupled-oscillator ensemble -- a ring
 of 8 Van der Pol oscillators (16 states) with diffusive coupling kappa = 0.05,
 mu = 10^U(-1, 3) per trajectory, u0 ~ U[-2, 2]^16, tspan (0, 20), reltol =
 abstol = 1e-5, saves every 1.0 (21 points), 1,000,000 trajectories; each
-trajectory runs Tsit5 if mu <= 100 and Rodas5 otherwise (GBDE_ALG_AUTO).
+trajectory runs Tsit5 if mu <= 60 and Rodas5 otherwise (GBDE_ALG_AUTO).
 Seeded synthetic inputs with the configuration's distributions (no dataset).
 Other configurations print their own line with --workload.
 
@@ -66,18 +66,23 @@ TRAFFIC_PER_TRAJ = {"fp64": (4.586752e6 + 8192.0) / 20000.0,
                     "f32x2": (31.265536e6 + 9.635328e6) / 100000.0,
                     "f32x2-learned": (30.901504e6 + 8.447488e6) / 100000.0}
 
-# The ring's stiff kernel in FP32 pairs (k_team8<TeamRodasFF8>), from one ncu
-# capture at 400,000 trajectories of the ring workload (100,078 stiff, 223.3
-# attempted steps each by the oracle's count; `python bench.py --trajectories
-# 400000 --steps 1 --warmup 1 --no-cpu-baseline` under ncu --metrics
-# dram__bytes_read.sum,dram__bytes_write.sum,smsp__inst_executed.sum):
-#   DRAM bytes (read + write) per stiff trajectory: 1,212 against ~1,536 bytes
-#   of inputs and outputs (the last saves are still in L2 when the kernel
-#   ends);
-#   warp instructions per trajectory and attempted step: 34.30e9 / (100,078 x
-#   223.3) = 1,535 (a warp carries 4 trajectories).
-RING_STIFF_TRAFFIC_PER_TRAJ = (33.384960e6 + 87.890176e6) / 100078.0
-RING_STIFF_INST_PER_ATTEMPT = 34.297503e9 / (100078.0 * 223.323)
+# The ring's two kernels in FP32 pairs, from one ncu capture at 400,000
+# trajectories of the ring workload (`python bench.py --trajectories 400000
+# --steps 1 --warmup 1 --no-cpu-baseline` under ncu --metrics
+# dram__bytes_read.sum,dram__bytes_write.sum,smsp__inst_executed.sum; the split
+# at mu = 60: 122,217 stiff, 277,783 non-stiff):
+#   k_team8<TeamRodasFF8> (stiff): 1,297 DRAM bytes (read + write) per
+#   trajectory against ~1,536 bytes of inputs and outputs (the last saves are
+#   still in L2 when the kernel ends); 43.61e9 warp instructions, 1,497 per
+#   trajectory and attempted step (238.4 attempts each by the oracle's count
+#   on the run's 2,000-trajectory sample; a warp carries 4 trajectories);
+#   k_team8<TeamTsit5FF> (non-stiff): 1,448 DRAM bytes and 136,285 warp
+#   instructions per trajectory (its attempted steps vary with mu; the
+#   workload's mu distribution is the same at every N).
+RING_STIFF_TRAFFIC_PER_TRAJ = (39.433472e6 + 119.043840e6) / 122217.0
+RING_STIFF_INST_PER_ATTEMPT = 43.609271e9 / (122217.0 * 238.4)
+RING_NONSTIFF_TRAFFIC_PER_TRAJ = (67.150592e6 + 334.981888e6) / 277783.0
+RING_NONSTIFF_INST_PER_TRAJ = 37.857549e9 / 277783.0
 
 WORKLOADS = ["vdp_auto", "robertson", "lorenz", "lv_em", "lv_sosri", "summary",
              "learned_lorenz", "learned_lv", "learned_vdp"]
@@ -131,7 +136,11 @@ def workload(N, seed):
 
 
 VDP_RTOL = 1e-5
-VDP_STIFF_MU = 100.0
+# The AUTO split of the ring workload: Rodas5 for mu above it, Tsit5 below (the
+# same split for every form and for the CPU port).  The AUTO solve time on GB300
+# against the split (1M trajectories, FP32 pairs): 286 / 266 / 255 / 256 / 265 /
+# 290 ms at 20 / 30 / 50 / 70 / 100 / 150.
+VDP_STIFF_MU = 60.0
 
 
 def vdp_inputs(N, seed):
@@ -349,7 +358,7 @@ VDP_FORMS = {  # name: (precision, batching, output dtype)
 
 
 def run_vdp(args, de):
-    """The 16-state ring, 1M trajectories, AUTO (Tsit5 if mu <= 100, else
+    """The 16-state ring, 1M trajectories, AUTO (Tsit5 if mu <= VDP_STIFF_MU, else
     Rodas5): chosen form vs the plain FP64 launch, both gated against the
     FP64 oracle before timing."""
     import torch
@@ -407,6 +416,7 @@ def run_vdp(args, de):
             raise SystemExit("bench: accuracy gate failed")
     method = res[chosen]["method"]
     st_idx = np.nonzero(method == capi.ALG_RODAS5)[0]
+    ns_idx = np.nonzero(method == capi.ALG_TSIT5)[0]
     del res
 
     # ---- timing
@@ -429,6 +439,11 @@ def run_vdp(args, de):
     dst = [t[torch.from_numpy(st_idx).to(dev)].contiguous() for t in dptr[:4]] + [dptr[4]]
     st_out = {"u": torch.empty((len(st_idx), S, 16), device=dev, dtype=outs[chosen]["u"].dtype),
               "retcode": torch.empty(len(st_idx), dtype=torch.int32, device=dev)}
+    # and the non-stiff trajectories' Tsit5, in the chosen form's precision
+    o_ns = opts(chosen, capi.ALG_TSIT5)
+    dns = [t[torch.from_numpy(ns_idx).to(dev)].contiguous() for t in dptr[:4]] + [dptr[4]]
+    ns_out = {"u": torch.empty((len(ns_idx), S, 16), device=dev, dtype=outs[chosen]["u"].dtype),
+              "retcode": torch.empty(len(ns_idx), dtype=torch.int32, device=dev)}
     K, W = args.steps, args.warmup
     with ClockSampler(local) as clk:
         chosen_ts = event_times(lambda: de.solve_arrays(M, opts(chosen), *dptr, capi.SAVE_GRID,
@@ -442,6 +457,9 @@ def run_vdp(args, de):
         stiff_ts = event_times(lambda: de.solve_arrays(M, o_st, *dst, capi.SAVE_GRID,
                                                        u_dtype=odt(chosen), out=st_out),
                                stream, min(K, 5), 1, flush, world)
+        nonstiff_ts = event_times(lambda: de.solve_arrays(M, o_ns, *dns, capi.SAVE_GRID,
+                                                          u_dtype=odt(chosen), out=ns_out),
+                                  stream, min(K, 5), 1, flush, world)
         # end to end through the C ABI: pinned host inputs and outputs, the
         # copies inside the timed region
         for _ in range(W):
@@ -474,6 +492,7 @@ def run_vdp(args, de):
     plain_ms = max_over_ranks(float(np.median(plain_ts)))
     e2e_ms = max_over_ranks(float(np.median(e2e_ts)))
     stiff_ms = max_over_ranks(float(np.median(stiff_ts)))
+    nonstiff_ms = max_over_ranks(float(np.median(nonstiff_ts)))
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -491,6 +510,23 @@ def run_vdp(args, de):
     sm_hz = (clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0) * 1e6
     issue_peak = 4.0 * n_sm * sm_hz / 1e12  # warp instructions per second, x 1e12
     issue_achieved = RING_STIFF_INST_PER_ATTEMPT * orc_steps * len(st_idx) / (stiff_ms * 1e-3) / 1e12
+    ns_issue = RING_NONSTIFF_INST_PER_TRAJ * len(ns_idx) / (nonstiff_ms * 1e-3) / 1e12
+    pairs_form = VDP_FORMS[chosen][0] == "PREC_F32X2"
+    roof_nonstiff = {
+        "bound": "issue", "kernel": "k_team8<TeamTsit5FF<VdpRing8>> (non-stiff trajectories)"
+        if pairs_form else "the non-stiff Tsit5 team kernel (%s)" % VDP_FORMS[chosen][0],
+        "achieved": ns_issue, "peak": issue_peak, "unit": "warp instructions/s x 1e12",
+        "frac": ns_issue / issue_peak if pairs_form else None,
+        "basis": "the kernel's warp instructions per trajectory (%d, ncu smsp__inst_executed.sum "
+                 "at 400,000 trajectories) x this launch's non-stiff trajectories, over the "
+                 "kernel's time on them alone (CUDA events, median); peak as above"
+                 % RING_NONSTIFF_INST_PER_TRAJ,
+        "kernel_ms": nonstiff_ms, "nonstiff_trajectories": int(len(ns_idx)),
+        "share_of_step": nonstiff_ms / chosen_ms,
+        "traffic": RING_NONSTIFF_TRAFFIC_PER_TRAJ * len(ns_idx) if pairs_form else None,
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
+                          "k_team8<TeamTsit5FF> at 400,000 trajectories (277,783 non-stiff), per "
+                          "trajectory x this launch's"}
     cpu = None
     if not args.no_cpu_baseline:
         nc = args.cpu_sample or 50000
@@ -564,14 +600,21 @@ def run_vdp(args, de):
                      "traffic": RING_STIFF_TRAFFIC_PER_TRAJ * len(st_idx)
                      if st_prec == capi.PREC_F32X2 else None,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
-                                       "k_team8<TeamRodasFF8> at 400,000 trajectories (100,078 "
+                                       "k_team8<TeamRodasFF8> at 400,000 trajectories (122,217 "
                                        "stiff), per stiff trajectory x this launch's"},
         "gpu_launches": K * 3,
         "clocks": clocks,
         "step_ms_spread": {"chosen": spread(chosen_ts), "plain": spread(plain_ts),
-                           "e2e": spread(e2e_ts), "stiff_kernel": spread(stiff_ts)},
+                           "e2e": spread(e2e_ts), "stiff_kernel": spread(stiff_ts),
+                           "nonstiff_kernel": spread(nonstiff_ts)},
         "cpu_baseline": cpu,
     }
+    # `roofline` describes the kernel with the larger share of the step
+    roof_stiff = line["roofline"]
+    if nonstiff_ms > stiff_ms:
+        line["roofline"], line["roofline_other"] = roof_nonstiff, roof_stiff
+    else:
+        line["roofline_other"] = roof_nonstiff
     if cpu:
         line["north_star"] = {
             "plain_vs_cpu": line["plain"]["value"] / cpu["value"],
@@ -642,12 +685,12 @@ def other_workload(de, name, N, seed):
         u0 = rng.uniform(-2, 2, (N, 16))
         t0, tf = np.zeros(N), np.full(N, 20.0)
         saveat = de.save_grid(0.0, 20.0, 1.0)
-        base = dict(reltol=1e-5, abstol=1e-5, stiff_threshold=100.0, maxiters=10 ** 6)
+        base = dict(reltol=1e-5, abstol=1e-5, stiff_threshold=VDP_STIFF_MU, maxiters=10 ** 6)
         plain = opts(capi.ALG_AUTO, **base)
         chosen = opts(capi.ALG_AUTO, precision=capi.PREC_F32X2, batching=capi.BATCH_PERSISTENT,
                       **base)
         cfg = {"workload": "vdp_ring8_auto_N%d" % N, "model": "vdp_ring8 (16 states)",
-               "alg": "auto: tsit5 if mu <= 100 else rodas5", "reltol": 1e-5,
+               "alg": "auto: tsit5 if mu <= %g else rodas5" % VDP_STIFF_MU, "reltol": 1e-5,
                "saveat": "0:1:20 (21 points)",
                "chosen_form": "persistent; Tsit5 and Rodas5 on 8-lane teams in FP32 pairs; "
                               "Rodas5's LU and W^-1 in FP32 with pair-refined solves"}
