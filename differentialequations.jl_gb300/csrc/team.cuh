@@ -456,6 +456,19 @@ GBDE_D double team8_mean_sq(const Team8& tm, float e0, float e1) {
   return f2d_bits(xmul(s, 1.0f / (2 * TEAM8)));
 }
 
+// The tolerances an 8-lane stepper's attempt reads: FP64, and the FP32 values
+// the pair steppers' norm ratios use (formed once per kernel: the split to a
+// pair runs an integer-to-float conversion on the FP64 pipe).
+struct TeamTol {
+  double abstol, reltol;
+  float atf, rtf;
+  GBDE_D TeamTol(double a, double r) : abstol(a), reltol(r) {
+    const ff as = ff_split(a), rs = ff_split(r);
+    atf = xadd(as.hi, as.lo);
+    rtf = xadd(rs.hi, rs.lo);
+  }
+};
+
 template <class M, class T>
 struct TeamTsit5P {
   static constexpr int ORDER = 5, ALG_ID = GBDE_ALG_TSIT5;
@@ -485,7 +498,7 @@ struct TeamTsit5P {
     ++nf;
   }
 
-  GBDE_D double attempt(double dt, const T* p, double abstol, double reltol, const Team8& tm,
+  GBDE_D double attempt(double dt, const T* p, const TeamTol& tol, const Team8& tm,
                         int& nf) {
     using namespace tab::tsit5;
     const T h = team_scalar<T>(dt);
@@ -515,7 +528,7 @@ struct TeamTsit5P {
     for (int c = 0; c < 2; ++c) {
       const T err = h * (T(bt1) * k1[c] + T(bt2) * k2[c] + T(bt3) * k3[c] + T(bt4) * k4[c] +
                          T(bt5) * k5[c] + T(bt6) * k6[c] + T(bt7) * k7[c]);
-      e2 += lane_err2(err, uu[c], un[c], abstol, reltol);
+      e2 += lane_err2(err, uu[c], un[c], tol.abstol, tol.reltol);
     }
     return tm.sum(e2) * (1.0 / M::N);
   }
@@ -575,7 +588,7 @@ struct TeamTsit5FF {
     ++nf;
   }
 
-  GBDE_D double attempt(double dt, const ff* p, double abstol, double reltol, const Team8& tm,
+  GBDE_D double attempt(double dt, const ff* p, const TeamTol& tol, const Team8& tm,
                         int& nf) {
     using namespace tab::tsit5;
     constexpr ff A21 = ff(a21);
@@ -649,8 +662,7 @@ struct TeamTsit5FF {
     a.fma(E6, hk[5]);
     a.fma(E7, hk[6]);
     a.get(err);
-    const ff as = ff_split(abstol), rs = ff_split(reltol);
-    const float atf = xadd(as.hi, as.lo), rtf = xadd(rs.hi, rs.lo);
+    const float atf = tol.atf, rtf = tol.rtf;
     float e[2];
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
@@ -833,7 +845,7 @@ struct TeamRodasFF8 {
     fresh = true;
   }
 
-  GBDE_D double attempt(double dt, const ff* p, double abstol, double reltol, const Team8& tm,
+  GBDE_D double attempt(double dt, const ff* p, const TeamTol& tol, const Team8& tm,
                         int& nf) {
     if (!fresh) {
       ++nf;
@@ -916,8 +928,7 @@ struct TeamRodasFF8 {
     nf += 7;
     // y1 = U_7 + u_8; error estimate u_8 (ratios FP32 on the leading parts,
     // their mean square in FP32)
-    const ff as = ff_split(abstol), rs = ff_split(reltol);
-    const float atf = xadd(as.hi, as.lo), rtf = xadd(rs.hi, rs.lo);
+    const float atf = tol.atf, rtf = tol.rtf;
     float e[2];
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
@@ -976,6 +987,7 @@ __device__ void integrate_team8(const KArgs& a) {
   Team8 tm;
   tm.init();
   const int64_t team_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / TEAM8;
+  const TeamTol tol(a.abstol, a.reltol);
   const uint64_t t_start = a.timeout_ns ? global_ns() : 0;
   bool first = true;
   Alg alg;
@@ -1096,7 +1108,7 @@ __device__ void integrate_team8(const KArgs& a) {
       h = rem;
       last = true;
     }
-    const double ms = alg.attempt(h, p, a.abstol, a.reltol, tm, nfev);
+    const double ms = alg.attempt(h, p, tol, tm, nfev);
     ++iters;
     if (!a.adaptive || mag_bits(ms) <= 0x3FF0000000000000ull) {  // ms <= 1 (integer pipe)
       double dtnew = h;
