@@ -90,6 +90,32 @@ GBDE_HD double f2d_bits(float x) {
 #endif
 }
 
+// double -> float, rounded to nearest even, on the integer pipe: the value the
+// conversion instruction gives (that one runs on GB300's narrow FP64 pipe),
+// for finite x whose float is normal (2^-126 <= |x| < 2^128 after rounding).
+GBDE_HD float d2f_rn_bits(double x) {
+  uint64_t b;
+#if defined(__CUDA_ARCH__)
+  b = (uint64_t)__double_as_longlong(x);
+#else
+  memcpy(&b, &x, sizeof(b));
+#endif
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const uint32_t e = (uint32_t)((b >> 52) & 0x7ffu) - 896u;  // float's biased exponent
+  const uint32_t rest = (uint32_t)b & 0x1fffffffu;           // the 29 bits dropped
+  uint32_t f = (e << 23) | (uint32_t)((b >> 29) & 0x7fffffu);
+  // a carry out of the significand moves into the exponent, as it should
+  f += (rest > 0x10000000u || (rest == 0x10000000u && (f & 1u))) ? 1u : 0u;
+  f |= sign;
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(f);
+#else
+  float r;
+  memcpy(&r, &f, sizeof(r));
+  return r;
+#endif
+}
+
 // Finiteness of a state component: through the FP64 value for double and
 // float; the pair type (ff.cuh) overloads it with a test of its leading part.
 template <class T>

@@ -107,7 +107,7 @@ GBDE_HD float ctl_log2_ms(double ms) {
 #else
   memcpy(&c, &b, sizeof(c));
 #endif
-  return ctl_log2f((float)c);
+  return ctl_log2f(d2f_rn_bits(c));  // (float)c, off the FP64 pipe
 }
 
 // Accepted step: returns r with dt_new = dt * r; updates lqold = log2(qold).

@@ -1270,6 +1270,12 @@ int oracle_lu_solve(int n, const double* A, const double* b, double* x) {
 // (controller.h, identical steps), 1 = FP64 pow() (see g_ctl_pow64).
 void oracle_set_controller(int mode) { g_ctl_pow64 = mode == 1; }
 
+// The controller's integer-pipe double -> float rounding (d2f_rn_bits,
+// common.cuh), for its test against the hardware conversion.
+void oracle_d2f_rn(const double* x, float* out, int64_t n) {
+  for (int64_t i = 0; i < n; ++i) out[i] = gbde::d2f_rn_bits(x[i]);
+}
+
 int oracle_hardware_threads(void) {
   const unsigned h = std::thread::hardware_concurrency();
   return h ? (int)h : 1;

@@ -134,6 +134,8 @@ def lib():
         L.oracle_lu_solve.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_set_controller.restype = None
         L.oracle_set_controller.argtypes = [C.c_int]
+        L.oracle_d2f_rn.restype = None
+        L.oracle_d2f_rn.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
         _lib = L
     return _lib
 
@@ -146,6 +148,14 @@ def set_controller(mode):
     """0: the kernels' FP32-series step-size factor (identical steps; the
     default); 1: the FP64 pow() form of the same PI controller."""
     lib().oracle_set_controller(int(mode))
+
+
+def d2f_rn(x):
+    """The controller's integer-pipe double -> float rounding (d2f_rn_bits)."""
+    x = np.ascontiguousarray(x, np.float64)
+    out = np.empty(x.shape, np.float32)
+    lib().oracle_d2f_rn(x.ctypes.data, out.ctypes.data, x.size)
+    return out
 
 
 def lu_solve(A, b):

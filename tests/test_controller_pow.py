@@ -94,3 +94,22 @@ def test_weighted_error_nan_is_a_failure(oracle):
     inf = np.array([[np.inf]])
     assert oracle.weighted_error(inf, inf, 1e-6, 1e-6) == 0.0
     assert oracle.weighted_error(-inf, inf, 1e-6, 1e-6) == np.inf
+
+
+def test_d2f_rn_bits_matches_the_conversion(oracle):
+    """The controller narrows its error norm (clamped to [2^-120, 2^120]) to
+    FP32 on the integer pipe: the same float as an IEEE round-to-nearest-even
+    conversion, for random doubles, exact ties and values that round up
+    across a power of two."""
+    rng = np.random.default_rng(21)
+    x = np.ldexp(rng.uniform(0.5, 1.0, 200000), rng.integers(-119, 121, 200000))
+    x *= rng.choice([-1.0, 1.0], x.size)
+    f = x.astype(np.float32).astype(np.float64)
+    ulp = np.spacing(np.abs(x).astype(np.float32)).astype(np.float64)
+    ties = np.concatenate([f + 0.5 * ulp, f - 0.5 * np.spacing(np.abs(f).astype(np.float32) * 0.5).astype(np.float64)])
+    below_two = np.nextafter(np.ldexp(1.0, np.arange(-110, 111)), 0.0)
+    xs = np.concatenate([x, ties, below_two, -below_two])
+    xs = xs[(np.abs(xs) >= 2.0 ** -120) & (np.abs(xs) <= 2.0 ** 120)]
+    got = oracle.d2f_rn(xs)
+    want = xs.astype(np.float32)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
