@@ -40,10 +40,42 @@ struct CtlK {
   float lqoldinit;  // log2(qoldinit)
 };
 
+// Exact helpers for the series below, on the integer pipe and FP32 adds
+// (GB300 runs conversion instructions on its narrow FP64 pipe).
+GBDE_HD uint32_t ctl_fbits(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(x);
+#else
+  uint32_t b;
+  memcpy(&b, &x, sizeof(b));
+  return b;
+#endif
+}
+GBDE_HD float ctl_bitsf(uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(b);
+#else
+  float x;
+  memcpy(&x, &b, sizeof(x));
+  return x;
+#endif
+}
+// 1.5 2^23: adding it to |y| < 2^22 leaves round-to-nearest-even(y) in the
+// low bits of the sum's significand
+constexpr float kCtlRound = 12582912.0f;
+// frexpf for positive normal x: x = m 2^e, m in [0.5, 1)
+GBDE_HD float ctl_frexp(float x, int& e) {
+  const uint32_t b = ctl_fbits(x);
+  e = (int)((b >> 23) & 0xffu) - 126;
+  return ctl_bitsf((b & 0x807fffffu) | 0x3f000000u);
+}
+// (float)i for |i| < 2^22
+GBDE_HD float ctl_i2f(int i) { return xadd(ctl_bitsf(0x4b400000u + (uint32_t)i), -kCtlRound); }
+
 GBDE_HD float ctl_log2f(float x) {
   // x > 0 and normal
   int e;
-  float m = frexpf(x, &e);  // x = m 2^e, m in [0.5, 1): exact
+  float m = ctl_frexp(x, e);  // x = m 2^e, m in [0.5, 1): exact
   if (m < 0.707106781f) {
     m = m + m;  // exact
     e -= 1;
@@ -59,12 +91,14 @@ GBDE_HD float ctl_log2f(float x) {
   pacc = xfma(pacc, s2, 1.0f / 3.0f);
   pacc = xfma(pacc, s2, 1.0f);
   const float ln_m = xmul(xadd(s, s), pacc);      // 2 atanh(s) = ln m
-  return xfma(ln_m, 1.44269504f, (float)e);       // e + ln m / ln 2
+  return xfma(ln_m, 1.44269504f, ctl_i2f(e));     // e + ln m / ln 2
 }
 
 GBDE_HD float ctl_exp2f(float y) {
-  // |y| <= 60 (the callers clamp)
-  const float k = rintf(y);
+  // |y| <= 60 (the callers clamp); k = rint(y) and its integer from one sum
+  const float r = xadd(y, kCtlRound);
+  const int ki = (int)(ctl_fbits(r) - 0x4b400000u);
+  const float k = xadd(r, -kCtlRound);
   const float f = y - k;  // exact, |f| <= 1/2
   const float x = xmul(f, 0.693147182f);  // f ln 2, |x| <= 0.347
   // exp(x) by Taylor series, degree 7 (truncation < 6e-9 relative)
@@ -76,7 +110,8 @@ GBDE_HD float ctl_exp2f(float y) {
   pacc = xfma(pacc, x, 0.5f);
   pacc = xfma(pacc, x, 1.0f);
   pacc = xfma(pacc, x, 1.0f);
-  return ldexpf(pacc, (int)k);  // exact scaling
+  // exact scaling by 2^k: pacc is in [0.70, 1.42] and |k| <= 60
+  return xmul(pacc, ctl_bitsf((uint32_t)(127 + ki) << 23));
 }
 
 inline CtlK ctl_consts(double beta1, double beta2, double gamma, double qmin, double qmax,

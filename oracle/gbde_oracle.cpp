@@ -1270,6 +1270,35 @@ int oracle_lu_solve(int n, const double* A, const double* b, double* x) {
 // (controller.h, identical steps), 1 = FP64 pow() (see g_ctl_pow64).
 void oracle_set_controller(int mode) { g_ctl_pow64 = mode == 1; }
 
+// Mismatches between the controller's exact helpers (controller.h: ctl_frexp,
+// ctl_i2f, the rint and ldexp steps of ctl_exp2f) and the C library's frexpf,
+// (float), rintf and ldexpf, over the ranges the controller feeds them: every
+// 97th positive normal float, every |i| <= 200, and y in [-60, 60] by 1/64
+// (the rounding ties at k + 1/2 included).
+int64_t oracle_ctl_selfcheck() {
+  int64_t bad = 0;
+  for (uint32_t b = 0x00800000u; b < 0x7f800000u; b += 97u) {
+    float x;
+    memcpy(&x, &b, sizeof(x));
+    int e0 = 0, e1 = 0;
+    const float m0 = frexpf(x, &e0), m1 = gbde::ctl_frexp(x, e1);
+    bad += (m0 != m1 || e0 != e1);
+  }
+  for (int i = -200; i <= 200; ++i) bad += ((float)i != gbde::ctl_i2f(i));
+  for (int j = -60 * 64; j <= 60 * 64; ++j) {
+    const float y = (float)j / 64.0f;
+    const float r = y + gbde::kCtlRound;
+    uint32_t rb;
+    memcpy(&rb, &r, sizeof(rb));
+    const int ki = (int)(rb - 0x4b400000u);
+    const float k = r - gbde::kCtlRound;
+    bad += (k != rintf(y) || (float)ki != k);
+    const float scaled = 1.25f * gbde::ctl_bitsf((uint32_t)(127 + ki) << 23);
+    bad += (scaled != ldexpf(1.25f, ki));
+  }
+  return bad;
+}
+
 // The controller's integer-pipe double -> float rounding (d2f_rn_bits,
 // common.cuh), for its test against the hardware conversion.
 void oracle_d2f_rn(const double* x, float* out, int64_t n) {

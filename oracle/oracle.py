@@ -134,6 +134,8 @@ def lib():
         L.oracle_lu_solve.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_set_controller.restype = None
         L.oracle_set_controller.argtypes = [C.c_int]
+        L.oracle_ctl_selfcheck.restype = C.c_int64
+        L.oracle_ctl_selfcheck.argtypes = []
         L.oracle_d2f_rn.restype = None
         L.oracle_d2f_rn.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
         _lib = L
@@ -148,6 +150,12 @@ def set_controller(mode):
     """0: the kernels' FP32-series step-size factor (identical steps; the
     default); 1: the FP64 pow() form of the same PI controller."""
     lib().oracle_set_controller(int(mode))
+
+
+def ctl_selfcheck():
+    """Mismatches of the controller's exact helpers against frexpf, (float),
+    rintf and ldexpf (0 expected)."""
+    return int(lib().oracle_ctl_selfcheck())
 
 
 def d2f_rn(x):

@@ -113,3 +113,10 @@ def test_d2f_rn_bits_matches_the_conversion(oracle):
     got = oracle.d2f_rn(xs)
     want = xs.astype(np.float32)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_controller_helpers_exact(oracle):
+    """The controller's series use exact integer-pipe helpers instead of
+    frexpf, int -> float, rintf and ldexpf: the same values over every input
+    the controller gives them."""
+    assert oracle.ctl_selfcheck() == 0
