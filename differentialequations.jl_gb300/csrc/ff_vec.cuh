@@ -30,6 +30,14 @@ GBDE_D ff ff_split(double d) {
   return ff(hi, sign ? -lo : lo);
 }
 
+// A tolerance (finite, >= 0) in FP32 for the norm ratios: rounded to nearest on
+// the integer pipe (d2f_rn_bits), values below FP32's normal range flushed to
+// 0 as ff_split does -- without the split's int-to-float conversion, which
+// runs on GB300's narrow FP64 pipe.
+GBDE_D float tol_f32(double x) {
+  return mag_bits(x) < 0x3810000000000000ull ? 0.0f : d2f_rn_bits(x);  // 2^-126
+}
+
 // 1 / x for a pair, relative error about 2^-47: the correctly rounded FP32
 // reciprocal r of the leading part, then one Newton correction on the pair,
 // 1/x ~ r + r e with e = 1 - x r.  The leading residual 1 - hi r is exact

@@ -265,8 +265,7 @@ struct RodasFF {
     // y1 = U_7 + u_8; error estimate u_8.  The norm's ratios
     // u_8 / (abstol + reltol max(|u0|, |y1|)) are FP32 on the leading parts
     // (as Tsit5FF); their squares accumulate in FP64.
-    const ff as = ff_split(abstol), rs = ff_split(reltol);
-    const float atf = xadd(as.hi, as.lo), rtf = xadd(rs.hi, rs.lo);
+    const float atf = tol_f32(abstol), rtf = tol_f32(reltol);
     double ms = 0.0;
 #pragma unroll
     for (int c = 0; c < N; ++c) {

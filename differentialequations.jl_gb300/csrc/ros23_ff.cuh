@@ -98,8 +98,7 @@ struct Ros23FF {
     L.solve(k3);
     // error estimate h/6 (k1 - 2 k2 + k3); norm ratios in FP32, squares in FP64
     const ff h6 = h * SIXTH;
-    const ff as = ff_split(abstol), rs = ff_split(reltol);
-    const float atf = xadd(as.hi, as.lo), rtf = xadd(rs.hi, rs.lo);
+    const float atf = tol_f32(abstol), rtf = tol_f32(reltol);
     double ms = 0.0;
 #pragma unroll
     for (int c = 0; c < N; ++c) {

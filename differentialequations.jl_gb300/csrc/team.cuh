@@ -457,16 +457,11 @@ GBDE_D double team8_mean_sq(const Team8& tm, float e0, float e1) {
 }
 
 // The tolerances an 8-lane stepper's attempt reads: FP64, and the FP32 values
-// the pair steppers' norm ratios use (formed once per kernel: the split to a
-// pair runs an integer-to-float conversion on the FP64 pipe).
+// the pair steppers' norm ratios use (tol_f32), formed once per kernel.
 struct TeamTol {
   double abstol, reltol;
   float atf, rtf;
-  GBDE_D TeamTol(double a, double r) : abstol(a), reltol(r) {
-    const ff as = ff_split(a), rs = ff_split(r);
-    atf = xadd(as.hi, as.lo);
-    rtf = xadd(rs.hi, rs.lo);
-  }
+  GBDE_D TeamTol(double a, double r) : abstol(a), reltol(r), atf(tol_f32(a)), rtf(tol_f32(r)) {}
 };
 
 template <class M, class T>

@@ -123,8 +123,7 @@ struct Tsit5FF {
     a.fma(E6, hk[5]);
     a.fma(E7, hk[6]);
     a.get(err);
-    const ff as = ff_split(abstol), rs = ff_split(reltol);
-    const float atf = xadd(as.hi, as.lo), rtf = xadd(rs.hi, rs.lo);
+    const float atf = tol_f32(abstol), rtf = tol_f32(reltol);
     double ms = 0.0;
 #pragma unroll
     for (int c = 0; c < N; ++c) {

@@ -146,8 +146,7 @@ struct Vern7FF {
     a.fma(E10, hk[9]);
     a.get(err);
     have11 = false;
-    const ff as = ff_split(abstol), rs = ff_split(reltol);
-    const float atf = xadd(as.hi, as.lo), rtf = xadd(rs.hi, rs.lo);
+    const float atf = tol_f32(abstol), rtf = tol_f32(reltol);
     double ms = 0.0;
 #pragma unroll
     for (int c = 0; c < N; ++c) {
