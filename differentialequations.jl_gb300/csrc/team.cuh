@@ -989,7 +989,14 @@ __device__ void integrate_team8(const KArgs& a) {
   T p[M::NP];
   const int c0 = 2 * tm.lane;  // this lane's first component
   int64_t i = -1;              // the team's trajectory (-1: none yet)
-  double t = 0.0, tf = 0.0, dt = 0.0, dt1 = 0.0;
+  // time, end, step and first step as FP64 bit patterns: the loop's copies and
+  // selects of them stay on the integer pipe (GB300's FP64 pipe is narrow);
+  // the arithmetic reads them through D()
+  uint64_t t = 0, tf = 0, dt = 0, dt1 = 0;
+  auto D = [](uint64_t b) { return __longlong_as_double((long long)b); };
+  auto B = [](double x) { return (uint64_t)__double_as_longlong(x); };
+  const bool clamp = a.dtmax > 0.0;
+  const uint64_t dtmax_b = B(a.dtmax);
   int js = 0, nacc = 0, nrej = 0, nfev = 0;
   int64_t iters = 0;
   float lqold = 0.0f;
@@ -1020,9 +1027,9 @@ __device__ void integrate_team8(const KArgs& a) {
           if (a.naccept) a.naccept[i] = nacc;
           if (a.nreject) a.nreject[i] = nrej;
           if (a.nf) a.nf[i] = nfev;
-          if (a.t_end) a.t_end[i] = t;
+          if (a.t_end) a.t_end[i] = D(t);
           if (a.method_out) a.method_out[i] = Alg::ALG_ID;
-          if (a.dt_first) a.dt_first[i] = dt1;
+          if (a.dt_first) a.dt_first[i] = D(dt1);
         }
       }
       // ---- next trajectory (team-uniform)
@@ -1042,27 +1049,28 @@ __device__ void integrate_team8(const KArgs& a) {
       const double u0x = __ldg(a.u0 + (size_t)i * M::N + c0);
       const double u0y = __ldg(a.u0 + (size_t)i * M::N + c0 + 1);
       const T u0[2] = {(T)u0x, (T)u0y};
-      t = __ldg(a.t0 + i);
-      tf = __ldg(a.tf + i);
+      const double t0d = __ldg(a.t0 + i), tfd = __ldg(a.tf + i);
+      t = B(t0d);
+      tf = B(tfd);
       js = nacc = nrej = nfev = 0;
       iters = 0;
       lqold = a.ctl.lqoldinit;
-      dt1 = __longlong_as_double(0x7ff8000000000000ll);
+      dt1 = 0x7ff8000000000000ull;  // NaN
       ret = GBDE_RET_DEFAULT;
       const bool bad_lane = !isfinite(u0x) || !isfinite(u0y);
-      const bool bad = !(tf >= t) || !isfinite(t) || !isfinite(tf) ||
+      const bool bad = !(tfd >= t0d) || !isfinite(t0d) || !isfinite(tfd) ||
                        __any_sync(tm.mask, bad_lane);
       // save points at t0 store u0 exactly (the FP64 input, whatever T)
-      while (js < a.n_save && save_time(a, i, js) <= t) store(js++, u0x, u0y);
-      dt = 0.0;
+      while (js < a.n_save && save_time(a, i, js) <= t0d) store(js++, u0x, u0y);
+      double dtd = 0.0;
       if (bad) {
         ret = GBDE_RET_INITIALFAILURE;
       } else {
         alg.init(u0, p, tm, nfev);
         if (a.pred_dt != nullptr && a.pred_dt[i] > 0.f) {
-          dt = fmin((double)a.pred_dt[i], tf - t);
+          dtd = fmin((double)a.pred_dt[i], tfd - t0d);
         } else if (a.dt0 > 0.0 || !a.adaptive) {
-          dt = a.dt0;
+          dtd = a.dt0;
         } else {
           // Hairer-Wanner starting step (hw_h0 / hw_dt, controller.h)
           double r[2], s0 = 0.0, s1 = 0.0;
@@ -1075,7 +1083,7 @@ __device__ void integrate_team8(const KArgs& a) {
           }
           s0 = tm.sum(s0) * (1.0 / M::N);
           s1 = tm.sum(s1) * (1.0 / M::N);
-          const double h0 = hw_h0(s0, s1, tf - t);
+          const double h0 = hw_h0(s0, s1, tfd - t0d);
           T y[2], f1[2];
 #pragma unroll
           for (int c = 0; c < 2; ++c) y[c] = alg.u()[c] + T(h0) * alg.f0()[c];
@@ -1087,29 +1095,27 @@ __device__ void integrate_team8(const KArgs& a) {
             const double z = ((double)f1[c] - (double)alg.f0()[c]) * r[c];
             s2 += z * z;
           }
-          dt = hw_dt(h0, s1, tm.sum(s2) * (1.0 / M::N), tf - t, Alg::ORDER);
+          dtd = hw_dt(h0, s1, tm.sum(s2) * (1.0 / M::N), tfd - t0d, Alg::ORDER);
         }
-        if (a.dtmax > 0.0) dt = fmin(dt, a.dtmax);
-        if (!(t < tf)) ret = GBDE_RET_SUCCESS;
-        else if (!(dt > 0.0)) ret = GBDE_RET_DTLESSTHANMIN;
+        if (clamp) dtd = fmin(dtd, a.dtmax);
+        if (!(t0d < tfd)) ret = GBDE_RET_SUCCESS;
+        else if (!(dtd > 0.0)) ret = GBDE_RET_DTLESSTHANMIN;
       }
+      dt = B(dtd);
       if (ret != GBDE_RET_DEFAULT) continue;  // ended before any step
     }
     // ---- one attempted step
-    const double rem = tf - t;
-    double h = dt;
-    bool last = false;
-    if (ord_bits(h * (1.0 + 1e-10)) >= ord_bits(rem)) {
-      h = rem;
-      last = true;
-    }
+    const double rem = D(tf) - D(t);
+    const bool last = ord_bits(D(dt) * (1.0 + 1e-10)) >= ord_bits(rem);
+    const uint64_t hb = last ? B(rem) : dt;
+    const double h = D(hb);
     const double ms = alg.attempt(h, p, tol, tm, nfev);
     ++iters;
     if (!a.adaptive || mag_bits(ms) <= 0x3FF0000000000000ull) {  // ms <= 1 (integer pipe)
       double dtnew = h;
       if (a.adaptive) dtnew = h * f2d_bits(ctl_accept(a.ctl, ms, lqold));
-      const double tnew = last ? tf : t + h;  // plain FP64, as the oracle
-      const uint64_t tnew_o = ord_bits(tnew);
+      const uint64_t tnew = last ? tf : B(D(t) + h);  // plain FP64, as the oracle
+      const uint64_t tnew_o = ord_bits(D(tnew));
       while (js < a.n_save) {
         const double ts = save_time(a, i, js);
         const uint64_t ts_o = ord_bits(ts);
@@ -1118,26 +1124,26 @@ __device__ void integrate_team8(const KArgs& a) {
           store(js, (double)alg.unew()[0], (double)alg.unew()[1]);
         } else {
           T v[2];
-          alg.interp((ts - t) * rcp64(h), h, v);
+          alg.interp((ts - D(t)) * rcp64(h), h, v);
           store(js, (double)v[0], (double)v[1]);
         }
         ++js;
       }
       alg.accept();
       t = tnew;
-      if (nacc == 0) dt1 = h;
+      if (nacc == 0) dt1 = hb;
       ++nacc;
       if (__any_sync(tm.mask, !val_finite(alg.u()[0]) || !val_finite(alg.u()[1])))
         ret = GBDE_RET_UNSTABLE;
       else if (last) ret = GBDE_RET_SUCCESS;
-      dt = a.dtmax > 0.0 && ord_bits(dtnew) > ord_bits(a.dtmax) ? a.dtmax : dtnew;
+      dt = clamp && ord_bits(dtnew) > ord_bits(a.dtmax) ? dtmax_b : B(dtnew);
     } else {
       ++nrej;
-      dt = h * f2d_bits(ctl_reject(a.ctl, ms));
+      dt = B(h * f2d_bits(ctl_reject(a.ctl, ms)));
     }
     if (ret == GBDE_RET_DEFAULT) {
       if (iters >= a.maxiters) ret = GBDE_RET_MAXITERS;
-      else if (a.adaptive && dt_too_small(dt, a.dtmin, t))
+      else if (a.adaptive && dt_too_small(D(dt), a.dtmin, D(t)))
         ret = GBDE_RET_DTLESSTHANMIN;
       else if (a.timeout_ns && (iters & 31) == 0) {
         // lane 0's clock decides for the team
