@@ -90,6 +90,30 @@ GBDE_HD double f2d_bits(float x) {
 #endif
 }
 
+// An FP64 value carried as its bit pattern: a driver loop's copies and selects
+// of it stay on the integer pipe (GB300 runs FP64 moves on its narrow FP64
+// pipe); reading it as a double is a reinterpretation.
+struct F64Bits {
+  uint64_t b;
+  F64Bits() = default;
+  GBDE_HD F64Bits(double x) {
+#if defined(__CUDA_ARCH__)
+    b = (uint64_t)__double_as_longlong(x);
+#else
+    memcpy(&b, &x, sizeof(b));
+#endif
+  }
+  GBDE_HD operator double() const {
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)b);
+#else
+    double x;
+    memcpy(&x, &b, sizeof(x));
+    return x;
+#endif
+  }
+};
+
 // double -> float, rounded to nearest even, on the integer pipe: the value the
 // conversion instruction gives (that one runs on GB300's narrow FP64 pipe),
 // for finite x whose float is normal (2^-126 <= |x| < 2^128 after rounding).

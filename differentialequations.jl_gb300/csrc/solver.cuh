@@ -430,7 +430,11 @@ __device__ void integrate_all(const KArgs& a) {
   T p[M::NP];
   int64_t i = -1;
   bool active = false;
-  double t = 0.0, tf = 0.0, dt = 0.0, dt1 = 0.0;
+  // time, end, step and first step as FP64 bit patterns (F64Bits): the loop's
+  // copies and selects of them stay on the integer pipe
+  F64Bits t = 0.0, tf = 0.0, dt = 0.0, dt1 = 0.0;
+  const bool clamp = a.dtmax > 0.0;
+  const F64Bits dtmax = a.dtmax;
   float lqold = 0.0f;  // log2(qold)
   int js = 0, nacc = 0, nrej = 0, nfev = 0;
   int64_t iters = 0;
@@ -500,24 +504,21 @@ __device__ void integrate_all(const KArgs& a) {
       if constexpr (switching<Alg>::v) {
         if (iters > 0) {  // the method for this attempt, from the last one's estimate
           dt = alg.choose(dt, p, nfev);
-          if (a.dtmax > 0.0 && ord_bits(dt) > ord_bits(a.dtmax)) dt = a.dtmax;
+          if (clamp && ord_bits(dt) > ord_bits(a.dtmax)) dt = dtmax;
         }
       }
       const double rem = tf - t;
-      double h = dt;
-      bool last = false;
-      if (ord_bits(h * (1.0 + 1e-10)) >= ord_bits(rem)) {
-        h = rem;
-        last = true;
-      }
+      const bool last = ord_bits(dt * (1.0 + 1e-10)) >= ord_bits(rem);
+      const F64Bits hb = last ? F64Bits(rem) : dt;
+      const double h = hb;
       // The step's end if the attempt is accepted: t + h in FP64, in every
       // precision, as the FP64 oracle and the reference form it.  Steppers
       // that declare EARLY_TIME get it before the attempt, so that its FP64
       // addition overlaps the attempt's work: worth it where one warp runs
       // alone on its SM sub-partition (small ensembles), at the cost of a
       // register pair live through the attempt.
-      double tnew_e = 0.0;
-      if constexpr (early_time<Alg>::v) tnew_e = last ? tf : t + h;
+      F64Bits tnew_e = 0.0;
+      if constexpr (early_time<Alg>::v) tnew_e = last ? tf : F64Bits(t + h);
       const double ms = alg.attempt(h, p, a.abstol, a.reltol, nfev);  // EEst^2
       ++iters;
       // ms <= 1 (ms >= 0; NaN rejects), compared on the integer pipe
@@ -526,9 +527,9 @@ __device__ void integrate_all(const KArgs& a) {
         // controller proposal for the next step
         double dtnew = h;
         if (a.adaptive) dtnew = h * f2d_bits(ctl_accept(ctl_of(alg, a), ms, lqold));
-        double tnew;
+        F64Bits tnew;
         if constexpr (early_time<Alg>::v) tnew = tnew_e;
-        else tnew = last ? tf : t + h;
+        else tnew = last ? tf : F64Bits(t + h);
         // continuous callbacks: crossings of the conditions in (t, tnew]
         // (for the condition that fired at t, in (t + h/100, tnew]: the
         // repeat nudge); the earliest located root is the event
@@ -597,7 +598,7 @@ __device__ void integrate_all(const KArgs& a) {
         }
         // saveat: dense output at every save time in (t, tnew], or up to the
         // event; `exact`: the last one stored falls on that end
-        const double te = event ? t + th_e * h : tnew;
+        const double te = event ? t + th_e * h : (double)tnew;
         const uint64_t tnew_o = ord_bits(tnew), lim_o = ord_bits(te);
         bool exact = false;
         while (js < a.n_save) {
@@ -664,7 +665,7 @@ __device__ void integrate_all(const KArgs& a) {
           for (int c = 0; c < N; ++c) fin &= val_finite(alg.u()[c]);
           if (!fin) ret = GBDE_RET_UNSTABLE;
           else if (term) ret = GBDE_RET_TERMINATED;
-          dt = a.dtmax > 0.0 && ord_bits(dtnew) > ord_bits(a.dtmax) ? a.dtmax : dtnew;
+          dt = clamp && ord_bits(dtnew) > ord_bits(a.dtmax) ? dtmax : F64Bits(dtnew);
         } else {
           alg.accept(p, nfev);
           t = tnew;
@@ -686,7 +687,7 @@ __device__ void integrate_all(const KArgs& a) {
               if (term) ret = GBDE_RET_TERMINATED;
             }
           }
-          dt = a.dtmax > 0.0 && ord_bits(dtnew) > ord_bits(a.dtmax) ? a.dtmax : dtnew;
+          dt = clamp && ord_bits(dtnew) > ord_bits(a.dtmax) ? dtmax : F64Bits(dtnew);
         }
       } else {
         ++nrej;
