@@ -882,10 +882,14 @@ def run_learned(args, de):
             ts.append(rr["device_ms"])
         return float(np.median(ts)), rr
 
+    # the ring: the learned stiffness choice alone (GBDE_LEARN_STIFF, the
+    # Hairer-Wanner start as the oracle), so the gate sees the choice's effect;
+    # Lorenz / LV: the learned first dt (GBDE_LEARN_START)
+    flag = capi.LEARN_STIFF if base == "vdp_auto" else capi.LEARN_START
     with ClockSampler(0) as clk:
         chosen.learned = 0
         base_ms, rb = timed(chosen, args.steps, args.warmup)
-        learned.learned = 1
+        learned.learned = flag
         learned_ms, rl = timed(learned, args.steps, args.warmup)
         learned.learned = 0
     ok = bool(np.all(rl["retcode"].cpu().numpy() == capi.RET_SUCCESS))
