@@ -730,10 +730,13 @@ struct RingSchur8 {
   float e[TEAM8];  // the row of A^-1 of the column this lane's row was the pivot of
   int src;         // the lane holding row l of A^-1, whose product is x_l
   ff w11, dg;
+  float w11f, dgf;
 
   GBDE_D void build(ff dg_, ff w10, ff w11_, ff ka, const Team8& tm) {
     dg = dg_;
     w11 = w11_;
+    w11f = (float)w11_;
+    dgf = (float)dg_;
     const int l = tm.lane;
     const float ad = (float)(w10 + w11 * dg), nk = -(float)ka;
     float a[TEAM8];
@@ -776,18 +779,29 @@ struct RingSchur8 {
     src = (int)((piv >> (3 * l)) & (TEAM8 - 1));
   }
 
-  // (x_l, v_l) in FP32 from this lane's b_2l, b_2l+1 (b[0], b[1], pairs)
-  GBDE_D void solve(const ff* b, float* xv, const Team8& tm) const {
-    const float c = (float)(b[1] + w11 * b[0]);
+  // x_l = (A^-1 c)_l for this lane's c_l
+  GBDE_D float apply(float c, const Team8& tm) const {
     float s0 = 0.0f, s1 = 0.0f;
 #pragma unroll
     for (int m = 0; m < TEAM8; m += 2) {
       s0 = xfma(e[m], tm.bcast(c, m), s0);
       s1 = xfma(e[m + 1], tm.bcast(c, m + 1), s1);
     }
-    const float x = tm.bcast(xadd(s0, s1), src);
+    return tm.bcast(xadd(s0, s1), src);
+  }
+  // (x_l, v_l) in FP32 from this lane's b_2l, b_2l+1 (b[0], b[1], pairs); c and
+  // v formed in pairs (they may cancel)
+  GBDE_D void solve(const ff* b, float* xv, const Team8& tm) const {
+    const float x = apply((float)(b[1] + w11 * b[0]), tm);
     xv[0] = x;
     xv[1] = (float)(dg * ff(x, 0.0f) - b[0]);
+  }
+  // the same from FP32 b, all in FP32: for a refinement's correction, whose
+  // relative error then only scales the (already small) correction
+  GBDE_D void solve32(const float* b, float* xv, const Team8& tm) const {
+    const float x = apply(xfma(w11f, b[0], b[1]), tm);
+    xv[0] = x;
+    xv[1] = xfma(dgf, x, -b[0]);
   }
 };
 
@@ -902,14 +916,16 @@ struct TeamRodasFF8 {
       ff x[2];
       {
         // W x = r: an FP32 solve (RingSchur8) and one refinement against W in
-        // pairs, x = x0 + d with W d ~ r - W x0 (residual in pairs).  W =
-        // I/(h gamma) - J is well conditioned here, so the refined error is
-        // about (cond 2^-24)^2 of |x|, far below the tolerances.
+        // pairs, x = x0 + d with W d ~ r - W x0 (residual in pairs, its
+        // correction solved in FP32).  W = I/(h gamma) - J is well conditioned
+        // here, so the refined error is about (cond 2^-24)^2 of |x|, far below
+        // the tolerances.
         float x0[2], d[2];
         L.solve(r, x0, tm);
         ff res[2];
         M::template w_osc_residual<FfAcc>(tm.lane, dg, w10, w11, p[1], r, x0, tm, res);
-        L.solve(res, d, tm);
+        const float rf[2] = {res[0].hi, res[1].hi};
+        L.solve32(rf, d, tm);
         x[0] = ff(x0[0], 0.0f) + ff(d[0], 0.0f);
         x[1] = ff(x0[1], 0.0f) + ff(d[1], 0.0f);
       }
