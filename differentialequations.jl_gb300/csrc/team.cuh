@@ -789,12 +789,13 @@ struct RingSchur8 {
     }
     return tm.bcast(xadd(s0, s1), src);
   }
-  // (x_l, v_l) in FP32 from this lane's b_2l, b_2l+1 (b[0], b[1], pairs); c and
-  // v formed in pairs (they may cancel)
+  // (x_l, v_l) in FP32 from this lane's b_2l, b_2l+1 (b[0], b[1], pairs): c
+  // formed in pairs (it may cancel); v in FP32 -- its rounding is exactly
+  // what the refinement's residual then sees in row 2l, and corrects
   GBDE_D void solve(const ff* b, float* xv, const Team8& tm) const {
     const float x = apply((float)(b[1] + w11 * b[0]), tm);
     xv[0] = x;
-    xv[1] = (float)(dg * ff(x, 0.0f) - b[0]);
+    xv[1] = xfma(dgf, x, -b[0].hi);
   }
   // the same from FP32 b, all in FP32: for a refinement's correction, whose
   // relative error then only scales the (already small) correction
