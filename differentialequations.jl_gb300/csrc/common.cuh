@@ -149,6 +149,13 @@ GBDE_HD bool val_finite(T x) {
 // FP32 values test directly: no conversion on the FP64 pipe
 GBDE_HD bool val_finite(float x) { return isfinite(x); }
 
+// A state component rounded to FP32 for the FP32 output; the pair type
+// (ff.cuh) overloads it with one rounding of hi + lo.
+template <class T>
+GBDE_HD float val_f32(T x) {
+  return (float)x;
+}
+
 // TwoSum in the working precision T (the FP32 path keeps its state as an
 // unevaluated sum hi + lo so that rounding does not accumulate over steps).
 template <class T>

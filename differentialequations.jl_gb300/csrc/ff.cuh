@@ -66,6 +66,9 @@ GBDE_HD bool operator<(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo
 
 // a pair is finite iff its leading part is
 GBDE_HD bool val_finite(ff x) { return isfinite(x.hi); }
+// a pair rounded to FP32: hi + lo in one correctly rounded FP32 addition
+// (the exact sum rounded once; the FP64 route rounds twice)
+GBDE_HD float val_f32(ff x) { return xadd(x.hi, x.lo); }
 
 template <class T> struct is_ff { static constexpr bool value = false; };
 template <> struct is_ff<ff> { static constexpr bool value = true; };

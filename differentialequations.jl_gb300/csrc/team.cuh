@@ -755,8 +755,7 @@ constexpr int kTeam8Threads = 96;
 // cancel) and rounded once.  The callers refine every solve once against W
 // in pairs.
 struct RingSchur8 {
-  float e[TEAM8];  // the row of A^-1 of the column this lane's row was the pivot of
-  int src;         // the lane holding row l of A^-1, whose product is x_l
+  float e[TEAM8];  // row l of A^-1 on lane l
   ff w11, dg;
   float w11f, dgf;
 
@@ -779,18 +778,20 @@ struct RingSchur8 {
     unsigned piv = 0;  // pivot lane of column k in bits [3k, 3k+3)
 #pragma unroll
     for (int k = 0; k < TEAM8; ++k) {
-      uint64_t m = open ? ((uint64_t)((__float_as_uint(a[k]) & 0x7fffffffu) + 1u) << 32) |
-                              (uint64_t)(~(unsigned)l)
-                        : 0ull;
+      // pivot: the open row of largest |a_k| (its bit pattern with the 3 low
+      // mantissa bits dropped), ties to the lowest lane; the key's low bits
+      // carry the lane, so one 32-bit max over the team decides
+      unsigned m = open ? ((((__float_as_uint(a[k]) & 0x7fffffffu) >> 3) + 1u) << 3) |
+                              (unsigned)(TEAM8 - 1 - l)
+                        : 0u;
 #pragma unroll
-      for (int o = TEAM8 / 2; o > 0; o >>= 1) {
-        const uint64_t x = __shfl_xor_sync(tm.mask, m, o, TEAM8);
-        m = x > m ? x : m;
-      }
-      const int p = (int)(~(unsigned)m & (TEAM8 - 1));
+      for (int o = TEAM8 / 2; o > 0; o >>= 1) m = umax(m, __shfl_xor_sync(tm.mask, m, o, TEAM8));
+      const int p = TEAM8 - 1 - (int)(m & (TEAM8 - 1));
       piv |= (unsigned)p << (3 * k);
       const bool me = l == p;
-      const float inv = __frcp_rn(tm.bcast(a[k], p));
+      // the fast reciprocal (within 1 ulp): the inverse is refined against
+      // in pairs anyway, and the IEEE-rounded one sat on the pivot chain
+      const float inv = __fdividef(1.0f, tm.bcast(a[k], p));
       const float f = me ? 0.0f : xmul(a[k], inv);  // this row's multiplier
 #pragma unroll
       for (int c = k + 1; c < TEAM8; ++c) {
@@ -804,7 +805,11 @@ struct RingSchur8 {
       }
       if (me) open = false;
     }
-    src = (int)((piv >> (3 * l)) & (TEAM8 - 1));
+    // lane l takes row l of A^-1 (held by the lane that pivoted column l),
+    // so that every product below lands on its own lane
+    const int src = (int)((piv >> (3 * l)) & (TEAM8 - 1));
+#pragma unroll
+    for (int m = 0; m < TEAM8; ++m) e[m] = tm.bcast(e[m], src);
   }
 
   // x_l = (A^-1 c)_l for this lane's c_l
@@ -815,7 +820,7 @@ struct RingSchur8 {
       s0 = xfma(e[m], tm.bcast(c, m), s0);
       s1 = xfma(e[m + 1], tm.bcast(c, m + 1), s1);
     }
-    return tm.bcast(xadd(s0, s1), src);
+    return xadd(s0, s1);
   }
   // (x_l, v_l) in FP32 from this lane's b_2l, b_2l+1 (b[0], b[1], pairs): c
   // formed in pairs (it may cancel); v in FP32 -- its rounding is exactly
@@ -1046,7 +1051,26 @@ __device__ void integrate_team8(const KArgs& a) {
   int64_t iters = 0;
   float lqold = 0.0f;
   int ret = GBDE_RET_SUCCESS;  // anything but DEFAULT: take a trajectory
-  auto store = [&](int j, double v0, double v1) {  // FP64 values of this lane's components
+  // FP64 values of this lane's components (the inputs at t0, NaN); store_t
+  // the stepper's own: the FP32 output takes a pair's hi + lo in one FP32
+  // addition (rounded once, no conversions on the FP64 pipe, where a save
+  // made by one team of the warp costs four times its lanes)
+  auto store_t = [&](int j, const T& v0, const T& v1) {
+    if (a.red) {
+      reduce_add(a, j, c0, M::N, (double)v0);
+      reduce_add(a, j, c0 + 1, M::N, (double)v1);
+    }
+    if (a.u_out == nullptr) return;
+    const size_t o = ((size_t)i * a.n_save + j) * M::N + c0;
+    if (a.out_f32) {
+      ((float*)a.u_out)[o] = val_f32(v0);
+      ((float*)a.u_out)[o + 1] = val_f32(v1);
+    } else {
+      ((double*)a.u_out)[o] = (double)v0;
+      ((double*)a.u_out)[o + 1] = (double)v1;
+    }
+  };
+  auto store = [&](int j, double v0, double v1) {
     if (a.red) {
       reduce_add(a, j, c0, M::N, v0);
       reduce_add(a, j, c0 + 1, M::N, v1);
@@ -1166,11 +1190,11 @@ __device__ void integrate_team8(const KArgs& a) {
         const uint64_t ts_o = ord_bits(ts);
         if (ts_o > tnew_o) break;
         if (ts_o == tnew_o) {
-          store(js, (double)alg.unew()[0], (double)alg.unew()[1]);
+          store_t(js, alg.unew()[0], alg.unew()[1]);
         } else {
           T v[2];
           alg.interp((ts - D(t)) * rcp64(h), h, v);
-          store(js, (double)v[0], (double)v[1]);
+          store_t(js, v[0], v[1]);
         }
         ++js;
       }
