@@ -71,18 +71,18 @@ TRAFFIC_PER_TRAJ = {"fp64": (4.586752e6 + 8192.0) / 20000.0,
 # --steps 1 --warmup 1 --no-cpu-baseline` under ncu --metrics
 # dram__bytes_read.sum,dram__bytes_write.sum,smsp__inst_executed.sum; the split
 # at mu = 60: 122,217 stiff, 277,783 non-stiff):
-#   k_team8<TeamRodasFF8> (stiff): 1,286 DRAM bytes (read + write) per
+#   k_team8<TeamRodasFF8> (stiff): 1,307 DRAM bytes (read + write) per
 #   trajectory against ~1,536 bytes of inputs and outputs (the last saves are
-#   still in L2 when the kernel ends); 38.96e9 warp instructions, 1,337 per
+#   still in L2 when the kernel ends); 37.38e9 warp instructions, 1,283 per
 #   trajectory and attempted step (238.4 attempts each by the oracle's count
 #   on the run's 2,000-trajectory sample; a warp carries 4 trajectories);
-#   k_team8<TeamTsit5FF> (non-stiff): 1,431 DRAM bytes and 128,616 warp
+#   k_team8<TeamTsit5FF> (non-stiff): 1,435 DRAM bytes and 136,005 warp
 #   instructions per trajectory (its attempted steps vary with mu; the
 #   workload's mu distribution is the same at every N).
-RING_STIFF_TRAFFIC_PER_TRAJ = (38.552832e6 + 118.672640e6) / 122217.0
-RING_STIFF_INST_PER_ATTEMPT = 38.956125e9 / (122217.0 * 238.4)
-RING_NONSTIFF_TRAFFIC_PER_TRAJ = (64.819200e6 + 332.542720e6) / 277783.0
-RING_NONSTIFF_INST_PER_TRAJ = 35.727274e9 / 277783.0
+RING_STIFF_TRAFFIC_PER_TRAJ = (39.101952e6 + 120.644096e6) / 122217.0
+RING_STIFF_INST_PER_ATTEMPT = 37.379764e9 / (122217.0 * 238.4)
+RING_NONSTIFF_TRAFFIC_PER_TRAJ = (63.819520e6 + 334.766592e6) / 277783.0
+RING_NONSTIFF_INST_PER_TRAJ = 37.779985e9 / 277783.0
 
 WORKLOADS = ["vdp_auto", "robertson", "lorenz", "lv_em", "lv_sosri", "summary",
              "learned_lorenz", "learned_lv", "learned_vdp"]
