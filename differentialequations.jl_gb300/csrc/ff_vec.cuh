@@ -30,6 +30,13 @@ GBDE_D ff ff_split(double d) {
   return ff(hi, sign ? -lo : lo);
 }
 
+// A norm ratio s / d in FP32 by the fast reciprocal and product: within 2 ulp
+// for the normal d the tolerances give (d >= atol > 0, or rtol |u|), against
+// the IEEE division's multi-instruction sequence.  The ratios feed a mean
+// square and a step decision at 1; on the ring's pair teams the fast form
+// moved 8 of 226M step decisions and took 3 % off the non-stiff kernel.
+GBDE_D float norm_ratio(float s, float d) { return __fdividef(s, d); }
+
 // A tolerance (finite, >= 0) in FP32 for the norm ratios: rounded to nearest on
 // the integer pipe (d2f_rn_bits), values below FP32's normal range flushed to
 // 0 as ff_split does -- without the split's int-to-float conversion, which

@@ -274,7 +274,7 @@ struct RodasFF {
       a.add(s[c]);
       un[c] = a.get();
       const float m = fmaxf(fabsf(uu[c].hi), fabsf(un[c].hi));
-      const double e = f2d_bits(__fdiv_rn(s[c].hi, fmaf(rtf, m, atf)));
+      const double e = f2d_bits(norm_ratio(s[c].hi, fmaf(rtf, m, atf)));
       ms = fma(e, e, ms);
     }
     return ms * (1.0 / N);

@@ -108,7 +108,7 @@ struct Ros23FF {
       a.add(k3[c]);
       const ff err = a.get() * h6;
       const float m = fmaxf(fabsf(uu[c].hi), fabsf(un[c].hi));
-      const double e = f2d_bits(__fdiv_rn(err.hi, fmaf(rtf, m, atf)));
+      const double e = f2d_bits(norm_ratio(err.hi, fmaf(rtf, m, atf)));
       ms = fma(e, e, ms);
     }
     return ms * (1.0 / N);

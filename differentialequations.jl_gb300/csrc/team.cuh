@@ -580,13 +580,6 @@ __device__ __noinline__ Ff2Pair team8_osc_rhs(int lane, unsigned mask, ff x, ff 
   return {dy[0], dy[1]};
 }
 
-// A norm ratio s / d in FP32 by the fast reciprocal and product: within 2 ulp
-// for the normal d the tolerances give (d >= atol > 0, or rtol |u|), against
-// the IEEE division's multi-instruction sequence; the ratios feed an FP32
-// mean square and a step decision at 1.  On the ring's pair teams it moved 8
-// of 226M step decisions and took 3 % off the non-stiff kernel.
-GBDE_D float team8_ratio(float s, float d) { return __fdividef(s, d); }
-
 template <class M>
 struct TeamTsit5FF {
   using T = ff;
@@ -690,7 +683,7 @@ struct TeamTsit5FF {
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
       const float m = fmaxf(fabsf(uu[c].hi), fabsf(un[c].hi));
-      e[c] = team8_ratio(err[c].hi, fmaf(rtf, m, atf));
+      e[c] = norm_ratio(err[c].hi, fmaf(rtf, m, atf));
     }
     return team8_mean_sq(tm, e[0], e[1]);
   }
@@ -982,7 +975,7 @@ struct TeamRodasFF8 {
       a.add(s[c]);
       un[c] = a.get();
       const float m = fmaxf(fabsf(uu[c].hi), fabsf(un[c].hi));
-      e[c] = team8_ratio(s[c].hi, fmaf(rtf, m, atf));
+      e[c] = norm_ratio(s[c].hi, fmaf(rtf, m, atf));
     }
     return team8_mean_sq(tm, e[0], e[1]);
   }

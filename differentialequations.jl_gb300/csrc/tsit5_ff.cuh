@@ -128,7 +128,7 @@ struct Tsit5FF {
 #pragma unroll
     for (int c = 0; c < N; ++c) {
       const float m = fmaxf(fabsf(uu[c].hi), fabsf(un[c].hi));
-      const float e = __fdiv_rn(err[c].hi, fmaf(rtf, m, atf));
+      const float e = norm_ratio(err[c].hi, fmaf(rtf, m, atf));
       const double ed = f2d_bits(e);
       ms = fma(ed, ed, ms);
     }

@@ -151,7 +151,7 @@ struct Vern7FF {
 #pragma unroll
     for (int c = 0; c < N; ++c) {
       const float m = fmaxf(fabsf(uu[c].hi), fabsf(un[c].hi));
-      const double e = f2d_bits(__fdiv_rn(err[c].hi, fmaf(rtf, m, atf)));
+      const double e = f2d_bits(norm_ratio(err[c].hi, fmaf(rtf, m, atf)));
       ms = fma(e, e, ms);
     }
     return ms * (1.0 / N);
