@@ -139,7 +139,9 @@ VDP_RTOL = 1e-5
 # The AUTO split of the ring workload: Rodas5 for mu above it, Tsit5 below (the
 # same split for every form and for the CPU port).  The AUTO solve time on GB300
 # against the split (1M trajectories, FP32 pairs): 286 / 266 / 255 / 256 / 265 /
-# 290 ms at 20 / 30 / 50 / 70 / 100 / 150.
+# 290 ms at 20 / 30 / 50 / 70 / 100 / 150; on the later kernels the two kernels'
+# times summed: 211.4 / 210.8 / 210.8 / 211.0 / 212.0 / 212.7 ms at 45 / 50 / 55
+# / 60 / 65 / 70.
 VDP_STIFF_MU = 60.0
 
 
